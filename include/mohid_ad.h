@@ -1,0 +1,256 @@
+/*
+ * mohid_ad.h -- C-ABI of the GB300 tracer advection-diffusion step.
+ *
+ * This is the drop-in boundary for MOHID Water's per-property transport call
+ *   ModuleWaterProperties::Advection_Diffusion_Processes
+ *     -> ModuleAdvectionDiffusion::AdvectionDiffusion
+ *        (Software/MOHIDWater/ModuleWaterProperties.F90:14776-14824,
+ *         Software/MOHIDBase2/ModuleAdvectionDiffusion.F90:1108-1509)
+ * and for the legacy CUDA Thomas binding it supersedes
+ *   SolveThomas_C / InitializeThomas_C / KillThomas_C
+ *        (Software/CudaThomas/Thomas.h:11-27, Software/MOHIDBase1/ModuleCuda.F90:49-121).
+ *
+ * Conventions (Fortran ISO_C_BINDING friendly):
+ *  - every scalar argument is passed by pointer (Fortran default by-reference);
+ *  - every array is the base pointer of a Fortran column-major array over the
+ *    `Size` box (ILB:IUB, JLB:JUB[, KLB:KUB]) with i fastest, exactly as MOHID
+ *    allocates it (Size = WorkSize +/- 1 halo cell on every side,
+ *    Software/MOHIDBase2/ModuleGeometry.F90:812-816);
+ *  - REAL arrays are double precision: the reference Linux build promotes the
+ *    default REAL to 8 bytes (-fdefault-real-8 / -real_size 64,
+ *    Solutions/mohid-in-linux/compile_mohid.sh:185,209);
+ *  - Fortran LOGICALs are passed as int (0 = .false., nonzero = .true.);
+ *  - every entry point returns its status and also stores it in *stat
+ *    (MOHID's STAT convention, SUCCESS_ = 0, Software/MOHIDBase1/ModuleGlobalData.F90:181).
+ *    No entry point ever aborts the host process (the legacy CuExe called exit(1),
+ *    Software/CudaWrapper/CuWrapper.cpp:11-19).
+ *
+ * Calls on one instance id must be serialised by the caller (MOHID calls the
+ * transport inside its property loop, outside OpenMP regions); different ids may
+ * be driven from different host threads -- each id owns its own CUDA stream.
+ */
+#ifndef MOHID_AD_H
+#define MOHID_AD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MOHID_AD_SUCCESS          0   /* SUCCESS_ (ModuleGlobalData.F90:181)                    */
+#define MOHID_AD_ERR_BOUNDS       1   /* inconsistent Size/WorkSize bounds or array extents      */
+#define MOHID_AD_ERR_ID           2   /* unknown / dead instance id (reference: ready_ /= IDLE)  */
+#define MOHID_AD_ERR_OPTION       3   /* option combination the reference rejects with `stop`   */
+#define MOHID_AD_ERR_UNSUPPORTED  4   /* option of the reference this build does not implement  */
+#define MOHID_AD_ERR_CUDA         5   /* CUDA runtime error (message via mohid_ad_last_error)    */
+#define MOHID_AD_ERR_ZERO_PIVOT   6   /* THOMASZ pivot |E + D*W| == 0 in some water column       */
+#define MOHID_AD_ERR_NONFINITE    7   /* a solved concentration is Inf/NaN                       */
+#define MOHID_AD_ERR_ALLOC        8   /* device or pinned-host allocation failed                 */
+#define MOHID_AD_ERR_NULLPTR      9   /* a required array pointer is NULL                        */
+#define MOHID_AD_ERR_TIMEOUT     10   /* a bounded device-side wait gave up                      */
+
+/* ---- option enums (values identical to the reference) ------------------ */
+/* ModuleGlobalData.F90:1810-1811 */
+#define MOHID_UPWIND_ORDER1   1
+#define MOHID_UPWIND_ORDER2   2
+#define MOHID_UPWIND_ORDER3   3
+#define MOHID_P2_TVD          4
+#define MOHID_CENTRAL_DIF     5
+#define MOHID_LEAP_FROG       6
+#define MOHID_TVD_MINMOD      1
+#define MOHID_TVD_VANLEER     2
+#define MOHID_TVD_MUSCL       3
+#define MOHID_TVD_SUPERBEE    4
+#define MOHID_TVD_PDM         5
+/* ModuleAdvectionDiffusion.F90:152-158 */
+#define MOHID_BC_MASS_CONSERVATION   1
+#define MOHID_BC_IMPOSED_VALUE       2
+#define MOHID_BC_NULL_GRADIENT       4
+#define MOHID_BC_SUBMODEL            5
+#define MOHID_BC_ORLANSKI            6
+#define MOHID_BC_MASS_CONSERV_NULLGRAD 7
+#define MOHID_BC_CYCLIC              8
+/* ModuleGlobalData.F90:143 */
+#define MOHID_NULL_REAL (-9.9e15)
+
+/* T_Size3D, ModuleGlobalData.F90:2042-2052 (bind(c) under _USE_CUDA). */
+typedef struct T_Size3D {
+    int ILB, IUB, JLB, JUB, KLB, KUB;
+} T_Size3D;
+
+/*
+ * Scalar arguments of AdvectionDiffusion (ModuleAdvectionDiffusion.F90:1108-1198),
+ * same names and meaning.  `real` arguments are double (default REAL is 8 bytes
+ * in the reference build).  Construction-time options of StartAdvectionDiffusion
+ * (Vertical1D, XZFlow, Docycle_method; ModuleAdvectionDiffusion.F90:400-480) are
+ * carried here too, so that one struct describes a call completely.
+ */
+typedef struct mohid_ad_params {
+    double schmidt_H;             /* Schmidt number, horizontal                     */
+    double SchmidtCoef_V;         /* Kz = SchmidtCoef_V * Diff_V + SchmidtBackground_V */
+    double SchmidtBackground_V;
+    int    AdvMethodH, TVDLimitationH;
+    int    AdvMethodV, TVDLimitationV;
+    int    Upwind2H, Upwind2V;    /* LOGICAL                                          */
+    double VolumeRelMax;
+    double DTProp;                /* property time step [s]                           */
+    double ImpExp_AdvV;           /* 1 = implicit (default), 0 = explicit             */
+    double ImpExp_DifV;           /* 1 = implicit, 0 = explicit, in between = theta   */
+    double ImpExp_AdvXX;          /* must be 0 (explicit) in this build               */
+    double ImpExp_AdvYY;          /* must be 0 (explicit) in this build               */
+    double ImpExp_DifH;           /* must be 0: the reference requires explicit H-diff */
+    int    NullDif;               /* LOGICAL                                          */
+    int    BoundaryCondition;     /* used only when ReferenceProp is given            */
+    double DecayTime;             /* [s]                                              */
+    int    AdvectionNudging;      /* LOGICAL, must be .false. in this build           */
+    int    AdvectionNudgingCells;
+    int    CellFluxes;            /* LOGICAL, must be .false. in this build           */
+    int    NoAdvFlux, NoDifFlux;  /* LOGICAL, must be .false. in this build           */
+    int    Optimize, FirstProperty; /* LOGICAL; accepted, results follow the general path */
+    int    Vertical1D, XZFlow;    /* LOGICAL, StartAdvectionDiffusion options          */
+    int    Docycle_method;        /* 1 (default) or 2, ModuleModel.F90:641-646        */
+} mohid_ad_params;
+
+/* Fill *p with the reference's defaults (ModuleWaterProperties.F90:9305-9680):
+ * UpwindOrder1 H and V, SuperBee limiters, Upwind2H/V false, VolumeRelMax 1.5,
+ * Schmidt numbers 1, background 1e-8, implicit V advection and diffusion,
+ * explicit H, MassConservation, DecayTime 0, Docycle_method 1. */
+void mohid_ad_default_params(mohid_ad_params* p);
+
+/* Text of the last error on this host thread (never NULL). */
+const char* mohid_ad_last_error(void);
+
+/* Library version string, e.g. "mohid-gb300 0.1 sm_103a". */
+const char* mohid_ad_version(void);
+
+/* ======================================================================== */
+/* Plain FP64 drop-in (one property per call, Fortran layout, in place)      */
+/* ======================================================================== */
+
+/*
+ * Construct an instance: StartAdvectionDiffusion (ModuleAdvectionDiffusion.F90:400)
+ * plus the grid getters AdvectionDiffusion performs each call
+ * (GetHorizontalGrid DUX/DVY/DZX/DZY, GetBoundaries, GetGeometryKFloor;
+ * ModuleAdvectionDiffusion.F90:1353-1401).  The static 2-D metrics are
+ * uploaded once.  `size` is the allocation box, `worksize` the computed box;
+ * size must equal worksize +/- 1 in i, j and k.
+ *   DUX, DVY, DZX, DZY : double (ILB:IUB, JLB:JUB)
+ *   KFloorZ, BoundaryPoints2D : int (ILB:IUB, JLB:JUB)
+ * On success *id > 0.
+ */
+int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize,
+                  const double* DUX, const double* DVY,
+                  const double* DZX, const double* DZY,
+                  const int* KFloorZ, const int* BoundaryPoints2D, int* stat);
+
+/*
+ * Upload the fields shared by every property of one time step (the arguments
+ * of AdvectionDiffusion that do not depend on the property).  All 3-D arrays
+ * are over the Size box.  `SmallDepths` (int, 2-D) may be NULL.
+ * Equivalent to the pointer-binding part of the reference call; lets a caller that
+ * transports N properties per step send the hydrodynamics once instead of N times.
+ */
+int mohid_ad_set_hydro(const int* id,
+                       const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
+                       const double* VolumeZOld, const double* VolumeZ,
+                       const double* Visc_H, const double* Diff_V,
+                       const double* AreaU, const double* AreaV,
+                       const double* DZZ, const double* DWZ,
+                       const int* OpenPoints3D, const int* LandPoints3D,
+                       const int* WaterPoints3D,
+                       const int* ComputeFacesU3D, const int* ComputeFacesV3D,
+                       const int* ComputeFacesW3D,
+                       const int* SmallDepths, int* stat);
+
+/*
+ * Transport one property over one step with the hydrodynamics of the last
+ * mohid_ad_set_hydro call: PROP (double, Size box) is read and overwritten in
+ * place, as AdvectionDiffusion does (THOMASZ_NewType2's RES aliases PROP,
+ * ModuleFunctions.F90:4026-4123).  ReferenceProp may be NULL (closed
+ * boundaries); when given, `p->BoundaryCondition` selects the open-boundary
+ * treatment (ModuleAdvectionDiffusion.F90:5369-5742).
+ */
+int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
+                           const mohid_ad_params* p, int* stat);
+
+/*
+ * All-in-one drop-in with the argument surface of AdvectionDiffusion:
+ * mohid_ad_set_hydro + mohid_ad_step_prop_f64.
+ */
+int mohid_ad_step_f64(const int* id, double* PROP, const mohid_ad_params* p,
+                      const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
+                      const double* VolumeZOld, const double* VolumeZ,
+                      const double* Visc_H, const double* Diff_V,
+                      const double* AreaU, const double* AreaV,
+                      const double* DZZ, const double* DWZ,
+                      const int* OpenPoints3D, const int* LandPoints3D,
+                      const int* WaterPoints3D,
+                      const int* ComputeFacesU3D, const int* ComputeFacesV3D,
+                      const int* ComputeFacesW3D,
+                      const int* SmallDepths,
+                      const double* ReferenceProp, int* stat);
+
+/*
+ * Device-resident variant of mohid_ad_step_prop_f64: PROP_in and PROP_out are
+ * device pointers (Size box, double), distinct; the call is asynchronous on the
+ * instance's stream (query it with mohid_ad_stream).  Every cell of PROP_out is
+ * written (cells the reference leaves untouched are copied from PROP_in).
+ * ReferenceProp, if not NULL, is a device pointer.  Device-side failures
+ * (zero pivot, non-finite result) are latched and reported by
+ * mohid_ad_sync.
+ */
+int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PROP_out,
+                               const double* ReferenceProp,
+                               const mohid_ad_params* p, int* stat);
+
+/* Upload hydrodynamics that already live on the device (same layout as
+ * mohid_ad_set_hydro, device pointers; copied device-to-device, async). */
+int mohid_ad_set_hydro_dev(const int* id,
+                           const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
+                           const double* VolumeZOld, const double* VolumeZ,
+                           const double* Visc_H, const double* Diff_V,
+                           const double* AreaU, const double* AreaV,
+                           const double* DZZ, const double* DWZ,
+                           const int* OpenPoints3D, const int* LandPoints3D,
+                           const int* WaterPoints3D,
+                           const int* ComputeFacesU3D, const int* ComputeFacesV3D,
+                           const int* ComputeFacesW3D,
+                           const int* SmallDepths, int* stat);
+
+/* Wait for the instance's stream and report latched device errors. */
+int mohid_ad_sync(const int* id, int* stat);
+
+/* The instance's cudaStream_t, as an opaque pointer. */
+void* mohid_ad_stream(const int* id);
+
+/* KillAdvectionDiffusion (ModuleAdvectionDiffusion.F90:5849): free the instance. */
+int mohid_ad_kill(int* id, int* stat);
+
+/* ======================================================================== */
+/* Stand-alone THOMASZ (replaces SolveThomas_C with dim = 2 = Z)             */
+/* ======================================================================== */
+
+/*
+ * Solve THOMASZ_NewType2 (ModuleFunctions.F90:4026-4123) for every column
+ * (i,j) of the work box with WaterPoints(i,j,KUB) == 1, rows KLB..KUB+1,
+ * exactly as the reference's CPU routine and the legacy CUDA path
+ * (SolveThomas_C, Software/CudaThomas/Thomas.cu:23-51, 464-491) do.
+ *   ILB..KUB  : WORK box bounds (the arguments the reference passes)
+ *   size      : allocation box of D, E, F, TI, RES, WaterPoints
+ *   D, E, F, TI : double (Size box), host pointers
+ *   RES        : double (Size box), host pointer, written for solved columns
+ * Columns not solved are left untouched.
+ */
+int mohid_thomasz_f64(const int* ILB, const int* IUB, const int* JLB, const int* JUB,
+                      const int* KLB, const int* KUB, const T_Size3D* size,
+                      const double* D, const double* E, const double* F,
+                      const double* TI, double* RES, const int* WaterPoints, int* stat);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOHID_AD_H */

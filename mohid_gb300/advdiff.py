@@ -1,0 +1,126 @@
+"""Host-side mirror of MOHID's transport interface, on the GB300 C-ABI.
+
+    StartAdvectionDiffusion   ModuleAdvectionDiffusion.F90:400    -> AdvectionDiffusion(domain)
+    AdvectionDiffusion(...)   ModuleAdvectionDiffusion.F90:1108   -> .step(PROP, params, ReferenceProp)
+    KillAdvectionDiffusion    ModuleAdvectionDiffusion.F90:5849   -> .kill()
+
+Argument names and meanings are the reference's; option errors that make the
+reference `stop` raise MohidAdError(ERR_OPTION) instead.  Every call runs the
+CUDA kernels of libmohid_ad.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .synth import Domain, F3, I3
+
+
+def params(**over) -> N.MohidAdParams:
+    """mohid_ad_params with the reference's defaults, then `over` applied."""
+    p = N.MohidAdParams()
+    N.ad_lib().mohid_ad_default_params(C.byref(p))
+    names = {f[0] for f in N.MohidAdParams._fields_}
+    for k, v in over.items():
+        if k not in names:
+            raise KeyError(f"unknown AdvectionDiffusion parameter {k!r}")
+        setattr(p, k, v)
+    return p
+
+
+def _size(ni, nj, nk):
+    work = N.T_Size3D(1, ni, 1, nj, 1, nk)
+    size = N.T_Size3D(0, ni + 1, 0, nj + 1, 0, nk + 1)
+    return size, work
+
+
+class AdvectionDiffusion:
+    """One transport instance on the current CUDA device (one grid)."""
+
+    def __init__(self, domain: Domain):
+        self.lib = N.ad_lib()
+        self.domain = domain
+        size, work = _size(domain.ni, domain.nj, domain.nk)
+        self._id = C.c_int(0)
+        st = C.c_int(0)
+        d = domain.arrays
+        rc = self.lib.mohid_ad_init(C.byref(self._id), C.byref(size), C.byref(work),
+                                    N.ptr(d["DUX"]), N.ptr(d["DVY"]), N.ptr(d["DZX"]),
+                                    N.ptr(d["DZY"]), N.iptr(d["KFloorZ"]),
+                                    N.iptr(d["BoundaryPoints2D"]), C.byref(st))
+        N.check(rc, "mohid_ad_init")
+        self._hydro_args = None
+
+    @property
+    def id(self) -> int:
+        return self._id.value
+
+    def set_hydro(self, domain: Domain | None = None, SmallDepths: np.ndarray | None = None):
+        d = (domain or self.domain).arrays
+        args = [N.ptr(d[n]) for n in F3] + [N.iptr(d[n]) for n in I3]
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_set_hydro(C.byref(self._id), *args,
+                                         N.iptr(SmallDepths) if SmallDepths is not None else None,
+                                         C.byref(st))
+        N.check(rc, "mohid_ad_set_hydro")
+
+    def set_hydro_device(self, t: dict, SmallDepths=None):
+        """Hydrodynamics already on the GPU: `t` maps field names to device tensors."""
+        args = [C.c_void_p(t[n].data_ptr()) for n in F3] + [C.c_void_p(t[n].data_ptr()) for n in I3]
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_set_hydro_dev(
+            C.byref(self._id), *[C.cast(a, N.c_double_p) for a in args[:11]],
+            *[C.cast(a, N.c_int_p) for a in args[11:]],
+            C.cast(C.c_void_p(SmallDepths.data_ptr()), N.c_int_p) if SmallDepths is not None else None,
+            C.byref(st))
+        N.check(rc, "mohid_ad_set_hydro_dev")
+
+    def step(self, PROP: np.ndarray, p: N.MohidAdParams, ReferenceProp: np.ndarray | None = None):
+        """AdvectionDiffusion for one property: PROP (float64, Size box) updated in place."""
+        if PROP.dtype != np.float64 or not PROP.flags.c_contiguous or PROP.shape != self.domain.shape3:
+            raise ValueError("PROP must be a C-contiguous float64 array of the Size box")
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_step_prop_f64(C.byref(self._id), N.ptr(PROP), N.ptr(ReferenceProp),
+                                             C.byref(p), C.byref(st))
+        N.check(rc, "mohid_ad_step_prop_f64")
+
+    def step_device(self, Pin, Pout, p: N.MohidAdParams, Ref=None):
+        """Device-resident step (torch CUDA float64 tensors); asynchronous on .stream."""
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_step_prop_f64_dev(
+            C.byref(self._id), C.c_void_p(Pin.data_ptr()), C.c_void_p(Pout.data_ptr()),
+            C.c_void_p(Ref.data_ptr()) if Ref is not None else None, C.byref(p), C.byref(st))
+        N.check(rc, "mohid_ad_step_prop_f64_dev")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.mohid_ad_stream(C.byref(self._id)) or 0
+
+    def sync(self):
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_sync(C.byref(self._id), C.byref(st)), "mohid_ad_sync")
+
+    def kill(self):
+        if self._id.value:
+            st = C.c_int(0)
+            N.check(self.lib.mohid_ad_kill(C.byref(self._id), C.byref(st)), "mohid_ad_kill")
+
+    def __del__(self):
+        try:
+            self.kill()
+        except Exception:
+            pass
+
+
+def thomasz(D, E, F, TI, RES, WaterPoints):
+    """THOMASZ_NewType2 on the GPU (replaces SolveThomas_C dim=2); RES updated in place."""
+    nk, nj, ni = (s - 2 for s in D.shape)
+    size = N.T_Size3D(0, ni + 1, 0, nj + 1, 0, nk + 1)
+    b = [C.c_int(v) for v in (1, ni, 1, nj, 1, nk)]
+    st = C.c_int(0)
+    rc = N.ad_lib().mohid_thomasz_f64(*[C.byref(x) for x in b], C.byref(size), N.ptr(D), N.ptr(E),
+                                      N.ptr(F), N.ptr(TI), N.ptr(RES), N.iptr(WaterPoints),
+                                      C.byref(st))
+    N.check(rc, "mohid_thomasz_f64")

@@ -1,0 +1,487 @@
+// abi.cpp -- C-ABI of the GB300 advection-diffusion step (declared in include/mohid_ad.h).
+//
+// Host-side replacement for the reference's transport entry point and for the
+// legacy CUDA Thomas binding:
+//   AdvectionDiffusion        ModuleAdvectionDiffusion.F90:1108-1509
+//   StartAdvectionDiffusion   ModuleAdvectionDiffusion.F90:400-535
+//   KillAdvectionDiffusion    ModuleAdvectionDiffusion.F90:5849
+//   SolveThomas_C & co.       Software/CudaThomas/Thomas.cu:6-56
+// Instances live in a mutex-protected registry keyed by an int id (the legacy
+// code used an unlocked static std::map, Thomas.cu:206).  Nothing here exits
+// the process: every failure becomes a status code.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "../../include/mohid_ad.h"
+#include "common.cuh"
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, int* stat, const std::string& msg)
+{
+    g_last_error = msg;
+    if (stat) *stat = code;
+    return code;
+}
+
+int ok(int* stat)
+{
+    if (stat) *stat = MOHID_AD_SUCCESS;
+    return MOHID_AD_SUCCESS;
+}
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        n = count;
+        return cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+struct Instance {
+    int device = 0;
+    int ni = 0, nj = 0, nk = 0;
+    size_t n2 = 0, n3 = 0;
+    cudaStream_t stream = nullptr;
+    // static 2-D metrics
+    DevBuf<double> DUX, DVY, DZX, DZY;
+    DevBuf<int> KFloor, BP2D;
+    // per-step hydrodynamics
+    DevBuf<double> Qx, Qy, Qz, Vold, V, ViscH, DiffV, AreaU, AreaV, DZZ, DWZ;
+    DevBuf<int> OP, LP, WP, CFU, CFV, CFW, SD;
+    bool hydro = false, hasSD = false;
+    // per-property staging for the host-pointer entry points
+    DevBuf<double> Pin, Pout, Ref;
+    DevBuf<unsigned int> status;
+    unsigned int* hstatus = nullptr;   // pinned
+
+    void release()
+    {
+        DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
+                               &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref};
+        for (auto* b : d) b->release();
+        DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD};
+        for (auto* b : i) b->release();
+        status.release();
+        if (hstatus) cudaFreeHost(hstatus);
+        hstatus = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+std::mutex g_mu;
+std::map<int, Instance*> g_inst;
+int g_next_id = 1;
+
+Instance* lookup(const int* id)
+{
+    if (!id) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_inst.find(*id);
+    return it == g_inst.end() ? nullptr : it->second;
+}
+
+std::string cuda_msg(const char* what, cudaError_t e)
+{
+    return std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+}
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg(#call, e_)); \
+    } while (0)
+
+// Option checks of AdvectionDiffusion (AD:1231-1239, AD:1340-1349,
+// Set_Internal_State AD:5816-5830) plus the options this build leaves out.
+int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why)
+{
+    if (!p) { why = "params is NULL"; return MOHID_AD_ERR_NULLPTR; }
+    if (!(p->DTProp > 0.0) || !std::isfinite(p->DTProp)) { why = "DTProp must be > 0"; return MOHID_AD_ERR_OPTION; }
+    const int mH = p->AdvMethodH, mV = p->AdvMethodV;
+    if (mH < 1 || mH > 6 || mV < 1 || mV > 6) { why = "AdvMethodH/V must be 1..6"; return MOHID_AD_ERR_OPTION; }
+    if ((p->ImpExp_AdvXX == 1.0 || p->ImpExp_AdvYY == 1.0) && (mH == 2 || mH == 3)) {
+        why = "implicit horizontal advection with UpwindOrder2/3 (reference ERR100)"; return MOHID_AD_ERR_OPTION;
+    }
+    if (p->ImpExp_AdvV == 1.0 && (mV == 2 || mV == 3)) {
+        why = "implicit vertical advection with UpwindOrder2/3 (reference ERR200)"; return MOHID_AD_ERR_OPTION;
+    }
+    if (p->ImpExp_DifH != 0.0) { why = "horizontal diffusion must be explicit (reference ERR02)"; return MOHID_AD_ERR_OPTION; }
+    if (p->ImpExp_AdvXX == 1.0 && p->ImpExp_AdvYY == 1.0) { why = "implicit advection in both horizontal directions (reference ERR03)"; return MOHID_AD_ERR_OPTION; }
+    if (p->ImpExp_AdvV != 0.0 && p->ImpExp_AdvV != 1.0) { why = "ImpExp_AdvV must be 0 or 1 (reference ERR01)"; return MOHID_AD_ERR_OPTION; }
+    if ((mH >= 2 && mH <= 4) && !p->Upwind2H) { why = "AdvMethodH 2..4 needs Upwind2H near boundaries"; return MOHID_AD_ERR_OPTION; }
+    if ((mV >= 2 && mV <= 4) && !p->Upwind2V) { why = "AdvMethodV 2..4 needs Upwind2V near boundaries"; return MOHID_AD_ERR_OPTION; }
+    if (mH == 4 && (p->TVDLimitationH < 1 || p->TVDLimitationH > 5)) { why = "TVDLimitationH must be 1..5"; return MOHID_AD_ERR_OPTION; }
+    if (mV == 4 && (p->TVDLimitationV < 1 || p->TVDLimitationV > 5)) { why = "TVDLimitationV must be 1..5"; return MOHID_AD_ERR_OPTION; }
+    if (p->Docycle_method != 1 && p->Docycle_method != 2) { why = "Docycle_method must be 1 or 2"; return MOHID_AD_ERR_OPTION; }
+    if (hasRef) {
+        const int bc = p->BoundaryCondition;
+        if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
+            why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
+        }
+        if (bc != 1 && bc != 2 && bc != 5) { why = "BoundaryCondition 4/6/7/8 not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    }
+    if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->CellFluxes) { why = "CellFluxes not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->NoAdvFlux || p->NoDifFlux) { why = "NoAdvFlux/NoDifFlux not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (nk > 200) { why = "KUB > 200 layers not supported"; return MOHID_AD_ERR_UNSUPPORTED; }
+    return MOHID_AD_SUCCESS;
+}
+
+int status_to_code(unsigned int s, std::string& why)
+{
+    if (s & MOHID_DEV_BAD_FACE) { why = "a compute face lies on the lower edge of the work box"; return MOHID_AD_ERR_BOUNDS; }
+    if (s & MOHID_DEV_ZERO_PIVOT) { why = "THOMASZ zero pivot in a water column"; return MOHID_AD_ERR_ZERO_PIVOT; }
+    if (s & MOHID_DEV_NONFINITE) { why = "non-finite concentration after the solve"; return MOHID_AD_ERR_NONFINITE; }
+    if (s & MOHID_DEV_TIMEOUT) { why = "bounded device wait expired"; return MOHID_AD_ERR_TIMEOUT; }
+    return MOHID_AD_SUCCESS;
+}
+
+mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const double* Ref,
+                           const mohid_ad_params* p)
+{
+    mohid::PlainArgs a;
+    a.ni = in->ni; a.nj = in->nj; a.nk = in->nk;
+    a.sj = in->ni + 2;
+    a.sk = (long long)(in->ni + 2) * (in->nj + 2);
+    a.P = Pin; a.Pout = Pout;
+    a.Qx = in->Qx.p; a.Qy = in->Qy.p; a.Qz = in->Qz.p; a.Vold = in->Vold.p; a.V = in->V.p;
+    a.ViscH = in->ViscH.p; a.DiffV = in->DiffV.p; a.AreaU = in->AreaU.p; a.AreaV = in->AreaV.p;
+    a.DZZ = in->DZZ.p; a.DWZ = in->DWZ.p;
+    a.OP = in->OP.p; a.LP = in->LP.p; a.WP = in->WP.p; a.CFU = in->CFU.p; a.CFV = in->CFV.p;
+    a.CFW = in->CFW.p; a.SD = in->hasSD ? in->SD.p : nullptr;
+    a.DUX = in->DUX.p; a.DVY = in->DVY.p; a.DZX = in->DZX.p; a.DZY = in->DZY.p;
+    a.KFloor = in->KFloor.p; a.BP2D = in->BP2D.p;
+    a.Ref = Ref;
+    a.DT = p->DTProp;
+    a.schmidtH = p->schmidt_H; a.schmidtCoefV = p->SchmidtCoef_V; a.schmidtBackV = p->SchmidtBackground_V;
+    a.volumeRelMax = p->VolumeRelMax; a.impExpDifV = p->ImpExp_DifV;
+    // OpenBoundaryCondition AD:5418-5419: TdecAux = 1/(1 + DecayTime/DTProp)
+    a.tdecAux = 1.0 / (1.0 + p->DecayTime / p->DTProp);
+    a.methodH = p->AdvMethodH; a.limiterH = p->TVDLimitationH;
+    a.methodV = p->AdvMethodV; a.limiterV = p->TVDLimitationV;
+    a.upwind2H = p->Upwind2H != 0; a.upwind2V = p->Upwind2V != 0;
+    a.nullDif = p->NullDif != 0;
+    a.explicitV = p->ImpExp_AdvV == 0.0;
+    a.docycle = p->Docycle_method;
+    a.vertical1D = p->Vertical1D != 0; a.xzflow = p->XZFlow != 0;
+    a.bc = p->BoundaryCondition;
+    a.status = in->status.p;
+    return a;
+}
+
+int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const double* Wflux_Y,
+                 const double* Wflux_Z, const double* VolumeZOld, const double* VolumeZ,
+                 const double* Visc_H, const double* Diff_V, const double* AreaU,
+                 const double* AreaV, const double* DZZ, const double* DWZ, const int* OpenPoints3D,
+                 const int* LandPoints3D, const int* WaterPoints3D, const int* ComputeFacesU3D,
+                 const int* ComputeFacesV3D, const int* ComputeFacesW3D, const int* SmallDepths,
+                 int* stat)
+{
+    const void* src[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU,
+                         AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
+                         ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D};
+    for (const void* s : src)
+        if (!s) return fail(MOHID_AD_ERR_NULLPTR, stat, "a required hydrodynamic array is NULL");
+    const cudaMemcpyKind kind = fromDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CK(cudaSetDevice(in->device));
+    const size_t bd = sizeof(double) * in->n3, bi = sizeof(int) * in->n3;
+    DevBuf<double>* dd[] = {&in->Qx, &in->Qy, &in->Qz, &in->Vold, &in->V, &in->ViscH, &in->DiffV,
+                            &in->AreaU, &in->AreaV, &in->DZZ, &in->DWZ};
+    const double* ds[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU, AreaV, DZZ, DWZ};
+    for (int q = 0; q < 11; ++q) CK(cudaMemcpyAsync(dd[q]->p, ds[q], bd, kind, in->stream));
+    DevBuf<int>* di[] = {&in->OP, &in->LP, &in->WP, &in->CFU, &in->CFV, &in->CFW};
+    const int* is[] = {OpenPoints3D, LandPoints3D, WaterPoints3D, ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D};
+    for (int q = 0; q < 6; ++q) CK(cudaMemcpyAsync(di[q]->p, is[q], bi, kind, in->stream));
+    in->hasSD = SmallDepths != nullptr;
+    if (SmallDepths) CK(cudaMemcpyAsync(in->SD.p, SmallDepths, sizeof(int) * in->n2, kind, in->stream));
+    CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
+    CK(mohid::launch_check_faces(in->ni, in->nj, in->nk, in->CFU.p, in->CFV.p, in->CFW.p,
+                                 in->status.p, in->stream));
+    CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
+    CK(cudaStreamSynchronize(in->stream));
+    std::string why;
+    int code = status_to_code(*in->hstatus, why);
+    in->hydro = code == MOHID_AD_SUCCESS;
+    if (code) return fail(code, stat, why);
+    return ok(stat);
+}
+
+}  // namespace
+
+extern "C" {
+
+void mohid_ad_default_params(mohid_ad_params* p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->schmidt_H = 1.0;
+    p->SchmidtCoef_V = 1.0;
+    p->SchmidtBackground_V = 1e-8;
+    p->AdvMethodH = MOHID_UPWIND_ORDER1;
+    p->TVDLimitationH = MOHID_TVD_SUPERBEE;
+    p->AdvMethodV = MOHID_UPWIND_ORDER1;
+    p->TVDLimitationV = MOHID_TVD_SUPERBEE;
+    p->VolumeRelMax = 1.5;
+    p->DTProp = 1.0;
+    p->ImpExp_AdvV = 1.0;
+    p->ImpExp_DifV = 1.0;
+    p->BoundaryCondition = MOHID_BC_MASS_CONSERVATION;
+    p->DecayTime = 0.0;
+    p->Docycle_method = 1;
+}
+
+const char* mohid_ad_last_error(void) { return g_last_error.c_str(); }
+
+const char* mohid_ad_version(void) { return "mohid-gb300 0.1 sm_103a"; }
+
+int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize, const double* DUX,
+                  const double* DVY, const double* DZX, const double* DZY, const int* KFloorZ,
+                  const int* BoundaryPoints2D, int* stat)
+{
+    if (!id || !size || !worksize || !DUX || !DVY || !DZX || !DZY || !KFloorZ || !BoundaryPoints2D)
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_ad_init: NULL argument");
+    const T_Size3D& s = *size;
+    const T_Size3D& w = *worksize;
+    if (w.ILB != 1 || w.JLB != 1 || w.KLB != 1 || w.IUB < 1 || w.JUB < 1 || w.KUB < 1 ||
+        s.ILB != w.ILB - 1 || s.IUB != w.IUB + 1 || s.JLB != w.JLB - 1 || s.JUB != w.JUB + 1 ||
+        s.KLB != w.KLB - 1 || s.KUB != w.KUB + 1)
+        return fail(MOHID_AD_ERR_BOUNDS, stat,
+                    "mohid_ad_init: WorkSize must start at 1 and Size must be WorkSize +/- 1");
+    Instance* in = new Instance();
+    in->ni = w.IUB; in->nj = w.JUB; in->nk = w.KUB;
+    in->n2 = (size_t)(in->ni + 2) * (size_t)(in->nj + 2);
+    in->n3 = in->n2 * (size_t)(in->nk + 2);
+    auto bad = [&](cudaError_t e, const char* what) {
+        std::string m = cuda_msg(what, e);
+        in->release();
+        delete in;
+        int code = (e == cudaErrorMemoryAllocation) ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA;
+        return fail(code, stat, m);
+    };
+    cudaError_t e = cudaGetDevice(&in->device);
+    if (e != cudaSuccess) return bad(e, "cudaGetDevice");
+    if ((e = cudaStreamCreateWithFlags(&in->stream, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "cudaStreamCreate");
+    DevBuf<double>* d2[] = {&in->DUX, &in->DVY, &in->DZX, &in->DZY};
+    for (auto* b : d2) if ((e = b->alloc(in->n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    DevBuf<int>* i2[] = {&in->KFloor, &in->BP2D, &in->SD};
+    for (auto* b : i2) if ((e = b->alloc(in->n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    DevBuf<double>* d3[] = {&in->Qx, &in->Qy, &in->Qz, &in->Vold, &in->V, &in->ViscH, &in->DiffV,
+                            &in->AreaU, &in->AreaV, &in->DZZ, &in->DWZ, &in->Pin, &in->Pout, &in->Ref};
+    for (auto* b : d3) if ((e = b->alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    DevBuf<int>* i3[] = {&in->OP, &in->LP, &in->WP, &in->CFU, &in->CFV, &in->CFW};
+    for (auto* b : i3) if ((e = b->alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = in->status.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaMallocHost((void**)&in->hstatus, sizeof(unsigned int))) != cudaSuccess) return bad(e, "cudaMallocHost");
+    const double* s2[] = {DUX, DVY, DZX, DZY};
+    for (int q = 0; q < 4; ++q)
+        if ((e = cudaMemcpy(d2[q]->p, s2[q], sizeof(double) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bad(e, "cudaMemcpy");
+    if ((e = cudaMemcpy(in->KFloor.p, KFloorZ, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
+    if ((e = cudaMemcpy(in->BP2D.p, BoundaryPoints2D, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        *id = g_next_id++;
+        g_inst[*id] = in;
+    }
+    return ok(stat);
+}
+
+int mohid_ad_set_hydro(const int* id, const double* Wflux_X, const double* Wflux_Y,
+                       const double* Wflux_Z, const double* VolumeZOld, const double* VolumeZ,
+                       const double* Visc_H, const double* Diff_V, const double* AreaU,
+                       const double* AreaV, const double* DZZ, const double* DWZ,
+                       const int* OpenPoints3D, const int* LandPoints3D, const int* WaterPoints3D,
+                       const int* ComputeFacesU3D, const int* ComputeFacesV3D,
+                       const int* ComputeFacesW3D, const int* SmallDepths, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    return upload_hydro(in, false, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
+                        AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
+                        ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
+}
+
+int mohid_ad_set_hydro_dev(const int* id, const double* Wflux_X, const double* Wflux_Y,
+                           const double* Wflux_Z, const double* VolumeZOld, const double* VolumeZ,
+                           const double* Visc_H, const double* Diff_V, const double* AreaU,
+                           const double* AreaV, const double* DZZ, const double* DWZ,
+                           const int* OpenPoints3D, const int* LandPoints3D,
+                           const int* WaterPoints3D, const int* ComputeFacesU3D,
+                           const int* ComputeFacesV3D, const int* ComputeFacesW3D,
+                           const int* SmallDepths, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    return upload_hydro(in, true, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
+                        AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
+                        ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
+}
+
+int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PROP_out,
+                               const double* ReferenceProp, const mohid_ad_params* p, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!PROP_in || !PROP_out) return fail(MOHID_AD_ERR_NULLPTR, stat, "PROP pointer is NULL");
+    if (PROP_in == PROP_out) return fail(MOHID_AD_ERR_OPTION, stat, "PROP_in and PROP_out must differ");
+    if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "no hydrodynamics set for this instance");
+    std::string why;
+    int code = check_params(p, ReferenceProp != nullptr, in->nk, why);
+    if (code) return fail(code, stat, why);
+    CK(cudaSetDevice(in->device));
+    mohid::PlainArgs a = make_args(in, PROP_in, PROP_out, ReferenceProp, p);
+    CK(mohid::launch_plain_f64(a, in->stream));
+    return ok(stat);
+}
+
+int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
+                           const mohid_ad_params* p, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!PROP) return fail(MOHID_AD_ERR_NULLPTR, stat, "PROP is NULL");
+    if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "no hydrodynamics set for this instance");
+    std::string why;
+    int code = check_params(p, ReferenceProp != nullptr, in->nk, why);
+    if (code) return fail(code, stat, why);
+    CK(cudaSetDevice(in->device));
+    const size_t bd = sizeof(double) * in->n3;
+    CK(cudaMemcpyAsync(in->Pin.p, PROP, bd, cudaMemcpyHostToDevice, in->stream));
+    if (ReferenceProp) CK(cudaMemcpyAsync(in->Ref.p, ReferenceProp, bd, cudaMemcpyHostToDevice, in->stream));
+    CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
+    mohid::PlainArgs a = make_args(in, in->Pin.p, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p);
+    CK(mohid::launch_plain_f64(a, in->stream));
+    CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
+    CK(cudaMemcpyAsync(PROP, in->Pout.p, bd, cudaMemcpyDeviceToHost, in->stream));
+    CK(cudaStreamSynchronize(in->stream));
+    code = status_to_code(*in->hstatus, why);
+    if (code) return fail(code, stat, why);
+    return ok(stat);
+}
+
+int mohid_ad_step_f64(const int* id, double* PROP, const mohid_ad_params* p, const double* Wflux_X,
+                      const double* Wflux_Y, const double* Wflux_Z, const double* VolumeZOld,
+                      const double* VolumeZ, const double* Visc_H, const double* Diff_V,
+                      const double* AreaU, const double* AreaV, const double* DZZ,
+                      const double* DWZ, const int* OpenPoints3D, const int* LandPoints3D,
+                      const int* WaterPoints3D, const int* ComputeFacesU3D,
+                      const int* ComputeFacesV3D, const int* ComputeFacesW3D,
+                      const int* SmallDepths, const double* ReferenceProp, int* stat)
+{
+    int code = mohid_ad_set_hydro(id, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H,
+                                  Diff_V, AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D,
+                                  WaterPoints3D, ComputeFacesU3D, ComputeFacesV3D,
+                                  ComputeFacesW3D, SmallDepths, stat);
+    if (code) return code;
+    return mohid_ad_step_prop_f64(id, PROP, ReferenceProp, p, stat);
+}
+
+int mohid_ad_sync(const int* id, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    CK(cudaSetDevice(in->device));
+    CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
+    CK(cudaStreamSynchronize(in->stream));
+    std::string why;
+    int code = status_to_code(*in->hstatus, why);
+    CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
+    if (code) return fail(code, stat, why);
+    return ok(stat);
+}
+
+void* mohid_ad_stream(const int* id)
+{
+    Instance* in = lookup(id);
+    return in ? (void*)in->stream : nullptr;
+}
+
+int mohid_ad_kill(int* id, int* stat)
+{
+    Instance* in = nullptr;
+    if (id) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_inst.find(*id);
+        if (it != g_inst.end()) { in = it->second; g_inst.erase(it); }
+    }
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    cudaSetDevice(in->device);
+    cudaStreamSynchronize(in->stream);
+    in->release();
+    delete in;
+    *id = 0;
+    return ok(stat);
+}
+
+int mohid_thomasz_f64(const int* ILB, const int* IUB, const int* JLB, const int* JUB,
+                      const int* KLB, const int* KUB, const T_Size3D* size, const double* D,
+                      const double* E, const double* F, const double* TI, double* RES,
+                      const int* WaterPoints, int* stat)
+{
+    if (!ILB || !IUB || !JLB || !JUB || !KLB || !KUB || !size || !D || !E || !F || !TI || !RES || !WaterPoints)
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_thomasz_f64: NULL argument");
+    if (*ILB != 1 || *JLB != 1 || *KLB != 1 || *IUB < 1 || *JUB < 1 || *KUB < 1 ||
+        size->ILB != 0 || size->JLB != 0 || size->KLB != 0 || size->IUB != *IUB + 1 ||
+        size->JUB != *JUB + 1 || size->KUB != *KUB + 1)
+        return fail(MOHID_AD_ERR_BOUNDS, stat, "mohid_thomasz_f64: bounds must be WorkSize 1..N inside Size 0..N+1");
+    if (*KUB > 200) return fail(MOHID_AD_ERR_UNSUPPORTED, stat, "KUB > 200 layers not supported");
+    const int ni = *IUB, nj = *JUB, nk = *KUB;
+    const size_t n3 = (size_t)(ni + 2) * (nj + 2) * (nk + 2);
+    const size_t bd = n3 * sizeof(double);
+    double *dD = nullptr, *dE = nullptr, *dF = nullptr, *dT = nullptr, *dR = nullptr;
+    int* dW = nullptr;
+    unsigned int* dS = nullptr;
+    unsigned int hS = 0;
+    cudaStream_t s = nullptr;
+    int code = MOHID_AD_SUCCESS;
+    std::string why;
+    auto run = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        double** bufs[] = {&dD, &dE, &dF, &dT, &dR};
+        for (auto* b : bufs) if ((e = cudaMalloc((void**)b, bd)) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&dW, n3 * sizeof(int))) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&dS, sizeof(unsigned int))) != cudaSuccess) return e;
+        const double* src[] = {D, E, F, TI, RES};
+        double* dst[] = {dD, dE, dF, dT, dR};
+        for (int q = 0; q < 5; ++q)
+            if ((e = cudaMemcpyAsync(dst[q], src[q], bd, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(dW, WaterPoints, n3 * sizeof(int), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(dS, 0, sizeof(unsigned int), s)) != cudaSuccess) return e;
+        if ((e = mohid::launch_thomasz_f64(ni, nj, nk, dD, dE, dF, dT, dR, dW, dS, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(RES, dR, bd, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(&hS, dS, sizeof(unsigned int), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        return cudaStreamSynchronize(s);
+    };
+    cudaError_t e = run();
+    double* bufs[] = {dD, dE, dF, dT, dR};
+    for (double* b : bufs) if (b) cudaFree(b);
+    if (dW) cudaFree(dW);
+    if (dS) cudaFree(dS);
+    if (s) cudaStreamDestroy(s);
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat, cuda_msg("mohid_thomasz_f64", e));
+    code = status_to_code(hS, why);
+    if (code) return fail(code, stat, why);
+    return ok(stat);
+}
+
+}  // extern "C"

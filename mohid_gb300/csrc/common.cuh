@@ -1,0 +1,43 @@
+// common.cuh -- shared definitions of the GB300 advection-diffusion kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define MOHID_NULL_REAL_D (-9.9e15)   // null_real, ModuleGlobalData.F90:143
+#define MOHID_MINVALUE_D 1.e-16       // MinValue,  ModuleGlobalData.F90:1812
+
+// Device status bits, latched with atomicOr and read by the host after a step.
+#define MOHID_DEV_ZERO_PIVOT 1u
+#define MOHID_DEV_NONFINITE  2u
+#define MOHID_DEV_BAD_FACE   4u
+#define MOHID_DEV_TIMEOUT    8u
+
+namespace mohid {
+
+// Arguments of the plain FP64 step: Fortran layout over the Size box
+// (0:ni+1, 0:nj+1, 0:nk+1), i fastest, strides sj = ni+2, sk = (ni+2)(nj+2).
+struct PlainArgs {
+    int ni, nj, nk;
+    long long sj, sk;
+    const double* P;
+    double* Pout;
+    const double *Qx, *Qy, *Qz, *Vold, *V, *ViscH, *DiffV, *AreaU, *AreaV, *DZZ, *DWZ;
+    const int *OP, *LP, *WP, *CFU, *CFV, *CFW, *SD;
+    const double *DUX, *DVY, *DZX, *DZY;
+    const int *KFloor, *BP2D;
+    const double* Ref;          // nullptr: closed boundaries
+    double DT, schmidtH, schmidtCoefV, schmidtBackV, volumeRelMax, impExpDifV, tdecAux;
+    int methodH, limiterH, methodV, limiterV, upwind2H, upwind2V;
+    int nullDif, explicitV, docycle, vertical1D, xzflow, bc;
+    unsigned int* status;
+};
+
+// Launchers (plain_f64.cu)
+cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s);
+cudaError_t launch_thomasz_f64(int ni, int nj, int nk, const double* D, const double* E,
+                               const double* F, const double* TI, double* RES, const int* WP,
+                               unsigned int* status, cudaStream_t s);
+cudaError_t launch_check_faces(int ni, int nj, int nk, const int* CFU, const int* CFV,
+                               const int* CFW, unsigned int* status, cudaStream_t s);
+
+}  // namespace mohid

@@ -1,0 +1,526 @@
+// plain_f64.cu -- the plain FP64 drop-in step (one property, Fortran layout).
+//
+// One thread owns one water column (i,j); lanes of a warp run along i, so every
+// load of a layer is coalesced.  Walking k = 1..KUB the thread assembles row k
+// of the tridiagonal system exactly as ModuleAdvectionDiffusion accumulates it
+// over its full-array passes (same operands, same order, no fused multiply-add:
+// this file is compiled with --fmad=false), eliminates it at once (THOMASZ
+// forward sweep, W in shared memory, G parked in the output array), then
+// back-substitutes from KUB+1.  The reference's coefficient arrays (D, E, F,
+// TI, 12 flux-coefficient arrays, Kx/Ky/Kz) never exist in memory.
+//
+// Row k of the system (reference passes, in call order):
+//   VolumeVariation                 AD:3966-4021
+//   HorizontalDiffusionXX / YY      AD:5156-5214 / AD:5313-5365 (Kx/Ky AD:2453-2595)
+//   HorizontalAdvectionXX / YY      AD:4368-4540 / AD:4739-4910
+//        face coefficients          FN:10534-10591, FN:10702-10894
+//   VerticalDiffusion               AD:2708-2784 (Kz AD:2364-2443)
+//   VerticalAdvection               AD:2941-3140
+//   OpenBoundaryCondition           AD:5369-5742
+//   land -> null_real               AD:1753
+//   THOMASZ_NewType2                FN:4026-4123
+#include "common.cuh"
+
+namespace mohid {
+namespace {
+
+constexpr int kBX = 32, kBY = 4, kThreads = kBX * kBY;
+
+__device__ __forceinline__ double dmin2(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dmax2(double a, double b) { return (b > a) ? b : a; }
+
+// ComputeAdvectionFace (FN:10702-10894) for options validated on the host.
+// Stencil values are fetched through `ld(n)` (n = 0..3 <-> cells f-2..f+1)
+// only by the methods that read them.
+template <class LP, class LV, class LD>
+__device__ __forceinline__ void face_coef(double Q, double dt, double VRM, int method, int limiter,
+                                          bool nb, bool up2, LP ldP, LV ldV, LD ldU, double CF[4])
+{
+    double Cup1[4] = {0., 0., 0., 0.};
+    if (Q > 0.) Cup1[1] = 1.; else Cup1[2] = 1.;
+    if (method == 1 || (nb && up2)) {            // UpwindOrder1: CupHigh = Cup1, Theta = 0
+        const double T = 0.;
+        for (int n = 0; n < 4; ++n) CF[n] = (1. - T) * Cup1[n] + T * Cup1[n];
+        return;
+    }
+    double Cr = 0., VolumeRel = 0.;
+    if (!nb) {
+        double v0 = ldV(0), v1 = ldV(1), v2 = ldV(2), v3 = ldV(3);
+        if (Q > 0) {
+            Cr = Q * dt / v1;
+            double Aux = dmin2(dmin2(v0, v1), v2);
+            VolumeRel = dmax2(dmax2(v0, v1), v2) / Aux;
+        } else {
+            Cr = Q * dt / v2;
+            double Aux = dmin2(dmin2(v1, v2), v3);
+            VolumeRel = dmax2(dmax2(v1, v2), v3) / Aux;
+        }
+    }
+    double CH[4] = {0., 0., 0., 0.};
+    double Theta;
+    if (method == 2) {                           // FaceConcUpSecondOrder FN:11055
+        if (Q > 0) { CH[0] = -1. / 8.; CH[1] = 6. / 8.; CH[2] = 3. / 8.; }
+        else if (Q < 0) { CH[3] = -1. / 8.; CH[2] = 6. / 8.; CH[1] = 3. / 8.; }
+        else { CH[2] = 1.; }
+        Theta = (VolumeRel > VRM) ? 0. : 1.;
+    } else if (method == 3) {                    // FaceConcUpThirdOrder FN:11086
+        double c = (1 - 2. * fabs(Cr)) / 6.;
+        double a = 0.5 + c, b = 0.5 - c, d = (1 - fabs(Cr)) / 2.;
+        if (Q > 0) { CH[0] = -d * b; CH[1] = 1 + d * (b - a); CH[2] = d * a; CH[3] = 0.; }
+        else if (Q < 0) { CH[3] = -d * b; CH[2] = 1 + d * (b - a); CH[1] = d * a; CH[0] = 0.; }
+        else { CH[2] = 1.; }
+        Theta = (VolumeRel > VRM) ? 0. : 1.;
+    } else if (method == 5 || method == 6) {     // CentralDif / LeapFrog
+        double u1 = ldU(1), u2 = ldU(2);
+        CH[1] = u2 / (u1 + u2);
+        CH[2] = u1 / (u1 + u2);
+        Theta = 1.;
+    } else {                                     // P2_TVD, not near a boundary
+        double p0 = ldP(0), p1 = ldP(1), p2 = ldP(2), p3 = ldP(3);
+        double u0 = ldU(0), u1 = ldU(1), u2 = ldU(2), u3 = ldU(3);
+        double dC, r;
+        if (Q > 0.) {
+            CH[2] = 1.;
+            dC = (p2 - p1) / (u2 + u1);
+            if (fabs(dC) < MOHID_MINVALUE_D) dC = (dC >= 0) ? MOHID_MINVALUE_D : -MOHID_MINVALUE_D;
+            r = (p1 - p0) / (u1 + u0) / dC;
+        } else {
+            CH[1] = 1.;
+            dC = (p1 - p2) / (u2 + u1);
+            if (fabs(dC) < MOHID_MINVALUE_D) dC = (dC >= 0) ? MOHID_MINVALUE_D : -MOHID_MINVALUE_D;
+            r = (p2 - p3) / (u2 + u3) / dC;
+        }
+        if (limiter == 1) {
+            Theta = dmax2(0., dmin2(1., r));
+        } else if (limiter == 2) {
+            Theta = (r < 0) ? 0. : 2. * r / (1 + r);
+        } else if (limiter == 3) {
+            Theta = dmax2(0., dmin2(dmin2(2., 2. * r), (1 + r) / 2.));
+        } else if (limiter == 4) {
+            Theta = dmax2(dmax2(0., dmin2(1., 2. * r)), dmin2(r, 2.));
+        } else {
+            double a = 0.5 + (1 - 2. * fabs(Cr)) / 6.;
+            double b = 0.5 - (1 - 2. * fabs(Cr)) / 6.;
+            double Aux = a + b * r;
+            if (fabs(Cr) < MOHID_MINVALUE_D) Cr = MOHID_MINVALUE_D;
+            Theta = dmax2(0., dmin2(dmin2(Aux, 2. / (1. - Cr)), 2. * r / Cr));
+        }
+        Theta = 0.5 * Theta * (1. - Cr);
+    }
+    for (int n = 0; n < 4; ++n) CF[n] = (1. - Theta) * Cup1[n] + Theta * CH[n];
+}
+
+// Explicit advective flux through the face between cells `m` (= a - s) and `a`
+// along stride `s`; `f` is the face index along that axis (1..N), du indexed
+// by du(f + n - 2).  Coefficients are computed only where both cells are
+// OpenPoints (FN:10559); elsewhere they stay zero, as the reference's arrays.
+template <class DU>
+__device__ __forceinline__ double adv_flux(const PlainArgs& A, size_t a, long long s, const double* Q,
+                                           int method, int limiter, bool up2, DU du)
+{
+    const double* P = A.P;
+    const int* OP = A.OP;
+    double C[4] = {0., 0., 0., 0.};
+    if (__ldg(OP + a - s) == 1 && __ldg(OP + a) == 1) {
+        double QF = __ldg(Q + a);
+        bool nb = (QF > 0) ? (__ldg(OP + a - 2 * s) != 1) : (__ldg(OP + a + s) != 1);
+        double CF[4];
+        face_coef(QF, A.DT, A.volumeRelMax, method, limiter, nb, up2,
+                  [&](int n) { return __ldg(P + a + (long long)(n - 2) * s); },
+                  [&](int n) { return __ldg(A.V + a + (long long)(n - 2) * s); },
+                  [&](int n) { return du(n); }, CF);
+        for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
+    }
+    return C[0] * __ldg(P + a - 2 * s) + C[1] * __ldg(P + a - s) + C[2] * __ldg(P + a) +
+           C[3] * __ldg(P + a + s);
+}
+
+__global__ void __launch_bounds__(kThreads)
+plain_f64_kernel(const PlainArgs A)
+{
+    extern __shared__ double sW[];               // W(k) at sW[k * kThreads + tid]
+    const int tid = threadIdx.y * kBX + threadIdx.x;
+    const int i = blockIdx.x * kBX + threadIdx.x;    // 0..ni+1 (Size box)
+    const int j = blockIdx.y * kBY + threadIdx.y;    // 0..nj+1
+    const int ni = A.ni, nj = A.nj, nk = A.nk;
+    if (i > ni + 1 || j > nj + 1) return;
+    const long long sj = A.sj, sk = A.sk;
+    const size_t c = (size_t)i + (size_t)sj * (size_t)j;     // (i,j,0)
+    const double* P = A.P;
+    double* Po = A.Pout;
+
+    const bool interior = i >= 1 && i <= ni && j >= 1 && j <= nj;
+    const bool solve = interior && __ldg(A.WP + c + (size_t)sk * nk) == 1;
+    if (!solve) {                                 // THOMASZ leaves the column untouched
+        for (int k = 0; k <= nk + 1; ++k) Po[c + (size_t)sk * k] = __ldg(P + c + (size_t)sk * k);
+        return;
+    }
+    Po[c] = __ldg(P + c);                         // row 0 is never solved
+
+    const double DT = A.DT;
+    const double DUXc = __ldg(A.DUX + c), DVYc = __ldg(A.DVY + c);
+    const int kb = __ldg(A.KFloor + c);
+    const bool sd = A.SD != nullptr && __ldg(A.SD + c) != 0;
+    const bool colOpenTop = __ldg(A.OP + c + (size_t)sk * nk) == 1;
+    const bool colCFWTop = __ldg(A.CFW + c + (size_t)sk * nk) == 1;
+    const bool bp = A.Ref != nullptr && __ldg(A.BP2D + c) == 1;
+    const int kbp = kb < 0 ? -kb : kb;
+    const double ie = A.impExpDifV;
+    const bool doVert = nk > 1;
+    const bool doVAdv = doVert && !A.vertical1D;
+
+    // vertical face helpers -------------------------------------------------
+    auto Kz = [&](size_t a) {                    // Convert_Dif_Vertical AD:2397-2424
+        double kz = A.schmidtCoefV * __ldg(A.DiffV + a) + A.schmidtBackV;
+        if (A.nullDif && __ldg(A.Qz + a) == 0.) kz = 0.;
+        return kz;
+    };
+    // vertical advection coefficients of face k (k = 1..nk), AD:2986-3001
+    auto vcoef = [&](int k, double C[4]) {
+        C[0] = C[1] = C[2] = C[3] = 0.;
+        size_t a = c + (size_t)sk * k;
+        if (colOpenTop && __ldg(A.OP + a - sk) == 1 && __ldg(A.OP + a) == 1) {
+            double QF = __ldg(A.Qz + a);
+            bool nb = (QF > 0) ? (__ldg(A.OP + a - 2 * sk) != 1) : (__ldg(A.OP + a + sk) != 1);
+            double CF[4];
+            face_coef(QF, DT, A.volumeRelMax, A.methodV, A.limiterV, nb, A.upwind2V != 0,
+                      [&](int n) { return __ldg(P + a + (long long)(n - 2) * sk); },
+                      [&](int n) { return __ldg(A.V + a + (long long)(n - 2) * sk); },
+                      [&](int n) { return __ldg(A.DWZ + a + (long long)(n - 2) * sk); }, CF);
+            for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
+        }
+    };
+
+    unsigned int flags = 0;
+    double Wp = 0., Gp = 0.;                      // W(k-1), G(k-1)
+    double Pk = __ldg(P + c + (size_t)sk);        // P(k) sliding window
+    for (int k = 1; k <= nk; ++k) {
+        const size_t a = c + (size_t)sk * k;
+        const double Vk = __ldg(A.V + a);
+        const int opk = __ldg(A.OP + a);
+        const double Pkp1 = __ldg(P + a + sk);
+        double D = 0., E = 1., F = 0., TI;
+
+        // VolumeVariation
+        if (opk == 1) {
+            TI = Pk * (__ldg(A.Vold + a) / Vk);
+            if (k == nk) {
+                double DT_V = DT / Vk;
+                E = 1.0 + DT_V * __ldg(A.Qz + a + sk);
+            }
+        } else {
+            TI = Pk;
+        }
+
+        if (!A.vertical1D) {
+            // HorizontalDiffusionXX: west face j, east face j+1 (loop runs j = JLB..JUB)
+            if (__ldg(A.CFU + a) == 1) {
+                size_t am = a - sj;
+                double Kx = A.schmidtH * (__ldg(A.ViscH + a) * __ldg(A.DUX + c - sj) +
+                                          __ldg(A.ViscH + am) * __ldg(A.DUX + c)) /
+                            (__ldg(A.DUX + c) + __ldg(A.DUX + c - sj));
+                if (A.nullDif && __ldg(A.Qx + a) == 0.) Kx = 0.;
+                double AuxJ = Kx * __ldg(A.AreaU + a) / __ldg(A.DZX + c - sj);
+                TI = TI - AuxJ * DT / Vk * (Pk - __ldg(P + am));
+            }
+            if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
+                size_t ap = a + sj;
+                double Kx = A.schmidtH * (__ldg(A.ViscH + ap) * __ldg(A.DUX + c) +
+                                          __ldg(A.ViscH + a) * __ldg(A.DUX + c + sj)) /
+                            (__ldg(A.DUX + c + sj) + __ldg(A.DUX + c));
+                if (A.nullDif && __ldg(A.Qx + ap) == 0.) Kx = 0.;
+                double AuxJ = Kx * __ldg(A.AreaU + ap) / __ldg(A.DZX + c);
+                TI = TI + AuxJ * DT / Vk * (__ldg(P + ap) - Pk);
+            }
+            // HorizontalDiffusionYY
+            if (!A.xzflow) {
+                if (__ldg(A.CFV + a) == 1) {
+                    size_t am = a - 1;
+                    double Ky = A.schmidtH * (__ldg(A.ViscH + a) * __ldg(A.DVY + c - 1) +
+                                              __ldg(A.ViscH + am) * __ldg(A.DVY + c)) /
+                                (__ldg(A.DVY + c) + __ldg(A.DVY + c - 1));
+                    if (A.nullDif && __ldg(A.Qy + a) == 0.) Ky = 0.;
+                    double AuxI = Ky * __ldg(A.AreaV + a) / __ldg(A.DZY + c - 1);
+                    TI = TI - AuxI * DT / Vk * (Pk - __ldg(P + am));
+                }
+                if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
+                    size_t ap = a + 1;
+                    double Ky = A.schmidtH * (__ldg(A.ViscH + ap) * __ldg(A.DVY + c) +
+                                              __ldg(A.ViscH + a) * __ldg(A.DVY + c + 1)) /
+                                (__ldg(A.DVY + c + 1) + __ldg(A.DVY + c));
+                    if (A.nullDif && __ldg(A.Qy + ap) == 0.) Ky = 0.;
+                    double AuxI = Ky * __ldg(A.AreaV + ap) / __ldg(A.DZY + c);
+                    TI = TI + AuxI * DT / Vk * (__ldg(P + ap) - Pk);
+                }
+            }
+            // HorizontalAdvectionXX (explicit)
+            const bool up2H = A.upwind2H != 0;
+            if (__ldg(A.CFU + a) == 1) {
+                double Fx = adv_flux(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H,
+                                     [&](int n) { return __ldg(A.DUX + c + (long long)(n - 2) * sj); });
+                TI = TI + Fx * DT / Vk;
+            }
+            if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
+                double Fx = adv_flux(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H,
+                                     [&](int n) { return __ldg(A.DUX + c + (long long)(n - 1) * sj); });
+                TI = TI - Fx * DT / Vk;
+            }
+            // HorizontalAdvectionYY (explicit)
+            if (!A.xzflow) {
+                if (__ldg(A.CFV + a) == 1) {
+                    double Fy = adv_flux(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H,
+                                         [&](int n) { return __ldg(A.DVY + c + (n - 2)); });
+                    TI = TI + Fy * DT / Vk;
+                }
+                if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
+                    double Fy = adv_flux(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H,
+                                         [&](int n) { return __ldg(A.DVY + c + (n - 1)); });
+                    TI = TI - Fy * DT / Vk;
+                }
+            }
+        }
+
+        if (doVert) {
+            // VerticalDiffusion: face k (below) then face k+1 (above)
+            const bool fk = __ldg(A.CFW + a) == 1 && !sd;
+            const bool fk1 = k + 1 <= nk && __ldg(A.CFW + a + sk) == 1 && !sd;
+            if (fk) {
+                double AuxK = Kz(a) * DUXc * DVYc / __ldg(A.DZZ + a - sk);
+                double Aux2 = AuxK * DT / Vk;
+                D = D - Aux2 * ie;
+                E = E + Aux2 * ie;
+                TI = TI - Aux2 * (Pk - __ldg(P + a - sk)) * (1. - ie);
+            }
+            if (fk1) {
+                double AuxK = Kz(a + sk) * DUXc * DVYc / __ldg(A.DZZ + a);
+                double Aux1 = AuxK * DT / Vk;
+                E = E + Aux1 * ie;
+                F = F - Aux1 * ie;
+                TI = TI + Aux1 * (Pkp1 - Pk) * (1. - ie);
+            }
+            if (doVAdv) {
+                if (A.explicitV) {
+                    if (__ldg(A.CFW + a) == 1) {
+                        double C[4];
+                        vcoef(k, C);
+                        double Fz = C[0] * __ldg(P + a - 2 * sk) + C[1] * __ldg(P + a - sk) +
+                                    C[2] * Pk + C[3] * Pkp1;
+                        TI = TI + Fz * DT / Vk;
+                    }
+                    if (k + 1 <= nk && __ldg(A.CFW + a + sk) == 1) {
+                        double C[4];
+                        vcoef(k + 1, C);
+                        double Fz = C[0] * __ldg(P + a - sk) + C[1] * Pk + C[2] * Pkp1 +
+                                    C[3] * __ldg(P + a + 2 * sk);
+                        TI = TI - Fz * DT / Vk;
+                    }
+                } else {
+                    bool gk, gk1;
+                    if (A.docycle == 1) {
+                        gk = colCFWTop && k >= kb + 1;
+                        gk1 = colCFWTop && k + 1 <= nk && k + 1 >= kb + 1;
+                    } else {
+                        gk = __ldg(A.CFW + a) == 1;
+                        gk1 = k + 1 <= nk && __ldg(A.CFW + a + sk) == 1;
+                    }
+                    if (gk) {
+                        double C[4];
+                        vcoef(k, C);
+                        double DT2 = DT / Vk;
+                        D = D - C[1] * DT2;
+                        E = E - C[2] * DT2;
+                    }
+                    if (gk1) {
+                        double C[4];
+                        vcoef(k + 1, C);
+                        double DT1 = DT / Vk;
+                        E = E + C[1] * DT1;
+                        F = F + C[2] * DT1;
+                    }
+                }
+            }
+        }
+
+        // OpenBoundaryCondition (boundary columns, open cells, k >= |KFloor|)
+        if (bp && k >= kbp && opk == 1) {
+            double DT_V = DT / Vk;
+            const double Rf = __ldg(A.Ref + a);
+            if (A.bc == 1) {
+                double WF = __ldg(A.Qx + a) * (double)__ldg(A.CFU + a) -
+                            __ldg(A.Qx + a + sj) * (double)__ldg(A.CFU + a + sj) +
+                            __ldg(A.Qy + a) * (double)__ldg(A.CFV + a) -
+                            __ldg(A.Qy + a + 1) * (double)__ldg(A.CFV + a + 1) +
+                            __ldg(A.Qz + a) * (double)__ldg(A.CFW + a) -
+                            __ldg(A.Qz + a + sk) * (double)__ldg(A.CFW + a + sk) -
+                            (Vk - __ldg(A.Vold + a)) / DT;
+                double Ext = Pk * (1.0 - A.tdecAux) + Rf * A.tdecAux;
+                if (WF < 0.0) TI = TI - WF * Ext * DT_V;
+                else E = E + WF * DT_V;
+            } else {                              // ImposedValue / SubModel
+                double A1 = (double)(__ldg(A.OP + a + 1) * (1 - __ldg(A.BP2D + c + 1)));
+                double A2 = (double)(__ldg(A.OP + a - 1) * (1 - __ldg(A.BP2D + c - 1)));
+                double A3 = (double)(__ldg(A.OP + a + sj) * (1 - __ldg(A.BP2D + c + sj)));
+                double A4 = (double)(__ldg(A.OP + a - sj) * (1 - __ldg(A.BP2D + c - sj)));
+                double P1 = __ldg(P + a + 1), P2 = __ldg(P + a - 1);
+                double P3 = __ldg(P + a + sj), P4 = __ldg(P + a - sj);
+                double At = A1 + A2 + A3 + A4;
+                double Ext;
+                if (At > 0) {
+                    double In = (P1 * A1 + P2 * A2 + P3 * A3 + P4 * A4) / At;
+                    Ext = In * (1.0 - A.tdecAux) + Rf * A.tdecAux;
+                } else {
+                    Ext = Rf;
+                }
+                TI = Ext; D = 0.0; E = 1.0; F = 0.0;
+            }
+        }
+
+        if (__ldg(A.LP + a) == 1) TI = MOHID_NULL_REAL_D;
+
+        // THOMASZ forward sweep (row 1 has no pivot test, FN:4087-4088)
+        double W, G;
+        if (k == 1) {
+            W = -F / E;
+            G = TI / E;
+        } else {
+            double aux = E + D * Wp;
+            if (fabs(aux) > 0) {
+                W = -F / aux;
+                G = (TI - D * Gp) / aux;
+            } else {
+                W = 0.; G = 0.; flags |= MOHID_DEV_ZERO_PIVOT;
+            }
+        }
+        sW[(size_t)k * kThreads + tid] = W;
+        Po[a] = G;
+        Wp = W; Gp = G;
+        Pk = Pkp1;
+    }
+
+    // row KUB+1: D = 0, E = 1, F = 0, TI = 0 (null_real if flagged land)
+    {
+        const size_t a = c + (size_t)sk * (nk + 1);
+        double TI = (__ldg(A.LP + a) == 1) ? MOHID_NULL_REAL_D : 0.;
+        double D = 0., E = 1., F = 0.;
+        double aux = E + D * Wp;
+        double G;
+        if (fabs(aux) > 0) { G = (TI - D * Gp) / aux; (void)F; }
+        else { G = 0.; flags |= MOHID_DEV_ZERO_PIVOT; }
+        Po[a] = G;
+        double R = G;                             // RES(KUB+1) = G(KUB+1)
+        for (int k = nk; k >= 1; --k) {
+            const size_t b = c + (size_t)sk * k;
+            R = sW[(size_t)k * kThreads + tid] * R + Po[b];
+            Po[b] = R;
+            if (!isfinite(R) && __ldg(A.LP + b) != 1) flags |= MOHID_DEV_NONFINITE;
+        }
+    }
+    if (flags) atomicOr(A.status, flags);
+}
+
+// Stand-alone THOMASZ_NewType2 (FN:4026-4123), columns with WaterPoints(KUB)==1.
+__global__ void thomasz_f64_kernel(int ni, int nj, int nk, const double* __restrict__ D,
+                                   const double* __restrict__ E, const double* __restrict__ F,
+                                   const double* __restrict__ TI, double* __restrict__ RES,
+                                   const int* __restrict__ WP, unsigned int* status)
+{
+    extern __shared__ double sW[];
+    const int tid = threadIdx.y * kBX + threadIdx.x;
+    const int i = 1 + blockIdx.x * kBX + threadIdx.x;
+    const int j = 1 + blockIdx.y * kBY + threadIdx.y;
+    if (i > ni || j > nj) return;
+    const size_t sj = (size_t)ni + 2, sk = sj * ((size_t)nj + 2);
+    const size_t c = (size_t)i + sj * (size_t)j;
+    if (__ldg(WP + c + sk * nk) != 1) return;
+    unsigned int flags = 0;
+    double Wp = -__ldg(F + c + sk) / __ldg(E + c + sk);
+    double Gp = __ldg(TI + c + sk) / __ldg(E + c + sk);
+    sW[kThreads + tid] = Wp;
+    RES[c + sk] = Gp;
+    for (int k = 2; k <= nk + 1; ++k) {
+        const size_t a = c + sk * k;
+        double d = __ldg(D + a);
+        double aux = __ldg(E + a) + d * Wp;
+        double W, G;
+        if (fabs(aux) > 0) { W = -__ldg(F + a) / aux; G = (__ldg(TI + a) - d * Gp) / aux; }
+        else { W = 0.; G = 0.; flags |= MOHID_DEV_ZERO_PIVOT; }
+        sW[(size_t)k * kThreads + tid] = W;
+        RES[a] = G;
+        Wp = W; Gp = G;
+    }
+    double R = Gp;
+    for (int k = nk; k >= 1; --k) {
+        const size_t b = c + sk * k;
+        R = sW[(size_t)k * kThreads + tid] * R + RES[b];
+        RES[b] = R;
+    }
+    if (flags) atomicOr(status, flags);
+}
+
+// Lower-edge faces (U at j = 1, V at i = 1, W at k = 1) must be closed.
+__global__ void check_faces_kernel(int ni, int nj, int nk, const int* __restrict__ CFU,
+                                   const int* __restrict__ CFV, const int* __restrict__ CFW,
+                                   unsigned int* status)
+{
+    const size_t sj = (size_t)ni + 2, sk = sj * ((size_t)nj + 2);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    if (t < (long long)ni * nk) {                         // U faces at j = 1
+        int i = 1 + (int)(t % ni), k = 1 + (int)(t / ni);
+        bad |= CFU[(size_t)i + sj + sk * k] == 1;
+    }
+    if (t < (long long)nj * nk) {                         // V faces at i = 1
+        int j = 1 + (int)(t % nj), k = 1 + (int)(t / nj);
+        bad |= CFV[1 + sj * j + sk * k] == 1;
+    }
+    if (t < (long long)ni * nj) {                         // W faces at k = 1
+        int i = 1 + (int)(t % ni), j = 1 + (int)(t / ni);
+        bad |= CFW[(size_t)i + sj * j + sk] == 1;
+    }
+    if (bad) atomicOr(status, MOHID_DEV_BAD_FACE);
+}
+
+}  // namespace
+
+cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s)
+{
+    dim3 blk(kBX, kBY);
+    dim3 grd((unsigned)((a.ni + 2 + kBX - 1) / kBX), (unsigned)((a.nj + 2 + kBY - 1) / kBY));
+    size_t smem = sizeof(double) * (size_t)(a.nk + 2) * kThreads;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(plain_f64_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    plain_f64_kernel<<<grd, blk, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_thomasz_f64(int ni, int nj, int nk, const double* D, const double* E,
+                               const double* F, const double* TI, double* RES, const int* WP,
+                               unsigned int* status, cudaStream_t s)
+{
+    dim3 blk(kBX, kBY);
+    dim3 grd((unsigned)((ni + kBX - 1) / kBX), (unsigned)((nj + kBY - 1) / kBY));
+    size_t smem = sizeof(double) * (size_t)(nk + 2) * kThreads;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(thomasz_f64_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    thomasz_f64_kernel<<<grd, blk, smem, s>>>(ni, nj, nk, D, E, F, TI, RES, WP, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_check_faces(int ni, int nj, int nk, const int* CFU, const int* CFV,
+                               const int* CFW, unsigned int* status, cudaStream_t s)
+{
+    long long n = (long long)ni * nk;
+    if ((long long)nj * nk > n) n = (long long)nj * nk;
+    if ((long long)ni * nj > n) n = (long long)ni * nj;
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    check_faces_kernel<<<blocks, 256, 0, s>>>(ni, nj, nk, CFU, CFV, CFW, status);
+    return cudaGetLastError();
+}
+
+}  // namespace mohid

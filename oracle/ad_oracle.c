@@ -1,0 +1,689 @@
+/*
+ * ad_oracle.c -- TEST INFRASTRUCTURE ONLY (checker and CPU baseline).
+ *
+ * FP64 restatement of one call of ModuleAdvectionDiffusion::AdvectionDiffusion
+ * (Software/MOHIDBase2/ModuleAdvectionDiffusion.F90, "AD" below) on the
+ * non-Optimize path, with its numerics from ModuleFunctions
+ * (Software/MOHIDBase1/ModuleFunctions.F90, "FN").  Every pass is a full-array
+ * sweep in the reference's order (k outer, j, i inner) with the reference's
+ * OpenMP work split, so that each floating-point accumulation happens in the
+ * same order as in the Fortran.  Compile with -ffp-contract=off: the Fortran
+ * evaluates a*b+c as two rounded operations.
+ *
+ * Deviations (documented, not reachable with consistent MOHID masks):
+ *  - THOMASZ with a zero pivot: the reference keeps W/G from whatever column
+ *    its OpenMP thread solved before (FN:4090-4099); here W = G = 0 for that
+ *    row and MOHID_AD_ERR_ZERO_PIVOT is returned.
+ *  - faces on the WorkSize lower edge (j = JLB for U, i = ILB for V, k = KLB
+ *    for W) must not be compute faces: the reference would read outside the
+ *    Size box there.  Such input returns MOHID_AD_ERR_BOUNDS.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "oracle.h"
+
+#define MINVALUE 1.e-16            /* MinValue, ModuleGlobalData.F90:1812 */
+#define NULL_REAL (-9.9e15)        /* null_real, ModuleGlobalData.F90:143 */
+
+typedef struct {
+    int NI, NJ, NK;                /* Size extents */
+    size_t n3, n2;
+} ora_ext;
+
+#define I3(i, j, k) ((size_t)(i) + (size_t)X.NI * ((size_t)(j) + (size_t)X.NJ * (size_t)(k)))
+#define I2(i, j) ((size_t)(i) + (size_t)X.NI * (size_t)(j))
+
+static inline double dmin2(double a, double b) { return (b < a) ? b : a; }
+static inline double dmax2(double a, double b) { return (b > a) ? b : a; }
+
+/* FaceConcUpFirstOrder, FN:11127-11140 */
+static void face_up1(double c[4], double Q)
+{
+    c[0] = c[1] = c[2] = c[3] = 0.;
+    if (Q > 0.) c[1] = 1.; else c[2] = 1.;
+}
+
+/* FaceConcUpSecondOrder, FN:11055-11084 */
+static void face_up2(double c[4], double Q)
+{
+    c[0] = c[1] = c[2] = c[3] = 0.;
+    if (Q > 0) { c[0] = -1. / 8.; c[1] = 6. / 8.; c[2] = 3. / 8.; }
+    else if (Q < 0) { c[3] = -1. / 8.; c[2] = 6. / 8.; c[1] = 3. / 8.; }
+    else face_up1(c, Q);
+}
+
+/* FaceConcUpThirdOrder, FN:11086-11125 */
+static void face_up3(double c[4], double Q, double Cr)
+{
+    double cc = (1 - 2. * fabs(Cr)) / 6.;
+    double a = 0.5 + cc, b = 0.5 - cc, d = (1 - fabs(Cr)) / 2.;
+    if (Q > 0) { c[0] = -d * b; c[1] = 1 + d * (b - a); c[2] = d * a; c[3] = 0.; }
+    else if (Q < 0) { c[3] = -d * b; c[2] = 1 + d * (b - a); c[1] = d * a; c[0] = 0.; }
+    else face_up1(c, Q);
+}
+
+/* ComputeAdvectionFace, FN:10702-10894 (Courant, FN:11045-11052). */
+int ora_advection_face(const double P[4], const double V[4], const double du[4], double dt,
+                       double Q, double VolumeRelMax, int method, int limiter,
+                       int nearBoundary, int upwind2, double CFace[4])
+{
+    double Cup1[4], CupH[4];
+    double Cr = 0., Theta = 0., VolumeRel = 0.;
+    face_up1(Cup1, Q);
+    if (!nearBoundary) {
+        double Aux;
+        if (Q > 0) {
+            Cr = Q * dt / V[1];
+            Aux = dmin2(dmin2(V[0], V[1]), V[2]);
+            VolumeRel = dmax2(dmax2(V[0], V[1]), V[2]) / Aux;
+        } else {
+            Cr = Q * dt / V[2];
+            Aux = dmin2(dmin2(V[1], V[2]), V[3]);
+            VolumeRel = dmax2(dmax2(V[1], V[2]), V[3]) / Aux;
+        }
+    }
+    if (method == MOHID_UPWIND_ORDER1 || (nearBoundary && upwind2)) {
+        memcpy(CupH, Cup1, sizeof CupH);
+        Theta = 0.;
+    } else if (method == MOHID_UPWIND_ORDER2 && !nearBoundary) {
+        face_up2(CupH, Q);
+        Theta = (VolumeRel > VolumeRelMax) ? 0. : 1.;
+    } else if (method == MOHID_UPWIND_ORDER3 && !nearBoundary) {
+        face_up3(CupH, Q, Cr);
+        Theta = (VolumeRel > VolumeRelMax) ? 0. : 1.;
+    } else if (method == MOHID_CENTRAL_DIF || method == MOHID_LEAP_FROG) {
+        double AuxLeft = du[2] / (du[1] + du[2]);
+        double AuxRight = du[1] / (du[1] + du[2]);
+        CupH[0] = 0.; CupH[1] = AuxLeft; CupH[2] = AuxRight; CupH[3] = 0.;
+        Theta = 1.;
+    } else if (method == MOHID_P2_TVD && !nearBoundary) {
+        double dC, r;
+        CupH[0] = CupH[1] = CupH[2] = CupH[3] = 0.;
+        if (Q > 0.) {
+            CupH[2] = 1.;
+            dC = (P[2] - P[1]) / (du[2] + du[1]);
+            if (fabs(dC) < MINVALUE) dC = (dC >= 0) ? MINVALUE : -MINVALUE;
+            r = (P[1] - P[0]) / (du[1] + du[0]) / dC;
+        } else {
+            CupH[1] = 1.;
+            dC = (P[1] - P[2]) / (du[2] + du[1]);
+            if (fabs(dC) < MINVALUE) dC = (dC >= 0) ? MINVALUE : -MINVALUE;
+            r = (P[2] - P[3]) / (du[2] + du[3]) / dC;
+        }
+        if (limiter == MOHID_TVD_MINMOD) {
+            Theta = dmax2(0., dmin2(1., r));
+        } else if (limiter == MOHID_TVD_VANLEER) {
+            Theta = (r < 0) ? 0. : 2. * r / (1 + r);
+        } else if (limiter == MOHID_TVD_MUSCL) {
+            Theta = dmax2(0., dmin2(dmin2(2., 2. * r), (1 + r) / 2.));
+        } else if (limiter == MOHID_TVD_SUPERBEE) {
+            Theta = dmax2(dmax2(0., dmin2(1., 2. * r)), dmin2(r, 2.));
+        } else if (limiter == MOHID_TVD_PDM) {
+            double a = 0.5 + (1 - 2. * fabs(Cr)) / 6.;
+            double b = 0.5 - (1 - 2. * fabs(Cr)) / 6.;
+            double Aux = a + b * r;
+            if (fabs(Cr) < MINVALUE) Cr = MINVALUE;
+            Theta = dmax2(0., dmin2(dmin2(Aux, 2. / (1. - Cr)), 2. * r / Cr));
+        } else {
+            return MOHID_AD_ERR_OPTION;
+        }
+        Theta = 0.5 * Theta * (1. - Cr);
+    } else {
+        return MOHID_AD_ERR_OPTION;
+    }
+    for (int n = 0; n < 4; ++n) CFace[n] = (1. - Theta) * Cup1[n] + Theta * CupH[n];
+    return 0;
+}
+
+/* ComputeAdvection1D_V2, FN:10534-10591, for one line.  The Fortran dummy
+ * arrays are assumed-shape (lower bound 1), so dummy face index ilb..iub of a
+ * line passed over the Size box 0..N+1 lands on actual faces ilb-1..iub-1;
+ * the caller passes actual face bounds [flo, fhi].  `at(n)` addresses element
+ * n (actual index, 0..N+1) of the line with stride `s` from base `o`. */
+static int advection_line(int flo, int fhi, double dt, const double* du, size_t sdu,
+                          const double* P, const double* Q, const double* V,
+                          const int* CP, size_t o, size_t s,
+                          double* Cf, double* Df, double* Ef, double* Ff,
+                          int method, int limiter, double VolumeRelMax, int upwind2)
+{
+    for (int f = flo; f <= fhi; ++f) {
+        size_t a = o + (size_t)f * s;
+        if (CP[a - s] == 1 && CP[a] == 1) {
+            double QF = Q[a];
+            int nb = 0;
+            if (QF > 0) { if (CP[a - 2 * s] != 1) nb = 1; }
+            else { if (CP[a + s] != 1) nb = 1; }
+            double P4[4], V4[4], du4[4], CF[4];
+            for (int n = 0; n < 4; ++n) {
+                size_t an = a + ((size_t)n - 2) * s;     /* f-2 .. f+1 */
+                P4[n] = P[an];
+                V4[n] = V[an];
+                du4[n] = du[(size_t)(f + n - 2) * sdu];
+            }
+            int e = ora_advection_face(P4, V4, du4, dt, QF, VolumeRelMax, method, limiter,
+                                       nb, upwind2, CF);
+            if (e) return e;
+            Cf[a] = QF * CF[0];
+            Df[a] = QF * CF[1];
+            Ef[a] = QF * CF[2];
+            Ff[a] = QF * CF[3];
+        }
+    }
+    return 0;
+}
+
+static int validate(const ora_domain* d, const double* PROP, const mohid_ad_params* p,
+                    const double* ReferenceProp)
+{
+    if (!d || !PROP || !p) return MOHID_AD_ERR_NULLPTR;
+    if (d->ni < 1 || d->nj < 1 || d->nk < 1) return MOHID_AD_ERR_BOUNDS;
+    /* AD:1231-1239, AD:1340-1349 */
+    if ((p->ImpExp_AdvXX == 1. || p->ImpExp_AdvYY == 1.) &&
+        (p->AdvMethodH == MOHID_UPWIND_ORDER2 || p->AdvMethodH == MOHID_UPWIND_ORDER3))
+        return MOHID_AD_ERR_OPTION;
+    if (p->ImpExp_AdvV == 1. &&
+        (p->AdvMethodV == MOHID_UPWIND_ORDER2 || p->AdvMethodV == MOHID_UPWIND_ORDER3))
+        return MOHID_AD_ERR_OPTION;
+    if (p->ImpExp_DifH != 0.) return MOHID_AD_ERR_OPTION;
+    if (p->ImpExp_AdvXX == 1. && p->ImpExp_AdvYY == 1.) return MOHID_AD_ERR_OPTION;
+    if (p->ImpExp_AdvV != 0. && p->ImpExp_AdvV != 1.) return MOHID_AD_ERR_OPTION;
+    if (p->ImpExp_AdvXX != 0. || p->ImpExp_AdvYY != 0.) return MOHID_AD_ERR_UNSUPPORTED;
+    if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux)
+        return MOHID_AD_ERR_UNSUPPORTED;
+    if (p->Docycle_method != 1 && p->Docycle_method != 2) return MOHID_AD_ERR_OPTION;
+    /* methods 2..4 reach `stop` at the first near-boundary face unless Upwind2 */
+    int mH = p->AdvMethodH, mV = p->AdvMethodV;
+    if (mH < 1 || mH > 6 || mV < 1 || mV > 6) return MOHID_AD_ERR_OPTION;
+    if ((mH >= 2 && mH <= 4) && !p->Upwind2H) return MOHID_AD_ERR_OPTION;
+    if ((mV >= 2 && mV <= 4) && !p->Upwind2V) return MOHID_AD_ERR_OPTION;
+    if (mH == MOHID_P2_TVD && (p->TVDLimitationH < 1 || p->TVDLimitationH > 5)) return MOHID_AD_ERR_OPTION;
+    if (mV == MOHID_P2_TVD && (p->TVDLimitationV < 1 || p->TVDLimitationV > 5)) return MOHID_AD_ERR_OPTION;
+    if (ReferenceProp) {
+        int bc = p->BoundaryCondition;
+        if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8)
+            return MOHID_AD_ERR_OPTION;              /* Set_Internal_State ERR01, AD:5816-5830 */
+        if (bc != MOHID_BC_MASS_CONSERVATION && bc != MOHID_BC_IMPOSED_VALUE && bc != MOHID_BC_SUBMODEL)
+            return MOHID_AD_ERR_UNSUPPORTED;
+    }
+    /* lower-edge faces must be closed (see header) */
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    for (int k = 1; k <= d->nk; ++k) {
+        for (int i = 1; i <= d->ni; ++i)
+            if (d->ComputeFacesU3D[I3(i, 1, k)] == 1) return MOHID_AD_ERR_BOUNDS;
+        for (int j = 1; j <= d->nj; ++j)
+            if (d->ComputeFacesV3D[I3(1, j, k)] == 1) return MOHID_AD_ERR_BOUNDS;
+    }
+    for (int j = 1; j <= d->nj; ++j)
+        for (int i = 1; i <= d->ni; ++i)
+            if (d->ComputeFacesW3D[I3(i, j, 1)] == 1) return MOHID_AD_ERR_BOUNDS;
+    return 0;
+}
+
+struct ora_work {
+    int ni, nj, nk;
+    double* pool;
+    double *Kx, *Ky, *Kz;
+    double *D, *E, *F, *TI;
+    double *XC, *XD, *XE, *XF, *YC, *YD, *YE, *YF, *VC, *VD, *VE, *VF;
+    double *WFOB;
+};
+
+/* AllocateVariables, AD:537-684: work arrays live for the instance's life and
+ * start at null_real (AD:640-675). */
+ora_work* ora_work_new(int ni, int nj, int nk)
+{
+    size_t n3 = (size_t)(ni + 2) * (size_t)(nj + 2) * (size_t)(nk + 2);
+    ora_work* w = (ora_work*)calloc(1, sizeof(ora_work));
+    if (!w) return NULL;
+    w->pool = (double*)malloc(sizeof(double) * n3 * 20);
+    if (!w->pool) { free(w); return NULL; }
+    w->ni = ni; w->nj = nj; w->nk = nk;
+    double** slots[20] = {&w->Kx, &w->Ky, &w->Kz, &w->D, &w->E, &w->F, &w->TI, &w->XC, &w->XD,
+                          &w->XE, &w->XF, &w->YC, &w->YD, &w->YE, &w->YF, &w->VC, &w->VD,
+                          &w->VE, &w->VF, &w->WFOB};
+    for (int s = 0; s < 20; ++s) *slots[s] = w->pool + (size_t)s * n3;
+    #pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < n3 * 20; ++q) w->pool[q] = NULL_REAL;
+    return w;
+}
+
+void ora_work_free(ora_work* w)
+{
+    if (w) { free(w->pool); free(w); }
+}
+
+/* SetMatrixValue over the Size box (FN:1599-1645: OpenMP over k, static). */
+static void fill3(ora_ext X, double* a, double v)
+{
+    #pragma omp parallel for schedule(static)
+    for (int k = 0; k < X.NK; ++k) {
+        double* s = a + (size_t)k * X.n2;
+        for (size_t q = 0; q < X.n2; ++q) s[q] = v;
+    }
+}
+
+int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
+                 const mohid_ad_params* p, ora_work* work, int nthreads)
+{
+    int st = validate(d, PROP, p, ReferenceProp);
+    if (st) return st;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    const int ni = d->ni, nj = d->nj, nk = d->nk;
+    ora_ext X = {ni + 2, nj + 2, nk + 2, 0, 0};
+    X.n3 = (size_t)X.NI * X.NJ * X.NK;
+    X.n2 = (size_t)X.NI * X.NJ;
+    const double DT = p->DTProp;
+    const int *CFU = d->ComputeFacesU3D, *CFV = d->ComputeFacesV3D, *CFW = d->ComputeFacesW3D;
+    const int *OP = d->OpenPoints3D;
+    const double *V = d->VolumeZ, *P = PROP;
+
+    ora_work* own = NULL;
+    if (!work) { own = work = ora_work_new(ni, nj, nk); if (!work) return MOHID_AD_ERR_ALLOC; }
+    if (work->ni != ni || work->nj != nj || work->nk != nk) return MOHID_AD_ERR_BOUNDS;
+    ora_work w = *work;
+    int err = 0;
+
+    /* Convert_Dif_Vertical, AD:2364-2443: do k = KLB+1,KUB / OMP DO j / do i */
+    #pragma omp parallel
+    for (int k = 2; k <= nk; ++k) {
+        #pragma omp for schedule(dynamic, 1)
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                size_t a = I3(i, j, k);
+                if (CFW[a] == 1) w.Kz[a] = p->SchmidtCoef_V * d->Diff_V[a] + p->SchmidtBackground_V;
+            }
+    }
+    if (p->NullDif) {
+        #pragma omp parallel
+        for (int k = 2; k <= nk; ++k) {
+            #pragma omp for schedule(dynamic, 1)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k);
+                    if (CFW[a] == 1 && d->Wflux_Z[a] == 0.) w.Kz[a] = 0.;
+                }
+        }
+    }
+    /* Convert_Visc_Dif_Horizontal, AD:2453-2595 */
+    #pragma omp parallel
+    {
+        for (int k = 1; k <= nk; ++k) {
+            #pragma omp for schedule(dynamic, 1) nowait
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k);
+                    if (CFU[a] == 1)
+                        w.Kx[a] = p->schmidt_H * (d->Visc_H[a] * d->DUX[I2(i, j - 1)] +
+                                                  d->Visc_H[I3(i, j - 1, k)] * d->DUX[I2(i, j)]) /
+                                  (d->DUX[I2(i, j)] + d->DUX[I2(i, j - 1)]);
+                }
+        }
+        for (int k = 1; k <= nk; ++k) {
+            #pragma omp for schedule(dynamic, 1)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k);
+                    if (CFV[a] == 1)
+                        w.Ky[a] = p->schmidt_H * (d->Visc_H[a] * d->DVY[I2(i - 1, j)] +
+                                                  d->Visc_H[I3(i - 1, j, k)] * d->DVY[I2(i, j)]) /
+                                  (d->DVY[I2(i, j)] + d->DVY[I2(i - 1, j)]);
+                }
+        }
+        if (p->NullDif) {
+            for (int k = 1; k <= nk; ++k) {
+                #pragma omp for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k);
+                        if (CFU[a] == 1 && d->Wflux_X[a] == 0.) w.Kx[a] = 0.;
+                        if (CFV[a] == 1 && d->Wflux_Y[a] == 0.) w.Ky[a] = 0.;
+                    }
+            }
+        }
+    }
+
+    /* AdvectionDiffusion cd8 (AD:1439-1456) and AdvectionDiffusionIteration
+     * init (AD:1660-1697): D=0, E=1, F=0, TI=0 and the flux-coefficient
+     * arrays zero over the Size box. */
+    fill3(X, w.D, 0.); fill3(X, w.E, 1.); fill3(X, w.F, 0.); fill3(X, w.TI, 0.);
+    {
+        double* c12[12] = {w.XC, w.XD, w.XE, w.XF, w.YC, w.YD, w.YE, w.YF, w.VC, w.VD, w.VE, w.VF};
+        for (int s = 0; s < 12; ++s) fill3(X, c12[s], 0.);
+    }
+
+    /* VolumeVariation, AD:3966-4021: do k / OMP DO j / do i */
+    #pragma omp parallel
+    for (int k = 1; k <= nk; ++k) {
+        #pragma omp for schedule(dynamic, 1)
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                size_t a = I3(i, j, k);
+                if (OP[a] == 1) {
+                    w.TI[a] = P[a] * (d->VolumeZOld[a] / V[a]);
+                    if (k == nk) {
+                        double DT_V = DT / V[a];
+                        w.E[a] = 1.0 + DT_V * d->Wflux_Z[I3(i, j, k + 1)];
+                    }
+                } else {
+                    w.TI[a] = P[a];
+                }
+            }
+    }
+
+    if (!p->Vertical1D) {
+        /* HorizontalDiffusionXX, AD:5156-5214: OMP DO k / do j / do i */
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 1; k <= nk; ++k)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k), am = I3(i, j - 1, k);
+                    if (CFU[a] == 1) {
+                        double AuxJ = w.Kx[a] * d->AreaU[a] / d->DZX[I2(i, j - 1)];
+                        w.TI[am] = w.TI[am] + AuxJ * DT / V[am] * (P[a] - P[am]);
+                        w.TI[a] = w.TI[a] - AuxJ * DT / V[a] * (P[a] - P[am]);
+                    }
+                }
+        /* HorizontalDiffusionYY, AD:5313-5365: do k / OMP DO j / do i */
+        if (!p->XZFlow) {
+            #pragma omp parallel
+            for (int k = 1; k <= nk; ++k) {
+                #pragma omp for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k), am = I3(i - 1, j, k);
+                        if (CFV[a] == 1) {
+                            double AuxI = w.Ky[a] * d->AreaV[a] / d->DZY[I2(i - 1, j)];
+                            w.TI[am] = w.TI[am] + AuxI * DT / V[am] * (P[a] - P[am]);
+                            w.TI[a] = w.TI[a] - AuxI * DT / V[a] * (P[a] - P[am]);
+                        }
+                    }
+            }
+        }
+
+        /* HorizontalAdvectionXX, AD:4368-4540: coefficients per line (i,:,k)
+         * (do k / OMP DO i), faces j = JLB..JUB after the dummy-index shift;
+         * explicit update OMP DO k / do j / do i. */
+        #pragma omp parallel reduction(|:err)
+        for (int k = 1; k <= nk; ++k) {
+            #pragma omp for schedule(dynamic, 1)
+            for (int i = 1; i <= ni; ++i)
+                err |= advection_line(1, nj, DT, d->DUX + I2(i, 0), (size_t)X.NI, P, d->Wflux_X, V,
+                                      OP, I3(i, 0, k), (size_t)X.NI, w.XC, w.XD, w.XE, w.XF,
+                                      p->AdvMethodH, p->TVDLimitationH, p->VolumeRelMax,
+                                      p->Upwind2H);
+        }
+        if (err) goto fail;
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 1; k <= nk; ++k)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k);
+                    if (CFU[a] == 1) {
+                        size_t am = I3(i, j - 1, k);
+                        double Fx = w.XC[a] * P[I3(i, j - 2, k)] + w.XD[a] * P[am] +
+                                    w.XE[a] * P[a] + w.XF[a] * P[I3(i, j + 1, k)];
+                        w.TI[a] = w.TI[a] + Fx * DT / V[a];
+                        w.TI[am] = w.TI[am] - Fx * DT / V[am];
+                    }
+                }
+        /* HorizontalAdvectionYY, AD:4739-4910: do k / OMP DO j for both parts */
+        if (!p->XZFlow) {
+            #pragma omp parallel reduction(|:err)
+            for (int k = 1; k <= nk; ++k) {
+                #pragma omp for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    err |= advection_line(1, ni, DT, d->DVY + I2(0, j), 1, P, d->Wflux_Y, V, OP,
+                                          I3(0, j, k), 1, w.YC, w.YD, w.YE, w.YF,
+                                          p->AdvMethodH, p->TVDLimitationH, p->VolumeRelMax,
+                                          p->Upwind2H);
+            }
+            if (err) goto fail;
+            #pragma omp parallel
+            for (int k = 1; k <= nk; ++k) {
+                #pragma omp for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k);
+                        if (CFV[a] == 1) {
+                            size_t am = I3(i - 1, j, k);
+                            double Fy = w.YC[a] * P[I3(i - 2, j, k)] + w.YD[a] * P[am] +
+                                        w.YE[a] * P[a] + w.YF[a] * P[I3(i + 1, j, k)];
+                            w.TI[a] = w.TI[a] + Fy * DT / V[a];
+                            w.TI[am] = w.TI[am] - Fy * DT / V[am];
+                        }
+                    }
+            }
+        }
+    }
+
+    if (nk > 1) {
+        /* VerticalDiffusion, AD:2708-2784: do k / OMP DO j / do i */
+        const double ie = p->ImpExp_DifV;
+        #pragma omp parallel
+        for (int k = 1; k <= nk; ++k) {
+            #pragma omp for schedule(dynamic, 1)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i) {
+                    size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                    int sd = d->SmallDepths ? d->SmallDepths[I2(i, j)] : 0;
+                    if (CFW[a] == 1 && !sd) {
+                        double AuxK = w.Kz[a] * d->DUX[I2(i, j)] * d->DVY[I2(i, j)] / d->DZZ[am];
+                        double Aux1 = AuxK * DT / V[am];
+                        double Aux2 = AuxK * DT / V[a];
+                        w.E[am] = w.E[am] + Aux1 * ie;
+                        w.F[am] = w.F[am] - Aux1 * ie;
+                        w.TI[am] = w.TI[am] + Aux1 * (P[a] - P[am]) * (1. - ie);
+                        w.D[a] = w.D[a] - Aux2 * ie;
+                        w.E[a] = w.E[a] + Aux2 * ie;
+                        w.TI[a] = w.TI[a] - Aux2 * (P[a] - P[am]) * (1. - ie);
+                    }
+                }
+        }
+
+        if (!p->Vertical1D) {
+            /* VerticalAdvection, AD:2941-3140: coefficients per column with
+             * OpenPoints3D(i,j,KUB) == 1 (OMP DO j / do i), faces k = KLB..KUB
+             * after the dummy-index shift. */
+            #pragma omp parallel for schedule(dynamic, 1) reduction(|:err)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i)
+                    if (OP[I3(i, j, nk)] == 1)
+                        err |= advection_line(1, nk, DT, d->DWZ + I3(i, j, 0), X.n2, P,
+                                              d->Wflux_Z, V, OP, I3(i, j, 0), X.n2,
+                                              w.VC, w.VD, w.VE, w.VF, p->AdvMethodV,
+                                              p->TVDLimitationV, p->VolumeRelMax, p->Upwind2V);
+            if (err) goto fail;
+
+            if (p->ImpExp_AdvV == 0.) {
+                /* explicit, AD:3036-3063: do k / OMP DO j / do i */
+                #pragma omp parallel
+                for (int k = 1; k <= nk; ++k) {
+                    #pragma omp for schedule(dynamic, 1)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                            if (CFW[a] == 1) {
+                                double Fz = w.VC[a] * P[I3(i, j, k - 2)] + w.VD[a] * P[am] +
+                                            w.VE[a] * P[a] + w.VF[a] * P[I3(i, j, k + 1)];
+                                w.TI[am] = w.TI[am] - Fz * DT / V[am];
+                                w.TI[a] = w.TI[a] + Fz * DT / V[a];
+                            }
+                        }
+                }
+            } else if (p->Docycle_method == 1) {
+                /* implicit, column cycle, AD:3070-3093: OMP DO j / do i / do k */
+                #pragma omp parallel for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i)
+                        if (CFW[I3(i, j, nk)] == 1) {
+                            int kb = d->KFloorZ[I2(i, j)];
+                            double Vb = V[I3(i, j, kb)];
+                            for (int k = kb + 1; k <= nk; ++k) {
+                                size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                                double DT1 = DT / Vb;
+                                double DT2 = DT / V[a];
+                                Vb = V[a];
+                                w.D[a] = w.D[a] - w.VD[a] * DT2;
+                                w.E[a] = w.E[a] - w.VE[a] * DT2;
+                                w.E[am] = w.E[am] + w.VD[a] * DT1;
+                                w.F[am] = w.F[am] + w.VE[a] * DT1;
+                            }
+                        }
+            } else {
+                /* implicit, layer cycle, AD:3094-3117: do k / OMP DO j / do i */
+                #pragma omp parallel
+                for (int k = 1; k <= nk; ++k) {
+                    #pragma omp for schedule(dynamic, 1)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                            if (CFW[a] == 1) {
+                                double DT1 = DT / V[am];
+                                double DT2 = DT / V[a];
+                                w.D[a] = w.D[a] - w.VD[a] * DT2;
+                                w.E[a] = w.E[a] - w.VE[a] * DT2;
+                                w.E[am] = w.E[am] + w.VD[a] * DT1;
+                                w.F[am] = w.F[am] + w.VE[a] * DT1;
+                            }
+                        }
+                }
+            }
+        }
+    }
+
+    if (ReferenceProp) {
+        /* OpenBoundaryCondition, AD:5369-5672 (serial); FluxAtOpenBoundary,
+         * AD:5680-5742 (OMP DO j / do i / do k). */
+        const int bc = p->BoundaryCondition;
+        const double TdecAux = 1.0 / (1.0 + p->DecayTime / DT);
+        if (bc == MOHID_BC_MASS_CONSERVATION) {
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (int j = 1; j <= nj; ++j)
+                for (int i = 1; i <= ni; ++i)
+                    if (d->BoundaryPoints2D[I2(i, j)] == 1) {
+                        int kl = abs(d->KFloorZ[I2(i, j)]);
+                        for (int k = kl; k <= nk; ++k) {
+                            size_t a = I3(i, j, k);
+                            w.WFOB[a] = d->Wflux_X[a] * CFU[a] -
+                                        d->Wflux_X[I3(i, j + 1, k)] * CFU[I3(i, j + 1, k)] +
+                                        d->Wflux_Y[a] * CFV[a] -
+                                        d->Wflux_Y[I3(i + 1, j, k)] * CFV[I3(i + 1, j, k)] +
+                                        d->Wflux_Z[a] * CFW[a] -
+                                        d->Wflux_Z[I3(i, j, k + 1)] * CFW[I3(i, j, k + 1)] -
+                                        (V[a] - d->VolumeZOld[a]) / DT;
+                        }
+                    }
+        }
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                if (d->BoundaryPoints2D[I2(i, j)] != 1) continue;
+                int kl = abs(d->KFloorZ[I2(i, j)]);
+                for (int k = kl; k <= nk; ++k) {
+                    size_t a = I3(i, j, k);
+                    if (OP[a] != 1) continue;
+                    double DT_V = DT / V[a];
+                    double Ext;
+                    if (bc == MOHID_BC_IMPOSED_VALUE || bc == MOHID_BC_SUBMODEL) {
+                        double A1 = OP[I3(i + 1, j, k)] * (1 - d->BoundaryPoints2D[I2(i + 1, j)]);
+                        double A2 = OP[I3(i - 1, j, k)] * (1 - d->BoundaryPoints2D[I2(i - 1, j)]);
+                        double A3 = OP[I3(i, j + 1, k)] * (1 - d->BoundaryPoints2D[I2(i, j + 1)]);
+                        double A4 = OP[I3(i, j - 1, k)] * (1 - d->BoundaryPoints2D[I2(i, j - 1)]);
+                        double P1 = P[I3(i + 1, j, k)], P2 = P[I3(i - 1, j, k)];
+                        double P3 = P[I3(i, j + 1, k)], P4 = P[I3(i, j - 1, k)];
+                        double At = A1 + A2 + A3 + A4;
+                        if (At > 0) {
+                            double Int = (P1 * A1 + P2 * A2 + P3 * A3 + P4 * A4) / At;
+                            Ext = Int * (1.0 - TdecAux) + ReferenceProp[a] * TdecAux;
+                        } else {
+                            Ext = ReferenceProp[a];
+                        }
+                        w.TI[a] = Ext;
+                        w.D[a] = 0.0; w.E[a] = 1.0; w.F[a] = 0.0;
+                    } else { /* MassConservation */
+                        double Int = P[a];
+                        Ext = Int * (1.0 - TdecAux) + ReferenceProp[a] * TdecAux;
+                        if (w.WFOB[a] < 0.0) w.TI[a] = w.TI[a] - w.WFOB[a] * Ext * DT_V;
+                        else w.E[a] = w.E[a] + w.WFOB[a] * DT_V;
+                    }
+                }
+            }
+    }
+
+    /* SetMatrixValue(TICOEF3, Size, Null_Real, LandPoints3D), AD:1753 */
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < X.NK; ++k)
+        for (size_t q = (size_t)k * X.n2; q < (size_t)(k + 1) * X.n2; ++q)
+            if (d->LandPoints3D[q] == 1) w.TI[q] = NULL_REAL;
+
+    st = ora_thomasz(ni, nj, nk, w.D, w.E, w.F, w.TI, PROP, d->WaterPoints3D);
+    ora_work_free(own);
+    return st;
+fail:
+    ora_work_free(own);
+    return MOHID_AD_ERR_OPTION;
+}
+
+/* THOMASZ_NewType2, FN:4026-4123, called with the WorkSize bounds (KLB = 1). */
+int ora_thomasz(int ni, int nj, int nk, const double* D, const double* E, const double* F,
+                const double* TI, double* RES, const int* WaterPoints)
+{
+    ora_ext X = {ni + 2, nj + 2, nk + 2, 0, 0};
+    int zero = 0;
+    #pragma omp parallel reduction(|:zero)
+    {
+        double* W = (double*)malloc(sizeof(double) * (size_t)(nk + 2));
+        double* G = (double*)malloc(sizeof(double) * (size_t)(nk + 2));
+        #pragma omp for schedule(dynamic, 4)
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                if (WaterPoints[I3(i, j, nk)] != 1) continue;
+                size_t a1 = I3(i, j, 1);
+                W[1] = -F[a1] / E[a1];
+                G[1] = TI[a1] / E[a1];
+                for (int k = 2; k <= nk + 1; ++k) {
+                    size_t a = I3(i, j, k);
+                    double aux = E[a] + D[a] * W[k - 1];
+                    if (fabs(aux) > 0) {
+                        W[k] = -F[a] / aux;
+                        G[k] = (TI[a] - D[a] * G[k - 1]) / aux;
+                    } else {
+                        W[k] = 0.; G[k] = 0.; zero = 1;
+                    }
+                }
+                RES[I3(i, j, nk + 1)] = G[nk + 1];
+                for (int k = nk; k >= 1; --k)
+                    RES[I3(i, j, k)] = W[k] * RES[I3(i, j, k + 1)] + G[k];
+            }
+        free(W); free(G);
+    }
+    return zero ? MOHID_AD_ERR_ZERO_PIVOT : 0;
+}
+
+/* Neumaier-compensated sum of V*P over water cells (budget diagnostic). */
+static double mass_impl(const ora_domain* d, const double* P64, const float* P32)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    double s = 0., c = 0.;
+    for (int k = 1; k <= d->nk; ++k)
+        for (int j = 1; j <= d->nj; ++j)
+            for (int i = 1; i <= d->ni; ++i) {
+                size_t a = I3(i, j, k);
+                if (d->WaterPoints3D[a] != 1) continue;
+                double x = d->VolumeZ[a] * (P64 ? P64[a] : (double)P32[a]);
+                double t = s + x;
+                if (fabs(s) >= fabs(x)) c += (s - t) + x; else c += (x - t) + s;
+                s = t;
+            }
+    return s + c;
+}
+
+double ora_mass(const ora_domain* d, const double* PROP) { return mass_impl(d, PROP, NULL); }
+double ora_mass_f32(const ora_domain* d, const float* PROP) { return mass_impl(d, NULL, PROP); }

@@ -1,0 +1,359 @@
+"""TEST INFRASTRUCTURE ONLY: pure-Python restatement of one AdvectionDiffusion call.
+
+A second, independent reading of the Fortran, written as plain loops over
+Python floats (IEEE double, no fused multiply-add), for grids of a few hundred
+cells.  tests/ require it to agree bit for bit with the C oracle
+(oracle/ad_oracle.c).  It follows, in call order:
+
+  Convert_Dif_Vertical        Software/MOHIDBase2/ModuleAdvectionDiffusion.F90:2364-2443
+  Convert_Visc_Dif_Horizontal ModuleAdvectionDiffusion.F90:2453-2595
+  AdvectionDiffusionIteration ModuleAdvectionDiffusion.F90:1624-1922
+    VolumeVariation           :3966-4021
+    HorizontalDiffusionXX/YY  :5156-5214, :5313-5365
+    HorizontalAdvectionXX/YY  :4368-4540, :4739-4910
+      ComputeAdvection1D_V2   Software/MOHIDBase1/ModuleFunctions.F90:10534-10591
+      ComputeAdvectionFace    ModuleFunctions.F90:10702-10894
+    VerticalDiffusion         ModuleAdvectionDiffusion.F90:2708-2784
+    VerticalAdvection         :2941-3140
+    OpenBoundaryCondition     :5369-5742
+    SetMatrixValue(TI, null)  :1753
+    THOMASZ_NewType2          ModuleFunctions.F90:4026-4123
+"""
+from __future__ import annotations
+
+NULL_REAL = -9.9e15
+MIN_VALUE = 1.0e-16
+
+
+def _mn(a, b):
+    return b if b < a else a
+
+
+def _mx(a, b):
+    return b if b > a else a
+
+
+def face(P, V, du, dt, Q, vrm, method, limiter, nb, up2):
+    """ComputeAdvectionFace; P, V, du are 4-lists for cells f-2..f+1."""
+    cup1 = [0.0, 0.0, 0.0, 0.0]
+    if Q > 0.0:
+        cup1[1] = 1.0
+    else:
+        cup1[2] = 1.0
+    Cr = 0.0
+    vrel = 0.0
+    if not nb:
+        if Q > 0:
+            Cr = Q * dt / V[1]
+            vrel = _mx(_mx(V[0], V[1]), V[2]) / _mn(_mn(V[0], V[1]), V[2])
+        else:
+            Cr = Q * dt / V[2]
+            vrel = _mx(_mx(V[1], V[2]), V[3]) / _mn(_mn(V[1], V[2]), V[3])
+    if method == 1 or (nb and up2):
+        high = list(cup1)
+        theta = 0.0
+    elif method == 2 and not nb:
+        if Q > 0:
+            high = [-1.0 / 8.0, 6.0 / 8.0, 3.0 / 8.0, 0.0]
+        elif Q < 0:
+            high = [0.0, 3.0 / 8.0, 6.0 / 8.0, -1.0 / 8.0]
+        else:
+            high = [0.0, 0.0, 1.0, 0.0]
+        theta = 0.0 if vrel > vrm else 1.0
+    elif method == 3 and not nb:
+        c = (1 - 2.0 * abs(Cr)) / 6.0
+        a = 0.5 + c
+        b = 0.5 - c
+        d = (1 - abs(Cr)) / 2.0
+        if Q > 0:
+            high = [-d * b, 1 + d * (b - a), d * a, 0.0]
+        elif Q < 0:
+            high = [0.0, d * a, 1 + d * (b - a), -d * b]
+        else:
+            high = [0.0, 0.0, 1.0, 0.0]
+        theta = 0.0 if vrel > vrm else 1.0
+    elif method in (5, 6):
+        high = [0.0, du[2] / (du[1] + du[2]), du[1] / (du[1] + du[2]), 0.0]
+        theta = 1.0
+    elif method == 4 and not nb:
+        high = [0.0, 0.0, 0.0, 0.0]
+        if Q > 0.0:
+            high[2] = 1.0
+            dC = (P[2] - P[1]) / (du[2] + du[1])
+            if abs(dC) < MIN_VALUE:
+                dC = MIN_VALUE if dC >= 0 else -MIN_VALUE
+            r = (P[1] - P[0]) / (du[1] + du[0]) / dC
+        else:
+            high[1] = 1.0
+            dC = (P[1] - P[2]) / (du[2] + du[1])
+            if abs(dC) < MIN_VALUE:
+                dC = MIN_VALUE if dC >= 0 else -MIN_VALUE
+            r = (P[2] - P[3]) / (du[2] + du[3]) / dC
+        if limiter == 1:
+            theta = _mx(0.0, _mn(1.0, r))
+        elif limiter == 2:
+            theta = 0.0 if r < 0 else 2.0 * r / (1 + r)
+        elif limiter == 3:
+            theta = _mx(0.0, _mn(_mn(2.0, 2.0 * r), (1 + r) / 2.0))
+        elif limiter == 4:
+            theta = _mx(_mx(0.0, _mn(1.0, 2.0 * r)), _mn(r, 2.0))
+        elif limiter == 5:
+            a = 0.5 + (1 - 2.0 * abs(Cr)) / 6.0
+            b = 0.5 - (1 - 2.0 * abs(Cr)) / 6.0
+            aux = a + b * r
+            if abs(Cr) < MIN_VALUE:
+                Cr = MIN_VALUE
+            theta = _mx(0.0, _mn(_mn(aux, 2.0 / (1.0 - Cr)), 2.0 * r / Cr))
+        else:
+            raise ValueError("limiter")
+        theta = 0.5 * theta * (1.0 - Cr)
+    else:
+        raise ValueError("method stops")
+    return [(1.0 - theta) * cup1[n] + theta * high[n] for n in range(4)]
+
+
+def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
+    """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
+    `p` is a dict of AdvectionDiffusion scalar arguments."""
+    ni, nj, nk = dom.ni, dom.nj, dom.nk
+    A = dom.arrays
+    f3 = lambda n: A[n].tolist()           # [k][j][i]
+    Qx, Qy, Qz = f3("Wflux_X"), f3("Wflux_Y"), f3("Wflux_Z")
+    V, Vo = f3("VolumeZ"), f3("VolumeZOld")
+    VH, DV = f3("Visc_H"), f3("Diff_V")
+    AU, AV, DZZ, DWZ = f3("AreaU"), f3("AreaV"), f3("DZZ"), f3("DWZ")
+    OP, LP, WP = f3("OpenPoints3D"), f3("LandPoints3D"), f3("WaterPoints3D")
+    CU, CV, CW = f3("ComputeFacesU3D"), f3("ComputeFacesV3D"), f3("ComputeFacesW3D")
+    DUX, DVY, DZX, DZY = (A[n].tolist() for n in ("DUX", "DVY", "DZX", "DZY"))
+    KF, BP = A["KFloorZ"].tolist(), A["BoundaryPoints2D"].tolist()
+    Pl = P.tolist()
+    R = ReferenceProp.tolist() if ReferenceProp is not None else None
+    SD = SmallDepths.tolist() if SmallDepths is not None else None
+    DT = p["DTProp"]
+    K, J, I = nk + 2, nj + 2, ni + 2
+    z3 = lambda v: [[[v] * I for _ in range(J)] for _ in range(K)]
+    Kx, Ky, Kz = z3(NULL_REAL), z3(NULL_REAL), z3(NULL_REAL)
+    for k in range(2, nk + 1):
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if CW[k][j][i] == 1:
+                    Kz[k][j][i] = p["SchmidtCoef_V"] * DV[k][j][i] + p["SchmidtBackground_V"]
+                    if p["NullDif"] and Qz[k][j][i] == 0.0:
+                        Kz[k][j][i] = 0.0
+    for k in range(1, nk + 1):
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if CU[k][j][i] == 1:
+                    Kx[k][j][i] = p["schmidt_H"] * (VH[k][j][i] * DUX[j - 1][i] + VH[k][j - 1][i] * DUX[j][i]) \
+                        / (DUX[j][i] + DUX[j - 1][i])
+                    if p["NullDif"] and Qx[k][j][i] == 0.0:
+                        Kx[k][j][i] = 0.0
+                if CV[k][j][i] == 1:
+                    Ky[k][j][i] = p["schmidt_H"] * (VH[k][j][i] * DVY[j][i - 1] + VH[k][j][i - 1] * DVY[j][i]) \
+                        / (DVY[j][i] + DVY[j][i - 1])
+                    if p["NullDif"] and Qy[k][j][i] == 0.0:
+                        Ky[k][j][i] = 0.0
+    D, E, F, TI = z3(0.0), z3(1.0), z3(0.0), z3(0.0)
+    XC, XD, XE, XF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
+    YC, YD, YE, YF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
+    ZC, ZD, ZE, ZF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
+
+    # VolumeVariation
+    for k in range(1, nk + 1):
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if OP[k][j][i] == 1:
+                    TI[k][j][i] = Pl[k][j][i] * (Vo[k][j][i] / V[k][j][i])
+                    if k == nk:
+                        E[k][j][i] = 1.0 + (DT / V[k][j][i]) * Qz[k + 1][j][i]
+                else:
+                    TI[k][j][i] = Pl[k][j][i]
+
+    mH, lH, u2H = p["AdvMethodH"], p["TVDLimitationH"], bool(p["Upwind2H"])
+    if not p["Vertical1D"]:
+        for k in range(1, nk + 1):
+            for j in range(1, nj + 1):
+                for i in range(1, ni + 1):
+                    if CU[k][j][i] == 1:
+                        aux = Kx[k][j][i] * AU[k][j][i] / DZX[j - 1][i]
+                        dP = Pl[k][j][i] - Pl[k][j - 1][i]
+                        TI[k][j - 1][i] = TI[k][j - 1][i] + aux * DT / V[k][j - 1][i] * dP
+                        TI[k][j][i] = TI[k][j][i] - aux * DT / V[k][j][i] * dP
+        if not p["XZFlow"]:
+            for k in range(1, nk + 1):
+                for j in range(1, nj + 1):
+                    for i in range(1, ni + 1):
+                        if CV[k][j][i] == 1:
+                            aux = Ky[k][j][i] * AV[k][j][i] / DZY[j][i - 1]
+                            dP = Pl[k][j][i] - Pl[k][j][i - 1]
+                            TI[k][j][i - 1] = TI[k][j][i - 1] + aux * DT / V[k][j][i - 1] * dP
+                            TI[k][j][i] = TI[k][j][i] - aux * DT / V[k][j][i] * dP
+        # XX: faces j = 1..nj of every line (i, :, k)
+        for k in range(1, nk + 1):
+            for i in range(1, ni + 1):
+                for j in range(1, nj + 1):
+                    if OP[k][j - 1][i] == 1 and OP[k][j][i] == 1:
+                        q = Qx[k][j][i]
+                        nb = (OP[k][j - 2][i] != 1) if q > 0 else (OP[k][j + 1][i] != 1)
+                        cf = face([Pl[k][j + n][i] for n in (-2, -1, 0, 1)],
+                                  [V[k][j + n][i] for n in (-2, -1, 0, 1)],
+                                  [DUX[j + n][i] for n in (-2, -1, 0, 1)], DT, q,
+                                  p["VolumeRelMax"], mH, lH, nb, u2H)
+                        XC[k][j][i], XD[k][j][i], XE[k][j][i], XF[k][j][i] = (q * c for c in cf)
+        for k in range(1, nk + 1):
+            for j in range(1, nj + 1):
+                for i in range(1, ni + 1):
+                    if CU[k][j][i] == 1:
+                        fl = XC[k][j][i] * Pl[k][j - 2][i] + XD[k][j][i] * Pl[k][j - 1][i] + \
+                            XE[k][j][i] * Pl[k][j][i] + XF[k][j][i] * Pl[k][j + 1][i]
+                        TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
+                        TI[k][j - 1][i] = TI[k][j - 1][i] - fl * DT / V[k][j - 1][i]
+        if not p["XZFlow"]:
+            for k in range(1, nk + 1):
+                for j in range(1, nj + 1):
+                    for i in range(1, ni + 1):
+                        if OP[k][j][i - 1] == 1 and OP[k][j][i] == 1:
+                            q = Qy[k][j][i]
+                            nb = (OP[k][j][i - 2] != 1) if q > 0 else (OP[k][j][i + 1] != 1)
+                            cf = face([Pl[k][j][i + n] for n in (-2, -1, 0, 1)],
+                                      [V[k][j][i + n] for n in (-2, -1, 0, 1)],
+                                      [DVY[j][i + n] for n in (-2, -1, 0, 1)], DT, q,
+                                      p["VolumeRelMax"], mH, lH, nb, u2H)
+                            YC[k][j][i], YD[k][j][i], YE[k][j][i], YF[k][j][i] = (q * c for c in cf)
+            for k in range(1, nk + 1):
+                for j in range(1, nj + 1):
+                    for i in range(1, ni + 1):
+                        if CV[k][j][i] == 1:
+                            fl = YC[k][j][i] * Pl[k][j][i - 2] + YD[k][j][i] * Pl[k][j][i - 1] + \
+                                YE[k][j][i] * Pl[k][j][i] + YF[k][j][i] * Pl[k][j][i + 1]
+                            TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
+                            TI[k][j][i - 1] = TI[k][j][i - 1] - fl * DT / V[k][j][i - 1]
+
+    if nk > 1:
+        ie = p["ImpExp_DifV"]
+        for k in range(1, nk + 1):
+            for j in range(1, nj + 1):
+                for i in range(1, ni + 1):
+                    sd = SD is not None and SD[j][i] != 0
+                    if CW[k][j][i] == 1 and not sd:
+                        auxk = Kz[k][j][i] * DUX[j][i] * DVY[j][i] / DZZ[k - 1][j][i]
+                        a1 = auxk * DT / V[k - 1][j][i]
+                        a2 = auxk * DT / V[k][j][i]
+                        dP = Pl[k][j][i] - Pl[k - 1][j][i]
+                        E[k - 1][j][i] = E[k - 1][j][i] + a1 * ie
+                        F[k - 1][j][i] = F[k - 1][j][i] - a1 * ie
+                        TI[k - 1][j][i] = TI[k - 1][j][i] + a1 * dP * (1.0 - ie)
+                        D[k][j][i] = D[k][j][i] - a2 * ie
+                        E[k][j][i] = E[k][j][i] + a2 * ie
+                        TI[k][j][i] = TI[k][j][i] - a2 * dP * (1.0 - ie)
+        if not p["Vertical1D"]:
+            mV, lV, u2V = p["AdvMethodV"], p["TVDLimitationV"], bool(p["Upwind2V"])
+            for j in range(1, nj + 1):
+                for i in range(1, ni + 1):
+                    if OP[nk][j][i] != 1:
+                        continue
+                    for k in range(1, nk + 1):
+                        if OP[k - 1][j][i] == 1 and OP[k][j][i] == 1:
+                            q = Qz[k][j][i]
+                            nb = (OP[k - 2][j][i] != 1) if q > 0 else (OP[k + 1][j][i] != 1)
+                            cf = face([Pl[k + n][j][i] for n in (-2, -1, 0, 1)],
+                                      [V[k + n][j][i] for n in (-2, -1, 0, 1)],
+                                      [DWZ[k + n][j][i] for n in (-2, -1, 0, 1)], DT, q,
+                                      p["VolumeRelMax"], mV, lV, nb, u2V)
+                            ZC[k][j][i], ZD[k][j][i], ZE[k][j][i], ZF[k][j][i] = (q * c for c in cf)
+            if p["ImpExp_AdvV"] == 0.0:
+                for k in range(1, nk + 1):
+                    for j in range(1, nj + 1):
+                        for i in range(1, ni + 1):
+                            if CW[k][j][i] == 1:
+                                fl = ZC[k][j][i] * Pl[k - 2][j][i] + ZD[k][j][i] * Pl[k - 1][j][i] + \
+                                    ZE[k][j][i] * Pl[k][j][i] + ZF[k][j][i] * Pl[k + 1][j][i]
+                                TI[k - 1][j][i] = TI[k - 1][j][i] - fl * DT / V[k - 1][j][i]
+                                TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
+            else:
+                def upd(k, j, i, dt1, dt2):
+                    D[k][j][i] = D[k][j][i] - ZD[k][j][i] * dt2
+                    E[k][j][i] = E[k][j][i] - ZE[k][j][i] * dt2
+                    E[k - 1][j][i] = E[k - 1][j][i] + ZD[k][j][i] * dt1
+                    F[k - 1][j][i] = F[k - 1][j][i] + ZE[k][j][i] * dt1
+                if p["Docycle_method"] == 1:
+                    for j in range(1, nj + 1):
+                        for i in range(1, ni + 1):
+                            if CW[nk][j][i] == 1:
+                                kb = KF[j][i]
+                                vb = V[kb][j][i]
+                                for k in range(kb + 1, nk + 1):
+                                    dt1 = DT / vb
+                                    dt2 = DT / V[k][j][i]
+                                    vb = V[k][j][i]
+                                    upd(k, j, i, dt1, dt2)
+                else:
+                    for k in range(1, nk + 1):
+                        for j in range(1, nj + 1):
+                            for i in range(1, ni + 1):
+                                if CW[k][j][i] == 1:
+                                    upd(k, j, i, DT / V[k - 1][j][i], DT / V[k][j][i])
+
+    if R is not None:
+        bc = p["BoundaryCondition"]
+        tdec = 1.0 / (1.0 + p["DecayTime"] / DT)
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if BP[j][i] != 1:
+                    continue
+                for k in range(abs(KF[j][i]), nk + 1):
+                    if OP[k][j][i] != 1:
+                        continue
+                    dtv = DT / V[k][j][i]
+                    if bc in (2, 5):
+                        a1 = OP[k][j][i + 1] * (1 - BP[j][i + 1])
+                        a2 = OP[k][j][i - 1] * (1 - BP[j][i - 1])
+                        a3 = OP[k][j + 1][i] * (1 - BP[j + 1][i])
+                        a4 = OP[k][j - 1][i] * (1 - BP[j - 1][i])
+                        at = float(a1 + a2 + a3 + a4)
+                        if at > 0:
+                            inner = (Pl[k][j][i + 1] * a1 + Pl[k][j][i - 1] * a2 + Pl[k][j + 1][i] * a3 +
+                                     Pl[k][j - 1][i] * a4) / at
+                            ext = inner * (1.0 - tdec) + R[k][j][i] * tdec
+                        else:
+                            ext = R[k][j][i]
+                        TI[k][j][i] = ext
+                        D[k][j][i], E[k][j][i], F[k][j][i] = 0.0, 1.0, 0.0
+                    else:
+                        wf = Qx[k][j][i] * CU[k][j][i] - Qx[k][j + 1][i] * CU[k][j + 1][i] + \
+                            Qy[k][j][i] * CV[k][j][i] - Qy[k][j][i + 1] * CV[k][j][i + 1] + \
+                            Qz[k][j][i] * CW[k][j][i] - Qz[k + 1][j][i] * CW[k + 1][j][i] - \
+                            (V[k][j][i] - Vo[k][j][i]) / DT
+                        ext = Pl[k][j][i] * (1.0 - tdec) + R[k][j][i] * tdec
+                        if wf < 0.0:
+                            TI[k][j][i] = TI[k][j][i] - wf * ext * dtv
+                        else:
+                            E[k][j][i] = E[k][j][i] + wf * dtv
+
+    for k in range(K):
+        for j in range(J):
+            for i in range(I):
+                if LP[k][j][i] == 1:
+                    TI[k][j][i] = NULL_REAL
+
+    # THOMASZ_NewType2
+    W = [0.0] * (nk + 2)
+    G = [0.0] * (nk + 2)
+    for j in range(1, nj + 1):
+        for i in range(1, ni + 1):
+            if WP[nk][j][i] != 1:
+                continue
+            W[1] = -F[1][j][i] / E[1][j][i]
+            G[1] = TI[1][j][i] / E[1][j][i]
+            for k in range(2, nk + 2):
+                aux = E[k][j][i] + D[k][j][i] * W[k - 1]
+                if abs(aux) > 0:
+                    W[k] = -F[k][j][i] / aux
+                    G[k] = (TI[k][j][i] - D[k][j][i] * G[k - 1]) / aux
+                else:
+                    W[k] = 0.0
+                    G[k] = 0.0
+            Pl[nk + 1][j][i] = G[nk + 1]
+            for k in range(nk, 0, -1):
+                Pl[k][j][i] = W[k] * Pl[k + 1][j][i] + G[k]
+    P[...] = Pl

@@ -1,0 +1,43 @@
+"""Seeded small domains and option sets shared by the parity tests."""
+from mohid_gb300 import synth
+
+# small grids: coastline block, z-level uneven columns, open boundaries with
+# moving volumes, single layer (2-D), fully open, single column
+SMALL = {
+    "coast": dict(ni=7, nj=9, nk=5, land_frac=0.2, land_kind=0, seed=3),
+    "zlevel": dict(ni=8, nj=6, nk=6, land_frac=0.25, land_kind=1, seed=4, zlevel=True,
+                   hmin=2.0, hmax=60.0, bathy_kind=2),
+    "open": dict(ni=9, nj=8, nk=4, land_frac=0.1, land_kind=1, seed=5, open_sides=3,
+                 vol_var=0.01, bathy_kind=1),
+    "layer1": dict(ni=6, nj=7, nk=1, land_frac=0.0, seed=6),
+    "nsopen": dict(ni=10, nj=6, nk=3, land_frac=0.0, seed=7, open_sides=12, bathy_kind=1),
+    "column": dict(ni=1, nj=1, nk=8, land_frac=0.0, seed=8),
+}
+
+# AdvectionDiffusion option sets (non-default values only)
+OPTIONS = {
+    "upwind1": dict(),
+    "tvd_superbee": dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+    "tvd_minmod": dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1),
+    "tvd_vanleer": dict(AdvMethodH=4, TVDLimitationH=2, Upwind2H=1),
+    "tvd_muscl": dict(AdvMethodH=4, TVDLimitationH=3, Upwind2H=1),
+    "tvd_pdm": dict(AdvMethodH=4, TVDLimitationH=5, Upwind2H=1),
+    "upwind2": dict(AdvMethodH=2, Upwind2H=1),
+    "upwind3": dict(AdvMethodH=3, Upwind2H=1),
+    "central": dict(AdvMethodH=5),
+    "leapfrog": dict(AdvMethodH=6),
+    "tvd_vertical": dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1),
+    "explicit_v_tvd": dict(ImpExp_AdvV=0.0, AdvMethodV=4, TVDLimitationV=1, Upwind2V=1),
+    "explicit_v_up3": dict(ImpExp_AdvV=0.0, AdvMethodV=3, Upwind2V=1),
+    "theta_difv": dict(ImpExp_DifV=0.5),
+    "explicit_difv": dict(ImpExp_DifV=0.0),
+    "docycle2": dict(Docycle_method=2),
+    "nulldif": dict(NullDif=1),
+    "vertical1d": dict(Vertical1D=1),
+    "xzflow": dict(XZFlow=1),
+    "background": dict(SchmidtBackground_V=1e-3, schmidt_H=0.7, SchmidtCoef_V=2.0),
+}
+
+
+def domain(name, dt=30.0):
+    return synth.generate(synth.GenSpec(**SMALL[name], dt=dt))

@@ -1,0 +1,195 @@
+"""Plain FP64 drop-in on the GPU against the FP64 oracle (through the C-ABI).
+
+Tolerance: the kernel evaluates every term in the reference's order without
+fused multiply-add, so results are expected to be bit-identical; the bar
+asserted is max relative difference <= 1e-12 over water cells plus exact
+equality of land/null/halo cells.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mohid_gb300 import advdiff, configs, synth
+from oracle import oracle as O
+from tests.cases import SMALL, OPTIONS, domain
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def _compare(d, Pg, Po):
+    wp = d.water_mask()
+    other = ~wp
+    assert np.array_equal(Pg[other], Po[other])
+    scale = np.maximum(np.abs(Po[wp]), 1e-30)
+    rel = np.max(np.abs(Pg[wp] - Po[wp]) / scale) if wp.any() else 0.0
+    assert rel <= RTOL, f"max rel diff {rel:.3e}"
+    return rel
+
+
+@pytest.mark.parametrize("grid", sorted(SMALL))
+@pytest.mark.parametrize("opt", sorted(OPTIONS))
+def test_gpu_matches_oracle_one_step(gpu, grid, opt):
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.7, seed=9)
+    pd = dict(DTProp=30.0, **OPTIONS[opt])
+    Po = P0.copy()
+    assert O.step(d, Po, O.params(**pd)) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(**pd))
+    ad.kill()
+    _compare(d, Pg, Po)
+    assert np.array_equal(Pg, Po), "expected bit-identical FP64 results"
+
+
+@pytest.mark.parametrize("grid", ["open", "nsopen"])
+@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0)])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod", "tvd_superbee"])
+def test_gpu_open_boundaries(gpu, grid, bc, decay, opt):
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    pd = dict(DTProp=30.0, BoundaryCondition=bc, DecayTime=decay, **OPTIONS[opt])
+    Po = P0.copy()
+    assert O.step(d, Po, O.params(**pd), ReferenceProp=R) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(**pd), ReferenceProp=R)
+    ad.kill()
+    _compare(d, Pg, Po)
+    assert np.array_equal(Pg, Po)
+
+
+def test_gpu_small_depths(gpu):
+    d = domain("coast")
+    sd = np.zeros(d.shape2, dtype=np.int32)
+    sd[2:5, 3:6] = 1
+    P0 = d.tracer(1, 10.0, 20.0, seed=3)
+    Po = P0.copy()
+    assert O.step(d, Po, O.params(DTProp=30.0), SmallDepths=sd) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro(SmallDepths=sd)
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(DTProp=30.0))
+    ad.kill()
+    assert np.array_equal(Pg, Po)
+
+
+def test_gpu_cfg1_100_steps_device_resident(gpu):
+    """Config 1 at full size: 100 steps device-resident (ping-pong) vs 100 oracle steps."""
+    import torch
+    w = configs.cfg1()
+    d = synth.generate(w.spec)
+    P0 = d.tracer(*w.tracers[0], seed=11)
+    pd = w.params()
+    Po = P0.copy()
+    work = O.Work(d)
+    for _ in range(w.steps):
+        assert O.step(d, Po, O.params(**pd), work=work) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    a = torch.from_numpy(P0).cuda()
+    b = torch.empty_like(a)
+    p = advdiff.params(**pd)
+    torch.cuda.synchronize()
+    for _ in range(w.steps):
+        ad.step_device(a, b, p)
+        a, b = b, a
+    ad.sync()
+    Pg = a.cpu().numpy()
+    ad.kill()
+    wp = d.water_mask()
+    rel_l2 = np.linalg.norm(Pg[wp] - Po[wp]) / np.linalg.norm(Po[wp])
+    assert rel_l2 <= 1e-12
+    assert np.array_equal(Pg, Po)
+    m0, m1 = O.mass(d, P0), O.mass(d, Pg)
+    assert abs(m1 - m0) / m0 < 1e-12
+
+
+def test_gpu_cfg2_full_size_one_step(gpu):
+    """Config 2 grid (512x512x40, P2_TVD SuperBee) at full size, both tracers."""
+    w = configs.cfg2()
+    d = synth.generate(w.spec)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    for t, (kind, a_, b_) in enumerate(w.tracers):
+        P0 = d.tracer(kind, a_, b_, seed=100 + t)
+        Po = P0.copy()
+        assert O.step(d, Po, O.params(**w.params())) == 0
+        Pg = P0.copy()
+        ad.step(Pg, advdiff.params(**w.params()))
+        _compare(d, Pg, Po)
+    ad.kill()
+
+
+def test_gpu_thomasz_matches_oracle(gpu):
+    rng = np.random.default_rng(1)
+    ni, nj, nk = 37, 29, 23
+    sh = (nk + 2, nj + 2, ni + 2)
+    D = rng.uniform(-1, 0, sh); F = rng.uniform(-1, 0, sh)
+    E = 2.5 + rng.uniform(0, 1, sh); TI = rng.normal(size=sh)
+    WP = (rng.random(sh) < 0.8).astype(np.int32)
+    R1 = rng.normal(size=sh); R2 = R1.copy()
+    assert O.thomasz(D, E, F, TI, R1, WP) == 0
+    advdiff.thomasz(D, E, F, TI, R2, WP)
+    assert np.array_equal(R1, R2)
+
+
+def test_gpu_zero_pivot_reported(gpu):
+    sh = (5, 3, 3)
+    D = np.zeros(sh); E = np.ones(sh); F = np.zeros(sh); TI = np.ones(sh)
+    D[2, 1, 1] = 1.0; E[2, 1, 1] = 0.0
+    WP = np.ones(sh, dtype=np.int32)
+    RES = np.zeros(sh)
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        advdiff.thomasz(D, E, F, TI, RES, WP)
+    assert ei.value.code == 6
+
+
+@pytest.mark.parametrize("bad,code", [
+    (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
+    (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
+    (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
+    (dict(ImpExp_AdvXX=1.0), 4), (dict(CellFluxes=1), 4), (dict(AdvectionNudging=1), 4),
+])
+def test_gpu_rejects_options_like_oracle(gpu, bad, code):
+    d = domain("coast")
+    P = d.tracer(4, 1.0, 0.0, seed=1)
+    P0 = P.copy()
+    assert O.step(d, P.copy(), O.params(DTProp=30.0, **bad)) == code
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        ad.step(P, advdiff.params(DTProp=30.0, **bad))
+    ad.kill()
+    assert ei.value.code == code
+    assert np.array_equal(P, P0)
+
+
+def test_gpu_rejects_lower_edge_face(gpu):
+    d = domain("coast")
+    d.arrays["ComputeFacesU3D"][2, 1, 3] = 1
+    ad = advdiff.AdvectionDiffusion(d)
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        ad.set_hydro()
+    assert ei.value.code == 1
+    ad.kill()
+
+
+def test_gpu_unknown_id_and_bad_bounds(gpu):
+    lib = advdiff.N.ad_lib()
+    st = C.c_int(0)
+    bogus = C.c_int(987654)
+    assert lib.mohid_ad_sync(C.byref(bogus), C.byref(st)) == 2 and st.value == 2
+    size = advdiff.N.T_Size3D(0, 5, 0, 5, 0, 5)
+    work = advdiff.N.T_Size3D(1, 4, 1, 3, 1, 4)      # JUB inconsistent with Size
+    z = np.zeros((6, 6)); zi = np.zeros((6, 6), dtype=np.int32)
+    idv = C.c_int(0)
+    rc = lib.mohid_ad_init(C.byref(idv), C.byref(size), C.byref(work), advdiff.N.ptr(z),
+                           advdiff.N.ptr(z), advdiff.N.ptr(z), advdiff.N.ptr(z),
+                           advdiff.N.iptr(zi), advdiff.N.iptr(zi), C.byref(st))
+    assert rc == 1

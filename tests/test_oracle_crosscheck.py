@@ -1,0 +1,44 @@
+"""The C oracle against the independent pure-Python restatement, bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O, ref_py
+from tests.cases import SMALL, OPTIONS, domain
+
+
+@pytest.mark.parametrize("grid", sorted(SMALL))
+@pytest.mark.parametrize("opt", sorted(OPTIONS))
+def test_c_oracle_equals_python_restatement(built, grid, opt):
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.7, seed=9)
+    pd = dict(O.DEFAULTS, DTProp=30.0, **OPTIONS[opt])
+    Pc, Pp = P0.copy(), P0.copy()
+    assert O.step(d, Pc, O.params(**pd)) == 0
+    ref_py.step(d, Pp, pd)
+    assert np.array_equal(Pc, Pp)
+
+
+@pytest.mark.parametrize("grid", ["open", "nsopen"])
+@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0)])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod"])
+def test_open_boundaries_c_equals_python(built, grid, bc, decay, opt):
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    pd = dict(O.DEFAULTS, DTProp=30.0, BoundaryCondition=bc, DecayTime=decay, **OPTIONS[opt])
+    Pc, Pp = P0.copy(), P0.copy()
+    assert O.step(d, Pc, O.params(**pd), ReferenceProp=R) == 0
+    ref_py.step(d, Pp, pd, ReferenceProp=R)
+    assert np.array_equal(Pc, Pp)
+
+
+def test_small_depths_c_equals_python(built):
+    d = domain("coast")
+    sd = np.zeros(d.shape2, dtype=np.int32)
+    sd[2:5, 3:6] = 1
+    P0 = d.tracer(1, 10.0, 20.0, seed=3)
+    pd = dict(O.DEFAULTS, DTProp=30.0)
+    Pc, Pp = P0.copy(), P0.copy()
+    assert O.step(d, Pc, O.params(**pd), SmallDepths=sd) == 0
+    ref_py.step(d, Pp, pd, SmallDepths=sd)
+    assert np.array_equal(Pc, Pp)

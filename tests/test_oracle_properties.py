@@ -1,0 +1,174 @@
+"""Known-answer properties of the FP64 oracle (the reference has no tests for this path)."""
+import numpy as np
+import pytest
+
+from mohid_gb300 import synth
+from oracle import oracle as O
+from tests.cases import domain
+
+NULL = -9.9e15
+
+
+def test_thomasz_matches_dense_solve(built):
+    rng = np.random.default_rng(0)
+    ni, nj, nk = 5, 4, 7
+    sh = (nk + 2, nj + 2, ni + 2)
+    D = rng.uniform(-1, 0, sh); F = rng.uniform(-1, 0, sh)
+    E = 2.5 + rng.uniform(0, 1, sh); TI = rng.normal(size=sh)
+    # row KUB+1 as AdvectionDiffusion leaves it: D = F = 0, E = 1, TI = 0
+    D[nk + 1] = 0.0; F[nk + 1] = 0.0; E[nk + 1] = 1.0; TI[nk + 1] = 0.0
+    D[1] = 0.0                      # row 1 has no sub-diagonal (THOMASZ ignores it)
+    F[nk] = 0.0                     # couple rows 1..nk only
+    WP = np.ones(sh, dtype=np.int32); WP[nk, 2, 3] = 0   # one column not solved
+    RES = np.full(sh, 7.0)
+    assert O.thomasz(D, E, F, TI, RES, WP) == 0
+    for j in range(1, nj + 1):
+        for i in range(1, ni + 1):
+            if WP[nk, j, i] != 1:
+                assert np.all(RES[:, j, i] == 7.0)
+                continue
+            A = np.zeros((nk + 1, nk + 1)); b = TI[1:, j, i].copy()
+            for r in range(nk + 1):
+                k = r + 1
+                A[r, r] = E[k, j, i]
+                if r > 0: A[r, r - 1] = D[k, j, i]
+                if r < nk: A[r, r + 1] = F[k, j, i]
+            x = np.linalg.solve(A, b)
+            np.testing.assert_allclose(RES[1:, j, i], x, rtol=1e-12, atol=1e-14)
+
+
+def test_thomasz_zero_pivot_reported(built):
+    sh = (5, 3, 3)
+    D = np.zeros(sh); E = np.ones(sh); F = np.zeros(sh); TI = np.ones(sh)
+    D[2, 1, 1] = 1.0; E[2, 1, 1] = 0.0              # aux = 0 + 1 * W(1) = 0 (W(1) = 0)
+    WP = np.ones(sh, dtype=np.int32)
+    RES = np.zeros(sh)
+    assert O.thomasz(D, E, F, TI, RES, WP) == 6      # MOHID_AD_ERR_ZERO_PIVOT
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "nsopen"])
+@pytest.mark.parametrize("opt", [dict(), dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+                                 dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1)])
+def test_constancy_preserved(built, grid, opt):
+    d = domain(grid)
+    wp = d.water_mask()
+    P = np.where(wp, 3.25, 0.0)
+    R = np.full(d.shape3, 3.25) if d.spec.open_sides else None
+    p = O.params(DTProp=30.0, **opt)
+    for _ in range(5):
+        assert O.step(d, P, p, ReferenceProp=R) == 0
+    assert np.max(np.abs(P[wp] - 3.25)) < 1e-12
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "layer1"])
+@pytest.mark.parametrize("opt", [dict(), dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+                                 dict(ImpExp_DifV=0.5), dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1)])
+def test_mass_conserved_closed(built, grid, opt):
+    d = domain(grid)
+    P = d.tracer(3, 1.0, 0.8, seed=4)
+    p = O.params(DTProp=30.0, **opt)
+    m0 = O.mass(d, P)
+    for _ in range(20):
+        assert O.step(d, P, p) == 0
+    m1 = O.mass(d, P)
+    assert abs(m1 - m0) / abs(m0) < 1e-13
+
+
+def test_mass_with_moving_volumes(built):
+    # sum V*P_new equals sum Vold*P_old when volumes change inside columns
+    d = synth.generate(synth.GenSpec(ni=12, nj=10, nk=6, land_frac=0.15, land_kind=1,
+                                     vol_var=0.02, seed=21, dt=30.0))
+    P = d.tracer(1, 5.0, 25.0, seed=2)
+    wp = d.water_mask()
+    before = np.sum(d.VolumeZOld[wp] * P[wp])
+    assert O.step(d, P, O.params(DTProp=30.0)) == 0
+    after = np.sum(d.VolumeZ[wp] * P[wp])
+    assert abs(after - before) / before < 1e-13
+
+
+def test_pure_vertical_diffusion_matches_discrete_solve(built):
+    d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
+                                     kz_median=1e-2, kz_logsigma=0.8))
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z"):
+        a[n][...] = 0.0
+    # a lone column has no horizontal compute face, so MOHID would not open its
+    # W faces (ModuleMap.F90:1598-1608); open them here to isolate the solve
+    a["ComputeFacesW3D"][2:d.nk + 1, 1, 1] = 1
+    a["OpenPoints3D"][1:d.nk + 1, 1, 1] = 1
+    P = d.tracer(1, 5.0, 25.0, seed=1)
+    dt = 600.0
+    p = O.params(DTProp=dt, SchmidtBackground_V=0.0)
+    P0 = P.copy()
+    assert O.step(d, P, p) == 0
+    nk = d.nk
+    V = a["VolumeZ"][:, 1, 1]; Kz = a["Diff_V"][:, 1, 1]; DZZ = a["DZZ"][:, 1, 1]
+    area = a["DUX"][1, 1] * a["DVY"][1, 1]
+    M = np.eye(nk)
+    for k in range(2, nk + 1):           # face k between cells k-1 and k
+        g = Kz[k] * area / DZZ[k - 1] * dt
+        r, s = k - 2, k - 1
+        M[r, r] += g / V[k - 1]; M[r, s] -= g / V[k - 1]
+        M[s, s] += g / V[k]; M[s, r] -= g / V[k]
+    x = np.linalg.solve(M, P0[1:nk + 1, 1, 1])
+    np.testing.assert_allclose(P[1:nk + 1, 1, 1], x, rtol=1e-12)
+
+
+@pytest.mark.parametrize("limiter", [1, 2, 3, 4])
+def test_tvd_step_creates_no_new_extrema(built, limiter):
+    # quasi 1-D channel, west-east through-flow, a step profile
+    d = synth.generate(synth.GenSpec(ni=1, nj=60, nk=1, land_frac=0.0, open_sides=3,
+                                     seed=5, dt=30.0, umax=0.5))
+    a = d.arrays
+    P = np.zeros(d.shape3)
+    P[1, 1, 1:31] = 1.0; P[1, 1, 31:61] = 0.2
+    R = np.full(d.shape3, 0.6)
+    p = O.params(DTProp=30.0, AdvMethodH=4, TVDLimitationH=limiter, Upwind2H=1)
+    for _ in range(30):
+        assert O.step(d, P, p, ReferenceProp=R) == 0
+        w = P[1, 1, 1:61]
+        assert w.max() <= 1.0 + 1e-12 and w.min() >= 0.2 - 1e-12
+
+
+def test_land_and_halo_handling(built):
+    d = domain("zlevel")
+    a = d.arrays
+    P = d.tracer(4, 2.0, 0.0, seed=1) + 0.0
+    P[a["WaterPoints3D"] == 0] = 5.0                  # land and halo values to watch
+    P0 = P.copy()
+    assert O.step(d, P, O.params(DTProp=30.0)) == 0
+    nk = d.nk
+    solved = a["WaterPoints3D"][nk] == 1
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            col = P[:, j, i]
+            if not solved[j, i]:
+                assert np.array_equal(col, P0[:, j, i])       # untouched
+                continue
+            kf = a["KFloorZ"][j, i]
+            assert np.all(col[1:kf] == NULL)                   # below KFloor: null_real
+            assert col[nk + 1] == 0.0                          # row KUB+1 solved to 0
+            assert col[0] == P0[0, j, i]                       # row 0 untouched
+    # halo columns untouched
+    assert np.array_equal(P[:, 0, :], P0[:, 0, :]) and np.array_equal(P[:, :, 0], P0[:, :, 0])
+
+
+@pytest.mark.parametrize("bad,code", [
+    (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
+    (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
+    (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
+    (dict(ImpExp_AdvXX=1.0), 4), (dict(CellFluxes=1), 4), (dict(AdvectionNudging=1), 4),
+])
+def test_rejected_options(built, bad, code):
+    d = domain("coast")
+    P = d.tracer(4, 1.0, 0.0, seed=1)
+    P0 = P.copy()
+    assert O.step(d, P, O.params(DTProp=30.0, **bad)) == code
+    assert np.array_equal(P, P0)
+
+
+def test_compute_face_on_lower_edge_rejected(built):
+    d = domain("coast")
+    d.arrays["ComputeFacesU3D"][2, 1, 3] = 1               # U face at j = JLB (k=2, i=3)
+    P = d.tracer(4, 1.0, 0.0, seed=1)
+    assert O.step(d, P, O.params(DTProp=30.0)) == 1
