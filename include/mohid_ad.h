@@ -230,6 +230,58 @@ void* mohid_ad_stream(const int* id);
 int mohid_ad_kill(int* id, int* stat);
 
 /* ======================================================================== */
+/* Batched FP32 form: many tracers of one property group per call            */
+/* ======================================================================== */
+
+/*
+ * A batch transports `ntracers` properties that share the grid, the
+ * hydrodynamics and the option set of plain instance `id` (one MOHID property
+ * group: Advection_Diffusion_Processes calls AdvectionDiffusion once per
+ * property with the same fluxes, volumes and masks, WP:14603-14824).  Tracers
+ * stay on the device in FP32 ping-pong buffers; arithmetic is FP32 except the
+ * volume difference V - Vold (FP64) and the mass budget (FP64, compensated).
+ *   storage: 0 = FP32 transports and diffusivities,
+ *            1 = FP16 transports with a per-field scale,
+ *            2 = FP16 transports and diffusivities with per-field scales.
+ * Supported options: AdvMethodH UpwindOrder1 or P2_TVD (any limiter),
+ * implicit upwind vertical advection, implicit vertical diffusion,
+ * Docycle_method 1, closed or MassConservation open boundaries.  Other
+ * options return MOHID_AD_ERR_UNSUPPORTED (use the plain form).
+ */
+int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat);
+
+/* Repack the plain instance's current hydrodynamics (mohid_ad_set_hydro[_dev])
+ * into the batched layout.  mohid_ad_batched_step does this itself when the
+ * hydrodynamics changed since the last pack. */
+int mohid_ad_batched_pack_hydro(const int* bid, int* stat);
+
+/* Load / read tracer t (0-based) from / to a Fortran-layout double array over
+ * the Size box, on the host (*on_device == 0) or on the device. */
+int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP, const int* on_device, int* stat);
+int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, const int* on_device, int* stat);
+
+/* Exterior (reference) concentration of tracer t for open boundaries
+ * (ReferenceProp of AdvectionDiffusion); once set for any tracer, every
+ * tracer of the batch uses open boundaries and must have one. */
+int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
+                                   const int* on_device, int* stat);
+
+/* Advance every tracer *nsteps steps with options *p, asynchronously on the
+ * plain instance's stream.  *use_graph != 0 captures the step loop in a CUDA
+ * graph (re-used while nsteps, the options and the buffer parity match). */
+int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
+                          int* stat);
+
+/* Global mass budget of tracer t: Neumaier-compensated FP64 sum of
+ * VolumeZ * PROP over water cells (synchronous). */
+int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat);
+
+/* Wait for the batch's stream and report latched device errors. */
+int mohid_ad_batched_sync(const int* bid, int* stat);
+
+int mohid_ad_batched_destroy(int* bid, int* stat);
+
+/* ======================================================================== */
 /* Stand-alone THOMASZ (replaces SolveThomas_C with dim = 2 = Z)             */
 /* ======================================================================== */
 

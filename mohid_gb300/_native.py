@@ -88,6 +88,15 @@ _AD_SIGS = {
     "mohid_ad_kill": (C.c_int, [c_int_p, c_int_p]),
     "mohid_thomasz_f64": (C.c_int, [c_int_p] * 6 + [C.POINTER(T_Size3D)] + [c_double_p] * 5 +
                           [c_int_p, c_int_p]),
+    "mohid_ad_batched_create": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_pack_hydro": (C.c_int, [c_int_p, c_int_p]),
+    "mohid_ad_batched_set_tracer": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_get_tracer": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_set_reference": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_step": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_mass": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
+    "mohid_ad_batched_sync": (C.c_int, [c_int_p, c_int_p]),
+    "mohid_ad_batched_destroy": (C.c_int, [c_int_p, c_int_p]),
 }
 
 _SYN_SIGS = {

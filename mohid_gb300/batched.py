@@ -1,0 +1,99 @@
+"""Host mirror of the batched FP32 form (mohid_ad_batched_* in include/mohid_ad.h).
+
+One Batch transports the tracers of one MOHID property group -- properties
+that Advection_Diffusion_Processes would pass to AdvectionDiffusion one by one
+with the same hydrodynamics and options (ModuleWaterProperties.F90:14603-14824)
+-- in a single device-resident call per step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .advdiff import AdvectionDiffusion
+
+FP32, FP16_Q, FP16_QK = 0, 1, 2
+
+
+class Batch:
+    def __init__(self, ad: AdvectionDiffusion, ntracers: int, storage: int = FP32):
+        self.ad = ad
+        self.lib = N.ad_lib()
+        self.nt = ntracers
+        self.storage = storage
+        self._bid = C.c_int(0)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_create(C.byref(self._bid), C.byref(ad._id),
+                                              C.byref(C.c_int(ntracers)), C.byref(C.c_int(storage)),
+                                              C.byref(st))
+        N.check(rc, "mohid_ad_batched_create")
+
+    def pack_hydro(self):
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_pack_hydro(C.byref(self._bid), C.byref(st)),
+                "mohid_ad_batched_pack_hydro")
+
+    def set_tracer(self, t: int, P):
+        """P: float64 Size-box numpy array (host) or torch CUDA tensor (device)."""
+        dev, p = self._addr(P)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_set_tracer(C.byref(self._bid), C.byref(C.c_int(t)), p,
+                                                  C.byref(C.c_int(dev)), C.byref(st))
+        N.check(rc, "mohid_ad_batched_set_tracer")
+
+    def get_tracer(self, t: int, out=None):
+        if out is None:
+            out = np.zeros(self.ad.domain.shape3, dtype=np.float64)
+        dev, p = self._addr(out)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_get_tracer(C.byref(self._bid), C.byref(C.c_int(t)), p,
+                                                  C.byref(C.c_int(dev)), C.byref(st))
+        N.check(rc, "mohid_ad_batched_get_tracer")
+        return out
+
+    def set_reference(self, t: int, R):
+        dev, p = self._addr(R)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_set_reference(C.byref(self._bid), C.byref(C.c_int(t)), p,
+                                                     C.byref(C.c_int(dev)), C.byref(st))
+        N.check(rc, "mohid_ad_batched_set_reference")
+
+    def step(self, p: N.MohidAdParams, nsteps: int = 1, graph: bool = False):
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_step(C.byref(self._bid), C.byref(p), C.byref(C.c_int(nsteps)),
+                                            C.byref(C.c_int(int(graph))), C.byref(st))
+        N.check(rc, "mohid_ad_batched_step")
+
+    def mass(self, t: int) -> float:
+        m = C.c_double(0.0)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_mass(C.byref(self._bid), C.byref(C.c_int(t)), C.byref(m),
+                                            C.byref(st))
+        N.check(rc, "mohid_ad_batched_mass")
+        return m.value
+
+    def sync(self):
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_sync(C.byref(self._bid), C.byref(st)), "mohid_ad_batched_sync")
+
+    def destroy(self):
+        if self._bid.value:
+            st = C.c_int(0)
+            N.check(self.lib.mohid_ad_batched_destroy(C.byref(self._bid), C.byref(st)),
+                    "mohid_ad_batched_destroy")
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _addr(a):
+        if isinstance(a, np.ndarray):
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("expected a C-contiguous float64 array")
+            return 0, C.c_void_p(a.ctypes.data)
+        return 1, C.c_void_p(a.data_ptr())          # torch CUDA tensor

@@ -25,7 +25,9 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra nvcc flags)
 CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
+    ("batched_f32.cu", []),
     ("abi.cpp", []),
+    ("batched_abi.cpp", []),
 ]
 
 
@@ -53,7 +55,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     LIB.mkdir(exist_ok=True)
     OBJ.mkdir(exist_ok=True)
     nvcc = _nvcc()
-    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "mohid_ad.h"]
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(CSRC.glob("*.hpp")) + [PKG.parent / "include" / "mohid_ad.h"]
     common = [nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
               "-I", str(PKG.parent / "include")]
     jobs = []

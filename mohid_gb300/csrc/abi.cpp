@@ -20,8 +20,9 @@
 
 #include "../../include/mohid_ad.h"
 #include "common.cuh"
+#include "instance.hpp"
 
-namespace {
+namespace mohid_abi {
 
 thread_local std::string g_last_error = "";
 
@@ -38,53 +39,19 @@ int ok(int* stat)
     return MOHID_AD_SUCCESS;
 }
 
-template <class T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t alloc(size_t count)
-    {
-        n = count;
-        return cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-    }
-};
-
-struct Instance {
-    int device = 0;
-    int ni = 0, nj = 0, nk = 0;
-    size_t n2 = 0, n3 = 0;
-    cudaStream_t stream = nullptr;
-    // static 2-D metrics
-    DevBuf<double> DUX, DVY, DZX, DZY;
-    DevBuf<int> KFloor, BP2D;
-    // per-step hydrodynamics
-    DevBuf<double> Qx, Qy, Qz, Vold, V, ViscH, DiffV, AreaU, AreaV, DZZ, DWZ;
-    DevBuf<int> OP, LP, WP, CFU, CFV, CFW, SD;
-    bool hydro = false, hasSD = false;
-    // per-property staging for the host-pointer entry points
-    DevBuf<double> Pin, Pout, Ref;
-    DevBuf<unsigned int> status;
-    unsigned int* hstatus = nullptr;   // pinned
-
-    void release()
-    {
-        DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
-                               &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref};
-        for (auto* b : d) b->release();
-        DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD};
-        for (auto* b : i) b->release();
-        status.release();
-        if (hstatus) cudaFreeHost(hstatus);
-        hstatus = nullptr;
-        if (stream) cudaStreamDestroy(stream);
-        stream = nullptr;
-    }
-};
+void Instance::release()
+{
+    DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
+                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref};
+    for (auto* b : d) b->release();
+    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD};
+    for (auto* b : i) b->release();
+    status.release();
+    if (hstatus) cudaFreeHost(hstatus);
+    hstatus = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+}
 
 std::mutex g_mu;
 std::map<int, Instance*> g_inst;
@@ -103,11 +70,6 @@ std::string cuda_msg(const char* what, cudaError_t e)
     return std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
 }
 
-#define CK(call)                                                                  \
-    do {                                                                          \
-        cudaError_t e_ = (call);                                                  \
-        if (e_ != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg(#call, e_)); \
-    } while (0)
 
 // Option checks of AdvectionDiffusion (AD:1231-1239, AD:1340-1349,
 // Set_Internal_State AD:5816-5830) plus the options this build leaves out.
@@ -221,11 +183,14 @@ int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const dou
     std::string why;
     int code = status_to_code(*in->hstatus, why);
     in->hydro = code == MOHID_AD_SUCCESS;
+    ++in->hydroVersion;
     if (code) return fail(code, stat, why);
     return ok(stat);
 }
 
-}  // namespace
+}  // namespace mohid_abi
+
+using namespace mohid_abi;
 
 extern "C" {
 

@@ -1,0 +1,101 @@
+// batched.cuh -- layout and arguments of the batched FP32 multi-tracer form.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mohid {
+
+// Batched layout of one domain: x = i + kXOff (i = -2..ni+2), y = j + kYOff
+// (j = -2..nj+2), z = k (k = 0..nk+1).  kXOff puts the first interior cell of
+// every 32-wide tile on a 128-byte boundary.
+constexpr int kXOff = 31;
+constexpr int kYOff = 2;
+constexpr int kTX = 32;   // tile width along i (one warp)
+constexpr int kTY = 8;    // tile height along j (warps per CTA)
+
+// cell flag bits
+constexpr uint8_t F_WP = 1, F_OP = 2, F_CFU = 4, F_CFV = 8, F_CFW = 16, F_LP = 32;
+// column flag bits
+constexpr uint8_t C_SOLVE = 1, C_OPTOP = 2, C_CFWTOP = 4, C_BP = 8, C_SD = 16;
+
+struct BLayout {
+    int ni, nj, nk;
+    int px, py;            // pitches in elements
+    long long sl;          // layer stride px * py
+    long long n3;          // px * py * (nk + 2)
+    long long n2;          // px * py
+    __host__ __device__ long long at(int i, int j, int k) const
+    {
+        return (long long)(i + kXOff) + (long long)px * ((long long)(j + kYOff) + (long long)py * k);
+    }
+    __host__ __device__ long long at2(int i, int j) const
+    {
+        return (long long)(i + kXOff) + (long long)px * (long long)(j + kYOff);
+    }
+};
+
+inline BLayout make_layout(int ni, int nj, int nk)
+{
+    BLayout L;
+    L.ni = ni; L.nj = nj; L.nk = nk;
+    L.px = ((ni + kXOff + 3 + kTX + 31) / 32) * 32;
+    L.py = nj + kYOff + 3 + kTY;
+    L.n2 = (long long)L.px * L.py;
+    L.sl = L.n2;
+    L.n3 = L.n2 * (nk + 2);
+    return L;
+}
+
+struct BatchArgs {
+    BLayout L;
+    // shared per-cell fields in the batched layout
+    const void *Qx, *Qy, *Qz;           // float or __half (west, south, bottom faces)
+    float qsx, qsy, qsz;                // scales for __half storage
+    const double *V, *Vold;
+    const void *ViscH, *DiffV;          // float or __half
+    float ksh, ksv;                     // scales for __half storage
+    const float *AreaU, *AreaV, *DZZ;
+    const uint8_t* flag;
+    // 2-D: per-face constants [6][py][px] for west (fx) and south (fy) faces:
+    //   0: weight of the cell's own Visc, 1: weight of the neighbour's Visc
+    //   2: 1/DZ between the two centres, 3: g_upup (Q > 0), 4: g_dn, 5: g_upup (Q <= 0)
+    const float *fx, *fy;
+    const float* areaCol;               // DUX * DVY
+    const int* kfloor;
+    const uint8_t* cflag;
+    // tracers: contiguous, stride `ts` elements
+    const float* Pin;
+    float* Pout;
+    long long ts;
+    int nt;
+    const float* Ref;                   // same layout as tracers (boundary cells read), or null
+    // scalars
+    float DT, schmidtH, coefV, backV, tdec;
+    int nullDif, vertical1D, xzflow;
+    unsigned* status;
+};
+
+cudaError_t launch_batched(const BatchArgs& a, int method, int limiter, bool halfQ, bool halfK,
+                           cudaStream_t s);
+
+// packing (Fortran FP64 Size box <-> batched layout)
+cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nzSrc, cudaStream_t s);
+cudaError_t pack_f64_to_f16(const double* src, __half* dst, float invScale, const BLayout& L, cudaStream_t s);
+cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s);
+cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,
+                       const int* LP, uint8_t* dst, const BLayout& L, cudaStream_t s);
+cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
+                         const int* KFloor, const int* BP2D, const int* WP, const int* OP,
+                         const int* CFW, const int* SD, float* fx, float* fy, float* areaCol,
+                         int* kfloor, uint8_t* cflag, const BLayout& L, cudaStream_t s);
+cudaError_t pack_tracer(const double* src, float* dstA, float* dstB, const int* KFloor,
+                        const int* WP, const BLayout& L, cudaStream_t s);
+cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
+                          const int* KFloor, const BLayout& L, cudaStream_t s);
+cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);
+cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, const BLayout& L,
+                         double* partial, int nblocks, cudaStream_t s);
+cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s);
+
+}  // namespace mohid

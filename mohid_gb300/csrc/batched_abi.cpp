@@ -1,0 +1,446 @@
+// batched_abi.cpp -- C-ABI of the batched FP32 multi-tracer form (include/mohid_ad.h).
+//
+// A batch shares the grid and hydrodynamics of a plain instance (the same
+// arguments AdvectionDiffusion receives per property) and transports `nt`
+// tracers per call, device-resident, with one option set for all of them
+// (one MOHID property group).  The hydrodynamics are repacked on the device
+// into the batched layout (FP32 or scaled FP16 transports, FP64 volumes,
+// 1-byte masks); tracers are held in FP32 ping-pong buffers.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mohid_ad.h"
+#include "batched.cuh"
+#include "instance.hpp"
+
+namespace mohid_abi {
+namespace {
+
+struct Batch {
+    int plain = 0;
+    Instance* in = nullptr;
+    int nt = 0;
+    int storage = 0;                     // 0 FP32, 1 FP16 transports, 2 FP16 transports + diffusivities
+    mohid::BLayout L{};
+    DevBuf<float> Qx32, Qy32, Qz32, Vis32, Dif32;
+    DevBuf<__half> Qx16, Qy16, Qz16, Vis16, Dif16;
+    float qsx = 1, qsy = 1, qsz = 1, ksh = 1, ksv = 1;
+    DevBuf<double> V, Vold;
+    DevBuf<float> AreaU, AreaV, DZZ;
+    DevBuf<uint8_t> flag, cflag;
+    DevBuf<float> fx, fy, areaCol;
+    DevBuf<int> kfloor;
+    DevBuf<float> PA, PB, Ref;
+    bool hasRef = false;
+    bool cur = false;                    // false: PA holds the current state
+    bool packed = false;
+    unsigned packedVersion = ~0u;
+    DevBuf<double> partial, scratch, stage;
+    double* hmass = nullptr;             // pinned
+    cudaGraphExec_t graph = nullptr;
+    int graphSteps = 0;
+    bool graphCur = false;
+    mohid_ad_params graphParams{};
+
+    void release()
+    {
+        DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ, &fx, &fy,
+                              &areaCol, &PA, &PB, &Ref};
+        for (auto* b : f) b->release();
+        DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
+        for (auto* b : h) b->release();
+        V.release(); Vold.release(); flag.release(); cflag.release(); kfloor.release();
+        partial.release(); scratch.release(); stage.release();
+        if (hmass) cudaFreeHost(hmass);
+        hmass = nullptr;
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    float* cur_in() { return cur ? PB.p : PA.p; }
+    float* cur_out() { return cur ? PA.p : PB.p; }
+};
+
+std::mutex g_bmu;
+std::map<int, Batch*> g_batch;
+int g_next_bid = 1;
+constexpr int kMassBlocks = 1024;
+
+Batch* blookup(const int* bid)
+{
+    if (!bid) return nullptr;
+    std::lock_guard<std::mutex> lk(g_bmu);
+    auto it = g_batch.find(*bid);
+    return it == g_batch.end() ? nullptr : it->second;
+}
+
+int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why)
+{
+    if (!p) { why = "params is NULL"; return MOHID_AD_ERR_NULLPTR; }
+    if (!(p->DTProp > 0.0) || !std::isfinite(p->DTProp)) { why = "DTProp must be > 0"; return MOHID_AD_ERR_OPTION; }
+    if (p->AdvMethodH != MOHID_UPWIND_ORDER1 && p->AdvMethodH != MOHID_P2_TVD) {
+        why = "batched form: AdvMethodH must be UpwindOrder1 or P2_TVD (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
+    }
+    if (p->AdvMethodH == MOHID_P2_TVD && !p->Upwind2H) { why = "P2_TVD needs Upwind2H near boundaries"; return MOHID_AD_ERR_OPTION; }
+    if (p->AdvMethodH == MOHID_P2_TVD && (p->TVDLimitationH < 1 || p->TVDLimitationH > 5)) { why = "TVDLimitationH must be 1..5"; return MOHID_AD_ERR_OPTION; }
+    if (p->AdvMethodV != MOHID_UPWIND_ORDER1 || p->ImpExp_AdvV != 1.0) {
+        why = "batched form: vertical advection must be implicit UpwindOrder1"; return MOHID_AD_ERR_UNSUPPORTED;
+    }
+    if (p->ImpExp_DifV != 1.0) { why = "batched form: vertical diffusion must be implicit"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->ImpExp_DifH != 0.0) { why = "horizontal diffusion must be explicit (reference ERR02)"; return MOHID_AD_ERR_OPTION; }
+    if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->Docycle_method != 1) { why = "batched form follows Docycle_method 1"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (hasRef && p->BoundaryCondition != MOHID_BC_MASS_CONSERVATION) {
+        why = "batched form: only MassConservation open boundaries"; return MOHID_AD_ERR_UNSUPPORTED;
+    }
+    return MOHID_AD_SUCCESS;
+}
+
+int pack_hydro(Batch* b, int* stat)
+{
+    Instance* in = b->in;
+    if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "the plain instance has no hydrodynamics set");
+    cudaStream_t s = in->stream;
+    const mohid::BLayout& L = b->L;
+    auto scale = [&](const double* src, float* sc) -> cudaError_t {
+        cudaError_t e = mohid::absmax_f64(src, (long long)in->n3, b->scratch.p, s);
+        if (e != cudaSuccess) return e;
+        double m = 0;
+        e = cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(s);
+        m = *b->hmass;
+        // map the largest magnitude to 2^14 so that FP16 keeps 11 significant bits
+        *sc = m > 0 ? (float)(m / 16384.0) : 1.0f;
+        return e;
+    };
+    if (b->storage >= 1) {
+        CK(scale(in->Qx.p, &b->qsx)); CK(scale(in->Qy.p, &b->qsy)); CK(scale(in->Qz.p, &b->qsz));
+        CK(mohid::pack_f64_to_f16(in->Qx.p, b->Qx16.p, 1.0f / b->qsx, L, s));
+        CK(mohid::pack_f64_to_f16(in->Qy.p, b->Qy16.p, 1.0f / b->qsy, L, s));
+        CK(mohid::pack_f64_to_f16(in->Qz.p, b->Qz16.p, 1.0f / b->qsz, L, s));
+    } else {
+        CK(mohid::pack_f64_to_f32(in->Qx.p, b->Qx32.p, L, in->nk + 2, s));
+        CK(mohid::pack_f64_to_f32(in->Qy.p, b->Qy32.p, L, in->nk + 2, s));
+        CK(mohid::pack_f64_to_f32(in->Qz.p, b->Qz32.p, L, in->nk + 2, s));
+    }
+    if (b->storage >= 2) {
+        CK(scale(in->ViscH.p, &b->ksh)); CK(scale(in->DiffV.p, &b->ksv));
+        CK(mohid::pack_f64_to_f16(in->ViscH.p, b->Vis16.p, 1.0f / b->ksh, L, s));
+        CK(mohid::pack_f64_to_f16(in->DiffV.p, b->Dif16.p, 1.0f / b->ksv, L, s));
+    } else {
+        CK(mohid::pack_f64_to_f32(in->ViscH.p, b->Vis32.p, L, in->nk + 2, s));
+        CK(mohid::pack_f64_to_f32(in->DiffV.p, b->Dif32.p, L, in->nk + 2, s));
+    }
+    CK(mohid::pack_f64_to_f64(in->V.p, b->V.p, L, s));
+    CK(mohid::pack_f64_to_f64(in->Vold.p, b->Vold.p, L, s));
+    CK(mohid::pack_f64_to_f32(in->AreaU.p, b->AreaU.p, L, in->nk + 2, s));
+    CK(mohid::pack_f64_to_f32(in->AreaV.p, b->AreaV.p, L, in->nk + 2, s));
+    CK(mohid::pack_f64_to_f32(in->DZZ.p, b->DZZ.p, L, in->nk + 2, s));
+    CK(mohid::pack_flags(in->WP.p, in->OP.p, in->CFU.p, in->CFV.p, in->CFW.p, in->LP.p, b->flag.p, L, s));
+    CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
+                           in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
+                           b->fx.p, b->fy.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
+    CK(cudaStreamSynchronize(s));
+    b->packed = true;
+    b->packedVersion = in->hydroVersion;
+    return ok(stat);
+}
+
+mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout)
+{
+    Instance* in = b->in;
+    mohid::BatchArgs a{};
+    a.L = b->L;
+    const bool hq = b->storage >= 1, hk = b->storage >= 2;
+    a.Qx = hq ? (const void*)b->Qx16.p : (const void*)b->Qx32.p;
+    a.Qy = hq ? (const void*)b->Qy16.p : (const void*)b->Qy32.p;
+    a.Qz = hq ? (const void*)b->Qz16.p : (const void*)b->Qz32.p;
+    a.qsx = b->qsx; a.qsy = b->qsy; a.qsz = b->qsz;
+    a.V = b->V.p; a.Vold = b->Vold.p;
+    a.ViscH = hk ? (const void*)b->Vis16.p : (const void*)b->Vis32.p;
+    a.DiffV = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
+    a.ksh = b->ksh; a.ksv = b->ksv;
+    a.AreaU = b->AreaU.p; a.AreaV = b->AreaV.p; a.DZZ = b->DZZ.p;
+    a.flag = b->flag.p;
+    a.fx = b->fx.p; a.fy = b->fy.p; a.areaCol = b->areaCol.p; a.kfloor = b->kfloor.p; a.cflag = b->cflag.p;
+    a.ts = b->L.n3;
+    a.Pin = Pin + (long long)t0 * a.ts;
+    a.Pout = Pout + (long long)t0 * a.ts;
+    a.nt = nt;
+    a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
+    a.DT = (float)p->DTProp;
+    a.schmidtH = (float)p->schmidt_H;
+    a.coefV = (float)p->SchmidtCoef_V;
+    a.backV = (float)p->SchmidtBackground_V;
+    a.tdec = (float)(1.0 / (1.0 + p->DecayTime / p->DTProp));
+    a.nullDif = p->NullDif != 0;
+    a.vertical1D = p->Vertical1D != 0;
+    a.xzflow = p->XZFlow != 0;
+    a.status = in->status.p;
+    return a;
+}
+
+// one transport step of every tracer: groups of 4, 2, 1 tracers per launch
+cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s)
+{
+    const float* Pin = b->cur_in();
+    float* Pout = b->cur_out();
+    int t0 = 0;
+    while (t0 < b->nt) {
+        const int left = b->nt - t0;
+        const int g = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
+        mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout);
+        cudaError_t e = mohid::launch_batched(a, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
+                                              b->storage >= 2, s);
+        if (e != cudaSuccess) return e;
+        t0 += g;
+    }
+    b->cur = !b->cur;
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace mohid_abi
+
+using namespace mohid_abi;
+
+extern "C" {
+
+int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat)
+{
+    if (!bid || !ntracers || !storage) return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_ad_batched_create: NULL argument");
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown plain instance id");
+    if (*ntracers < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "ntracers must be >= 1");
+    if (*storage < 0 || *storage > 2) return fail(MOHID_AD_ERR_OPTION, stat, "storage must be 0, 1 or 2");
+    if (in->nk > 200) return fail(MOHID_AD_ERR_UNSUPPORTED, stat, "KUB > 200 layers not supported");
+    CK(cudaSetDevice(in->device));
+    Batch* b = new Batch();
+    b->plain = *id;
+    b->in = in;
+    b->nt = *ntracers;
+    b->storage = *storage;
+    b->L = mohid::make_layout(in->ni, in->nj, in->nk);
+    const size_t n3 = (size_t)b->L.n3, n2 = (size_t)b->L.n2;
+    auto bad = [&](cudaError_t e, const char* what) {
+        std::string m = cuda_msg(what, e);
+        b->release();
+        delete b;
+        return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat, m);
+    };
+    cudaError_t e;
+    if (b->storage >= 1) {
+        DevBuf<__half>* h[] = {&b->Qx16, &b->Qy16, &b->Qz16};
+        for (auto* x : h) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    } else {
+        DevBuf<float>* f[] = {&b->Qx32, &b->Qy32, &b->Qz32};
+        for (auto* x : f) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    }
+    if (b->storage >= 2) {
+        DevBuf<__half>* h[] = {&b->Vis16, &b->Dif16};
+        for (auto* x : h) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    } else {
+        DevBuf<float>* f[] = {&b->Vis32, &b->Dif32};
+        for (auto* x : f) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    }
+    DevBuf<float>* f3[] = {&b->AreaU, &b->AreaV, &b->DZZ};
+    for (auto* x : f3) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->V.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->Vold.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->flag.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->cflag.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->fx.alloc(6 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->fy.alloc(6 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->areaCol.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->kfloor.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->PA.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->PB.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaMallocHost((void**)&b->hmass, 4 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMallocHost");
+    {
+        std::lock_guard<std::mutex> lk(g_bmu);
+        *bid = g_next_bid++;
+        g_batch[*bid] = b;
+    }
+    return ok(stat);
+}
+
+int mohid_ad_batched_pack_hydro(const int* bid, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    CK(cudaSetDevice(b->in->device));
+    return pack_hydro(b, stat);
+}
+
+int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP, const int* on_device, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    cudaStream_t s = in->stream;
+    const double* src = PROP;
+    if (!*on_device) {
+        CK(cudaMemcpyAsync(b->stage.p, PROP, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
+        src = b->stage.p;
+    }
+    const long long off = (long long)*t * b->L.n3;
+    CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, b->L, s));
+    if (!*on_device) CK(cudaStreamSynchronize(s));
+    return ok(stat);
+}
+
+int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, const int* on_device, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    cudaStream_t s = in->stream;
+    const long long off = (long long)*t * b->L.n3;
+    double* dst = *on_device ? PROP : b->stage.p;
+    CK(mohid::unpack_tracer(b->cur_in() + off, dst, nullptr, in->WP.p, in->KFloor.p, b->L, s));
+    if (!*on_device) {
+        CK(cudaMemcpyAsync(PROP, b->stage.p, sizeof(double) * in->n3, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return ok(stat);
+}
+
+int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
+                                   const int* on_device, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !ReferenceProp || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    if (!b->Ref.p) {
+        cudaError_t e = b->Ref.alloc((size_t)b->L.n3 * b->nt);
+        if (e != cudaSuccess) return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
+    }
+    cudaStream_t s = in->stream;
+    const double* src = ReferenceProp;
+    if (!*on_device) {
+        CK(cudaMemcpyAsync(b->stage.p, ReferenceProp, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
+        src = b->stage.p;
+    }
+    CK(mohid::pack_f64_to_f32(src, b->Ref.p + (long long)*t * b->L.n3, b->L, in->nk + 2, s));
+    CK(cudaStreamSynchronize(s));
+    b->hasRef = true;
+    return ok(stat);
+}
+
+int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
+                          int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!nsteps || !use_graph) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    std::string why;
+    int code = check_batched_params(p, b->hasRef, why);
+    if (code) return fail(code, stat, why);
+    if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
+    Instance* in = b->in;
+    if (!b->packed || b->packedVersion != in->hydroVersion) {
+        int c = pack_hydro(b, stat);
+        if (c) return c;
+    }
+    CK(cudaSetDevice(in->device));
+    cudaStream_t s = in->stream;
+    if (!*use_graph) {
+        for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s));
+        return ok(stat);
+    }
+    // CUDA graph of an even number of steps: the ping-pong returns to the
+    // buffer it started from, so the graph stays valid for that parity; an
+    // odd remainder step is launched directly.
+    const int pairs = *nsteps / 2;
+    if (pairs > 0) {
+        const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
+                           std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
+        if (!reuse) {
+            if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+            const bool cur0 = b->cur;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            for (int n = 0; n < 2 * pairs && e == cudaSuccess; ++n) e = enqueue_step(b, p, s);
+            cudaError_t e2 = cudaStreamEndCapture(s, &g);
+            b->cur = cur0;
+            if (e != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("capture", e));
+            if (e2 != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaStreamEndCapture", e2));
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { b->graph = nullptr; return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaGraphInstantiate", e)); }
+            b->graphSteps = 2 * pairs;
+            b->graphCur = cur0;
+            b->graphParams = *p;
+        }
+        CK(cudaGraphLaunch(b->graph, s));
+    }
+    if (*nsteps % 2) CK(enqueue_step(b, p, s));
+    return ok(stat);
+}
+
+int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !mass) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    if (!b->packed) return fail(MOHID_AD_ERR_OPTION, stat, "hydrodynamics not packed yet");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    cudaStream_t s = in->stream;
+    const float* P = b->cur_in() + (long long)*t * b->L.n3;
+    CK(mohid::mass_batched(P, b->V.p, b->flag.p, b->L, b->partial.p, kMassBlocks, s));
+    CK(mohid::mass_finish(b->partial.p, kMassBlocks, b->scratch.p, s));
+    CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *mass = *b->hmass;
+    return ok(stat);
+}
+
+int mohid_ad_batched_sync(const int* bid, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    return mohid_ad_sync(&b->plain, stat);
+}
+
+int mohid_ad_batched_destroy(int* bid, int* stat)
+{
+    Batch* b = nullptr;
+    if (bid) {
+        std::lock_guard<std::mutex> lk(g_bmu);
+        auto it = g_batch.find(*bid);
+        if (it != g_batch.end()) { b = it->second; g_batch.erase(it); }
+    }
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    cudaSetDevice(b->in->device);
+    cudaStreamSynchronize(b->in->stream);
+    b->release();
+    delete b;
+    *bid = 0;
+    return ok(stat);
+}
+
+}  // extern "C"

@@ -1,0 +1,67 @@
+// instance.hpp -- internal state shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "../../include/mohid_ad.h"
+#include "common.cuh"
+
+namespace mohid_abi {
+
+int fail(int code, int* stat, const std::string& msg);
+int ok(int* stat);
+std::string cuda_msg(const char* what, cudaError_t e);
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        n = count;
+        cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
+        if (e == cudaSuccess) e = cudaMemset(p, 0, sizeof(T) * (count ? count : 1));
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+struct Instance {
+    int device = 0;
+    int ni = 0, nj = 0, nk = 0;
+    size_t n2 = 0, n3 = 0;
+    cudaStream_t stream = nullptr;
+    // static 2-D metrics
+    DevBuf<double> DUX, DVY, DZX, DZY;
+    DevBuf<int> KFloor, BP2D;
+    // per-step hydrodynamics
+    DevBuf<double> Qx, Qy, Qz, Vold, V, ViscH, DiffV, AreaU, AreaV, DZZ, DWZ;
+    DevBuf<int> OP, LP, WP, CFU, CFV, CFW, SD;
+    bool hydro = false, hasSD = false;
+    unsigned hydroVersion = 0;
+    // per-property staging for the host-pointer entry points
+    DevBuf<double> Pin, Pout, Ref;
+    DevBuf<unsigned int> status;
+    unsigned int* hstatus = nullptr;   // pinned
+
+    void release();
+};
+
+Instance* lookup(const int* id);
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) return ::mohid_abi::fail(MOHID_AD_ERR_CUDA, stat, ::mohid_abi::cuda_msg(#call, e_)); \
+    } while (0)
+
+int status_to_code(unsigned int s, std::string& why);
+
+}  // namespace mohid_abi

@@ -1,0 +1,161 @@
+"""Batched FP32 multi-tracer form on the GPU against the FP64 oracle.
+
+Tolerance (FP32 arithmetic, FP64 volume difference): relative L2 over water
+cells <= 1e-5 after the stated number of steps; a single step is expected to
+agree to ~1e-6.  With FP16-stored transports the oracle is run on the same
+FP16-rounded transports, so the bar measures the arithmetic alone.
+"""
+import numpy as np
+import pytest
+
+from mohid_gb300 import advdiff, batched, configs, synth
+from oracle import oracle as O
+from tests.cases import domain
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+BATCH_OPTIONS = {
+    "upwind1": dict(),
+    "tvd_superbee": dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+    "tvd_minmod": dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1),
+    "tvd_vanleer": dict(AdvMethodH=4, TVDLimitationH=2, Upwind2H=1),
+    "tvd_muscl": dict(AdvMethodH=4, TVDLimitationH=3, Upwind2H=1),
+    "tvd_pdm": dict(AdvMethodH=4, TVDLimitationH=5, Upwind2H=1),
+    "nulldif": dict(NullDif=1),
+    "xzflow": dict(XZFlow=1),
+    "vertical1d": dict(Vertical1D=1),
+    "background": dict(SchmidtBackground_V=1e-3, schmidt_H=0.7, SchmidtCoef_V=2.0),
+}
+
+
+def rel_l2(d, a, b):
+    wp = d.water_mask()
+    return float(np.linalg.norm(a[wp] - b[wp]) / np.linalg.norm(b[wp]))
+
+
+def run_pair(d, tracers, pd, steps, storage=batched.FP32, refs=None, graph=False):
+    """(oracle results, batched results) after `steps` steps."""
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, len(tracers), storage)
+    for t, P in enumerate(tracers):
+        b.set_tracer(t, P)
+        if refs is not None:
+            b.set_reference(t, refs[t])
+    b.step(advdiff.params(**pd), nsteps=steps, graph=graph)
+    b.sync()
+    got = [b.get_tracer(t) for t in range(len(tracers))]
+    b.destroy()
+    ad.kill()
+    want = []
+    work = O.Work(d)
+    for t, P in enumerate(tracers):
+        Q = P.copy()
+        for _ in range(steps):
+            assert O.step(d, Q, O.params(**pd), ReferenceProp=None if refs is None else refs[t],
+                          work=work) == 0
+        want.append(Q)
+    return want, got
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "layer1", "column"])
+@pytest.mark.parametrize("opt", sorted(BATCH_OPTIONS))
+@pytest.mark.parametrize("nt", [1, 3])
+def test_batched_one_step(gpu, grid, opt, nt):
+    d = domain(grid)
+    tr = [d.tracer(3, 1.0 + t, 0.7, seed=9 + t) for t in range(nt)]
+    want, got = run_pair(d, tr, dict(DTProp=30.0, **BATCH_OPTIONS[opt]), 1)
+    wp = d.water_mask()
+    for w, g in zip(want, got):
+        assert rel_l2(d, g, w) <= 1e-6
+        # land, null and halo cells exactly as the reference leaves them
+        assert np.array_equal(g[~wp], w[~wp])
+
+
+@pytest.mark.parametrize("grid", ["open", "nsopen"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod", "tvd_superbee"])
+@pytest.mark.parametrize("decay", [0.0, 600.0])
+def test_batched_open_boundaries(gpu, grid, opt, decay):
+    d = domain(grid)
+    tr = [d.tracer(3, 1.0, 0.5, seed=1), d.tracer(1, 5.0, 20.0, seed=4)]
+    refs = [d.reference(2.0, 0.3, seed=2), d.reference(12.0, 0.2, seed=3)]
+    pd = dict(DTProp=30.0, BoundaryCondition=1, DecayTime=decay, **BATCH_OPTIONS[opt])
+    want, got = run_pair(d, tr, pd, 5, refs=refs)
+    for w, g in zip(want, got):
+        assert rel_l2(d, g, w) <= TOL
+
+
+def test_batched_cfg1_100_steps(gpu):
+    w = configs.cfg1()
+    d = synth.generate(w.spec)
+    tr = [d.tracer(*w.tracers[0], seed=11)]
+    want, got = run_pair(d, tr, w.params(), w.steps)
+    assert rel_l2(d, got[0], want[0]) <= TOL
+
+
+def test_batched_cfg2_grid_300_steps(gpu):
+    """Config 2 options (P2_TVD SuperBee, T and S) on a 128x128x40 cut, 300 steps."""
+    w = configs.cfg2().scaled(ni=128, nj=128)
+    d = synth.generate(w.spec)
+    tr = [d.tracer(k, a, b, seed=100 + t) for t, (k, a, b) in enumerate(w.tracers)]
+    want, got = run_pair(d, tr, w.params(), 300, graph=True)
+    for a_, b_ in zip(got, want):
+        assert rel_l2(d, a_, b_) <= TOL
+
+
+def test_batched_graph_equals_direct(gpu):
+    d = domain("coast")
+    tr = [d.tracer(3, 1.0, 0.7, seed=9), d.tracer(1, 3.0, 9.0, seed=2)]
+    pd = dict(DTProp=30.0, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1)
+    _, direct = run_pair(d, tr, pd, 7, graph=False)
+    _, graphed = run_pair(d, tr, pd, 7, graph=True)
+    for a_, b_ in zip(direct, graphed):
+        assert np.array_equal(a_, b_)
+
+
+@pytest.mark.parametrize("storage", [batched.FP16_Q, batched.FP16_QK])
+def test_batched_fp16_storage(gpu, storage):
+    """FP16-stored transports (and diffusivities): oracle on the same rounded inputs."""
+    import torch
+    w = configs.cfg3().scaled(ni=96, nj=64, nk=20)
+    d = synth.generate(w.spec)
+    a = d.arrays
+    names = ["Wflux_X", "Wflux_Y", "Wflux_Z"] + (["Visc_H", "Diff_V"] if storage == batched.FP16_QK else [])
+    for n in names:     # the same per-field scaling the library applies
+        m = float(np.abs(a[n]).max())
+        s = np.float32(m / 16384.0) if m > 0 else np.float32(1.0)
+        q = (a[n] * np.float64(np.float32(1.0) / s)).astype(np.float32).astype(np.float16)
+        a[n][...] = (s * q.astype(np.float32)).astype(np.float64)
+    tr = [d.tracer(k, a_, b_, seed=7 + t) for t, (k, a_, b_) in enumerate(w.tracers[:4])]
+    want, got = run_pair(d, tr, w.params(), 20, storage=storage)
+    for g_, w_ in zip(got, want):
+        assert rel_l2(d, g_, w_) <= TOL
+
+
+def test_batched_mass_budget_matches_oracle_sum(gpu):
+    d = domain("zlevel")
+    P = d.tracer(3, 2.0, 0.5, seed=5)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, P)
+    b.step(advdiff.params(DTProp=30.0), nsteps=3)
+    m = b.mass(0)
+    Pg = b.get_tracer(0)
+    b.destroy(); ad.kill()
+    assert abs(m - O.mass(d, Pg.astype(np.float32))) <= 1e-14 * abs(m)
+
+
+@pytest.mark.parametrize("bad", [dict(AdvMethodH=5), dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1),
+                                 dict(ImpExp_DifV=0.5), dict(Docycle_method=2), dict(ImpExp_AdvV=0.0)])
+def test_batched_rejects_unsupported(gpu, bad):
+    d = domain("coast")
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, d.tracer(4, 1.0, 0.0, seed=1))
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        b.step(advdiff.params(DTProp=30.0, **bad))
+    assert ei.value.code == 4
+    b.destroy(); ad.kill()
