@@ -89,13 +89,20 @@ cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
                          const int* CFW, const int* SD, float* fx, float* fy, float* areaCol,
                          int* kfloor, uint8_t* cflag, const BLayout& L, cudaStream_t s);
+// Tracers are held as the anomaly P - shift on water cells (shift: a per-tracer
+// constant, the mid-range of the field): the step is shift-equivariant, and the
+// FP32 rounding then scales with the anomaly rather than the absolute value.
 cudaError_t pack_tracer(const double* src, float* dstA, float* dstB, const int* KFloor,
-                        const int* WP, const BLayout& L, cudaStream_t s);
+                        const int* WP, double shift, const BLayout& L, cudaStream_t s);
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                          const int* KFloor, const BLayout& L, cudaStream_t s);
+                          const int* KFloor, double shift, const BLayout& L, cudaStream_t s);
+cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
+                           cudaStream_t s);
+cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys,
+                        cudaStream_t s);
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);
-cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, const BLayout& L,
-                         double* partial, int nblocks, cudaStream_t s);
+cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
+                         const BLayout& L, double* partial, int nblocks, cudaStream_t s);
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s);
 
 }  // namespace mohid

@@ -39,6 +39,9 @@ struct Batch {
     DevBuf<float> fx, fy, areaCol;
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
+    std::vector<double> shift;           // per tracer: water cells hold P - shift
+    std::vector<double> refShift;        // shift each stored reference was packed with
+    DevBuf<unsigned long long> keys;
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
     bool packed = false;
@@ -58,7 +61,7 @@ struct Batch {
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
         V.release(); Vold.release(); flag.release(); cflag.release(); kfloor.release();
-        partial.release(); scratch.release(); stage.release();
+        partial.release(); scratch.release(); stage.release(); keys.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -267,6 +270,8 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->keys.alloc(2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    b->shift.assign(b->nt, 0.0);
     if ((e = cudaMallocHost((void**)&b->hmass, 4 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMallocHost");
     {
         std::lock_guard<std::mutex> lk(g_bmu);
@@ -299,8 +304,25 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
         src = b->stage.p;
     }
     const long long off = (long long)*t * b->L.n3;
-    CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, b->L, s));
-    if (!*on_device) CK(cudaStreamSynchronize(s));
+    // shift = mid-range of the water cells (exactly representable in FP32)
+    unsigned long long kk[2];
+    CK(mohid::water_range(src, in->WP.p, (long long)in->n3, b->keys.p, s));
+    CK(cudaMemcpyAsync(kk, b->keys.p, sizeof(kk), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    double sh = 0.0;
+    if (kk[0] <= kk[1]) {
+        auto unkey = [](unsigned long long k) {
+            unsigned long long bits = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+            double x;
+            std::memcpy(&x, &bits, sizeof x);
+            return x;
+        };
+        const double lo = unkey(kk[0]), hi = unkey(kk[1]);
+        if (std::isfinite(lo) && std::isfinite(hi)) sh = (double)(float)(0.5 * (lo + hi));
+    }
+    b->shift[*t] = sh;
+    CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, sh, b->L, s));
+    CK(cudaStreamSynchronize(s));
     return ok(stat);
 }
 
@@ -315,7 +337,7 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
     cudaStream_t s = in->stream;
     const long long off = (long long)*t * b->L.n3;
     double* dst = *on_device ? PROP : b->stage.p;
-    CK(mohid::unpack_tracer(b->cur_in() + off, dst, nullptr, in->WP.p, in->KFloor.p, b->L, s));
+    CK(mohid::unpack_tracer(b->cur_in() + off, dst, nullptr, in->WP.p, in->KFloor.p, b->shift[*t], b->L, s));
     if (!*on_device) {
         CK(cudaMemcpyAsync(PROP, b->stage.p, sizeof(double) * in->n3, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -342,9 +364,11 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
         CK(cudaMemcpyAsync(b->stage.p, ReferenceProp, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
         src = b->stage.p;
     }
-    CK(mohid::pack_f64_to_f32(src, b->Ref.p + (long long)*t * b->L.n3, b->L, in->nk + 2, s));
+    CK(mohid::pack_shift_f32(src, b->Ref.p + (long long)*t * b->L.n3, in->WP.p, b->shift[*t], b->L, s));
     CK(cudaStreamSynchronize(s));
     b->hasRef = true;
+    b->refShift.resize(b->nt, 0.0);
+    b->refShift[*t] = b->shift[*t];
     return ok(stat);
 }
 
@@ -358,6 +382,11 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     int code = check_batched_params(p, b->hasRef, why);
     if (code) return fail(code, stat, why);
     if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
+    if (b->hasRef)
+        for (int t = 0; t < b->nt; ++t)
+            if (t >= (int)b->refShift.size() || b->refShift[t] != b->shift[t])
+                return fail(MOHID_AD_ERR_OPTION, stat,
+                            "set the reference of every tracer after (re)loading the tracer");
     Instance* in = b->in;
     if (!b->packed || b->packedVersion != in->hydroVersion) {
         int c = pack_hydro(b, stat);
@@ -411,7 +440,7 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     CK(cudaSetDevice(in->device));
     cudaStream_t s = in->stream;
     const float* P = b->cur_in() + (long long)*t * b->L.n3;
-    CK(mohid::mass_batched(P, b->V.p, b->flag.p, b->L, b->partial.p, kMassBlocks, s));
+    CK(mohid::mass_batched(P, b->V.p, b->flag.p, b->shift[*t], b->L, b->partial.p, kMassBlocks, s));
     CK(mohid::mass_finish(b->partial.p, kMassBlocks, b->scratch.p, s));
     CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

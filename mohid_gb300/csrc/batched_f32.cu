@@ -399,6 +399,43 @@ __global__ void k_pack_f16(const double* __restrict__ src, __half* __restrict__ 
     }
 }
 
+__global__ void k_pack_shift_f32(const double* __restrict__ src, float* __restrict__ dst,
+                                 const int* __restrict__ WP, double shift, BLayout L)
+{
+    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % (L.ni + 2));
+        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
+        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
+        dst[L.at(i, j, k)] = (float)(src[e] - (WP[e] == 1 ? shift : 0.0));
+    }
+}
+
+// min and max over water cells, as order-preserving 64-bit keys
+__device__ __forceinline__ unsigned long long dkey(double x)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_water_range(const double* src, const int* WP, long long n, unsigned long long* out)
+{
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        if (WP[e] == 1) {
+            const unsigned long long kx = dkey(src[e]);
+            lo = kx < lo ? kx : lo;
+            hi = kx > hi ? kx : hi;
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0) { atomicMin(out, lo); atomicMax(out + 1, hi); }
+}
+
 __global__ void k_pack_f64(const double* __restrict__ src, double* __restrict__ dst, BLayout L)
 {
     const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
@@ -487,7 +524,8 @@ __global__ void k_pack_cols(const double* DUX, const double* DVY, const double* 
 // tracer: Fortran FP64 -> batched FP32 in both ping-pong buffers; cells below
 // KFloor of solved columns hold null_real and row KUB+1 holds 0, which is what
 // one reference step leaves there.
-__global__ void k_pack_tracer(const double* src, float* A, float* B, const int* KF, const int* WP, BLayout L)
+__global__ void k_pack_tracer(const double* src, float* A, float* B, const int* KF, const int* WP,
+                              double shift, BLayout L)
 {
     const int NI = L.ni + 2, NJ = L.nj + 2;
     const long long sk = (long long)NI * NJ;
@@ -503,6 +541,7 @@ __global__ void k_pack_tracer(const double* src, float* A, float* B, const int* 
             if (k == L.nk + 1) v = 0.0;
             else if (k >= 1 && k < KF[c]) v = MOHID_NULL_REAL_D;
         }
+        if (WP[e] == 1) v -= shift;               // water cells hold the anomaly P - shift
         const long long g = L.at(i, j, k);
         A[g] = (float)v;
         if (B) B[g] = (float)v;
@@ -510,7 +549,7 @@ __global__ void k_pack_tracer(const double* src, float* A, float* B, const int* 
 }
 
 __global__ void k_unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                                const int* KF, BLayout L)
+                                const int* KF, double shift, BLayout L)
 {
     const int NI = L.ni + 2, NJ = L.nj + 2;
     const long long sk = (long long)NI * NJ;
@@ -523,7 +562,7 @@ __global__ void k_unpack_tracer(const float* src, double* dst, const double* ori
         const bool interior = i >= 1 && i <= L.ni && j >= 1 && j <= L.nj;
         const bool solved = interior && WP[c + sk * L.nk] == 1 && k >= 1;
         if (solved) {
-            if (k >= KF[c] && k <= L.nk) dst[e] = (double)src[L.at(i, j, k)];
+            if (k >= KF[c] && k <= L.nk) dst[e] = (double)src[L.at(i, j, k)] + (WP[e] == 1 ? shift : 0.0);
             else if (k > L.nk) dst[e] = 0.0;
             else dst[e] = MOHID_NULL_REAL_D;
         } else {
@@ -550,7 +589,8 @@ __device__ __forceinline__ void neu_add(double& s, double& c, double x)
     s = t;
 }
 
-__global__ void k_mass(const float* P, const double* V, const uint8_t* flag, BLayout L, double* partial)
+__global__ void k_mass(const float* P, const double* V, const uint8_t* flag, double shift, BLayout L,
+                       double* partial)
 {
     __shared__ double ss[256], sc[256];
     double s = 0.0, c = 0.0;
@@ -560,7 +600,7 @@ __global__ void k_mass(const float* P, const double* V, const uint8_t* flag, BLa
         const int j = 1 + (int)((e / L.ni) % L.nj);
         const int k = 1 + (int)(e / ((long long)L.ni * L.nj));
         const long long g = L.at(i, j, k);
-        if (flag[g] & F_WP) neu_add(s, c, V[g] * (double)P[g]);
+        if (flag[g] & F_WP) neu_add(s, c, V[g] * ((double)P[g] + shift));
     }
     ss[threadIdx.x] = s; sc[threadIdx.x] = c;
     __syncthreads();
@@ -623,15 +663,29 @@ cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX
     return cudaGetLastError();
 }
 cudaError_t pack_tracer(const double* src, float* dA, float* dB, const int* KFloor, const int* WP,
-                        const BLayout& L, cudaStream_t s)
+                        double shift, const BLayout& L, cudaStream_t s)
 {
-    k_pack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dA, dB, KFloor, WP, L);
+    k_pack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dA, dB, KFloor, WP, shift, L);
     return cudaGetLastError();
 }
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                          const int* KFloor, const BLayout& L, cudaStream_t s)
+                          const int* KFloor, double shift, const BLayout& L, cudaStream_t s)
 {
-    k_unpack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, orig, WP, KFloor, L);
+    k_unpack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, orig, WP, KFloor, shift, L);
+    return cudaGetLastError();
+}
+cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
+                           cudaStream_t s)
+{
+    k_pack_shift_f32<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, WP, shift, L);
+    return cudaGetLastError();
+}
+cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys, cudaStream_t s)
+{
+    const unsigned long long init[2] = {~0ull, 0ull};
+    cudaError_t e = cudaMemcpyAsync(keys, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    k_water_range<<<blocks_for(n) > 2048 ? 2048 : blocks_for(n), 256, 0, s>>>(src, WP, n, keys);
     return cudaGetLastError();
 }
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s)
@@ -641,10 +695,10 @@ cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t
     k_absmax<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(src, n, reinterpret_cast<unsigned long long*>(out));
     return cudaGetLastError();
 }
-cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, const BLayout& L,
-                         double* partial, int nblocks, cudaStream_t s)
+cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
+                         const BLayout& L, double* partial, int nblocks, cudaStream_t s)
 {
-    k_mass<<<nblocks, 256, 0, s>>>(P, V, flag, L, partial);
+    k_mass<<<nblocks, 256, 0, s>>>(P, V, flag, shift, L, partial);
     return cudaGetLastError();
 }
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s)
