@@ -100,6 +100,11 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
                            cudaStream_t s);
 cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys,
                         cudaStream_t s);
+cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
+                                const double* Vold, const int* OP, const int* CFU, const int* CFV,
+                                const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
+                                double* out, cudaStream_t s);
+cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s);
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);
 cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
                          const BLayout& L, double* partial, int nblocks, cudaStream_t s);

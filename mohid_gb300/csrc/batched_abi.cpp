@@ -41,6 +41,12 @@ struct Batch {
     DevBuf<float> PA, PB, Ref;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
+    // anomaly storage is exact only when the step preserves constants; this
+    // is re-checked when the hydrodynamics, DT or the flux-set flags change
+    unsigned checkedVersion = ~0u;
+    double checkedDT = -1.0;
+    int checkedFlags = -1;
+    bool shiftOk = true;
     DevBuf<unsigned long long> keys;
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
@@ -190,6 +196,46 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.xzflow = p->XZFlow != 0;
     a.status = in->status.p;
     return a;
+}
+
+constexpr double kContinuityTol = 1e-9;
+
+// Decide whether tracers may stay stored as anomalies for this step; convert
+// them (and their references) back to absolute values if not.
+int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
+{
+    Instance* in = b->in;
+    cudaStream_t s = in->stream;
+    const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0);
+    if (b->checkedVersion != in->hydroVersion || b->checkedDT != p->DTProp || b->checkedFlags != flags) {
+        bool okc = flags == 0;
+        if (okc) {
+            CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p,
+                                          in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp,
+                                          in->ni, in->nj, in->nk, b->scratch.p, s));
+            CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            okc = *b->hmass <= kContinuityTol;
+        }
+        b->shiftOk = okc;
+        b->checkedVersion = in->hydroVersion;
+        b->checkedDT = p->DTProp;
+        b->checkedFlags = flags;
+    }
+    if (!b->shiftOk) {
+        for (int t = 0; t < b->nt; ++t) {
+            if (b->shift[t] == 0.0) continue;
+            const long long off = (long long)t * b->L.n3;
+            CK(mohid::unshift(b->PA.p + off, b->flag.p, b->shift[t], b->L.n3, s));
+            CK(mohid::unshift(b->PB.p + off, b->flag.p, b->shift[t], b->L.n3, s));
+            if (b->hasRef && t < (int)b->refShift.size() && b->refShift[t] != 0.0) {
+                CK(mohid::unshift(b->Ref.p + off, b->flag.p, b->refShift[t], b->L.n3, s));
+                b->refShift[t] = 0.0;
+            }
+            b->shift[t] = 0.0;
+        }
+    }
+    return ok(stat);
 }
 
 // one transport step of every tracer: groups of 4, 2, 1 tracers per launch
@@ -393,6 +439,10 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     CK(cudaSetDevice(in->device));
+    {
+        int c = ensure_shift_valid(b, p, stat);
+        if (c) return c;
+    }
     cudaStream_t s = in->stream;
     if (!*use_graph) {
         for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s));

@@ -436,6 +436,47 @@ __global__ void k_water_range(const double* src, const int* WP, long long n, uns
     if ((threadIdx.x & 31) == 0) { atomicMin(out, lo); atomicMax(out + 1, hi); }
 }
 
+// Largest relative continuity residual over open, non-boundary water cells,
+// with the fluxes the step applies (Fortran-layout FP64 inputs):
+//   R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT
+// over compute faces, relative to the sum of the magnitudes.  When it is at
+// round-off level the step maps a constant field onto itself.
+__global__ void k_continuity(const double* Qx, const double* Qy, const double* Qz, const double* V,
+                             const double* Vold, const int* OP, const int* CFU, const int* CFV,
+                             const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
+                             unsigned long long* out)
+{
+    const long long NI = ni + 2, NJ = nj + 2, sk = NI * NJ;
+    const long long n = (long long)ni * nj * nk;
+    double m = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(e % ni);
+        const int j = 1 + (int)((e / ni) % nj);
+        const int k = 1 + (int)(e / ((long long)ni * nj));
+        const long long a = i + NI * j + sk * k, c2 = i + NI * j;
+        if (OP[a] != 1 || BP2D[c2] == 1) continue;
+        double r = 0.0, s = 0.0, f;
+        f = CFU[a] == 1 ? Qx[a] : 0.0; r += f; s += fabs(f);
+        f = CFU[a + NI] == 1 ? Qx[a + NI] : 0.0; r -= f; s += fabs(f);
+        f = CFV[a] == 1 ? Qy[a] : 0.0; r += f; s += fabs(f);
+        f = CFV[a + 1] == 1 ? Qy[a + 1] : 0.0; r -= f; s += fabs(f);
+        f = CFW[a] == 1 ? Qz[a] : 0.0; r += f; s += fabs(f);
+        f = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0); r -= f; s += fabs(f);
+        f = (V[a] - Vold[a]) / DT; r -= f; s += fabs(f);
+        const double rel = fabs(r) / (s + 1e-300);
+        m = fmax(m, rel);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// add the stored constant back: anomaly -> absolute values (water cells)
+__global__ void k_unshift(float* P, const uint8_t* flag, double shift, long long n)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        if (flag[e] & F_WP) P[e] = (float)((double)P[e] + shift);
+}
+
 __global__ void k_pack_f64(const double* __restrict__ src, double* __restrict__ dst, BLayout L)
 {
     const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
@@ -678,6 +719,23 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
                            cudaStream_t s)
 {
     k_pack_shift_f32<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, WP, shift, L);
+    return cudaGetLastError();
+}
+cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
+                                const double* Vold, const int* OP, const int* CFU, const int* CFV,
+                                const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
+                                double* out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    const long long n = (long long)ni * nj * nk;
+    k_continuity<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(
+        Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, DT, ni, nj, nk, reinterpret_cast<unsigned long long*>(out));
+    return cudaGetLastError();
+}
+cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s)
+{
+    k_unshift<<<blocks_for(n) > 8192 ? 8192 : blocks_for(n), 256, 0, s>>>(P, flag, shift, n);
     return cudaGetLastError();
 }
 cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys, cudaStream_t s)
