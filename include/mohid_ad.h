@@ -264,7 +264,7 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
  * (ReferenceProp of AdvectionDiffusion); once set for any tracer, every
  * tracer of the batch uses open boundaries and must have one.  Set it after
  * the tracer itself: a tracer is held as its anomaly from a per-tracer
- * constant (the mid-range of its water cells, chosen when it is loaded), and
+ * constant (the mean over its water cells, chosen when it is loaded), and
  * its reference is stored relative to the same constant. */
 int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
                                    const int* on_device, int* stat);

@@ -90,16 +90,17 @@ cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX
                          const int* CFW, const int* SD, float* fx, float* fy, float* areaCol,
                          int* kfloor, uint8_t* cflag, const BLayout& L, cudaStream_t s);
 // Tracers are held as the anomaly P - shift on water cells (shift: a per-tracer
-// constant, the mid-range of the field): the step is shift-equivariant, and the
-// FP32 rounding then scales with the anomaly rather than the absolute value.
+// constant, the mean over water cells): when the step preserves constants it is
+// shift-equivariant, and the FP32 rounding then scales with the anomaly rather
+// than with the absolute value.
 cudaError_t pack_tracer(const double* src, float* dstA, float* dstB, const int* KFloor,
                         const int* WP, double shift, const BLayout& L, cudaStream_t s);
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
                           const int* KFloor, double shift, const BLayout& L, cudaStream_t s);
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s);
-cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys,
-                        cudaStream_t s);
+cudaError_t water_mean(const double* src, const int* WP, long long n, double* partial, int nblocks,
+                       double* out, cudaStream_t s);
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
                                 const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,

@@ -47,7 +47,6 @@ struct Batch {
     double checkedDT = -1.0;
     int checkedFlags = -1;
     bool shiftOk = true;
-    DevBuf<unsigned long long> keys;
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
     bool packed = false;
@@ -67,7 +66,7 @@ struct Batch {
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
         V.release(); Vold.release(); flag.release(); cflag.release(); kfloor.release();
-        partial.release(); scratch.release(); stage.release(); keys.release();
+        partial.release(); scratch.release(); stage.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -316,7 +315,6 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->keys.alloc(2)) != cudaSuccess) return bad(e, "cudaMalloc");
     b->shift.assign(b->nt, 0.0);
     if ((e = cudaMallocHost((void**)&b->hmass, 4 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMallocHost");
     {
@@ -350,22 +348,11 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
         src = b->stage.p;
     }
     const long long off = (long long)*t * b->L.n3;
-    // shift = mid-range of the water cells (exactly representable in FP32)
-    unsigned long long kk[2];
-    CK(mohid::water_range(src, in->WP.p, (long long)in->n3, b->keys.p, s));
-    CK(cudaMemcpyAsync(kk, b->keys.p, sizeof(kk), cudaMemcpyDeviceToHost, s));
+    // shift = mean over the water cells, rounded to an FP32 value
+    CK(mohid::water_mean(src, in->WP.p, (long long)in->n3, b->partial.p, kMassBlocks, b->scratch.p, s));
+    CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    double sh = 0.0;
-    if (kk[0] <= kk[1]) {
-        auto unkey = [](unsigned long long k) {
-            unsigned long long bits = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
-            double x;
-            std::memcpy(&x, &bits, sizeof x);
-            return x;
-        };
-        const double lo = unkey(kk[0]), hi = unkey(kk[1]);
-        if (std::isfinite(lo) && std::isfinite(hi)) sh = (double)(float)(0.5 * (lo + hi));
-    }
+    double sh = std::isfinite(*b->hmass) ? (double)(float)*b->hmass : 0.0;
     b->shift[*t] = sh;
     CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, sh, b->L, s));
     CK(cudaStreamSynchronize(s));

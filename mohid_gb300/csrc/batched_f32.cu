@@ -411,29 +411,30 @@ __global__ void k_pack_shift_f32(const double* __restrict__ src, float* __restri
     }
 }
 
-// min and max over water cells, as order-preserving 64-bit keys
-__device__ __forceinline__ unsigned long long dkey(double x)
+// mean over water cells: per-block sums and counts, then one ordered final pass
+// (deterministic, so the stored anomalies are reproducible bit for bit)
+__global__ void k_water_sum(const double* src, const int* WP, long long n, double* partial)
 {
-    unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+    __shared__ double ss[256];
+    __shared__ double sc[256];
+    double s = 0.0, cnt = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        if (WP[e] == 1) { s += src[e]; cnt += 1.0; }
+    ss[threadIdx.x] = s; sc[threadIdx.x] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0.0, Cn = 0.0;
+        for (int q = 0; q < (int)blockDim.x; ++q) { S += ss[q]; Cn += sc[q]; }
+        partial[2 * blockIdx.x] = S;
+        partial[2 * blockIdx.x + 1] = Cn;
+    }
 }
 
-__global__ void k_water_range(const double* src, const int* WP, long long n, unsigned long long* out)
+__global__ void k_water_mean(const double* partial, int nb, double* out)
 {
-    unsigned long long lo = ~0ull, hi = 0ull;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-        if (WP[e] == 1) {
-            const unsigned long long kx = dkey(src[e]);
-            lo = kx < lo ? kx : lo;
-            hi = kx > hi ? kx : hi;
-        }
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
-        const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
-        lo = l2 < lo ? l2 : lo;
-        hi = h2 > hi ? h2 : hi;
-    }
-    if ((threadIdx.x & 31) == 0) { atomicMin(out, lo); atomicMax(out + 1, hi); }
+    double S = 0.0, Cn = 0.0;
+    for (int q = 0; q < nb; ++q) { S += partial[2 * q]; Cn += partial[2 * q + 1]; }
+    *out = Cn > 0.0 ? S / Cn : 0.0;
 }
 
 // Largest relative continuity residual over open, non-boundary water cells,
@@ -738,19 +739,11 @@ cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cu
     k_unshift<<<blocks_for(n) > 8192 ? 8192 : blocks_for(n), 256, 0, s>>>(P, flag, shift, n);
     return cudaGetLastError();
 }
-cudaError_t water_range(const double* src, const int* WP, long long n, unsigned long long* keys, cudaStream_t s)
+cudaError_t water_mean(const double* src, const int* WP, long long n, double* partial, int nblocks,
+                       double* out, cudaStream_t s)
 {
-    const unsigned long long init[2] = {~0ull, 0ull};
-    cudaError_t e = cudaMemcpyAsync(keys, init, sizeof(init), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
-    k_water_range<<<blocks_for(n) > 2048 ? 2048 : blocks_for(n), 256, 0, s>>>(src, WP, n, keys);
-    return cudaGetLastError();
-}
-cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s)
-{
-    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
-    if (e != cudaSuccess) return e;
-    k_absmax<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(src, n, reinterpret_cast<unsigned long long*>(out));
+    k_water_sum<<<nblocks, 256, 0, s>>>(src, WP, n, partial);
+    k_water_mean<<<1, 1, 0, s>>>(partial, nblocks, out);
     return cudaGetLastError();
 }
 cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
