@@ -72,7 +72,8 @@ def build(verbose: bool = False, force: bool = False) -> dict:
             fut.result()
     so = LIB / "libmohid_ad.so"
     if force or jobs or _stale(so, objs):
-        _run([nvcc, GENCODE, "-shared", "-o", str(so)] + [str(o) for o in objs] + ["-lcudart"])
+        _run([nvcc, GENCODE, "-shared", "-Xlinker", "--no-undefined", "-o", str(so)] +
+             [str(o) for o in objs] + ["-lcudart"])
     # synthetic-input generator (host C)
     cc = os.environ.get("CC", "gcc")
     syn = LIB / "libmohid_synth.so"

@@ -746,6 +746,13 @@ cudaError_t water_mean(const double* src, const int* WP, long long n, double* pa
     k_water_mean<<<1, 1, 0, s>>>(partial, nblocks, out);
     return cudaGetLastError();
 }
+cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    k_absmax<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(src, n, reinterpret_cast<unsigned long long*>(out));
+    return cudaGetLastError();
+}
 cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
                          const BLayout& L, double* partial, int nblocks, cudaStream_t s)
 {
