@@ -472,9 +472,12 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !mass) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
     if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
-    if (!b->packed) return fail(MOHID_AD_ERR_OPTION, stat, "hydrodynamics not packed yet");
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
+    if (!b->packed || b->packedVersion != in->hydroVersion) {
+        int c = pack_hydro(b, stat);
+        if (c) return c;
+    }
     cudaStream_t s = in->stream;
     const float* P = b->cur_in() + (long long)*t * b->L.n3;
     CK(mohid::mass_batched(P, b->V.p, b->flag.p, b->shift[*t], b->L, b->partial.p, kMassBlocks, s));
