@@ -55,7 +55,7 @@ struct BatchArgs {
     const double *V, *Vold;
     const void *ViscH, *DiffV;          // float or __half
     float ksh, ksv;                     // scales for __half storage
-    const float *AreaU, *AreaV, *DZZ;
+    const float *AreaU, *AreaV, *DZZ;   // DZZ holds 1/DZZ
     const uint8_t* flag;
     // 2-D: per-face constants [6][py][px] for west (fx) and south (fy) faces:
     //   0: weight of the cell's own Visc, 1: weight of the neighbour's Visc
@@ -81,6 +81,7 @@ cudaError_t launch_batched(const BatchArgs& a, int method, int limiter, bool hal
 
 // packing (Fortran FP64 Size box <-> batched layout)
 cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nzSrc, cudaStream_t s);
+cudaError_t pack_recip_f32(const double* src, float* dst, const BLayout& L, cudaStream_t s);
 cudaError_t pack_f64_to_f16(const double* src, __half* dst, float invScale, const BLayout& L, cudaStream_t s);
 cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s);
 cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,

@@ -152,7 +152,7 @@ int pack_hydro(Batch* b, int* stat)
     CK(mohid::pack_f64_to_f64(in->Vold.p, b->Vold.p, L, s));
     CK(mohid::pack_f64_to_f32(in->AreaU.p, b->AreaU.p, L, in->nk + 2, s));
     CK(mohid::pack_f64_to_f32(in->AreaV.p, b->AreaV.p, L, in->nk + 2, s));
-    CK(mohid::pack_f64_to_f32(in->DZZ.p, b->DZZ.p, L, in->nk + 2, s));
+    CK(mohid::pack_recip_f32(in->DZZ.p, b->DZZ.p, L, s));
     CK(mohid::pack_flags(in->WP.p, in->OP.p, in->CFU.p, in->CFV.p, in->CFW.p, in->LP.p, b->flag.p, L, s));
     CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,

@@ -41,7 +41,7 @@ constexpr int PW = TX + 4, PH = TY + 4;     // tracer / flag tile with 2-cell ha
 constexpr int VW = TX + 2, VH = TY + 2;     // halo-1 tiles
 
 template <int NT>
-struct Tiles {
+struct Stage {                // one layer of the tile, staged from global memory
     float P[NT][PH][PW];
     float V[VH][VW];
     float Vis[VH][VW];
@@ -49,11 +49,16 @@ struct Tiles {
     float AU[TY + 1][TX];
     float QY[TY][TX + 1];     // south faces of cells (i0..i0+TX, j0..j0+TY-1)
     float AV[TY][TX + 1];
+    uint8_t F[PH][PW];
+};
+
+template <int NT>
+struct Tiles {
+    Stage<NT> st[2];          // double buffer: layer k+1 is staged while k is solved
     float FX[NT][TY + 1][TX];
     float FY[NT][TY][TX + 1];
     float CX[6][TY + 1][TX];
     float CY[6][TY][TX + 1];
-    uint8_t F[PH][PW];
     int kmin;
 };
 
@@ -75,45 +80,60 @@ __device__ __forceinline__ float ldq(const void* p, long long a, float s)
     return QLoad<QT>::get(reinterpret_cast<const QT*>(p), a, s);
 }
 
-// One horizontal face: tracer-independent preparation, then the flux of each
-// tracer into shared memory.  `a`/`b` are the lower/upper cells along the face
-// normal in the P tile, `st` the tile stride along that normal, `va`/`vb` the
-// same cells in the halo-1 tiles; q, area and the 2-D constants `cc` (stride
-// cs) are the face's.
+// A face of the tile, fixed for the whole walk: pb is the P/F-tile index of its
+// upper cell b (lower cell a = pb - st), vb the V-tile index of b (a = vb - vst),
+// fi the index in the face arrays (QX/AU/CX/FX for west faces, QY/AV/CY/FY for
+// south faces).
+struct FaceRef {
+    int pb, vb, fi;
+    bool west, valid;
+};
+
+// One face at one layer: tracer-independent preparation (upwind side, Courant
+// number, limiter weights, diffusive conductance), then the flux of every
+// tracer, F = q*P_up + (q*theta + kd)*(P_dn - P_up), into shared memory.
+// The reference's face coefficients: ComputeAdvectionFace FN:10702-10894
+// (first-order upwind, P2_TVD limiters), the diffusive flux of
+// HorizontalDiffusionXX/YY AD:5185-5196 with Kx from AD:2487-2494.
 template <int NT, int METHOD, int LIM>
-__device__ __forceinline__ void face_flux(Tiles<NT>& S, const BatchArgs& A, int ja, int ia, int jb, int ib,
-                                          int dj, int di, int vja, int via, int vjb, int vib,
-                                          bool act, float q, float area, const float* cc, int cs,
-                                          float* out, int ostride)
+__device__ __forceinline__ void face_flux(const Stage<NT>& T, float* FX, float* FY, const float* CX,
+                                          const float* CY, const BatchArgs& A, const FaceRef& f)
 {
-    if (!act) {
-        for (int t = 0; t < NT; ++t) out[t * ostride] = 0.f;
-        return;
-    }
-    const uint8_t fa = S.F[ja][ia], fb = S.F[jb][ib];
-    const bool adv = (fa & F_OP) && (fb & F_OP);
+    constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
+    const int st = f.west ? PW : 1, vst = f.west ? VW : 1;
+    const int cs = f.west ? NWF : NSF;
+    const float* cc = (f.west ? CX : CY) + f.fi;
+    float* out = (f.west ? FX : FY) + f.fi;
+    const int pa = f.pb - st;
+    const uint8_t* Fl = &T.F[0][0];
+    const uint8_t fb = Fl[f.pb], fa = Fl[pa];
+    const bool act = f.west ? (fb & F_CFU) && !A.vertical1D : (fb & F_CFV) && !A.vertical1D && !A.xzflow;
+    const float q = f.west ? (&T.QX[0][0])[f.fi] : (&T.QY[0][0])[f.fi];
+    const float area = f.west ? (&T.AU[0][0])[f.fi] : (&T.AV[0][0])[f.fi];
+    const bool adv = act && (fa & F_OP) && (fb & F_OP);
     const bool pos = q > 0.f;
-    // diffusive conductance: Kx*Area/DZX (Convert_Visc_Dif_Horizontal AD:2487-2494)
-    float K = A.schmidtH * (S.Vis[vjb][vib] * cc[0] + S.Vis[vja][via] * cc[cs]);
+    // diffusive conductance Kx*Area/DZX; F_dif = -auxK*(Pb - Pa) = kd*(Pdn - Pup)
+    float K = A.schmidtH * ((&T.Vis[0][0])[f.vb] * cc[0] + (&T.Vis[0][0])[f.vb - vst] * cc[cs]);
     if (A.nullDif && q == 0.f) K = 0.f;
-    const float auxK = K * area * cc[2 * cs];
-    float c = 0.f, gup = 0.f, gdn = 0.f, pa = 0.f, pb = 0.f, p2 = 0.f, pcr = 0.f;
+    const float auxK = act ? K * area * cc[2 * cs] : 0.f;
+    const float kd = pos ? -auxK : auxK;
+    const float qv = adv ? q : 0.f;
+    const int iup = pos ? pa : f.pb, idn = pos ? f.pb : pa;
+    int iuu = iup;
+    float c = 0.f, gup = 0.f, gdn = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
     bool tvd = false;
-    int juu = 0, iuu = 0;
     if (METHOD == 4 && adv) {
-        juu = pos ? ja - dj : jb + dj;
-        iuu = pos ? ia - di : ib + di;
-        const bool nb = !(S.F[juu][iuu] & F_OP);
-        if (!nb) {
+        iuu = pos ? pa - st : f.pb + st;
+        if (Fl[iuu] & F_OP) {                      // not near a boundary
             tvd = true;
-            const float vup = pos ? S.V[vja][via] : S.V[vjb][vib];
-            float Cr = q * A.DT / vup;
+            const float vup = (&T.V[0][0])[pos ? f.vb - vst : f.vb];
+            float Cr = __fdividef(q * A.DT, vup);
             gdn = cc[4 * cs];
             gup = pos ? cc[3 * cs] : cc[5 * cs];
             if (LIM == 5) {
                 const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
-                pa = 0.5f + t6;
-                pb = 0.5f - t6;
+                pa5 = 0.5f + t6;
+                pb5 = 0.5f - t6;
                 if (fabsf(Cr) < 1e-16f) Cr = 1e-16f;
                 p2 = 2.f / (1.f - Cr);
                 pcr = 2.f / Cr;
@@ -121,32 +141,40 @@ __device__ __forceinline__ void face_flux(Tiles<NT>& S, const BatchArgs& A, int 
             c = 0.5f * (1.f - Cr);
         }
     }
+#pragma unroll
     for (int t = 0; t < NT; ++t) {
-        const float Pa = S.P[t][ja][ia], Pb = S.P[t][jb][ib];
-        float F = -auxK * (Pb - Pa);
-        if (adv) {
-            const float Pup = pos ? Pa : Pb, Pdn = pos ? Pb : Pa;
-            float theta = 0.f;
-            if (METHOD == 4 && tvd) {
-                const float Puu = S.P[t][juu][iuu];
-                float dC = (Pdn - Pup) * gdn;
-                if (fabsf(dC) < 1e-16f) dC = dC >= 0.f ? 1e-16f : -1e-16f;
-                const float r = __fdividef((Pup - Puu) * gup, dC);
-                theta = limiter<LIM>(r, pa, pb, p2, pcr) * c;
-            }
-            F += q * (Pup + theta * (Pdn - Pup));
+        const float* Pt = &T.P[t][0][0];
+        const float Pup = Pt[iup], Pdn = Pt[idn];
+        const float dd = Pdn - Pup;
+        float coef = kd;
+        if (METHOD == 4) {
+            const float du = Pup - Pt[iuu];
+            float dC = dd * gdn;
+            if (fabsf(dC) < 1e-16f) dC = copysignf(1e-16f, dC);
+            const float r = du * gup * __frcp_rn(dC);
+            const float th = tvd ? limiter<LIM>(r, pa5, pb5, p2, pcr) * c : 0.f;
+            coef = fmaf(qv, th, kd);
         }
-        out[t * ostride] = F;
+        out[t * cs] = fmaf(coef, dd, qv * Pup);
     }
 }
 
+// Staging slots: every thread moves up to two elements of each layer tile;
+// their shared-memory index and layer-0 global offset are fixed for the walk.
+struct Slot2 {
+    int s[2];
+    long long g[2];
+    bool v[2];
+};
+
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
-__global__ void __launch_bounds__(NTH)
+__global__ void __launch_bounds__(NTH, 2)
 batched_kernel(const BatchArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tiles<NT>& S = *reinterpret_cast<Tiles<NT>*>(smem_raw);
     float* Wcol = reinterpret_cast<float*>(smem_raw + ((sizeof(Tiles<NT>) + 15) / 16) * 16);
+    constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
 
     const BLayout& L = A.L;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -159,13 +187,12 @@ batched_kernel(const BatchArgs A)
     const int kb = solve ? A.kfloor[c2] : L.nk + 1;
 
     if (tid == 0) S.kmin = L.nk + 1;
-    // 2-D face constants of this tile
-    for (int e = tid; e < (TY + 1) * TX; e += NTH) {
+    for (int e = tid; e < NWF; e += NTH) {
         const int a = e / TX, b = e % TX;
         const long long g = L.at2(i0 + b, j0 + a);
         for (int q = 0; q < 6; ++q) S.CX[q][a][b] = A.fx[q * L.n2 + g];
     }
-    for (int e = tid; e < TY * (TX + 1); e += NTH) {
+    for (int e = tid; e < NSF; e += NTH) {
         const int a = e / (TX + 1), b = e % (TX + 1);
         const long long g = L.at2(i0 + b, j0 + a);
         for (int q = 0; q < 6; ++q) S.CY[q][a][b] = A.fy[q * L.n2 + g];
@@ -176,92 +203,161 @@ batched_kernel(const BatchArgs A)
     const int kmin = S.kmin;
     if (kmin > L.nk) return;                       // no water column in this tile
 
+    const bool horiz = !A.vertical1D;
+    // ---- this thread's faces for the whole walk (west faces, then south faces)
+    FaceRef fr[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int f = tid + q * NTH;
+        fr[q].valid = horiz && f < NWF + NSF;
+        if (f < NWF) {
+            const int a = f / TX, b = f % TX;
+            fr[q].west = true;
+            fr[q].pb = (a + 2) * PW + b + 2;
+            fr[q].vb = (a + 1) * VW + b + 1;
+            fr[q].fi = a * TX + b;
+        } else {
+            const int g = f - NWF, a = g / (TX + 1), b = g % (TX + 1);
+            fr[q].west = false;
+            fr[q].pb = (a + 2) * PW + b + 2;
+            fr[q].vb = (a + 1) * VW + b + 1;
+            fr[q].fi = fr[q].valid ? a * (TX + 1) + b : 0;
+        }
+    }
+    // ---- staging slots (P and flags: halo 2; V, Visc: halo 1; faces)
+    Slot2 sp, sv, sx, sy;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        int e = tid + q * NTH;
+        sp.v[q] = e < PH * PW;
+        sp.s[q] = sp.v[q] ? e : 0;
+        sp.g[q] = sp.v[q] ? L.at(i0 - 2 + e % PW, j0 - 2 + e / PW, 0) : 0;
+        sv.v[q] = e < VH * VW;
+        sv.s[q] = sv.v[q] ? e : 0;
+        sv.g[q] = sv.v[q] ? L.at(i0 - 1 + e % VW, j0 - 1 + e / VW, 0) : 0;
+        sx.v[q] = horiz && e < NWF;
+        sx.s[q] = sx.v[q] ? e : 0;
+        sx.g[q] = sx.v[q] ? L.at(i0 + e % TX, j0 + e / TX, 0) : 0;
+        sy.v[q] = horiz && e < NSF;
+        sy.s[q] = sy.v[q] ? e : 0;
+        sy.g[q] = sy.v[q] ? L.at(i0 + e % (TX + 1), j0 + e / (TX + 1), 0) : 0;
+    }
+    float rP[NT][2], rV[2], rVis[2], rQX[2], rAU[2], rQY[2], rAV[2];
+    uint8_t rF[2];
+    auto fetch = [&](int k) {
+        const long long ko = (long long)k * L.sl;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (sp.v[q]) {
+                rF[q] = A.flag[sp.g[q] + ko];
+#pragma unroll
+                for (int t = 0; t < NT; ++t) rP[t][q] = __ldg(A.Pin + t * A.ts + sp.g[q] + ko);
+            }
+            if (sv.v[q]) {
+                rV[q] = (float)__ldg(A.V + sv.g[q] + ko);
+                rVis[q] = ldq<KT>(A.ViscH, sv.g[q] + ko, A.ksh);
+            }
+            if (sx.v[q]) {
+                rQX[q] = ldq<QT>(A.Qx, sx.g[q] + ko, A.qsx);
+                rAU[q] = __ldg(A.AreaU + sx.g[q] + ko);
+            }
+            if (sy.v[q]) {
+                rQY[q] = ldq<QT>(A.Qy, sy.g[q] + ko, A.qsy);
+                rAV[q] = __ldg(A.AreaV + sy.g[q] + ko);
+            }
+        }
+    };
+    auto stage = [&](Stage<NT>& T) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (sp.v[q]) {
+                (&T.F[0][0])[sp.s[q]] = rF[q];
+#pragma unroll
+                for (int t = 0; t < NT; ++t) (&T.P[t][0][0])[sp.s[q]] = rP[t][q];
+            }
+            if (sv.v[q]) {
+                (&T.V[0][0])[sv.s[q]] = rV[q];
+                (&T.Vis[0][0])[sv.s[q]] = rVis[q];
+            }
+            if (sx.v[q]) {
+                (&T.QX[0][0])[sx.s[q]] = rQX[q];
+                (&T.AU[0][0])[sx.s[q]] = rAU[q];
+            }
+            if (sy.v[q]) {
+                (&T.QY[0][0])[sy.s[q]] = rQY[q];
+                (&T.AV[0][0])[sy.s[q]] = rAV[q];
+            }
+        }
+    };
+
     const float DT = A.DT;
     const float areaCol = solve ? A.areaCol[c2] : 0.f;
     const bool sd = cf & C_SD, opTop = cf & C_OPTOP, cfwTop = cf & C_CFWTOP, bp = cf & C_BP;
-    const bool horiz = !A.vertical1D;
 
-    // own-column sliding window
+    // own-column window: values of rows k-1 / k slide, the next row is prefetched
     float qz = 0.f, dv = 0.f, dzzm = 1.f;
-    uint8_t flm = 0;                               // flag of layer k-1
+    uint8_t flm = 0;
+    double nV = 1.0, nVo = 1.0;
+    float nQz = 0.f, nDv = 0.f, nDzz = 1.f;
+    uint8_t nFl = 0;
+    const long long cb = L.at(i, j, 0);
+    auto fetch_col = [&](int k) {                  // values first needed by row k
+        const long long a = cb + (long long)k * L.sl;
+        nV = __ldg(A.V + a);
+        nVo = __ldg(A.Vold + a);
+        nQz = ldq<QT>(A.Qz, a + L.sl, A.qsz);
+        nDv = (k < L.nk) ? ldq<KT>(A.DiffV, a + L.sl, A.ksv) : 0.f;
+        nDzz = __ldg(A.DZZ + a);
+        nFl = (k < L.nk) ? A.flag[a + L.sl] : 0;
+    };
     if (solve) {
-        const long long a = L.at(i, j, kb);
+        const long long a = cb + (long long)kb * L.sl;
         qz = ldq<QT>(A.Qz, a, A.qsz);
         dv = ldq<KT>(A.DiffV, a, A.ksv);
-        dzzm = A.DZZ[a - L.sl];
+        dzzm = __ldg(A.DZZ + a - L.sl);
         flm = A.flag[a - L.sl];
+        fetch_col(kb);
     }
     float Gp[NT];
+#pragma unroll
     for (int t = 0; t < NT; ++t) Gp[t] = 0.f;
     float Wp = 0.f;
     unsigned bad = 0;
+    const int jj = ty + 2, ii = tx + 2;
+    const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
 
+    fetch(kmin);
+    stage(S.st[kmin & 1]);
+    if (kmin < L.nk) fetch(kmin + 1);
     for (int k = kmin; k <= L.nk; ++k) {
-        __syncthreads();
-        // ---- stage layer k
-        for (int e = tid; e < PH * PW; e += NTH) {
-            const int a = e / PW, b = e % PW;
-            const long long g = L.at(i0 - 2 + b, j0 - 2 + a, k);
-            S.F[a][b] = A.flag[g];
-            for (int t = 0; t < NT; ++t) S.P[t][a][b] = A.Pin[t * A.ts + g];
-        }
-        for (int e = tid; e < VH * VW; e += NTH) {
-            const int a = e / VW, b = e % VW;
-            const long long g = L.at(i0 - 1 + b, j0 - 1 + a, k);
-            S.V[a][b] = (float)A.V[g];
-            S.Vis[a][b] = ldq<KT>(A.ViscH, g, A.ksh);
-        }
-        if (horiz) {
-            for (int e = tid; e < (TY + 1) * TX; e += NTH) {
-                const int a = e / TX, b = e % TX;
-                const long long g = L.at(i0 + b, j0 + a, k);
-                S.QX[a][b] = ldq<QT>(A.Qx, g, A.qsx);
-                S.AU[a][b] = A.AreaU[g];
-            }
-            for (int e = tid; e < TY * (TX + 1); e += NTH) {
-                const int a = e / (TX + 1), b = e % (TX + 1);
-                const long long g = L.at(i0 + b, j0 + a, k);
-                S.QY[a][b] = ldq<QT>(A.Qy, g, A.qsy);
-                S.AV[a][b] = A.AreaV[g];
-            }
-        }
-        __syncthreads();
+        Stage<NT>& T = S.st[k & 1];
+        __syncthreads();                           // layer k staged; previous layer's rows done
+        const bool active = solve && k >= kb;
+        const double Vd = nV, Vod = nVo;
+        const float qzp = nQz, dvp = nDv, dzz = nDzz;
+        const uint8_t flp = nFl;
+        if (active && k < L.nk) fetch_col(k + 1);
 
-        // ---- faces owned by this thread (west, south; tile edges also east, north)
-        const int jj = ty + 2, ii = tx + 2, vj = ty + 1, vi = tx + 1;
-        if (horiz) {
-            // west face of (i,j): a = (i, j-1), b = (i, j)
-            face_flux<NT, METHOD, LIM>(S, A, jj - 1, ii, jj, ii, 1, 0, vj - 1, vi, vj, vi,
-                                       (S.F[jj][ii] & F_CFU) != 0, S.QX[ty][tx], S.AU[ty][tx],
-                                       &S.CX[0][ty][tx], (TY + 1) * TX, &S.FX[0][ty][tx], (TY + 1) * TX);
-            if (ty == TY - 1)
-                face_flux<NT, METHOD, LIM>(S, A, jj, ii, jj + 1, ii, 1, 0, vj, vi, vj + 1, vi,
-                                           (S.F[jj + 1][ii] & F_CFU) != 0, S.QX[ty + 1][tx],
-                                           S.AU[ty + 1][tx], &S.CX[0][ty + 1][tx], (TY + 1) * TX,
-                                           &S.FX[0][ty + 1][tx], (TY + 1) * TX);
-            const bool yy = !A.xzflow;
-            face_flux<NT, METHOD, LIM>(S, A, jj, ii - 1, jj, ii, 0, 1, vj, vi - 1, vj, vi,
-                                       yy && (S.F[jj][ii] & F_CFV) != 0, S.QY[ty][tx], S.AV[ty][tx],
-                                       &S.CY[0][ty][tx], TY * (TX + 1), &S.FY[0][ty][tx], TY * (TX + 1));
-            if (tx == TX - 1)
-                face_flux<NT, METHOD, LIM>(S, A, jj, ii, jj, ii + 1, 0, 1, vj, vi, vj, vi + 1,
-                                           yy && (S.F[jj][ii + 1] & F_CFV) != 0, S.QY[ty][tx + 1],
-                                           S.AV[ty][tx + 1], &S.CY[0][ty][tx + 1], TY * (TX + 1),
-                                           &S.FY[0][ty][tx + 1], TY * (TX + 1));
+        // ---- the tile's faces at layer k
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            if (fr[q].valid)
+                face_flux<NT, METHOD, LIM>(T, &S.FX[0][0][0], &S.FY[0][0][0], &S.CX[0][0][0],
+                                           &S.CY[0][0][0], A, fr[q]);
+        // stage layer k+1 into the other buffer (its readers finished before
+        // the barrier above) and start fetching layer k+2
+        if (k < L.nk) {
+            stage(S.st[(k + 1) & 1]);
+            if (k + 1 < L.nk) fetch(k + 2);
         }
-        __syncthreads();
+        __syncthreads();                           // face fluxes of layer k complete
 
-        if (!solve || k < kb) continue;
+        if (!active) continue;
         // ---- row k of column (i,j): tracer-independent matrix
-        const long long a = L.at(i, j, k);
-        const uint8_t fl = S.F[jj][ii];
-        const uint8_t flp = (k < L.nk) ? A.flag[a + L.sl] : 0;
-        const double Vd = A.V[a], Vod = A.Vold[a];
+        const long long a = cb + (long long)k * L.sl;
+        const uint8_t fl = T.F[jj][ii];
         const float Vk = (float)Vd;
         const float dtv = DT / Vk;
-        const float qzp = ldq<QT>(A.Qz, a + L.sl, A.qsz);
-        const float dvp = (k < L.nk) ? ldq<KT>(A.DiffV, a + L.sl, A.ksv) : 0.f;
-        const float dzz = A.DZZ[a];
         const bool open = fl & F_OP;
         // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term
         const float ratio = open ? 1.f - (float)(Vd - Vod) / Vk : 1.f;
@@ -271,13 +367,13 @@ batched_kernel(const BatchArgs A)
             if ((fl & F_CFW) && !sd) {                       // VerticalDiffusion, face k
                 float kz = A.coefV * dv + A.backV;
                 if (A.nullDif && qz == 0.f) kz = 0.f;
-                const float aux2 = kz * areaCol / dzzm * dtv;
+                const float aux2 = kz * areaCol * dzzm * dtv;     // dzzm holds 1/DZZ(k-1)
                 D -= aux2; E += aux2;
             }
             if ((flp & F_CFW) && !sd) {                      // face k+1
                 float kz = A.coefV * dvp + A.backV;
                 if (A.nullDif && qzp == 0.f) kz = 0.f;
-                const float aux1 = kz * areaCol / dzz * dtv;
+                const float aux1 = kz * areaCol * dzz * dtv;      // dzz holds 1/DZZ(k)
                 E += aux1; Fc -= aux1;
             }
             if (!A.vertical1D && cfwTop) {                   // VerticalAdvection, upwind, implicit
@@ -295,10 +391,10 @@ batched_kernel(const BatchArgs A)
         float wfob = 0.f;
         const bool obc = bp && A.Ref && open;
         if (obc) {
-            const double hz = (double)(((fl & F_CFU) ? S.QX[ty][tx] : 0.f) -
-                                       ((S.F[jj + 1][ii] & F_CFU) ? S.QX[ty + 1][tx] : 0.f) +
-                                       ((fl & F_CFV) ? S.QY[ty][tx] : 0.f) -
-                                       ((S.F[jj][ii + 1] & F_CFV) ? S.QY[ty][tx + 1] : 0.f) +
+            const double hz = (double)(((fl & F_CFU) ? T.QX[ty][tx] : 0.f) -
+                                       ((T.F[jj + 1][ii] & F_CFU) ? T.QX[ty + 1][tx] : 0.f) +
+                                       ((fl & F_CFV) ? T.QY[ty][tx] : 0.f) -
+                                       ((T.F[jj][ii + 1] & F_CFV) ? T.QY[ty][tx + 1] : 0.f) +
                                        ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
             wfob = (float)(hz - (Vd - Vod) / (double)DT);
             if (wfob >= 0.f) E += wfob * dtv;
@@ -310,10 +406,15 @@ batched_kernel(const BatchArgs A)
         const float W = -Fc * inv;
         Wcol[k * NTH + tid] = W;
         Wp = W;
+#pragma unroll
         for (int t = 0; t < NT; ++t) {
-            const float P = S.P[t][jj][ii];
+            const float P = T.P[t][jj][ii];
             float TI = P * ratio;
-            if (horiz) TI += dtv * (S.FX[t][ty][tx] - S.FX[t][ty + 1][tx] + S.FY[t][ty][tx] - S.FY[t][ty][tx + 1]);
+            if (horiz) {
+                const float* fx = &S.FX[t][0][0];
+                const float* fy = &S.FY[t][0][0];
+                TI += dtv * ((fx[fw] - fx[fw + TX]) + (fy[fs] - fy[fs + 1]));
+            }
             if (obc && wfob < 0.f) {
                 const float ext = P * (1.f - A.tdec) + A.Ref[t * A.ts + a] * A.tdec;
                 TI -= wfob * ext * dtv;
@@ -322,20 +423,27 @@ batched_kernel(const BatchArgs A)
             Gp[t] = G;
             A.Pout[t * A.ts + a] = G;
         }
-        // slide the column window
         qz = qzp; dv = dvp; dzzm = dzz; flm = fl;
     }
 
-    // ---- back-substitution (row KUB+1 solves to 0)
+    // ---- back-substitution (row KUB+1 solves to 0), G loads issued 8 rows at a time
     if (solve) {
+#pragma unroll 1
         for (int t = 0; t < NT; ++t) {
             float x = 0.f;
-            float* Po = A.Pout + t * A.ts;
-            for (int k = L.nk; k >= kb; --k) {
-                const long long a = L.at(i, j, k);
-                x = Wcol[k * NTH + tid] * x + Po[a];
-                Po[a] = x;
-                if (!isfinite(x)) bad |= MOHID_DEV_NONFINITE;
+            float* Po = A.Pout + t * A.ts + cb;
+            for (int k = L.nk; k >= kb; k -= 8) {
+                float g[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (k - q >= kb) g[q] = __ldcg(Po + (long long)(k - q) * L.sl);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (k - q >= kb) {
+                        x = Wcol[(k - q) * NTH + tid] * x + g[q];
+                        Po[(long long)(k - q) * L.sl] = x;
+                        if (!isfinite(x)) bad |= MOHID_DEV_NONFINITE;
+                    }
             }
         }
     }
@@ -385,6 +493,17 @@ __global__ void k_pack_f32(const double* __restrict__ src, float* __restrict__ d
         const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
         const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
         dst[L.at(i, j, k)] = (float)src[e];
+    }
+}
+
+__global__ void k_pack_recip(const double* __restrict__ src, float* __restrict__ dst, BLayout L)
+{
+    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % (L.ni + 2));
+        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
+        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
+        dst[L.at(i, j, k)] = src[e] != 0.0 ? (float)(1.0 / src[e]) : 0.f;
     }
 }
 
@@ -677,6 +796,11 @@ cudaError_t launch_batched(const BatchArgs& a, int method, int limiter, bool hal
 cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nz, cudaStream_t s)
 {
     k_pack_f32<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * nz), 256, 0, s>>>(src, dst, L, nz);
+    return cudaGetLastError();
+}
+cudaError_t pack_recip_f32(const double* src, float* dst, const BLayout& L, cudaStream_t s)
+{
+    k_pack_recip<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, L);
     return cudaGetLastError();
 }
 cudaError_t pack_f64_to_f16(const double* src, __half* dst, float inv, const BLayout& L, cudaStream_t s)
