@@ -25,7 +25,8 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra nvcc flags)
 CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
-    ("batched_f32.cu", []),
+    ("batched_kernel.cu", []),
+    ("batched_pack.cu", []),
     ("abi.cpp", []),
     ("batched_abi.cpp", []),
 ]

@@ -1,5 +1,6 @@
 // batched.cuh -- layout and arguments of the batched FP32 multi-tracer form.
 #pragma once
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -73,11 +74,27 @@ struct BatchArgs {
     // scalars
     float DT, schmidtH, coefV, backV, tdec;
     int nullDif, vertical1D, xzflow;
+    int t0;                             // first tracer of this launch (TMA coordinate)
     unsigned* status;
 };
 
-cudaError_t launch_batched(const BatchArgs& a, int method, int limiter, bool halfQ, bool halfK,
-                           cudaStream_t s);
+// Tensor maps of one launch: one tiled bulk copy per field and layer.
+struct TmaMaps {
+    CUtensorMap P;                      // tracers (x, y, z, tracer): box (40, TY+4, 1, NT)
+    CUtensorMap F;                      // cell flags: box (64, TY+4, 1)
+    CUtensorMap V;                      // VolumeZ, f64: box (36, TY+2, 1)
+    CUtensorMap Vis;                    // Visc_H: box (40 | 48, TY+2, 1)
+    CUtensorMap QX, AU;                 // west faces: box (32, TY+1, 1)
+    CUtensorMap QY, AV;                 // south faces: box (36 | 40, TY, 1), (36, TY, 1)
+    CUtensorMap Vo;                     // VolumeZOld, f64, own cells: box (32, TY, 1)
+    CUtensorMap Qz, Dv, Dz, Fn;         // own cells of the layer above / 1/DZZ: box (32, TY, 1)
+};
+
+cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
+                           bool halfK, cudaStream_t s);
+size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
+// box extents (elements, x y z w) of the 13 maps in TmaMaps order
+void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4]);
 
 // packing (Fortran FP64 Size box <-> batched layout)
 cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nzSrc, cudaStream_t s);

@@ -6,6 +6,8 @@
 // (one MOHID property group).  The hydrodynamics are repacked on the device
 // into the batched layout (FP32 or scaled FP16 transports, FP64 volumes,
 // 1-byte masks); tracers are held in FP32 ping-pong buffers.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -53,6 +55,9 @@ struct Batch {
     unsigned packedVersion = ~0u;
     DevBuf<double> partial, scratch, stage;
     double* hmass = nullptr;             // pinned
+    mohid::TmaMaps maps{};               // shared-field maps (valid after a pack)
+    CUtensorMap mapP[2][3];              // tracer maps: input buffer (A/B) x group size (1, 2, 4)
+    bool mapsOk = false;
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
     bool graphCur = false;
@@ -87,6 +92,39 @@ Batch* blookup(const int* bid)
     std::lock_guard<std::mutex> lk(g_bmu);
     auto it = g_batch.find(*bid);
     return it == g_batch.end() ? nullptr : it->second;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point
+PFN_cuTensorMapEncodeTiled_v12000 encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// Tiled map over a batched-layout array (x = px, y = py, z = nk+2[, w = nt]).
+bool encode_map(CUtensorMap* m, CUtensorMapDataType dt, int elt, const void* base, const mohid::BLayout& L,
+                int nw, const int box[4], int rank = 3)
+{
+    auto enc = encoder();
+    if (!enc) return false;
+    cuuint64_t dims[4] = {(cuuint64_t)L.px, (cuuint64_t)L.py, (cuuint64_t)(L.nk + 2), (cuuint64_t)nw};
+    cuuint64_t strides[3] = {(cuuint64_t)L.px * elt, (cuuint64_t)L.px * L.py * elt,
+                             (cuuint64_t)L.px * L.py * (L.nk + 2) * elt};
+    cuuint32_t bx[4] = {(cuuint32_t)box[0], (cuuint32_t)box[1], (cuuint32_t)box[2], (cuuint32_t)box[3]};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = enc(m, dt, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, bx, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
 }
 
 int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why)
@@ -158,6 +196,45 @@ int pack_hydro(Batch* b, int* stat)
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
                            b->fx.p, b->fy.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
     CK(cudaStreamSynchronize(s));
+    // tensor maps of the shared fields and of the tracer buffers
+    {
+        const bool hq = b->storage >= 1, hk = b->storage >= 2;
+        int box[13][4];
+        mohid::batched_boxes(hq, hk, 1, box);
+        const CUtensorMapDataType tq = hq ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        const CUtensorMapDataType tk = hk ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        const int eq = hq ? 2 : 4, ek = hk ? 2 : 4;
+        const void* qx = hq ? (const void*)b->Qx16.p : (const void*)b->Qx32.p;
+        const void* qy = hq ? (const void*)b->Qy16.p : (const void*)b->Qy32.p;
+        const void* qz = hq ? (const void*)b->Qz16.p : (const void*)b->Qz32.p;
+        const void* vis = hk ? (const void*)b->Vis16.p : (const void*)b->Vis32.p;
+        const void* dif = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
+        bool okm = true;
+        mohid::TmaMaps& M = b->maps;
+        okm &= encode_map(&M.F, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[1]);
+        okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b->V.p, L, 1, box[2]);
+        okm &= encode_map(&M.Vis, tk, ek, vis, L, 1, box[3]);
+        okm &= encode_map(&M.QX, tq, eq, qx, L, 1, box[4]);
+        okm &= encode_map(&M.AU, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->AreaU.p, L, 1, box[5]);
+        okm &= encode_map(&M.QY, tq, eq, qy, L, 1, box[6]);
+        okm &= encode_map(&M.AV, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->AreaV.p, L, 1, box[7]);
+        okm &= encode_map(&M.Vo, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b->Vold.p, L, 1, box[8]);
+        okm &= encode_map(&M.Qz, tq, eq, qz, L, 1, box[9]);
+        okm &= encode_map(&M.Dv, tk, ek, dif, L, 1, box[10]);
+        okm &= encode_map(&M.Dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DZZ.p, L, 1, box[11]);
+        okm &= encode_map(&M.Fn, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[12]);
+        const int gs[3] = {1, 2, 4};
+        for (int buf = 0; buf < 2; ++buf)
+            for (int g = 0; g < 3; ++g) {
+                if (gs[g] > b->nt) continue;
+                int bb[13][4];
+                mohid::batched_boxes(hq, hk, gs[g], bb);
+                okm &= encode_map(&b->mapP[buf][g], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                                  buf ? b->PB.p : b->PA.p, L, b->nt, bb[0], 4);
+            }
+        if (!okm) return fail(MOHID_AD_ERR_CUDA, stat, "cuTensorMapEncodeTiled failed");
+        b->mapsOk = true;
+    }
     b->packed = true;
     b->packedVersion = in->hydroVersion;
     return ok(stat);
@@ -184,6 +261,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Pin = Pin + (long long)t0 * a.ts;
     a.Pout = Pout + (long long)t0 * a.ts;
     a.nt = nt;
+    a.t0 = t0;
     a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
     a.DT = (float)p->DTProp;
     a.schmidtH = (float)p->schmidt_H;
@@ -247,7 +325,9 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s)
         const int left = b->nt - t0;
         const int g = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
         mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout);
-        cudaError_t e = mohid::launch_batched(a, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
+        mohid::TmaMaps m = b->maps;
+        m.P = b->mapP[b->cur ? 1 : 0][g == 4 ? 2 : (g == 2 ? 1 : 0)];
+        cudaError_t e = mohid::launch_batched(a, m, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
                                               b->storage >= 2, s);
         if (e != cudaSuccess) return e;
         t0 += g;

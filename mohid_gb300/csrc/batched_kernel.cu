@@ -1,0 +1,569 @@
+// batched_kernel.cu -- batched FP32 multi-tracer transport step (TMA-staged).
+//
+// Same operator as the plain FP64 drop-in (ModuleAdvectionDiffusion's
+// AdvectionDiffusion: VolumeVariation, explicit horizontal diffusion and
+// advection with ComputeAdvectionFace coefficients, implicit vertical
+// diffusion and upwind advection, MassConservation open boundaries, THOMASZ),
+// re-organised for many tracers sharing one hydrodynamic state:
+//
+//  * a CTA owns a 32 x 8 tile of water columns and walks k upwards.  Each
+//    layer's fields (all tracers of the launch with a 2-cell halo, masks,
+//    volumes, viscosity, face transports and areas, and the own-column values
+//    of the layer above) arrive in shared memory as tiled bulk-tensor copies
+//    (TMA), double-buffered on two mbarriers: layer k+1 streams in while layer
+//    k is solved.  One thread issues 13 copies per layer; no thread spends
+//    instructions or registers on staging;
+//  * every horizontal face is evaluated once per layer: its tracer-independent
+//    part (Courant number, upwind side, limiter weights, diffusive
+//    conductance) once, then the flux of each tracer; cells gather their four
+//    face fluxes from shared memory;
+//  * the vertical tridiagonal matrix does not depend on the tracer (upwind
+//    vertical advection + diffusion, AD:2708-2784, AD:3066-3117), so each row
+//    is factorised once (W, 1/pivot) and every tracer only runs
+//    G = (TI - D*G_prev) / pivot and the back-substitution (THOMASZ,
+//    FN:4026-4123); W lives in shared memory, G is parked in the output array;
+//  * the volume ratio Vold/V is formed as 1 - (V - Vold)/V with the difference
+//    taken in FP64 (thin layers make it cancel); everything else is FP32;
+//  * rows below KFloor are never touched (they hold null_real, as after any
+//    reference step), so a z-level column costs what it holds.
+//
+// Every wait on an mbarrier is bounded; a stage that never arrives makes the
+// whole CTA set MOHID_DEV_TIMEOUT and return.
+#include <type_traits>
+
+#include "batched.cuh"
+#include "common.cuh"
+
+namespace mohid {
+namespace {
+
+constexpr int TX = kTX, TY = kTY, NTH = TX * TY;
+constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
+
+// ---- TMA stage layout -------------------------------------------------------
+// Box origins sit on 16-byte boundaries of the batched layout (x = i + 31):
+// the tracer tile starts 4 cells before i0, the flag tile 16 cells before, the
+// FP64 volume tile 2 cells before, the viscosity tile 4 (FP32) or 8 (FP16)
+// cells before; face and own-cell tiles start at i0.
+constexpr int PBX = 40, FBX = 64, VBX = 36, OWN = 32, AVX = 36;
+template <typename T> struct Box;
+template <> struct Box<float> { static constexpr int visX = 40, visOff = 4, qyX = 36; };
+template <> struct Box<__half> { static constexpr int visX = 48, visOff = 8, qyX = 40; };
+
+constexpr int al128(int b) { return (b + 127) / 128 * 128; }
+
+template <int NT, typename QT, typename KT>
+struct StageLayout {
+    static constexpr int qyX = Box<QT>::qyX, visX = Box<KT>::visX;
+    static constexpr int bP = NT * (TY + 4) * PBX * 4;
+    static constexpr int bF = (TY + 4) * FBX;
+    static constexpr int bV = (TY + 2) * VBX * 8;
+    static constexpr int bVis = (TY + 2) * visX * (int)sizeof(KT);
+    static constexpr int bQX = (TY + 1) * TX * (int)sizeof(QT);
+    static constexpr int bAU = (TY + 1) * TX * 4;
+    static constexpr int bQY = TY * qyX * (int)sizeof(QT);
+    static constexpr int bAV = TY * AVX * 4;
+    static constexpr int bVo = TY * OWN * 8;
+    static constexpr int bQz = TY * OWN * (int)sizeof(QT);
+    static constexpr int bDv = TY * OWN * (int)sizeof(KT);
+    static constexpr int bDz = TY * OWN * 4;
+    static constexpr int bFn = TY * OWN;
+    static constexpr int oP = 0;
+    static constexpr int oF = oP + al128(bP);
+    static constexpr int oV = oF + al128(bF);
+    static constexpr int oVis = oV + al128(bV);
+    static constexpr int oQX = oVis + al128(bVis);
+    static constexpr int oAU = oQX + al128(bQX);
+    static constexpr int oQY = oAU + al128(bAU);
+    static constexpr int oAV = oQY + al128(bQY);
+    static constexpr int oVo = oAV + al128(bAV);
+    static constexpr int oQz = oVo + al128(bVo);
+    static constexpr int oDv = oQz + al128(bQz);
+    static constexpr int oDz = oDv + al128(bDv);
+    static constexpr int oFn = oDz + al128(bDz);
+    static constexpr int size = oFn + al128(bFn);
+    static constexpr unsigned tx_bytes =
+        bP + bF + bV + bVis + bQX + bAU + bQY + bAV + bVo + bQz + bDv + bDz + bFn;
+};
+
+template <int NT, typename QT, typename KT>
+struct Smem {
+    using SL = StageLayout<NT, QT, KT>;
+    static constexpr int oStage0 = 0;
+    static constexpr int oStage1 = SL::size;
+    static constexpr int oFX = 2 * SL::size;
+    static constexpr int oFY = oFX + al128(NT * NWF * 4);
+    static constexpr int oCX = oFY + al128(NT * NSF * 4);
+    static constexpr int oCY = oCX + al128(6 * NWF * 4);
+    static constexpr int oBar = oCY + al128(6 * NSF * 4);
+    static constexpr int oW = oBar + 128;
+    static size_t bytes(int nk) { return (size_t)oW + sizeof(float) * (size_t)(nk + 2) * NTH; }
+};
+
+// ---- PTX helpers: mbarrier and bulk tensor copies ---------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit)
+{
+    for (uint32_t it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, int x, int y, int z, int w, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+        : "memory");
+}
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+template <int LIM>
+__device__ __forceinline__ float limiter(float r, float pa, float pb, float p2, float pcr)
+{
+    // ComputeAdvectionFace limiters, FN:10823-10856
+    if (LIM == 1) return fmaxf(0.f, fminf(1.f, r));
+    if (LIM == 2) return r < 0.f ? 0.f : 2.f * r / (1.f + r);
+    if (LIM == 3) return fmaxf(0.f, fminf(fminf(2.f, 2.f * r), (1.f + r) * 0.5f));
+    if (LIM == 4) return fmaxf(fmaxf(0.f, fminf(1.f, 2.f * r)), fminf(r, 2.f));
+    // PDM: pa, pb from |Cr|, p2 = 2/(1-Cr'), pcr = 2/Cr'
+    return fmaxf(0.f, fminf(fminf(pa + pb * r, p2), r * pcr));
+}
+
+template <typename T> __device__ __forceinline__ float tofl(T v, float s);
+template <> __device__ __forceinline__ float tofl<float>(float v, float) { return v; }
+template <> __device__ __forceinline__ float tofl<__half>(__half v, float s) { return s * __half2float(v); }
+
+template <typename T>
+__device__ __forceinline__ float ldg_as(const void* p, long long a, float s)
+{
+    return tofl<T>(reinterpret_cast<const T*>(p)[a], s);
+}
+
+// One face of the tile at one layer.  WEST: the face between cells
+// (i0+b, j0+a-1) and (i0+b, j0+a), a = 0..TY; otherwise the face between
+// (i0+b-1, j0+a) and (i0+b, j0+a), b = 0..TX.  Tracer-independent part first
+// (upwind side, Courant number, limiter weights, diffusive conductance), then
+// for every tracer F = q*P_up + (q*theta + kd)*(P_dn - P_up) into shared memory.
+// Reference face coefficients: ComputeAdvectionFace FN:10702-10894 (upwind,
+// P2_TVD limiters); diffusive flux HorizontalDiffusionXX/YY AD:5185-5196 with
+// Kx from Convert_Visc_Dif_Horizontal AD:2487-2494.
+template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT>
+__device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, const float* CXY,
+                                          const BatchArgs& A, int a, int b)
+{
+    using SL = StageLayout<NT, QT, KT>;
+    constexpr int pst = WEST ? PBX : 1, fst = WEST ? FBX : 1, vst = WEST ? VBX : 1;
+    constexpr int visst = WEST ? Box<KT>::visX : 1;
+    constexpr int cs = WEST ? NWF : NSF;
+    const float* P = reinterpret_cast<const float*>(st + SL::oP);
+    const uint8_t* Fl = st + SL::oF;
+    const double* Vt = reinterpret_cast<const double*>(st + SL::oV);
+    const KT* Vis = reinterpret_cast<const KT*>(st + SL::oVis);
+    const int pb = (a + 2) * PBX + b + 4;
+    const int fb = (a + 2) * FBX + b + 16;
+    const int vb = (a + 1) * VBX + b + 2;
+    const int visb = (a + 1) * Box<KT>::visX + b + Box<KT>::visOff;
+    const int fi = WEST ? a * TX + b : a * (TX + 1) + b;
+    float q, area;
+    if (WEST) {
+        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQX)[a * TX + b], A.qsx);
+        area = reinterpret_cast<const float*>(st + SL::oAU)[a * TX + b];
+    } else {
+        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQY)[a * SL::qyX + b], A.qsy);
+        area = reinterpret_cast<const float*>(st + SL::oAV)[a * AVX + b];
+    }
+    const uint8_t fbv = Fl[fb], fav = Fl[fb - fst];
+    const bool act = WEST ? (fbv & F_CFU) != 0 : ((fbv & F_CFV) != 0 && !A.xzflow);
+    const bool adv = act && (fav & F_OP) && (fbv & F_OP);
+    const bool pos = q > 0.f;
+    const float* cc = CXY + fi;
+    float K = A.schmidtH * (tofl<KT>(Vis[visb], A.ksh) * cc[0] + tofl<KT>(Vis[visb - visst], A.ksh) * cc[cs]);
+    if (A.nullDif && q == 0.f) K = 0.f;
+    const float auxK = act ? K * area * cc[2 * cs] : 0.f;
+    const float kd = pos ? -auxK : auxK;
+    const float qv = adv ? q : 0.f;
+    const int pa = pb - pst;
+    const int iup = pos ? pa : pb, idn = pos ? pb : pa;
+    int iuu = iup;
+    float c = 0.f, gup = 0.f, gdn = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
+    bool tvd = false;
+    if (METHOD == 4 && adv) {
+        iuu = pos ? pa - pst : pb + pst;
+        const int fuu = pos ? fb - 2 * fst : fb + fst;
+        if (Fl[fuu] & F_OP) {                      // not near a boundary
+            tvd = true;
+            const float vup = (float)Vt[pos ? vb - vst : vb];
+            float Cr = __fdividef(q * A.DT, vup);
+            gdn = cc[4 * cs];
+            gup = pos ? cc[3 * cs] : cc[5 * cs];
+            if (LIM == 5) {
+                const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
+                pa5 = 0.5f + t6;
+                pb5 = 0.5f - t6;
+                if (fabsf(Cr) < 1e-16f) Cr = 1e-16f;
+                p2 = 2.f / (1.f - Cr);
+                pcr = 2.f / Cr;
+            }
+            c = 0.5f * (1.f - Cr);
+        }
+    }
+    float* out = FXY + fi;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const float* Pt = P + t * (TY + 4) * PBX;
+        const float Pup = Pt[iup], Pdn = Pt[idn];
+        const float dd = Pdn - Pup;
+        float coef = kd;
+        if (METHOD == 4) {
+            const float du = Pup - Pt[iuu];
+            float dC = dd * gdn;
+            if (fabsf(dC) < 1e-16f) dC = copysignf(1e-16f, dC);
+            const float r = __fdividef(du * gup, dC);
+            const float th = tvd ? limiter<LIM>(r, pa5, pb5, p2, pcr) * c : 0.f;
+            coef = fmaf(qv, th, kd);
+        }
+        out[t * cs] = fmaf(coef, dd, qv * Pup);
+    }
+}
+
+template <int NT, int METHOD, int LIM, typename QT, typename KT>
+__global__ void __launch_bounds__(NTH, 2)
+batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
+{
+    using SL = StageLayout<NT, QT, KT>;
+    using SM = Smem<NT, QT, KT>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX);
+    float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY);
+    float* CX = reinterpret_cast<float*>(smem_raw + SM::oCX);
+    float* CY = reinterpret_cast<float*>(smem_raw + SM::oCY);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::oBar);
+    int* kminp = reinterpret_cast<int*>(smem_raw + SM::oBar + 32);
+    float* Wcol = reinterpret_cast<float*>(smem_raw + SM::oW);
+
+    const BLayout& L = A.L;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = 1 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
+    const int i = i0 + tx, j = j0 + ty;
+    const bool inside = i <= L.ni && j <= L.nj;
+    const long long c2 = L.at2(i, j);
+    const uint8_t cf = inside ? A.cflag[c2] : 0;
+    const bool solve = cf & C_SOLVE;
+    const int kb = solve ? A.kfloor[c2] : L.nk + 1;
+
+    if (tid == 0) {
+        *kminp = L.nk + 1;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    for (int e = tid; e < NWF; e += NTH) {
+        const long long g = L.at2(i0 + e % TX, j0 + e / TX);
+        for (int q = 0; q < 6; ++q) CX[q * NWF + e] = A.fx[q * L.n2 + g];
+    }
+    for (int e = tid; e < NSF; e += NTH) {
+        const long long g = L.at2(i0 + e % (TX + 1), j0 + e / (TX + 1));
+        for (int q = 0; q < 6; ++q) CY[q * NSF + e] = A.fy[q * L.n2 + g];
+    }
+    __syncthreads();
+    if (solve) atomicMin(kminp, kb);
+    __syncthreads();
+    const int kmin = *kminp;
+    if (kmin > L.nk) return;                       // no water column in this tile
+
+    // TMA box origins (x on 16-byte boundaries of the batched layout)
+    const int xP = i0 + kXOff - 4, xF = i0 + kXOff - 16, xV = i0 + kXOff - 2;
+    const int xVis = i0 + kXOff - Box<KT>::visOff, xO = i0 + kXOff;
+    const int yP = j0 + kYOff - 2, yV = j0 + kYOff - 1, yO = j0 + kYOff;
+    auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
+        unsigned char* d = smem_raw + (s ? SM::oStage1 : SM::oStage0);
+        uint64_t* br = &bar[s];
+        mbar_expect_tx(br, SL::tx_bytes);
+        tma4(d + SL::oP, &M.P, xP, yP, k, A.t0, br);
+        tma3(d + SL::oF, &M.F, xF, yP, k, br);
+        tma3(d + SL::oV, &M.V, xV, yV, k, br);
+        tma3(d + SL::oVis, &M.Vis, xVis, yV, k, br);
+        tma3(d + SL::oQX, &M.QX, xO, yO, k, br);
+        tma3(d + SL::oAU, &M.AU, xO, yO, k, br);
+        tma3(d + SL::oQY, &M.QY, xO, yO, k, br);
+        tma3(d + SL::oAV, &M.AV, xO, yO, k, br);
+        tma3(d + SL::oVo, &M.Vo, xO, yO, k, br);
+        tma3(d + SL::oQz, &M.Qz, xO, yO, k + 1, br);
+        tma3(d + SL::oDv, &M.Dv, xO, yO, k + 1, br);
+        tma3(d + SL::oDz, &M.Dz, xO, yO, k, br);
+        tma3(d + SL::oFn, &M.Fn, xO, yO, k + 1, br);
+    };
+    if (tid == 0) {
+        issue(kmin, kmin & 1);
+        if (kmin < L.nk) issue(kmin + 1, (kmin + 1) & 1);
+    }
+
+    const bool horiz = !A.vertical1D;
+    const float DT = A.DT;
+    const float areaCol = solve ? A.areaCol[c2] : 0.f;
+    const bool sd = cf & C_SD, opTop = cf & C_OPTOP, cfwTop = cf & C_CFWTOP, bp = cf & C_BP;
+    // own-column values of the row below slide up the walk
+    float qz = 0.f, dv = 0.f, dzzm = 1.f;
+    uint8_t flm = 0;
+    const long long cb = L.at(i, j, 0);
+    if (solve) {
+        const long long a = cb + (long long)kb * L.sl;
+        qz = ldg_as<QT>(A.Qz, a, A.qsz);
+        dv = ldg_as<KT>(A.DiffV, a, A.ksv);
+        dzzm = A.DZZ[a - L.sl];
+        flm = A.flag[a - L.sl];
+    }
+    float Gp[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) Gp[t] = 0.f;
+    float Wp = 0.f;
+    unsigned bad = 0;
+    uint32_t phase = 0;                            // bit s: parity of buffer s
+    const int own = ty * OWN + tx;
+    const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
+
+    for (int k = kmin; k <= L.nk; ++k) {
+        const int s = k & 1;
+        const unsigned char* st = smem_raw + (s ? SM::oStage1 : SM::oStage0);
+        const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
+        phase ^= 1u << s;
+
+        // ---- faces of the tile at layer k: own west and south faces; the
+        //      east row (warp 0) and north column (warp 1) close the tile
+        if (horiz && ok) {
+            face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, ty, tx);
+            face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, ty, tx);
+            if (ty == 0) face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, TY, tx);
+            else if (ty == 1 && tx < TY) face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, tx, TX);
+        }
+        if (__syncthreads_or(!ok)) {               // a stage never arrived: leave cleanly
+            if (tid == 0) {
+                atomicOr(A.status, MOHID_DEV_TIMEOUT);
+                mbar_wait_bounded(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u, kWaitLimit);
+            }
+            return;
+        }
+
+        if (solve && k >= kb) {
+            // ---- row k of column (i,j): tracer-independent matrix
+            const long long a = cb + (long long)k * L.sl;
+            const uint8_t* Fl = st + SL::oF;
+            const int fo = (ty + 2) * FBX + tx + 16;
+            const uint8_t fl = Fl[fo];
+            const uint8_t flp = (k < L.nk) ? (st + SL::oFn)[own] : 0;
+            const double Vd = reinterpret_cast<const double*>(st + SL::oV)[(ty + 1) * VBX + tx + 2];
+            const double Vod = reinterpret_cast<const double*>(st + SL::oVo)[own];
+            const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
+            const float dvp = (k < L.nk) ? tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) : 0.f;
+            const float dzz = reinterpret_cast<const float*>(st + SL::oDz)[own];
+            const float Vk = (float)Vd;
+            const float dtv = DT / Vk;
+            const bool open = fl & F_OP;
+            // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term
+            const float ratio = open ? 1.f - (float)(Vd - Vod) / Vk : 1.f;
+            float E = 1.f, D = 0.f, Fc = 0.f;
+            if (open && k == L.nk) E = 1.f + dtv * qzp;
+            if (L.nk > 1) {
+                if ((fl & F_CFW) && !sd) {                   // VerticalDiffusion, face k
+                    float kz = A.coefV * dv + A.backV;
+                    if (A.nullDif && qz == 0.f) kz = 0.f;
+                    const float aux2 = kz * areaCol * dzzm * dtv;     // dzzm holds 1/DZZ(k-1)
+                    D -= aux2; E += aux2;
+                }
+                if ((flp & F_CFW) && !sd) {                  // face k+1
+                    float kz = A.coefV * dvp + A.backV;
+                    if (A.nullDif && qzp == 0.f) kz = 0.f;
+                    const float aux1 = kz * areaCol * dzz * dtv;      // dzz holds 1/DZZ(k)
+                    E += aux1; Fc -= aux1;
+                }
+                if (!A.vertical1D && cfwTop) {               // VerticalAdvection, upwind, implicit
+                    if (k >= kb + 1 && opTop && (flm & F_OP) && open) {
+                        D -= (qz > 0.f ? qz : 0.f) * dtv;
+                        E -= (qz > 0.f ? 0.f : qz) * dtv;
+                    }
+                    if (k + 1 <= L.nk && opTop && open && (flp & F_OP)) {
+                        E += (qzp > 0.f ? qzp : 0.f) * dtv;
+                        Fc += (qzp > 0.f ? 0.f : qzp) * dtv;
+                    }
+                }
+            }
+            // open boundary (MassConservation): net flux through the exterior faces
+            float wfob = 0.f;
+            const bool obc = bp && A.Ref && open;
+            if (obc) {
+                const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
+                const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
+                const double hz =
+                    (double)(((fl & F_CFU) ? tofl<QT>(qx[fw], A.qsx) : 0.f) -
+                             ((Fl[fo + FBX] & F_CFU) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f) +
+                             ((fl & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
+                             ((Fl[fo + 1] & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
+                             ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
+                wfob = (float)(hz - (Vd - Vod) / (double)DT);
+                if (wfob >= 0.f) E += wfob * dtv;
+            }
+            // THOMASZ factorisation of row k
+            const float aux = E + D * Wp;
+            float inv;
+            if (aux != 0.f) inv = 1.f / aux; else { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
+            const float W = -Fc * inv;
+            Wcol[k * NTH + tid] = W;
+            Wp = W;
+            const float* P = reinterpret_cast<const float*>(st + SL::oP);
+            const int po = (ty + 2) * PBX + tx + 4;
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                const float Pc = P[t * (TY + 4) * PBX + po];
+                float TI = Pc * ratio;
+                if (horiz)
+                    TI += dtv * ((FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
+                                 (FY[t * NSF + fs] - FY[t * NSF + fs + 1]));
+                if (obc && wfob < 0.f) {
+                    const float ext = Pc * (1.f - A.tdec) + A.Ref[(long long)t * A.ts + a] * A.tdec;
+                    TI -= wfob * ext * dtv;
+                }
+                const float G = (TI - D * Gp[t]) * inv;
+                Gp[t] = G;
+                A.Pout[(long long)t * A.ts + a] = G;
+            }
+            qz = qzp; dv = dvp; dzzm = dzz; flm = fl;
+        }
+        __syncthreads();                           // buffer s and the face fluxes are free
+        if (tid == 0 && k + 2 <= L.nk) issue(k + 2, s);
+    }
+
+    // ---- back-substitution (row KUB+1 solves to 0), G loads issued 8 rows at a time
+    if (solve) {
+#pragma unroll 1
+        for (int t = 0; t < NT; ++t) {
+            float x = 0.f;
+            float* Po = A.Pout + (long long)t * A.ts + cb;
+            for (int k = L.nk; k >= kb; k -= 8) {
+                float g[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (k - q >= kb) g[q] = __ldcg(Po + (long long)(k - q) * L.sl);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (k - q >= kb) {
+                        x = Wcol[(k - q) * NTH + tid] * x + g[q];
+                        Po[(long long)(k - q) * L.sl] = x;
+                        if (!isfinite(x)) bad |= MOHID_DEV_NONFINITE;
+                    }
+            }
+        }
+    }
+    if (bad) atomicOr(A.status, bad);
+}
+
+template <int NT, int METHOD, int LIM, typename QT, typename KT>
+cudaError_t launch_t(const BatchArgs& a, const TmaMaps& m, cudaStream_t s)
+{
+    const size_t smem = Smem<NT, QT, KT>::bytes(a.L.nk);
+    auto kern = batched_kernel<NT, METHOD, LIM, QT, KT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grd((unsigned)((a.L.ni + TX - 1) / TX), (unsigned)((a.L.nj + TY - 1) / TY));
+    kern<<<grd, dim3(TX, TY), smem, s>>>(a, m);
+    return cudaGetLastError();
+}
+
+template <int NT, typename QT, typename KT>
+cudaError_t launch_m(const BatchArgs& a, const TmaMaps& m, int method, int limiter, cudaStream_t s)
+{
+    if (method == 1) return launch_t<NT, 1, 0, QT, KT>(a, m, s);
+    switch (limiter) {
+    case 1: return launch_t<NT, 4, 1, QT, KT>(a, m, s);
+    case 2: return launch_t<NT, 4, 2, QT, KT>(a, m, s);
+    case 3: return launch_t<NT, 4, 3, QT, KT>(a, m, s);
+    case 4: return launch_t<NT, 4, 4, QT, KT>(a, m, s);
+    default: return launch_t<NT, 4, 5, QT, KT>(a, m, s);
+    }
+}
+
+template <int NT>
+cudaError_t launch_n(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ, bool halfK,
+                     cudaStream_t s)
+{
+    if (halfQ && halfK) return launch_m<NT, __half, __half>(a, m, method, limiter, s);
+    if (halfQ) return launch_m<NT, __half, float>(a, m, method, limiter, s);
+    return launch_m<NT, float, float>(a, m, method, limiter, s);
+}
+
+template <int NT>
+size_t smem_n(bool halfQ, bool halfK, int nk)
+{
+    if (halfQ && halfK) return Smem<NT, __half, __half>::bytes(nk);
+    if (halfQ) return Smem<NT, __half, float>::bytes(nk);
+    return Smem<NT, float, float>::bytes(nk);
+}
+
+}  // namespace
+
+cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
+                           bool halfK, cudaStream_t s)
+{
+    if (a.nt == 4) return launch_n<4>(a, m, method, limiter, halfQ, halfK, s);
+    if (a.nt == 2) return launch_n<2>(a, m, method, limiter, halfQ, halfK, s);
+    if (a.nt == 1) return launch_n<1>(a, m, method, limiter, halfQ, halfK, s);
+    return cudaErrorInvalidValue;
+}
+
+size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk)
+{
+    if (nt == 4) return smem_n<4>(halfQ, halfK, nk);
+    if (nt == 2) return smem_n<2>(halfQ, halfK, nk);
+    return smem_n<1>(halfQ, halfK, nk);
+}
+
+// box extents of the tensor maps (elements), for the host-side encoder
+void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4])
+{
+    const int qyX = halfQ ? Box<__half>::qyX : Box<float>::qyX;
+    const int visX = halfK ? Box<__half>::visX : Box<float>::visX;
+    const int b[13][4] = {{PBX, TY + 4, 1, nt}, {FBX, TY + 4, 1, 1}, {VBX, TY + 2, 1, 1},
+                          {visX, TY + 2, 1, 1}, {TX, TY + 1, 1, 1},   {TX, TY + 1, 1, 1},
+                          {qyX, TY, 1, 1},      {AVX, TY, 1, 1},      {OWN, TY, 1, 1},
+                          {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1},
+                          {OWN, TY, 1, 1}};
+    for (int q = 0; q < 13; ++q)
+        for (int d = 0; d < 4; ++d) box[q][d] = b[q][d];
+}
+
+}  // namespace mohid
