@@ -304,6 +304,33 @@ int mohid_thomasz_f64(const int* ILB, const int* IUB, const int* JLB, const int*
                       const double* D, const double* E, const double* F,
                       const double* TI, double* RES, const int* WaterPoints, int* stat);
 
+/* ======================================================================== */
+/* Mass budget without allocation                                            */
+/* ======================================================================== */
+
+/*
+ * No counterpart in the reference.  Global mass budget of one property:
+ * Neumaier-compensated FP64 sum of VolumeZ * PROP over the water cells
+ * (WaterPoints3D == 1) of the work box, written to *mass.  All pointers are
+ * device pointers over the Size box (0:IUB, 0:JUB, 0:KUB of `size`); the call is
+ * asynchronous on `stream` (a cudaStream_t, NULL for the default stream).
+ *
+ * For callers that cannot allocate device memory when they need the budget --
+ * a model whose device memory belongs to another allocator (a caching
+ * allocator that already holds the GPU, or a fixed budget reserved at start-up)
+ * or one that must not synchronise the device inside its time step -- this
+ * entry point allocates nothing: its scratch is a file-scope device array of
+ * 2 x 8192 doubles (128 KiB) that every GPU loading the library holds until the
+ * process exits.  Limit: at most 8192 work-box rows (JUB - 1 <= 8192); larger
+ * grids return MOHID_AD_ERR_BOUNDS.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU (other streams or
+ * other host threads) race; every call overwrites the part it reads, so
+ * nothing needs clearing between calls.
+ */
+int mohid_ad_mass_f64_noalloc(const T_Size3D* size, const double* PROP, const double* VolumeZ,
+                              const int* WaterPoints3D, double* mass, void* stream, int* stat);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,7 @@ CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
     ("batched_kernel.cu", []),
     ("batched_pack.cu", []),
+    ("mass_noalloc.cu", []),
     ("abi.cpp", []),
     ("batched_abi.cpp", []),
 ]
