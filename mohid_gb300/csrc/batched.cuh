@@ -71,6 +71,7 @@ struct BatchArgs {
     long long ts;
     int nt;
     const float* Ref;                   // same layout as tracers (boundary cells read), or null
+    float* W;                           // scratch: THOMASZ W per cell (batched layout)
     // scalars
     float DT, schmidtH, coefV, backV, tdec;
     int nullDif, vertical1D, xzflow;

@@ -41,6 +41,7 @@ struct Batch {
     DevBuf<float> fx, fy, areaCol;
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
+    DevBuf<float> Wsc;                   // THOMASZ W per cell, scratch of the step kernel
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
     // anomaly storage is exact only when the step preserves constants; this
@@ -66,7 +67,7 @@ struct Batch {
     void release()
     {
         DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ, &fx, &fy,
-                              &areaCol, &PA, &PB, &Ref};
+                              &areaCol, &PA, &PB, &Ref, &Wsc};
         for (auto* b : f) b->release();
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
@@ -263,6 +264,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.nt = nt;
     a.t0 = t0;
     a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
+    a.W = b->Wsc.p;
     a.DT = (float)p->DTProp;
     a.schmidtH = (float)p->schmidt_H;
     a.coefV = (float)p->SchmidtCoef_V;
@@ -392,6 +394,7 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->kfloor.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->PA.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->PB.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->Wsc.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");

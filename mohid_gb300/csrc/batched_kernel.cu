@@ -21,7 +21,8 @@
 //    vertical advection + diffusion, AD:2708-2784, AD:3066-3117), so each row
 //    is factorised once (W, 1/pivot) and every tracer only runs
 //    G = (TI - D*G_prev) / pivot and the back-substitution (THOMASZ,
-//    FN:4026-4123); W lives in shared memory, G is parked in the output array;
+//    FN:4026-4123); W goes to a per-cell scratch array and G into the output
+//    array, both read back from L2 by the same thread on the way down;
 //  * the volume ratio Vold/V is formed as 1 - (V - Vold)/V with the difference
 //    taken in FP64 (thin layers make it cancel); everything else is FP32;
 //  * rows below KFloor are never touched (they hold null_real, as after any
@@ -96,8 +97,8 @@ struct Smem {
     static constexpr int oCX = oFY + al128(NT * NSF * 4);
     static constexpr int oCY = oCX + al128(6 * NWF * 4);
     static constexpr int oBar = oCY + al128(6 * NSF * 4);
-    static constexpr int oW = oBar + 128;
-    static size_t bytes(int nk) { return (size_t)oW + sizeof(float) * (size_t)(nk + 2) * NTH; }
+    static constexpr int oEnd = oBar + 128;
+    static size_t bytes(int) { return (size_t)oEnd; }
 };
 
 // ---- PTX helpers: mbarrier and bulk tensor copies ---------------------------
@@ -263,7 +264,7 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
 }
 
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
-__global__ void __launch_bounds__(NTH, 2)
+__global__ void __launch_bounds__(NTH, 3)
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
 {
     using SL = StageLayout<NT, QT, KT>;
@@ -275,7 +276,6 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     float* CY = reinterpret_cast<float*>(smem_raw + SM::oCY);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::oBar);
     int* kminp = reinterpret_cast<int*>(smem_raw + SM::oBar + 32);
-    float* Wcol = reinterpret_cast<float*>(smem_raw + SM::oW);
 
     const BLayout& L = A.L;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -443,7 +443,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
             float inv;
             if (aux != 0.f) inv = 1.f / aux; else { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
             const float W = -Fc * inv;
-            Wcol[k * NTH + tid] = W;
+            A.W[a] = W;                                  // read back by the back-substitution
             Wp = W;
             const float* P = reinterpret_cast<const float*>(st + SL::oP);
             const int po = (ty + 2) * PBX + tx + 4;
@@ -468,25 +468,35 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         if (tid == 0 && k + 2 <= L.nk) issue(k + 2, s);
     }
 
-    // ---- back-substitution (row KUB+1 solves to 0), G loads issued 8 rows at a time
+    // ---- back-substitution (row KUB+1 solves to 0); W and G loads are issued
+    //      8 rows at a time, all tracers of the column together
     if (solve) {
-#pragma unroll 1
-        for (int t = 0; t < NT; ++t) {
-            float x = 0.f;
-            float* Po = A.Pout + (long long)t * A.ts + cb;
-            for (int k = L.nk; k >= kb; k -= 8) {
-                float g[8];
+        float x[NT];
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (k - q >= kb) g[q] = __ldcg(Po + (long long)(k - q) * L.sl);
+        for (int t = 0; t < NT; ++t) x[t] = 0.f;
+        const float* Wc = A.W + cb;
+        float* Po = A.Pout + cb;
+        for (int k = L.nk; k >= kb; k -= 8) {
+            float w[8], g[NT][8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (k - q >= kb) {
-                        x = Wcol[(k - q) * NTH + tid] * x + g[q];
-                        Po[(long long)(k - q) * L.sl] = x;
-                        if (!isfinite(x)) bad |= MOHID_DEV_NONFINITE;
+            for (int q = 0; q < 8; ++q)
+                if (k - q >= kb) {
+                    const long long o = (long long)(k - q) * L.sl;
+                    w[q] = __ldcg(Wc + o);
+#pragma unroll
+                    for (int t = 0; t < NT; ++t) g[t][q] = __ldcg(Po + (long long)t * A.ts + o);
+                }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (k - q >= kb) {
+                    const long long o = (long long)(k - q) * L.sl;
+#pragma unroll
+                    for (int t = 0; t < NT; ++t) {
+                        x[t] = w[q] * x[t] + g[t][q];
+                        Po[(long long)t * A.ts + o] = x[t];
+                        if (!isfinite(x[t])) bad |= MOHID_DEV_NONFINITE;
                     }
-            }
+                }
         }
     }
     if (bad) atomicOr(A.status, bad);
