@@ -53,7 +53,8 @@ struct BatchArgs {
     // shared per-cell fields in the batched layout
     const void *Qx, *Qy, *Qz;           // float or __half (west, south, bottom faces)
     float qsx, qsy, qsz;                // scales for __half storage
-    const double *V, *Vold;
+    const float *V;                     // VolumeZ (FP32 copy)
+    const float *DVR;                   // (VolumeZ - VolumeZOld)/VolumeZ, formed in FP64
     const void *ViscH, *DiffV;          // float or __half
     float ksh, ksv;                     // scales for __half storage
     const float *AreaU, *AreaV, *DZZ;   // DZZ holds 1/DZZ
@@ -83,11 +84,11 @@ struct BatchArgs {
 struct TmaMaps {
     CUtensorMap P;                      // tracers (x, y, z, tracer): box (40, TY+4, 1, NT)
     CUtensorMap F;                      // cell flags: box (64, TY+4, 1)
-    CUtensorMap V;                      // VolumeZ, f64: box (36, TY+2, 1)
+    CUtensorMap V;                      // VolumeZ, f32: box (40, TY+2, 1)
     CUtensorMap Vis;                    // Visc_H: box (40 | 48, TY+2, 1)
     CUtensorMap QX, AU;                 // west faces: box (32, TY+1, 1)
     CUtensorMap QY, AV;                 // south faces: box (36 | 40, TY, 1), (36, TY, 1)
-    CUtensorMap Vo;                     // VolumeZOld, f64, own cells: box (32, TY, 1)
+    CUtensorMap Vo;                     // (V - Vold)/V, f32, own cells: box (32, TY, 1)
     CUtensorMap Qz, Dv, Dz, Fn;         // own cells of the layer above / 1/DZZ: box (32, TY, 1)
 };
 
@@ -126,8 +127,10 @@ cudaError_t continuity_residual(const double* Qx, const double* Qy, const double
                                 double* out, cudaStream_t s);
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s);
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);
+// V: VolumeZ in the Fortran Size-box layout (FP64)
 cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
                          const BLayout& L, double* partial, int nblocks, cudaStream_t s);
+cudaError_t pack_dvr(const double* V, const double* Vold, float* dst, const BLayout& L, cudaStream_t s);
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s);
 
 }  // namespace mohid

@@ -35,7 +35,7 @@ struct Batch {
     DevBuf<float> Qx32, Qy32, Qz32, Vis32, Dif32;
     DevBuf<__half> Qx16, Qy16, Qz16, Vis16, Dif16;
     float qsx = 1, qsy = 1, qsz = 1, ksh = 1, ksv = 1;
-    DevBuf<double> V, Vold;
+    DevBuf<float> V, DVR;                // FP32 VolumeZ, (V - Vold)/V formed in FP64
     DevBuf<float> AreaU, AreaV, DZZ;
     DevBuf<uint8_t> flag, cflag;
     DevBuf<float> fx, fy, areaCol;
@@ -71,7 +71,7 @@ struct Batch {
         for (auto* b : f) b->release();
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
-        V.release(); Vold.release(); flag.release(); cflag.release(); kfloor.release();
+        V.release(); DVR.release(); flag.release(); cflag.release(); kfloor.release();
         partial.release(); scratch.release(); stage.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
@@ -187,8 +187,8 @@ int pack_hydro(Batch* b, int* stat)
         CK(mohid::pack_f64_to_f32(in->ViscH.p, b->Vis32.p, L, in->nk + 2, s));
         CK(mohid::pack_f64_to_f32(in->DiffV.p, b->Dif32.p, L, in->nk + 2, s));
     }
-    CK(mohid::pack_f64_to_f64(in->V.p, b->V.p, L, s));
-    CK(mohid::pack_f64_to_f64(in->Vold.p, b->Vold.p, L, s));
+    CK(mohid::pack_f64_to_f32(in->V.p, b->V.p, L, in->nk + 2, s));
+    CK(mohid::pack_dvr(in->V.p, in->Vold.p, b->DVR.p, L, s));
     CK(mohid::pack_f64_to_f32(in->AreaU.p, b->AreaU.p, L, in->nk + 2, s));
     CK(mohid::pack_f64_to_f32(in->AreaV.p, b->AreaV.p, L, in->nk + 2, s));
     CK(mohid::pack_recip_f32(in->DZZ.p, b->DZZ.p, L, s));
@@ -213,13 +213,13 @@ int pack_hydro(Batch* b, int* stat)
         bool okm = true;
         mohid::TmaMaps& M = b->maps;
         okm &= encode_map(&M.F, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[1]);
-        okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b->V.p, L, 1, box[2]);
+        okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->V.p, L, 1, box[2]);
         okm &= encode_map(&M.Vis, tk, ek, vis, L, 1, box[3]);
         okm &= encode_map(&M.QX, tq, eq, qx, L, 1, box[4]);
         okm &= encode_map(&M.AU, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->AreaU.p, L, 1, box[5]);
         okm &= encode_map(&M.QY, tq, eq, qy, L, 1, box[6]);
         okm &= encode_map(&M.AV, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->AreaV.p, L, 1, box[7]);
-        okm &= encode_map(&M.Vo, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b->Vold.p, L, 1, box[8]);
+        okm &= encode_map(&M.Vo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DVR.p, L, 1, box[8]);
         okm &= encode_map(&M.Qz, tq, eq, qz, L, 1, box[9]);
         okm &= encode_map(&M.Dv, tk, ek, dif, L, 1, box[10]);
         okm &= encode_map(&M.Dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DZZ.p, L, 1, box[11]);
@@ -251,7 +251,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Qy = hq ? (const void*)b->Qy16.p : (const void*)b->Qy32.p;
     a.Qz = hq ? (const void*)b->Qz16.p : (const void*)b->Qz32.p;
     a.qsx = b->qsx; a.qsy = b->qsy; a.qsz = b->qsz;
-    a.V = b->V.p; a.Vold = b->Vold.p;
+    a.V = b->V.p; a.DVR = b->DVR.p;
     a.ViscH = hk ? (const void*)b->Vis16.p : (const void*)b->Vis32.p;
     a.DiffV = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
     a.ksh = b->ksh; a.ksv = b->ksv;
@@ -385,7 +385,7 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     DevBuf<float>* f3[] = {&b->AreaU, &b->AreaV, &b->DZZ};
     for (auto* x : f3) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->V.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->Vold.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->DVR.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->flag.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->cflag.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->fx.alloc(6 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
@@ -563,7 +563,7 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     }
     cudaStream_t s = in->stream;
     const float* P = b->cur_in() + (long long)*t * b->L.n3;
-    CK(mohid::mass_batched(P, b->V.p, b->flag.p, b->shift[*t], b->L, b->partial.p, kMassBlocks, s));
+    CK(mohid::mass_batched(P, in->V.p, b->flag.p, b->shift[*t], b->L, b->partial.p, kMassBlocks, s));
     CK(mohid::mass_finish(b->partial.p, kMassBlocks, b->scratch.p, s));
     CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

@@ -23,8 +23,10 @@
 //    G = (TI - D*G_prev) / pivot and the back-substitution (THOMASZ,
 //    FN:4026-4123); W goes to a per-cell scratch array and G into the output
 //    array, both read back from L2 by the same thread on the way down;
-//  * the volume ratio Vold/V is formed as 1 - (V - Vold)/V with the difference
-//    taken in FP64 (thin layers make it cancel); everything else is FP32;
+//  * the volume ratio Vold/V is applied as 1 - (V - Vold)/V, the relative
+//    change being formed in FP64 when the volumes are packed (thin layers make
+//    the difference cancel); the kernel itself runs no FP64 arithmetic, which
+//    GB300 issues at a small fraction of the FP32 rate;
 //  * rows below KFloor are never touched (they hold null_real, as after any
 //    reference step), so a z-level column costs what it holds.
 //
@@ -43,10 +45,10 @@ constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
 
 // ---- TMA stage layout -------------------------------------------------------
 // Box origins sit on 16-byte boundaries of the batched layout (x = i + 31):
-// the tracer tile starts 4 cells before i0, the flag tile 16 cells before, the
-// FP64 volume tile 2 cells before, the viscosity tile 4 (FP32) or 8 (FP16)
-// cells before; face and own-cell tiles start at i0.
-constexpr int PBX = 40, FBX = 64, VBX = 36, OWN = 32, AVX = 36;
+// the tracer and volume tiles start 4 cells before i0, the flag tile 16 cells
+// before, the viscosity tile 4 (FP32) or 8 (FP16) cells before; face and
+// own-cell tiles start at i0.
+constexpr int PBX = 40, FBX = 64, VBX = 40, OWN = 32, AVX = 36;
 template <typename T> struct Box;
 template <> struct Box<float> { static constexpr int visX = 40, visOff = 4, qyX = 36; };
 template <> struct Box<__half> { static constexpr int visX = 48, visOff = 8, qyX = 40; };
@@ -58,13 +60,13 @@ struct StageLayout {
     static constexpr int qyX = Box<QT>::qyX, visX = Box<KT>::visX;
     static constexpr int bP = NT * (TY + 4) * PBX * 4;
     static constexpr int bF = (TY + 4) * FBX;
-    static constexpr int bV = (TY + 2) * VBX * 8;
+    static constexpr int bV = (TY + 2) * VBX * 4;
     static constexpr int bVis = (TY + 2) * visX * (int)sizeof(KT);
     static constexpr int bQX = (TY + 1) * TX * (int)sizeof(QT);
     static constexpr int bAU = (TY + 1) * TX * 4;
     static constexpr int bQY = TY * qyX * (int)sizeof(QT);
     static constexpr int bAV = TY * AVX * 4;
-    static constexpr int bVo = TY * OWN * 8;
+    static constexpr int bVo = TY * OWN * 4;
     static constexpr int bQz = TY * OWN * (int)sizeof(QT);
     static constexpr int bDv = TY * OWN * (int)sizeof(KT);
     static constexpr int bDz = TY * OWN * 4;
@@ -194,11 +196,11 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
     constexpr int cs = WEST ? NWF : NSF;
     const float* P = reinterpret_cast<const float*>(st + SL::oP);
     const uint8_t* Fl = st + SL::oF;
-    const double* Vt = reinterpret_cast<const double*>(st + SL::oV);
+    const float* Vt = reinterpret_cast<const float*>(st + SL::oV);
     const KT* Vis = reinterpret_cast<const KT*>(st + SL::oVis);
     const int pb = (a + 2) * PBX + b + 4;
     const int fb = (a + 2) * FBX + b + 16;
-    const int vb = (a + 1) * VBX + b + 2;
+    const int vb = (a + 1) * VBX + b + 4;
     const int visb = (a + 1) * Box<KT>::visX + b + Box<KT>::visOff;
     const int fi = WEST ? a * TX + b : a * (TX + 1) + b;
     float q, area;
@@ -229,7 +231,7 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
         const int fuu = pos ? fb - 2 * fst : fb + fst;
         if (Fl[fuu] & F_OP) {                      // not near a boundary
             tvd = true;
-            const float vup = (float)Vt[pos ? vb - vst : vb];
+            const float vup = Vt[pos ? vb - vst : vb];
             float Cr = __fdividef(q * A.DT, vup);
             gdn = cc[4 * cs];
             gup = pos ? cc[3 * cs] : cc[5 * cs];
@@ -264,7 +266,7 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
 }
 
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
-__global__ void __launch_bounds__(NTH, 3)
+__global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
 {
     using SL = StageLayout<NT, QT, KT>;
@@ -308,7 +310,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     if (kmin > L.nk) return;                       // no water column in this tile
 
     // TMA box origins (x on 16-byte boundaries of the batched layout)
-    const int xP = i0 + kXOff - 4, xF = i0 + kXOff - 16, xV = i0 + kXOff - 2;
+    const int xP = i0 + kXOff - 4, xF = i0 + kXOff - 16, xV = i0 + kXOff - 4;
     const int xVis = i0 + kXOff - Box<KT>::visOff, xO = i0 + kXOff;
     const int yP = j0 + kYOff - 2, yV = j0 + kYOff - 1, yO = j0 + kYOff;
     auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
@@ -387,16 +389,17 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
             const int fo = (ty + 2) * FBX + tx + 16;
             const uint8_t fl = Fl[fo];
             const uint8_t flp = (k < L.nk) ? (st + SL::oFn)[own] : 0;
-            const double Vd = reinterpret_cast<const double*>(st + SL::oV)[(ty + 1) * VBX + tx + 2];
-            const double Vod = reinterpret_cast<const double*>(st + SL::oVo)[own];
+            const float Vk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
+            const float dvr = reinterpret_cast<const float*>(st + SL::oVo)[own];   // (V - Vold)/V
             const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
             const float dvp = (k < L.nk) ? tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) : 0.f;
             const float dzz = reinterpret_cast<const float*>(st + SL::oDz)[own];
-            const float Vk = (float)Vd;
-            const float dtv = DT / Vk;
+            const float rV = __frcp_rn(Vk);
+            const float dtv = DT * rV;
             const bool open = fl & F_OP;
-            // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term
-            const float ratio = open ? 1.f - (float)(Vd - Vod) / Vk : 1.f;
+            // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term;
+            // (V-Vold)/V was formed in FP64 when the volumes were packed
+            const float ratio = open ? 1.f - dvr : 1.f;
             float E = 1.f, D = 0.f, Fc = 0.f;
             if (open && k == L.nk) E = 1.f + dtv * qzp;
             if (L.nk > 1) {
@@ -435,13 +438,13 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
                              ((fl & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
                              ((Fl[fo + 1] & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
                              ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
-                wfob = (float)(hz - (Vd - Vod) / (double)DT);
+                wfob = (float)(hz - (double)(dvr * Vk) / (double)DT);
                 if (wfob >= 0.f) E += wfob * dtv;
             }
             // THOMASZ factorisation of row k
             const float aux = E + D * Wp;
             float inv;
-            if (aux != 0.f) inv = 1.f / aux; else { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
+            if (aux != 0.f) inv = __frcp_rn(aux); else { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
             const float W = -Fc * inv;
             A.W[a] = W;                                  // read back by the back-substitution
             Wp = W;

@@ -120,6 +120,19 @@ __global__ void k_unshift(float* P, const uint8_t* flag, double shift, long long
         if (flag[e] & F_WP) P[e] = (float)((double)P[e] + shift);
 }
 
+// relative volume change (V - Vold)/V formed in FP64, stored as FP32
+__global__ void k_pack_dvr(const double* __restrict__ V, const double* __restrict__ Vo, float* __restrict__ dst,
+                           BLayout L)
+{
+    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % (L.ni + 2));
+        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
+        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
+        dst[L.at(i, j, k)] = V[e] != 0.0 ? (float)((V[e] - Vo[e]) / V[e]) : 0.f;
+    }
+}
+
 __global__ void k_pack_f64(const double* __restrict__ src, double* __restrict__ dst, BLayout L)
 {
     const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
@@ -284,7 +297,8 @@ __global__ void k_mass(const float* P, const double* V, const uint8_t* flag, dou
         const int j = 1 + (int)((e / L.ni) % L.nj);
         const int k = 1 + (int)(e / ((long long)L.ni * L.nj));
         const long long g = L.at(i, j, k);
-        if (flag[g] & F_WP) neu_add(s, c, V[g] * ((double)P[g] + shift));
+        const long long f = i + (long long)(L.ni + 2) * (j + (long long)(L.nj + 2) * k);
+        if (flag[g] & F_WP) neu_add(s, c, V[f] * ((double)P[g] + shift));
     }
     ss[threadIdx.x] = s; sc[threadIdx.x] = c;
     __syncthreads();
@@ -320,6 +334,11 @@ cudaError_t pack_recip_f32(const double* src, float* dst, const BLayout& L, cuda
 cudaError_t pack_f64_to_f16(const double* src, __half* dst, float inv, const BLayout& L, cudaStream_t s)
 {
     k_pack_f16<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, inv, L);
+    return cudaGetLastError();
+}
+cudaError_t pack_dvr(const double* V, const double* Vold, float* dst, const BLayout& L, cudaStream_t s)
+{
+    k_pack_dvr<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(V, Vold, dst, L);
     return cudaGetLastError();
 }
 cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s)
