@@ -235,7 +235,8 @@ def run_plain(w, d, tracers, steps, warmup, world):
     ad.kill()
     cells = d.ni * d.nj * d.nk
     return dict(ms=ms, kernel_ms=ms / nt, launches=steps * nt, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
-                cells=cells, nt=nt, bytes_per_update=96.0, dtype="f64", clocks=clocks,
+                cells=cells, nt=nt, bytes_per_update=96.0, bytes_per_launch=96.0 * cells, dtype="f64",
+                clocks=clocks,
                 kernel="plain_f64_kernel")
 
 
@@ -270,7 +271,11 @@ def run_batched(w, d, tracers, steps, warmup, world, storage=0):
     clocks = clk.stop()
     ms = e0.elapsed_time(e1) / steps
     barrier(world)
-    launches = steps * ((nt + 3) // 4 if nt >= 4 else 1)
+    groups, left = 0, nt                       # launches per step: groups of 4, 2, 1 tracers
+    while left > 0:
+        left -= 4 if left >= 4 else (2 if left >= 2 else 1)
+        groups += 1
+    launches = steps * groups
 
     # e2e: a host-resident caller sends the step's hydrodynamics and tracers,
     # runs the step through the C-ABI and reads the tracers back, every step
@@ -299,8 +304,10 @@ def run_batched(w, d, tracers, steps, warmup, world, storage=0):
     ad.kill()
     cells = d.ni * d.nj * d.nk
     shared = {0: 48.0, 1: 42.0, 2: 38.0}[storage]
-    return dict(ms=ms, kernel_ms=ms, launches=launches, e2e_s=e2e_s, h2d=h2d, d2h=d2h, cells=cells,
-                nt=nt, bytes_per_update=8.0 + shared / nt, dtype="f32", clocks=clocks,
+    # one launch per step when nt <= 2 or nt == 4: the launch moves cells * (8 nt + shared) bytes
+    return dict(ms=ms, kernel_ms=ms / groups, launches=launches, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
+                cells=cells, nt=nt, bytes_per_update=8.0 + shared / nt,
+                bytes_per_launch=cells * (8.0 * nt + shared) / groups, dtype="f32", clocks=clocks,
                 kernel="batched_kernel<2,P2_TVD,SuperBee>")
 
 
@@ -326,7 +333,7 @@ def main():
     tracers = [d.tracer(k, a, b, seed=100 + t) for t, (k, a, b) in enumerate(w.tracers)]
     cells = d.ni * d.nj * d.nk
     unit = "cell-tracer-updates/s"
-    metric = "cell-tracer-updates/s (FP32 batched vs FP64 plain, 1 GB300)"
+    metric = "cell-tracer-updates/s, FP32 batched vs FP64 plain on 1 GB300 at \u22641e-5 rel L2; HBM GB/s"
 
     if args.impl == "reference":
         if rank != 0:
@@ -369,7 +376,7 @@ def main():
     e2e_s = max_over_ranks(r["e2e_s"], world)
     e2e_value = world * cells * r["nt"] / e2e_s
     peak, peak_kind = load_peaks()
-    achieved = r["bytes_per_update"] * cells / (r["kernel_ms"] / 1e3) / 1e9
+    achieved = r["bytes_per_launch"] / (r["kernel_ms"] / 1e3) / 1e9
     traffic = TRAFFIC.get(r["kernel"])
     if rank != 0:
         return
@@ -386,7 +393,8 @@ def main():
                    "l2": f"inputs larger than L2 ({resident / 2**30:.2f} GiB resident per step > 129 MiB)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
+                     "bytes_per_launch": r["bytes_per_launch"],
                      "kernel": r["kernel"], "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "bytes_per_update": r["bytes_per_update"]},
@@ -404,8 +412,13 @@ def main():
     print(json.dumps(line))
 
 
-# DRAM bytes per launch of the dominant kernel from one ncu capture (profiles/), or None.
-TRAFFIC: dict = {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# dominant kernel, from one ncu capture of the 512x512x40 two-tracer workload
+# (profiles/batched_kernel_512x512x40_2tracers.md, profiles/plain_f64_kernel_512x512x40.md).
+TRAFFIC: dict = {
+    "batched_kernel<2,P2_TVD,SuperBee>": 644.790272e6 + 145.795840e6,
+    "plain_f64_kernel": 1181.614e6 + 139.056384e6,
+}
 
 if __name__ == "__main__":
     main()
