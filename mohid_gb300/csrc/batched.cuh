@@ -19,6 +19,12 @@ constexpr int kTY = 8;    // tile height along j (warps per CTA)
 constexpr uint8_t F_WP = 1, F_OP = 2, F_CFU = 4, F_CFV = 8, F_CFW = 16, F_LP = 32;
 // column flag bits
 constexpr uint8_t C_SOLVE = 1, C_OPTOP = 2, C_CFWTOP = 4, C_BP = 8, C_SD = 16;
+// face flag bits of a cell's west (U: between j-1 and j) and south (V: between
+// i-1 and i) faces: ACT the face is a compute face (ComputeFacesU/V3D), ADV it
+// also carries advection (both cells open), TVDP/TVDN the cell upstream of the
+// upwind cell is open for a positive/negative transport (not NearBoundary)
+constexpr uint8_t FU_ACT = 1, FU_ADV = 2, FU_TVDP = 4, FU_TVDN = 8;
+constexpr uint8_t FV_ACT = 16, FV_ADV = 32, FV_TVDP = 64, FV_TVDN = 128;
 
 struct BLayout {
     int ni, nj, nk;
@@ -53,16 +59,18 @@ struct BatchArgs {
     // shared per-cell fields in the batched layout
     const void *Qx, *Qy, *Qz;           // float or __half (west, south, bottom faces)
     float qsx, qsy, qsz;                // scales for __half storage
-    const float *V;                     // VolumeZ (FP32 copy)
+    const float *RV;                    // 1/VolumeZ, formed in FP64 (0 where VolumeZ = 0)
     const float *DVR;                   // (VolumeZ - VolumeZOld)/VolumeZ, formed in FP64
     const void *ViscH, *DiffV;          // float or __half
     float ksh, ksv;                     // scales for __half storage
     const float *AreaU, *AreaV, *DZZ;   // DZZ holds 1/DZZ
     const uint8_t* flag;
-    // 2-D: per-face constants [6][py][px] for west (fx) and south (fy) faces:
-    //   0: weight of the cell's own Visc, 1: weight of the neighbour's Visc
-    //   2: 1/DZ between the two centres, 3: g_upup (Q > 0), 4: g_dn, 5: g_upup (Q <= 0)
-    const float *fx, *fy;
+    const uint8_t* fflag;               // face flag bits (FU_*, FV_*)
+    // 2-D: per-face constants [2][py][px] for west (0) and south (1) faces:
+    //   x: weight of the cell's own Visc / DZ between the centres
+    //   y: weight of the neighbour's Visc / DZ between the centres
+    //   z: (du_up + du_dn) / (du_up + du_upup) for Q > 0, w: the same for Q <= 0
+    const float4* fc;
     const float* areaCol;               // DUX * DVY
     const int* kfloor;
     const uint8_t* cflag;
@@ -83,8 +91,8 @@ struct BatchArgs {
 // Tensor maps of one launch: one tiled bulk copy per field and layer.
 struct TmaMaps {
     CUtensorMap P;                      // tracers (x, y, z, tracer): box (40, TY+4, 1, NT)
-    CUtensorMap F;                      // cell flags: box (64, TY+4, 1)
-    CUtensorMap V;                      // VolumeZ, f32: box (40, TY+2, 1)
+    CUtensorMap F;                      // face flags: box (48, TY+1, 1)
+    CUtensorMap V;                      // 1/VolumeZ, f32: box (40, TY+2, 1)
     CUtensorMap Vis;                    // Visc_H: box (40 | 48, TY+2, 1)
     CUtensorMap QX, AU;                 // west faces: box (32, TY+1, 1)
     CUtensorMap QY, AV;                 // south faces: box (36 | 40, TY, 1), (36, TY, 1)
@@ -105,9 +113,11 @@ cudaError_t pack_f64_to_f16(const double* src, __half* dst, float invScale, cons
 cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s);
 cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,
                        const int* LP, uint8_t* dst, const BLayout& L, cudaStream_t s);
+cudaError_t pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, const BLayout& L,
+                            cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
-                         const int* CFW, const int* SD, float* fx, float* fy, float* areaCol,
+                         const int* CFW, const int* SD, float4* fc, float* areaCol,
                          int* kfloor, uint8_t* cflag, const BLayout& L, cudaStream_t s);
 // Tracers are held as the anomaly P - shift on water cells (shift: a per-tracer
 // constant, the mean over water cells): when the step preserves constants it is

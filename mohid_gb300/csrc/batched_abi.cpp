@@ -35,10 +35,11 @@ struct Batch {
     DevBuf<float> Qx32, Qy32, Qz32, Vis32, Dif32;
     DevBuf<__half> Qx16, Qy16, Qz16, Vis16, Dif16;
     float qsx = 1, qsy = 1, qsz = 1, ksh = 1, ksv = 1;
-    DevBuf<float> V, DVR;                // FP32 VolumeZ, (V - Vold)/V formed in FP64
+    DevBuf<float> RV, DVR;               // 1/V and (V - Vold)/V, both formed in FP64
     DevBuf<float> AreaU, AreaV, DZZ;
-    DevBuf<uint8_t> flag, cflag;
-    DevBuf<float> fx, fy, areaCol;
+    DevBuf<uint8_t> flag, fflag, cflag;
+    DevBuf<float4> fc;
+    DevBuf<float> areaCol;
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
     DevBuf<float> Wsc;                   // THOMASZ W per cell, scratch of the step kernel
@@ -66,12 +67,13 @@ struct Batch {
 
     void release()
     {
-        DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ, &fx, &fy,
+        DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ,
                               &areaCol, &PA, &PB, &Ref, &Wsc};
         for (auto* b : f) b->release();
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
-        V.release(); DVR.release(); flag.release(); cflag.release(); kfloor.release();
+        RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
+        kfloor.release();
         partial.release(); scratch.release(); stage.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
@@ -187,15 +189,16 @@ int pack_hydro(Batch* b, int* stat)
         CK(mohid::pack_f64_to_f32(in->ViscH.p, b->Vis32.p, L, in->nk + 2, s));
         CK(mohid::pack_f64_to_f32(in->DiffV.p, b->Dif32.p, L, in->nk + 2, s));
     }
-    CK(mohid::pack_f64_to_f32(in->V.p, b->V.p, L, in->nk + 2, s));
+    CK(mohid::pack_recip_f32(in->V.p, b->RV.p, L, s));
     CK(mohid::pack_dvr(in->V.p, in->Vold.p, b->DVR.p, L, s));
     CK(mohid::pack_f64_to_f32(in->AreaU.p, b->AreaU.p, L, in->nk + 2, s));
     CK(mohid::pack_f64_to_f32(in->AreaV.p, b->AreaV.p, L, in->nk + 2, s));
     CK(mohid::pack_recip_f32(in->DZZ.p, b->DZZ.p, L, s));
     CK(mohid::pack_flags(in->WP.p, in->OP.p, in->CFU.p, in->CFV.p, in->CFW.p, in->LP.p, b->flag.p, L, s));
+    CK(mohid::pack_face_flags(in->OP.p, in->CFU.p, in->CFV.p, b->fflag.p, L, s));
     CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
-                           b->fx.p, b->fy.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
+                           b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
     CK(cudaStreamSynchronize(s));
     // tensor maps of the shared fields and of the tracer buffers
     {
@@ -212,8 +215,8 @@ int pack_hydro(Batch* b, int* stat)
         const void* dif = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
         bool okm = true;
         mohid::TmaMaps& M = b->maps;
-        okm &= encode_map(&M.F, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[1]);
-        okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->V.p, L, 1, box[2]);
+        okm &= encode_map(&M.F, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->fflag.p, L, 1, box[1]);
+        okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->RV.p, L, 1, box[2]);
         okm &= encode_map(&M.Vis, tk, ek, vis, L, 1, box[3]);
         okm &= encode_map(&M.QX, tq, eq, qx, L, 1, box[4]);
         okm &= encode_map(&M.AU, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->AreaU.p, L, 1, box[5]);
@@ -251,13 +254,14 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Qy = hq ? (const void*)b->Qy16.p : (const void*)b->Qy32.p;
     a.Qz = hq ? (const void*)b->Qz16.p : (const void*)b->Qz32.p;
     a.qsx = b->qsx; a.qsy = b->qsy; a.qsz = b->qsz;
-    a.V = b->V.p; a.DVR = b->DVR.p;
+    a.RV = b->RV.p; a.DVR = b->DVR.p;
     a.ViscH = hk ? (const void*)b->Vis16.p : (const void*)b->Vis32.p;
     a.DiffV = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
     a.ksh = b->ksh; a.ksv = b->ksv;
     a.AreaU = b->AreaU.p; a.AreaV = b->AreaV.p; a.DZZ = b->DZZ.p;
     a.flag = b->flag.p;
-    a.fx = b->fx.p; a.fy = b->fy.p; a.areaCol = b->areaCol.p; a.kfloor = b->kfloor.p; a.cflag = b->cflag.p;
+    a.fflag = b->fflag.p;
+    a.fc = b->fc.p; a.areaCol = b->areaCol.p; a.kfloor = b->kfloor.p; a.cflag = b->cflag.p;
     a.ts = b->L.n3;
     a.Pin = Pin + (long long)t0 * a.ts;
     a.Pout = Pout + (long long)t0 * a.ts;
@@ -384,12 +388,12 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     }
     DevBuf<float>* f3[] = {&b->AreaU, &b->AreaV, &b->DZZ};
     for (auto* x : f3) if ((e = x->alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->V.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->RV.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->DVR.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->flag.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->fflag.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->cflag.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->fx.alloc(6 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->fy.alloc(6 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->fc.alloc(2 * n2)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->areaCol.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->kfloor.alloc(n2)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->PA.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");

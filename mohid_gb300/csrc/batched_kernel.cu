@@ -45,10 +45,9 @@ constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
 
 // ---- TMA stage layout -------------------------------------------------------
 // Box origins sit on 16-byte boundaries of the batched layout (x = i + 31):
-// the tracer and volume tiles start 4 cells before i0, the flag tile 16 cells
-// before, the viscosity tile 4 (FP32) or 8 (FP16) cells before; face and
-// own-cell tiles start at i0.
-constexpr int PBX = 40, FBX = 64, VBX = 40, OWN = 32, AVX = 36;
+// the tracer and 1/V tiles start 4 cells before i0, the viscosity tile 4 (FP32)
+// or 8 (FP16) cells before; face, face-flag and own-cell tiles start at i0.
+constexpr int PBX = 40, FBX = 48, VBX = 40, OWN = 32, AVX = 36;
 template <typename T> struct Box;
 template <> struct Box<float> { static constexpr int visX = 40, visOff = 4, qyX = 36; };
 template <> struct Box<__half> { static constexpr int visX = 48, visOff = 8, qyX = 40; };
@@ -59,7 +58,7 @@ template <int NT, typename QT, typename KT>
 struct StageLayout {
     static constexpr int qyX = Box<QT>::qyX, visX = Box<KT>::visX;
     static constexpr int bP = NT * (TY + 4) * PBX * 4;
-    static constexpr int bF = (TY + 4) * FBX;
+    static constexpr int bF = (TY + 1) * FBX;
     static constexpr int bV = (TY + 2) * VBX * 4;
     static constexpr int bVis = (TY + 2) * visX * (int)sizeof(KT);
     static constexpr int bQX = (TY + 1) * TX * (int)sizeof(QT);
@@ -97,8 +96,8 @@ struct Smem {
     static constexpr int oFX = 2 * SL::size;
     static constexpr int oFY = oFX + al128(NT * NWF * 4);
     static constexpr int oCX = oFY + al128(NT * NSF * 4);
-    static constexpr int oCY = oCX + al128(6 * NWF * 4);
-    static constexpr int oBar = oCY + al128(6 * NSF * 4);
+    static constexpr int oCY = oCX + al128(NWF * 16);
+    static constexpr int oBar = oCY + al128(NSF * 16);
     static constexpr int oEnd = oBar + 128;
     static size_t bytes(int) { return (size_t)oEnd; }
 };
@@ -156,16 +155,24 @@ __device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, int x, i
 }
 constexpr uint32_t kWaitLimit = 1u << 24;
 
+// psi(r) * d for r = n / d, psi one of the ComputeAdvectionFace limiters
+// (FN:10823-10856).  Each min/max of psi(r) is multiplied through by |d|, so
+// with a = |d| and b = n * sign(d) no division is needed (VanLeer keeps one);
+// d = 0 gives 0, as the reference's theta * 0.
+// PDM: pa, pb from |Cr|, p2 = 2/(1-Cr), pcr = 2/Cr.
 template <int LIM>
-__device__ __forceinline__ float limiter(float r, float pa, float pb, float p2, float pcr)
+__device__ __forceinline__ float limited_slope(float n, float d, float pa, float pb, float p2, float pcr)
 {
-    // ComputeAdvectionFace limiters, FN:10823-10856
-    if (LIM == 1) return fmaxf(0.f, fminf(1.f, r));
-    if (LIM == 2) return r < 0.f ? 0.f : 2.f * r / (1.f + r);
-    if (LIM == 3) return fmaxf(0.f, fminf(fminf(2.f, 2.f * r), (1.f + r) * 0.5f));
-    if (LIM == 4) return fmaxf(fmaxf(0.f, fminf(1.f, 2.f * r)), fminf(r, 2.f));
-    // PDM: pa, pb from |Cr|, p2 = 2/(1-Cr'), pcr = 2/Cr'
-    return fmaxf(0.f, fminf(fminf(pa + pb * r, p2), r * pcr));
+    const unsigned sd = __float_as_uint(d) & 0x80000000u;
+    const float a = fabsf(d);
+    const float b = __uint_as_float(__float_as_uint(n) ^ sd);
+    float v;
+    if (LIM == 1) v = fmaxf(0.f, fminf(a, b));                                          // MinMod
+    else if (LIM == 2) v = b > 0.f ? __fdividef(2.f * a * b, a + b) : 0.f;             // VanLeer
+    else if (LIM == 3) v = fmaxf(0.f, fminf(fminf(2.f * a, 2.f * b), 0.5f * (a + b))); // MUSCL
+    else if (LIM == 4) v = fmaxf(fmaxf(0.f, fminf(a, 2.f * b)), fminf(b, 2.f * a));    // SuperBee
+    else v = fmaxf(0.f, fminf(fminf(fmaf(pb, b, pa * a), p2 * a), pcr * b));          // PDM
+    return __uint_as_float(__float_as_uint(v) | sd);
 }
 
 template <typename T> __device__ __forceinline__ float tofl(T v, float s);
@@ -181,25 +188,26 @@ __device__ __forceinline__ float ldg_as(const void* p, long long a, float s)
 // One face of the tile at one layer.  WEST: the face between cells
 // (i0+b, j0+a-1) and (i0+b, j0+a), a = 0..TY; otherwise the face between
 // (i0+b-1, j0+a) and (i0+b, j0+a), b = 0..TX.  Tracer-independent part first
-// (upwind side, Courant number, limiter weights, diffusive conductance), then
-// for every tracer F = q*P_up + (q*theta + kd)*(P_dn - P_up) into shared memory.
+// (upwind side, Courant number, diffusive conductance), then for every tracer
+// F = q*P_up + kd*(P_dn - P_up) + q*c*psi(r)*(P_dn - P_up) into shared memory.
 // Reference face coefficients: ComputeAdvectionFace FN:10702-10894 (upwind,
-// P2_TVD limiters); diffusive flux HorizontalDiffusionXX/YY AD:5185-5196 with
-// Kx from Convert_Visc_Dif_Horizontal AD:2487-2494.
+// P2_TVD limiters, theta = psi*(1-Cr)/2); diffusive flux
+// HorizontalDiffusionXX/YY AD:5185-5196 with Kx from
+// Convert_Visc_Dif_Horizontal AD:2487-2494.
 template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT>
-__device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, const float* CXY,
+__device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, const float4* CXY,
                                           const BatchArgs& A, int a, int b)
 {
     using SL = StageLayout<NT, QT, KT>;
-    constexpr int pst = WEST ? PBX : 1, fst = WEST ? FBX : 1, vst = WEST ? VBX : 1;
+    constexpr int pst = WEST ? PBX : 1, vst = WEST ? VBX : 1;
     constexpr int visst = WEST ? Box<KT>::visX : 1;
     constexpr int cs = WEST ? NWF : NSF;
+    constexpr uint8_t ACT = WEST ? FU_ACT : FV_ACT, ADV = WEST ? FU_ADV : FV_ADV;
+    constexpr uint8_t TVDP = WEST ? FU_TVDP : FV_TVDP, TVDN = WEST ? FU_TVDN : FV_TVDN;
     const float* P = reinterpret_cast<const float*>(st + SL::oP);
-    const uint8_t* Fl = st + SL::oF;
-    const float* Vt = reinterpret_cast<const float*>(st + SL::oV);
+    const float* RVt = reinterpret_cast<const float*>(st + SL::oV);
     const KT* Vis = reinterpret_cast<const KT*>(st + SL::oVis);
     const int pb = (a + 2) * PBX + b + 4;
-    const int fb = (a + 2) * FBX + b + 16;
     const int vb = (a + 1) * VBX + b + 4;
     const int visb = (a + 1) * Box<KT>::visX + b + Box<KT>::visOff;
     const int fi = WEST ? a * TX + b : a * (TX + 1) + b;
@@ -211,57 +219,41 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
         q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQY)[a * SL::qyX + b], A.qsy);
         area = reinterpret_cast<const float*>(st + SL::oAV)[a * AVX + b];
     }
-    const uint8_t fbv = Fl[fb], fav = Fl[fb - fst];
-    const bool act = WEST ? (fbv & F_CFU) != 0 : ((fbv & F_CFV) != 0 && !A.xzflow);
-    const bool adv = act && (fav & F_OP) && (fbv & F_OP);
+    const uint8_t ff = (WEST || !A.xzflow) ? st[SL::oF + a * FBX + b] : 0;
     const bool pos = q > 0.f;
-    const float* cc = CXY + fi;
-    float K = A.schmidtH * (tofl<KT>(Vis[visb], A.ksh) * cc[0] + tofl<KT>(Vis[visb - visst], A.ksh) * cc[cs]);
+    const float4 cf = CXY[fi];                     // Visc weights (Schmidt and 1/DZ folded in), TVD ratios
+    float K = tofl<KT>(Vis[visb], A.ksh) * cf.x + tofl<KT>(Vis[visb - visst], A.ksh) * cf.y;
     if (A.nullDif && q == 0.f) K = 0.f;
-    const float auxK = act ? K * area * cc[2 * cs] : 0.f;
+    const float auxK = (ff & ACT) ? K * area : 0.f;
     const float kd = pos ? -auxK : auxK;
-    const float qv = adv ? q : 0.f;
+    const float qv = (ff & ADV) ? q : 0.f;
     const int pa = pb - pst;
     const int iup = pos ? pa : pb, idn = pos ? pb : pa;
-    int iuu = iup;
-    float c = 0.f, gup = 0.f, gdn = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
-    bool tvd = false;
-    if (METHOD == 4 && adv) {
-        iuu = pos ? pa - pst : pb + pst;
-        const int fuu = pos ? fb - 2 * fst : fb + fst;
-        if (Fl[fuu] & F_OP) {                      // not near a boundary
-            tvd = true;
-            const float vup = Vt[pos ? vb - vst : vb];
-            float Cr = __fdividef(q * A.DT, vup);
-            gdn = cc[4 * cs];
-            gup = pos ? cc[3 * cs] : cc[5 * cs];
-            if (LIM == 5) {
-                const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
-                pa5 = 0.5f + t6;
-                pb5 = 0.5f - t6;
-                if (fabsf(Cr) < 1e-16f) Cr = 1e-16f;
-                p2 = 2.f / (1.f - Cr);
-                pcr = 2.f / Cr;
-            }
-            c = 0.5f * (1.f - Cr);
+    const int iuu = pos ? pa - pst : pb + pst;
+    float gr = 0.f, qvc = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
+    if (METHOD == 4) {
+        const bool tvd = (ff & ADV) && (ff & (pos ? TVDP : TVDN));   // not NearBoundary
+        gr = pos ? cf.z : cf.w;
+        float Cr = q * A.DT * RVt[pos ? vb - vst : vb];
+        if (LIM == 5) {
+            const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
+            pa5 = 0.5f + t6;
+            pb5 = 0.5f - t6;
+            if (fabsf(Cr) < 1e-16f) Cr = 1e-16f;
+            p2 = 2.f / (1.f - Cr);
+            pcr = 2.f / Cr;
         }
+        qvc = tvd ? q * (0.5f - 0.5f * Cr) : 0.f;
     }
     float* out = FXY + fi;
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
         const float* Pt = P + t * (TY + 4) * PBX;
-        const float Pup = Pt[iup], Pdn = Pt[idn];
-        const float dd = Pdn - Pup;
-        float coef = kd;
-        if (METHOD == 4) {
-            const float du = Pup - Pt[iuu];
-            float dC = dd * gdn;
-            if (fabsf(dC) < 1e-16f) dC = copysignf(1e-16f, dC);
-            const float r = __fdividef(du * gup, dC);
-            const float th = tvd ? limiter<LIM>(r, pa5, pb5, p2, pcr) * c : 0.f;
-            coef = fmaf(qv, th, kd);
-        }
-        out[t * cs] = fmaf(coef, dd, qv * Pup);
+        const float Pup = Pt[iup];
+        const float dd = Pt[idn] - Pup;
+        float o = fmaf(kd, dd, qv * Pup);
+        if (METHOD == 4) o = fmaf(qvc, limited_slope<LIM>((Pup - Pt[iuu]) * gr, dd, pa5, pb5, p2, pcr), o);
+        out[t * cs] = o;
     }
 }
 
@@ -274,8 +266,8 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX);
     float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY);
-    float* CX = reinterpret_cast<float*>(smem_raw + SM::oCX);
-    float* CY = reinterpret_cast<float*>(smem_raw + SM::oCY);
+    float4* CX = reinterpret_cast<float4*>(smem_raw + SM::oCX);
+    float4* CY = reinterpret_cast<float4*>(smem_raw + SM::oCY);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::oBar);
     int* kminp = reinterpret_cast<int*>(smem_raw + SM::oBar + 32);
 
@@ -296,12 +288,14 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         fence_mbar_init();
     }
     for (int e = tid; e < NWF; e += NTH) {
-        const long long g = L.at2(i0 + e % TX, j0 + e / TX);
-        for (int q = 0; q < 6; ++q) CX[q * NWF + e] = A.fx[q * L.n2 + g];
+        float4 c = A.fc[L.at2(i0 + e % TX, j0 + e / TX)];
+        c.x *= A.schmidtH; c.y *= A.schmidtH;
+        CX[e] = c;
     }
     for (int e = tid; e < NSF; e += NTH) {
-        const long long g = L.at2(i0 + e % (TX + 1), j0 + e / (TX + 1));
-        for (int q = 0; q < 6; ++q) CY[q * NSF + e] = A.fy[q * L.n2 + g];
+        float4 c = A.fc[L.n2 + L.at2(i0 + e % (TX + 1), j0 + e / (TX + 1))];
+        c.x *= A.schmidtH; c.y *= A.schmidtH;
+        CY[e] = c;
     }
     __syncthreads();
     if (solve) atomicMin(kminp, kb);
@@ -310,7 +304,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     if (kmin > L.nk) return;                       // no water column in this tile
 
     // TMA box origins (x on 16-byte boundaries of the batched layout)
-    const int xP = i0 + kXOff - 4, xF = i0 + kXOff - 16, xV = i0 + kXOff - 4;
+    const int xP = i0 + kXOff - 4, xV = i0 + kXOff - 4;
     const int xVis = i0 + kXOff - Box<KT>::visOff, xO = i0 + kXOff;
     const int yP = j0 + kYOff - 2, yV = j0 + kYOff - 1, yO = j0 + kYOff;
     auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
@@ -318,7 +312,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         uint64_t* br = &bar[s];
         mbar_expect_tx(br, SL::tx_bytes);
         tma4(d + SL::oP, &M.P, xP, yP, k, A.t0, br);
-        tma3(d + SL::oF, &M.F, xF, yP, k, br);
+        tma3(d + SL::oF, &M.F, xO, yO, k, br);
         tma3(d + SL::oV, &M.V, xV, yV, k, br);
         tma3(d + SL::oVis, &M.Vis, xVis, yV, k, br);
         tma3(d + SL::oQX, &M.QX, xO, yO, k, br);
@@ -342,7 +336,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     const bool sd = cf & C_SD, opTop = cf & C_OPTOP, cfwTop = cf & C_CFWTOP, bp = cf & C_BP;
     // own-column values of the row below slide up the walk
     float qz = 0.f, dv = 0.f, dzzm = 1.f;
-    uint8_t flm = 0;
+    uint8_t flm = 0, fl = 0;
     const long long cb = L.at(i, j, 0);
     if (solve) {
         const long long a = cb + (long long)kb * L.sl;
@@ -350,6 +344,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         dv = ldg_as<KT>(A.DiffV, a, A.ksv);
         dzzm = A.DZZ[a - L.sl];
         flm = A.flag[a - L.sl];
+        fl = A.flag[a];
     }
     float Gp[NT];
 #pragma unroll
@@ -385,17 +380,13 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         if (solve && k >= kb) {
             // ---- row k of column (i,j): tracer-independent matrix
             const long long a = cb + (long long)k * L.sl;
-            const uint8_t* Fl = st + SL::oF;
-            const int fo = (ty + 2) * FBX + tx + 16;
-            const uint8_t fl = Fl[fo];
             const uint8_t flp = (k < L.nk) ? (st + SL::oFn)[own] : 0;
-            const float Vk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
+            const float rVk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
             const float dvr = reinterpret_cast<const float*>(st + SL::oVo)[own];   // (V - Vold)/V
             const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
             const float dvp = (k < L.nk) ? tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) : 0.f;
             const float dzz = reinterpret_cast<const float*>(st + SL::oDz)[own];
-            const float rV = __frcp_rn(Vk);
-            const float dtv = DT * rV;
+            const float dtv = DT * rVk;
             const bool open = fl & F_OP;
             // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term;
             // (V-Vold)/V was formed in FP64 when the volumes were packed
@@ -432,13 +423,14 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
             if (obc) {
                 const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
                 const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
+                const uint8_t* ffl = st + SL::oF + ty * FBX + tx;
                 const double hz =
-                    (double)(((fl & F_CFU) ? tofl<QT>(qx[fw], A.qsx) : 0.f) -
-                             ((Fl[fo + FBX] & F_CFU) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f) +
-                             ((fl & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
-                             ((Fl[fo + 1] & F_CFV) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
+                    (double)(((ffl[0] & FU_ACT) ? tofl<QT>(qx[fw], A.qsx) : 0.f) -
+                             ((ffl[FBX] & FU_ACT) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f) +
+                             ((ffl[0] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
+                             ((ffl[1] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
                              ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
-                wfob = (float)(hz - (double)(dvr * Vk) / (double)DT);
+                wfob = (float)(hz - (double)dvr / ((double)rVk * (double)DT));
                 if (wfob >= 0.f) E += wfob * dtv;
             }
             // THOMASZ factorisation of row k
@@ -465,7 +457,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
                 Gp[t] = G;
                 A.Pout[(long long)t * A.ts + a] = G;
             }
-            qz = qzp; dv = dvp; dzzm = dzz; flm = fl;
+            qz = qzp; dv = dvp; dzzm = dzz; flm = fl; fl = flp;
         }
         __syncthreads();                           // buffer s and the face fluxes are free
         if (tid == 0 && k + 2 <= L.nk) issue(k + 2, s);
@@ -570,7 +562,7 @@ void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4])
 {
     const int qyX = halfQ ? Box<__half>::qyX : Box<float>::qyX;
     const int visX = halfK ? Box<__half>::visX : Box<float>::visX;
-    const int b[13][4] = {{PBX, TY + 4, 1, nt}, {FBX, TY + 4, 1, 1}, {VBX, TY + 2, 1, 1},
+    const int b[13][4] = {{PBX, TY + 4, 1, nt}, {FBX, TY + 1, 1, 1}, {VBX, TY + 2, 1, 1},
                           {visX, TY + 2, 1, 1}, {TX, TY + 1, 1, 1},   {TX, TY + 1, 1, 1},
                           {qyX, TY, 1, 1},      {AVX, TY, 1, 1},      {OWN, TY, 1, 1},
                           {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1},

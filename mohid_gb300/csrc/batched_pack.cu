@@ -167,10 +167,44 @@ __global__ void k_pack_flags(const int* WP, const int* OP, const int* CFU, const
     }
 }
 
+// face flag bits of every cell's west (U) and south (V) faces.  The bits restate
+// the per-face conditions of ComputeAdvection1D_V2 (FN:10559: both cells open;
+// NearBoundary when the cell upstream of the upwind cell is not open) and the
+// compute-face masks, so the step reads one byte per face.  Faces on the
+// j = JUB+1 / i = IUB+1 planes are never applied by the reference.
+__global__ void k_pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, BLayout L)
+{
+    const int NI = L.ni + 2, NJ = L.nj + 2;
+    const long long sk = (long long)NI * NJ;
+    const long long n = sk * (L.nk + 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % NI);
+        const int j = (int)((e / NI) % NJ);
+        const int k = (int)(e / sk);
+        auto op = [&](int ii, int jj) -> bool {
+            return ii >= 0 && ii < NI && jj >= 0 && jj < NJ && OP[ii + (long long)NI * jj + sk * k] == 1;
+        };
+        uint8_t f = 0;
+        if (CFU[e] == 1 && j != L.nj + 1) {
+            f |= FU_ACT;
+            if (op(i, j - 1) && op(i, j)) f |= FU_ADV;
+        }
+        if (op(i, j - 2)) f |= FU_TVDP;
+        if (op(i, j + 1)) f |= FU_TVDN;
+        if (CFV[e] == 1 && i != L.ni + 1) {
+            f |= FV_ACT;
+            if (op(i - 1, j) && op(i, j)) f |= FV_ADV;
+        }
+        if (op(i - 2, j)) f |= FV_TVDP;
+        if (op(i + 1, j)) f |= FV_TVDN;
+        dst[L.at(i, j, k)] = f;
+    }
+}
+
 // per-column data and per-face 2-D constants
 __global__ void k_pack_cols(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                             const int* KF, const int* BP, const int* WP, const int* OP, const int* CFW,
-                            const int* SD, float* fx, float* fy, float* areaCol, int* kfloor,
+                            const int* SD, float4* fc, float* areaCol, int* kfloor,
                             uint8_t* cflag, BLayout L)
 {
     const int NI = L.ni + 2, NJ = L.nj + 2;
@@ -184,27 +218,25 @@ __global__ void k_pack_cols(const double* DUX, const double* DVY, const double* 
             jj = jj < 0 ? 0 : (jj > NJ - 1 ? NJ - 1 : jj);
             return a[ii + (long long)NI * jj];
         };
+        // Kx weights (Convert_Visc_Dif_Horizontal, AD:2487-2494) over the
+        // distance between the centres (HorizontalDiffusionXX, AD:5185), and
+        // the TVD slope ratio (du_dn + du_up) / (du_up + du_upup) of
+        // ComputeAdvectionFace (FN:10785-10822) for either flow direction
+        auto face = [&](double a, double b, double aa, double bb, double dz) -> float4 {
+            const double rdz = dz != 0.0 ? 1.0 / dz : 0.0;
+            const double s = a + b;
+            float4 c;
+            c.x = s != 0.0 ? (float)(a / s * rdz) : 0.f;            // weight of Visc(b), the cell's own
+            c.y = s != 0.0 ? (float)(b / s * rdz) : 0.f;            // weight of Visc(a)
+            c.z = (a + aa) != 0.0 ? (float)(s / (a + aa)) : 0.f;    // Q > 0: upwind a, upup aa
+            c.w = (b + bb) != 0.0 ? (float)(s / (b + bb)) : 0.f;    // Q <= 0: upwind b, upup bb
+            return c;
+        };
         // west face of (i,j): a = (i, j-1), b = (i, j); du = DUX along j
-        {
-            const double ua = d2(DUX, i, j - 1), ub = d2(DUX, i, j);
-            const double uaa = d2(DUX, i, j - 2), ubb = d2(DUX, i, j + 1);
-            fx[0 * L.n2 + g] = (float)(ua / (ub + ua));       // weight of Visc(b)
-            fx[1 * L.n2 + g] = (float)(ub / (ub + ua));       // weight of Visc(a)
-            fx[2 * L.n2 + g] = (float)(1.0 / d2(DZX, i, j - 1));
-            fx[3 * L.n2 + g] = (float)(1.0 / (ua + uaa));
-            fx[4 * L.n2 + g] = (float)(1.0 / (ub + ua));
-            fx[5 * L.n2 + g] = (float)(1.0 / (ub + ubb));
-        }
-        {
-            const double va = d2(DVY, i - 1, j), vb = d2(DVY, i, j);
-            const double vaa = d2(DVY, i - 2, j), vbb = d2(DVY, i + 1, j);
-            fy[0 * L.n2 + g] = (float)(va / (vb + va));
-            fy[1 * L.n2 + g] = (float)(vb / (vb + va));
-            fy[2 * L.n2 + g] = (float)(1.0 / d2(DZY, i - 1, j));
-            fy[3 * L.n2 + g] = (float)(1.0 / (va + vaa));
-            fy[4 * L.n2 + g] = (float)(1.0 / (vb + va));
-            fy[5 * L.n2 + g] = (float)(1.0 / (vb + vbb));
-        }
+        fc[g] = face(d2(DUX, i, j - 1), d2(DUX, i, j), d2(DUX, i, j - 2), d2(DUX, i, j + 1), d2(DZX, i, j - 1));
+        // south face of (i,j): a = (i-1, j), b = (i, j); du = DVY along i
+        fc[L.n2 + g] = face(d2(DVY, i - 1, j), d2(DVY, i, j), d2(DVY, i - 2, j), d2(DVY, i + 1, j),
+                            d2(DZY, i - 1, j));
         areaCol[g] = (float)(DUX[e] * DVY[e]);
         kfloor[g] = KF[e];
         uint8_t c = 0;
@@ -352,13 +384,20 @@ cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* 
     k_pack_flags<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(WP, OP, CFU, CFV, CFW, LP, dst, L);
     return cudaGetLastError();
 }
+cudaError_t pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, const BLayout& L,
+                            cudaStream_t s)
+{
+    k_pack_face_flags<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(OP, CFU, CFV,
+                                                                                                 dst, L);
+    return cudaGetLastError();
+}
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
-                         const int* CFW, const int* SD, float* fx, float* fy, float* areaCol,
+                         const int* CFW, const int* SD, float4* fc, float* areaCol,
                          int* kfloor, uint8_t* cflag, const BLayout& L, cudaStream_t s)
 {
     k_pack_cols<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2)), 256, 0, s>>>(
-        DUX, DVY, DZX, DZY, KFloor, BP2D, WP, OP, CFW, SD, fx, fy, areaCol, kfloor, cflag, L);
+        DUX, DVY, DZX, DZY, KFloor, BP2D, WP, OP, CFW, SD, fc, areaCol, kfloor, cflag, L);
     return cudaGetLastError();
 }
 cudaError_t pack_tracer(const double* src, float* dA, float* dB, const int* KFloor, const int* WP,
