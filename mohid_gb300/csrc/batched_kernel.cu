@@ -93,9 +93,11 @@ struct Smem {
     using SL = StageLayout<NT, QT, KT>;
     static constexpr int oStage0 = 0;
     static constexpr int oStage1 = SL::size;
+    // face fluxes, double-buffered by layer parity: [FX | FY] x 2
+    static constexpr int FXYStride = al128(NT * NWF * 4) + al128(NT * NSF * 4);
     static constexpr int oFX = 2 * SL::size;
     static constexpr int oFY = oFX + al128(NT * NWF * 4);
-    static constexpr int oCX = oFY + al128(NT * NSF * 4);
+    static constexpr int oCX = oFX + 2 * FXYStride;
     static constexpr int oCY = oCX + al128(NWF * 16);
     static constexpr int oBar = oCY + al128(NSF * 16);
     static constexpr int oEnd = oBar + 128;
@@ -257,6 +259,14 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
     }
 }
 
+// reciprocal with at most 1 ulp error (PTX rcp.approx), for the pivots
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
 __global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
@@ -264,12 +274,11 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     using SL = StageLayout<NT, QT, KT>;
     using SM = Smem<NT, QT, KT>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX);
-    float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY);
     float4* CX = reinterpret_cast<float4*>(smem_raw + SM::oCX);
     float4* CY = reinterpret_cast<float4*>(smem_raw + SM::oCY);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::oBar);
     int* kminp = reinterpret_cast<int*>(smem_raw + SM::oBar + 32);
+    unsigned* done = reinterpret_cast<unsigned*>(smem_raw + SM::oBar + 64);
 
     const BLayout& L = A.L;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -283,6 +292,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
 
     if (tid == 0) {
         *kminp = L.nk + 1;
+        *done = 0;
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
@@ -310,6 +320,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
         unsigned char* d = smem_raw + (s ? SM::oStage1 : SM::oStage0);
         uint64_t* br = &bar[s];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // earlier reads of buffer s
         mbar_expect_tx(br, SL::tx_bytes);
         tma4(d + SL::oP, &M.P, xP, yP, k, A.t0, br);
         tma3(d + SL::oF, &M.F, xO, yO, k, br);
@@ -333,18 +344,25 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     const bool horiz = !A.vertical1D;
     const float DT = A.DT;
     const float areaCol = solve ? A.areaCol[c2] : 0.f;
-    const bool sd = cf & C_SD, opTop = cf & C_OPTOP, cfwTop = cf & C_CFWTOP, bp = cf & C_BP;
-    // own-column values of the row below slide up the walk
-    float qz = 0.f, dv = 0.f, dzzm = 1.f;
+    // k-invariant conditions of the column's vertical terms
+    const bool vdif = L.nk > 1 && !(cf & C_SD);
+    const bool vadv = L.nk > 1 && !A.vertical1D && (cf & C_CFWTOP) && (cf & C_OPTOP);
+    const bool obcCol = (cf & C_BP) && A.Ref != nullptr;
+    // own-column values of the face below row k slide up the walk: transport,
+    // conductance Kz * area / DZZ (AD:2736-2765), cell flags of rows k-1 and k
+    float qz = 0.f, kzb = 0.f;
     uint8_t flm = 0, fl = 0;
     const long long cb = L.at(i, j, 0);
     if (solve) {
         const long long a = cb + (long long)kb * L.sl;
         qz = ldg_as<QT>(A.Qz, a, A.qsz);
-        dv = ldg_as<KT>(A.DiffV, a, A.ksv);
-        dzzm = A.DZZ[a - L.sl];
-        flm = A.flag[a - L.sl];
         fl = A.flag[a];
+        flm = A.flag[a - L.sl];
+        if (vdif && (fl & F_CFW)) {
+            float kz = A.coefV * ldg_as<KT>(A.DiffV, a, A.ksv) + A.backV;
+            if (A.nullDif && qz == 0.f) kz = 0.f;
+            kzb = kz * areaCol * A.DZZ[a - L.sl];          // DZZ holds 1/DZZ
+        }
     }
     float Gp[NT];
 #pragma unroll
@@ -354,10 +372,14 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
     uint32_t phase = 0;                            // bit s: parity of buffer s
     const int own = ty * OWN + tx;
     const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
+    float* const Wc = A.W + cb;
+    float* const Po = A.Pout + cb;
 
     for (int k = kmin; k <= L.nk; ++k) {
         const int s = k & 1;
         const unsigned char* st = smem_raw + (s ? SM::oStage1 : SM::oStage0);
+        float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX + s * SM::FXYStride);
+        float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY + s * SM::FXYStride);
         const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
         phase ^= 1u << s;
 
@@ -379,47 +401,40 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
 
         if (solve && k >= kb) {
             // ---- row k of column (i,j): tracer-independent matrix
-            const long long a = cb + (long long)k * L.sl;
-            const uint8_t flp = (k < L.nk) ? (st + SL::oFn)[own] : 0;
+            const long long ko = (long long)k * L.sl;
+            const bool top = k == L.nk;
+            const uint8_t flp = top ? 0 : (st + SL::oFn)[own];
             const float rVk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
             const float dvr = reinterpret_cast<const float*>(st + SL::oVo)[own];   // (V - Vold)/V
             const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
-            const float dvp = (k < L.nk) ? tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) : 0.f;
-            const float dzz = reinterpret_cast<const float*>(st + SL::oDz)[own];
             const float dtv = DT * rVk;
             const bool open = fl & F_OP;
             // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term;
             // (V-Vold)/V was formed in FP64 when the volumes were packed
             const float ratio = open ? 1.f - dvr : 1.f;
-            float E = 1.f, D = 0.f, Fc = 0.f;
-            if (open && k == L.nk) E = 1.f + dtv * qzp;
-            if (L.nk > 1) {
-                if ((fl & F_CFW) && !sd) {                   // VerticalDiffusion, face k
-                    float kz = A.coefV * dv + A.backV;
-                    if (A.nullDif && qz == 0.f) kz = 0.f;
-                    const float aux2 = kz * areaCol * dzzm * dtv;     // dzzm holds 1/DZZ(k-1)
-                    D -= aux2; E += aux2;
+            // VerticalDiffusion, implicit: faces k (below) and k+1 (above)
+            float kza = 0.f;
+            if (vdif && (flp & F_CFW)) {
+                float kz = A.coefV * tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) + A.backV;
+                if (A.nullDif && qzp == 0.f) kz = 0.f;
+                kza = kz * areaCol * reinterpret_cast<const float*>(st + SL::oDz)[own];   // 1/DZZ(k)
+            }
+            const float aux2 = kzb * dtv, aux1 = kza * dtv;
+            float D = -aux2, E = 1.f + aux2 + aux1, Fc = -aux1;
+            if (open && top) E += dtv * qzp;
+            if (vadv && open) {                          // VerticalAdvection, upwind, implicit
+                if (k > kb && (flm & F_OP)) {
+                    D -= fmaxf(qz, 0.f) * dtv;
+                    E -= fminf(qz, 0.f) * dtv;
                 }
-                if ((flp & F_CFW) && !sd) {                  // face k+1
-                    float kz = A.coefV * dvp + A.backV;
-                    if (A.nullDif && qzp == 0.f) kz = 0.f;
-                    const float aux1 = kz * areaCol * dzz * dtv;      // dzz holds 1/DZZ(k)
-                    E += aux1; Fc -= aux1;
-                }
-                if (!A.vertical1D && cfwTop) {               // VerticalAdvection, upwind, implicit
-                    if (k >= kb + 1 && opTop && (flm & F_OP) && open) {
-                        D -= (qz > 0.f ? qz : 0.f) * dtv;
-                        E -= (qz > 0.f ? 0.f : qz) * dtv;
-                    }
-                    if (k + 1 <= L.nk && opTop && open && (flp & F_OP)) {
-                        E += (qzp > 0.f ? qzp : 0.f) * dtv;
-                        Fc += (qzp > 0.f ? 0.f : qzp) * dtv;
-                    }
+                if (!top && (flp & F_OP)) {
+                    E += fmaxf(qzp, 0.f) * dtv;
+                    Fc += fminf(qzp, 0.f) * dtv;
                 }
             }
             // open boundary (MassConservation): net flux through the exterior faces
             float wfob = 0.f;
-            const bool obc = bp && A.Ref && open;
+            const bool obc = obcCol && open;
             if (obc) {
                 const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
                 const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
@@ -434,11 +449,11 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
                 if (wfob >= 0.f) E += wfob * dtv;
             }
             // THOMASZ factorisation of row k
-            const float aux = E + D * Wp;
-            float inv;
-            if (aux != 0.f) inv = __frcp_rn(aux); else { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
+            const float aux = fmaf(D, Wp, E);
+            float inv = rcp_approx(aux);
+            if (aux == 0.f) { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
             const float W = -Fc * inv;
-            A.W[a] = W;                                  // read back by the back-substitution
+            Wc[ko] = W;                                  // read back by the back-substitution
             Wp = W;
             const float* P = reinterpret_cast<const float*>(st + SL::oP);
             const int po = (ty + 2) * PBX + tx + 4;
@@ -447,20 +462,26 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
                 const float Pc = P[t * (TY + 4) * PBX + po];
                 float TI = Pc * ratio;
                 if (horiz)
-                    TI += dtv * ((FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
-                                 (FY[t * NSF + fs] - FY[t * NSF + fs + 1]));
+                    TI = fmaf(dtv, (FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
+                                   (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
                 if (obc && wfob < 0.f) {
-                    const float ext = Pc * (1.f - A.tdec) + A.Ref[(long long)t * A.ts + a] * A.tdec;
+                    const float ext = Pc * (1.f - A.tdec) + A.Ref[(long long)t * A.ts + cb + ko] * A.tdec;
                     TI -= wfob * ext * dtv;
                 }
                 const float G = (TI - D * Gp[t]) * inv;
                 Gp[t] = G;
-                A.Pout[(long long)t * A.ts + a] = G;
+                Po[(long long)t * A.ts + ko] = G;
             }
-            qz = qzp; dv = dvp; dzzm = dzz; flm = fl; fl = flp;
+            qz = qzp; kzb = kza; flm = fl; fl = flp;
         }
-        __syncthreads();                           // buffer s and the face fluxes are free
-        if (tid == 0 && k + 2 <= L.nk) issue(k + 2, s);
+        // buffer s is free once every warp has finished row k: the last warp
+        // to get here refills it with layer k + 2 (all warps pass the barrier
+        // of layer k + 1 only after all of them got here for layer k)
+        __syncwarp();
+        if (tx == 0) {
+            const unsigned n = atomicAdd(done, 1u);
+            if ((n & (TY - 1)) == TY - 1 && k + 2 <= L.nk) issue(k + 2, s);
+        }
     }
 
     // ---- back-substitution (row KUB+1 solves to 0); W and G loads are issued
@@ -469,8 +490,7 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
         float x[NT];
 #pragma unroll
         for (int t = 0; t < NT; ++t) x[t] = 0.f;
-        const float* Wc = A.W + cb;
-        float* Po = A.Pout + cb;
+        float chk = 0.f;                           // NaN / Inf anywhere in the column shows here
         for (int k = L.nk; k >= kb; k -= 8) {
             float w[8], g[NT][8];
 #pragma unroll
@@ -487,12 +507,13 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
                     const long long o = (long long)(k - q) * L.sl;
 #pragma unroll
                     for (int t = 0; t < NT; ++t) {
-                        x[t] = w[q] * x[t] + g[t][q];
+                        x[t] = fmaf(w[q], x[t], g[t][q]);
                         Po[(long long)t * A.ts + o] = x[t];
-                        if (!isfinite(x[t])) bad |= MOHID_DEV_NONFINITE;
+                        chk += x[t];
                     }
                 }
         }
+        if (!isfinite(chk)) bad |= MOHID_DEV_NONFINITE;
     }
     if (bad) atomicOr(A.status, bad);
 }
