@@ -285,6 +285,32 @@ int mohid_ad_batched_sync(const int* bid, int* stat);
 int mohid_ad_batched_destroy(int* bid, int* stat);
 
 /* ======================================================================== */
+/* Ensemble: many independent batched domains in one launch                  */
+/* ======================================================================== */
+
+/*
+ * No counterpart in the reference, which runs one domain per process (nested
+ * and ensemble runs of MOHID Water are separate model instances).  An
+ * ensemble steps *nmembers batches (bids[0..nmembers-1]) together: one
+ * persistent grid walks the tiles of every member, largest layer count first.
+ * Members must live on the same device and have the same tracer count (1, 2
+ * or 4) and FP32 storage (storage 0); each keeps its own grid, hydrodynamics,
+ * tracers, DT and options.  Members stay usable as batches (set_tracer,
+ * get_tracer, mass); do not step a member on its own while it is in an
+ * ensemble.  The ensemble runs on the stream of the first member's instance.
+ */
+int mohid_ad_ensemble_create(int* eid, const int* nmembers, const int* bids, int* stat);
+
+/* Advance every member *nsteps steps, member m with options p[m] (same
+ * AdvMethodH and TVDLimitationH for all members).  *use_graph != 0 captures
+ * the step loop in a CUDA graph, as mohid_ad_batched_step does. */
+int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
+                           int* stat);
+
+/* Release the ensemble (the member batches are not destroyed). */
+int mohid_ad_ensemble_destroy(int* eid, int* stat);
+
+/* ======================================================================== */
 /* Stand-alone THOMASZ (replaces SolveThomas_C with dim = 2 = Z)             */
 /* ======================================================================== */
 

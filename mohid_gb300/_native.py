@@ -97,6 +97,9 @@ _AD_SIGS = {
     "mohid_ad_batched_mass": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
     "mohid_ad_batched_sync": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_batched_destroy": (C.c_int, [c_int_p, c_int_p]),
+    "mohid_ad_ensemble_create": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_ensemble_step": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_ensemble_destroy": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_mass_f64_noalloc": (C.c_int, [C.POINTER(T_Size3D), C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, c_int_p]),
 }

@@ -97,3 +97,45 @@ class Batch:
                 raise ValueError("expected a C-contiguous float64 array")
             return 0, C.c_void_p(a.ctypes.data)
         return 1, C.c_void_p(a.data_ptr())          # torch CUDA tensor
+
+
+class Ensemble:
+    """Independent batched domains stepped together in one persistent launch
+    (mohid_ad_ensemble_*).  Members keep their own grid, hydrodynamics, DT and
+    tracers; they need the same tracer count (1, 2 or 4) and FP32 storage."""
+
+    def __init__(self, members: list):
+        self.members = list(members)
+        self.lib = N.ad_lib()
+        self._eid = C.c_int(0)
+        ids = (C.c_int * len(self.members))(*[b._bid.value for b in self.members])
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_ensemble_create(C.byref(self._eid), C.byref(C.c_int(len(self.members))), ids,
+                                               C.byref(st))
+        N.check(rc, "mohid_ad_ensemble_create")
+
+    def step(self, params: list, nsteps: int = 1, graph: bool = False):
+        """params: one MohidAdParams per member."""
+        if len(params) != len(self.members):
+            raise ValueError("one parameter set per member")
+        arr = (N.MohidAdParams * len(params))(*params)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_ensemble_step(C.byref(self._eid), arr, C.byref(C.c_int(nsteps)),
+                                             C.byref(C.c_int(int(graph))), C.byref(st))
+        N.check(rc, "mohid_ad_ensemble_step")
+
+    def sync(self):
+        for b in self.members:
+            b.sync()
+
+    def destroy(self):
+        if self._eid.value:
+            st = C.c_int(0)
+            N.check(self.lib.mohid_ad_ensemble_destroy(C.byref(self._eid), C.byref(st)),
+                    "mohid_ad_ensemble_destroy")
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

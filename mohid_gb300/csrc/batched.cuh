@@ -103,6 +103,12 @@ struct TmaMaps {
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
                            bool halfK, cudaStream_t s);
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
+// ensemble: one persistent grid over the (domain, bx, by, -) tiles of many
+// domains with FP32 storage; As/Ms are device tables indexed by domain
+cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
+                            int nt, int method, int limiter, cudaStream_t s);
+// resident CTAs of the ensemble kernel on `device` (0 on error)
+int ensemble_slots(int nt, int method, int limiter, int device);
 // box extents (elements, x y z w) of the 13 maps in TmaMaps order
 void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4]);
 

@@ -53,6 +53,7 @@ struct Batch {
     bool shiftOk = true;
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
+    int ensemble = 0;                    // id of the ensemble stepping this batch, or 0
     bool packed = false;
     unsigned packedVersion = ~0u;
     DevBuf<double> partial, scratch, stage;
@@ -247,7 +248,8 @@ int pack_hydro(Batch* b, int* stat)
 mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout)
 {
     Instance* in = b->in;
-    mohid::BatchArgs a{};
+    mohid::BatchArgs a;
+    std::memset(&a, 0, sizeof a);                // padding too: ensembles compare argument tables bytewise
     a.L = b->L;
     const bool hq = b->storage >= 1, hk = b->storage >= 2;
     a.Qx = hq ? (const void*)b->Qx16.p : (const void*)b->Qx32.p;
@@ -340,6 +342,55 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s)
     }
     b->cur = !b->cur;
     return cudaSuccess;
+}
+
+// ---- ensembles --------------------------------------------------------------
+struct Ensemble {
+    std::vector<Batch*> m;
+    std::vector<int> bids;
+    int nt = 0;
+    int device = 0;
+    cudaStream_t s = nullptr;
+    DevBuf<mohid::BatchArgs> dA;         // [2][n]: arguments for each buffer parity
+    DevBuf<mohid::TmaMaps> dM;           // [2][n]
+    DevBuf<int4> tiles;                  // (member, bx, by, 0), costliest first
+    int ntiles = 0;
+    std::vector<mohid::BatchArgs> hA;    // what dA holds
+    std::vector<mohid::TmaMaps> hM;
+    bool uploaded = false;
+    bool cur = false;                    // buffer parity of every member
+    cudaGraphExec_t graph = nullptr;
+    int graphSteps = 0;
+    bool graphCur = false;
+    int graphMethod = 0, graphLimiter = 0;
+    void release()
+    {
+        dA.release(); dM.release(); tiles.release();
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+};
+
+std::map<int, Ensemble*> g_ens;
+int g_next_eid = 1;
+
+Ensemble* elookup(const int* eid)
+{
+    if (!eid) return nullptr;
+    std::lock_guard<std::mutex> lk(g_bmu);
+    auto it = g_ens.find(*eid);
+    return it == g_ens.end() ? nullptr : it->second;
+}
+
+// one step of every member: one launch over all tiles, then every parity flips
+cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
+{
+    const size_t n = E->m.size();
+    const size_t off = E->cur ? n : 0;
+    cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
+                                           method, limiter, E->s);
+    E->cur = !E->cur;
+    return e;
 }
 
 }  // namespace
@@ -498,6 +549,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!nsteps || !use_graph) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (b->ensemble) return fail(MOHID_AD_ERR_OPTION, stat, "the batch is stepped by an ensemble");
     std::string why;
     int code = check_batched_params(p, b->hasRef, why);
     if (code) return fail(code, stat, why);
@@ -588,7 +640,11 @@ int mohid_ad_batched_destroy(int* bid, int* stat)
     if (bid) {
         std::lock_guard<std::mutex> lk(g_bmu);
         auto it = g_batch.find(*bid);
-        if (it != g_batch.end()) { b = it->second; g_batch.erase(it); }
+        if (it != g_batch.end()) {
+            if (it->second->ensemble) return fail(MOHID_AD_ERR_OPTION, stat, "the batch belongs to an ensemble");
+            b = it->second;
+            g_batch.erase(it);
+        }
     }
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     cudaSetDevice(b->in->device);
@@ -596,6 +652,183 @@ int mohid_ad_batched_destroy(int* bid, int* stat)
     b->release();
     delete b;
     *bid = 0;
+    return ok(stat);
+}
+
+int mohid_ad_ensemble_create(int* eid, const int* nmembers, const int* bids, int* stat)
+{
+    if (!eid || !nmembers || !bids) return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_ad_ensemble_create: NULL argument");
+    if (*nmembers < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nmembers must be >= 1");
+    std::vector<Batch*> m;
+    for (int q = 0; q < *nmembers; ++q) {
+        Batch* b = blookup(&bids[q]);
+        if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id " + std::to_string(bids[q]));
+        if (b->ensemble) return fail(MOHID_AD_ERR_OPTION, stat, "batch " + std::to_string(bids[q]) + " is already in an ensemble");
+        if (std::find(m.begin(), m.end(), b) != m.end()) return fail(MOHID_AD_ERR_OPTION, stat, "a batch is listed twice");
+        if (b->storage != 0) return fail(MOHID_AD_ERR_UNSUPPORTED, stat, "ensemble members must use FP32 storage");
+        if (b->nt != 1 && b->nt != 2 && b->nt != 4)
+            return fail(MOHID_AD_ERR_UNSUPPORTED, stat, "ensemble members must hold 1, 2 or 4 tracers");
+        if (!m.empty() && b->nt != m[0]->nt) return fail(MOHID_AD_ERR_OPTION, stat, "members hold different tracer counts");
+        if (!m.empty() && b->in->device != m[0]->in->device) return fail(MOHID_AD_ERR_OPTION, stat, "members on different devices");
+        if (!m.empty() && b->cur != m[0]->cur) return fail(MOHID_AD_ERR_OPTION, stat, "members at different buffer parities");
+        m.push_back(b);
+    }
+    CK(cudaSetDevice(m[0]->in->device));
+    Ensemble* E = new Ensemble();
+    E->m = m;
+    E->bids.assign(bids, bids + *nmembers);
+    E->nt = m[0]->nt;
+    E->device = m[0]->in->device;
+    E->s = m[0]->in->stream;
+    E->cur = m[0]->cur;
+    // tiles of every member, the deepest domains first (a tile's cost grows with its layers)
+    std::vector<int4> t;
+    for (int q = 0; q < (int)m.size(); ++q) {
+        const mohid::BLayout& L = m[q]->L;
+        const int gx = (L.ni + mohid::kTX - 1) / mohid::kTX, gy = (L.nj + mohid::kTY - 1) / mohid::kTY;
+        for (int by = 0; by < gy; ++by)
+            for (int bx = 0; bx < gx; ++bx) t.push_back(make_int4(q, bx, by, 0));
+    }
+    std::stable_sort(t.begin(), t.end(), [&](const int4& a, const int4& b) { return m[a.x]->L.nk > m[b.x]->L.nk; });
+    E->ntiles = (int)t.size();
+    const size_t n = m.size();
+    cudaError_t e;
+    if ((e = E->dA.alloc(2 * n)) != cudaSuccess || (e = E->dM.alloc(2 * n)) != cudaSuccess ||
+        (e = E->tiles.alloc(t.size())) != cudaSuccess) {
+        E->release();
+        delete E;
+        return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaMalloc", e));
+    }
+    if ((e = cudaMemcpy(E->tiles.p, t.data(), t.size() * sizeof(int4), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        E->release();
+        delete E;
+        return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaMemcpy", e));
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_bmu);
+        *eid = g_next_eid++;
+        g_ens[*eid] = E;
+        for (Batch* b : m) b->ensemble = *eid;
+    }
+    return ok(stat);
+}
+
+int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
+                           int* stat)
+{
+    Ensemble* E = elookup(eid);
+    if (!E) return fail(MOHID_AD_ERR_ID, stat, "unknown ensemble id");
+    if (!p || !nsteps || !use_graph) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
+    const size_t n = E->m.size();
+    const int method = p[0].AdvMethodH, limiter = p[0].TVDLimitationH;
+    CK(cudaSetDevice(E->device));
+    for (size_t q = 0; q < n; ++q) {
+        Batch* b = E->m[q];
+        std::string why;
+        int code = check_batched_params(&p[q], b->hasRef, why);
+        if (code) return fail(code, stat, "member " + std::to_string(q) + ": " + why);
+        if (p[q].AdvMethodH != method || (method != MOHID_UPWIND_ORDER1 && p[q].TVDLimitationH != limiter))
+            return fail(MOHID_AD_ERR_OPTION, stat, "members must share AdvMethodH and TVDLimitationH");
+        if (b->hasRef)
+            for (int t = 0; t < b->nt; ++t)
+                if (t >= (int)b->refShift.size() || b->refShift[t] != b->shift[t])
+                    return fail(MOHID_AD_ERR_OPTION, stat,
+                                "set the reference of every tracer after (re)loading the tracer");
+        if (!b->packed || b->packedVersion != b->in->hydroVersion) {
+            int c = pack_hydro(b, stat);
+            if (c) return c;
+        }
+        int c = ensure_shift_valid(b, &p[q], stat);
+        if (c) return c;
+        if (b->cur != E->cur) return fail(MOHID_AD_ERR_OPTION, stat, "a member was stepped outside the ensemble");
+    }
+    // members' own streams (packing, tracer loads) before the ensemble's
+    for (size_t q = 0; q < n; ++q)
+        if (E->m[q]->in->stream != E->s) CK(cudaStreamSynchronize(E->m[q]->in->stream));
+    // argument and tensor-map tables for both buffer parities
+    std::vector<mohid::BatchArgs> hA(2 * n);
+    std::vector<mohid::TmaMaps> hM(2 * n);
+    const int gi = E->nt == 4 ? 2 : (E->nt == 2 ? 1 : 0);
+    for (int c = 0; c < 2; ++c)
+        for (size_t q = 0; q < n; ++q) {
+            Batch* b = E->m[q];
+            const float* Pin = c ? b->PB.p : b->PA.p;
+            float* Pout = c ? b->PA.p : b->PB.p;
+            hA[c * n + q] = make_bargs(b, &p[q], 0, b->nt, Pin, Pout);
+            hM[c * n + q] = b->maps;
+            hM[c * n + q].P = b->mapP[c][gi];
+        }
+    const bool same = E->uploaded && std::memcmp(hA.data(), E->hA.data(), hA.size() * sizeof(hA[0])) == 0 &&
+                      std::memcmp(hM.data(), E->hM.data(), hM.size() * sizeof(hM[0])) == 0;
+    if (!same) {
+        CK(cudaStreamSynchronize(E->s));             // no launch still reads the tables
+        CK(cudaMemcpy(E->dA.p, hA.data(), hA.size() * sizeof(hA[0]), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(E->dM.p, hM.data(), hM.size() * sizeof(hM[0]), cudaMemcpyHostToDevice));
+        E->hA.swap(hA);
+        E->hM.swap(hM);
+        E->uploaded = true;
+    }
+    const int slots = mohid::ensemble_slots(E->nt, method, limiter, E->device);
+    if (slots <= 0) return fail(MOHID_AD_ERR_CUDA, stat, "ensemble kernel occupancy query failed");
+    const int grid = std::min(slots, E->ntiles);
+    const bool cur0 = E->cur;
+    auto flip_members = [&](int steps) {
+        if (steps % 2)
+            for (Batch* b : E->m) b->cur = !b->cur;
+    };
+    if (!*use_graph) {
+        for (int q = 0; q < *nsteps; ++q) CK(enqueue_ens_step(E, method, limiter, grid));
+        flip_members(*nsteps);
+        return ok(stat);
+    }
+    const int pairs = *nsteps / 2;
+    if (pairs > 0) {
+        const bool reuse = E->graph && E->graphSteps == 2 * pairs && E->graphCur == E->cur &&
+                           E->graphMethod == method && E->graphLimiter == limiter && same;
+        if (!reuse) {
+            if (E->graph) { cudaGraphExecDestroy(E->graph); E->graph = nullptr; }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(E->s, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            for (int q = 0; q < 2 * pairs && e == cudaSuccess; ++q) e = enqueue_ens_step(E, method, limiter, grid);
+            cudaError_t e2 = cudaStreamEndCapture(E->s, &g);
+            E->cur = cur0;
+            if (e != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("capture", e));
+            if (e2 != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaStreamEndCapture", e2));
+            e = cudaGraphInstantiate(&E->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { E->graph = nullptr; return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaGraphInstantiate", e)); }
+            E->graphSteps = 2 * pairs;
+            E->graphCur = cur0;
+            E->graphMethod = method;
+            E->graphLimiter = limiter;
+        }
+        CK(cudaGraphLaunch(E->graph, E->s));
+    }
+    if (*nsteps % 2) CK(enqueue_ens_step(E, method, limiter, grid));
+    flip_members(*nsteps);
+    return ok(stat);
+}
+
+int mohid_ad_ensemble_destroy(int* eid, int* stat)
+{
+    Ensemble* E = nullptr;
+    if (eid) {
+        std::lock_guard<std::mutex> lk(g_bmu);
+        auto it = g_ens.find(*eid);
+        if (it != g_ens.end()) {
+            E = it->second;
+            g_ens.erase(it);
+            for (Batch* b : E->m) b->ensemble = 0;
+        }
+    }
+    if (!E) return fail(MOHID_AD_ERR_ID, stat, "unknown ensemble id");
+    cudaSetDevice(E->device);
+    cudaStreamSynchronize(E->s);
+    E->release();
+    delete E;
+    *eid = 0;
     return ok(stat);
 }
 

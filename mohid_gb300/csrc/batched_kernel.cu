@@ -1,521 +1,19 @@
-// batched_kernel.cu -- batched FP32 multi-tracer transport step (TMA-staged).
-//
-// Same operator as the plain FP64 drop-in (ModuleAdvectionDiffusion's
-// AdvectionDiffusion: VolumeVariation, explicit horizontal diffusion and
-// advection with ComputeAdvectionFace coefficients, implicit vertical
-// diffusion and upwind advection, MassConservation open boundaries, THOMASZ),
-// re-organised for many tracers sharing one hydrodynamic state:
-//
-//  * a CTA owns a 32 x 8 tile of water columns and walks k upwards.  Each
-//    layer's fields (all tracers of the launch with a 2-cell halo, masks,
-//    volumes, viscosity, face transports and areas, and the own-column values
-//    of the layer above) arrive in shared memory as tiled bulk-tensor copies
-//    (TMA), double-buffered on two mbarriers: layer k+1 streams in while layer
-//    k is solved.  One thread issues 13 copies per layer; no thread spends
-//    instructions or registers on staging;
-//  * every horizontal face is evaluated once per layer: its tracer-independent
-//    part (Courant number, upwind side, limiter weights, diffusive
-//    conductance) once, then the flux of each tracer; cells gather their four
-//    face fluxes from shared memory;
-//  * the vertical tridiagonal matrix does not depend on the tracer (upwind
-//    vertical advection + diffusion, AD:2708-2784, AD:3066-3117), so each row
-//    is factorised once (W, 1/pivot) and every tracer only runs
-//    G = (TI - D*G_prev) / pivot and the back-substitution (THOMASZ,
-//    FN:4026-4123); W goes to a per-cell scratch array and G into the output
-//    array, both read back from L2 by the same thread on the way down;
-//  * the volume ratio Vold/V is applied as 1 - (V - Vold)/V, the relative
-//    change being formed in FP64 when the volumes are packed (thin layers make
-//    the difference cancel); the kernel itself runs no FP64 arithmetic, which
-//    GB300 issues at a small fraction of the FP32 rate;
-//  * rows below KFloor are never touched (they hold null_real, as after any
-//    reference step), so a z-level column costs what it holds.
-//
-// Every wait on an mbarrier is bounded; a stage that never arrives makes the
-// whole CTA set MOHID_DEV_TIMEOUT and return.
-#include <type_traits>
-
-#include "batched.cuh"
-#include "common.cuh"
+// batched_kernel.cu -- single-domain launch of the batched FP32 multi-tracer
+// transport step: one CTA per 32 x 8 tile (the walk is in batched_tile.cuh).
+#include "batched_tile.cuh"
 
 namespace mohid {
+using namespace tile;
 namespace {
-
-constexpr int TX = kTX, TY = kTY, NTH = TX * TY;
-constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
-
-// ---- TMA stage layout -------------------------------------------------------
-// Box origins sit on 16-byte boundaries of the batched layout (x = i + 31):
-// the tracer and 1/V tiles start 4 cells before i0, the viscosity tile 4 (FP32)
-// or 8 (FP16) cells before; face, face-flag and own-cell tiles start at i0.
-constexpr int PBX = 40, FBX = 48, VBX = 40, OWN = 32, AVX = 36;
-template <typename T> struct Box;
-template <> struct Box<float> { static constexpr int visX = 40, visOff = 4, qyX = 36; };
-template <> struct Box<__half> { static constexpr int visX = 48, visOff = 8, qyX = 40; };
-
-constexpr int al128(int b) { return (b + 127) / 128 * 128; }
-
-template <int NT, typename QT, typename KT>
-struct StageLayout {
-    static constexpr int qyX = Box<QT>::qyX, visX = Box<KT>::visX;
-    static constexpr int bP = NT * (TY + 4) * PBX * 4;
-    static constexpr int bF = (TY + 1) * FBX;
-    static constexpr int bV = (TY + 2) * VBX * 4;
-    static constexpr int bVis = (TY + 2) * visX * (int)sizeof(KT);
-    static constexpr int bQX = (TY + 1) * TX * (int)sizeof(QT);
-    static constexpr int bAU = (TY + 1) * TX * 4;
-    static constexpr int bQY = TY * qyX * (int)sizeof(QT);
-    static constexpr int bAV = TY * AVX * 4;
-    static constexpr int bVo = TY * OWN * 4;
-    static constexpr int bQz = TY * OWN * (int)sizeof(QT);
-    static constexpr int bDv = TY * OWN * (int)sizeof(KT);
-    static constexpr int bDz = TY * OWN * 4;
-    static constexpr int bFn = TY * OWN;
-    static constexpr int oP = 0;
-    static constexpr int oF = oP + al128(bP);
-    static constexpr int oV = oF + al128(bF);
-    static constexpr int oVis = oV + al128(bV);
-    static constexpr int oQX = oVis + al128(bVis);
-    static constexpr int oAU = oQX + al128(bQX);
-    static constexpr int oQY = oAU + al128(bAU);
-    static constexpr int oAV = oQY + al128(bQY);
-    static constexpr int oVo = oAV + al128(bAV);
-    static constexpr int oQz = oVo + al128(bVo);
-    static constexpr int oDv = oQz + al128(bQz);
-    static constexpr int oDz = oDv + al128(bDv);
-    static constexpr int oFn = oDz + al128(bDz);
-    static constexpr int size = oFn + al128(bFn);
-    static constexpr unsigned tx_bytes =
-        bP + bF + bV + bVis + bQX + bAU + bQY + bAV + bVo + bQz + bDv + bDz + bFn;
-};
-
-template <int NT, typename QT, typename KT>
-struct Smem {
-    using SL = StageLayout<NT, QT, KT>;
-    static constexpr int oStage0 = 0;
-    static constexpr int oStage1 = SL::size;
-    // face fluxes, double-buffered by layer parity: [FX | FY] x 2
-    static constexpr int FXYStride = al128(NT * NWF * 4) + al128(NT * NSF * 4);
-    static constexpr int oFX = 2 * SL::size;
-    static constexpr int oFY = oFX + al128(NT * NWF * 4);
-    static constexpr int oCX = oFX + 2 * FXYStride;
-    static constexpr int oCY = oCX + al128(NWF * 16);
-    static constexpr int oBar = oCY + al128(NSF * 16);
-    static constexpr int oEnd = oBar + 128;
-    static size_t bytes(int) { return (size_t)oEnd; }
-};
-
-// ---- PTX helpers: mbarrier and bulk tensor copies ---------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init()
-{
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: gives up after `limit` polls
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit)
-{
-    for (uint32_t it = 0; it < limit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, int x, int y, int z, int w, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
-        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
-        : "memory");
-}
-constexpr uint32_t kWaitLimit = 1u << 24;
-
-// psi(r) * d for r = n / d, psi one of the ComputeAdvectionFace limiters
-// (FN:10823-10856).  Each min/max of psi(r) is multiplied through by |d|, so
-// with a = |d| and b = n * sign(d) no division is needed (VanLeer keeps one);
-// d = 0 gives 0, as the reference's theta * 0.
-// PDM: pa, pb from |Cr|, p2 = 2/(1-Cr), pcr = 2/Cr.
-template <int LIM>
-__device__ __forceinline__ float limited_slope(float n, float d, float pa, float pb, float p2, float pcr)
-{
-    const unsigned sd = __float_as_uint(d) & 0x80000000u;
-    const float a = fabsf(d);
-    const float b = __uint_as_float(__float_as_uint(n) ^ sd);
-    float v;
-    if (LIM == 1) v = fmaxf(0.f, fminf(a, b));                                          // MinMod
-    else if (LIM == 2) v = b > 0.f ? __fdividef(2.f * a * b, a + b) : 0.f;             // VanLeer
-    else if (LIM == 3) v = fmaxf(0.f, fminf(fminf(2.f * a, 2.f * b), 0.5f * (a + b))); // MUSCL
-    else if (LIM == 4) v = fmaxf(fmaxf(0.f, fminf(a, 2.f * b)), fminf(b, 2.f * a));    // SuperBee
-    else v = fmaxf(0.f, fminf(fminf(fmaf(pb, b, pa * a), p2 * a), pcr * b));          // PDM
-    return __uint_as_float(__float_as_uint(v) | sd);
-}
-
-template <typename T> __device__ __forceinline__ float tofl(T v, float s);
-template <> __device__ __forceinline__ float tofl<float>(float v, float) { return v; }
-template <> __device__ __forceinline__ float tofl<__half>(__half v, float s) { return s * __half2float(v); }
-
-template <typename T>
-__device__ __forceinline__ float ldg_as(const void* p, long long a, float s)
-{
-    return tofl<T>(reinterpret_cast<const T*>(p)[a], s);
-}
-
-// One face of the tile at one layer.  WEST: the face between cells
-// (i0+b, j0+a-1) and (i0+b, j0+a), a = 0..TY; otherwise the face between
-// (i0+b-1, j0+a) and (i0+b, j0+a), b = 0..TX.  Tracer-independent part first
-// (upwind side, Courant number, diffusive conductance), then for every tracer
-// F = q*P_up + kd*(P_dn - P_up) + q*c*psi(r)*(P_dn - P_up) into shared memory.
-// Reference face coefficients: ComputeAdvectionFace FN:10702-10894 (upwind,
-// P2_TVD limiters, theta = psi*(1-Cr)/2); diffusive flux
-// HorizontalDiffusionXX/YY AD:5185-5196 with Kx from
-// Convert_Visc_Dif_Horizontal AD:2487-2494.
-template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT>
-__device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, const float4* CXY,
-                                          const BatchArgs& A, int a, int b)
-{
-    using SL = StageLayout<NT, QT, KT>;
-    constexpr int pst = WEST ? PBX : 1, vst = WEST ? VBX : 1;
-    constexpr int visst = WEST ? Box<KT>::visX : 1;
-    constexpr int cs = WEST ? NWF : NSF;
-    constexpr uint8_t ACT = WEST ? FU_ACT : FV_ACT, ADV = WEST ? FU_ADV : FV_ADV;
-    constexpr uint8_t TVDP = WEST ? FU_TVDP : FV_TVDP, TVDN = WEST ? FU_TVDN : FV_TVDN;
-    const float* P = reinterpret_cast<const float*>(st + SL::oP);
-    const float* RVt = reinterpret_cast<const float*>(st + SL::oV);
-    const KT* Vis = reinterpret_cast<const KT*>(st + SL::oVis);
-    const int pb = (a + 2) * PBX + b + 4;
-    const int vb = (a + 1) * VBX + b + 4;
-    const int visb = (a + 1) * Box<KT>::visX + b + Box<KT>::visOff;
-    const int fi = WEST ? a * TX + b : a * (TX + 1) + b;
-    float q, area;
-    if (WEST) {
-        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQX)[a * TX + b], A.qsx);
-        area = reinterpret_cast<const float*>(st + SL::oAU)[a * TX + b];
-    } else {
-        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQY)[a * SL::qyX + b], A.qsy);
-        area = reinterpret_cast<const float*>(st + SL::oAV)[a * AVX + b];
-    }
-    const uint8_t ff = (WEST || !A.xzflow) ? st[SL::oF + a * FBX + b] : 0;
-    const bool pos = q > 0.f;
-    const float4 cf = CXY[fi];                     // Visc weights (Schmidt and 1/DZ folded in), TVD ratios
-    float K = tofl<KT>(Vis[visb], A.ksh) * cf.x + tofl<KT>(Vis[visb - visst], A.ksh) * cf.y;
-    if (A.nullDif && q == 0.f) K = 0.f;
-    const float auxK = (ff & ACT) ? K * area : 0.f;
-    const float kd = pos ? -auxK : auxK;
-    const float qv = (ff & ADV) ? q : 0.f;
-    const int pa = pb - pst;
-    const int iup = pos ? pa : pb, idn = pos ? pb : pa;
-    const int iuu = pos ? pa - pst : pb + pst;
-    float gr = 0.f, qvc = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
-    if (METHOD == 4) {
-        const bool tvd = (ff & ADV) && (ff & (pos ? TVDP : TVDN));   // not NearBoundary
-        gr = pos ? cf.z : cf.w;
-        float Cr = q * A.DT * RVt[pos ? vb - vst : vb];
-        if (LIM == 5) {
-            const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
-            pa5 = 0.5f + t6;
-            pb5 = 0.5f - t6;
-            if (fabsf(Cr) < 1e-16f) Cr = 1e-16f;
-            p2 = 2.f / (1.f - Cr);
-            pcr = 2.f / Cr;
-        }
-        qvc = tvd ? q * (0.5f - 0.5f * Cr) : 0.f;
-    }
-    float* out = FXY + fi;
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-        const float* Pt = P + t * (TY + 4) * PBX;
-        const float Pup = Pt[iup];
-        const float dd = Pt[idn] - Pup;
-        float o = fmaf(kd, dd, qv * Pup);
-        if (METHOD == 4) o = fmaf(qvc, limited_slope<LIM>((Pup - Pt[iuu]) * gr, dd, pa5, pb5, p2, pcr), o);
-        out[t * cs] = o;
-    }
-}
-
-// reciprocal with at most 1 ulp error (PTX rcp.approx), for the pivots
-__device__ __forceinline__ float rcp_approx(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
 __global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M)
 {
-    using SL = StageLayout<NT, QT, KT>;
-    using SM = Smem<NT, QT, KT>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4* CX = reinterpret_cast<float4*>(smem_raw + SM::oCX);
-    float4* CY = reinterpret_cast<float4*>(smem_raw + SM::oCY);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::oBar);
-    int* kminp = reinterpret_cast<int*>(smem_raw + SM::oBar + 32);
-    unsigned* done = reinterpret_cast<unsigned*>(smem_raw + SM::oBar + 64);
-
-    const BLayout& L = A.L;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int i0 = 1 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
-    const int i = i0 + tx, j = j0 + ty;
-    const bool inside = i <= L.ni && j <= L.nj;
-    const long long c2 = L.at2(i, j);
-    const uint8_t cf = inside ? A.cflag[c2] : 0;
-    const bool solve = cf & C_SOLVE;
-    const int kb = solve ? A.kfloor[c2] : L.nk + 1;
-
-    if (tid == 0) {
-        *kminp = L.nk + 1;
-        *done = 0;
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
-    for (int e = tid; e < NWF; e += NTH) {
-        float4 c = A.fc[L.at2(i0 + e % TX, j0 + e / TX)];
-        c.x *= A.schmidtH; c.y *= A.schmidtH;
-        CX[e] = c;
-    }
-    for (int e = tid; e < NSF; e += NTH) {
-        float4 c = A.fc[L.n2 + L.at2(i0 + e % (TX + 1), j0 + e / (TX + 1))];
-        c.x *= A.schmidtH; c.y *= A.schmidtH;
-        CY[e] = c;
-    }
-    __syncthreads();
-    if (solve) atomicMin(kminp, kb);
-    __syncthreads();
-    const int kmin = *kminp;
-    if (kmin > L.nk) return;                       // no water column in this tile
-
-    // TMA box origins (x on 16-byte boundaries of the batched layout)
-    const int xP = i0 + kXOff - 4, xV = i0 + kXOff - 4;
-    const int xVis = i0 + kXOff - Box<KT>::visOff, xO = i0 + kXOff;
-    const int yP = j0 + kYOff - 2, yV = j0 + kYOff - 1, yO = j0 + kYOff;
-    auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
-        unsigned char* d = smem_raw + (s ? SM::oStage1 : SM::oStage0);
-        uint64_t* br = &bar[s];
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // earlier reads of buffer s
-        mbar_expect_tx(br, SL::tx_bytes);
-        tma4(d + SL::oP, &M.P, xP, yP, k, A.t0, br);
-        tma3(d + SL::oF, &M.F, xO, yO, k, br);
-        tma3(d + SL::oV, &M.V, xV, yV, k, br);
-        tma3(d + SL::oVis, &M.Vis, xVis, yV, k, br);
-        tma3(d + SL::oQX, &M.QX, xO, yO, k, br);
-        tma3(d + SL::oAU, &M.AU, xO, yO, k, br);
-        tma3(d + SL::oQY, &M.QY, xO, yO, k, br);
-        tma3(d + SL::oAV, &M.AV, xO, yO, k, br);
-        tma3(d + SL::oVo, &M.Vo, xO, yO, k, br);
-        tma3(d + SL::oQz, &M.Qz, xO, yO, k + 1, br);
-        tma3(d + SL::oDv, &M.Dv, xO, yO, k + 1, br);
-        tma3(d + SL::oDz, &M.Dz, xO, yO, k, br);
-        tma3(d + SL::oFn, &M.Fn, xO, yO, k + 1, br);
-    };
-    if (tid == 0) {
-        issue(kmin, kmin & 1);
-        if (kmin < L.nk) issue(kmin + 1, (kmin + 1) & 1);
-    }
-
-    const bool horiz = !A.vertical1D;
-    const float DT = A.DT;
-    const float areaCol = solve ? A.areaCol[c2] : 0.f;
-    // k-invariant conditions of the column's vertical terms
-    const bool vdif = L.nk > 1 && !(cf & C_SD);
-    const bool vadv = L.nk > 1 && !A.vertical1D && (cf & C_CFWTOP) && (cf & C_OPTOP);
-    const bool obcCol = (cf & C_BP) && A.Ref != nullptr;
-    // own-column values of the face below row k slide up the walk: transport,
-    // conductance Kz * area / DZZ (AD:2736-2765), cell flags of rows k-1 and k
-    float qz = 0.f, kzb = 0.f;
-    uint8_t flm = 0, fl = 0;
-    const long long cb = L.at(i, j, 0);
-    if (solve) {
-        const long long a = cb + (long long)kb * L.sl;
-        qz = ldg_as<QT>(A.Qz, a, A.qsz);
-        fl = A.flag[a];
-        flm = A.flag[a - L.sl];
-        if (vdif && (fl & F_CFW)) {
-            float kz = A.coefV * ldg_as<KT>(A.DiffV, a, A.ksv) + A.backV;
-            if (A.nullDif && qz == 0.f) kz = 0.f;
-            kzb = kz * areaCol * A.DZZ[a - L.sl];          // DZZ holds 1/DZZ
-        }
-    }
-    float Gp[NT];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) Gp[t] = 0.f;
-    float Wp = 0.f;
-    unsigned bad = 0;
-    uint32_t phase = 0;                            // bit s: parity of buffer s
-    const int own = ty * OWN + tx;
-    const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
-    float* const Wc = A.W + cb;
-    float* const Po = A.Pout + cb;
-
-    for (int k = kmin; k <= L.nk; ++k) {
-        const int s = k & 1;
-        const unsigned char* st = smem_raw + (s ? SM::oStage1 : SM::oStage0);
-        float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX + s * SM::FXYStride);
-        float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY + s * SM::FXYStride);
-        const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
-        phase ^= 1u << s;
-
-        // ---- faces of the tile at layer k: own west and south faces; the
-        //      east row (warp 0) and north column (warp 1) close the tile
-        if (horiz && ok) {
-            face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, ty, tx);
-            face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, ty, tx);
-            if (ty == 0) face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, TY, tx);
-            else if (ty == 1 && tx < TY) face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, tx, TX);
-        }
-        if (__syncthreads_or(!ok)) {               // a stage never arrived: leave cleanly
-            if (tid == 0) {
-                atomicOr(A.status, MOHID_DEV_TIMEOUT);
-                mbar_wait_bounded(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u, kWaitLimit);
-            }
-            return;
-        }
-
-        if (solve && k >= kb) {
-            // ---- row k of column (i,j): tracer-independent matrix
-            const long long ko = (long long)k * L.sl;
-            const bool top = k == L.nk;
-            const uint8_t flp = top ? 0 : (st + SL::oFn)[own];
-            const float rVk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
-            const float dvr = reinterpret_cast<const float*>(st + SL::oVo)[own];   // (V - Vold)/V
-            const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
-            const float dtv = DT * rVk;
-            const bool open = fl & F_OP;
-            // VolumeVariation: TI = P*Vold/V = P*(1 - (V-Vold)/V), E(KUB) surface term;
-            // (V-Vold)/V was formed in FP64 when the volumes were packed
-            const float ratio = open ? 1.f - dvr : 1.f;
-            // VerticalDiffusion, implicit: faces k (below) and k+1 (above)
-            float kza = 0.f;
-            if (vdif && (flp & F_CFW)) {
-                float kz = A.coefV * tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) + A.backV;
-                if (A.nullDif && qzp == 0.f) kz = 0.f;
-                kza = kz * areaCol * reinterpret_cast<const float*>(st + SL::oDz)[own];   // 1/DZZ(k)
-            }
-            const float aux2 = kzb * dtv, aux1 = kza * dtv;
-            float D = -aux2, E = 1.f + aux2 + aux1, Fc = -aux1;
-            if (open && top) E += dtv * qzp;
-            if (vadv && open) {                          // VerticalAdvection, upwind, implicit
-                if (k > kb && (flm & F_OP)) {
-                    D -= fmaxf(qz, 0.f) * dtv;
-                    E -= fminf(qz, 0.f) * dtv;
-                }
-                if (!top && (flp & F_OP)) {
-                    E += fmaxf(qzp, 0.f) * dtv;
-                    Fc += fminf(qzp, 0.f) * dtv;
-                }
-            }
-            // open boundary (MassConservation): net flux through the exterior faces
-            float wfob = 0.f;
-            const bool obc = obcCol && open;
-            if (obc) {
-                const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
-                const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
-                const uint8_t* ffl = st + SL::oF + ty * FBX + tx;
-                const double hz =
-                    (double)(((ffl[0] & FU_ACT) ? tofl<QT>(qx[fw], A.qsx) : 0.f) -
-                             ((ffl[FBX] & FU_ACT) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f) +
-                             ((ffl[0] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
-                             ((ffl[1] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
-                             ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
-                wfob = (float)(hz - (double)dvr / ((double)rVk * (double)DT));
-                if (wfob >= 0.f) E += wfob * dtv;
-            }
-            // THOMASZ factorisation of row k
-            const float aux = fmaf(D, Wp, E);
-            float inv = rcp_approx(aux);
-            if (aux == 0.f) { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
-            const float W = -Fc * inv;
-            Wc[ko] = W;                                  // read back by the back-substitution
-            Wp = W;
-            const float* P = reinterpret_cast<const float*>(st + SL::oP);
-            const int po = (ty + 2) * PBX + tx + 4;
-#pragma unroll
-            for (int t = 0; t < NT; ++t) {
-                const float Pc = P[t * (TY + 4) * PBX + po];
-                float TI = Pc * ratio;
-                if (horiz)
-                    TI = fmaf(dtv, (FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
-                                   (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
-                if (obc && wfob < 0.f) {
-                    const float ext = Pc * (1.f - A.tdec) + A.Ref[(long long)t * A.ts + cb + ko] * A.tdec;
-                    TI -= wfob * ext * dtv;
-                }
-                const float G = (TI - D * Gp[t]) * inv;
-                Gp[t] = G;
-                Po[(long long)t * A.ts + ko] = G;
-            }
-            qz = qzp; kzb = kza; flm = fl; fl = flp;
-        }
-        // buffer s is free once every warp has finished row k: the last warp
-        // to get here refills it with layer k + 2 (all warps pass the barrier
-        // of layer k + 1 only after all of them got here for layer k)
-        __syncwarp();
-        if (tx == 0) {
-            const unsigned n = atomicAdd(done, 1u);
-            if ((n & (TY - 1)) == TY - 1 && k + 2 <= L.nk) issue(k + 2, s);
-        }
-    }
-
-    // ---- back-substitution (row KUB+1 solves to 0); W and G loads are issued
-    //      8 rows at a time, all tracers of the column together
-    if (solve) {
-        float x[NT];
-#pragma unroll
-        for (int t = 0; t < NT; ++t) x[t] = 0.f;
-        float chk = 0.f;                           // NaN / Inf anywhere in the column shows here
-        for (int k = L.nk; k >= kb; k -= 8) {
-            float w[8], g[NT][8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (k - q >= kb) {
-                    const long long o = (long long)(k - q) * L.sl;
-                    w[q] = __ldcg(Wc + o);
-#pragma unroll
-                    for (int t = 0; t < NT; ++t) g[t][q] = __ldcg(Po + (long long)t * A.ts + o);
-                }
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (k - q >= kb) {
-                    const long long o = (long long)(k - q) * L.sl;
-#pragma unroll
-                    for (int t = 0; t < NT; ++t) {
-                        x[t] = fmaf(w[q], x[t], g[t][q]);
-                        Po[(long long)t * A.ts + o] = x[t];
-                        chk += x[t];
-                    }
-                }
-        }
-        if (!isfinite(chk)) bad |= MOHID_DEV_NONFINITE;
-    }
-    if (bad) atomicOr(A.status, bad);
+    uint32_t phase = 0;                            // bit s: parity of stage buffer s
+    walk_init<NT, QT, KT>(smem_raw);
+    tile_walk<NT, METHOD, LIM, QT, KT>(A, M, blockIdx.x, blockIdx.y, smem_raw, phase);
 }
 
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
