@@ -255,16 +255,41 @@ class Case:
         return float(self.d.water_mask().sum()) / self.cells
 
 
+def mem_available_gb() -> float:
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 2**20
+    except Exception:
+        pass
+    return 0.0
+
+
 def make_cases(name: str):
     from mohid_gb300 import configs
     if name == "cfg4":
         return [Case(w) for w in configs.cfg4_members()]
     if name == "cfg5":
+        # about 62 GB of FP64/int32 hydrodynamics plus 4 distinct tracer and 4
+        # reference fields (4.3 GB each) and transient copies on the host
+        need = 160.0
+        have = mem_available_gb()
+        if have < need:
+            raise SystemExit(f"cfg5 needs about {need:.0f} GB of free host memory, {have:.0f} GB available")
         return [Case(configs.cfg5(), distinct_tracers=4)]
     return [Case({"cfg2": configs.cfg2, "cfg3": configs.cfg3}[name]())]
 
 
 # ----------------------------------------------------------------------------- CPU baseline
+def oracle_cases(cases):
+    """The oracle's sample of a workload: the workload itself, or for the
+    500 M-cell grid (whose FP64 work arrays alone take ~70 GB) a 1024x1024 cut
+    of it with the same layers, options and tracer kinds."""
+    if sum(c.cells for c in cases) <= 2.5e8:
+        return cases
+    return [Case(cases[0].w.scaled(ni=1024, nj=1024), distinct_tracers=1)]
+
+
 def cpu_baseline(cases, budget_s: float = 12.0, nthreads: int = 0):
     """The oracle (FP64 restatement of the reference CPU path, OpenMP) on a bounded
     sample: whole steps of one tracer on each domain in turn, until `budget_s` is spent."""
@@ -399,6 +424,10 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
     from mohid_gb300.synth import Domain, F3, I3
 
     ensemble = len(cases) > 1
+    free, total = torch.cuda.mem_get_info()
+    need = sum(c.cells for c in cases) * (120 + 12 * cases[0].nt + (4 * cases[0].nt if cases[0].refs else 0))
+    if need > 0.9 * free:
+        raise SystemExit(f"the workload needs about {need / 2**30:.0f} GiB of device memory, {free / 2**30:.0f} free")
     objs = [load_batch(c, storage) for c in cases]
     pars = [advdiff.params(**c.w.params()) for c in cases]
     if ensemble:
@@ -418,7 +447,10 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
     for _, b in objs:
         b.sync()
     nt = cases[0].nt
-    launches = steps * (1 if ensemble else groups_of(nt))
+    # the step kernel(s), plus the mass fixer's finish kernel on closed domains
+    # (every workload here has static volumes and a continuity-consistent step)
+    fix = 1 if cases[0].refs is None else 0
+    launches = steps * ((1 if ensemble else groups_of(nt)) + fix)
 
     e2e_s = h2d = d2h = None
     if e2e:
@@ -494,6 +526,8 @@ def main():
             return
         from oracle import oracle as O
         cores = os.cpu_count() or 1
+        cases = oracle_cases(cases)
+        cells = sum(c.cells for c in cases)
         for c in cases[:1]:
             P = c.tracer(0).copy()
             for _ in range(args.warmup):
@@ -559,7 +593,7 @@ def main():
     traffic = TRAFFIC.get((args.workload, r["kernel"]))
     if rank != 0:
         return
-    cpu = cpu_baseline(cases, budget_s=args.cpu_budget)
+    cpu = cpu_baseline(oracle_cases(cases), budget_s=args.cpu_budget)
     resident = sum(sum(a.nbytes for a in c.d.arrays.values()) for c in cases)
     line = {
         "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,

@@ -275,6 +275,19 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
 int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
                           int* stat);
 
+/* Mass fixer (*on != 0, the default).  No counterpart in the reference, whose
+ * FP64 arithmetic conserves mass to round-off; it restores that for the FP32
+ * form.  After every step each tracer's mass (compensated sum of VolumeZ *
+ * PROP over water cells, accumulated in the step kernel) is brought back to
+ * the FP64 mass of the field as loaded by adding one FP64 constant to every
+ * water cell, which leaves the step's result otherwise unchanged.  It runs only
+ * where mass is conserved exactly in the reference: closed boundaries (no
+ * reference concentration set), a step that maps constants onto themselves
+ * (continuity holds, XZFlow and Vertical1D off) and VolumeZ == VolumeZOld on
+ * every cell; a new hydrodynamic state moves the target by the change of
+ * VolumeZ.  Elsewhere the step runs without it. */
+int mohid_ad_batched_set_mass_fix(const int* bid, const int* on, int* stat);
+
 /* Global mass budget of tracer t: Neumaier-compensated FP64 sum of
  * VolumeZ * PROP over water cells (synchronous). */
 int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat);

@@ -66,6 +66,12 @@ class Batch:
                                             C.byref(C.c_int(int(graph))), C.byref(st))
         N.check(rc, "mohid_ad_batched_step")
 
+    def set_mass_fix(self, on: bool):
+        """Mass fixer on (default) or off (mohid_ad_batched_set_mass_fix)."""
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_set_mass_fix(C.byref(self._bid), C.byref(C.c_int(int(on))), C.byref(st)),
+                "mohid_ad_batched_set_mass_fix")
+
     def mass(self, t: int) -> float:
         m = C.c_double(0.0)
         st = C.c_int(0)

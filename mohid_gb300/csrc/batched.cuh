@@ -81,6 +81,14 @@ struct BatchArgs {
     int nt;
     const float* Ref;                   // same layout as tracers (boundary cells read), or null
     float* W;                           // scratch: THOMASZ W per cell (batched layout)
+    // mass budget of the fixer (closed domains), or mpart == null: VolumeZ as
+    // an FP32 pair hi + lo (batched layout), and per tile and tracer of the
+    // batch the sum of VolumeZ * stored value written to
+    // mpart[(t0 + t) * ntiles + by * tilesX + bx]
+    const float *Vhi, *Vlo;
+    double* mpart;
+    double* mfix;                       // the batch's fixer state (below)
+    int tilesX, ntiles, ntAll;          // tiles along i, tiles, tracers of the whole batch
     // scalars
     float DT, schmidtH, coefV, backV, tdec;
     int nullDif, vertical1D, xzflow;
@@ -113,14 +121,38 @@ int ensemble_slots(int nt, int method, int limiter, int device);
 void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4]);
 
 // packing (Fortran FP64 Size box <-> batched layout)
-cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nzSrc, cudaStream_t s);
-cudaError_t pack_recip_f32(const double* src, float* dst, const BLayout& L, cudaStream_t s);
-cudaError_t pack_f64_to_f16(const double* src, __half* dst, float invScale, const BLayout& L, cudaStream_t s);
-cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s);
-cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,
-                       const int* LP, uint8_t* dst, const BLayout& L, cudaStream_t s);
-cudaError_t pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, const BLayout& L,
-                            cudaStream_t s);
+// All hydrodynamic fields of one update in one pass: transports and
+// diffusivities to FP32 or (halfQ / halfK) to FP16 times inv[0..2] / inv[3..4],
+// areas to FP32, 1/DZZ, 1/VolumeZ and (VolumeZ - VolumeZOld)/VolumeZ formed in
+// FP64, the cell flag byte (F_*) and the face flag byte (FU_*, FV_*).
+cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, const double* V, const double* Vold,
+                        const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
+                        const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
+                        void* oQx, void* oQy, void* oQz, void* oVis, void* oDif, bool halfQ, bool halfK,
+                        const float inv[5], float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
+                        float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
+                        const BLayout& L, cudaStream_t s);
+
+// ---- mass fixer (closed domains).  Per batch a device array
+//   mfix[0] = sum of VolumeZ over water cells, mfix[1 + t] = target mass of
+//   tracer t (its FP64 mass when loaded), mfix[1 + nt + t] = the constant the
+//   stored values are relative to when loaded, mfix[1 + 2 nt + t] = the
+//   correction added to that constant since.
+// sum of VolumeZ over water cells -> mfix[0] (deterministic)
+cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, double* partial, int nblocks,
+                         double* mfix, cudaStream_t s);
+// tracer t loaded: target = FP64 mass of the Fortran-layout field P, constant = shift, correction = 0
+cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const BLayout& L, double* partial,
+                          int nblocks, double shift, int t, int nt, double* mfix, cudaStream_t s);
+// new static-volume hydrodynamics: target[t] += sum of (Vnew - (Vhi + Vlo)) * value over water
+// cells (partial: 2 * nblocks * nt doubles)
+cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, const float* Vhi,
+                            const float* Vlo, const int* WP, double* mfix, const BLayout& L, double* partial,
+                            int nblocks, cudaStream_t s);
+// after a step: correction[t] += (target[t] - mass now) / volume for every tracer of the batch
+cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s);
+// the same for `nb` batches whose argument records (device) have mpart != null
+cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
                          const int* CFW, const int* SD, float4* fc, float* areaCol,
@@ -131,22 +163,22 @@ cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX
 // than with the absolute value.
 cudaError_t pack_tracer(const double* src, float* dstA, float* dstB, const int* KFloor,
                         const int* WP, double shift, const BLayout& L, cudaStream_t s);
+// shift: the stored values' constant; corr (device, may be null): a correction added to it
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                          const int* KFloor, double shift, const BLayout& L, cudaStream_t s);
+                          const int* KFloor, double shift, const double* corr, const BLayout& L, cudaStream_t s);
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s);
-cudaError_t water_mean(const double* src, const int* WP, long long n, double* partial, int nblocks,
+cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s);
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
-                                const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
+                                const int* CFW, const int* BP2D, double DT, const BLayout& L,
                                 double* out, cudaStream_t s);
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s);
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);
 // V: VolumeZ in the Fortran Size-box layout (FP64)
-cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
+cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift, const double* corr,
                          const BLayout& L, double* partial, int nblocks, cudaStream_t s);
-cudaError_t pack_dvr(const double* V, const double* Vold, float* dst, const BLayout& L, cudaStream_t s);
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s);
 
 }  // namespace mohid

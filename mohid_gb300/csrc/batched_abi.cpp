@@ -43,6 +43,16 @@ struct Batch {
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
     DevBuf<float> Wsc;                   // THOMASZ W per cell, scratch of the step kernel
+    // mass fixer (closed domains, static volumes): VolumeZ as an FP32 pair,
+    // the fixer state (volume, targets, constants, corrections), per-tile sums
+    DevBuf<float> Vhi, Vlo;
+    DevBuf<double> mfix, mpart, fixpart;
+    DevBuf<unsigned> moving;
+    bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
+    bool staticVol = false;              // the packed hydrodynamics have VolumeZ == VolumeZOld
+    bool packedOnce = false;
+    bool fixDirty = false;               // the device constants / corrections differ from `shift`
+    int tilesX = 0, ntiles = 0;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
     // anomaly storage is exact only when the step preserves constants; this
@@ -69,13 +79,14 @@ struct Batch {
     void release()
     {
         DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ,
-                              &areaCol, &PA, &PB, &Ref, &Wsc};
+                              &areaCol, &PA, &PB, &Ref, &Wsc, &Vhi, &Vlo};
         for (auto* b : f) b->release();
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
+        mfix.release(); mpart.release(); fixpart.release(); moving.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -154,6 +165,46 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     return MOHID_AD_SUCCESS;
 }
 
+constexpr int kFixBlocks = 256;
+
+// the mass fixer runs on closed domains whose step maps constants onto
+// themselves (anomaly storage valid) and whose volumes do not move
+bool fix_active(const Batch* b)
+{
+    return b->massFix && !b->hasRef && b->shiftOk && b->staticVol;
+}
+
+// Fold the fixer's corrections into the host-side constants (shift[t] = constant
+// + correction, correction = 0) and forget the targets: the field stays exactly
+// what it was, the fixer stops until the tracers are reloaded.
+cudaError_t fix_fold(Batch* b)
+{
+    if (!b->fixDirty) return cudaSuccess;
+    const int nt = b->nt;
+    std::vector<double> mf(1 + 3 * nt);
+    cudaError_t e = cudaStreamSynchronize(b->in->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(mf.data(), b->mfix.p, sizeof(double) * mf.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    for (int t = 0; t < nt; ++t) {
+        b->shift[t] = mf[1 + nt + t] + mf[1 + 2 * nt + t];
+        mf[1 + t] = std::nan("");
+        mf[1 + nt + t] = b->shift[t];
+        mf[1 + 2 * nt + t] = 0.0;
+    }
+    e = cudaMemcpy(b->mfix.p, mf.data(), sizeof(double) * mf.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) b->fixDirty = false;
+    return e;
+}
+
+// forget the fixer targets (the mass they hold no longer applies)
+cudaError_t fix_invalidate(Batch* b, cudaStream_t s)
+{
+    std::vector<double> nan(b->nt, std::nan(""));
+    cudaError_t e = cudaMemcpyAsync(b->mfix.p + 1, nan.data(), sizeof(double) * b->nt, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+
 int pack_hydro(Batch* b, int* stat)
 {
     Instance* in = b->in;
@@ -172,35 +223,36 @@ int pack_hydro(Batch* b, int* stat)
         *sc = m > 0 ? (float)(m / 16384.0) : 1.0f;
         return e;
     };
-    if (b->storage >= 1) {
-        CK(scale(in->Qx.p, &b->qsx)); CK(scale(in->Qy.p, &b->qsy)); CK(scale(in->Qz.p, &b->qsz));
-        CK(mohid::pack_f64_to_f16(in->Qx.p, b->Qx16.p, 1.0f / b->qsx, L, s));
-        CK(mohid::pack_f64_to_f16(in->Qy.p, b->Qy16.p, 1.0f / b->qsy, L, s));
-        CK(mohid::pack_f64_to_f16(in->Qz.p, b->Qz16.p, 1.0f / b->qsz, L, s));
-    } else {
-        CK(mohid::pack_f64_to_f32(in->Qx.p, b->Qx32.p, L, in->nk + 2, s));
-        CK(mohid::pack_f64_to_f32(in->Qy.p, b->Qy32.p, L, in->nk + 2, s));
-        CK(mohid::pack_f64_to_f32(in->Qz.p, b->Qz32.p, L, in->nk + 2, s));
-    }
-    if (b->storage >= 2) {
-        CK(scale(in->ViscH.p, &b->ksh)); CK(scale(in->DiffV.p, &b->ksv));
-        CK(mohid::pack_f64_to_f16(in->ViscH.p, b->Vis16.p, 1.0f / b->ksh, L, s));
-        CK(mohid::pack_f64_to_f16(in->DiffV.p, b->Dif16.p, 1.0f / b->ksv, L, s));
-    } else {
-        CK(mohid::pack_f64_to_f32(in->ViscH.p, b->Vis32.p, L, in->nk + 2, s));
-        CK(mohid::pack_f64_to_f32(in->DiffV.p, b->Dif32.p, L, in->nk + 2, s));
-    }
-    CK(mohid::pack_recip_f32(in->V.p, b->RV.p, L, s));
-    CK(mohid::pack_dvr(in->V.p, in->Vold.p, b->DVR.p, L, s));
-    CK(mohid::pack_f64_to_f32(in->AreaU.p, b->AreaU.p, L, in->nk + 2, s));
-    CK(mohid::pack_f64_to_f32(in->AreaV.p, b->AreaV.p, L, in->nk + 2, s));
-    CK(mohid::pack_recip_f32(in->DZZ.p, b->DZZ.p, L, s));
-    CK(mohid::pack_flags(in->WP.p, in->OP.p, in->CFU.p, in->CFV.p, in->CFW.p, in->LP.p, b->flag.p, L, s));
-    CK(mohid::pack_face_flags(in->OP.p, in->CFU.p, in->CFV.p, b->fflag.p, L, s));
+    const bool hq = b->storage >= 1, hk = b->storage >= 2;
+    if (hq) { CK(scale(in->Qx.p, &b->qsx)); CK(scale(in->Qy.p, &b->qsy)); CK(scale(in->Qz.p, &b->qsz)); }
+    if (hk) { CK(scale(in->ViscH.p, &b->ksh)); CK(scale(in->DiffV.p, &b->ksv)); }
+    const float inv[5] = {1.0f / b->qsx, 1.0f / b->qsy, 1.0f / b->qsz, 1.0f / b->ksh, 1.0f / b->ksv};
+    // static volumes before and after: the tracers' target masses follow the
+    // volume change (previous VolumeZ is still in Vhi + Vlo)
+    if (b->packedOnce && b->staticVol && b->massFix && !b->hasRef)
+        CK(mohid::mass_fix_rebase(b->cur_in(), L.n3, b->nt, in->V.p, b->Vhi.p, b->Vlo.p, in->WP.p, b->mfix.p, L,
+                                  b->fixpart.p, kFixBlocks, s));
+    CK(mohid::pack_fields(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
+                          in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
+                          in->CFV.p, in->CFW.p,
+                          hq ? (void*)b->Qx16.p : (void*)b->Qx32.p, hq ? (void*)b->Qy16.p : (void*)b->Qy32.p,
+                          hq ? (void*)b->Qz16.p : (void*)b->Qz32.p, hk ? (void*)b->Vis16.p : (void*)b->Vis32.p,
+                          hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, inv, b->AreaU.p, b->AreaV.p,
+                          b->DZZ.p, b->RV.p, b->DVR.p, b->Vhi.p, b->Vlo.p, b->flag.p, b->fflag.p, b->moving.p,
+                          L, s));
+    CK(mohid::water_volume(in->V.p, in->WP.p, L, b->partial.p, kMassBlocks, b->mfix.p, s));
     CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
                            b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
     CK(cudaStreamSynchronize(s));
+    {
+        unsigned mv = 0;
+        CK(cudaMemcpy(&mv, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        const bool wasStatic = b->staticVol || !b->packedOnce;
+        b->staticVol = mv == 0;
+        if (!b->staticVol && wasStatic) CK(fix_invalidate(b, s));
+        b->packedOnce = true;
+    }
     // tensor maps of the shared fields and of the tracer buffers
     {
         const bool hq = b->storage >= 1, hk = b->storage >= 2;
@@ -271,6 +323,13 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.t0 = t0;
     a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
     a.W = b->Wsc.p;
+    a.Vhi = b->Vhi.p;
+    a.Vlo = b->Vlo.p;
+    a.mfix = b->mfix.p;
+    a.mpart = fix_active(b) ? b->mpart.p : nullptr;
+    a.tilesX = b->tilesX;
+    a.ntiles = b->ntiles;
+    a.ntAll = b->nt;
     a.DT = (float)p->DTProp;
     a.schmidtH = (float)p->schmidt_H;
     a.coefV = (float)p->SchmidtCoef_V;
@@ -297,7 +356,7 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
         if (okc) {
             CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p,
                                           in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp,
-                                          in->ni, in->nj, in->nk, b->scratch.p, s));
+                                          b->L, b->scratch.p, s));
             CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             okc = *b->hmass <= kContinuityTol;
@@ -308,6 +367,7 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
         b->checkedFlags = flags;
     }
     if (!b->shiftOk) {
+        CK(fix_fold(b));                         // constants as corrected by the mass fixer
         for (int t = 0; t < b->nt; ++t) {
             if (b->shift[t] == 0.0) continue;
             const long long off = (long long)t * b->L.n3;
@@ -339,6 +399,10 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s)
                                               b->storage >= 2, s);
         if (e != cudaSuccess) return e;
         t0 += g;
+    }
+    if (fix_active(b)) {
+        cudaError_t e = mohid::mass_fix_step(b->mpart.p, b->ntiles, b->nt, b->mfix.p, s);
+        if (e != cudaSuccess) return e;
     }
     b->cur = !b->cur;
     return cudaSuccess;
@@ -389,6 +453,8 @@ cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
     const size_t off = E->cur ? n : 0;
     cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
                                            method, limiter, E->s);
+    if (e == cudaSuccess && std::any_of(E->m.begin(), E->m.end(), fix_active))
+        e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->s);
     E->cur = !E->cur;
     return e;
 }
@@ -450,6 +516,14 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->PA.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->PB.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Wsc.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    b->tilesX = (in->ni + mohid::kTX - 1) / mohid::kTX;
+    b->ntiles = b->tilesX * ((in->nj + mohid::kTY - 1) / mohid::kTY);
+    if ((e = b->Vhi.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->Vlo.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->mfix.alloc(1 + 3 * (size_t)b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->fixpart.alloc(2 * (size_t)kFixBlocks * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->moving.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
@@ -487,12 +561,16 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
     }
     const long long off = (long long)*t * b->L.n3;
     // shift = mean over the water cells, rounded to an FP32 value
-    CK(mohid::water_mean(src, in->WP.p, (long long)in->n3, b->partial.p, kMassBlocks, b->scratch.p, s));
+    CK(mohid::water_mean(src, in->WP.p, b->L, b->partial.p, kMassBlocks, b->scratch.p, s));
     CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     double sh = std::isfinite(*b->hmass) ? (double)(float)*b->hmass : 0.0;
     b->shift[*t] = sh;
     CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, sh, b->L, s));
+    // the mass fixer keeps the FP64 mass of the field as loaded (with the volume it starts the step in)
+    CK(mohid::mass_fix_load(src, in->Vold.p, in->WP.p, b->L, b->partial.p, kMassBlocks, sh, *t, b->nt,
+                            b->mfix.p, s));
+    b->fixDirty = true;
     CK(cudaStreamSynchronize(s));
     return ok(stat);
 }
@@ -508,7 +586,8 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
     cudaStream_t s = in->stream;
     const long long off = (long long)*t * b->L.n3;
     double* dst = *on_device ? PROP : b->stage.p;
-    CK(mohid::unpack_tracer(b->cur_in() + off, dst, nullptr, in->WP.p, in->KFloor.p, b->shift[*t], b->L, s));
+    CK(mohid::unpack_tracer(b->cur_in() + off, dst, nullptr, in->WP.p, in->KFloor.p, b->shift[*t],
+                            b->mfix.p + 1 + 2 * b->nt + *t, b->L, s));
     if (!*on_device) {
         CK(cudaMemcpyAsync(PROP, b->stage.p, sizeof(double) * in->n3, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -535,6 +614,7 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
         CK(cudaMemcpyAsync(b->stage.p, ReferenceProp, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
         src = b->stage.p;
     }
+    CK(fix_fold(b));                             // open boundaries: the mass fixer stops
     CK(mohid::pack_shift_f32(src, b->Ref.p + (long long)*t * b->L.n3, in->WP.p, b->shift[*t], b->L, s));
     CK(cudaStreamSynchronize(s));
     b->hasRef = true;
@@ -570,6 +650,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     cudaStream_t s = in->stream;
+    if (fix_active(b)) b->fixDirty = true;
     if (!*use_graph) {
         for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s));
         return ok(stat);
@@ -605,6 +686,15 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     return ok(stat);
 }
 
+int mohid_ad_batched_set_mass_fix(const int* bid, const int* on, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!on) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    b->massFix = *on != 0;
+    return ok(stat);
+}
+
 int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
 {
     Batch* b = blookup(bid);
@@ -619,7 +709,8 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     }
     cudaStream_t s = in->stream;
     const float* P = b->cur_in() + (long long)*t * b->L.n3;
-    CK(mohid::mass_batched(P, in->V.p, b->flag.p, b->shift[*t], b->L, b->partial.p, kMassBlocks, s));
+    CK(mohid::mass_batched(P, in->V.p, b->flag.p, b->shift[*t], b->mfix.p + 1 + 2 * b->nt + *t, b->L,
+                           b->partial.p, kMassBlocks, s));
     CK(mohid::mass_finish(b->partial.p, kMassBlocks, b->scratch.p, s));
     CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -741,6 +832,7 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
         }
         int c = ensure_shift_valid(b, &p[q], stat);
         if (c) return c;
+        if (fix_active(b)) b->fixDirty = true;
         if (b->cur != E->cur) return fail(MOHID_AD_ERR_OPTION, stat, "a member was stepped outside the ensemble");
     }
     // members' own streams (packing, tracer loads) before the ensemble's

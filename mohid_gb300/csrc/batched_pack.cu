@@ -1,67 +1,145 @@
 // batched_pack.cu -- conversions between the Fortran FP64 Size-box arrays and
 // the batched layout, tracer anomaly bookkeeping, continuity check and the
 // compensated mass budget of the batched form.
+//
+// Every 3-D pass walks rows (j, k) of the Size box: one block per row at a
+// time, threads along i, so the Fortran reads and the batched-layout writes
+// are both contiguous and no thread divides a 64-bit index.
 #include "batched.cuh"
 #include "common.cuh"
 
 namespace mohid {
 namespace {
 
-// ------------------------------------------------------------------ packing kernels
-__global__ void k_pack_f32(const double* __restrict__ src, float* __restrict__ dst, BLayout L, int nz)
+constexpr int kRowThreads = 256;
+
+// rows (j, k), j = 0..NJ-1, k = 0..nz-1 of the Size box, shared out over the grid;
+// f(e, g, i, j, k): e Fortran index, g batched-layout index
+template <typename F>
+__device__ __forceinline__ void for_rows(const BLayout& L, int k0, int nz, F f)
 {
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * nz;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = (float)src[e];
+    const int NI = L.ni + 2, NJ = L.nj + 2;
+    const int rows = NJ * nz;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int j = r % NJ, k = k0 + r / NJ;
+        const long long e0 = (long long)NI * ((long long)j + (long long)NJ * k);
+        const long long g0 = L.at(0, j, k);
+        for (int i = threadIdx.x; i < NI; i += blockDim.x) f(e0 + i, g0 + i, i, j, k);
     }
 }
 
-__global__ void k_pack_recip(const double* __restrict__ src, float* __restrict__ dst, BLayout L)
+inline unsigned row_blocks(const BLayout& L, int nz)
 {
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = src[e] != 0.0 ? (float)(1.0 / src[e]) : 0.f;
-    }
+    const long long rows = (long long)(L.nj + 2) * nz;
+    return (unsigned)(rows < 1 ? 1 : (rows > 16384 ? 16384 : rows));
 }
 
-__global__ void k_pack_f16(const double* __restrict__ src, __half* __restrict__ dst, float inv, BLayout L)
+// 1/x to about 2^-46 relative (normal, finite x != 0): the FP32 reciprocal
+// refined by one Newton-Raphson step r' = r (2 - x r) in FP64.  The packed
+// fields are rounded to FP32 afterwards, so this is as good as a division at a
+// fraction of the GB300's FP64 division cost.
+__device__ __forceinline__ double recip64(double x)
 {
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = __float2half_rn((float)(src[e] * (double)inv));
-    }
+    const double r = (double)__frcp_rn((float)x);
+    return r * fma(-x, r, 2.0);
 }
 
-__global__ void k_pack_shift_f32(const double* __restrict__ src, float* __restrict__ dst,
-                                 const int* __restrict__ WP, double shift, BLayout L)
+// ------------------------------------------------------------------ hydrodynamic fields
+struct PackIn {
+    const double *Qx, *Qy, *Qz, *V, *Vold, *Vis, *Dif, *AU, *AV, *DZZ;
+    const int *WP, *OP, *LP, *CFU, *CFV, *CFW;
+};
+struct PackOut {
+    void *Qx, *Qy, *Qz, *Vis, *Dif;     // float, or __half (scaled) when halfQ / halfK
+    float iqx, iqy, iqz, ikh, ikv;      // 1/scale of the __half fields
+    int halfQ, halfK;
+    float *AU, *AV, *rDZZ, *RV, *DVR, *Vhi, *Vlo;
+    uint8_t *flag, *fflag;
+    unsigned* moving;                   // set when VolumeZ != VolumeZOld on any cell
+};
+
+__device__ __forceinline__ void put(void* dst, bool half, float inv, long long g, double v)
 {
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = (float)(src[e] - (WP[e] == 1 ? shift : 0.0));
-    }
+    if (half) reinterpret_cast<__half*>(dst)[g] = __float2half_rn((float)(v * (double)inv));
+    else reinterpret_cast<float*>(dst)[g] = (float)v;
+}
+
+// one pass over every cell of the Size box: transports and diffusivities
+// (FP32 or scaled FP16), areas, 1/DZZ, 1/V and (V - Vold)/V formed in FP64,
+// the cell flag byte and the face flag byte.  Face flags restate the per-face
+// conditions of ComputeAdvection1D_V2 (FN:10559: both cells open; NearBoundary
+// when the cell upstream of the upwind cell is not open) and the compute-face
+// masks; faces on the j = JUB+1 / i = IUB+1 planes are never applied by the
+// reference.
+__global__ void __launch_bounds__(kRowThreads) k_pack_fields(PackIn in, PackOut out, BLayout L)
+{
+    const int NI = L.ni + 2, NJ = L.nj + 2;
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
+        put(out.Qx, out.halfQ, out.iqx, g, in.Qx[e]);
+        put(out.Qy, out.halfQ, out.iqy, g, in.Qy[e]);
+        put(out.Qz, out.halfQ, out.iqz, g, in.Qz[e]);
+        put(out.Vis, out.halfK, out.ikh, g, in.Vis[e]);
+        put(out.Dif, out.halfK, out.ikv, g, in.Dif[e]);
+        out.AU[g] = (float)in.AU[e];
+        out.AV[g] = (float)in.AV[e];
+        const double dz = in.DZZ[e];
+        out.rDZZ[g] = dz != 0.0 ? (float)recip64(dz) : 0.f;
+        const double v = in.V[e];
+        if (v != in.Vold[e]) *out.moving = 1u;
+        const float vh = (float)v;
+        out.Vhi[g] = vh;
+        out.Vlo[g] = (float)(v - (double)vh);
+        if (v != 0.0) {
+            const double rv = recip64(v);
+            out.RV[g] = (float)rv;
+            out.DVR[g] = (float)((v - in.Vold[e]) * rv);
+        } else {
+            out.RV[g] = 0.f;
+            out.DVR[g] = 0.f;
+        }
+        const bool cfu = in.CFU[e] == 1 && j != L.nj + 1, cfv = in.CFV[e] == 1 && i != L.ni + 1;
+        const bool op = in.OP[e] == 1;
+        uint8_t f = 0;
+        if (in.WP[e] == 1) f |= F_WP;
+        if (op) f |= F_OP;
+        if (cfu) f |= F_CFU;
+        if (cfv) f |= F_CFV;
+        if (in.CFW[e] == 1) f |= F_CFW;
+        if (in.LP[e] == 1) f |= F_LP;
+        out.flag[g] = f;
+        auto opn = [&](int di, int dj) -> bool {
+            const int ii = i + di, jj = j + dj;
+            return ii >= 0 && ii < NI && jj >= 0 && jj < NJ && in.OP[e + di + (long long)NI * dj] == 1;
+        };
+        uint8_t ff = 0;
+        if (cfu) { ff |= FU_ACT; if (op && opn(0, -1)) ff |= FU_ADV; }
+        if (opn(0, -2)) ff |= FU_TVDP;
+        if (opn(0, 1)) ff |= FU_TVDN;
+        if (cfv) { ff |= FV_ACT; if (op && opn(-1, 0)) ff |= FV_ADV; }
+        if (opn(-2, 0)) ff |= FV_TVDP;
+        if (opn(1, 0)) ff |= FV_TVDN;
+        out.fflag[g] = ff;
+    });
+}
+
+__global__ void __launch_bounds__(kRowThreads) k_pack_shift_f32(const double* __restrict__ src, float* __restrict__ dst,
+                                                               const int* __restrict__ WP, double shift, BLayout L)
+{
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int, int, int) {
+        dst[g] = (float)(src[e] - (WP[e] == 1 ? shift : 0.0));
+    });
 }
 
 // mean over water cells: per-block sums and counts, then one ordered final pass
 // (deterministic, so the stored anomalies are reproducible bit for bit)
-__global__ void k_water_sum(const double* src, const int* WP, long long n, double* partial)
+__global__ void __launch_bounds__(kRowThreads) k_water_sum(const double* src, const int* WP, BLayout L, double* partial)
 {
-    __shared__ double ss[256];
-    __shared__ double sc[256];
+    __shared__ double ss[kRowThreads];
+    __shared__ double sc[kRowThreads];
     double s = 0.0, cnt = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long, int, int, int) {
         if (WP[e] == 1) { s += src[e]; cnt += 1.0; }
+    });
     ss[threadIdx.x] = s; sc[threadIdx.x] = cnt;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -84,20 +162,18 @@ __global__ void k_water_mean(const double* partial, int nb, double* out)
 //   R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT
 // over compute faces, relative to the sum of the magnitudes.  When it is at
 // round-off level the step maps a constant field onto itself.
-__global__ void k_continuity(const double* Qx, const double* Qy, const double* Qz, const double* V,
-                             const double* Vold, const int* OP, const int* CFU, const int* CFV,
-                             const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
-                             unsigned long long* out)
+__global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, const double* Qy, const double* Qz,
+                                                          const double* V, const double* Vold, const int* OP,
+                                                          const int* CFU, const int* CFV, const int* CFW,
+                                                          const int* BP2D, double rDT, BLayout L,
+                                                          unsigned long long* out)
 {
-    const long long NI = ni + 2, NJ = nj + 2, sk = NI * NJ;
-    const long long n = (long long)ni * nj * nk;
+    const int NI = L.ni + 2, nk = L.nk;
+    const long long sk = (long long)NI * (L.nj + 2);
     double m = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(e % ni);
-        const int j = 1 + (int)((e / ni) % nj);
-        const int k = 1 + (int)(e / ((long long)ni * nj));
-        const long long a = i + NI * j + sk * k, c2 = i + NI * j;
-        if (OP[a] != 1 || BP2D[c2] == 1) continue;
+    for_rows(L, 1, nk, [&](long long a, long long, int i, int j, int k) {
+        if (i < 1 || i > L.ni || j < 1 || j > L.nj) return;
+        if (OP[a] != 1 || BP2D[i + (long long)NI * j] == 1) return;
         double r = 0.0, s = 0.0, f;
         f = CFU[a] == 1 ? Qx[a] : 0.0; r += f; s += fabs(f);
         f = CFU[a + NI] == 1 ? Qx[a + NI] : 0.0; r -= f; s += fabs(f);
@@ -105,10 +181,10 @@ __global__ void k_continuity(const double* Qx, const double* Qy, const double* Q
         f = CFV[a + 1] == 1 ? Qy[a + 1] : 0.0; r -= f; s += fabs(f);
         f = CFW[a] == 1 ? Qz[a] : 0.0; r += f; s += fabs(f);
         f = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0); r -= f; s += fabs(f);
-        f = (V[a] - Vold[a]) / DT; r -= f; s += fabs(f);
-        const double rel = fabs(r) / (s + 1e-300);
+        f = (V[a] - Vold[a]) * rDT; r -= f; s += fabs(f);
+        const double rel = s > 0.0 ? fabs(r) * recip64(s) : (r != 0.0 ? 1.0 : 0.0);
         m = fmax(m, rel);
-    }
+    });
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
@@ -118,87 +194,6 @@ __global__ void k_unshift(float* P, const uint8_t* flag, double shift, long long
 {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
         if (flag[e] & F_WP) P[e] = (float)((double)P[e] + shift);
-}
-
-// relative volume change (V - Vold)/V formed in FP64, stored as FP32
-__global__ void k_pack_dvr(const double* __restrict__ V, const double* __restrict__ Vo, float* __restrict__ dst,
-                           BLayout L)
-{
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = V[e] != 0.0 ? (float)((V[e] - Vo[e]) / V[e]) : 0.f;
-    }
-}
-
-__global__ void k_pack_f64(const double* __restrict__ src, double* __restrict__ dst, BLayout L)
-{
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        dst[L.at(i, j, k)] = src[e];
-    }
-}
-
-__global__ void k_pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,
-                             const int* LP, uint8_t* dst, BLayout L)
-{
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % (L.ni + 2));
-        const int j = (int)((e / (L.ni + 2)) % (L.nj + 2));
-        const int k = (int)(e / ((long long)(L.ni + 2) * (L.nj + 2)));
-        uint8_t f = 0;
-        if (WP[e] == 1) f |= F_WP;
-        if (OP[e] == 1) f |= F_OP;
-        if (CFU[e] == 1) f |= F_CFU;
-        if (CFV[e] == 1) f |= F_CFV;
-        if (CFW[e] == 1) f |= F_CFW;
-        if (LP[e] == 1) f |= F_LP;
-        // faces only inside the work box (the reference never applies the
-        // faces on the j = JUB+1 / i = IUB+1 planes)
-        if (j == L.nj + 1) f &= (uint8_t)~F_CFU;
-        if (i == L.ni + 1) f &= (uint8_t)~F_CFV;
-        dst[L.at(i, j, k)] = f;
-    }
-}
-
-// face flag bits of every cell's west (U) and south (V) faces.  The bits restate
-// the per-face conditions of ComputeAdvection1D_V2 (FN:10559: both cells open;
-// NearBoundary when the cell upstream of the upwind cell is not open) and the
-// compute-face masks, so the step reads one byte per face.  Faces on the
-// j = JUB+1 / i = IUB+1 planes are never applied by the reference.
-__global__ void k_pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, BLayout L)
-{
-    const int NI = L.ni + 2, NJ = L.nj + 2;
-    const long long sk = (long long)NI * NJ;
-    const long long n = sk * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % NI);
-        const int j = (int)((e / NI) % NJ);
-        const int k = (int)(e / sk);
-        auto op = [&](int ii, int jj) -> bool {
-            return ii >= 0 && ii < NI && jj >= 0 && jj < NJ && OP[ii + (long long)NI * jj + sk * k] == 1;
-        };
-        uint8_t f = 0;
-        if (CFU[e] == 1 && j != L.nj + 1) {
-            f |= FU_ACT;
-            if (op(i, j - 1) && op(i, j)) f |= FU_ADV;
-        }
-        if (op(i, j - 2)) f |= FU_TVDP;
-        if (op(i, j + 1)) f |= FU_TVDN;
-        if (CFV[e] == 1 && i != L.ni + 1) {
-            f |= FV_ACT;
-            if (op(i - 1, j) && op(i, j)) f |= FV_ADV;
-        }
-        if (op(i - 2, j)) f |= FV_TVDP;
-        if (op(i + 1, j)) f |= FV_TVDN;
-        dst[L.at(i, j, k)] = f;
-    }
 }
 
 // per-column data and per-face 2-D constants
@@ -250,19 +245,16 @@ __global__ void k_pack_cols(const double* DUX, const double* DVY, const double* 
     }
 }
 
+
 // tracer: Fortran FP64 -> batched FP32 in both ping-pong buffers; cells below
 // KFloor of solved columns hold null_real and row KUB+1 holds 0, which is what
 // one reference step leaves there.
-__global__ void k_pack_tracer(const double* src, float* A, float* B, const int* KF, const int* WP,
-                              double shift, BLayout L)
+__global__ void __launch_bounds__(kRowThreads) k_pack_tracer(const double* src, float* A, float* B, const int* KF,
+                                                           const int* WP, double shift, BLayout L)
 {
-    const int NI = L.ni + 2, NJ = L.nj + 2;
-    const long long sk = (long long)NI * NJ;
-    const long long n = sk * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % NI);
-        const int j = (int)((e / NI) % NJ);
-        const int k = (int)(e / sk);
+    const int NI = L.ni + 2;
+    const long long sk = (long long)NI * (L.nj + 2);
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
         const long long c = i + (long long)NI * j;
         double v = src[e];
         const bool interior = i >= 1 && i <= L.ni && j >= 1 && j <= L.nj;
@@ -271,33 +263,30 @@ __global__ void k_pack_tracer(const double* src, float* A, float* B, const int* 
             else if (k >= 1 && k < KF[c]) v = MOHID_NULL_REAL_D;
         }
         if (WP[e] == 1) v -= shift;               // water cells hold the anomaly P - shift
-        const long long g = L.at(i, j, k);
         A[g] = (float)v;
         if (B) B[g] = (float)v;
-    }
+    });
 }
 
-__global__ void k_unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                                const int* KF, double shift, BLayout L)
+__global__ void __launch_bounds__(kRowThreads) k_unpack_tracer(const float* src, double* dst, const double* orig,
+                                                             const int* WP, const int* KF, double shift0,
+                                                             const double* corr, BLayout L)
 {
-    const int NI = L.ni + 2, NJ = L.nj + 2;
-    const long long sk = (long long)NI * NJ;
-    const long long n = sk * (L.nk + 2);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % NI);
-        const int j = (int)((e / NI) % NJ);
-        const int k = (int)(e / sk);
+    const double shift = shift0 + (corr ? *corr : 0.0);
+    const int NI = L.ni + 2;
+    const long long sk = (long long)NI * (L.nj + 2);
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
         const long long c = i + (long long)NI * j;
         const bool interior = i >= 1 && i <= L.ni && j >= 1 && j <= L.nj;
         const bool solved = interior && WP[c + sk * L.nk] == 1 && k >= 1;
         if (solved) {
-            if (k >= KF[c] && k <= L.nk) dst[e] = (double)src[L.at(i, j, k)] + (WP[e] == 1 ? shift : 0.0);
+            if (k >= KF[c] && k <= L.nk) dst[e] = (double)src[g] + (WP[e] == 1 ? shift : 0.0);
             else if (k > L.nk) dst[e] = 0.0;
             else dst[e] = MOHID_NULL_REAL_D;
         } else {
-            dst[e] = orig ? orig[e] : (double)src[L.at(i, j, k)];
+            dst[e] = orig ? orig[e] : (double)src[g];
         }
-    }
+    });
 }
 
 __global__ void k_absmax(const double* src, long long n, unsigned long long* out)
@@ -318,20 +307,16 @@ __device__ __forceinline__ void neu_add(double& s, double& c, double x)
     s = t;
 }
 
-__global__ void k_mass(const float* P, const double* V, const uint8_t* flag, double shift, BLayout L,
-                       double* partial)
+__global__ void __launch_bounds__(kRowThreads) k_mass(const float* P, const double* V, const uint8_t* flag,
+                                                    double shift0, const double* corr, BLayout L, double* partial)
 {
-    __shared__ double ss[256], sc[256];
+    __shared__ double ss[kRowThreads], sc[kRowThreads];
+    const double shift = shift0 + (corr ? *corr : 0.0);
     double s = 0.0, c = 0.0;
-    const long long n = (long long)L.ni * L.nj * L.nk;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(e % L.ni);
-        const int j = 1 + (int)((e / L.ni) % L.nj);
-        const int k = 1 + (int)(e / ((long long)L.ni * L.nj));
-        const long long g = L.at(i, j, k);
-        const long long f = i + (long long)(L.ni + 2) * (j + (long long)(L.nj + 2) * k);
-        if (flag[g] & F_WP) neu_add(s, c, V[f] * ((double)P[g] + shift));
-    }
+    for_rows(L, 1, L.nk, [&](long long f, long long g, int i, int j, int) {
+        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && (flag[g] & F_WP))
+            neu_add(s, c, V[f] * ((double)P[g] + shift));
+    });
     ss[threadIdx.x] = s; sc[threadIdx.x] = c;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -349,46 +334,127 @@ __global__ void k_mass_finish(const double* partial, int nb, double* out)
     *out = S + C;
 }
 
+// ------------------------------------------------------------------ mass fixer
+// compensated FP64 sums over water cells of the Fortran-layout arrays: V (P == null) or V * P
+__global__ void __launch_bounds__(kRowThreads) k_water_vsum(const double* V, const double* P, const int* WP,
+                                                          BLayout L, double* partial)
+{
+    __shared__ double ss[kRowThreads], sc[kRowThreads];
+    double s = 0.0, c = 0.0;
+    for_rows(L, 1, L.nk, [&](long long f, long long, int i, int j, int) {
+        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1) neu_add(s, c, P ? V[f] * P[f] : V[f]);
+    });
+    ss[threadIdx.x] = s; sc[threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0.0, C = 0.0;
+        for (int q = 0; q < (int)blockDim.x; ++q) { neu_add(S, C, ss[q]); C += sc[q]; }
+        partial[2 * blockIdx.x] = S;
+        partial[2 * blockIdx.x + 1] = C;
+    }
+}
+
+// volume: mfix[0] = sum; load: target, constant, zero correction of tracer t
+__global__ void k_fix_set(const double* partial, int nb, double* mfix, int mode, int t, int nt, double shift)
+{
+    double S = 0.0, C = 0.0;
+    for (int q = 0; q < nb; ++q) { neu_add(S, C, partial[2 * q]); C += partial[2 * q + 1]; }
+    if (mode == 0) {
+        mfix[0] = S + C;
+    } else {
+        mfix[1 + t] = S + C;
+        mfix[1 + nt + t] = shift;
+        mfix[1 + 2 * nt + t] = 0.0;
+    }
+}
+
+// one warp per tracer: the tiles' sums of VolumeZ * stored value in a fixed
+// order, then correction += (target - mass) / volume, where mass = that sum +
+// (constant + correction) * volume.  Adding the correction to every water
+// cell (through the constant) leaves the step's result otherwise unchanged:
+// the fixer only runs when the step maps constants onto themselves.
+__device__ void fix_tracers(const double* mpart, int ntiles, int nt, double* mfix)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const double W = mfix[0];
+    for (int t = warp; t < nt; t += nw) {
+        double s = 0.0, c = 0.0;
+        for (int q = lane; q < ntiles; q += 32) neu_add(s, c, mpart[(long long)t * ntiles + q]);
+        s += c;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0 && W > 0.0) {
+            const double cnow = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
+            const double mass = s + cnow * W;
+            mfix[1 + 2 * nt + t] += (mfix[1 + t] - mass) / W;
+        }
+    }
+}
+
+__global__ void k_fix_step(const double* mpart, int ntiles, int nt, double* mfix)
+{
+    fix_tracers(mpart, ntiles, nt, mfix);
+}
+
+__global__ void k_fix_step_many(const BatchArgs* As)
+{
+    const BatchArgs& a = As[blockIdx.x];
+    if (a.mpart) fix_tracers(a.mpart, a.ntiles, a.ntAll, a.mfix);
+}
+
+// new hydrodynamics with static volumes: the mass each tracer keeps changes by
+// sum over water cells of (VolumeZ_new - VolumeZ_prev) * value, VolumeZ_prev
+// being the previous pack's hi + lo pair (read before it is overwritten);
+// block y = tracer
+__global__ void __launch_bounds__(kRowThreads) k_fix_rebase(const float* P, long long ts, const double* Vnew,
+                                                          const float* Vhi, const float* Vlo, const int* WP,
+                                                          const double* mfix, int nt, BLayout L, double* partial)
+{
+    __shared__ double ss[kRowThreads], sc[kRowThreads];
+    const int t = blockIdx.y;
+    const double c0 = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
+    const float* Pt = P + (long long)t * ts;
+    double s = 0.0, c = 0.0;
+    for_rows(L, 1, L.nk, [&](long long f, long long g, int i, int j, int) {
+        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1)
+            neu_add(s, c, (Vnew[f] - ((double)Vhi[g] + (double)Vlo[g])) * ((double)Pt[g] + c0));
+    });
+    ss[threadIdx.x] = s; sc[threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0.0, C = 0.0;
+        for (int q = 0; q < (int)blockDim.x; ++q) { neu_add(S, C, ss[q]); C += sc[q]; }
+        partial[2 * ((long long)t * gridDim.x + blockIdx.x)] = S;
+        partial[2 * ((long long)t * gridDim.x + blockIdx.x) + 1] = C;
+    }
+}
+
+__global__ void k_fix_rebase_finish(const double* partial, int nb, int nt, double* mfix)
+{
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        double S = 0.0, C = 0.0;
+        for (int q = 0; q < nb; ++q) { neu_add(S, C, partial[2 * ((long long)t * nb + q)]); C += partial[2 * ((long long)t * nb + q) + 1]; }
+        mfix[1 + t] += S + C;
+    }
+}
+
 inline unsigned blocks_for(long long n) { long long b = (n + 255) / 256; return (unsigned)(b > 65535 * 8 ? 65535 * 8 : (b < 1 ? 1 : b)); }
 
 }  // namespace
 
-cudaError_t pack_f64_to_f32(const double* src, float* dst, const BLayout& L, int nz, cudaStream_t s)
+cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, const double* V, const double* Vold,
+                        const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
+                        const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
+                        void* oQx, void* oQy, void* oQz, void* oVis, void* oDif, bool halfQ, bool halfK,
+                        const float inv[5], float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
+                        float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
+                        const BLayout& L, cudaStream_t s)
 {
-    k_pack_f32<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * nz), 256, 0, s>>>(src, dst, L, nz);
-    return cudaGetLastError();
-}
-cudaError_t pack_recip_f32(const double* src, float* dst, const BLayout& L, cudaStream_t s)
-{
-    k_pack_recip<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, L);
-    return cudaGetLastError();
-}
-cudaError_t pack_f64_to_f16(const double* src, __half* dst, float inv, const BLayout& L, cudaStream_t s)
-{
-    k_pack_f16<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, inv, L);
-    return cudaGetLastError();
-}
-cudaError_t pack_dvr(const double* V, const double* Vold, float* dst, const BLayout& L, cudaStream_t s)
-{
-    k_pack_dvr<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(V, Vold, dst, L);
-    return cudaGetLastError();
-}
-cudaError_t pack_f64_to_f64(const double* src, double* dst, const BLayout& L, cudaStream_t s)
-{
-    k_pack_f64<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, L);
-    return cudaGetLastError();
-}
-cudaError_t pack_flags(const int* WP, const int* OP, const int* CFU, const int* CFV, const int* CFW,
-                       const int* LP, uint8_t* dst, const BLayout& L, cudaStream_t s)
-{
-    k_pack_flags<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(WP, OP, CFU, CFV, CFW, LP, dst, L);
-    return cudaGetLastError();
-}
-cudaError_t pack_face_flags(const int* OP, const int* CFU, const int* CFV, uint8_t* dst, const BLayout& L,
-                            cudaStream_t s)
-{
-    k_pack_face_flags<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(OP, CFU, CFV,
-                                                                                                 dst, L);
+    PackIn in{Qx, Qy, Qz, V, Vold, Vis, Dif, AU, AV, DZZ, WP, OP, LP, CFU, CFV, CFW};
+    PackOut out{oQx, oQy, oQz, oVis, oDif, inv[0], inv[1], inv[2], inv[3], inv[4], halfQ ? 1 : 0, halfK ? 1 : 0,
+                oAU, oAV, orDZZ, oRV, oDVR, oVhi, oVlo, oflag, offlag, moving};
+    cudaError_t e = cudaMemsetAsync(moving, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    k_pack_fields<<<row_blocks(L, L.nk + 2), kRowThreads, 0, s>>>(in, out, L);
     return cudaGetLastError();
 }
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
@@ -403,31 +469,30 @@ cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX
 cudaError_t pack_tracer(const double* src, float* dA, float* dB, const int* KFloor, const int* WP,
                         double shift, const BLayout& L, cudaStream_t s)
 {
-    k_pack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dA, dB, KFloor, WP, shift, L);
+    k_pack_tracer<<<row_blocks(L, L.nk + 2), kRowThreads, 0, s>>>(src, dA, dB, KFloor, WP, shift, L);
     return cudaGetLastError();
 }
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
-                          const int* KFloor, double shift, const BLayout& L, cudaStream_t s)
+                          const int* KFloor, double shift, const double* corr, const BLayout& L, cudaStream_t s)
 {
-    k_unpack_tracer<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, orig, WP, KFloor, shift, L);
+    k_unpack_tracer<<<row_blocks(L, L.nk + 2), kRowThreads, 0, s>>>(src, dst, orig, WP, KFloor, shift, corr, L);
     return cudaGetLastError();
 }
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s)
 {
-    k_pack_shift_f32<<<blocks_for((long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2)), 256, 0, s>>>(src, dst, WP, shift, L);
+    k_pack_shift_f32<<<row_blocks(L, L.nk + 2), kRowThreads, 0, s>>>(src, dst, WP, shift, L);
     return cudaGetLastError();
 }
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
-                                const int* CFW, const int* BP2D, double DT, int ni, int nj, int nk,
+                                const int* CFW, const int* BP2D, double DT, const BLayout& L,
                                 double* out, cudaStream_t s)
 {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
     if (e != cudaSuccess) return e;
-    const long long n = (long long)ni * nj * nk;
-    k_continuity<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(
-        Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, DT, ni, nj, nk, reinterpret_cast<unsigned long long*>(out));
+    k_continuity<<<row_blocks(L, L.nk), kRowThreads, 0, s>>>(Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, 1.0 / DT,
+                                                              L, reinterpret_cast<unsigned long long*>(out));
     return cudaGetLastError();
 }
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s)
@@ -435,10 +500,10 @@ cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cu
     k_unshift<<<blocks_for(n) > 8192 ? 8192 : blocks_for(n), 256, 0, s>>>(P, flag, shift, n);
     return cudaGetLastError();
 }
-cudaError_t water_mean(const double* src, const int* WP, long long n, double* partial, int nblocks,
+cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s)
 {
-    k_water_sum<<<nblocks, 256, 0, s>>>(src, WP, n, partial);
+    k_water_sum<<<nblocks, kRowThreads, 0, s>>>(src, WP, L, partial);
     k_water_mean<<<1, 1, 0, s>>>(partial, nblocks, out);
     return cudaGetLastError();
 }
@@ -449,15 +514,50 @@ cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t
     k_absmax<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(src, n, reinterpret_cast<unsigned long long*>(out));
     return cudaGetLastError();
 }
-cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift,
+cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, double shift, const double* corr,
                          const BLayout& L, double* partial, int nblocks, cudaStream_t s)
 {
-    k_mass<<<nblocks, 256, 0, s>>>(P, V, flag, shift, L, partial);
+    k_mass<<<nblocks, kRowThreads, 0, s>>>(P, V, flag, shift, corr, L, partial);
     return cudaGetLastError();
 }
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s)
 {
     k_mass_finish<<<1, 1, 0, s>>>(partial, nblocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, double* partial, int nblocks,
+                         double* mfix, cudaStream_t s)
+{
+    k_water_vsum<<<nblocks, kRowThreads, 0, s>>>(V, nullptr, WP, L, partial);
+    k_fix_set<<<1, 1, 0, s>>>(partial, nblocks, mfix, 0, 0, 0, 0.0);
+    return cudaGetLastError();
+}
+cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const BLayout& L, double* partial,
+                          int nblocks, double shift, int t, int nt, double* mfix, cudaStream_t s)
+{
+    k_water_vsum<<<nblocks, kRowThreads, 0, s>>>(V, P, WP, L, partial);
+    k_fix_set<<<1, 1, 0, s>>>(partial, nblocks, mfix, 1, t, nt, shift);
+    return cudaGetLastError();
+}
+cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s)
+{
+    const int warps = nt < 8 ? nt : 8;
+    k_fix_step<<<1, 32 * warps, 0, s>>>(mpart, ntiles, nt, mfix);
+    return cudaGetLastError();
+}
+cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, cudaStream_t s)
+{
+    k_fix_step_many<<<nb, 128, 0, s>>>(As);
+    return cudaGetLastError();
+}
+
+cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, const float* Vhi,
+                            const float* Vlo, const int* WP, double* mfix, const BLayout& L, double* partial,
+                            int nblocks, cudaStream_t s)
+{
+    k_fix_rebase<<<dim3(nblocks, nt), kRowThreads, 0, s>>>(P, ts, Vnew, Vhi, Vlo, WP, mfix, nt, L, partial);
+    k_fix_rebase_finish<<<1, 32, 0, s>>>(partial, nblocks, nt, mfix);
     return cudaGetLastError();
 }
 

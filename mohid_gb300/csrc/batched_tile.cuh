@@ -263,6 +263,16 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
     }
 }
 
+// s + c += a as an unevaluated FP32 pair (Knuth's TwoSum: the rounding error of
+// s + a is carried in c); the _rn intrinsics keep the compiler from fusing
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float a)
+{
+    const float t = __fadd_rn(s, a);
+    const float z = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(a, z)));
+    s = t;
+}
+
 // reciprocal with at most 1 ulp error (PTX rcp.approx), for the pivots
 __device__ __forceinline__ float rcp_approx(float x)
 {
@@ -336,7 +346,11 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     if (solve) atomicMin(kminp, kb);
     __syncthreads();
     const int kmin = *kminp;
-    if (kmin > L.nk) return true;                  // no water column in this tile
+    const int tile = by * A.tilesX + bx;
+    if (kmin > L.nk) {                             // no water column in this tile
+        if (A.mpart && tid < NT) A.mpart[(long long)(A.t0 + tid) * A.ntiles + tile] = 0.0;
+        return true;
+    }
 
     // TMA box origins (x on 16-byte boundaries of the batched layout)
     const int xP = i0 + kXOff - 4, xV = i0 + kXOff - 4;
@@ -509,24 +523,35 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     }
 
     // ---- back-substitution (row KUB+1 solves to 0); W and G loads are issued
-    //      8 rows at a time, all tracers of the column together
+    //      RB rows at a time, all tracers of the column together.  With the mass
+    //      fixer on, the column's sum of VolumeZ * value is accumulated as an
+    //      FP32 pair per tracer from VolumeZ = hi + lo (about 2^-44 relative).
+    const bool mf = A.mpart != nullptr;
+    constexpr int RB = 4;                          // rows per batch of loads
+    float mh[NT], ml[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) { mh[t] = 0.f; ml[t] = 0.f; }
     if (solve) {
         float x[NT];
 #pragma unroll
         for (int t = 0; t < NT; ++t) x[t] = 0.f;
         float chk = 0.f;                           // NaN / Inf anywhere in the column shows here
-        for (int k = L.nk; k >= kb; k -= 8) {
-            float w[8], g[NT][8];
+        for (int k = L.nk; k >= kb; k -= RB) {
+            float w[RB], g[NT][RB], vh[RB], vl[RB];
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
+            for (int q = 0; q < RB; ++q)
                 if (k - q >= kb) {
                     const long long o = (long long)(k - q) * L.sl;
                     w[q] = __ldcg(Wc + o);
 #pragma unroll
                     for (int t = 0; t < NT; ++t) g[t][q] = __ldcg(Po + (long long)t * A.ts + o);
+                    if (mf) {
+                        vh[q] = __ldg(A.Vhi + cb + o);
+                        vl[q] = __ldg(A.Vlo + cb + o);
+                    }
                 }
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
+            for (int q = 0; q < RB; ++q)
                 if (k - q >= kb) {
                     const long long o = (long long)(k - q) * L.sl;
 #pragma unroll
@@ -534,10 +559,40 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                         x[t] = fmaf(w[q], x[t], g[t][q]);
                         Po[(long long)t * A.ts + o] = x[t];
                         chk += x[t];
+                        if (mf) {
+                            const float pr = __fmul_rn(vh[q], x[t]);
+                            two_sum_acc(mh[t], ml[t], pr);
+                            ml[t] = __fadd_rn(ml[t], __fmaf_rn(vh[q], x[t], -pr) + vl[q] * x[t]);
+                        }
                     }
                 }
         }
         if (!isfinite(chk)) bad |= MOHID_DEV_NONFINITE;
+    }
+    if (mf) {
+        // fixed-order reduction: lanes by a shuffle tree, warps in order
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                const float oh = __shfl_down_sync(0xffffffffu, mh[t], o);
+                const float ol = __shfl_down_sync(0xffffffffu, ml[t], o);
+                two_sum_acc(mh[t], ml[t], oh);
+                ml[t] = __fadd_rn(ml[t], ol);
+            }
+        float* red = reinterpret_cast<float*>(CX);   // the face constants are no longer needed
+        if (tx == 0)
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                red[2 * (ty * NT + t)] = mh[t];
+                red[2 * (ty * NT + t) + 1] = ml[t];
+            }
+        __syncthreads();
+        if (tid < NT) {
+            double sum = 0.0;
+            for (int w = 0; w < TY; ++w) sum += (double)red[2 * (w * NT + tid)] + (double)red[2 * (w * NT + tid) + 1];
+            A.mpart[(long long)(A.t0 + tid) * A.ntiles + tile] = sum;
+        }
     }
     if (bad) atomicOr(A.status, bad);
     return true;
