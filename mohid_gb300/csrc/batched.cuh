@@ -144,11 +144,12 @@ cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, doubl
 // tracer t loaded: target = FP64 mass of the Fortran-layout field P, constant = shift, correction = 0
 cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const BLayout& L, double* partial,
                           int nblocks, double shift, int t, int nt, double* mfix, cudaStream_t s);
-// new static-volume hydrodynamics: target[t] += sum of (Vnew - (Vhi + Vlo)) * value over water
-// cells (partial: 2 * nblocks * nt doubles)
-cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, const float* Vhi,
-                            const float* Vlo, const int* WP, double* mfix, const BLayout& L, double* partial,
-                            int nblocks, cudaStream_t s);
+// new hydrodynamics: with `rebase`, target[t] += sum over water cells of
+// (Vnew - Vprev) * value (partial: 2 * nblocks * nt doubles); then Vprev = Vnew
+// (both FP64, Fortran Size-box layout)
+cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, double* Vprev, bool rebase,
+                            const int* WP, double* mfix, const BLayout& L, double* partial, int nblocks,
+                            cudaStream_t s);
 // after a step: correction[t] += (target[t] - mass now) / volume for every tracer of the batch
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s);
 // the same for `nb` batches whose argument records (device) have mpart != null
@@ -170,9 +171,10 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s);
+// *out = max(0, max over open non-boundary water cells of |R| - tol * sum |terms|)
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
-                                const int* CFW, const int* BP2D, double DT, const BLayout& L,
+                                const int* CFW, const int* BP2D, double DT, double tol, const BLayout& L,
                                 double* out, cudaStream_t s);
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s);
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s);

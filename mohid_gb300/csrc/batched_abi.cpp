@@ -47,6 +47,7 @@ struct Batch {
     // the fixer state (volume, targets, constants, corrections), per-tile sums
     DevBuf<float> Vhi, Vlo;
     DevBuf<double> mfix, mpart, fixpart;
+    DevBuf<double> Vprev;                // VolumeZ of the last pack (Fortran layout)
     DevBuf<unsigned> moving;
     bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
     bool staticVol = false;              // the packed hydrodynamics have VolumeZ == VolumeZOld
@@ -86,7 +87,7 @@ struct Batch {
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
-        mfix.release(); mpart.release(); fixpart.release(); moving.release();
+        mfix.release(); mpart.release(); fixpart.release(); moving.release(); Vprev.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -229,9 +230,9 @@ int pack_hydro(Batch* b, int* stat)
     const float inv[5] = {1.0f / b->qsx, 1.0f / b->qsy, 1.0f / b->qsz, 1.0f / b->ksh, 1.0f / b->ksv};
     // static volumes before and after: the tracers' target masses follow the
     // volume change (previous VolumeZ is still in Vhi + Vlo)
-    if (b->packedOnce && b->staticVol && b->massFix && !b->hasRef)
-        CK(mohid::mass_fix_rebase(b->cur_in(), L.n3, b->nt, in->V.p, b->Vhi.p, b->Vlo.p, in->WP.p, b->mfix.p, L,
-                                  b->fixpart.p, kFixBlocks, s));
+    CK(mohid::mass_fix_rebase(b->cur_in(), L.n3, b->nt, in->V.p, b->Vprev.p,
+                              b->packedOnce && b->staticVol && b->massFix && !b->hasRef, in->WP.p, b->mfix.p, L,
+                              b->fixpart.p, kFixBlocks, s));
     CK(mohid::pack_fields(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
                           in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
                           in->CFV.p, in->CFW.p,
@@ -355,11 +356,11 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
         bool okc = flags == 0;
         if (okc) {
             CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p,
-                                          in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp,
+                                          in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp, kContinuityTol,
                                           b->L, b->scratch.p, s));
             CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            okc = *b->hmass <= kContinuityTol;
+            okc = *b->hmass <= 0.0;
         }
         b->shiftOk = okc;
         b->checkedVersion = in->hydroVersion;
@@ -524,6 +525,7 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->fixpart.alloc(2 * (size_t)kFixBlocks * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->moving.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->Vprev.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");

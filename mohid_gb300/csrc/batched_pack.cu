@@ -34,14 +34,62 @@ inline unsigned row_blocks(const BLayout& L, int nz)
     return (unsigned)(rows < 1 ? 1 : (rows > 16384 ? 16384 : rows));
 }
 
-// 1/x to about 2^-46 relative (normal, finite x != 0): the FP32 reciprocal
-// refined by one Newton-Raphson step r' = r (2 - x r) in FP64.  The packed
-// fields are rounded to FP32 afterwards, so this is as good as a division at a
-// fraction of the GB300's FP64 division cost.
-__device__ __forceinline__ double recip64(double x)
+// FP64 -> FP32, rounded to nearest even, with integer instructions only (GB300
+// runs FP64 instructions at a small fraction of the integer rate).  Values
+// below the FP32 normal range (|x| < 2^-126) become a signed zero; overflow
+// gives a signed infinity, NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32(double x)
 {
-    const double r = (double)__frcp_rn((float)x);
-    return r * fma(-x, r, 2.0);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    const int ef = e - 1023 + 127;
+    if (ef >= 255) return __uint_as_float(sign | 0x7f800000u);
+    if (ef <= 0) return __uint_as_float(sign);
+    const unsigned mf = (unsigned)(m >> 29);
+    const unsigned long long rem = m & 0x1fffffffull;
+    unsigned r = ((unsigned)ef << 23) | mf;
+    if (rem > 0x10000000ull || (rem == 0x10000000ull && (mf & 1u))) r += 1u;   // a carry may reach infinity
+    return __uint_as_float(sign | r);
+}
+
+// the 64-bit patterns of two doubles are equal (no FP64 instruction)
+__device__ __forceinline__ bool same_bits(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// Neumaier-compensated accumulation s + c += x
+__device__ __forceinline__ void neu_add(double& s, double& c, double x)
+{
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x; else c += (x - t) + s;
+    s = t;
+}
+
+// Neumaier pairs (s, c) of a warp combined in a fixed order; lane 0 holds the result
+__device__ __forceinline__ void warp_neu(double& s, double& c)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, s, o), oc = __shfl_down_sync(0xffffffffu, c, o);
+        neu_add(s, c, os);
+        c += oc;
+    }
+}
+
+// (s, c) of all kRowThreads threads combined in a fixed order; the sum is valid in thread 0
+__device__ __forceinline__ double block_neu(double s, double c)
+{
+    __shared__ double ws[kRowThreads / 32], wc[kRowThreads / 32];
+    warp_neu(s, c);
+    if ((threadIdx.x & 31) == 0) { ws[threadIdx.x >> 5] = s; wc[threadIdx.x >> 5] = c; }
+    __syncthreads();
+    double S = 0.0, C = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kRowThreads / 32; ++q) { neu_add(S, C, ws[q]); C += wc[q]; }
+    return S + C;
 }
 
 // ------------------------------------------------------------------ hydrodynamic fields
@@ -60,12 +108,14 @@ struct PackOut {
 
 __device__ __forceinline__ void put(void* dst, bool half, float inv, long long g, double v)
 {
-    if (half) reinterpret_cast<__half*>(dst)[g] = __float2half_rn((float)(v * (double)inv));
-    else reinterpret_cast<float*>(dst)[g] = (float)v;
+    const float f = f64_to_f32(v);
+    if (half) reinterpret_cast<__half*>(dst)[g] = __float2half_rn(f * inv);
+    else reinterpret_cast<float*>(dst)[g] = f;
 }
 
 // one pass over every cell of the Size box: transports and diffusivities
-// (FP32 or scaled FP16), areas, 1/DZZ, 1/V and (V - Vold)/V formed in FP64,
+// (FP32 or scaled FP16), areas, 1/DZZ, 1/V, (V - Vold)/V with the difference
+// formed in FP64 (thin layers make it cancel), VolumeZ as an FP32 pair,
 // the cell flag byte and the face flag byte.  Face flags restate the per-face
 // conditions of ComputeAdvection1D_V2 (FN:10559: both cells open; NearBoundary
 // when the cell upstream of the upwind cell is not open) and the compute-face
@@ -80,22 +130,23 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_fields(PackIn in, PackOut 
         put(out.Qz, out.halfQ, out.iqz, g, in.Qz[e]);
         put(out.Vis, out.halfK, out.ikh, g, in.Vis[e]);
         put(out.Dif, out.halfK, out.ikv, g, in.Dif[e]);
-        out.AU[g] = (float)in.AU[e];
-        out.AV[g] = (float)in.AV[e];
-        const double dz = in.DZZ[e];
-        out.rDZZ[g] = dz != 0.0 ? (float)recip64(dz) : 0.f;
-        const double v = in.V[e];
-        if (v != in.Vold[e]) *out.moving = 1u;
-        const float vh = (float)v;
+        out.AU[g] = f64_to_f32(in.AU[e]);
+        out.AV[g] = f64_to_f32(in.AV[e]);
+        const float dz = f64_to_f32(in.DZZ[e]);
+        out.rDZZ[g] = dz != 0.f ? __frcp_rn(dz) : 0.f;
+        const double v = in.V[e], vo = in.Vold[e];
+        const float vh = f64_to_f32(v);
         out.Vhi[g] = vh;
-        out.Vlo[g] = (float)(v - (double)vh);
-        if (v != 0.0) {
-            const double rv = recip64(v);
-            out.RV[g] = (float)rv;
-            out.DVR[g] = (float)((v - in.Vold[e]) * rv);
-        } else {
-            out.RV[g] = 0.f;
+        if (same_bits(v, vo)) {
+            out.Vlo[g] = f64_to_f32(v - (double)vh);
+            out.RV[g] = vh != 0.f ? __frcp_rn(vh) : 0.f;
             out.DVR[g] = 0.f;
+        } else {
+            *out.moving = 1u;
+            out.Vlo[g] = f64_to_f32(v - (double)vh);
+            const float rv = vh != 0.f ? __frcp_rn(vh) : 0.f;
+            out.RV[g] = rv;
+            out.DVR[g] = f64_to_f32(v - vo) * rv;
         }
         const bool cfu = in.CFU[e] == 1 && j != L.nj + 1, cfv = in.CFV[e] == 1 && i != L.ni + 1;
         const bool op = in.OP[e] == 1;
@@ -134,38 +185,52 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_shift_f32(const double* __
 // (deterministic, so the stored anomalies are reproducible bit for bit)
 __global__ void __launch_bounds__(kRowThreads) k_water_sum(const double* src, const int* WP, BLayout L, double* partial)
 {
-    __shared__ double ss[kRowThreads];
-    __shared__ double sc[kRowThreads];
-    double s = 0.0, cnt = 0.0;
+    __shared__ int scount[kRowThreads / 32];
+    double s = 0.0;
+    int cnt = 0;
     for_rows(L, 0, L.nk + 2, [&](long long e, long long, int, int, int) {
-        if (WP[e] == 1) { s += src[e]; cnt += 1.0; }
+        if (WP[e] == 1) { s += src[e]; ++cnt; }
     });
-    ss[threadIdx.x] = s; sc[threadIdx.x] = cnt;
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) scount[threadIdx.x >> 5] = cnt;
+    const double S = block_neu(s, 0.0);
     if (threadIdx.x == 0) {
-        double S = 0.0, Cn = 0.0;
-        for (int q = 0; q < (int)blockDim.x; ++q) { S += ss[q]; Cn += sc[q]; }
+        long long C = 0;
+        for (int q = 0; q < kRowThreads / 32; ++q) C += scount[q];
         partial[2 * blockIdx.x] = S;
-        partial[2 * blockIdx.x + 1] = Cn;
+        partial[2 * blockIdx.x + 1] = (double)C;
     }
+}
+
+// one warp: partial[2q] summed (compensated, fixed order), and partial[2q+1] summed
+__device__ void warp_partials(const double* partial, int nb, double& sum, double& second)
+{
+    const int lane = threadIdx.x & 31;
+    double s = 0.0, c = 0.0, t = 0.0;
+    for (int q = lane; q < nb; q += 32) { neu_add(s, c, partial[2 * q]); t += partial[2 * q + 1]; }
+    warp_neu(s, c);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    sum = s + c;
+    second = t;
 }
 
 __global__ void k_water_mean(const double* partial, int nb, double* out)
 {
-    double S = 0.0, Cn = 0.0;
-    for (int q = 0; q < nb; ++q) { S += partial[2 * q]; Cn += partial[2 * q + 1]; }
-    *out = Cn > 0.0 ? S / Cn : 0.0;
+    double S, Cn;
+    warp_partials(partial, nb, S, Cn);
+    if (threadIdx.x == 0) *out = Cn > 0.0 ? S / Cn : 0.0;
 }
 
-// Largest relative continuity residual over open, non-boundary water cells,
-// with the fluxes the step applies (Fortran-layout FP64 inputs):
+// Continuity over open, non-boundary water cells, with the fluxes the step
+// applies (Fortran-layout FP64 inputs):
 //   R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT
-// over compute faces, relative to the sum of the magnitudes.  When it is at
-// round-off level the step maps a constant field onto itself.
+// over compute faces; the result is max(0, max over cells of |R| - tol * sum of
+// the terms' magnitudes).  When it is 0 the step maps a constant field onto
+// itself to round-off.
 __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, const double* Qy, const double* Qz,
                                                           const double* V, const double* Vold, const int* OP,
                                                           const int* CFU, const int* CFV, const int* CFW,
-                                                          const int* BP2D, double rDT, BLayout L,
+                                                          const int* BP2D, double rDT, double tol, BLayout L,
                                                           unsigned long long* out)
 {
     const int NI = L.ni + 2, nk = L.nk;
@@ -182,8 +247,7 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
         f = CFW[a] == 1 ? Qz[a] : 0.0; r += f; s += fabs(f);
         f = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0); r -= f; s += fabs(f);
         f = (V[a] - Vold[a]) * rDT; r -= f; s += fabs(f);
-        const double rel = s > 0.0 ? fabs(r) * recip64(s) : (r != 0.0 ? 1.0 : 0.0);
-        m = fmax(m, rel);
+        m = fmax(m, fma(-tol, s, fabs(r)));       // > 0 where |R| exceeds tol * sum |terms|
     });
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
@@ -300,69 +364,57 @@ __global__ void k_absmax(const double* src, long long n, unsigned long long* out
 
 // Neumaier-compensated FP64 sum of V*P over water cells: per-thread compensated
 // partial sums, exact-order block reduction, then one deterministic final pass.
-__device__ __forceinline__ void neu_add(double& s, double& c, double x)
-{
-    const double t = s + x;
-    if (fabs(s) >= fabs(x)) c += (s - t) + x; else c += (x - t) + s;
-    s = t;
-}
-
 __global__ void __launch_bounds__(kRowThreads) k_mass(const float* P, const double* V, const uint8_t* flag,
                                                     double shift0, const double* corr, BLayout L, double* partial)
 {
-    __shared__ double ss[kRowThreads], sc[kRowThreads];
     const double shift = shift0 + (corr ? *corr : 0.0);
     double s = 0.0, c = 0.0;
     for_rows(L, 1, L.nk, [&](long long f, long long g, int i, int j, int) {
         if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && (flag[g] & F_WP))
             neu_add(s, c, V[f] * ((double)P[g] + shift));
     });
-    ss[threadIdx.x] = s; sc[threadIdx.x] = c;
-    __syncthreads();
+    const double S = block_neu(s, c);
     if (threadIdx.x == 0) {
-        double S = 0.0, C = 0.0;
-        for (int q = 0; q < (int)blockDim.x; ++q) { neu_add(S, C, ss[q]); C += sc[q]; }
         partial[2 * blockIdx.x] = S;
-        partial[2 * blockIdx.x + 1] = C;
+        partial[2 * blockIdx.x + 1] = 0.0;
     }
 }
 
 __global__ void k_mass_finish(const double* partial, int nb, double* out)
 {
-    double S = 0.0, C = 0.0;
-    for (int q = 0; q < nb; ++q) { neu_add(S, C, partial[2 * q]); C += partial[2 * q + 1]; }
-    *out = S + C;
+    double S, Z;
+    warp_partials(partial, nb, S, Z);
+    if (threadIdx.x == 0) *out = S;
 }
 
 // ------------------------------------------------------------------ mass fixer
-// compensated FP64 sums over water cells of the Fortran-layout arrays: V (P == null) or V * P
+// FP64 sums over water cells of the Fortran-layout arrays: V (P == null) or
+// V * P.  Each thread sums its cells (a few dozen) in FP64; the threads' and
+// blocks' sums are combined with Neumaier compensation in a fixed order.
 __global__ void __launch_bounds__(kRowThreads) k_water_vsum(const double* V, const double* P, const int* WP,
                                                           BLayout L, double* partial)
 {
-    __shared__ double ss[kRowThreads], sc[kRowThreads];
-    double s = 0.0, c = 0.0;
+    double s = 0.0;
     for_rows(L, 1, L.nk, [&](long long f, long long, int i, int j, int) {
-        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1) neu_add(s, c, P ? V[f] * P[f] : V[f]);
+        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1) s = P ? fma(V[f], P[f], s) : s + V[f];
     });
-    ss[threadIdx.x] = s; sc[threadIdx.x] = c;
-    __syncthreads();
+    const double S = block_neu(s, 0.0);
     if (threadIdx.x == 0) {
-        double S = 0.0, C = 0.0;
-        for (int q = 0; q < (int)blockDim.x; ++q) { neu_add(S, C, ss[q]); C += sc[q]; }
         partial[2 * blockIdx.x] = S;
-        partial[2 * blockIdx.x + 1] = C;
+        partial[2 * blockIdx.x + 1] = 0.0;
     }
 }
 
 // volume: mfix[0] = sum; load: target, constant, zero correction of tracer t
 __global__ void k_fix_set(const double* partial, int nb, double* mfix, int mode, int t, int nt, double shift)
 {
-    double S = 0.0, C = 0.0;
-    for (int q = 0; q < nb; ++q) { neu_add(S, C, partial[2 * q]); C += partial[2 * q + 1]; }
+    double S, Z;
+    warp_partials(partial, nb, S, Z);
+    if (threadIdx.x != 0) return;
     if (mode == 0) {
-        mfix[0] = S + C;
+        mfix[0] = S;
     } else {
-        mfix[1 + t] = S + C;
+        mfix[1 + t] = S;
         mfix[1 + nt + t] = shift;
         mfix[1 + 2 * nt + t] = 0.0;
     }
@@ -402,39 +454,43 @@ __global__ void k_fix_step_many(const BatchArgs* As)
 }
 
 // new hydrodynamics with static volumes: the mass each tracer keeps changes by
-// sum over water cells of (VolumeZ_new - VolumeZ_prev) * value, VolumeZ_prev
-// being the previous pack's hi + lo pair (read before it is overwritten);
-// block y = tracer
+// the sum over water cells of (VolumeZ_new - VolumeZ_prev) * value; cells whose
+// volume did not change (bit for bit) cost no FP64 instruction.  VolumeZ_prev
+// is then replaced by VolumeZ_new.  Block y = tracer.
 __global__ void __launch_bounds__(kRowThreads) k_fix_rebase(const float* P, long long ts, const double* Vnew,
-                                                          const float* Vhi, const float* Vlo, const int* WP,
-                                                          const double* mfix, int nt, BLayout L, double* partial)
+                                                          double* Vprev, const int* WP, const double* mfix, int nt,
+                                                          BLayout L, double* partial)
 {
-    __shared__ double ss[kRowThreads], sc[kRowThreads];
     const int t = blockIdx.y;
     const double c0 = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
     const float* Pt = P + (long long)t * ts;
-    double s = 0.0, c = 0.0;
+    double s = 0.0;
     for_rows(L, 1, L.nk, [&](long long f, long long g, int i, int j, int) {
-        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1)
-            neu_add(s, c, (Vnew[f] - ((double)Vhi[g] + (double)Vlo[g])) * ((double)Pt[g] + c0));
+        const double vn = Vnew[f], vp = Vprev[f];
+        if (same_bits(vn, vp)) return;
+        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1) s = fma(vn - vp, (double)Pt[g] + c0, s);
     });
-    ss[threadIdx.x] = s; sc[threadIdx.x] = c;
-    __syncthreads();
+    const double S = block_neu(s, 0.0);
     if (threadIdx.x == 0) {
-        double S = 0.0, C = 0.0;
-        for (int q = 0; q < (int)blockDim.x; ++q) { neu_add(S, C, ss[q]); C += sc[q]; }
         partial[2 * ((long long)t * gridDim.x + blockIdx.x)] = S;
-        partial[2 * ((long long)t * gridDim.x + blockIdx.x) + 1] = C;
+        partial[2 * ((long long)t * gridDim.x + blockIdx.x) + 1] = 0.0;
     }
 }
 
 __global__ void k_fix_rebase_finish(const double* partial, int nb, int nt, double* mfix)
 {
-    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-        double S = 0.0, C = 0.0;
-        for (int q = 0; q < nb; ++q) { neu_add(S, C, partial[2 * ((long long)t * nb + q)]); C += partial[2 * ((long long)t * nb + q) + 1]; }
-        mfix[1 + t] += S + C;
+    for (int t = 0; t < nt; ++t) {
+        double S, Z;
+        warp_partials(partial + 2 * (long long)t * nb, nb, S, Z);
+        if (threadIdx.x == 0) mfix[1 + t] += S;
     }
+}
+
+// Vprev = Vnew over the Size box
+__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst, long long n)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        dst[e] = src[e];
 }
 
 inline unsigned blocks_for(long long n) { long long b = (n + 255) / 256; return (unsigned)(b > 65535 * 8 ? 65535 * 8 : (b < 1 ? 1 : b)); }
@@ -486,12 +542,12 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
 }
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
-                                const int* CFW, const int* BP2D, double DT, const BLayout& L,
+                                const int* CFW, const int* BP2D, double DT, double tol, const BLayout& L,
                                 double* out, cudaStream_t s)
 {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
     if (e != cudaSuccess) return e;
-    k_continuity<<<row_blocks(L, L.nk), kRowThreads, 0, s>>>(Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, 1.0 / DT,
+    k_continuity<<<row_blocks(L, L.nk), kRowThreads, 0, s>>>(Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, 1.0 / DT, tol,
                                                               L, reinterpret_cast<unsigned long long*>(out));
     return cudaGetLastError();
 }
@@ -504,7 +560,7 @@ cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, doubl
                        double* out, cudaStream_t s)
 {
     k_water_sum<<<nblocks, kRowThreads, 0, s>>>(src, WP, L, partial);
-    k_water_mean<<<1, 1, 0, s>>>(partial, nblocks, out);
+    k_water_mean<<<1, 32, 0, s>>>(partial, nblocks, out);
     return cudaGetLastError();
 }
 cudaError_t absmax_f64(const double* src, long long n, double* out, cudaStream_t s)
@@ -522,7 +578,7 @@ cudaError_t mass_batched(const float* P, const double* V, const uint8_t* flag, d
 }
 cudaError_t mass_finish(const double* partial, int nblocks, double* out, cudaStream_t s)
 {
-    k_mass_finish<<<1, 1, 0, s>>>(partial, nblocks, out);
+    k_mass_finish<<<1, 32, 0, s>>>(partial, nblocks, out);
     return cudaGetLastError();
 }
 
@@ -530,14 +586,14 @@ cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, doubl
                          double* mfix, cudaStream_t s)
 {
     k_water_vsum<<<nblocks, kRowThreads, 0, s>>>(V, nullptr, WP, L, partial);
-    k_fix_set<<<1, 1, 0, s>>>(partial, nblocks, mfix, 0, 0, 0, 0.0);
+    k_fix_set<<<1, 32, 0, s>>>(partial, nblocks, mfix, 0, 0, 0, 0.0);
     return cudaGetLastError();
 }
 cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const BLayout& L, double* partial,
                           int nblocks, double shift, int t, int nt, double* mfix, cudaStream_t s)
 {
     k_water_vsum<<<nblocks, kRowThreads, 0, s>>>(V, P, WP, L, partial);
-    k_fix_set<<<1, 1, 0, s>>>(partial, nblocks, mfix, 1, t, nt, shift);
+    k_fix_set<<<1, 32, 0, s>>>(partial, nblocks, mfix, 1, t, nt, shift);
     return cudaGetLastError();
 }
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s)
@@ -552,12 +608,16 @@ cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, const float* Vhi,
-                            const float* Vlo, const int* WP, double* mfix, const BLayout& L, double* partial,
-                            int nblocks, cudaStream_t s)
+cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, double* Vprev, bool rebase,
+                            const int* WP, double* mfix, const BLayout& L, double* partial, int nblocks,
+                            cudaStream_t s)
 {
-    k_fix_rebase<<<dim3(nblocks, nt), kRowThreads, 0, s>>>(P, ts, Vnew, Vhi, Vlo, WP, mfix, nt, L, partial);
-    k_fix_rebase_finish<<<1, 32, 0, s>>>(partial, nblocks, nt, mfix);
+    if (rebase) {
+        k_fix_rebase<<<dim3(nblocks, nt), kRowThreads, 0, s>>>(P, ts, Vnew, Vprev, WP, mfix, nt, L, partial);
+        k_fix_rebase_finish<<<1, 32, 0, s>>>(partial, nblocks, nt, mfix);
+    }
+    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
+    k_copy_f64<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(Vnew, Vprev, n);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@ def main():
     ap.add_argument("--ni", type=int, default=0)
     ap.add_argument("--nj", type=int, default=0)
     ap.add_argument("--tracers", type=int, default=0)
+    ap.add_argument("--no-mass-fix", action="store_true", help="batched form without the mass fixer")
     args = ap.parse_args()
     build.build()
     import torch
@@ -38,6 +39,7 @@ def main():
     p = advdiff.params(**w.params())
     if args.form == "batched":
         b = batched.Batch(ad, len(tr), args.storage)
+        b.set_mass_fix(not args.no_mass_fix)
         for t, P in enumerate(tr):
             b.set_tracer(t, P)
             if refs:
