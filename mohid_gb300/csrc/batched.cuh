@@ -106,6 +106,7 @@ struct TmaMaps {
     CUtensorMap QY, AV;                 // south faces: box (36 | 40, TY, 1), (36, TY, 1)
     CUtensorMap Vo;                     // (V - Vold)/V, f32, own cells: box (32, TY, 1)
     CUtensorMap Qz, Dv, Dz, Fn;         // own cells of the layer above / 1/DZZ: box (32, TY, 1)
+    CUtensorMap Vh, Vl;                 // VolumeZ as an FP32 pair, own cells (L2 prefetch only): box (32, TY, 1)
 };
 
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
@@ -117,8 +118,9 @@ cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* 
                             int nt, int method, int limiter, cudaStream_t s);
 // resident CTAs of the ensemble kernel on `device` (0 on error)
 int ensemble_slots(int nt, int method, int limiter, int device);
-// box extents (elements, x y z w) of the 13 maps in TmaMaps order
-void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4]);
+// box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order
+constexpr int kNumMaps = 15;
+void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4]);
 
 // packing (Fortran FP64 Size box <-> batched layout)
 // All hydrodynamic fields of one update in one pass: transports and
@@ -153,7 +155,7 @@ cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* 
 // after a step: correction[t] += (target[t] - mass now) / volume for every tracer of the batch
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s);
 // the same for `nb` batches whose argument records (device) have mpart != null
-cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, cudaStream_t s);
+cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
                          const int* CFW, const int* SD, float4* fc, float* areaCol,

@@ -257,7 +257,7 @@ int pack_hydro(Batch* b, int* stat)
     // tensor maps of the shared fields and of the tracer buffers
     {
         const bool hq = b->storage >= 1, hk = b->storage >= 2;
-        int box[13][4];
+        int box[mohid::kNumMaps][4];
         mohid::batched_boxes(hq, hk, 1, box);
         const CUtensorMapDataType tq = hq ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         const CUtensorMapDataType tk = hk ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -281,11 +281,13 @@ int pack_hydro(Batch* b, int* stat)
         okm &= encode_map(&M.Dv, tk, ek, dif, L, 1, box[10]);
         okm &= encode_map(&M.Dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DZZ.p, L, 1, box[11]);
         okm &= encode_map(&M.Fn, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[12]);
+        okm &= encode_map(&M.Vh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vhi.p, L, 1, box[13]);
+        okm &= encode_map(&M.Vl, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vlo.p, L, 1, box[14]);
         const int gs[3] = {1, 2, 4};
         for (int buf = 0; buf < 2; ++buf)
             for (int g = 0; g < 3; ++g) {
                 if (gs[g] > b->nt) continue;
-                int bb[13][4];
+                int bb[mohid::kNumMaps][4];
                 mohid::batched_boxes(hq, hk, gs[g], bb);
                 okm &= encode_map(&b->mapP[buf][g], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                                   buf ? b->PB.p : b->PA.p, L, b->nt, bb[0], 4);
@@ -455,7 +457,7 @@ cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
     cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
                                            method, limiter, E->s);
     if (e == cudaSuccess && std::any_of(E->m.begin(), E->m.end(), fix_active))
-        e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->s);
+        e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->nt, E->s);
     E->cur = !E->cur;
     return e;
 }

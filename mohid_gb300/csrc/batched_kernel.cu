@@ -77,16 +77,16 @@ size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk)
 }
 
 // box extents of the tensor maps (elements), for the host-side encoder
-void batched_boxes(bool halfQ, bool halfK, int nt, int box[13][4])
+void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4])
 {
     const int qyX = halfQ ? Box<__half>::qyX : Box<float>::qyX;
     const int visX = halfK ? Box<__half>::visX : Box<float>::visX;
-    const int b[13][4] = {{PBX, TY + 4, 1, nt}, {FBX, TY + 1, 1, 1}, {VBX, TY + 2, 1, 1},
-                          {visX, TY + 2, 1, 1}, {TX, TY + 1, 1, 1},   {TX, TY + 1, 1, 1},
-                          {qyX, TY, 1, 1},      {AVX, TY, 1, 1},      {OWN, TY, 1, 1},
-                          {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1},
-                          {OWN, TY, 1, 1}};
-    for (int q = 0; q < 13; ++q)
+    const int b[kNumMaps][4] = {{PBX, TY + 4, 1, nt}, {FBX, TY + 1, 1, 1}, {VBX, TY + 2, 1, 1},
+                                {visX, TY + 2, 1, 1}, {TX, TY + 1, 1, 1},   {TX, TY + 1, 1, 1},
+                                {qyX, TY, 1, 1},      {AVX, TY, 1, 1},      {OWN, TY, 1, 1},
+                                {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1},
+                                {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1}};
+    for (int q = 0; q < kNumMaps; ++q)
         for (int d = 0; d < 4; ++d) box[q][d] = b[q][d];
 }
 

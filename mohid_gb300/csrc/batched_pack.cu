@@ -420,37 +420,38 @@ __global__ void k_fix_set(const double* partial, int nb, double* mfix, int mode,
     }
 }
 
-// one warp per tracer: the tiles' sums of VolumeZ * stored value in a fixed
-// order, then correction += (target - mass) / volume, where mass = that sum +
-// (constant + correction) * volume.  Adding the correction to every water
+// one block per tracer: the tiles' sums of VolumeZ * stored value (each
+// thread a strided share in FP64, the threads combined by a compensated tree in
+// a fixed order), then correction += (target - mass) / volume, where mass = that
+// sum + (constant + correction) * volume.  Adding the correction to every water
 // cell (through the constant) leaves the step's result otherwise unchanged:
 // the fixer only runs when the step maps constants onto themselves.
-__device__ void fix_tracers(const double* mpart, int ntiles, int nt, double* mfix)
+__device__ void fix_tracer(const double* mpart, int ntiles, int nt, int t, double* mfix)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const double W = mfix[0];
-    for (int t = warp; t < nt; t += nw) {
-        double s = 0.0, c = 0.0;
-        for (int q = lane; q < ntiles; q += 32) neu_add(s, c, mpart[(long long)t * ntiles + q]);
-        s += c;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0 && W > 0.0) {
+    double s = 0.0;
+    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) s += mpart[(long long)t * ntiles + q];
+    const double sum = block_neu(s, 0.0);
+    if (threadIdx.x == 0) {
+        const double W = mfix[0];
+        if (W > 0.0) {
             const double cnow = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
-            const double mass = s + cnow * W;
-            mfix[1 + 2 * nt + t] += (mfix[1 + t] - mass) / W;
+            mfix[1 + 2 * nt + t] += (mfix[1 + t] - (sum + cnow * W)) / W;
         }
     }
 }
 
-__global__ void k_fix_step(const double* mpart, int ntiles, int nt, double* mfix)
+// block t: tracer t of the batch
+__global__ void __launch_bounds__(kRowThreads) k_fix_step(const double* mpart, int ntiles, int nt, double* mfix)
 {
-    fix_tracers(mpart, ntiles, nt, mfix);
+    fix_tracer(mpart, ntiles, nt, blockIdx.x, mfix);
 }
 
-__global__ void k_fix_step_many(const BatchArgs* As)
+// block (b, t): tracer t of batch b (blocks past a batch's tracer count return)
+__global__ void __launch_bounds__(kRowThreads) k_fix_step_many(const BatchArgs* As)
 {
     const BatchArgs& a = As[blockIdx.x];
-    if (a.mpart) fix_tracers(a.mpart, a.ntiles, a.ntAll, a.mfix);
+    if (!a.mpart || (int)blockIdx.y >= a.ntAll) return;
+    fix_tracer(a.mpart, a.ntiles, a.ntAll, blockIdx.y, a.mfix);
 }
 
 // new hydrodynamics with static volumes: the mass each tracer keeps changes by
@@ -598,13 +599,12 @@ cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const
 }
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s)
 {
-    const int warps = nt < 8 ? nt : 8;
-    k_fix_step<<<1, 32 * warps, 0, s>>>(mpart, ntiles, nt, mfix);
+    k_fix_step<<<nt, kRowThreads, 0, s>>>(mpart, ntiles, nt, mfix);
     return cudaGetLastError();
 }
-cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, cudaStream_t s)
+cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s)
 {
-    k_fix_step_many<<<nb, 128, 0, s>>>(As);
+    k_fix_step_many<<<dim3(nb, ntmax), kRowThreads, 0, s>>>(As);
     return cudaGetLastError();
 }
 

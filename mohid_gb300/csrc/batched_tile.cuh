@@ -159,6 +159,38 @@ __device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, int x, i
         ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
         : "memory");
 }
+// L2 eviction priorities: the THOMASZ scratch (W, G) written on the way up and
+// read once on the way down is kept in L2 ahead of the streamed layer inputs
+__device__ __forceinline__ uint64_t l2_policy_evict_last()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void st_l2hint(float* a, float v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ float ld_l2hint(const float* a, uint64_t pol)
+{
+    float v;
+    asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol) : "memory");
+    return v;
+}
+
+// bulk-tensor prefetch of one tile into L2 (no shared memory, no completion)
+__device__ __forceinline__ void tma3_prefetch_l2(const CUtensorMap* map, int x, int y, int z)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];"
+                 ::"l"(map), "r"(x), "r"(y), "r"(z)
+                 : "memory");
+}
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // psi(r) * d for r = n / d, psi one of the ComputeAdvectionFace limiters
@@ -412,6 +444,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
     float* const Wc = A.W + cb;
     float* const Po = A.Pout + cb;
+    const uint64_t keep = l2_policy_evict_last(), drop = l2_policy_evict_first();
 
     for (int k = kmin; k <= L.nk; ++k) {
         const int s = k & 1;
@@ -491,7 +524,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             float inv = rcp_approx(aux);
             if (aux == 0.f) { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
             const float W = -Fc * inv;
-            Wc[ko] = W;                                  // read back by the back-substitution
+            st_l2hint(Wc + ko, W, keep);                 // read back by the back-substitution
             Wp = W;
             const float* P = reinterpret_cast<const float*>(st + SL::oP);
             const int po = (ty + 2) * PBX + tx + 4;
@@ -508,7 +541,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                 }
                 const float G = (TI - D * Gp[t]) * inv;
                 Gp[t] = G;
-                Po[(long long)t * A.ts + ko] = G;
+                st_l2hint(Po + (long long)t * A.ts + ko, G, keep);
             }
             qz = qzp; kzb = kza; flm = fl; fl = flp;
         }
@@ -542,12 +575,12 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             for (int q = 0; q < RB; ++q)
                 if (k - q >= kb) {
                     const long long o = (long long)(k - q) * L.sl;
-                    w[q] = __ldcg(Wc + o);
+                    w[q] = ld_l2hint(Wc + o, drop);
 #pragma unroll
-                    for (int t = 0; t < NT; ++t) g[t][q] = __ldcg(Po + (long long)t * A.ts + o);
+                    for (int t = 0; t < NT; ++t) g[t][q] = ld_l2hint(Po + (long long)t * A.ts + o, drop);
                     if (mf) {
-                        vh[q] = __ldg(A.Vhi + cb + o);
-                        vl[q] = __ldg(A.Vlo + cb + o);
+                        vh[q] = ld_l2hint(A.Vhi + cb + o, drop);
+                        vl[q] = ld_l2hint(A.Vlo + cb + o, drop);
                     }
                 }
 #pragma unroll
