@@ -447,10 +447,14 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
     for _, b in objs:
         b.sync()
     nt = cases[0].nt
-    # the step kernel(s), plus the mass fixer's finish kernel on closed domains
-    # (every workload here has static volumes and a continuity-consistent step)
-    fix = 1 if cases[0].refs is None else 0
-    launches = steps * ((1 if ensemble else groups_of(nt)) + fix)
+    if ensemble:
+        # one ensemble launch, plus the mass fixer's finish on closed domains
+        # (every ensemble workload here has static volumes)
+        launches = steps * (1 + (1 if cases[0].refs is None else 0))
+        sched = {"launches": launches // steps, "sched": "persistent tile list (ensemble)", "split": nt}
+    else:
+        sched = objs[0][1].schedule()              # as chosen by the autotuner
+        launches = steps * sched["launches"]
 
     e2e_s = h2d = d2h = None
     if e2e:
@@ -487,8 +491,9 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
         b.destroy()
         ad.kill()
     cells = sum(c.cells for c in cases)
-    g = 1 if ensemble else groups_of(nt)
-    return dict(ms=ms, kernel_ms=ms / g, launches=launches, e2e_s=e2e_s, h2d=h2d, d2h=d2h, cells=cells,
+    # step-kernel launches per step (the fixer's finish excluded; its time stays in ms)
+    g = 1 if ensemble else sched["launches"] - (1 if cases[0].refs is None else 0)
+    return dict(ms=ms, kernel_ms=ms / g, launches=launches, e2e_s=e2e_s, h2d=h2d, d2h=d2h, cells=cells, sched=sched,
                 nt=nt, bytes_per_update=8.0 + SHARED_BYTES[storage] / nt,
                 bytes_per_launch=cells * (8.0 * nt + SHARED_BYTES[storage]) / g, dtype="f32", clocks=clocks,
                 kernel=("ensemble_kernel" if ensemble else "batched_kernel") + f"<{min(nt, 4)}>")
@@ -603,6 +608,7 @@ def main():
         "config": {"workload": workload_name, "form": args.form,
                    "time_loop": "CUDA graph of K steps" if args.form == "batched" else "stream launches",
                    "cells": cells, "tracers": nt, "domains": len(cases), "water_fraction": water,
+                   "schedule": r.get("sched"),
                    "l2": f"inputs larger than L2 ({resident / 2**30:.2f} GiB of FP64 hydrodynamics, "
                          f"the packed fields and tracers > 129 MiB)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},

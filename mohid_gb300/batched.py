@@ -66,6 +66,26 @@ class Batch:
                                             C.byref(C.c_int(int(graph))), C.byref(st))
         N.check(rc, "mohid_ad_batched_step")
 
+    def autotune(self, p: N.MohidAdParams):
+        """Time the launch schedules on this batch and keep the fastest (mohid_ad_batched_autotune)."""
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_autotune(C.byref(self._bid), C.byref(p), C.byref(st)),
+                "mohid_ad_batched_autotune")
+
+    def set_schedule(self, sched: int, split: int = 4):
+        """Fix the launch schedule by hand (0 one CTA per tile, 1 tile list; 4 or 2 tracers per launch)."""
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_set_schedule(C.byref(self._bid), C.byref(C.c_int(sched)),
+                                                       C.byref(C.c_int(split)), C.byref(st)),
+                "mohid_ad_batched_set_schedule")
+
+    def schedule(self) -> dict:
+        """{'launches': kernel launches per step, 'sched': 0 grid / 1 tile list, 'split': 4 or 2}."""
+        n, sc, sp, st = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        N.check(self.lib.mohid_ad_batched_schedule(C.byref(self._bid), C.byref(n), C.byref(sc), C.byref(sp),
+                                                   C.byref(st)), "mohid_ad_batched_schedule")
+        return {"launches": n.value, "sched": sc.value, "split": sp.value}
+
     def set_mass_fix(self, on: bool):
         """Mass fixer on (default) or off (mohid_ad_batched_set_mass_fix)."""
         st = C.c_int(0)

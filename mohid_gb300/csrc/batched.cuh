@@ -109,8 +109,13 @@ struct TmaMaps {
     CUtensorMap Vh, Vl;                 // VolumeZ as an FP32 pair, own cells (L2 prefetch only): box (32, TY, 1)
 };
 
+// tiles == null: one CTA per tile of the grid; otherwise a persistent grid over
+// the ntl (bx, by) tiles listed
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                           bool halfK, cudaStream_t s);
+                           bool halfK, const int2* tiles, int ntl, cudaStream_t s);
+// per tile (by * tilesX + bx): layers the walk visits, 0 for a tile without water
+cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int* cost,
+                       cudaStream_t s);
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
 // ensemble: one persistent grid over the (domain, bx, by, -) tiles of many
 // domains with FP32 storage; As/Ms are device tables indexed by domain

@@ -54,6 +54,15 @@ struct Batch {
     bool packedOnce = false;
     bool fixDirty = false;               // the device constants / corrections differ from `shift`
     int tilesX = 0, ntiles = 0;
+    // launch schedule: one CTA per tile, or a persistent grid over the tiles
+    // holding water, costliest first; tracers per launch; chosen by timing
+    DevBuf<int2> tl;
+    DevBuf<int> tcost;
+    int ntl = 0;
+    int sched = 0;                       // 0 grid, 1 tile list
+    int split = 4;                       // largest tracer group per launch: 4 or 2
+    bool tuned = false;
+    int graphSched = -1, graphSplit = -1;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
     // anomaly storage is exact only when the step preserves constants; this
@@ -88,6 +97,7 @@ struct Batch {
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
         mfix.release(); mpart.release(); fixpart.release(); moving.release(); Vprev.release();
+        tl.release(); tcost.release();
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -254,6 +264,23 @@ int pack_hydro(Batch* b, int* stat)
         if (!b->staticVol && wasStatic) CK(fix_invalidate(b, s));
         b->packedOnce = true;
     }
+    // tile schedule: tiles holding water, most layers first (stable by tile index)
+    {
+        CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
+        std::vector<int> cost(b->ntiles);
+        CK(cudaMemcpyAsync(cost.data(), b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::vector<int> order;
+        for (int q = 0; q < b->ntiles; ++q)
+            if (cost[q] > 0) order.push_back(q);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+        std::vector<int2> list(order.size());
+        for (size_t q = 0; q < order.size(); ++q) list[q] = make_int2(order[q] % b->tilesX, order[q] / b->tilesX);
+        b->ntl = (int)list.size();
+        if (b->ntl) CK(cudaMemcpy(b->tl.p, list.data(), sizeof(int2) * list.size(), cudaMemcpyHostToDevice));
+        // tiles left out of the list keep no stale mass-fixer sums
+        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
+    }
     // tensor maps of the shared fields and of the tracer buffers
     {
         const bool hq = b->storage >= 1, hk = b->storage >= 2;
@@ -386,29 +413,86 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     return ok(stat);
 }
 
-// one transport step of every tracer: groups of 4, 2, 1 tracers per launch
-cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s)
+// tracers of the next launch: groups of b->split (4 or 2), then 2, then 1
+inline int group_size(const Batch* b, int left)
+{
+    if (left >= 4 && b->split >= 4) return 4;
+    return left >= 2 ? 2 : 1;
+}
+
+int launches_per_step(const Batch* b)
+{
+    int n = 0;
+    for (int left = b->nt; left > 0; left -= group_size(b, left)) ++n;
+    return n + (fix_active(b) ? 1 : 0);
+}
+
+// one transport step of every tracer.  real == false (the autotuner): the step
+// writes the other buffer and the scratch only -- no mass-fixer update, no
+// parity flip -- so the tracer state is unchanged.
+cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, bool real = true)
 {
     const float* Pin = b->cur_in();
     float* Pout = b->cur_out();
+    const int2* tiles = (b->sched == 1 && b->ntl > 0) ? b->tl.p : nullptr;
     int t0 = 0;
     while (t0 < b->nt) {
-        const int left = b->nt - t0;
-        const int g = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
+        const int g = group_size(b, b->nt - t0);
         mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout);
         mohid::TmaMaps m = b->maps;
         m.P = b->mapP[b->cur ? 1 : 0][g == 4 ? 2 : (g == 2 ? 1 : 0)];
         cudaError_t e = mohid::launch_batched(a, m, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
-                                              b->storage >= 2, s);
+                                              b->storage >= 2, tiles, b->ntl, s);
         if (e != cudaSuccess) return e;
         t0 += g;
     }
+    if (!real) return cudaSuccess;
     if (fix_active(b)) {
         cudaError_t e = mohid::mass_fix_step(b->mpart.p, b->ntiles, b->nt, b->mfix.p, s);
         if (e != cudaSuccess) return e;
     }
     b->cur = !b->cur;
     return cudaSuccess;
+}
+
+// Autotuner: time every candidate launch schedule (one CTA per tile, or the
+// persistent tile list) and tracer grouping (4 or 2 per launch when there are
+// 4 or more tracers) on the batch itself -- a warm-up step and two timed steps
+// each, which leave the tracer state as it was -- and keep the fastest.
+int autotune(Batch* b, const mohid_ad_params* p, int* stat)
+{
+    cudaStream_t s = b->in->stream;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int bestSched = 0, bestSplit = 4;
+    float best = 1e30f;
+    cudaError_t err = cudaSuccess;
+    for (int split : {4, 2}) {
+        if (split == 2 && b->nt < 4) continue;
+        for (int sched : {0, 1}) {
+            if (sched == 1 && b->ntl == 0) continue;
+            b->sched = sched;
+            b->split = split;
+            err = enqueue_step(b, p, s, false);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+            for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err != cudaSuccess) break;
+            if (ms < best) { best = ms; bestSched = sched; bestSplit = split; }
+        }
+        if (err != cudaSuccess) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->sched = bestSched;
+    b->split = bestSplit;
+    if (err != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("autotune", err));
+    b->tuned = true;
+    return ok(stat);
 }
 
 // ---- ensembles --------------------------------------------------------------
@@ -528,6 +612,8 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->fixpart.alloc(2 * (size_t)kFixBlocks * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->moving.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Vprev.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->tl.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->tcost.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
@@ -654,6 +740,10 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     cudaStream_t s = in->stream;
+    if (!b->tuned) {
+        int c = autotune(b, p, stat);
+        if (c) return c;
+    }
     if (fix_active(b)) b->fixDirty = true;
     if (!*use_graph) {
         for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s));
@@ -665,6 +755,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     const int pairs = *nsteps / 2;
     if (pairs > 0) {
         const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
+                           b->graphSched == b->sched && b->graphSplit == b->split &&
                            std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
         if (!reuse) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -683,10 +774,55 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphSteps = 2 * pairs;
             b->graphCur = cur0;
             b->graphParams = *p;
+            b->graphSched = b->sched;
+            b->graphSplit = b->split;
         }
         CK(cudaGraphLaunch(b->graph, s));
     }
     if (*nsteps % 2) CK(enqueue_step(b, p, s));
+    return ok(stat);
+}
+
+int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!p) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (b->ensemble) return fail(MOHID_AD_ERR_OPTION, stat, "the batch is stepped by an ensemble");
+    std::string why;
+    int code = check_batched_params(p, b->hasRef, why);
+    if (code) return fail(code, stat, why);
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    if (!b->packed || b->packedVersion != in->hydroVersion) {
+        int c = pack_hydro(b, stat);
+        if (c) return c;
+    }
+    int c = ensure_shift_valid(b, p, stat);
+    if (c) return c;
+    return autotune(b, p, stat);
+}
+
+int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!sched || !split) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if ((*sched != 0 && *sched != 1) || (*split != 4 && *split != 2))
+        return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 4 or 2");
+    b->sched = *sched;
+    b->split = *split;
+    b->tuned = true;
+    return ok(stat);
+}
+
+int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (launches) *launches = launches_per_step(b);
+    if (sched) *sched = b->sched;
+    if (split) *split = b->split;
     return ok(stat);
 }
 

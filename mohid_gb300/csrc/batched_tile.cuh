@@ -173,14 +173,16 @@ __device__ __forceinline__ uint64_t l2_policy_evict_first()
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+// (volatile asm keeps these in program order among themselves; the scratch is
+// only ever read back by the thread that wrote it, after a data dependence)
 __device__ __forceinline__ void st_l2hint(float* a, float v, uint64_t pol)
 {
-    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol));
 }
 __device__ __forceinline__ float ld_l2hint(const float* a, uint64_t pol)
 {
     float v;
-    asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol) : "memory");
+    asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
     return v;
 }
 

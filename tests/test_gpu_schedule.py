@@ -1,0 +1,85 @@
+"""Launch schedules of the batched form and the autotuner.
+
+The schedules (one CTA per tile, or a persistent grid over the tiles holding
+water with the deepest first; 4 or 2 tracers per launch) run the same tile walk
+and must give the same result bit for bit; the autotuner must leave the tracers
+as they were and report what it chose.
+"""
+import numpy as np
+import pytest
+
+from mohid_gb300 import advdiff, batched, synth
+from oracle import oracle as O
+from tests.cases import domain
+
+pytestmark = pytest.mark.gpu
+
+ZLEVEL = dict(ni=70, nj=45, nk=12, land_frac=0.35, land_kind=2, seed=41, zlevel=True, hmin=2.0, hmax=80.0,
+              bathy_kind=2, dt=20.0)
+PD = dict(DTProp=20.0, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1)
+
+
+def _run(d, tr, sched, split, steps=6, graph=True):
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, len(tr))
+    for t, P in enumerate(tr):
+        b.set_tracer(t, P)
+    b.set_schedule(sched, split)
+    b.step(advdiff.params(**PD), nsteps=steps, graph=graph)
+    b.sync()
+    info = b.schedule()
+    got = [b.get_tracer(t) for t in range(len(tr))]
+    b.destroy()
+    ad.kill()
+    return got, info
+
+
+@pytest.mark.parametrize("nt", [1, 3, 5])
+def test_schedules_agree(gpu, nt):
+    d = synth.generate(synth.GenSpec(**ZLEVEL))
+    tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(nt)]
+    ref, info = _run(d, tr, 0, 4)
+    assert info == {"launches": (2 if nt == 5 else (1 if nt == 1 else 2)) + 1, "sched": 0, "split": 4}
+    for sched, split in [(1, 4), (0, 2), (1, 2)]:
+        got, info = _run(d, tr, sched, split)
+        assert info["sched"] == sched and info["split"] == split
+        for a, b in zip(ref, got):
+            assert np.array_equal(a, b)
+
+
+def test_tile_list_matches_oracle(gpu):
+    d = synth.generate(synth.GenSpec(**ZLEVEL))
+    tr = [d.tracer(3, 2.0, 0.5, seed=3), d.tracer(1, 5.0, 20.0, seed=4)]
+    got, _ = _run(d, tr, 1, 4, steps=10)
+    wp = d.water_mask()
+    work = O.Work(d)
+    for P, g in zip(tr, got):
+        Q = P.copy()
+        for _ in range(10):
+            assert O.step(d, Q, O.params(**PD), work=work) == 0
+        assert np.linalg.norm(g[wp] - Q[wp]) / np.linalg.norm(Q[wp]) <= 1e-5
+        assert np.array_equal(g[~wp], Q[~wp])
+
+
+def test_autotune_keeps_state(gpu):
+    d = domain("zlevel")
+    tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(4)]
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, 4)
+    for t, P in enumerate(tr):
+        b.set_tracer(t, P)
+    before = [b.get_tracer(t) for t in range(4)]
+    m0 = [b.mass(t) for t in range(4)]
+    b.autotune(advdiff.params(**PD))
+    info = b.schedule()
+    assert info["sched"] in (0, 1) and info["split"] in (2, 4)
+    after = [b.get_tracer(t) for t in range(4)]
+    for x, y in zip(before, after):
+        assert np.array_equal(x, y)
+    assert [b.mass(t) for t in range(4)] == m0
+    with pytest.raises(advdiff.N.MohidAdError):
+        b.set_schedule(2, 4)
+    b.destroy()
+    ad.kill()
