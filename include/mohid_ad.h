@@ -279,13 +279,14 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
  * the batch on the batch itself and keeps the fastest.  The schedules are one
  * CTA per 32 x 8 tile, or a persistent grid over the tiles that hold water with
  * the deepest first (the column-length-aware schedule for z-level domains);
- * with 4 or more tracers, 4 or 2 tracers per launch.  Each candidate runs a
- * warm-up and two timed steps that leave the tracers unchanged.  The first
- * mohid_ad_batched_step of a batch runs it; call it again after a change that
+ * with 4 or more tracers, 4 or 2 tracers per launch (with 8 or more also 8).
+ * Each candidate runs a warm-up and two timed steps that leave the tracers
+ * unchanged.  The first mohid_ad_batched_step of a batch runs it; call it
+ * again after a change that
  * may favour another schedule. */
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat);
 
-/* Set the schedule by hand (*sched 0 or 1, *split 4 or 2) instead of the autotuner. */
+/* Set the schedule by hand (*sched 0 or 1, *split 8, 4 or 2) instead of the autotuner. */
 int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat);
 
 /* The schedule in use: kernel launches per step (including the mass fixer's),

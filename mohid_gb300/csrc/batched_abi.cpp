@@ -60,7 +60,7 @@ struct Batch {
     DevBuf<int> tcost;
     int ntl = 0;
     int sched = 0;                       // 0 grid, 1 tile list
-    int split = 4;                       // largest tracer group per launch: 4 or 2
+    int split = 4;                       // largest tracer group per launch: 8, 4 or 2
     bool tuned = false;
     int graphSched = -1, graphSplit = -1;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
@@ -79,7 +79,7 @@ struct Batch {
     DevBuf<double> partial, scratch, stage;
     double* hmass = nullptr;             // pinned
     mohid::TmaMaps maps{};               // shared-field maps (valid after a pack)
-    CUtensorMap mapP[2][3];              // tracer maps: input buffer (A/B) x group size (1, 2, 4)
+    CUtensorMap mapP[2][4];              // tracer maps: input buffer (A/B) x group size (1, 2, 4, 8)
     bool mapsOk = false;
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
@@ -310,9 +310,9 @@ int pack_hydro(Batch* b, int* stat)
         okm &= encode_map(&M.Fn, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[12]);
         okm &= encode_map(&M.Vh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vhi.p, L, 1, box[13]);
         okm &= encode_map(&M.Vl, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vlo.p, L, 1, box[14]);
-        const int gs[3] = {1, 2, 4};
+        const int gs[4] = {1, 2, 4, 8};
         for (int buf = 0; buf < 2; ++buf)
-            for (int g = 0; g < 3; ++g) {
+            for (int g = 0; g < 4; ++g) {
                 if (gs[g] > b->nt) continue;
                 int bb[mohid::kNumMaps][4];
                 mohid::batched_boxes(hq, hk, gs[g], bb);
@@ -413,12 +413,15 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     return ok(stat);
 }
 
-// tracers of the next launch: groups of b->split (4 or 2), then 2, then 1
+// tracers of the next launch: groups of b->split (8, 4 or 2), then 4, 2, 1
 inline int group_size(const Batch* b, int left)
 {
+    if (left >= 8 && b->split >= 8) return 8;
     if (left >= 4 && b->split >= 4) return 4;
     return left >= 2 ? 2 : 1;
 }
+
+inline int map_index(int g) { return g == 8 ? 3 : (g == 4 ? 2 : (g == 2 ? 1 : 0)); }
 
 int launches_per_step(const Batch* b)
 {
@@ -440,7 +443,7 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
         const int g = group_size(b, b->nt - t0);
         mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout);
         mohid::TmaMaps m = b->maps;
-        m.P = b->mapP[b->cur ? 1 : 0][g == 4 ? 2 : (g == 2 ? 1 : 0)];
+        m.P = b->mapP[b->cur ? 1 : 0][map_index(g)];
         cudaError_t e = mohid::launch_batched(a, m, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
                                               b->storage >= 2, tiles, b->ntl, s);
         if (e != cudaSuccess) return e;
@@ -468,8 +471,8 @@ int autotune(Batch* b, const mohid_ad_params* p, int* stat)
     int bestSched = 0, bestSplit = 4;
     float best = 1e30f;
     cudaError_t err = cudaSuccess;
-    for (int split : {4, 2}) {
-        if (split == 2 && b->nt < 4) continue;
+    for (int split : {8, 4, 2}) {
+        if ((split == 8 && b->nt < 8) || (split == 2 && b->nt < 4)) continue;
         for (int sched : {0, 1}) {
             if (sched == 1 && b->ntl == 0) continue;
             b->sched = sched;
@@ -808,8 +811,8 @@ int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* s
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!sched || !split) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
-    if ((*sched != 0 && *sched != 1) || (*split != 4 && *split != 2))
-        return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 4 or 2");
+    if ((*sched != 0 && *sched != 1) || (*split != 8 && *split != 4 && *split != 2))
+        return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 8, 4 or 2");
     b->sched = *sched;
     b->split = *split;
     b->tuned = true;

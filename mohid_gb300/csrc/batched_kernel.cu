@@ -10,7 +10,7 @@ using namespace tile;
 namespace {
 
 template <int NT, int METHOD, int LIM, typename QT, typename KT>
-__global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
+__global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : (NT <= 4 ? 3 : 2))
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M, const int2* __restrict__ tiles, int ntl)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -109,6 +109,7 @@ size_t smem_n(bool halfQ, bool halfK, int nk)
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
                            bool halfK, const int2* tiles, int ntl, cudaStream_t s)
 {
+    if (a.nt == 8) return launch_n<8>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
     if (a.nt == 4) return launch_n<4>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
     if (a.nt == 2) return launch_n<2>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
     if (a.nt == 1) return launch_n<1>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
@@ -124,6 +125,7 @@ cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L
 
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk)
 {
+    if (nt == 8) return smem_n<8>(halfQ, halfK, nk);
     if (nt == 4) return smem_n<4>(halfQ, halfK, nk);
     if (nt == 2) return smem_n<2>(halfQ, halfK, nk);
     return smem_n<1>(halfQ, halfK, nk);

@@ -562,7 +562,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     //      fixer on, the column's sum of VolumeZ * value is accumulated as an
     //      FP32 pair per tracer from VolumeZ = hi + lo (about 2^-44 relative).
     const bool mf = A.mpart != nullptr;
-    constexpr int RB = 4;                          // rows per batch of loads
+    constexpr int RB = NT >= 8 ? 2 : 4;            // rows per batch of loads (registers)
     float mh[NT], ml[NT];
 #pragma unroll
     for (int t = 0; t < NT; ++t) { mh[t] = 0.f; ml[t] = 0.f; }

@@ -35,13 +35,15 @@ def _run(d, tr, sched, split, steps=6, graph=True):
     return got, info
 
 
-@pytest.mark.parametrize("nt", [1, 3, 5])
+@pytest.mark.parametrize("nt", [1, 3, 5, 9])
 def test_schedules_agree(gpu, nt):
     d = synth.generate(synth.GenSpec(**ZLEVEL))
     tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(nt)]
     ref, info = _run(d, tr, 0, 4)
-    assert info == {"launches": (2 if nt == 5 else (1 if nt == 1 else 2)) + 1, "sched": 0, "split": 4}
-    for sched, split in [(1, 4), (0, 2), (1, 2)]:
+    groups4 = {1: 1, 3: 2, 5: 2, 9: 3}[nt]                 # 4-tracer groups, then 2, then 1
+    assert info == {"launches": groups4 + 1, "sched": 0, "split": 4}
+    cands = [(1, 4), (0, 2), (1, 2)] + ([(0, 8), (1, 8)] if nt >= 8 else [])
+    for sched, split in cands:
         got, info = _run(d, tr, sched, split)
         assert info["sched"] == sched and info["split"] == split
         for a, b in zip(ref, got):
