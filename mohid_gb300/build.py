@@ -26,6 +26,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
     ("batched_kernel.cu", []),
+    ("batched_kernel_obc.cu", []),
     ("ensemble_kernel.cu", []),
     ("batched_pack.cu", []),
     ("mass_noalloc.cu", []),

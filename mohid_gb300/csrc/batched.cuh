@@ -119,8 +119,9 @@ cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
 // ensemble: one persistent grid over the (domain, bx, by, -) tiles of many
 // domains with FP32 storage; As/Ms are device tables indexed by domain
+// open: some member has reference concentrations (open-boundary instantiation)
 cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
-                            int nt, int method, int limiter, cudaStream_t s);
+                            int nt, int method, int limiter, bool open, cudaStream_t s);
 // resident CTAs of the ensemble kernel on `device` (0 on error)
 int ensemble_slots(int nt, int method, int limiter, int device);
 // box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order

@@ -541,8 +541,9 @@ cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
 {
     const size_t n = E->m.size();
     const size_t off = E->cur ? n : 0;
+    const bool open = std::any_of(E->m.begin(), E->m.end(), [](const Batch* b) { return b->hasRef; });
     cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
-                                           method, limiter, E->s);
+                                           method, limiter, open, E->s);
     if (e == cudaSuccess && std::any_of(E->m.begin(), E->m.end(), fix_active))
         e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->nt, E->s);
     E->cur = !E->cur;

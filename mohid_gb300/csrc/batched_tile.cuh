@@ -342,7 +342,7 @@ __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
 // next in the same CTA.  Returns false when a stage never arrived (the status
 // word then holds MOHID_DEV_TIMEOUT).  The caller must have every warp of the
 // CTA past its previous walk before calling (a barrier between walks).
-template <int NT, int METHOD, int LIM, typename QT, typename KT>
+template <int NT, int METHOD, int LIM, typename QT, typename KT, bool OBC>
 __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, int bx, int by,
                                           unsigned char* smem_raw, uint32_t& phase)
 {
@@ -420,7 +420,9 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     // k-invariant conditions of the column's vertical terms
     const bool vdif = L.nk > 1 && !(cf & C_SD);
     const bool vadv = L.nk > 1 && !A.vertical1D && (cf & C_CFWTOP) && (cf & C_OPTOP);
-    const bool obcCol = (cf & C_BP) && A.Ref != nullptr;
+    // open boundaries are compiled in only where the batch has reference
+    // concentrations: the closed form carries none of their instructions
+    const bool obcCol = OBC && (cf & C_BP) && A.Ref != nullptr;
     // own-column values of the face below row k slide up the walk: transport,
     // conductance Kz * area / DZZ (AD:2736-2765), cell flags of rows k-1 and k
     float qz = 0.f, kzb = 0.f;

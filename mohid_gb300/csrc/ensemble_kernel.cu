@@ -14,7 +14,7 @@ namespace mohid {
 using namespace tile;
 namespace {
 
-template <int NT, int METHOD, int LIM>
+template <int NT, int METHOD, int LIM, bool OBC>
 __global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
 ensemble_kernel(const BatchArgs* __restrict__ As, const TmaMaps* __restrict__ Ms,
                 const int4* __restrict__ tiles, int ntiles)
@@ -36,16 +36,16 @@ ensemble_kernel(const BatchArgs* __restrict__ As, const TmaMaps* __restrict__ Ms
             __syncthreads();
             cur = t.x;
         }
-        if (!tile_walk<NT, METHOD, LIM, float, float>(sA, Ms[t.x], t.y, t.z, smem_raw, phase)) return;
+        if (!tile_walk<NT, METHOD, LIM, float, float, OBC>(sA, Ms[t.x], t.y, t.z, smem_raw, phase)) return;
     }
 }
 
-template <int NT, int METHOD, int LIM>
+template <int NT, int METHOD, int LIM, bool OBC>
 cudaError_t ens_launch_t(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
                          cudaStream_t s)
 {
     const size_t smem = Smem<NT, float, float>::bytes(0);
-    auto kern = ensemble_kernel<NT, METHOD, LIM>;
+    auto kern = ensemble_kernel<NT, METHOD, LIM, OBC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, dim3(TX, TY), smem, s>>>(As, Ms, tiles, ntiles);
@@ -56,7 +56,7 @@ template <int NT, int METHOD, int LIM>
 int ens_slots_t(int device)
 {
     const size_t smem = Smem<NT, float, float>::bytes(0);
-    auto kern = ensemble_kernel<NT, METHOD, LIM>;
+    auto kern = ensemble_kernel<NT, METHOD, LIM, true>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
     int per = 0, sms = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, NTH, smem) != cudaSuccess) return 0;
@@ -64,18 +64,26 @@ int ens_slots_t(int device)
     return per * sms;
 }
 
-template <int NT>
-cudaError_t ens_launch_n(int method, int limiter, const BatchArgs* As, const TmaMaps* Ms, const int4* tiles,
+template <int NT, bool OBC>
+cudaError_t ens_launch_o(int method, int limiter, const BatchArgs* As, const TmaMaps* Ms, const int4* tiles,
                          int ntiles, int grid, cudaStream_t s)
 {
-    if (method == 1) return ens_launch_t<NT, 1, 0>(As, Ms, tiles, ntiles, grid, s);
+    if (method == 1) return ens_launch_t<NT, 1, 0, OBC>(As, Ms, tiles, ntiles, grid, s);
     switch (limiter) {
-    case 1: return ens_launch_t<NT, 4, 1>(As, Ms, tiles, ntiles, grid, s);
-    case 2: return ens_launch_t<NT, 4, 2>(As, Ms, tiles, ntiles, grid, s);
-    case 3: return ens_launch_t<NT, 4, 3>(As, Ms, tiles, ntiles, grid, s);
-    case 4: return ens_launch_t<NT, 4, 4>(As, Ms, tiles, ntiles, grid, s);
-    default: return ens_launch_t<NT, 4, 5>(As, Ms, tiles, ntiles, grid, s);
+    case 1: return ens_launch_t<NT, 4, 1, OBC>(As, Ms, tiles, ntiles, grid, s);
+    case 2: return ens_launch_t<NT, 4, 2, OBC>(As, Ms, tiles, ntiles, grid, s);
+    case 3: return ens_launch_t<NT, 4, 3, OBC>(As, Ms, tiles, ntiles, grid, s);
+    case 4: return ens_launch_t<NT, 4, 4, OBC>(As, Ms, tiles, ntiles, grid, s);
+    default: return ens_launch_t<NT, 4, 5, OBC>(As, Ms, tiles, ntiles, grid, s);
     }
+}
+
+template <int NT>
+cudaError_t ens_launch_n(int method, int limiter, bool open, const BatchArgs* As, const TmaMaps* Ms,
+                         const int4* tiles, int ntiles, int grid, cudaStream_t s)
+{
+    if (open) return ens_launch_o<NT, true>(method, limiter, As, Ms, tiles, ntiles, grid, s);
+    return ens_launch_o<NT, false>(method, limiter, As, Ms, tiles, ntiles, grid, s);
 }
 
 template <int NT>
@@ -94,11 +102,11 @@ int ens_slots_n(int method, int limiter, int device)
 }  // namespace
 
 cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
-                            int nt, int method, int limiter, cudaStream_t s)
+                            int nt, int method, int limiter, bool open, cudaStream_t s)
 {
-    if (nt == 4) return ens_launch_n<4>(method, limiter, As, Ms, tiles, ntiles, grid, s);
-    if (nt == 2) return ens_launch_n<2>(method, limiter, As, Ms, tiles, ntiles, grid, s);
-    if (nt == 1) return ens_launch_n<1>(method, limiter, As, Ms, tiles, ntiles, grid, s);
+    if (nt == 4) return ens_launch_n<4>(method, limiter, open, As, Ms, tiles, ntiles, grid, s);
+    if (nt == 2) return ens_launch_n<2>(method, limiter, open, As, Ms, tiles, ntiles, grid, s);
+    if (nt == 1) return ens_launch_n<1>(method, limiter, open, As, Ms, tiles, ntiles, grid, s);
     return cudaErrorInvalidValue;
 }
 
