@@ -106,7 +106,6 @@ struct TmaMaps {
     CUtensorMap QY, AV;                 // south faces: box (36 | 40, TY, 1), (36, TY, 1)
     CUtensorMap Vo;                     // (V - Vold)/V, f32, own cells: box (32, TY, 1)
     CUtensorMap Qz, Dv, Dz, Fn;         // own cells of the layer above / 1/DZZ: box (32, TY, 1)
-    CUtensorMap Vh, Vl;                 // VolumeZ as an FP32 pair, own cells (L2 prefetch only): box (32, TY, 1)
 };
 
 // tiles == null: one CTA per tile of the grid; otherwise a persistent grid over
@@ -125,7 +124,7 @@ cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* 
 // resident CTAs of the ensemble kernel on `device` (0 on error)
 int ensemble_slots(int nt, int method, int limiter, int device);
 // box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order
-constexpr int kNumMaps = 15;
+constexpr int kNumMaps = 13;
 void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4]);
 
 // packing (Fortran FP64 Size box <-> batched layout)

@@ -308,8 +308,6 @@ int pack_hydro(Batch* b, int* stat)
         okm &= encode_map(&M.Dv, tk, ek, dif, L, 1, box[10]);
         okm &= encode_map(&M.Dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DZZ.p, L, 1, box[11]);
         okm &= encode_map(&M.Fn, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[12]);
-        okm &= encode_map(&M.Vh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vhi.p, L, 1, box[13]);
-        okm &= encode_map(&M.Vl, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->Vlo.p, L, 1, box[14]);
         const int gs[4] = {1, 2, 4, 8};
         for (int buf = 0; buf < 2; ++buf)
             for (int g = 0; g < 4; ++g) {

@@ -73,7 +73,7 @@ void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4])
                                 {visX, TY + 2, 1, 1}, {TX, TY + 1, 1, 1},   {TX, TY + 1, 1, 1},
                                 {qyX, TY, 1, 1},      {AVX, TY, 1, 1},      {OWN, TY, 1, 1},
                                 {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1},
-                                {OWN, TY, 1, 1},      {OWN, TY, 1, 1},      {OWN, TY, 1, 1}};
+                                {OWN, TY, 1, 1}};
     for (int q = 0; q < kNumMaps; ++q)
         for (int d = 0; d < 4; ++d) box[q][d] = b[q][d];
 }

@@ -186,13 +186,6 @@ __device__ __forceinline__ float ld_l2hint(const float* a, uint64_t pol)
     return v;
 }
 
-// bulk-tensor prefetch of one tile into L2 (no shared memory, no completion)
-__device__ __forceinline__ void tma3_prefetch_l2(const CUtensorMap* map, int x, int y, int z)
-{
-    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];"
-                 ::"l"(map), "r"(x), "r"(y), "r"(z)
-                 : "memory");
-}
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // psi(r) * d for r = n / d, psi one of the ComputeAdvectionFace limiters
