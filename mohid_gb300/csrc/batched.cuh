@@ -131,12 +131,14 @@ void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4]);
 // All hydrodynamic fields of one update in one pass: transports and
 // diffusivities to FP32 or (halfQ / halfK) to FP16 times inv[0..2] / inv[3..4],
 // areas to FP32, 1/DZZ, 1/VolumeZ and (VolumeZ - VolumeZOld)/VolumeZ formed in
-// FP64, the cell flag byte (F_*) and the face flag byte (FU_*, FV_*).
+// FP64, the cell flag byte (F_*) and the face flag byte (FU_*, FV_*).  dinv
+// (device, 5 floats: 1/scale of Qx, Qy, Qz, Visc_H, Diff_V) is read for the
+// FP16 fields; may be null for FP32 storage.
 cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, const double* V, const double* Vold,
                         const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
                         const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
                         void* oQx, void* oQy, void* oQz, void* oVis, void* oDif, bool halfQ, bool halfK,
-                        const float inv[5], float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
+                        const float* dinv, float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
                         float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
                         const BLayout& L, cudaStream_t s);
 
@@ -151,12 +153,12 @@ cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, doubl
 // tracer t loaded: target = FP64 mass of the Fortran-layout field P, constant = shift, correction = 0
 cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const BLayout& L, double* partial,
                           int nblocks, double shift, int t, int nt, double* mfix, cudaStream_t s);
-// new hydrodynamics: with `rebase`, target[t] += sum over water cells of
-// (Vnew - Vprev) * value (partial: 2 * nblocks * nt doubles); then Vprev = Vnew
-// (both FP64, Fortran Size-box layout)
-cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, double* Vprev, bool rebase,
-                            const int* WP, double* mfix, const BLayout& L, double* partial, int nblocks,
-                            cudaStream_t s);
+// new hydrodynamics: *changed = 1 where VolumeZ differs bit for bit from the
+// last pack's (Vprev, Fortran layout), and Vprev = Vnew
+cudaError_t vol_changed(const double* Vnew, double* Vprev, long long n, unsigned* changed, cudaStream_t s);
+// FP16 storage scales of nf FP64 fields on the device (absmax: nf doubles of scratch)
+cudaError_t fp16_scales(const double* const* fields, int nf, long long n, double* absmax, float* scale, float* inv,
+                        cudaStream_t s);
 // after a step: correction[t] += (target[t] - mass now) / volume for every tracer of the batch
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s);
 // the same for `nb` batches whose argument records (device) have mpart != null

@@ -46,7 +46,7 @@ struct Batch {
     // mass fixer (closed domains, static volumes): VolumeZ as an FP32 pair,
     // the fixer state (volume, targets, constants, corrections), per-tile sums
     DevBuf<float> Vhi, Vlo;
-    DevBuf<double> mfix, mpart, fixpart;
+    DevBuf<double> mfix, mpart;
     DevBuf<double> Vprev;                // VolumeZ of the last pack (Fortran layout)
     DevBuf<unsigned> moving;
     bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
@@ -63,6 +63,28 @@ struct Batch {
     int split = 4;                       // largest tracer group per launch: 8, 4 or 2
     bool tuned = false;
     int graphSched = -1, graphSplit = -1;
+    // asynchronous repack of a new hydrodynamic state (on the instance's
+    // stream) and tracer loads (on their own stream, with their own scratch),
+    // so that the two overlap; the host-side results of the repack are read
+    // when a step needs them (pack_finalize)
+    cudaStream_t cs = nullptr;           // tracer loads
+    cudaEvent_t packEv = nullptr;
+    bool packPending = false;
+    unsigned packingVersion = ~0u;
+    struct PackHost {
+        unsigned moving, vchanged;
+        float scale[5];
+        double cont;                     // continuity excess for contDT, or -1 when not computed
+        double contDT;
+    };
+    PackHost* hp = nullptr;              // pinned
+    int* hcost = nullptr;                // pinned, per tile
+    DevBuf<float> dscale, dinv;
+    DevBuf<unsigned> vchanged;
+    DevBuf<double> tpartial, tscratch;   // scratch of the tracer loads
+    std::vector<unsigned> targetVersion; // hydro version each tracer's mass target was taken at
+    double preCont = -1.0, preContDT = -1.0;
+    unsigned preContVersion = ~0u;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
     // anomaly storage is exact only when the step preserves constants; this
@@ -96,8 +118,17 @@ struct Batch {
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
-        mfix.release(); mpart.release(); fixpart.release(); moving.release(); Vprev.release();
+        mfix.release(); mpart.release(); moving.release(); Vprev.release();
         tl.release(); tcost.release();
+        dscale.release(); dinv.release(); vchanged.release(); tpartial.release(); tscratch.release();
+        if (hp) cudaFreeHost(hp);
+        if (hcost) cudaFreeHost(hcost);
+        hp = nullptr;
+        hcost = nullptr;
+        if (cs) cudaStreamDestroy(cs);
+        if (packEv) cudaEventDestroy(packEv);
+        cs = nullptr;
+        packEv = nullptr;
         if (hmass) cudaFreeHost(hmass);
         hmass = nullptr;
         if (graph) cudaGraphExecDestroy(graph);
@@ -176,7 +207,8 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     return MOHID_AD_SUCCESS;
 }
 
-constexpr int kFixBlocks = 256;
+// relative continuity residual below which the step maps constants onto themselves
+constexpr double kContinuityTol = 1e-9;
 
 // the mass fixer runs on closed domains whose step maps constants onto
 // themselves (anomaly storage valid) and whose volumes do not move
@@ -216,74 +248,53 @@ cudaError_t fix_invalidate(Batch* b, cudaStream_t s)
     return cudaStreamSynchronize(s);
 }
 
-int pack_hydro(Batch* b, int* stat)
+// Enqueue the repack of the instance's current hydrodynamics on the instance's
+// stream, without waiting for it: FP16 scales (device side), the fused field
+// pack, the water volume of the mass fixer, the per-column data, the tile
+// costs of the schedule, the volume-change flag and (for the last DT a step
+// used) the continuity check.  pack_finalize collects the results.
+int pack_enqueue(Batch* b, int* stat)
 {
     Instance* in = b->in;
     if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "the plain instance has no hydrodynamics set");
     cudaStream_t s = in->stream;
     const mohid::BLayout& L = b->L;
-    auto scale = [&](const double* src, float* sc) -> cudaError_t {
-        cudaError_t e = mohid::absmax_f64(src, (long long)in->n3, b->scratch.p, s);
-        if (e != cudaSuccess) return e;
-        double m = 0;
-        e = cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) return e;
-        e = cudaStreamSynchronize(s);
-        m = *b->hmass;
-        // map the largest magnitude to 2^14 so that FP16 keeps 11 significant bits
-        *sc = m > 0 ? (float)(m / 16384.0) : 1.0f;
-        return e;
-    };
     const bool hq = b->storage >= 1, hk = b->storage >= 2;
-    if (hq) { CK(scale(in->Qx.p, &b->qsx)); CK(scale(in->Qy.p, &b->qsy)); CK(scale(in->Qz.p, &b->qsz)); }
-    if (hk) { CK(scale(in->ViscH.p, &b->ksh)); CK(scale(in->DiffV.p, &b->ksv)); }
-    const float inv[5] = {1.0f / b->qsx, 1.0f / b->qsy, 1.0f / b->qsz, 1.0f / b->ksh, 1.0f / b->ksv};
-    // static volumes before and after: the tracers' target masses follow the
-    // volume change (previous VolumeZ is still in Vhi + Vlo)
-    CK(mohid::mass_fix_rebase(b->cur_in(), L.n3, b->nt, in->V.p, b->Vprev.p,
-                              b->packedOnce && b->staticVol && b->massFix && !b->hasRef, in->WP.p, b->mfix.p, L,
-                              b->fixpart.p, kFixBlocks, s));
+    if (hq || hk) {
+        const double* f[5] = {in->Qx.p, in->Qy.p, in->Qz.p, in->ViscH.p, in->DiffV.p};
+        CK(mohid::fp16_scales(f, 5, (long long)in->n3, b->scratch.p, b->dscale.p, b->dinv.p, s));
+        CK(cudaMemcpyAsync(b->hp->scale, b->dscale.p, 5 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    }
+    CK(mohid::vol_changed(in->V.p, b->Vprev.p, (long long)in->n3, b->vchanged.p, s));
     CK(mohid::pack_fields(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
                           in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
                           in->CFV.p, in->CFW.p,
                           hq ? (void*)b->Qx16.p : (void*)b->Qx32.p, hq ? (void*)b->Qy16.p : (void*)b->Qy32.p,
                           hq ? (void*)b->Qz16.p : (void*)b->Qz32.p, hk ? (void*)b->Vis16.p : (void*)b->Vis32.p,
-                          hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, inv, b->AreaU.p, b->AreaV.p,
-                          b->DZZ.p, b->RV.p, b->DVR.p, b->Vhi.p, b->Vlo.p, b->flag.p, b->fflag.p, b->moving.p,
-                          L, s));
+                          hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, (hq || hk) ? b->dinv.p : nullptr,
+                          b->AreaU.p, b->AreaV.p, b->DZZ.p, b->RV.p, b->DVR.p, b->Vhi.p, b->Vlo.p, b->flag.p,
+                          b->fflag.p, b->moving.p, L, s));
     CK(mohid::water_volume(in->V.p, in->WP.p, L, b->partial.p, kMassBlocks, b->mfix.p, s));
     CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
                            b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
-    CK(cudaStreamSynchronize(s));
-    {
-        unsigned mv = 0;
-        CK(cudaMemcpy(&mv, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
-        const bool wasStatic = b->staticVol || !b->packedOnce;
-        b->staticVol = mv == 0;
-        if (!b->staticVol && wasStatic) CK(fix_invalidate(b, s));
-        b->packedOnce = true;
+    CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
+    // tiles left out of a schedule keep no stale mass-fixer sums
+    CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
+    CK(cudaMemcpyAsync(b->hcost, b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&b->hp->moving, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&b->hp->vchanged, b->vchanged.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    b->hp->cont = -1.0;
+    b->hp->contDT = b->checkedDT;
+    if (b->checkedDT > 0.0 && b->checkedFlags == 0) {   // continuity for the DT of the last step
+        CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p, in->CFU.p,
+                                      in->CFV.p, in->CFW.p, in->BP2D.p, b->checkedDT, kContinuityTol, L,
+                                      b->scratch.p + 5, s));
+        CK(cudaMemcpyAsync(&b->hp->cont, b->scratch.p + 5, sizeof(double), cudaMemcpyDeviceToHost, s));
     }
-    // tile schedule: tiles holding water, most layers first (stable by tile index)
+    CK(cudaEventRecord(b->packEv, s));
+    // tensor maps of the shared fields and of the tracer buffers (host only)
     {
-        CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
-        std::vector<int> cost(b->ntiles);
-        CK(cudaMemcpyAsync(cost.data(), b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        std::vector<int> order;
-        for (int q = 0; q < b->ntiles; ++q)
-            if (cost[q] > 0) order.push_back(q);
-        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
-        std::vector<int2> list(order.size());
-        for (size_t q = 0; q < order.size(); ++q) list[q] = make_int2(order[q] % b->tilesX, order[q] / b->tilesX);
-        b->ntl = (int)list.size();
-        if (b->ntl) CK(cudaMemcpy(b->tl.p, list.data(), sizeof(int2) * list.size(), cudaMemcpyHostToDevice));
-        // tiles left out of the list keep no stale mass-fixer sums
-        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
-    }
-    // tensor maps of the shared fields and of the tracer buffers
-    {
-        const bool hq = b->storage >= 1, hk = b->storage >= 2;
         int box[mohid::kNumMaps][4];
         mohid::batched_boxes(hq, hk, 1, box);
         const CUtensorMapDataType tq = hq ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -320,9 +331,65 @@ int pack_hydro(Batch* b, int* stat)
         if (!okm) return fail(MOHID_AD_ERR_CUDA, stat, "cuTensorMapEncodeTiled failed");
         b->mapsOk = true;
     }
-    b->packed = true;
-    b->packedVersion = in->hydroVersion;
+    b->packPending = true;
+    b->packingVersion = in->hydroVersion;
     return ok(stat);
+}
+
+// Wait for an enqueued repack and take its host-side results: FP16 scales,
+// static or moving volumes, the mass fixer's validity, the tile schedule and
+// the precomputed continuity check.
+int pack_finalize(Batch* b, int* stat)
+{
+    if (!b->packPending) return ok(stat);
+    cudaStream_t s = b->in->stream;
+    CK(cudaEventSynchronize(b->packEv));
+    b->packPending = false;
+    const Batch::PackHost& h = *b->hp;
+    if (b->storage >= 1) { b->qsx = h.scale[0]; b->qsy = h.scale[1]; b->qsz = h.scale[2]; }
+    if (b->storage >= 2) { b->ksh = h.scale[3]; b->ksv = h.scale[4]; }
+    b->staticVol = h.moving == 0;
+    // the fixer keeps the masses of tracers loaded under this state; a volume
+    // change (or moving volumes) ends it for tracers loaded before
+    if (h.moving || (h.vchanged && b->packedOnce))
+        for (int t = 0; t < b->nt; ++t)
+            if (b->targetVersion[t] != b->packingVersion) {
+                const double nan = std::nan("");
+                CK(cudaMemcpyAsync(b->mfix.p + 1 + t, &nan, sizeof(double), cudaMemcpyHostToDevice, s));
+                CK(cudaStreamSynchronize(s));
+            }
+    b->packedOnce = true;
+    // tile schedule: tiles holding water, most layers first (stable by tile index)
+    std::vector<int> order;
+    for (int q = 0; q < b->ntiles; ++q)
+        if (b->hcost[q] > 0) order.push_back(q);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->hcost[x] > b->hcost[y]; });
+    std::vector<int2> list(order.size());
+    for (size_t q = 0; q < order.size(); ++q) list[q] = make_int2(order[q] % b->tilesX, order[q] / b->tilesX);
+    b->ntl = (int)list.size();
+    if (b->ntl) CK(cudaMemcpy(b->tl.p, list.data(), sizeof(int2) * list.size(), cudaMemcpyHostToDevice));
+    b->preCont = h.cont;
+    b->preContDT = h.contDT;
+    b->preContVersion = b->packingVersion;
+    b->packed = true;
+    b->packedVersion = b->packingVersion;
+    return ok(stat);
+}
+
+// the batched layout holds the instance's current hydrodynamics
+int ensure_packed(Batch* b, int* stat)
+{
+    Instance* in = b->in;
+    if (b->packed && b->packedVersion == in->hydroVersion && !b->packPending) return ok(stat);
+    if (!b->packPending || b->packingVersion != in->hydroVersion) {
+        if (b->packPending) {                    // an older state still in flight
+            int c = pack_finalize(b, stat);
+            if (c) return c;
+        }
+        int c = pack_enqueue(b, stat);
+        if (c) return c;
+    }
+    return pack_finalize(b, stat);
 }
 
 mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout)
@@ -370,8 +437,6 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     return a;
 }
 
-constexpr double kContinuityTol = 1e-9;
-
 // Decide whether tracers may stay stored as anomalies for this step; convert
 // them (and their references) back to absolute values if not.
 int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
@@ -381,7 +446,9 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0);
     if (b->checkedVersion != in->hydroVersion || b->checkedDT != p->DTProp || b->checkedFlags != flags) {
         bool okc = flags == 0;
-        if (okc) {
+        if (okc && b->preContVersion == in->hydroVersion && b->preContDT == p->DTProp && b->preCont >= 0.0) {
+            okc = b->preCont <= 0.0;             // computed with the repack
+        } else if (okc) {
             CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p,
                                           in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp, kContinuityTol,
                                           b->L, b->scratch.p, s));
@@ -611,13 +678,24 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->Vlo.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->mfix.alloc(1 + 3 * (size_t)b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->fixpart.alloc(2 * (size_t)kFixBlocks * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaMallocHost((void**)&b->hcost, sizeof(int) * (size_t)b->ntiles)) != cudaSuccess)
+        return bad(e, "cudaMallocHost");
     if ((e = b->moving.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Vprev.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->tl.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->tcost.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->scratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->scratch.alloc(8)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->tscratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->tpartial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->dscale.alloc(5)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->dinv.alloc(5)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->vchanged.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaStreamCreateWithFlags(&b->cs, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "cudaStreamCreate");
+    if ((e = cudaEventCreateWithFlags(&b->packEv, cudaEventDisableTiming)) != cudaSuccess)
+        return bad(e, "cudaEventCreate");
+    if ((e = cudaMallocHost((void**)&b->hp, sizeof(Batch::PackHost))) != cudaSuccess) return bad(e, "cudaMallocHost");
+    b->targetVersion.assign(b->nt, ~0u);
     if ((e = b->stage.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     b->shift.assign(b->nt, 0.0);
     if ((e = cudaMallocHost((void**)&b->hmass, 4 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMallocHost");
@@ -634,7 +712,7 @@ int mohid_ad_batched_pack_hydro(const int* bid, int* stat)
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     CK(cudaSetDevice(b->in->device));
-    return pack_hydro(b, stat);
+    return ensure_packed(b, stat);
 }
 
 int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP, const int* on_device, int* stat)
@@ -644,26 +722,46 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
     if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
     if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
     Instance* in = b->in;
+    if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "the plain instance has no hydrodynamics set");
     CK(cudaSetDevice(in->device));
     cudaStream_t s = in->stream;
+    // earlier work on the tracer buffers (a step) comes first; a new
+    // hydrodynamic state starts repacking on the instance's stream meanwhile
+    cudaEvent_t before;
+    CK(cudaEventCreateWithFlags(&before, cudaEventDisableTiming));
+    cudaError_t ev = cudaEventRecord(before, s);
+    if (ev == cudaSuccess) ev = cudaStreamWaitEvent(b->cs, before, 0);
+    cudaEventDestroy(before);
+    if (ev != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("cudaStreamWaitEvent", ev));
+    if ((!b->packed || b->packedVersion != in->hydroVersion) &&
+        !(b->packPending && b->packingVersion == in->hydroVersion)) {
+        if (b->packPending) {
+            int c = pack_finalize(b, stat);
+            if (c) return c;
+        }
+        int c = pack_enqueue(b, stat);
+        if (c) return c;
+    }
+    cudaStream_t ts = b->cs;
     const double* src = PROP;
     if (!*on_device) {
-        CK(cudaMemcpyAsync(b->stage.p, PROP, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(b->stage.p, PROP, sizeof(double) * in->n3, cudaMemcpyHostToDevice, ts));
         src = b->stage.p;
     }
     const long long off = (long long)*t * b->L.n3;
     // shift = mean over the water cells, rounded to an FP32 value
-    CK(mohid::water_mean(src, in->WP.p, b->L, b->partial.p, kMassBlocks, b->scratch.p, s));
-    CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    double sh = std::isfinite(*b->hmass) ? (double)(float)*b->hmass : 0.0;
+    CK(mohid::water_mean(src, in->WP.p, b->L, b->tpartial.p, kMassBlocks, b->tscratch.p, ts));
+    CK(cudaMemcpyAsync(b->hmass + 1, b->tscratch.p, sizeof(double), cudaMemcpyDeviceToHost, ts));
+    CK(cudaStreamSynchronize(ts));
+    double sh = std::isfinite(b->hmass[1]) ? (double)(float)b->hmass[1] : 0.0;
     b->shift[*t] = sh;
-    CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, sh, b->L, s));
+    CK(mohid::pack_tracer(src, b->PA.p + off, b->PB.p + off, in->KFloor.p, in->WP.p, sh, b->L, ts));
     // the mass fixer keeps the FP64 mass of the field as loaded (with the volume it starts the step in)
-    CK(mohid::mass_fix_load(src, in->Vold.p, in->WP.p, b->L, b->partial.p, kMassBlocks, sh, *t, b->nt,
-                            b->mfix.p, s));
+    CK(mohid::mass_fix_load(src, in->Vold.p, in->WP.p, b->L, b->tpartial.p, kMassBlocks, sh, *t, b->nt,
+                            b->mfix.p, ts));
     b->fixDirty = true;
-    CK(cudaStreamSynchronize(s));
+    b->targetVersion[*t] = in->hydroVersion;
+    CK(cudaStreamSynchronize(ts));
     return ok(stat);
 }
 
@@ -732,8 +830,8 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
                 return fail(MOHID_AD_ERR_OPTION, stat,
                             "set the reference of every tracer after (re)loading the tracer");
     Instance* in = b->in;
-    if (!b->packed || b->packedVersion != in->hydroVersion) {
-        int c = pack_hydro(b, stat);
+    {
+        int c = ensure_packed(b, stat);
         if (c) return c;
     }
     CK(cudaSetDevice(in->device));
@@ -796,8 +894,8 @@ int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* sta
     if (code) return fail(code, stat, why);
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
-    if (!b->packed || b->packedVersion != in->hydroVersion) {
-        int c = pack_hydro(b, stat);
+    {
+        int c = ensure_packed(b, stat);
         if (c) return c;
     }
     int c = ensure_shift_valid(b, p, stat);
@@ -845,8 +943,8 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
-    if (!b->packed || b->packedVersion != in->hydroVersion) {
-        int c = pack_hydro(b, stat);
+    {
+        int c = ensure_packed(b, stat);
         if (c) return c;
     }
     cudaStream_t s = in->stream;
@@ -968,8 +1066,8 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
                 if (t >= (int)b->refShift.size() || b->refShift[t] != b->shift[t])
                     return fail(MOHID_AD_ERR_OPTION, stat,
                                 "set the reference of every tracer after (re)loading the tracer");
-        if (!b->packed || b->packedVersion != b->in->hydroVersion) {
-            int c = pack_hydro(b, stat);
+        {
+            int c = ensure_packed(b, stat);
             if (c) return c;
         }
         int c = ensure_shift_valid(b, &p[q], stat);

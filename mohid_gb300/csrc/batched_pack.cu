@@ -99,7 +99,7 @@ struct PackIn {
 };
 struct PackOut {
     void *Qx, *Qy, *Qz, *Vis, *Dif;     // float, or __half (scaled) when halfQ / halfK
-    float iqx, iqy, iqz, ikh, ikv;      // 1/scale of the __half fields
+    const float* inv;                   // 1/scale of the __half fields (device, 5), or null
     int halfQ, halfK;
     float *AU, *AV, *rDZZ, *RV, *DVR, *Vhi, *Vlo;
     uint8_t *flag, *fflag;
@@ -124,12 +124,15 @@ __device__ __forceinline__ void put(void* dst, bool half, float inv, long long g
 __global__ void __launch_bounds__(kRowThreads) k_pack_fields(PackIn in, PackOut out, BLayout L)
 {
     const int NI = L.ni + 2, NJ = L.nj + 2;
+    float iv[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
+    if (out.inv)
+        for (int q = 0; q < 5; ++q) iv[q] = out.inv[q];
     for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
-        put(out.Qx, out.halfQ, out.iqx, g, in.Qx[e]);
-        put(out.Qy, out.halfQ, out.iqy, g, in.Qy[e]);
-        put(out.Qz, out.halfQ, out.iqz, g, in.Qz[e]);
-        put(out.Vis, out.halfK, out.ikh, g, in.Vis[e]);
-        put(out.Dif, out.halfK, out.ikv, g, in.Dif[e]);
+        put(out.Qx, out.halfQ, iv[0], g, in.Qx[e]);
+        put(out.Qy, out.halfQ, iv[1], g, in.Qy[e]);
+        put(out.Qz, out.halfQ, iv[2], g, in.Qz[e]);
+        put(out.Vis, out.halfK, iv[3], g, in.Vis[e]);
+        put(out.Dif, out.halfK, iv[4], g, in.Dif[e]);
         out.AU[g] = f64_to_f32(in.AU[e]);
         out.AV[g] = f64_to_f32(in.AV[e]);
         const float dz = f64_to_f32(in.DZZ[e]);
@@ -454,44 +457,29 @@ __global__ void __launch_bounds__(kRowThreads) k_fix_step_many(const BatchArgs* 
     fix_tracer(a.mpart, a.ntiles, a.ntAll, blockIdx.y, a.mfix);
 }
 
-// new hydrodynamics with static volumes: the mass each tracer keeps changes by
-// the sum over water cells of (VolumeZ_new - VolumeZ_prev) * value; cells whose
-// volume did not change (bit for bit) cost no FP64 instruction.  VolumeZ_prev
-// is then replaced by VolumeZ_new.  Block y = tracer.
-__global__ void __launch_bounds__(kRowThreads) k_fix_rebase(const float* P, long long ts, const double* Vnew,
-                                                          double* Vprev, const int* WP, const double* mfix, int nt,
-                                                          BLayout L, double* partial)
+// new hydrodynamics: flag any cell whose VolumeZ differs (bit for bit) from the
+// last pack's, and keep the new volumes for the next comparison
+__global__ void k_vol_changed(const double* __restrict__ Vnew, double* __restrict__ Vprev, long long n,
+                              unsigned* changed)
 {
-    const int t = blockIdx.y;
-    const double c0 = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
-    const float* Pt = P + (long long)t * ts;
-    double s = 0.0;
-    for_rows(L, 1, L.nk, [&](long long f, long long g, int i, int j, int) {
-        const double vn = Vnew[f], vp = Vprev[f];
-        if (same_bits(vn, vp)) return;
-        if (i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && WP[f] == 1) s = fma(vn - vp, (double)Pt[g] + c0, s);
-    });
-    const double S = block_neu(s, 0.0);
-    if (threadIdx.x == 0) {
-        partial[2 * ((long long)t * gridDim.x + blockIdx.x)] = S;
-        partial[2 * ((long long)t * gridDim.x + blockIdx.x) + 1] = 0.0;
+    bool c = false;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const double v = Vnew[e];
+        if (!same_bits(v, Vprev[e])) { c = true; Vprev[e] = v; }
     }
+    if (__any_sync(0xffffffffu, c) && (threadIdx.x & 31) == 0) *changed = 1u;
 }
 
-__global__ void k_fix_rebase_finish(const double* partial, int nb, int nt, double* mfix)
+// FP16 storage scales: the largest magnitude of a field maps to 2^14, so that
+// FP16 keeps 11 significant bits; scale[q] = absmax / 2^14, inv[q] = 1 / scale[q]
+__global__ void k_scales(const double* absmax, int n, float* scale, float* inv)
 {
-    for (int t = 0; t < nt; ++t) {
-        double S, Z;
-        warp_partials(partial + 2 * (long long)t * nb, nb, S, Z);
-        if (threadIdx.x == 0) mfix[1 + t] += S;
-    }
-}
-
-// Vprev = Vnew over the Size box
-__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst, long long n)
-{
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-        dst[e] = src[e];
+    const int q = threadIdx.x;
+    if (q >= n) return;
+    const double m = absmax[q];
+    const float sc = m > 0 ? (float)(m / 16384.0) : 1.0f;
+    scale[q] = sc;
+    inv[q] = 1.0f / sc;
 }
 
 inline unsigned blocks_for(long long n) { long long b = (n + 255) / 256; return (unsigned)(b > 65535 * 8 ? 65535 * 8 : (b < 1 ? 1 : b)); }
@@ -502,12 +490,12 @@ cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, co
                         const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
                         const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
                         void* oQx, void* oQy, void* oQz, void* oVis, void* oDif, bool halfQ, bool halfK,
-                        const float inv[5], float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
+                        const float* dinv, float* oAU, float* oAV, float* orDZZ, float* oRV, float* oDVR,
                         float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
                         const BLayout& L, cudaStream_t s)
 {
     PackIn in{Qx, Qy, Qz, V, Vold, Vis, Dif, AU, AV, DZZ, WP, OP, LP, CFU, CFV, CFW};
-    PackOut out{oQx, oQy, oQz, oVis, oDif, inv[0], inv[1], inv[2], inv[3], inv[4], halfQ ? 1 : 0, halfK ? 1 : 0,
+    PackOut out{oQx, oQy, oQz, oVis, oDif, dinv, halfQ ? 1 : 0, halfK ? 1 : 0,
                 oAU, oAV, orDZZ, oRV, oDVR, oVhi, oVlo, oflag, offlag, moving};
     cudaError_t e = cudaMemsetAsync(moving, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
@@ -608,16 +596,21 @@ cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStrea
     return cudaGetLastError();
 }
 
-cudaError_t mass_fix_rebase(const float* P, long long ts, int nt, const double* Vnew, double* Vprev, bool rebase,
-                            const int* WP, double* mfix, const BLayout& L, double* partial, int nblocks,
-                            cudaStream_t s)
+cudaError_t vol_changed(const double* Vnew, double* Vprev, long long n, unsigned* changed, cudaStream_t s)
 {
-    if (rebase) {
-        k_fix_rebase<<<dim3(nblocks, nt), kRowThreads, 0, s>>>(P, ts, Vnew, Vprev, WP, mfix, nt, L, partial);
-        k_fix_rebase_finish<<<1, 32, 0, s>>>(partial, nblocks, nt, mfix);
+    cudaError_t e = cudaMemsetAsync(changed, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    k_vol_changed<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(Vnew, Vprev, n, changed);
+    return cudaGetLastError();
+}
+cudaError_t fp16_scales(const double* const* fields, int nf, long long n, double* absmax, float* scale, float* inv,
+                        cudaStream_t s)
+{
+    for (int q = 0; q < nf; ++q) {
+        cudaError_t e = absmax_f64(fields[q], n, absmax + q, s);
+        if (e != cudaSuccess) return e;
     }
-    const long long n = (long long)(L.ni + 2) * (L.nj + 2) * (L.nk + 2);
-    k_copy_f64<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(Vnew, Vprev, n);
+    k_scales<<<1, 32, 0, s>>>(absmax, nf, scale, inv);
     return cudaGetLastError();
 }
 
