@@ -303,8 +303,10 @@ int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* sp
  * where mass is conserved exactly in the reference: closed boundaries (no
  * reference concentration set), a step that maps constants onto themselves
  * (continuity holds, XZFlow and Vertical1D off) and VolumeZ == VolumeZOld on
- * every cell; a new hydrodynamic state moves the target by the change of
- * VolumeZ.  Elsewhere the step runs without it. */
+ * every cell.  A new hydrodynamic state whose VolumeZ differs from the last one
+ * ends it for the tracers loaded before that state (their target no longer
+ * applies); tracers loaded afterwards keep it.  Elsewhere the step runs
+ * without it. */
 int mohid_ad_batched_set_mass_fix(const int* bid, const int* on, int* stat);
 
 /* Global mass budget of tracer t: Neumaier-compensated FP64 sum of
