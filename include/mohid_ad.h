@@ -265,7 +265,8 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
  * tracer of the batch uses open boundaries and must have one.  Set it after
  * the tracer itself: a tracer is held as its anomaly from a per-tracer
  * constant (the mean over its water cells, chosen when it is loaded), and
- * its reference is stored relative to the same constant. */
+ * its reference is stored relative to the same constant (the step subtracts
+ * the mass fixer's correction to that constant). */
 int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
                                    const int* on_device, int* stat);
 
@@ -297,17 +298,27 @@ int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* sp
 /* Mass fixer (*on != 0, the default).  No counterpart in the reference, whose
  * FP64 arithmetic conserves mass to round-off; it restores that for the FP32
  * form.  After every step each tracer's mass (compensated sum of VolumeZ *
- * PROP over water cells, accumulated in the step kernel) is brought back to
- * the FP64 mass of the field as loaded by adding one FP64 constant to every
- * water cell, which leaves the step's result otherwise unchanged.  It runs only
- * where mass is conserved exactly in the reference: closed boundaries (no
- * reference concentration set), a step that maps constants onto themselves
- * (continuity holds, XZFlow and Vertical1D off) and VolumeZ == VolumeZOld on
- * every cell.  A new hydrodynamic state whose VolumeZ differs from the last one
- * ends it for the tracers loaded before that state (their target no longer
- * applies); tracers loaded afterwards keep it.  Elsewhere the step runs
- * without it. */
+ * PROP over water cells, accumulated in the step kernel) is brought to its
+ * target by adding one FP64 constant to every water cell, which leaves the
+ * step's result otherwise unchanged.  The target is the FP64 mass of the
+ * field as loaded plus, with MassConservation open boundaries, the mass the
+ * steps moved through them since (FluxAtOpenBoundary: WFOB * DT times the
+ * inflow concentration where WFOB < 0 and times the new value where
+ * WFOB >= 0, summed in FP64 over the open boundary cells).  It runs where the
+ * reference's budget closes exactly: a step that maps constants onto
+ * themselves (continuity holds, XZFlow and Vertical1D off) and VolumeZ ==
+ * VolumeZOld on every cell.  A new hydrodynamic state whose VolumeZ differs
+ * from the last one ends it for the tracers loaded before that state (their
+ * target no longer applies); tracers loaded afterwards keep it.  With open
+ * boundaries, a step made without the fixer ends it for every tracer loaded
+ * before.  Elsewhere the step runs without it. */
 int mohid_ad_batched_set_mass_fix(const int* bid, const int* on, int* stat);
+
+/* Mass that entered tracer t through open boundaries since it was loaded, as
+ * the mass fixer's target followed it: mass = loaded mass + *flux while the
+ * fixer runs (0 on closed domains), NaN once the fixer stopped for the tracer
+ * (synchronous).  No counterpart in the reference. */
+int mohid_ad_batched_boundary_flux(const int* bid, const int* t, double* flux, int* stat);
 
 /* Global mass budget of tracer t: Neumaier-compensated FP64 sum of
  * VolumeZ * PROP over water cells (synchronous). */

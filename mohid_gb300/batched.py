@@ -100,6 +100,17 @@ class Batch:
         N.check(rc, "mohid_ad_batched_mass")
         return m.value
 
+    def boundary_flux(self, t: int) -> float:
+        """Mass that entered tracer t through open boundaries since it was
+        loaded, as the mass fixer follows it (0 on closed domains, NaN once the
+        fixer stopped for the tracer)."""
+        m = C.c_double(0.0)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_boundary_flux(C.byref(self._bid), C.byref(C.c_int(t)), C.byref(m),
+                                                     C.byref(st))
+        N.check(rc, "mohid_ad_batched_boundary_flux")
+        return m.value
+
     def sync(self):
         st = C.c_int(0)
         N.check(self.lib.mohid_ad_batched_sync(C.byref(self._bid), C.byref(st)), "mohid_ad_batched_sync")

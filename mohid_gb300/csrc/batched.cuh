@@ -88,6 +88,12 @@ struct BatchArgs {
     const float *Vhi, *Vlo;
     double* mpart;
     double* mfix;                       // the batch's fixer state (below)
+    // open boundaries under the fixer (else null): the step's boundary mass
+    // flux as partials of the obc_flux blocks, obpart[t * nob + blk] = sum of
+    // WFOB * DT * value over the block's boundary cells, obpart[ntAll * nob +
+    // blk] = sum of WFOB * DT
+    double* obpart;
+    int nob;
     int tilesX, ntiles, ntAll;          // tiles along i, tiles, tracers of the whole batch
     // scalars
     float DT, schmidtH, coefV, backV, tdec;
@@ -142,11 +148,13 @@ cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, co
                         float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
                         const BLayout& L, cudaStream_t s);
 
-// ---- mass fixer (closed domains).  Per batch a device array
+// ---- mass fixer.  Per batch a device array
 //   mfix[0] = sum of VolumeZ over water cells, mfix[1 + t] = target mass of
-//   tracer t (its FP64 mass when loaded), mfix[1 + nt + t] = the constant the
-//   stored values are relative to when loaded, mfix[1 + 2 nt + t] = the
-//   correction added to that constant since.
+//   tracer t (its FP64 mass when loaded plus the boundary flux since),
+//   mfix[1 + nt + t] = the constant the stored values are relative to when
+//   loaded, mfix[1 + 2 nt + t] = the correction added to that constant since,
+//   mfix[1 + 3 nt + t] = the mass that entered through open boundaries since
+//   (NaN once the targets are dropped).
 // sum of VolumeZ over water cells -> mfix[0] (deterministic)
 cudaError_t water_volume(const double* V, const int* WP, const BLayout& L, double* partial, int nblocks,
                          double* mfix, cudaStream_t s);
@@ -159,8 +167,22 @@ cudaError_t vol_changed(const double* Vnew, double* Vprev, long long n, unsigned
 // FP16 storage scales of nf FP64 fields on the device (absmax: nf doubles of scratch)
 cudaError_t fp16_scales(const double* const* fields, int nf, long long n, double* absmax, float* scale, float* inv,
                         cudaStream_t s);
-// after a step: correction[t] += (target[t] - mass now) / volume for every tracer of the batch
-cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s);
+// after a step: target[t] += the step's boundary flux (obpart != null, nob
+// blocks), then correction[t] += (target[t] - mass now) / volume for every
+// tracer of the batch whose target is set
+cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, const double* obpart, int nob,
+                          cudaStream_t s);
+// targets and boundary fluxes of every tracer dropped (NaN): a step with open
+// boundaries ran without the fixer following its boundary flux
+cudaError_t mass_fix_drop(double* mfix, int nt, cudaStream_t s);
+// Boundary columns (cflag has C_SOLVE and C_BP) in increasing 2-D offset:
+// list[0] = count, list[1 .. count] = offsets.  cnt: kObcBlocks ints of scratch.
+constexpr int kObcBlocks = 128;
+cudaError_t obc_columns(const uint8_t* cflag, const BLayout& L, int* cnt, int* list, cudaStream_t s);
+// The step's mass flux through the MassConservation open boundaries, for the
+// mass fixer: a covers every tracer of the batch (t0 = 0) with the step's input
+// and output buffers; partials to a.obpart (a.nob = kObcBlocks blocks).
+cudaError_t obc_flux(const BatchArgs& a, const int* list, bool halfQ, cudaStream_t s);
 // the same for `nb` batches whose argument records (device) have mpart != null
 cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,

@@ -43,10 +43,13 @@ struct Batch {
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
     DevBuf<float> Wsc;                   // THOMASZ W per cell, scratch of the step kernel
-    // mass fixer (closed domains, static volumes): VolumeZ as an FP32 pair,
-    // the fixer state (volume, targets, constants, corrections), per-tile sums
+    // mass fixer (static volumes): VolumeZ as an FP32 pair, the fixer state
+    // (volume, targets, constants, corrections, boundary fluxes), per-tile
+    // sums; with open boundaries the boundary columns and the per-block
+    // boundary fluxes of a step
     DevBuf<float> Vhi, Vlo;
-    DevBuf<double> mfix, mpart;
+    DevBuf<double> mfix, mpart, obpart;
+    DevBuf<int> obcol, obcnt;
     DevBuf<double> Vprev;                // VolumeZ of the last pack (Fortran layout)
     DevBuf<unsigned> moving;
     bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
@@ -63,6 +66,7 @@ struct Batch {
     int split = 4;                       // largest tracer group per launch: 8, 4 or 2
     bool tuned = false;
     int graphSched = -1, graphSplit = -1;
+    int graphFix = -1;                   // fixer / open-boundary launches the graph holds
     // asynchronous repack of a new hydrodynamic state (on the instance's
     // stream) and tracer loads (on their own stream, with their own scratch),
     // so that the two overlap; the host-side results of the repack are read
@@ -119,6 +123,7 @@ struct Batch {
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
         mfix.release(); mpart.release(); moving.release(); Vprev.release();
+        obpart.release(); obcol.release(); obcnt.release();
         tl.release(); tcost.release();
         dscale.release(); dinv.release(); vchanged.release(); tpartial.release(); tscratch.release();
         if (hp) cudaFreeHost(hp);
@@ -210,11 +215,18 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
 // relative continuity residual below which the step maps constants onto themselves
 constexpr double kContinuityTol = 1e-9;
 
-// the mass fixer runs on closed domains whose step maps constants onto
-// themselves (anomaly storage valid) and whose volumes do not move
+// the mass fixer runs where the step maps constants onto themselves (anomaly
+// storage valid) and the volumes do not move; with open boundaries its
+// targets follow the boundary flux of every step
 bool fix_active(const Batch* b)
 {
-    return b->massFix && !b->hasRef && b->shiftOk && b->staticVol;
+    return b->massFix && b->shiftOk && b->staticVol;
+}
+
+// which of the fixer's launches a step makes (fixer, boundary flux, target drop)
+int fix_key(const Batch* b)
+{
+    return (fix_active(b) ? 1 : 0) | (b->hasRef ? 2 : 0);
 }
 
 // Fold the fixer's corrections into the host-side constants (shift[t] = constant
@@ -224,7 +236,7 @@ cudaError_t fix_fold(Batch* b)
 {
     if (!b->fixDirty) return cudaSuccess;
     const int nt = b->nt;
-    std::vector<double> mf(1 + 3 * nt);
+    std::vector<double> mf(1 + 4 * nt);
     cudaError_t e = cudaStreamSynchronize(b->in->stream);
     if (e == cudaSuccess) e = cudaMemcpy(mf.data(), b->mfix.p, sizeof(double) * mf.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return e;
@@ -233,19 +245,11 @@ cudaError_t fix_fold(Batch* b)
         mf[1 + t] = std::nan("");
         mf[1 + nt + t] = b->shift[t];
         mf[1 + 2 * nt + t] = 0.0;
+        mf[1 + 3 * nt + t] = std::nan("");
     }
     e = cudaMemcpy(b->mfix.p, mf.data(), sizeof(double) * mf.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) b->fixDirty = false;
     return e;
-}
-
-// forget the fixer targets (the mass they hold no longer applies)
-cudaError_t fix_invalidate(Batch* b, cudaStream_t s)
-{
-    std::vector<double> nan(b->nt, std::nan(""));
-    cudaError_t e = cudaMemcpyAsync(b->mfix.p + 1, nan.data(), sizeof(double) * b->nt, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
-    return cudaStreamSynchronize(s);
 }
 
 // Enqueue the repack of the instance's current hydrodynamics on the instance's
@@ -279,6 +283,7 @@ int pack_enqueue(Batch* b, int* stat)
                            in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
                            b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
     CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
+    CK(mohid::obc_columns(b->cflag.p, L, b->obcnt.p, b->obcol.p, s));
     // tiles left out of a schedule keep no stale mass-fixer sums
     CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
     CK(cudaMemcpyAsync(b->hcost, b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
@@ -356,6 +361,7 @@ int pack_finalize(Batch* b, int* stat)
             if (b->targetVersion[t] != b->packingVersion) {
                 const double nan = std::nan("");
                 CK(cudaMemcpyAsync(b->mfix.p + 1 + t, &nan, sizeof(double), cudaMemcpyHostToDevice, s));
+                CK(cudaMemcpyAsync(b->mfix.p + 1 + 3 * b->nt + t, &nan, sizeof(double), cudaMemcpyHostToDevice, s));
                 CK(cudaStreamSynchronize(s));
             }
     b->packedOnce = true;
@@ -422,6 +428,8 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Vlo = b->Vlo.p;
     a.mfix = b->mfix.p;
     a.mpart = fix_active(b) ? b->mpart.p : nullptr;
+    a.obpart = fix_active(b) && b->hasRef ? b->obpart.p : nullptr;
+    a.nob = mohid::kObcBlocks;
     a.tilesX = b->tilesX;
     a.ntiles = b->ntiles;
     a.ntAll = b->nt;
@@ -492,7 +500,9 @@ int launches_per_step(const Batch* b)
 {
     int n = 0;
     for (int left = b->nt; left > 0; left -= group_size(b, left)) ++n;
-    return n + (fix_active(b) ? 1 : 0);
+    if (fix_active(b)) n += b->hasRef ? 2 : 1;       // boundary flux, fixer
+    else if (b->hasRef) n += 1;                      // targets dropped
+    return n;
 }
 
 // one transport step of every tracer.  real == false (the autotuner): the step
@@ -516,7 +526,16 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
     }
     if (!real) return cudaSuccess;
     if (fix_active(b)) {
-        cudaError_t e = mohid::mass_fix_step(b->mpart.p, b->ntiles, b->nt, b->mfix.p, s);
+        cudaError_t e = cudaSuccess;
+        if (b->hasRef)                           // the target follows the boundary flux
+            e = mohid::obc_flux(make_bargs(b, p, 0, b->nt, Pin, Pout), b->obcol.p, b->storage >= 1, s);
+        if (e == cudaSuccess)
+            e = mohid::mass_fix_step(b->mpart.p, b->ntiles, b->nt, b->mfix.p, b->hasRef ? b->obpart.p : nullptr,
+                                     mohid::kObcBlocks, s);
+        if (e != cudaSuccess) return e;
+    } else if (b->hasRef) {
+        // a boundary flux the targets did not follow: they no longer apply
+        cudaError_t e = mohid::mass_fix_drop(b->mfix.p, b->nt, s);
         if (e != cudaSuccess) return e;
     }
     b->cur = !b->cur;
@@ -609,6 +628,12 @@ cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
     const bool open = std::any_of(E->m.begin(), E->m.end(), [](const Batch* b) { return b->hasRef; });
     cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
                                            method, limiter, open, E->s);
+    for (size_t q = 0; q < n && e == cudaSuccess; ++q) {
+        Batch* b = E->m[q];
+        if (!b->hasRef) continue;
+        if (fix_active(b)) e = mohid::obc_flux(E->hA[off + q], b->obcol.p, false, E->s);
+        else e = mohid::mass_fix_drop(b->mfix.p, b->nt, E->s);
+    }
     if (e == cudaSuccess && std::any_of(E->m.begin(), E->m.end(), fix_active))
         e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->nt, E->s);
     E->cur = !E->cur;
@@ -676,7 +701,10 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     b->ntiles = b->tilesX * ((in->nj + mohid::kTY - 1) / mohid::kTY);
     if ((e = b->Vhi.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Vlo.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->mfix.alloc(1 + 3 * (size_t)b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->mfix.alloc(1 + 4 * (size_t)b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->obpart.alloc((size_t)(b->nt + 1) * mohid::kObcBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->obcol.alloc(n2 + 1)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->obcnt.alloc(mohid::kObcBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = cudaMallocHost((void**)&b->hcost, sizeof(int) * (size_t)b->ntiles)) != cudaSuccess)
         return bad(e, "cudaMallocHost");
@@ -804,7 +832,8 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
         CK(cudaMemcpyAsync(b->stage.p, ReferenceProp, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
         src = b->stage.p;
     }
-    CK(fix_fold(b));                             // open boundaries: the mass fixer stops
+    // stored relative to the tracer's loaded constant, like the tracer; the
+    // step subtracts the mass fixer's correction to that constant
     CK(mohid::pack_shift_f32(src, b->Ref.p + (long long)*t * b->L.n3, in->WP.p, b->shift[*t], b->L, s));
     CK(cudaStreamSynchronize(s));
     b->hasRef = true;
@@ -856,6 +885,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     if (pairs > 0) {
         const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
                            b->graphSched == b->sched && b->graphSplit == b->split &&
+                           b->graphFix == fix_key(b) &&
                            std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
         if (!reuse) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -876,6 +906,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphParams = *p;
             b->graphSched = b->sched;
             b->graphSplit = b->split;
+            b->graphFix = fix_key(b);
         }
         CK(cudaGraphLaunch(b->graph, s));
     }
@@ -955,6 +986,21 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     *mass = *b->hmass;
+    return ok(stat);
+}
+
+int mohid_ad_batched_boundary_flux(const int* bid, const int* t, double* flux, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !flux) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    cudaStream_t s = in->stream;
+    CK(cudaMemcpyAsync(b->hmass, b->mfix.p + 1 + 3 * b->nt + *t, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *flux = *b->hmass;
     return ok(stat);
 }
 

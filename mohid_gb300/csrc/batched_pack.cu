@@ -420,33 +420,60 @@ __global__ void k_fix_set(const double* partial, int nb, double* mfix, int mode,
         mfix[1 + t] = S;
         mfix[1 + nt + t] = shift;
         mfix[1 + 2 * nt + t] = 0.0;
+        mfix[1 + 3 * nt + t] = 0.0;
     }
 }
 
-// one block per tracer: the tiles' sums of VolumeZ * stored value (each
+// One block per tracer: the tiles' sums of VolumeZ * stored value (each
 // thread a strided share in FP64, the threads combined by a compensated tree in
 // a fixed order), then correction += (target - mass) / volume, where mass = that
 // sum + (constant + correction) * volume.  Adding the correction to every water
 // cell (through the constant) leaves the step's result otherwise unchanged:
-// the fixer only runs when the step maps constants onto themselves.
-__device__ void fix_tracer(const double* mpart, int ntiles, int nt, int t, double* mfix)
+// the fixer only runs when the step maps constants onto themselves.  With open
+// boundaries (obpart != null) the target first takes the step's boundary flux
+//   phi = -(sum of WFOB * DT) * (constant + correction) - sum of WFOB * DT * value,
+// the value being the stored inflow concentration where WFOB < 0 and the new
+// stored value where WFOB >= 0 (obc_flux).  A tracer whose target was dropped
+// (NaN) is left alone.
+__device__ void fix_tracer(const double* mpart, int ntiles, int nt, int t, double* mfix, const double* obpart,
+                           int nob)
 {
     double s = 0.0;
     for (int q = threadIdx.x; q < ntiles; q += blockDim.x) s += mpart[(long long)t * ntiles + q];
     const double sum = block_neu(s, 0.0);
+    double zs = 0.0, ws = 0.0;
+    if (obpart) {
+        double z = 0.0, w = 0.0;
+        for (int q = threadIdx.x; q < nob; q += blockDim.x) {
+            z += obpart[(long long)t * nob + q];
+            w += obpart[(long long)nt * nob + q];
+        }
+        __syncthreads();                         // block_neu's shared words are reused
+        zs = block_neu(z, 0.0);
+        __syncthreads();
+        ws = block_neu(w, 0.0);
+    }
     if (threadIdx.x == 0) {
         const double W = mfix[0];
-        if (W > 0.0) {
+        double target = mfix[1 + t];
+        if (W > 0.0 && !isnan(target)) {
             const double cnow = mfix[1 + nt + t] + mfix[1 + 2 * nt + t];
-            mfix[1 + 2 * nt + t] += (mfix[1 + t] - (sum + cnow * W)) / W;
+            if (obpart) {
+                const double phi = -(ws * cnow) - zs;
+                target += phi;
+                mfix[1 + t] = target;
+                mfix[1 + 3 * nt + t] += phi;
+            }
+            mfix[1 + 2 * nt + t] += (target - (sum + cnow * W)) / W;
         }
     }
 }
 
 // block t: tracer t of the batch
-__global__ void __launch_bounds__(kRowThreads) k_fix_step(const double* mpart, int ntiles, int nt, double* mfix)
+__global__ void __launch_bounds__(kRowThreads) k_fix_step(const double* mpart, int ntiles, int nt, double* mfix,
+                                                         const double* obpart, int nob)
 {
-    fix_tracer(mpart, ntiles, nt, blockIdx.x, mfix);
+    fix_tracer(mpart, ntiles, nt, blockIdx.x, mfix, obpart, nob);
 }
 
 // block (b, t): tracer t of batch b (blocks past a batch's tracer count return)
@@ -454,7 +481,75 @@ __global__ void __launch_bounds__(kRowThreads) k_fix_step_many(const BatchArgs* 
 {
     const BatchArgs& a = As[blockIdx.x];
     if (!a.mpart || (int)blockIdx.y >= a.ntAll) return;
-    fix_tracer(a.mpart, a.ntiles, a.ntAll, blockIdx.y, a.mfix);
+    fix_tracer(a.mpart, a.ntiles, a.ntAll, blockIdx.y, a.mfix, a.obpart, a.nob);
+}
+
+// targets and boundary fluxes dropped
+__global__ void k_fix_drop(double* mfix, int nt)
+{
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        mfix[1 + t] = nan;
+        mfix[1 + 3 * nt + t] = nan;
+    }
+}
+
+// ------------------------------------------------------------------ open-boundary columns
+__device__ __forceinline__ bool obc_column(uint8_t c)
+{
+    return (c & (C_SOLVE | C_BP)) == (C_SOLVE | C_BP);
+}
+
+// block b counts the boundary columns of its chunk [b * chunk, (b + 1) * chunk)
+__global__ void __launch_bounds__(kRowThreads) k_obc_count(const uint8_t* __restrict__ cflag, long long n2,
+                                                          long long chunk, int* cnt)
+{
+    __shared__ int wsum[kRowThreads / 32];
+    const long long b0 = blockIdx.x * chunk, b1 = min(n2, b0 + chunk);
+    int c = 0;
+    for (long long e = b0 + threadIdx.x; e < b1; e += blockDim.x) c += obc_column(cflag[e]) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int q = 0; q < kRowThreads / 32; ++q) n += wsum[q];
+        cnt[blockIdx.x] = n;
+    }
+}
+
+// block b writes its chunk's boundary columns, in order, after those of blocks 0 .. b-1
+__global__ void __launch_bounds__(kRowThreads) k_obc_write(const uint8_t* __restrict__ cflag, long long n2,
+                                                          long long chunk, const int* __restrict__ cnt, int* list)
+{
+    __shared__ int wsum[kRowThreads / 32];
+    __shared__ int base;
+    if (threadIdx.x == 0) {
+        int o = 0;
+        for (int q = 0; q < (int)blockIdx.x; ++q) o += cnt[q];
+        base = o;
+        if (blockIdx.x == gridDim.x - 1) list[0] = o + cnt[blockIdx.x];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long b0 = blockIdx.x * chunk, b1 = min(n2, b0 + chunk);
+    for (long long e0 = b0; e0 < b1; e0 += blockDim.x) {
+        const long long e = e0 + threadIdx.x;
+        const bool f = e < b1 && obc_column(cflag[e]);
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) wsum[w] = __popc(m);
+        __syncthreads();
+        int off = base;
+        for (int q = 0; q < w; ++q) off += wsum[q];
+        if (f) list[1 + off + __popc(m & ((1u << lane) - 1u))] = (int)e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int n = 0;
+            for (int q = 0; q < kRowThreads / 32; ++q) n += wsum[q];
+            base += n;
+        }
+        __syncthreads();
+    }
 }
 
 // new hydrodynamics: flag any cell whose VolumeZ differs (bit for bit) from the
@@ -585,9 +680,22 @@ cudaError_t mass_fix_load(const double* P, const double* V, const int* WP, const
     k_fix_set<<<1, 32, 0, s>>>(partial, nblocks, mfix, 1, t, nt, shift);
     return cudaGetLastError();
 }
-cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, cudaStream_t s)
+cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, const double* obpart, int nob,
+                          cudaStream_t s)
 {
-    k_fix_step<<<nt, kRowThreads, 0, s>>>(mpart, ntiles, nt, mfix);
+    k_fix_step<<<nt, kRowThreads, 0, s>>>(mpart, ntiles, nt, mfix, obpart, nob);
+    return cudaGetLastError();
+}
+cudaError_t mass_fix_drop(double* mfix, int nt, cudaStream_t s)
+{
+    k_fix_drop<<<1, 128, 0, s>>>(mfix, nt);
+    return cudaGetLastError();
+}
+cudaError_t obc_columns(const uint8_t* cflag, const BLayout& L, int* cnt, int* list, cudaStream_t s)
+{
+    const long long chunk = (L.n2 + kObcBlocks - 1) / kObcBlocks;
+    k_obc_count<<<kObcBlocks, kRowThreads, 0, s>>>(cflag, L.n2, chunk, cnt);
+    k_obc_write<<<kObcBlocks, kRowThreads, 0, s>>>(cflag, L.n2, chunk, cnt, list);
     return cudaGetLastError();
 }
 cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s)

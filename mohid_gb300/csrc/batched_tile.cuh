@@ -218,6 +218,20 @@ __device__ __forceinline__ float ldg_as(const void* p, long long a, float s)
     return tofl<T>(reinterpret_cast<const T*>(p)[a], s);
 }
 
+// Net water flux out of a MassConservation open-boundary cell through its
+// exterior faces (AD:5680-5742, FluxAtOpenBoundary): the transports into the
+// cell through its west, south and bottom faces less those out through east,
+// north and top (faces that are not compute faces count zero), less the
+// volume change rate (V - Vold) / DT = dvr / (rV * DT).  The face sum is
+// formed in FP32 with rounded adds, which are never contracted, so the step
+// and the mass fixer's boundary budget get the same value.
+__device__ __forceinline__ float obc_wfob(float qw, float qe, float qs, float qn, float qb, float qt, float dvr,
+                                          float rV, float DT)
+{
+    const float h = __fsub_rn(__fadd_rn(__fsub_rn(__fadd_rn(__fsub_rn(qw, qe), qs), qn), qb), qt);
+    return (float)((double)h - (double)dvr / ((double)rV * (double)DT));
+}
+
 // One face of the tile at one layer.  WEST: the face between cells
 // (i0+b, j0+a-1) and (i0+b, j0+a), a = 0..TY; otherwise the face between
 // (i0+b-1, j0+a) and (i0+b, j0+a), b = 0..TX.  Tracer-independent part first
@@ -507,13 +521,11 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                 const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
                 const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
                 const uint8_t* ffl = st + SL::oF + ty * FBX + tx;
-                const double hz =
-                    (double)(((ffl[0] & FU_ACT) ? tofl<QT>(qx[fw], A.qsx) : 0.f) -
-                             ((ffl[FBX] & FU_ACT) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f) +
-                             ((ffl[0] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f) -
-                             ((ffl[1] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f) +
-                             ((fl & F_CFW) ? qz : 0.f) - ((flp & F_CFW) ? qzp : 0.f));
-                wfob = (float)(hz - (double)dvr / ((double)rVk * (double)DT));
+                wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[fw], A.qsx) : 0.f,
+                                (ffl[FBX] & FU_ACT) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f,
+                                (ffl[0] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f,
+                                (ffl[1] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f,
+                                (fl & F_CFW) ? qz : 0.f, (flp & F_CFW) ? qzp : 0.f, dvr, rVk, DT);
                 if (wfob >= 0.f) E += wfob * dtv;
             }
             // THOMASZ factorisation of row k
@@ -533,7 +545,11 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                     TI = fmaf(dtv, (FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
                                    (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
                 if (obc && wfob < 0.f) {
-                    const float ext = Pc * (1.f - A.tdec) + A.Ref[(long long)t * A.ts + cb + ko] * A.tdec;
+                    // the reference is stored relative to the tracer's loaded
+                    // constant; the fixer's correction moves it with the field
+                    const float ref = A.Ref[(long long)t * A.ts + cb + ko] -
+                                      (float)A.mfix[1 + 2 * A.ntAll + A.t0 + t];
+                    const float ext = Pc * (1.f - A.tdec) + ref * A.tdec;
                     TI -= wfob * ext * dtv;
                 }
                 const float G = (TI - D * Gp[t]) * inv;

@@ -86,6 +86,31 @@ def test_mass_with_moving_volumes(built):
     assert abs(after - before) / before < 1e-13
 
 
+@pytest.mark.parametrize("spec", [dict(ni=10, nj=6, nk=3, land_frac=0.0, seed=7, open_sides=12, bathy_kind=1),
+                                  dict(ni=11, nj=9, nk=5, land_frac=0.15, land_kind=1, seed=9, open_sides=3,
+                                       bathy_kind=1)])
+@pytest.mark.parametrize("opt", [dict(), dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1)])
+@pytest.mark.parametrize("decay", [0.0, 300.0])
+def test_mass_budget_open_boundaries(built, spec, opt, decay):
+    # static volumes, MassConservation open boundaries: the mass changes by
+    # exactly the flux through the boundary cells' exterior faces
+    from tests.cases import boundary_flux
+    d = synth.generate(synth.GenSpec(**spec, dt=30.0))
+    P = d.tracer(3, 1.0, 0.6, seed=5)
+    R = d.reference(2.5, 0.3, seed=6)
+    p = O.params(DTProp=30.0, BoundaryCondition=1, DecayTime=decay, **opt)
+    wp = d.water_mask()
+    scale = np.sum(np.abs(d.VolumeZ[wp] * P[wp]))
+    moved = 0.0
+    for _ in range(5):
+        m0, P0 = O.mass(d, P), P.copy()
+        assert O.step(d, P, p, ReferenceProp=R) == 0
+        phi = boundary_flux(d, P0, P, R, 30.0, decay)
+        assert abs(O.mass(d, P) - m0 - phi) <= 1e-13 * scale
+        moved += abs(phi)
+    assert moved > 1e-6 * scale                  # the boundaries do move mass
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
