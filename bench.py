@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -226,6 +227,7 @@ class Case:
         # large workloads reuse a few distinct seeded fields, scaled per tracer
         self.distinct = distinct_tracers or self.nt
         self._base = {}
+        self._mass = {}
         self.refs = None
         if w.open_boundary:
             self.refs = [self.d.reference(1.0 + 0.1 * t, 0.3, seed=500 + t) for t in range(min(self.nt, 4))]
@@ -246,6 +248,18 @@ class Case:
 
     def ref(self, t: int):
         return None if self.refs is None else self.refs[t % len(self.refs)]
+
+    def load_mass(self, t: int) -> float:
+        """FP64 mass (sum of VolumeZ * value over water cells) of tracer t as
+        loaded, layer by layer; a scaled tracer's is the scaled mass of its base."""
+        import numpy as np
+        q = t % self.distinct if self.distinct < self.nt else t
+        if q not in self._mass:
+            P = self.tracer(q)
+            V, wp = self.d.arrays["VolumeZ"], self.d.water_mask()
+            self._mass[q] = float(sum(np.dot(V[k][wp[k]], P[k][wp[k]]) for k in range(V.shape[0])))
+        scale = self.w.tracers[t][1] / self.w.tracers[q][1] if self.distinct < self.nt else 1.0
+        return self._mass[q] * scale
 
     @property
     def cells(self) -> int:
@@ -418,6 +432,27 @@ def time_steps(step, stream, steps, world):
     return e0.elapsed_time(e1) / steps, clocks
 
 
+def tracer_groups(nt: int, split: int) -> list:
+    """Tracers per step-kernel launch: groups of `split` (8, 4 or 2), then 4, 2, 1."""
+    out, left = [], nt
+    while left > 0:
+        g = 8 if left >= 8 and split >= 8 else 4 if left >= 4 and split >= 4 else 2 if left >= 2 else 1
+        out.append(g)
+        left -= g
+    return out
+
+
+def mass_defects(objs, cases):
+    """Per tracer |mass now - mass loaded - boundary flux since| / mass loaded:
+    the FP64 budget of the batched form (NaN where the mass fixer did not run)."""
+    out = []
+    for (_, b), c in zip(objs, cases):
+        for t in range(c.nt):
+            m0 = c.load_mass(t)
+            out.append(abs(b.mass(t) - m0 - b.boundary_flux(t)) / abs(m0))
+    return out
+
+
 def run_batched(cases, storage, steps, warmup, world, e2e=True):
     import torch
     from mohid_gb300 import advdiff, batched
@@ -447,14 +482,18 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
     for _, b in objs:
         b.sync()
     nt = cases[0].nt
+    defects = mass_defects(objs, cases)
     if ensemble:
-        # one ensemble launch, plus the mass fixer's finish on closed domains
-        # (every ensemble workload here has static volumes)
-        launches = steps * (1 + (1 if cases[0].refs is None else 0))
-        sched = {"launches": launches // steps, "sched": "persistent tile list (ensemble)", "split": nt}
+        # one ensemble launch, the boundary flux of each open member and the
+        # mass fixer's finish (every ensemble workload here has static volumes)
+        per = 1 + sum(1 for c in cases if c.refs is not None) + 1
+        launches = steps * per
+        sched = {"launches": per, "sched": "persistent tile list (ensemble)", "split": nt}
+        groups = [min(nt, 4)]
     else:
         sched = objs[0][1].schedule()              # as chosen by the autotuner
         launches = steps * sched["launches"]
+        groups = tracer_groups(nt, sched["split"])
 
     e2e_s = h2d = d2h = None
     if e2e:
@@ -491,12 +530,14 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
         b.destroy()
         ad.kill()
     cells = sum(c.cells for c in cases)
-    # step-kernel launches per step (the fixer's finish excluded; its time stays in ms)
-    g = 1 if ensemble else sched["launches"] - (1 if cases[0].refs is None else 0)
+    # step-kernel launches per step (the fixer's and boundary flux's launches
+    # excluded; their time stays in ms)
+    g = len(groups)
     return dict(ms=ms, kernel_ms=ms / g, launches=launches, e2e_s=e2e_s, h2d=h2d, d2h=d2h, cells=cells, sched=sched,
                 nt=nt, bytes_per_update=8.0 + SHARED_BYTES[storage] / nt,
                 bytes_per_launch=cells * (8.0 * nt + SHARED_BYTES[storage]) / g, dtype="f32", clocks=clocks,
-                kernel=("ensemble_kernel" if ensemble else "batched_kernel") + f"<{min(nt, 4)}>")
+                kernel=("ensemble_kernel" if ensemble else "batched_kernel") + f"<{max(groups)}>",
+                mass_defects=defects)
 
 
 # ----------------------------------------------------------------------------- main
@@ -623,6 +664,12 @@ def main():
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
+    if r.get("mass_defects"):
+        md = r["mass_defects"]
+        line["mass_defect"] = {
+            "max": None if any(math.isnan(x) for x in md) else max(md), "tracers": len(md),
+            "definition": "per tracer |mass now - mass loaded - open-boundary flux since| / mass loaded after "
+                          "the warm-up and timed steps; mass = FP64 sum of VolumeZ * value over water cells"}
     if plain is not None:
         pv = world * cells * plain["nt"] / (max_over_ranks(plain["ms"], world) / 1e3)
         line["plain_f64"] = {"value": pv, "unit": unit, "ms_per_step": plain["ms"],
