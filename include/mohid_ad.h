@@ -103,7 +103,7 @@ typedef struct mohid_ad_params {
     double ImpExp_AdvYY;          /* must be 0 (explicit) in this build               */
     double ImpExp_DifH;           /* must be 0: the reference requires explicit H-diff */
     int    NullDif;               /* LOGICAL                                          */
-    int    BoundaryCondition;     /* used only when ReferenceProp is given            */
+    int    BoundaryCondition;     /* MOHID_BC_*; 4 and 8 also act without a reference */
     double DecayTime;             /* [s]                                              */
     int    AdvectionNudging;      /* LOGICAL, must be .false. in this build           */
     int    AdvectionNudgingCells;
@@ -171,7 +171,12 @@ int mohid_ad_set_hydro(const int* id,
  * place, as AdvectionDiffusion does (THOMASZ_NewType2's RES aliases PROP,
  * ModuleFunctions.F90:4026-4123).  ReferenceProp may be NULL (closed
  * boundaries); when given, `p->BoundaryCondition` selects the open-boundary
- * treatment (ModuleAdvectionDiffusion.F90:5369-5742).
+ * treatment (ModuleAdvectionDiffusion.F90:5369-5742): MassConservation,
+ * ImposedValue, SubModel, NullGradient, MassConservNullGrad or Cyclic
+ * (Orlanski returns MOHID_AD_ERR_UNSUPPORTED).  As in the reference,
+ * NullGradient sets the boundary columns to their neighbours' mean after the
+ * solve whether or not ReferenceProp is given (AD:1874-1987), and Cyclic
+ * (AD:2121-2224) needs ReferenceProp (MOHID_AD_ERR_OPTION without it).
  */
 int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
                            const mohid_ad_params* p, int* stat);
@@ -246,7 +251,8 @@ int mohid_ad_kill(int* id, int* stat);
  * Supported options: AdvMethodH UpwindOrder1 or P2_TVD (any limiter),
  * implicit upwind vertical advection, implicit vertical diffusion,
  * Docycle_method 1, closed or MassConservation open boundaries.  Other
- * options return MOHID_AD_ERR_UNSUPPORTED (use the plain form).
+ * options (NullGradient and Cyclic boundaries among them, with or without a
+ * reference) return MOHID_AD_ERR_UNSUPPORTED (use the plain form).
  */
 int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat);
 

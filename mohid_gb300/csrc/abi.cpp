@@ -17,6 +17,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/mohid_ad.h"
 #include "common.cuh"
@@ -44,7 +45,7 @@ void Instance::release()
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
                            &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref};
     for (auto* b : d) b->release();
-    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD};
+    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl};
     for (auto* b : i) b->release();
     status.release();
     if (hstatus) cudaFreeHost(hstatus);
@@ -93,12 +94,16 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
     if (mH == 4 && (p->TVDLimitationH < 1 || p->TVDLimitationH > 5)) { why = "TVDLimitationH must be 1..5"; return MOHID_AD_ERR_OPTION; }
     if (mV == 4 && (p->TVDLimitationV < 1 || p->TVDLimitationV > 5)) { why = "TVDLimitationV must be 1..5"; return MOHID_AD_ERR_OPTION; }
     if (p->Docycle_method != 1 && p->Docycle_method != 2) { why = "Docycle_method must be 1 or 2"; return MOHID_AD_ERR_OPTION; }
-    if (hasRef) {
+    {
         const int bc = p->BoundaryCondition;
-        if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
-            why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
+        if (hasRef) {
+            if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
+                why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
+            }
+            if (bc == MOHID_BC_ORLANSKI) { why = "Orlanski open boundaries not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+        } else if (bc == MOHID_BC_CYCLIC) {
+            why = "cyclic boundaries read ReferenceProp (reference Prop_CyclicBoundary)"; return MOHID_AD_ERR_OPTION;
         }
-        if (bc != 1 && bc != 2 && bc != 5) { why = "BoundaryCondition 4/6/7/8 not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     }
     if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
@@ -115,6 +120,19 @@ int status_to_code(unsigned int s, std::string& why)
     if (s & MOHID_DEV_NONFINITE) { why = "non-finite concentration after the solve"; return MOHID_AD_ERR_NONFINITE; }
     if (s & MOHID_DEV_TIMEOUT) { why = "bounded device wait expired"; return MOHID_AD_ERR_TIMEOUT; }
     return MOHID_AD_SUCCESS;
+}
+
+// boundary conditions the reference applies after the solve (AD:1874-1880),
+// whether or not a reference is given
+cudaError_t post_solve(Instance* in, double* P, const double* Ref, const mohid_ad_params* p)
+{
+    if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT)
+        return mohid::launch_null_gradient(in->ni, in->nj, in->nk, P, in->CFU.p, in->CFV.p, in->KFloor.p,
+                                           in->bcols.p, in->nbcols, in->stream);
+    if (p->BoundaryCondition == MOHID_BC_CYCLIC)
+        return mohid::launch_cyclic(in->ni, in->nj, in->nk, P, Ref, in->KFloor.p, in->bcols.p, in->nbcols,
+                                    in->cycl.p, in->nrows, in->ncyc, in->stream);
+    return cudaSuccess;
 }
 
 mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const double* Ref,
@@ -263,6 +281,31 @@ int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize, const
     if ((e = cudaMemcpy(in->KFloor.p, KFloorZ, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
     if ((e = cudaMemcpy(in->BP2D.p, BoundaryPoints2D, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
     {
+        // boundary columns in the reference's sweep order (j outer, i inner);
+        // rows i with boundary points at j = 1 and nj, columns j with boundary
+        // points at i = 1 and ni (Prop_CyclicBoundary AD:2171-2220)
+        std::vector<int> cols, rows, cyc;
+        const int ni = in->ni, nj = in->nj, sj = ni + 2;
+        auto bp = [&](int i, int j) { return BoundaryPoints2D[(size_t)i + (size_t)sj * j] == 1; };
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i)
+                if (bp(i, j)) cols.push_back(i + sj * j);
+        for (int i = 2; i <= ni - 1; ++i)
+            if (bp(i, 1) && bp(i, nj)) rows.push_back(i);
+        for (int j = 2; j <= nj - 1; ++j)
+            if (bp(1, j) && bp(ni, j)) cyc.push_back(j);
+        in->nbcols = (int)cols.size();
+        in->nrows = (int)rows.size();
+        in->ncyc = (int)cyc.size();
+        rows.insert(rows.end(), cyc.begin(), cyc.end());
+        if ((e = in->bcols.alloc(cols.size())) != cudaSuccess) return bad(e, "cudaMalloc");
+        if ((e = in->cycl.alloc(rows.size())) != cudaSuccess) return bad(e, "cudaMalloc");
+        if (!cols.empty() && (e = cudaMemcpy(in->bcols.p, cols.data(), sizeof(int) * cols.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
+        if (!rows.empty() && (e = cudaMemcpy(in->cycl.p, rows.data(), sizeof(int) * rows.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
+    }
+    {
         std::lock_guard<std::mutex> lk(g_mu);
         *id = g_next_id++;
         g_inst[*id] = in;
@@ -315,6 +358,7 @@ int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PRO
     CK(cudaSetDevice(in->device));
     mohid::PlainArgs a = make_args(in, PROP_in, PROP_out, ReferenceProp, p);
     CK(mohid::launch_plain_f64(a, in->stream));
+    CK(post_solve(in, PROP_out, ReferenceProp, p));
     return ok(stat);
 }
 
@@ -335,6 +379,7 @@ int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceP
     CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
     mohid::PlainArgs a = make_args(in, in->Pin.p, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p);
     CK(mohid::launch_plain_f64(a, in->stream));
+    CK(post_solve(in, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p));
     CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
     CK(cudaMemcpyAsync(PROP, in->Pout.p, bd, cudaMemcpyDeviceToHost, in->stream));
     CK(cudaStreamSynchronize(in->stream));

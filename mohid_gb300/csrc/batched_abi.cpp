@@ -209,6 +209,10 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     if (hasRef && p->BoundaryCondition != MOHID_BC_MASS_CONSERVATION) {
         why = "batched form: only MassConservation open boundaries"; return MOHID_AD_ERR_UNSUPPORTED;
     }
+    // applied after the solve even without a reference (AD:1874-1880)
+    if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT || p->BoundaryCondition == MOHID_BC_CYCLIC) {
+        why = "batched form: NullGradient / Cyclic boundaries (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
+    }
     return MOHID_AD_SUCCESS;
 }
 

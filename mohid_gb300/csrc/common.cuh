@@ -39,5 +39,15 @@ cudaError_t launch_thomasz_f64(int ni, int nj, int nk, const double* D, const do
                                unsigned int* status, cudaStream_t s);
 cudaError_t launch_check_faces(int ni, int nj, int nk, const int* CFU, const int* CFV,
                                const int* CFW, unsigned int* status, cudaStream_t s);
+// Boundary conditions applied after the solve (AD:1874-1880), in place on P
+// (Fortran layout).  cols: the 2-D offsets i + sj*j of the boundary columns in
+// the reference's sweep order (j outer, i inner), ncols of them.
+cudaError_t launch_null_gradient(int ni, int nj, int nk, double* P, const int* CFU, const int* CFV,
+                                 const int* KFloor, const int* cols, int ncols, cudaStream_t s);
+// rows: the i of the rows whose ends j = 1 and j = nj are both boundary points
+// (i = 2..ni-1, in order), then the j of the columns whose ends i = 1 and
+// i = ni are (j = 2..nj-1); nrows + ncyc entries.
+cudaError_t launch_cyclic(int ni, int nj, int nk, double* P, const double* Ref, const int* KFloor,
+                          const int* cols, int ncols, const int* rows, int nrows, int ncyc, cudaStream_t s);
 
 }  // namespace mohid

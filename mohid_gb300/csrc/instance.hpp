@@ -41,6 +41,10 @@ struct Instance {
     // static 2-D metrics
     DevBuf<double> DUX, DVY, DZX, DZY;
     DevBuf<int> KFloor, BP2D;
+    // boundary columns (2-D offsets, the reference's sweep order) and the rows
+    // and columns whose two ends are boundary points (cyclic boundaries)
+    DevBuf<int> bcols, cycl;
+    int nbcols = 0, nrows = 0, ncyc = 0;
     // per-step hydrodynamics
     DevBuf<double> Qx, Qy, Qz, Vold, V, ViscH, DiffV, AreaU, AreaV, DZZ, DWZ;
     DevBuf<int> OP, LP, WP, CFU, CFV, CFW, SD;

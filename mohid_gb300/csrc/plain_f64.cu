@@ -19,6 +19,9 @@
 //   OpenBoundaryCondition           AD:5369-5742
 //   land -> null_real               AD:1753
 //   THOMASZ_NewType2                FN:4026-4123
+// then, for NullGradient and Cyclic boundaries, the post-solve passes
+//   ImposeNullGradient              AD:1926-1987
+//   Prop_CyclicBoundary             AD:2121-2224
 #include "common.cuh"
 
 namespace mohid {
@@ -108,6 +111,20 @@ __device__ __forceinline__ void face_coef(double Q, double dt, double VRM, int m
         Theta = 0.5 * Theta * (1. - Cr);
     }
     for (int n = 0; n < 4; ++n) CF[n] = (1. - Theta) * Cup1[n] + Theta * CH[n];
+}
+
+// NullGradProp (AD:2071-2110): the mean of the four neighbours of cell `a`
+// across compute faces (V faces i, i+1; U faces j, j+1).  Plain loads: the
+// post-solve pass reads values it wrote itself.
+__device__ __forceinline__ bool null_grad(const double* P, const int* CFU, const int* CFV, size_t a,
+                                          long long sj, double& out)
+{
+    const int cv1 = CFV[a + 1], cv0 = CFV[a], cu1 = CFU[a + sj], cu0 = CFU[a];
+    const int Aux = cv1 + cv0 + cu1 + cu0;
+    if (Aux <= 0) return false;
+    out = (P[a + 1] * (double)cv1 + P[a - 1] * (double)cv0 + P[a + sj] * (double)cu1 +
+           P[a - sj] * (double)cu0) / (double)Aux;
+    return true;
 }
 
 // Explicit advective flux through the face between cells `m` (= a - s) and `a`
@@ -345,7 +362,7 @@ plain_f64_kernel(const PlainArgs A)
         if (bp && k >= kbp && opk == 1) {
             double DT_V = DT / Vk;
             const double Rf = __ldg(A.Ref + a);
-            if (A.bc == 1) {
+            if (A.bc == 1 || A.bc == 7) {         // MassConservation, MassConservNullGrad
                 double WF = __ldg(A.Qx + a) * (double)__ldg(A.CFU + a) -
                             __ldg(A.Qx + a + sj) * (double)__ldg(A.CFU + a + sj) +
                             __ldg(A.Qy + a) * (double)__ldg(A.CFV + a) -
@@ -353,9 +370,19 @@ plain_f64_kernel(const PlainArgs A)
                             __ldg(A.Qz + a) * (double)__ldg(A.CFW + a) -
                             __ldg(A.Qz + a + sk) * (double)__ldg(A.CFW + a + sk) -
                             (Vk - __ldg(A.Vold + a)) / DT;
-                double Ext = Pk * (1.0 - A.tdecAux) + Rf * A.tdecAux;
-                if (WF < 0.0) TI = TI - WF * Ext * DT_V;
-                else E = E + WF * DT_V;
+                if (A.bc == 1) {
+                    double Ext = Pk * (1.0 - A.tdecAux) + Rf * A.tdecAux;
+                    if (WF < 0.0) TI = TI - WF * Ext * DT_V;
+                    else E = E + WF * DT_V;
+                } else if (WF < 0.0) {            // inflow: interior mean of the old field
+                    double g;
+                    TI = null_grad(P, A.CFU, A.CFV, a, sj, g) ? g : Pk;
+                    D = 0.0; E = 1.0; F = 0.0;
+                } else {
+                    E = E + WF * DT_V;
+                }
+            } else if (A.bc == 4 || A.bc == 8) {  // NullGradient / Cyclic: set after the solve
+                TI = Pk; D = 0.0; E = 1.0; F = 0.0;
             } else {                              // ImposedValue / SubModel
                 double A1 = (double)(__ldg(A.OP + a + 1) * (1 - __ldg(A.BP2D + c + 1)));
                 double A2 = (double)(__ldg(A.OP + a - 1) * (1 - __ldg(A.BP2D + c - 1)));
@@ -480,7 +507,84 @@ __global__ void check_faces_kernel(int ni, int nj, int nk, const int* __restrict
     if (bad) atomicOr(status, MOHID_DEV_BAD_FACE);
 }
 
+// ImposeNullGradient (AD:1926-1987).  The reference sweeps the boundary
+// columns in order and a cell reads the new values of the boundary cells
+// swept before it, so each layer is one sequential sweep: thread k walks the
+// column list at layer k (layers never mix).
+__global__ void null_gradient_kernel(int nk, long long sj, long long sk, double* P, const int* __restrict__ CFU,
+                                     const int* __restrict__ CFV, const int* __restrict__ KFloor,
+                                     const int* __restrict__ cols, int ncols)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > nk) return;
+    for (int q = 0; q < ncols; ++q) {
+        const size_t c = (size_t)cols[q];
+        const int kf = KFloor[c];
+        if (k < (kf < 0 ? -kf : kf)) continue;
+        const size_t a = c + (size_t)sk * k;
+        double g;
+        if (null_grad(P, CFU, CFV, a, sj, g)) P[a] = g;
+    }
+}
+
+// Prop_CyclicBoundary (AD:2121-2224), first part: boundary columns take the
+// reference at k = 1..KUB (cell (q, k) of the column list per thread)
+__global__ void cyclic_ref_kernel(int nk, long long sk, double* P, const double* __restrict__ Ref,
+                                  const int* __restrict__ cols, int ncols)
+{
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)ncols * nk) return;
+    const size_t a = (size_t)cols[e / nk] + (size_t)sk * (size_t)(1 + e % nk);
+    P[a] = Ref[a];
+}
+
+// second part: rows i (ends j = 1, nj) copy the interior next to the opposite
+// end, then columns j (ends i = 1, ni); from KFloorZ as stored (a negative
+// value starts at the box's lower layer), in the reference's order; thread k
+// does layer k
+__global__ void cyclic_copy_kernel(int ni, int nj, int nk, long long sj, long long sk, double* P,
+                                   const int* __restrict__ KFloor, const int* __restrict__ rows, int nrows,
+                                   int ncyc)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > nk) return;
+    auto from = [&](int i, int j) { const int kf = KFloor[(size_t)i + (size_t)sj * j]; return kf < 0 ? 0 : kf; };
+    auto at = [&](int i, int j) { return (size_t)i + (size_t)sj * j + (size_t)sk * k; };
+    for (int q = 0; q < nrows; ++q) {
+        const int i = rows[q];
+        if (k >= from(i, nj - 1)) P[at(i, 1)] = P[at(i, nj - 1)];
+        if (k >= from(i, 2)) P[at(i, nj)] = P[at(i, 2)];
+    }
+    for (int q = nrows; q < nrows + ncyc; ++q) {
+        const int j = rows[q];
+        if (k >= from(ni - 1, j)) P[at(1, j)] = P[at(ni - 1, j)];
+        if (k >= from(2, j)) P[at(ni, j)] = P[at(2, j)];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_null_gradient(int ni, int nj, int nk, double* P, const int* CFU, const int* CFV,
+                                 const int* KFloor, const int* cols, int ncols, cudaStream_t s)
+{
+    if (ncols <= 0) return cudaSuccess;
+    const long long sj = ni + 2, sk = (long long)(ni + 2) * (nj + 2);
+    null_gradient_kernel<<<(nk + 1 + 63) / 64, 64, 0, s>>>(nk, sj, sk, P, CFU, CFV, KFloor, cols, ncols);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cyclic(int ni, int nj, int nk, double* P, const double* Ref, const int* KFloor,
+                          const int* cols, int ncols, const int* rows, int nrows, int ncyc, cudaStream_t s)
+{
+    const long long sj = ni + 2, sk = (long long)(ni + 2) * (nj + 2);
+    if (ncols > 0) {
+        const long long n = (long long)ncols * nk;
+        cyclic_ref_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(nk, sk, P, Ref, cols, ncols);
+    }
+    if (nrows + ncyc > 0)
+        cyclic_copy_kernel<<<(nk + 1 + 63) / 64, 64, 0, s>>>(ni, nj, nk, sj, sk, P, KFloor, rows, nrows, ncyc);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s)
 {

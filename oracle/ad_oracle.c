@@ -202,12 +202,15 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     if ((mV >= 2 && mV <= 4) && !p->Upwind2V) return MOHID_AD_ERR_OPTION;
     if (mH == MOHID_P2_TVD && (p->TVDLimitationH < 1 || p->TVDLimitationH > 5)) return MOHID_AD_ERR_OPTION;
     if (mV == MOHID_P2_TVD && (p->TVDLimitationV < 1 || p->TVDLimitationV > 5)) return MOHID_AD_ERR_OPTION;
-    if (ReferenceProp) {
+    {
         int bc = p->BoundaryCondition;
-        if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8)
-            return MOHID_AD_ERR_OPTION;              /* Set_Internal_State ERR01, AD:5816-5830 */
-        if (bc != MOHID_BC_MASS_CONSERVATION && bc != MOHID_BC_IMPOSED_VALUE && bc != MOHID_BC_SUBMODEL)
-            return MOHID_AD_ERR_UNSUPPORTED;
+        if (ReferenceProp) {
+            if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8)
+                return MOHID_AD_ERR_OPTION;          /* Set_Internal_State ERR01, AD:5816-5830 */
+            if (bc == MOHID_BC_ORLANSKI) return MOHID_AD_ERR_UNSUPPORTED;
+        } else if (bc == MOHID_BC_CYCLIC) {
+            return MOHID_AD_ERR_OPTION;              /* Prop_CyclicBoundary reads ReferenceProp, AD:2150 */
+        }
     }
     /* lower-edge faces must be closed (see header) */
     ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
@@ -263,6 +266,64 @@ static void fill3(ora_ext X, double* a, double v)
     for (int k = 0; k < X.NK; ++k) {
         double* s = a + (size_t)k * X.n2;
         for (size_t q = 0; q < X.n2; ++q) s[q] = v;
+    }
+}
+
+/* NullGradProp, AD:2071-2110: the mean of the four neighbours across compute
+ * faces (V faces i, i+1; U faces j, j+1); 0 when the cell has none. */
+static int null_grad_prop(const ora_domain* d, const double* P, int i, int j, int k, double* out)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    const int *CFU = d->ComputeFacesU3D, *CFV = d->ComputeFacesV3D;
+    int Aux = CFV[I3(i + 1, j, k)] + CFV[I3(i, j, k)] + CFU[I3(i, j + 1, k)] + CFU[I3(i, j, k)];
+    if (Aux <= 0) return 0;
+    *out = (P[I3(i + 1, j, k)] * (double)CFV[I3(i + 1, j, k)] + P[I3(i - 1, j, k)] * (double)CFV[I3(i, j, k)] +
+            P[I3(i, j + 1, k)] * (double)CFU[I3(i, j + 1, k)] + P[I3(i, j - 1, k)] * (double)CFU[I3(i, j, k)]) /
+           (double)Aux;
+    return 1;
+}
+
+/* ImposeNullGradient, AD:1926-1987: in place after the solve, boundary
+ * columns in the reference's order (j, i, k from |KFloorZ| to KUB), so a cell
+ * reads the new values of boundary neighbours set before it. */
+static void impose_null_gradient(const ora_domain* d, double* P)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    for (int j = 1; j <= d->nj; ++j)
+        for (int i = 1; i <= d->ni; ++i) {
+            if (d->BoundaryPoints2D[I2(i, j)] != 1) continue;
+            for (int k = abs(d->KFloorZ[I2(i, j)]); k <= d->nk; ++k) {
+                double v;
+                if (null_grad_prop(d, P, i, j, k, &v)) P[I3(i, j, k)] = v;
+            }
+        }
+}
+
+/* Prop_CyclicBoundary, AD:2121-2224: boundary columns take the reference
+ * (k = 1..KUB), then a row (column) whose two ends are boundary points copies
+ * the interior values next to the opposite end, from that column's KFloorZ. */
+/* the reference loops from KFloorZ as stored; a negative KFloorZ would index
+ * below the Size box there, here the loop starts at the box's lower layer */
+static inline int kfloor_clamp(int kf) { return kf < 0 ? 0 : kf; }
+
+static void cyclic_boundary(const ora_domain* d, double* P, const double* Ref)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    const int ni = d->ni, nj = d->nj, nk = d->nk;
+    const int* BP = d->BoundaryPoints2D;
+    for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i)
+            if (BP[I2(i, j)] == 1)
+                for (int k = 1; k <= nk; ++k) P[I3(i, j, k)] = Ref[I3(i, j, k)];
+    for (int i = 2; i <= ni - 1; ++i) {
+        if (BP[I2(i, 1)] != 1 || BP[I2(i, nj)] != 1) continue;
+        for (int k = kfloor_clamp(d->KFloorZ[I2(i, nj - 1)]); k <= nk; ++k) P[I3(i, 1, k)] = P[I3(i, nj - 1, k)];
+        for (int k = kfloor_clamp(d->KFloorZ[I2(i, 2)]); k <= nk; ++k) P[I3(i, nj, k)] = P[I3(i, 2, k)];
+    }
+    for (int j = 2; j <= nj - 1; ++j) {
+        if (BP[I2(1, j)] != 1 || BP[I2(ni, j)] != 1) continue;
+        for (int k = kfloor_clamp(d->KFloorZ[I2(ni - 1, j)]); k <= nk; ++k) P[I3(1, j, k)] = P[I3(ni - 1, j, k)];
+        for (int k = kfloor_clamp(d->KFloorZ[I2(2, j)]); k <= nk; ++k) P[I3(ni, j, k)] = P[I3(2, j, k)];
     }
 }
 
@@ -564,7 +625,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
          * AD:5680-5742 (OMP DO j / do i / do k). */
         const int bc = p->BoundaryCondition;
         const double TdecAux = 1.0 / (1.0 + p->DecayTime / DT);
-        if (bc == MOHID_BC_MASS_CONSERVATION) {
+        if (bc == MOHID_BC_MASS_CONSERVATION || bc == MOHID_BC_MASS_CONSERV_NULLGRAD) {
             #pragma omp parallel for schedule(dynamic, 1)
             for (int j = 1; j <= nj; ++j)
                 for (int i = 1; i <= ni; ++i)
@@ -607,6 +668,21 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                         w.TI[a] = Ext;
                         w.D[a] = 0.0; w.E[a] = 1.0; w.F[a] = 0.0;
+                    } else if (bc == MOHID_BC_NULL_GRADIENT || bc == MOHID_BC_CYCLIC) {
+                        /* AD:5645-5650: the row keeps the old value; the
+                         * boundary is set after the solve */
+                        w.TI[a] = P[a];
+                        w.D[a] = 0.0; w.E[a] = 1.0; w.F[a] = 0.0;
+                    } else if (bc == MOHID_BC_MASS_CONSERV_NULLGRAD) {
+                        /* AD:5603-5631: inflow takes the interior mean across
+                         * compute faces (old values), outflow leaves implicitly */
+                        if (w.WFOB[a] < 0.0) {
+                            double bprop;
+                            w.TI[a] = null_grad_prop(d, P, i, j, k, &bprop) ? bprop : P[a];
+                            w.E[a] = 1.0; w.D[a] = 0.0; w.F[a] = 0.0;
+                        } else {
+                            w.E[a] = w.E[a] + w.WFOB[a] * DT_V;
+                        }
                     } else { /* MassConservation */
                         double Int = P[a];
                         Ext = Int * (1.0 - TdecAux) + ReferenceProp[a] * TdecAux;
@@ -624,6 +700,9 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
             if (d->LandPoints3D[q] == 1) w.TI[q] = NULL_REAL;
 
     st = ora_thomasz(ni, nj, nk, w.D, w.E, w.F, w.TI, PROP, d->WaterPoints3D);
+    /* AD:1874-1880: whether or not a reference is given */
+    if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT) impose_null_gradient(d, PROP);
+    else if (p->BoundaryCondition == MOHID_BC_CYCLIC) cyclic_boundary(d, PROP, ReferenceProp);
     ora_work_free(own);
     return st;
 fail:

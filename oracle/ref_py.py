@@ -112,6 +112,15 @@ def face(P, V, du, dt, Q, vrm, method, limiter, nb, up2):
     return [(1.0 - theta) * cup1[n] + theta * high[n] for n in range(4)]
 
 
+def _null_grad(Pl, CU, CV, k, j, i):
+    """NullGradProp (AD:2071-2110): mean of the neighbours across compute faces, or None."""
+    aux = CV[k][j][i + 1] + CV[k][j][i] + CU[k][j + 1][i] + CU[k][j][i]
+    if aux <= 0:
+        return None
+    return (Pl[k][j][i + 1] * CV[k][j][i + 1] + Pl[k][j][i - 1] * CV[k][j][i] +
+            Pl[k][j + 1][i] * CU[k][j + 1][i] + Pl[k][j - 1][i] * CU[k][j][i]) / float(aux)
+
+
 def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
     `p` is a dict of AdvectionDiffusion scalar arguments."""
@@ -319,6 +328,20 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                             ext = R[k][j][i]
                         TI[k][j][i] = ext
                         D[k][j][i], E[k][j][i], F[k][j][i] = 0.0, 1.0, 0.0
+                    elif bc in (4, 8):                 # AD:5645-5650
+                        TI[k][j][i] = Pl[k][j][i]
+                        D[k][j][i], E[k][j][i], F[k][j][i] = 0.0, 1.0, 0.0
+                    elif bc == 7:                      # AD:5603-5631
+                        wf = Qx[k][j][i] * CU[k][j][i] - Qx[k][j + 1][i] * CU[k][j + 1][i] + \
+                            Qy[k][j][i] * CV[k][j][i] - Qy[k][j][i + 1] * CV[k][j][i + 1] + \
+                            Qz[k][j][i] * CW[k][j][i] - Qz[k + 1][j][i] * CW[k + 1][j][i] - \
+                            (V[k][j][i] - Vo[k][j][i]) / DT
+                        if wf < 0.0:
+                            g = _null_grad(Pl, CU, CV, k, j, i)
+                            TI[k][j][i] = Pl[k][j][i] if g is None else g
+                            D[k][j][i], E[k][j][i], F[k][j][i] = 0.0, 1.0, 0.0
+                        else:
+                            E[k][j][i] = E[k][j][i] + wf * dtv
                     else:
                         wf = Qx[k][j][i] * CU[k][j][i] - Qx[k][j + 1][i] * CU[k][j + 1][i] + \
                             Qy[k][j][i] * CV[k][j][i] - Qy[k][j][i + 1] * CV[k][j][i + 1] + \
@@ -356,4 +379,33 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
             Pl[nk + 1][j][i] = G[nk + 1]
             for k in range(nk, 0, -1):
                 Pl[k][j][i] = W[k] * Pl[k + 1][j][i] + G[k]
+
+    # boundary conditions applied after the solve (AD:1874-1880)
+    if p["BoundaryCondition"] == 4:                  # ImposeNullGradient AD:1926-1987
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if BP[j][i] != 1:
+                    continue
+                for k in range(abs(KF[j][i]), nk + 1):
+                    g = _null_grad(Pl, CU, CV, k, j, i)
+                    if g is not None:
+                        Pl[k][j][i] = g
+    elif p["BoundaryCondition"] == 8:                # Prop_CyclicBoundary AD:2121-2224
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if BP[j][i] == 1:
+                    for k in range(1, nk + 1):
+                        Pl[k][j][i] = R[k][j][i]
+        for i in range(2, ni):
+            if BP[1][i] == 1 and BP[nj][i] == 1:
+                for k in range(max(KF[nj - 1][i], 0), nk + 1):
+                    Pl[k][1][i] = Pl[k][nj - 1][i]
+                for k in range(max(KF[2][i], 0), nk + 1):
+                    Pl[k][nj][i] = Pl[k][2][i]
+        for j in range(2, nj):
+            if BP[j][1] == 1 and BP[j][ni] == 1:
+                for k in range(max(KF[j][ni - 1], 0), nk + 1):
+                    Pl[k][j][1] = Pl[k][j][ni - 1]
+                for k in range(max(KF[j][2], 0), nk + 1):
+                    Pl[k][j][ni] = Pl[k][j][2]
     P[...] = Pl

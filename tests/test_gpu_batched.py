@@ -149,7 +149,8 @@ def test_batched_mass_budget_matches_oracle_sum(gpu):
 
 
 @pytest.mark.parametrize("bad", [dict(AdvMethodH=5), dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1),
-                                 dict(ImpExp_DifV=0.5), dict(Docycle_method=2), dict(ImpExp_AdvV=0.0)])
+                                 dict(ImpExp_DifV=0.5), dict(Docycle_method=2), dict(ImpExp_AdvV=0.0),
+                                 dict(BoundaryCondition=4), dict(BoundaryCondition=8)])
 def test_batched_rejects_unsupported(gpu, bad):
     d = domain("coast")
     ad = advdiff.AdvectionDiffusion(d)

@@ -46,7 +46,8 @@ def test_gpu_matches_oracle_one_step(gpu, grid, opt):
 
 
 @pytest.mark.parametrize("grid", ["open", "nsopen"])
-@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0)])
+@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0), (4, 0.0), (7, 0.0),
+                                      (8, 0.0)])
 @pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod", "tvd_superbee"])
 def test_gpu_open_boundaries(gpu, grid, bc, decay, opt):
     d = domain(grid)
@@ -62,6 +63,55 @@ def test_gpu_open_boundaries(gpu, grid, bc, decay, opt):
     ad.kill()
     _compare(d, Pg, Po)
     assert np.array_equal(Pg, Po)
+
+
+@pytest.mark.parametrize("bc", [4, 7, 8])
+@pytest.mark.parametrize("with_ref", [True, False])
+def test_gpu_boundary_sweeps_many_steps(gpu, bc, with_ref):
+    # all four sides open (cyclic rows and columns, corners), a few steps on
+    # the host and the device entry points: the post-solve sweeps in the
+    # reference's order, bit for bit
+    if bc in (7, 8) and not with_ref:
+        pytest.skip("needs the reference")
+    d = synth.generate(synth.GenSpec(ni=61, nj=47, nk=7, land_frac=0.1, land_kind=1, seed=13, open_sides=15,
+                                     bathy_kind=1, dt=30.0))
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2) if with_ref else None
+    pd = dict(DTProp=30.0, BoundaryCondition=bc, **OPTIONS["tvd_superbee"])
+    Po = P0.copy()
+    for _ in range(4):
+        assert O.step(d, Po, O.params(**pd), ReferenceProp=R) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    for _ in range(4):
+        ad.step(Pg, advdiff.params(**pd), R)
+    assert np.array_equal(Pg, Po)
+    import torch
+    a = torch.from_numpy(P0.copy()).cuda()
+    b = torch.empty_like(a)
+    Rd = torch.from_numpy(R).cuda() if with_ref else None
+    for _ in range(4):
+        ad.step_device(a, b, advdiff.params(**pd), Rd)
+        a, b = b, a
+    ad.sync()
+    ad.kill()
+    assert np.array_equal(a.cpu().numpy(), Po)
+
+
+def test_gpu_boundary_condition_rules(gpu):
+    d = domain("open")
+    P = d.tracer(4, 1.0, 0.0, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    for pd, ref, code in [(dict(BoundaryCondition=8), None, 3), (dict(BoundaryCondition=6), R, 4),
+                          (dict(BoundaryCondition=3), R, 3)]:
+        assert O.step(d, P.copy(), O.params(DTProp=30.0, **pd), ReferenceProp=ref) == code
+        with pytest.raises(advdiff.N.MohidAdError) as ei:
+            ad.step(P.copy(), advdiff.params(DTProp=30.0, **pd), ref)
+        assert ei.value.code == code
+    ad.kill()
 
 
 def test_gpu_small_depths(gpu):

@@ -19,7 +19,8 @@ def test_c_oracle_equals_python_restatement(built, grid, opt):
 
 
 @pytest.mark.parametrize("grid", ["open", "nsopen"])
-@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0)])
+@pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0), (4, 0.0), (7, 0.0),
+                                      (8, 0.0)])
 @pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod"])
 def test_open_boundaries_c_equals_python(built, grid, bc, decay, opt):
     d = domain(grid)
@@ -30,6 +31,21 @@ def test_open_boundaries_c_equals_python(built, grid, bc, decay, opt):
     assert O.step(d, Pc, O.params(**pd), ReferenceProp=R) == 0
     ref_py.step(d, Pp, pd, ReferenceProp=R)
     assert np.array_equal(Pc, Pp)
+
+
+@pytest.mark.parametrize("grid", ["open", "nsopen"])
+def test_null_gradient_without_reference_c_equals_python(built, grid):
+    # ImposeNullGradient runs after the solve whether or not a reference is given (AD:1874-1876)
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=3)
+    pd = dict(O.DEFAULTS, DTProp=30.0, BoundaryCondition=4, **OPTIONS["tvd_minmod"])
+    Pc, Pp = P0.copy(), P0.copy()
+    assert O.step(d, Pc, O.params(**pd)) == 0
+    ref_py.step(d, Pp, pd)
+    assert np.array_equal(Pc, Pp)
+    Q = P0.copy()
+    assert O.step(d, Q, O.params(**dict(pd, BoundaryCondition=1))) == 0
+    assert not np.array_equal(Pc, Q)                 # the boundary columns changed
 
 
 def test_small_depths_c_equals_python(built):

@@ -49,12 +49,15 @@ def test_thomasz_zero_pivot_reported(built):
 @pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "nsopen"])
 @pytest.mark.parametrize("opt", [dict(), dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
                                  dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1)])
-def test_constancy_preserved(built, grid, opt):
+@pytest.mark.parametrize("bc", [1, 2, 4, 7, 8])
+def test_constancy_preserved(built, grid, opt, bc):
     d = domain(grid)
     wp = d.water_mask()
     P = np.where(wp, 3.25, 0.0)
     R = np.full(d.shape3, 3.25) if d.spec.open_sides else None
-    p = O.params(DTProp=30.0, **opt)
+    if R is None and bc == 8:
+        pytest.skip("cyclic boundaries read the reference")
+    p = O.params(DTProp=30.0, BoundaryCondition=bc, **opt)
     for _ in range(5):
         assert O.step(d, P, p, ReferenceProp=R) == 0
     assert np.max(np.abs(P[wp] - 3.25)) < 1e-12
@@ -190,6 +193,63 @@ def test_rejected_options(built, bad, code):
     P0 = P.copy()
     assert O.step(d, P, O.params(DTProp=30.0, **bad)) == code
     assert np.array_equal(P, P0)
+
+
+def test_boundary_condition_rules(built):
+    d = domain("open")
+    P = d.tracer(4, 1.0, 0.0, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    # cyclic boundaries read the reference (AD:2150); Orlanski is not built
+    assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=8)) == 3
+    assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=6), ReferenceProp=R) == 4
+    assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=3), ReferenceProp=R) == 3
+    # without a reference a BC other than 4 and 8 changes nothing (AD:1874-1880, AD:5816)
+    a, b = P.copy(), P.copy()
+    assert O.step(d, a, O.params(DTProp=30.0, BoundaryCondition=6)) == 0
+    assert O.step(d, b, O.params(DTProp=30.0, BoundaryCondition=1)) == 0
+    assert np.array_equal(a, b)
+
+
+def test_null_gradient_sets_boundary_to_neighbour_mean(built):
+    # the solve as without open boundaries, then every boundary cell with a
+    # compute face takes the mean of its neighbours across compute faces, swept
+    # in the reference's order (a cell sees the new values of the boundary
+    # cells swept before it)
+    d = domain("nsopen")
+    P = d.tracer(3, 1.0, 0.5, seed=4)
+    X = P.copy()
+    assert O.step(d, P, O.params(DTProp=30.0, BoundaryCondition=4)) == 0
+    assert O.step(d, X, O.params(DTProp=30.0, BoundaryCondition=1)) == 0
+    a = d.arrays
+    CU, CV, BP, KF = a["ComputeFacesU3D"], a["ComputeFacesV3D"], a["BoundaryPoints2D"], a["KFloorZ"]
+    n = 0
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            if BP[j, i] != 1:
+                continue
+            for k in range(abs(KF[j, i]), d.nk + 1):
+                aux = CV[k, j, i + 1] + CV[k, j, i] + CU[k, j + 1, i] + CU[k, j, i]
+                if aux > 0:
+                    X[k, j, i] = (X[k, j, i + 1] * CV[k, j, i + 1] + X[k, j, i - 1] * CV[k, j, i] +
+                                  X[k, j + 1, i] * CU[k, j + 1, i] + X[k, j - 1, i] * CU[k, j, i]) / aux
+                    n += 1
+    assert n > 0
+    assert np.array_equal(P, X)
+
+
+def test_cyclic_boundary_copies_opposite_interior(built):
+    d = domain("nsopen")                                  # boundary rows i = 1 and i = ni
+    P = d.tracer(3, 1.0, 0.5, seed=4)
+    R = d.reference(2.0, 0.3, seed=5)
+    assert O.step(d, P, O.params(DTProp=30.0, BoundaryCondition=8), ReferenceProp=R) == 0
+    KF = d.arrays["KFloorZ"]
+    for j in range(2, d.nj):
+        for k in range(KF[j, d.ni - 1], d.nk + 1):
+            assert P[k, j, 1] == P[k, j, d.ni - 1]
+        for k in range(KF[j, 2], d.nk + 1):
+            assert P[k, j, d.ni] == P[k, j, 2]
+    # the corner columns keep the reference
+    assert np.array_equal(P[1:d.nk + 1, 1, 1], R[1:d.nk + 1, 1, 1])
 
 
 def test_compute_face_on_lower_edge_rejected(built):
