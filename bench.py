@@ -484,15 +484,19 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
     nt = cases[0].nt
     defects = mass_defects(objs, cases)
     if ensemble:
-        # one ensemble launch, the boundary flux of each open member and the
-        # mass fixer's finish (every ensemble workload here has static volumes)
-        per = 1 + sum(1 for c in cases if c.refs is not None) + 1
-        launches = steps * per
-        sched = {"launches": per, "sched": "persistent tile list (ensemble)", "split": nt}
+        # per step one ensemble launch, with open members their boundary flux
+        # and the mass fixer's finish; on closed members the finish runs once
+        # after the timed call's last step (every ensemble workload here has
+        # static volumes)
+        nopen = sum(1 for c in cases if c.refs is not None)
+        per = 1 + nopen + (1 if nopen else 0)
+        per_call = 0 if nopen else 1
+        launches = steps * per + per_call
+        sched = {"launches": per, "per_call": per_call, "sched": "persistent tile list (ensemble)", "split": nt}
         groups = [min(nt, 4)]
     else:
         sched = objs[0][1].schedule()              # as chosen by the autotuner
-        launches = steps * sched["launches"]
+        launches = steps * sched["launches"] + sched["per_call"]   # one timed call
         groups = tracer_groups(nt, sched["split"])
 
     e2e_s = h2d = d2h = None

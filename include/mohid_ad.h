@@ -296,10 +296,13 @@ int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* sta
 /* Set the schedule by hand (*sched 0 or 1, *split 8, 4 or 2) instead of the autotuner. */
 int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat);
 
-/* The schedule in use: kernel launches per step (including the mass fixer's),
- * schedule (0 one CTA per tile, 1 tile list), largest tracer group per launch.
- * Any output pointer may be NULL. */
-int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* stat);
+/* The schedule in use: kernel launches per step (the step kernels, and with
+ * open boundaries the boundary flux and the mass fixer's finish), schedule (0
+ * one CTA per tile, 1 tile list), largest tracer group per launch, and
+ * launches made once per mohid_ad_batched_step call (the mass fixer's finish on
+ * closed domains, which runs after the call's last step only).  Any output
+ * pointer may be NULL. */
+int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call, int* stat);
 
 /* Mass fixer (*on != 0, the default).  No counterpart in the reference, whose
  * FP64 arithmetic conserves mass to round-off; it restores that for the FP32

@@ -98,7 +98,7 @@ _AD_SIGS = {
     "mohid_ad_batched_boundary_flux": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
     "mohid_ad_batched_set_mass_fix": (C.c_int, [c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_autotune": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p]),
-    "mohid_ad_batched_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_set_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_sync": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_batched_destroy": (C.c_int, [c_int_p, c_int_p]),

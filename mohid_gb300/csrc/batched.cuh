@@ -168,8 +168,9 @@ cudaError_t vol_changed(const double* Vnew, double* Vprev, long long n, unsigned
 cudaError_t fp16_scales(const double* const* fields, int nf, long long n, double* absmax, float* scale, float* inv,
                         cudaStream_t s);
 // after a step: target[t] += the step's boundary flux (obpart != null, nob
-// blocks), then correction[t] += (target[t] - mass now) / volume for every
-// tracer of the batch whose target is set
+// blocks), then, with the step's tile sums (mpart != null),
+// correction[t] += (target[t] - mass now) / volume, for every tracer of the
+// batch whose target is set
 cudaError_t mass_fix_step(const double* mpart, int ntiles, int nt, double* mfix, const double* obpart, int nob,
                           cudaStream_t s);
 // targets and boundary fluxes of every tracer dropped (NaN): a step with open
@@ -183,7 +184,8 @@ cudaError_t obc_columns(const uint8_t* cflag, const BLayout& L, int* cnt, int* l
 // mass fixer: a covers every tracer of the batch (t0 = 0) with the step's input
 // and output buffers; partials to a.obpart (a.nob = kObcBlocks blocks).
 cudaError_t obc_flux(const BatchArgs& a, const int* list, bool halfQ, cudaStream_t s);
-// the same for `nb` batches whose argument records (device) have mpart != null
+// the same for `nb` batches from their argument records (device): mpart and
+// obpart of each record select what runs for that batch
 cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,

@@ -67,6 +67,7 @@ struct Batch {
     bool tuned = false;
     int graphSched = -1, graphSplit = -1;
     int graphFix = -1;                   // fixer / open-boundary launches the graph holds
+    bool graphLast = false;              // the graph ends with the call's last step
     // asynchronous repack of a new hydrodynamic state (on the instance's
     // stream) and tracer loads (on their own stream, with their own scratch),
     // so that the two overlap; the host-side results of the repack are read
@@ -402,7 +403,9 @@ int ensure_packed(Batch* b, int* stat)
     return pack_finalize(b, stat);
 }
 
-mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout)
+// sums: the launch accumulates the mass fixer's per-tile sums (when the fixer runs)
+mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout,
+                            bool sums = true)
 {
     Instance* in = b->in;
     mohid::BatchArgs a;
@@ -431,7 +434,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Vhi = b->Vhi.p;
     a.Vlo = b->Vlo.p;
     a.mfix = b->mfix.p;
-    a.mpart = fix_active(b) ? b->mpart.p : nullptr;
+    a.mpart = sums && fix_active(b) ? b->mpart.p : nullptr;
     a.obpart = fix_active(b) && b->hasRef ? b->obpart.p : nullptr;
     a.nob = mohid::kObcBlocks;
     a.tilesX = b->tilesX;
@@ -504,23 +507,37 @@ int launches_per_step(const Batch* b)
 {
     int n = 0;
     for (int left = b->nt; left > 0; left -= group_size(b, left)) ++n;
-    if (fix_active(b)) n += b->hasRef ? 2 : 1;       // boundary flux, fixer
+    if (fix_active(b) && b->hasRef) n += 2;          // boundary flux, fixer
     else if (b->hasRef) n += 1;                      // targets dropped
     return n;
 }
 
-// one transport step of every tracer.  real == false (the autotuner): the step
+// launches made once per step call: the closed-domain fixer's finish
+int launches_per_call(const Batch* b)
+{
+    return fix_active(b) && !b->hasRef ? 1 : 0;
+}
+
+// One transport step of every tracer.  real == false (the autotuner): the step
 // writes the other buffer and the scratch only -- no mass-fixer update, no
 // parity flip -- so the tracer state is unchanged.
-cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, bool real = true)
+// last: the final step of a step call.  The correction to the tracers'
+// constant is held during a call: the stored anomalies evolve independently of
+// it on closed domains, and with open boundaries the reference is shifted by
+// the same held value.  The correction that brings the mass to its target then
+// depends only on the anomalies' sum after the last step, so only that step
+// accumulates the sums and corrects.  With open boundaries the target follows
+// every step's boundary flux (with the held correction).
+cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, bool real = true, bool last = true)
 {
+    const bool sums = last;
     const float* Pin = b->cur_in();
     float* Pout = b->cur_out();
     const int2* tiles = (b->sched == 1 && b->ntl > 0) ? b->tl.p : nullptr;
     int t0 = 0;
     while (t0 < b->nt) {
         const int g = group_size(b, b->nt - t0);
-        mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout);
+        mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout, sums);
         mohid::TmaMaps m = b->maps;
         m.P = b->mapP[b->cur ? 1 : 0][map_index(g)];
         cudaError_t e = mohid::launch_batched(a, m, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
@@ -529,15 +546,15 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
         t0 += g;
     }
     if (!real) return cudaSuccess;
-    if (fix_active(b)) {
+    if (fix_active(b) && (sums || b->hasRef)) {
         cudaError_t e = cudaSuccess;
         if (b->hasRef)                           // the target follows the boundary flux
             e = mohid::obc_flux(make_bargs(b, p, 0, b->nt, Pin, Pout), b->obcol.p, b->storage >= 1, s);
         if (e == cudaSuccess)
-            e = mohid::mass_fix_step(b->mpart.p, b->ntiles, b->nt, b->mfix.p, b->hasRef ? b->obpart.p : nullptr,
-                                     mohid::kObcBlocks, s);
+            e = mohid::mass_fix_step(sums ? b->mpart.p : nullptr, b->ntiles, b->nt, b->mfix.p,
+                                     b->hasRef ? b->obpart.p : nullptr, mohid::kObcBlocks, s);
         if (e != cudaSuccess) return e;
-    } else if (b->hasRef) {
+    } else if (!fix_active(b) && b->hasRef) {
         // a boundary flux the targets did not follow: they no longer apply
         cudaError_t e = mohid::mass_fix_drop(b->mfix.p, b->nt, s);
         if (e != cudaSuccess) return e;
@@ -565,9 +582,9 @@ int autotune(Batch* b, const mohid_ad_params* p, int* stat)
             if (sched == 1 && b->ntl == 0) continue;
             b->sched = sched;
             b->split = split;
-            err = enqueue_step(b, p, s, false);
+            err = enqueue_step(b, p, s, false, false);
             if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-            for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false);
+            for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false, false);
             if (err == cudaSuccess) err = cudaEventRecord(e1, s);
             if (err == cudaSuccess) err = cudaEventSynchronize(e1);
             float ms = 0.f;
@@ -593,7 +610,8 @@ struct Ensemble {
     int nt = 0;
     int device = 0;
     cudaStream_t s = nullptr;
-    DevBuf<mohid::BatchArgs> dA;         // [2][n]: arguments for each buffer parity
+    DevBuf<mohid::BatchArgs> dA;         // [2][2][n]: arguments per buffer parity, without / with the
+                                         // closed-domain fixer's sums (a call's last step)
     DevBuf<mohid::TmaMaps> dM;           // [2][n]
     DevBuf<int4> tiles;                  // (member, bx, by, 0), costliest first
     int ntiles = 0;
@@ -605,6 +623,7 @@ struct Ensemble {
     int graphSteps = 0;
     bool graphCur = false;
     int graphMethod = 0, graphLimiter = 0;
+    bool graphLast = false;
     void release()
     {
         dA.release(); dM.release(); tiles.release();
@@ -624,22 +643,27 @@ Ensemble* elookup(const int* eid)
     return it == g_ens.end() ? nullptr : it->second;
 }
 
-// one step of every member: one launch over all tiles, then every parity flips
-cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid)
+// One step of every member: one launch over all tiles, then every parity
+// flips.  last: the final step of the call, after which the members' mass
+// fixer corrects (members with open boundaries follow their boundary flux
+// every step).
+cudaError_t enqueue_ens_step(Ensemble* E, int method, int limiter, int grid, bool last)
 {
     const size_t n = E->m.size();
-    const size_t off = E->cur ? n : 0;
+    const size_t moff = E->cur ? n : 0;
+    const size_t aoff = ((E->cur ? 2 : 0) + (last ? 1 : 0)) * n;
     const bool open = std::any_of(E->m.begin(), E->m.end(), [](const Batch* b) { return b->hasRef; });
-    cudaError_t e = mohid::launch_ensemble(E->dA.p + off, E->dM.p + off, E->tiles.p, E->ntiles, grid, E->nt,
+    cudaError_t e = mohid::launch_ensemble(E->dA.p + aoff, E->dM.p + moff, E->tiles.p, E->ntiles, grid, E->nt,
                                            method, limiter, open, E->s);
+    bool fix = false;
     for (size_t q = 0; q < n && e == cudaSuccess; ++q) {
         Batch* b = E->m[q];
+        fix |= fix_active(b) && (last || b->hasRef);   // records without sums or flux return
         if (!b->hasRef) continue;
-        if (fix_active(b)) e = mohid::obc_flux(E->hA[off + q], b->obcol.p, false, E->s);
+        if (fix_active(b)) e = mohid::obc_flux(E->hA[aoff + q], b->obcol.p, false, E->s);
         else e = mohid::mass_fix_drop(b->mfix.p, b->nt, E->s);
     }
-    if (e == cudaSuccess && std::any_of(E->m.begin(), E->m.end(), fix_active))
-        e = mohid::mass_fix_step_many(E->dA.p + off, (int)n, E->nt, E->s);
+    if (e == cudaSuccess && fix) e = mohid::mass_fix_step_many(E->dA.p + aoff, (int)n, E->nt, E->s);
     E->cur = !E->cur;
     return e;
 }
@@ -879,7 +903,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     }
     if (fix_active(b)) b->fixDirty = true;
     if (!*use_graph) {
-        for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s));
+        for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s, true, n == *nsteps - 1));
         return ok(stat);
     }
     // CUDA graph of an even number of steps: the ping-pong returns to the
@@ -887,9 +911,10 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     // odd remainder step is launched directly.
     const int pairs = *nsteps / 2;
     if (pairs > 0) {
+        const bool glast = *nsteps % 2 == 0;          // the graph holds the call's last step
         const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
                            b->graphSched == b->sched && b->graphSplit == b->split &&
-                           b->graphFix == fix_key(b) &&
+                           b->graphFix == fix_key(b) && b->graphLast == glast &&
                            std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
         if (!reuse) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -897,7 +922,8 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = cudaSuccess;
-            for (int n = 0; n < 2 * pairs && e == cudaSuccess; ++n) e = enqueue_step(b, p, s);
+            for (int n = 0; n < 2 * pairs && e == cudaSuccess; ++n)
+                e = enqueue_step(b, p, s, true, glast && n == 2 * pairs - 1);
             cudaError_t e2 = cudaStreamEndCapture(s, &g);
             b->cur = cur0;
             if (e != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("capture", e));
@@ -911,10 +937,11 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphSched = b->sched;
             b->graphSplit = b->split;
             b->graphFix = fix_key(b);
+            b->graphLast = glast;
         }
         CK(cudaGraphLaunch(b->graph, s));
     }
-    if (*nsteps % 2) CK(enqueue_step(b, p, s));
+    if (*nsteps % 2) CK(enqueue_step(b, p, s, true, true));
     return ok(stat);
 }
 
@@ -951,11 +978,12 @@ int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* s
     return ok(stat);
 }
 
-int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* stat)
+int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call, int* stat)
 {
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (launches) *launches = launches_per_step(b);
+    if (per_call) *per_call = launches_per_call(b);
     if (sched) *sched = b->sched;
     if (split) *split = b->split;
     return ok(stat);
@@ -1074,7 +1102,7 @@ int mohid_ad_ensemble_create(int* eid, const int* nmembers, const int* bids, int
     E->ntiles = (int)t.size();
     const size_t n = m.size();
     cudaError_t e;
-    if ((e = E->dA.alloc(2 * n)) != cudaSuccess || (e = E->dM.alloc(2 * n)) != cudaSuccess ||
+    if ((e = E->dA.alloc(4 * n)) != cudaSuccess || (e = E->dM.alloc(2 * n)) != cudaSuccess ||
         (e = E->tiles.alloc(t.size())) != cudaSuccess) {
         E->release();
         delete E;
@@ -1128,8 +1156,9 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
     // members' own streams (packing, tracer loads) before the ensemble's
     for (size_t q = 0; q < n; ++q)
         if (E->m[q]->in->stream != E->s) CK(cudaStreamSynchronize(E->m[q]->in->stream));
-    // argument and tensor-map tables for both buffer parities
-    std::vector<mohid::BatchArgs> hA(2 * n);
+    // argument tables for both buffer parities, without and with the fixer's
+    // sums; tensor-map tables for both parities
+    std::vector<mohid::BatchArgs> hA(4 * n);
     std::vector<mohid::TmaMaps> hM(2 * n);
     const int gi = E->nt == 4 ? 2 : (E->nt == 2 ? 1 : 0);
     for (int c = 0; c < 2; ++c)
@@ -1137,7 +1166,8 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
             Batch* b = E->m[q];
             const float* Pin = c ? b->PB.p : b->PA.p;
             float* Pout = c ? b->PA.p : b->PB.p;
-            hA[c * n + q] = make_bargs(b, &p[q], 0, b->nt, Pin, Pout);
+            for (int l = 0; l < 2; ++l)
+                hA[(c * 2 + l) * n + q] = make_bargs(b, &p[q], 0, b->nt, Pin, Pout, l == 1);
             hM[c * n + q] = b->maps;
             hM[c * n + q].P = b->mapP[c][gi];
         }
@@ -1160,20 +1190,22 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
             for (Batch* b : E->m) b->cur = !b->cur;
     };
     if (!*use_graph) {
-        for (int q = 0; q < *nsteps; ++q) CK(enqueue_ens_step(E, method, limiter, grid));
+        for (int q = 0; q < *nsteps; ++q) CK(enqueue_ens_step(E, method, limiter, grid, q == *nsteps - 1));
         flip_members(*nsteps);
         return ok(stat);
     }
     const int pairs = *nsteps / 2;
     if (pairs > 0) {
+        const bool glast = *nsteps % 2 == 0;          // the graph holds the call's last step
         const bool reuse = E->graph && E->graphSteps == 2 * pairs && E->graphCur == E->cur &&
-                           E->graphMethod == method && E->graphLimiter == limiter && same;
+                           E->graphMethod == method && E->graphLimiter == limiter && E->graphLast == glast && same;
         if (!reuse) {
             if (E->graph) { cudaGraphExecDestroy(E->graph); E->graph = nullptr; }
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(E->s, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = cudaSuccess;
-            for (int q = 0; q < 2 * pairs && e == cudaSuccess; ++q) e = enqueue_ens_step(E, method, limiter, grid);
+            for (int q = 0; q < 2 * pairs && e == cudaSuccess; ++q)
+                e = enqueue_ens_step(E, method, limiter, grid, glast && q == 2 * pairs - 1);
             cudaError_t e2 = cudaStreamEndCapture(E->s, &g);
             E->cur = cur0;
             if (e != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("capture", e));
@@ -1185,10 +1217,11 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
             E->graphCur = cur0;
             E->graphMethod = method;
             E->graphLimiter = limiter;
+            E->graphLast = glast;
         }
         CK(cudaGraphLaunch(E->graph, E->s));
     }
-    if (*nsteps % 2) CK(enqueue_ens_step(E, method, limiter, grid));
+    if (*nsteps % 2) CK(enqueue_ens_step(E, method, limiter, grid, true));
     flip_members(*nsteps);
     return ok(stat);
 }

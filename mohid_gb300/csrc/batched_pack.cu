@@ -433,13 +433,16 @@ __global__ void k_fix_set(const double* partial, int nb, double* mfix, int mode,
 // boundaries (obpart != null) the target first takes the step's boundary flux
 //   phi = -(sum of WFOB * DT) * (constant + correction) - sum of WFOB * DT * value,
 // the value being the stored inflow concentration where WFOB < 0 and the new
-// stored value where WFOB >= 0 (obc_flux).  A tracer whose target was dropped
-// (NaN) is left alone.
+// stored value where WFOB >= 0 (obc_flux).  Without tile sums (mpart null:
+// not the last step of a step call) only the target follows the flux; the
+// correction, which the flux reads, stays as it is.  A tracer whose target was
+// dropped (NaN) is left alone.
 __device__ void fix_tracer(const double* mpart, int ntiles, int nt, int t, double* mfix, const double* obpart,
                            int nob)
 {
     double s = 0.0;
-    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) s += mpart[(long long)t * ntiles + q];
+    if (mpart)
+        for (int q = threadIdx.x; q < ntiles; q += blockDim.x) s += mpart[(long long)t * ntiles + q];
     const double sum = block_neu(s, 0.0);
     double zs = 0.0, ws = 0.0;
     if (obpart) {
@@ -464,7 +467,7 @@ __device__ void fix_tracer(const double* mpart, int ntiles, int nt, int t, doubl
                 mfix[1 + t] = target;
                 mfix[1 + 3 * nt + t] += phi;
             }
-            mfix[1 + 2 * nt + t] += (target - (sum + cnow * W)) / W;
+            if (mpart) mfix[1 + 2 * nt + t] += (target - (sum + cnow * W)) / W;
         }
     }
 }
@@ -476,11 +479,12 @@ __global__ void __launch_bounds__(kRowThreads) k_fix_step(const double* mpart, i
     fix_tracer(mpart, ntiles, nt, blockIdx.x, mfix, obpart, nob);
 }
 
-// block (b, t): tracer t of batch b (blocks past a batch's tracer count return)
+// block (b, t): tracer t of batch b (blocks past a batch's tracer count, and
+// batches with neither tile sums nor a boundary flux this step, return)
 __global__ void __launch_bounds__(kRowThreads) k_fix_step_many(const BatchArgs* As)
 {
     const BatchArgs& a = As[blockIdx.x];
-    if (!a.mpart || (int)blockIdx.y >= a.ntAll) return;
+    if ((!a.mpart && !a.obpart) || (int)blockIdx.y >= a.ntAll) return;
     fix_tracer(a.mpart, a.ntiles, a.ntAll, blockIdx.y, a.mfix, a.obpart, a.nob);
 }
 

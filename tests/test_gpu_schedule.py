@@ -41,7 +41,7 @@ def test_schedules_agree(gpu, nt):
     tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(nt)]
     ref, info = _run(d, tr, 0, 4)
     groups4 = {1: 1, 3: 2, 5: 2, 9: 3}[nt]                 # 4-tracer groups, then 2, then 1
-    assert info == {"launches": groups4 + 1, "sched": 0, "split": 4}
+    assert info == {"launches": groups4, "sched": 0, "split": 4, "per_call": 1}
     cands = [(1, 4), (0, 2), (1, 2)] + ([(0, 8), (1, 8)] if nt >= 8 else [])
     for sched, split in cands:
         got, info = _run(d, tr, sched, split)
