@@ -50,6 +50,7 @@ def main():
         b.step(p, nsteps=args.steps)
         b.sync()
         el = time.perf_counter() - t0
+        print(f"schedule {b.schedule()}")
         b.destroy()
     else:
         bufs = [(torch.from_numpy(P).cuda(), torch.empty_like(torch.from_numpy(P)).cuda()) for P in tr]
