@@ -99,8 +99,8 @@ typedef struct mohid_ad_params {
     double DTProp;                /* property time step [s]                           */
     double ImpExp_AdvV;           /* 1 = implicit (default), 0 = explicit             */
     double ImpExp_DifV;           /* 1 = implicit, 0 = explicit, in between = theta   */
-    double ImpExp_AdvXX;          /* must be 0 (explicit) in this build               */
-    double ImpExp_AdvYY;          /* must be 0 (explicit) in this build               */
+    double ImpExp_AdvXX;          /* 0 explicit, 1 implicit (plain form only)         */
+    double ImpExp_AdvYY;          /* 0 explicit, 1 implicit (plain form only)         */
     double ImpExp_DifH;           /* must be 0: the reference requires explicit H-diff */
     int    NullDif;               /* LOGICAL                                          */
     int    BoundaryCondition;     /* MOHID_BC_*; 4 and 8 also act without a reference */

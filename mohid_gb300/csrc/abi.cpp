@@ -43,7 +43,7 @@ int ok(int* stat)
 void Instance::release()
 {
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
-                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref};
+                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid};
     for (auto* b : d) b->release();
     DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl};
     for (auto* b : i) b->release();
@@ -105,7 +105,10 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
             why = "cyclic boundaries read ReferenceProp (reference Prop_CyclicBoundary)"; return MOHID_AD_ERR_OPTION;
         }
     }
-    if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if ((p->ImpExp_AdvXX != 0.0 && p->ImpExp_AdvXX != 1.0) || (p->ImpExp_AdvYY != 0.0 && p->ImpExp_AdvYY != 1.0)) {
+        why = "ImpExp_AdvXX / ImpExp_AdvYY must be 0 or 1 (reference HorizontalAdvectionXX/YY ERR01)";
+        return MOHID_AD_ERR_OPTION;
+    }
     if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->CellFluxes) { why = "CellFluxes not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->NoAdvFlux || p->NoDifFlux) { why = "NoAdvFlux/NoDifFlux not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
@@ -120,6 +123,54 @@ int status_to_code(unsigned int s, std::string& why)
     if (s & MOHID_DEV_NONFINITE) { why = "non-finite concentration after the solve"; return MOHID_AD_ERR_NONFINITE; }
     if (s & MOHID_DEV_TIMEOUT) { why = "bounded device wait expired"; return MOHID_AD_ERR_TIMEOUT; }
     return MOHID_AD_SUCCESS;
+}
+
+mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const double* Ref,
+                           const mohid_ad_params* p);
+
+// One step of one property, P_in -> P_out (device, Size box), on the
+// instance's stream.  Implicit horizontal advection (AD:4167-4254,
+// AD:1758-1858): in 3-D the rows of the horizontal system, its line solve into
+// Pmid, then the column step from Pmid; with one layer the rows (open
+// boundaries and land included) and the line solve instead of the columns.
+int run_step(Instance* in, const double* Pin, double* Pout, const double* Ref, const mohid_ad_params* p,
+             int* stat)
+{
+    cudaStream_t s = in->stream;
+    mohid::PlainArgs a = make_args(in, Pin, Pout, Ref, p);
+    const bool imp = a.impXX || a.impYY;
+    const bool lines3D = imp && in->nk > 1 && !a.vertical1D;
+    const bool lines2D = imp && in->nk == 1;
+    if (!lines3D && !lines2D) {
+        CK(mohid::launch_plain_f64(a, s));
+        return ok(stat);
+    }
+    if (!in->sys.p) {
+        cudaError_t e = in->sys.alloc(4 * in->n3);
+        if (e == cudaSuccess) e = in->Wl.alloc(in->n3);
+        if (e == cudaSuccess) e = in->Pmid.alloc(in->n3);
+        if (e != cudaSuccess) {
+            in->sys.release(); in->Wl.release(); in->Pmid.release();
+            return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat,
+                        cuda_msg("cudaMalloc", e));
+        }
+    }
+    a.sD = in->sys.p; a.sE = a.sD + in->n3; a.sF = a.sE + in->n3; a.sTI = a.sF + in->n3;
+    const size_t bd = sizeof(double) * in->n3;
+    if (lines3D) {
+        CK(mohid::launch_plain_f64(a, s, mohid::kPlainHorizRows));
+        CK(cudaMemcpyAsync(in->Pmid.p, Pin, bd, cudaMemcpyDeviceToDevice, s));
+        CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p, false,
+                                    in->Wl.p, in->Pmid.p, in->status.p, s));
+        mohid::PlainArgs v = make_args(in, in->Pmid.p, Pout, Ref, p);
+        CK(mohid::launch_plain_f64(v, s, mohid::kPlainVertical));
+    } else {
+        CK(mohid::launch_plain_f64(a, s, mohid::kPlainRows2D));
+        CK(cudaMemcpyAsync(Pout, Pin, bd, cudaMemcpyDeviceToDevice, s));
+        CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p, true,
+                                    in->Wl.p, Pout, in->status.p, s));
+    }
+    return ok(stat);
 }
 
 // boundary conditions the reference applies after the solve (AD:1874-1880),
@@ -164,6 +215,9 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.docycle = p->Docycle_method;
     a.vertical1D = p->Vertical1D != 0; a.xzflow = p->XZFlow != 0;
     a.bc = p->BoundaryCondition;
+    a.impXX = p->ImpExp_AdvXX == 1.0;
+    a.impYY = p->ImpExp_AdvYY == 1.0;
+    a.sD = a.sE = a.sF = a.sTI = nullptr;
     a.status = in->status.p;
     return a;
 }
@@ -356,8 +410,8 @@ int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PRO
     int code = check_params(p, ReferenceProp != nullptr, in->nk, why);
     if (code) return fail(code, stat, why);
     CK(cudaSetDevice(in->device));
-    mohid::PlainArgs a = make_args(in, PROP_in, PROP_out, ReferenceProp, p);
-    CK(mohid::launch_plain_f64(a, in->stream));
+    code = run_step(in, PROP_in, PROP_out, ReferenceProp, p, stat);
+    if (code) return code;
     CK(post_solve(in, PROP_out, ReferenceProp, p));
     return ok(stat);
 }
@@ -377,8 +431,8 @@ int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceP
     CK(cudaMemcpyAsync(in->Pin.p, PROP, bd, cudaMemcpyHostToDevice, in->stream));
     if (ReferenceProp) CK(cudaMemcpyAsync(in->Ref.p, ReferenceProp, bd, cudaMemcpyHostToDevice, in->stream));
     CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
-    mohid::PlainArgs a = make_args(in, in->Pin.p, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p);
-    CK(mohid::launch_plain_f64(a, in->stream));
+    code = run_step(in, in->Pin.p, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p, stat);
+    if (code) return code;
     CK(post_solve(in, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p));
     CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
     CK(cudaMemcpyAsync(PROP, in->Pout.p, bd, cudaMemcpyDeviceToHost, in->stream));

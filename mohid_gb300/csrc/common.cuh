@@ -29,11 +29,29 @@ struct PlainArgs {
     double DT, schmidtH, schmidtCoefV, schmidtBackV, volumeRelMax, impExpDifV, tdecAux;
     int methodH, limiterH, methodV, limiterV, upwind2H, upwind2V;
     int nullDif, explicitV, docycle, vertical1D, xzflow, bc;
+    int impXX, impYY;           // implicit horizontal advection along j (XX) or i (YY)
+    double *sD, *sE, *sF, *sTI; // rows of the implicit horizontal system (Size box), or null
     unsigned int* status;
 };
 
+// Steps of the plain kernel (launch_plain_f64 `mode`)
+enum PlainMode {
+    kPlainFull = 0,         // the whole step, explicit horizontal advection
+    kPlainHorizRows = 1,    // 3-D implicit: rows of the horizontal system to sD..sTI
+    kPlainVertical = 2,     // 3-D implicit: the column step from the line solution
+    kPlainRows2D = 3,       // one layer, implicit: rows with open boundaries and land to sD..sTI
+};
+
 // Launchers (plain_f64.cu)
-cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s);
+cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s, int mode = kPlainFull);
+// THOMAS_3D (FN:3760-3876): one tridiagonal system per work-box line along j
+// (alongJ) or i, from the first work cell to the halo cell past the last, at
+// every layer; rows from D..TI, the halo row D = 0, E = 1, F = 0 and TI = 0
+// (null_real on land when landHalo).  W: scratch (Size box); the answer to P,
+// which must hold the other cells already.
+cudaError_t launch_line_solve(int ni, int nj, int nk, bool alongJ, const double* D, const double* E,
+                              const double* F, const double* TI, const int* LP, bool landHalo, double* W,
+                              double* P, unsigned int* status, cudaStream_t s);
 cudaError_t launch_thomasz_f64(int ni, int nj, int nk, const double* D, const double* E,
                                const double* F, const double* TI, double* RES, const int* WP,
                                unsigned int* status, cudaStream_t s);

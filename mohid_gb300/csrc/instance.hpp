@@ -52,6 +52,9 @@ struct Instance {
     unsigned hydroVersion = 0;
     // per-property staging for the host-pointer entry points
     DevBuf<double> Pin, Pout, Ref;
+    // implicit horizontal advection (allocated on first use): the rows of the
+    // horizontal system (4 x Size box), the line solver's W, the line solution
+    DevBuf<double> sys, Wl, Pmid;
     DevBuf<unsigned int> status;
     unsigned int* hstatus = nullptr;   // pinned
 

@@ -132,12 +132,12 @@ __device__ __forceinline__ bool null_grad(const double* P, const int* CFU, const
 // by du(f + n - 2).  Coefficients are computed only where both cells are
 // OpenPoints (FN:10559); elsewhere they stay zero, as the reference's arrays.
 template <class DU>
-__device__ __forceinline__ double adv_flux(const PlainArgs& A, size_t a, long long s, const double* Q,
-                                           int method, int limiter, bool up2, DU du)
+__device__ __forceinline__ void adv_coef(const PlainArgs& A, size_t a, long long s, const double* Q,
+                                         int method, int limiter, bool up2, DU du, double C[4])
 {
     const double* P = A.P;
     const int* OP = A.OP;
-    double C[4] = {0., 0., 0., 0.};
+    C[0] = C[1] = C[2] = C[3] = 0.;
     if (__ldg(OP + a - s) == 1 && __ldg(OP + a) == 1) {
         double QF = __ldg(Q + a);
         bool nb = (QF > 0) ? (__ldg(OP + a - 2 * s) != 1) : (__ldg(OP + a + s) != 1);
@@ -148,13 +148,27 @@ __device__ __forceinline__ double adv_flux(const PlainArgs& A, size_t a, long lo
                   [&](int n) { return du(n); }, CF);
         for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
     }
+}
+
+template <class DU>
+__device__ __forceinline__ double adv_flux(const PlainArgs& A, size_t a, long long s, const double* Q,
+                                           int method, int limiter, bool up2, DU du)
+{
+    const double* P = A.P;
+    double C[4];
+    adv_coef(A, a, s, Q, method, limiter, up2, du, C);
     return C[0] * __ldg(P + a - 2 * s) + C[1] * __ldg(P + a - s) + C[2] * __ldg(P + a) +
            C[3] * __ldg(P + a + s);
 }
 
+// MODE (PlainMode): the full step; or, for implicit horizontal advection
+// (AD:4167-4254, AD:1758-1858), the rows of the horizontal system, the column
+// step that follows its solution, or the one-layer rows.
+template <int MODE>
 __global__ void __launch_bounds__(kThreads)
 plain_f64_kernel(const PlainArgs A)
 {
+    constexpr bool kRows = MODE == kPlainHorizRows || MODE == kPlainRows2D;
     extern __shared__ double sW[];               // W(k) at sW[k * kThreads + tid]
     const int tid = threadIdx.y * kBX + threadIdx.x;
     const int i = blockIdx.x * kBX + threadIdx.x;    // 0..ni+1 (Size box)
@@ -167,12 +181,13 @@ plain_f64_kernel(const PlainArgs A)
     double* Po = A.Pout;
 
     const bool interior = i >= 1 && i <= ni && j >= 1 && j <= nj;
-    const bool solve = interior && __ldg(A.WP + c + (size_t)sk * nk) == 1;
+    if (kRows && !interior) return;               // every work-box cell has a row
+    const bool solve = interior && (kRows || __ldg(A.WP + c + (size_t)sk * nk) == 1);
     if (!solve) {                                 // THOMASZ leaves the column untouched
         for (int k = 0; k <= nk + 1; ++k) Po[c + (size_t)sk * k] = __ldg(P + c + (size_t)sk * k);
         return;
     }
-    Po[c] = __ldg(P + c);                         // row 0 is never solved
+    if (!kRows) Po[c] = __ldg(P + c);             // row 0 is never solved
 
     const double DT = A.DT;
     const double DUXc = __ldg(A.DUX + c), DVYc = __ldg(A.DVY + c);
@@ -218,6 +233,9 @@ plain_f64_kernel(const PlainArgs A)
         const double Pkp1 = __ldg(P + a + sk);
         double D = 0., E = 1., F = 0., TI;
 
+        if (MODE == kPlainVertical) {
+            TI = Pk;                              // the step restarts from the line solution
+        } else {
         // VolumeVariation
         if (opk == 1) {
             TI = Pk * (__ldg(A.Vold + a) / Vk);
@@ -270,31 +288,71 @@ plain_f64_kernel(const PlainArgs A)
                     TI = TI + AuxI * DT / Vk * (__ldg(P + ap) - Pk);
                 }
             }
-            // HorizontalAdvectionXX (explicit)
+            // HorizontalAdvectionXX: explicit (AD:4454-4488), or implicit
+            // (AD:4490-4515: west face j into D, E; east face j+1 into E, F)
             const bool up2H = A.upwind2H != 0;
+            auto duW = [&](int n) { return __ldg(A.DUX + c + (long long)(n - 2) * sj); };
+            auto duE = [&](int n) { return __ldg(A.DUX + c + (long long)(n - 1) * sj); };
             if (__ldg(A.CFU + a) == 1) {
-                double Fx = adv_flux(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H,
-                                     [&](int n) { return __ldg(A.DUX + c + (long long)(n - 2) * sj); });
-                TI = TI + Fx * DT / Vk;
+                if (!A.impXX) {
+                    double Fx = adv_flux(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW);
+                    TI = TI + Fx * DT / Vk;
+                } else {
+                    double C[4];
+                    adv_coef(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW, C);
+                    double DT2 = DT / Vk;
+                    D = D - C[1] * DT2;
+                    E = E - C[2] * DT2;
+                }
             }
             if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
-                double Fx = adv_flux(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H,
-                                     [&](int n) { return __ldg(A.DUX + c + (long long)(n - 1) * sj); });
-                TI = TI - Fx * DT / Vk;
+                if (!A.impXX) {
+                    double Fx = adv_flux(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H, duE);
+                    TI = TI - Fx * DT / Vk;
+                } else {
+                    double C[4];
+                    adv_coef(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H, duE, C);
+                    double DT1 = DT / Vk;
+                    E = E + C[1] * DT1;
+                    F = F + C[2] * DT1;
+                }
             }
-            // HorizontalAdvectionYY (explicit)
+            // HorizontalAdvectionYY: explicit, or implicit (AD:4855-4880)
             if (!A.xzflow) {
+                auto dvS = [&](int n) { return __ldg(A.DVY + c + (n - 2)); };
+                auto dvN = [&](int n) { return __ldg(A.DVY + c + (n - 1)); };
                 if (__ldg(A.CFV + a) == 1) {
-                    double Fy = adv_flux(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H,
-                                         [&](int n) { return __ldg(A.DVY + c + (n - 2)); });
-                    TI = TI + Fy * DT / Vk;
+                    if (!A.impYY) {
+                        double Fy = adv_flux(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS);
+                        TI = TI + Fy * DT / Vk;
+                    } else {
+                        double C[4];
+                        adv_coef(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS, C);
+                        double DT2 = DT / Vk;
+                        D = D - C[1] * DT2;
+                        E = E - C[2] * DT2;
+                    }
                 }
                 if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
-                    double Fy = adv_flux(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H,
-                                         [&](int n) { return __ldg(A.DVY + c + (n - 1)); });
-                    TI = TI - Fy * DT / Vk;
+                    if (!A.impYY) {
+                        double Fy = adv_flux(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H, dvN);
+                        TI = TI - Fy * DT / Vk;
+                    } else {
+                        double C[4];
+                        adv_coef(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H, dvN, C);
+                        double DT1 = DT / Vk;
+                        E = E + C[1] * DT1;
+                        F = F + C[2] * DT1;
+                    }
                 }
             }
+        }
+        }
+
+        if (MODE == kPlainHorizRows) {            // the horizontal system, solved by lines
+            A.sD[a] = D; A.sE[a] = E; A.sF[a] = F; A.sTI[a] = TI;
+            Pk = Pkp1;
+            continue;
         }
 
         if (doVert) {
@@ -404,6 +462,12 @@ plain_f64_kernel(const PlainArgs A)
 
         if (__ldg(A.LP + a) == 1) TI = MOHID_NULL_REAL_D;
 
+        if (MODE == kPlainRows2D) {               // one layer: solved by lines instead
+            A.sD[a] = D; A.sE[a] = E; A.sF[a] = F; A.sTI[a] = TI;
+            Pk = Pkp1;
+            continue;
+        }
+
         // THOMASZ forward sweep (row 1 has no pivot test, FN:4087-4088)
         double W, G;
         if (k == 1) {
@@ -424,10 +488,12 @@ plain_f64_kernel(const PlainArgs A)
         Pk = Pkp1;
     }
 
-    // row KUB+1: D = 0, E = 1, F = 0, TI = 0 (null_real if flagged land)
+    if (kRows) return;
+    // row KUB+1: D = 0, E = 1, F = 0, TI = 0 (null_real if flagged land); after
+    // a line solve TI there is the field's value (the matrix restarted from it)
     {
         const size_t a = c + (size_t)sk * (nk + 1);
-        double TI = (__ldg(A.LP + a) == 1) ? MOHID_NULL_REAL_D : 0.;
+        double TI = (__ldg(A.LP + a) == 1) ? MOHID_NULL_REAL_D : (MODE == kPlainVertical ? __ldg(P + a) : 0.);
         double D = 0., E = 1., F = 0.;
         double aux = E + D * Wp;
         double G;
@@ -505,6 +571,52 @@ __global__ void check_faces_kernel(int ni, int nj, int nk, const int* __restrict
         bad |= CFW[(size_t)i + sj * j + sk] == 1;
     }
     if (bad) atomicOr(status, MOHID_DEV_BAD_FACE);
+}
+
+// THOMAS_3D_i0_j1_NewType / _i1_j0_NewType (FN:3760-3876): thread e solves
+// line (l, k), l = 1 + e % m over i (lines along j) or j (lines along i), in
+// the reference's arithmetic; W to the scratch, G parked in P, then the
+// back-substitution.  A zero pivot, on which the reference stops, is reported.
+__global__ void line_solve_kernel(int ni, int nj, int nk, bool alongJ, const double* __restrict__ D,
+                                  const double* __restrict__ E, const double* __restrict__ F,
+                                  const double* __restrict__ TI, const int* __restrict__ LP, bool landHalo,
+                                  double* W, double* P, unsigned int* status)
+{
+    const int m = alongJ ? ni : nj, n = alongJ ? nj : ni;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)m * nk) return;
+    const int l = 1 + (int)(e % m), k = 1 + (int)(e / m);
+    const long long sj = ni + 2, sk = (long long)(ni + 2) * (nj + 2);
+    const long long st = alongJ ? sj : 1;
+    const size_t base = (size_t)(alongJ ? l : sj * l) + (size_t)(sk * k);
+    unsigned int flags = 0;
+    size_t a = base + st;
+    double Wp = -F[a] / E[a];
+    double Gp = TI[a] / E[a];
+    W[a] = Wp; P[a] = Gp;
+    for (int x = 2; x <= n + 1; ++x) {
+        a = base + (size_t)(st * x);
+        double d, ee, f, ti;
+        if (x <= n) { d = D[a]; ee = E[a]; f = F[a]; ti = TI[a]; }
+        else { d = 0.; ee = 1.; f = 0.; ti = (landHalo && LP[a] == 1) ? MOHID_NULL_REAL_D : 0.; }
+        double aux = ee + d * Wp;
+        double w, g;
+        if (fabs(aux) > 0) {
+            w = -f / aux;
+            g = (ti - d * Gp) / aux;
+        } else {
+            w = 0.; g = 0.; flags |= MOHID_DEV_ZERO_PIVOT;
+        }
+        W[a] = w; P[a] = g;
+        Wp = w; Gp = g;
+    }
+    double R = Gp;                                 // ANSWER(n+1) = G(n+1)
+    for (int x = n; x >= 1; --x) {
+        a = base + (size_t)(st * x);
+        R = W[a] * R + P[a];
+        P[a] = R;
+    }
+    if (flags) atomicOr(status, flags);
 }
 
 // ImposeNullGradient (AD:1926-1987).  The reference sweeps the boundary
@@ -586,17 +698,45 @@ cudaError_t launch_cyclic(int ni, int nj, int nk, double* P, const double* Ref, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s)
+template <int MODE>
+cudaError_t launch_plain_mode(const PlainArgs& a, cudaStream_t s)
 {
     dim3 blk(kBX, kBY);
     dim3 grd((unsigned)((a.ni + 2 + kBX - 1) / kBX), (unsigned)((a.nj + 2 + kBY - 1) / kBY));
-    size_t smem = sizeof(double) * (size_t)(a.nk + 2) * kThreads;
+    const bool rows = MODE == kPlainHorizRows || MODE == kPlainRows2D;
+    size_t smem = rows ? 0 : sizeof(double) * (size_t)(a.nk + 2) * kThreads;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(plain_f64_kernel,
+        cudaError_t e = cudaFuncSetAttribute(plain_f64_kernel<MODE>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    plain_f64_kernel<<<grd, blk, smem, s>>>(a);
+    plain_f64_kernel<MODE><<<grd, blk, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s, int mode)
+{
+    switch (mode) {
+    case kPlainFull: return launch_plain_mode<kPlainFull>(a, s);
+    case kPlainHorizRows:
+    case kPlainRows2D:
+        if (!a.sD || !a.sE || !a.sF || !a.sTI) return cudaErrorInvalidValue;
+        return mode == kPlainHorizRows ? launch_plain_mode<kPlainHorizRows>(a, s)
+                                       : launch_plain_mode<kPlainRows2D>(a, s);
+    case kPlainVertical: return launch_plain_mode<kPlainVertical>(a, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_line_solve(int ni, int nj, int nk, bool alongJ, const double* D, const double* E,
+                              const double* F, const double* TI, const int* LP, bool landHalo, double* W,
+                              double* P, unsigned int* status, cudaStream_t s)
+{
+    const int m = alongJ ? ni : nj;
+    const long long lines = (long long)m * nk;
+    if (lines <= 0) return cudaSuccess;
+    line_solve_kernel<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(ni, nj, nk, alongJ, D, E, F, TI, LP,
+                                                                      landHalo, W, P, status);
     return cudaGetLastError();
 }
 

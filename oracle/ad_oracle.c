@@ -191,7 +191,9 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     if (p->ImpExp_DifH != 0.) return MOHID_AD_ERR_OPTION;
     if (p->ImpExp_AdvXX == 1. && p->ImpExp_AdvYY == 1.) return MOHID_AD_ERR_OPTION;
     if (p->ImpExp_AdvV != 0. && p->ImpExp_AdvV != 1.) return MOHID_AD_ERR_OPTION;
-    if (p->ImpExp_AdvXX != 0. || p->ImpExp_AdvYY != 0.) return MOHID_AD_ERR_UNSUPPORTED;
+    /* HorizontalAdvectionXX / YY ERR01: explicit (0) or implicit (1) only */
+    if ((p->ImpExp_AdvXX != 0. && p->ImpExp_AdvXX != 1.) || (p->ImpExp_AdvYY != 0. && p->ImpExp_AdvYY != 1.))
+        return MOHID_AD_ERR_OPTION;
     if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux)
         return MOHID_AD_ERR_UNSUPPORTED;
     if (p->Docycle_method != 1 && p->Docycle_method != 2) return MOHID_AD_ERR_OPTION;
@@ -267,6 +269,49 @@ static void fill3(ora_ext X, double* a, double v)
         double* s = a + (size_t)k * X.n2;
         for (size_t q = 0; q < X.n2; ++q) s[q] = v;
     }
+}
+
+/* THOMAS_3D_i0_j1_NewType / THOMAS_3D_i1_j0_NewType, FN:3760-3876: one
+ * tridiagonal system per line of the work box along j (alongJ) or i, from the
+ * first work cell to the halo cell past the last (the row there is whatever
+ * the matrix holds: D = 0, E = 1, F = 0, TI = 0 unless assembled), every
+ * layer k = 1..KUB.  The first row is divided by E without a test; a zero
+ * pivot later stops the reference (ERR10), here it is reported.  The answer
+ * goes to P. */
+static int thomas_3d(const ora_domain* d, int alongJ, const double* D, const double* E, const double* F,
+                     const double* TI, double* P)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    const int n = alongJ ? d->nj : d->ni, m = alongJ ? d->ni : d->nj, nk = d->nk;
+    int zero = 0;
+    #pragma omp parallel reduction(|:zero)
+    {
+        double* W = (double*)malloc(sizeof(double) * (size_t)(n + 2));
+        double* G = (double*)malloc(sizeof(double) * (size_t)(n + 2));
+        #pragma omp for schedule(dynamic, 1) collapse(2)
+        for (int k = 1; k <= nk; ++k)
+            for (int l = 1; l <= m; ++l) {
+                #define CELL(x) (alongJ ? I3(l, (x), k) : I3((x), l, k))
+                size_t a1 = CELL(1);
+                W[1] = -F[a1] / E[a1];
+                G[1] = TI[a1] / E[a1];
+                for (int x = 2; x <= n + 1; ++x) {
+                    size_t a = CELL(x);
+                    double aux = E[a] + D[a] * W[x - 1];
+                    if (fabs(aux) > 0) {
+                        W[x] = -F[a] / aux;
+                        G[x] = (TI[a] - D[a] * G[x - 1]) / aux;
+                    } else {
+                        W[x] = 0.; G[x] = 0.; zero = 1;
+                    }
+                }
+                P[CELL(n + 1)] = G[n + 1];
+                for (int x = n; x >= 1; --x) P[CELL(x)] = W[x] * P[CELL(x + 1)] + G[x];
+                #undef CELL
+            }
+        free(W); free(G);
+    }
+    return zero;
 }
 
 /* NullGradProp, AD:2071-2110: the mean of the four neighbours across compute
@@ -350,7 +395,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
     if (!work) { own = work = ora_work_new(ni, nj, nk); if (!work) return MOHID_AD_ERR_ALLOC; }
     if (work->ni != ni || work->nj != nj || work->nk != nk) return MOHID_AD_ERR_BOUNDS;
     ora_work w = *work;
-    int err = 0;
+    int err = 0, zeroH = 0;
 
     /* Convert_Dif_Vertical, AD:2364-2443: do k = KLB+1,KUB / OMP DO j / do i */
     #pragma omp parallel
@@ -482,6 +527,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                       p->Upwind2H);
         }
         if (err) goto fail;
+        if (p->ImpExp_AdvXX == 0.) {
         #pragma omp parallel for schedule(dynamic, 1)
         for (int k = 1; k <= nk; ++k)
             for (int j = 1; j <= nj; ++j)
@@ -495,6 +541,23 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         w.TI[am] = w.TI[am] - Fx * DT / V[am];
                     }
                 }
+        } else {
+            /* implicit, AD:4490-4515: OMP DO k / do j / do i */
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (int k = 1; k <= nk; ++k)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k);
+                        if (CFU[a] == 1) {
+                            size_t am = I3(i, j - 1, k);
+                            double DT2 = DT / V[a], DT1 = DT / V[am];
+                            w.D[a] = w.D[a] - w.XD[a] * DT2;
+                            w.E[a] = w.E[a] - w.XE[a] * DT2;
+                            w.E[am] = w.E[am] + w.XD[a] * DT1;
+                            w.F[am] = w.F[am] + w.XE[a] * DT1;
+                        }
+                    }
+        }
         /* HorizontalAdvectionYY, AD:4739-4910: do k / OMP DO j for both parts */
         if (!p->XZFlow) {
             #pragma omp parallel reduction(|:err)
@@ -507,6 +570,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                           p->Upwind2H);
             }
             if (err) goto fail;
+            if (p->ImpExp_AdvYY == 0.) {
             #pragma omp parallel
             for (int k = 1; k <= nk; ++k) {
                 #pragma omp for schedule(dynamic, 1)
@@ -522,6 +586,32 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                     }
             }
+            } else {
+                /* implicit, AD:4855-4880: do k / do j / do i */
+                for (int k = 1; k <= nk; ++k)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            size_t a = I3(i, j, k);
+                            if (CFV[a] == 1) {
+                                size_t am = I3(i - 1, j, k);
+                                double DT2 = DT / V[a], DT1 = DT / V[am];
+                                w.D[a] = w.D[a] - w.YD[a] * DT2;
+                                w.E[a] = w.E[a] - w.YE[a] * DT2;
+                                w.E[am] = w.E[am] + w.YD[a] * DT1;
+                                w.F[am] = w.F[am] + w.YE[a] * DT1;
+                            }
+                        }
+            }
+        }
+        /* HorizontalAdvection AD:4167-4254: in 3-D the implicit direction is
+         * solved now (THOMAS_3D into PROP), and the vertical step starts again
+         * from D = 0, E = 1, F = 0, TI = PROP over the Size box */
+        if ((p->ImpExp_AdvXX == 1. || p->ImpExp_AdvYY == 1.) && nk > 1) {
+            zeroH |= thomas_3d(d, p->ImpExp_AdvXX == 1., w.D, w.E, w.F, w.TI, PROP);
+            fill3(X, w.D, 0.); fill3(X, w.E, 1.); fill3(X, w.F, 0.);
+            #pragma omp parallel for schedule(static)
+            for (int k = 0; k < X.NK; ++k)
+                for (size_t q = (size_t)k * X.n2; q < (size_t)(k + 1) * X.n2; ++q) w.TI[q] = PROP[q];
         }
     }
 
@@ -699,7 +789,14 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
         for (size_t q = (size_t)k * X.n2; q < (size_t)(k + 1) * X.n2; ++q)
             if (d->LandPoints3D[q] == 1) w.TI[q] = NULL_REAL;
 
-    st = ora_thomasz(ni, nj, nk, w.D, w.E, w.F, w.TI, PROP, d->WaterPoints3D);
+    /* AD:1758-1858: a one-layer domain solves the implicit direction instead of the columns */
+    if (nk == 1 && p->ImpExp_AdvXX == 1.)
+        st = thomas_3d(d, 1, w.D, w.E, w.F, w.TI, PROP) ? MOHID_AD_ERR_ZERO_PIVOT : 0;
+    else if (nk == 1 && p->ImpExp_AdvYY == 1.)
+        st = thomas_3d(d, 0, w.D, w.E, w.F, w.TI, PROP) ? MOHID_AD_ERR_ZERO_PIVOT : 0;
+    else
+        st = ora_thomasz(ni, nj, nk, w.D, w.E, w.F, w.TI, PROP, d->WaterPoints3D);
+    if (zeroH && !st) st = MOHID_AD_ERR_ZERO_PIVOT;
     /* AD:1874-1880: whether or not a reference is given */
     if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT) impose_null_gradient(d, PROP);
     else if (p->BoundaryCondition == MOHID_BC_CYCLIC) cyclic_boundary(d, PROP, ReferenceProp);

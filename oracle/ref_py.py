@@ -121,6 +121,41 @@ def _null_grad(Pl, CU, CV, k, j, i):
             Pl[k][j + 1][i] * CU[k][j + 1][i] + Pl[k][j - 1][i] * CU[k][j][i]) / float(aux)
 
 
+def _thomas_lines(D, E, F, TI, Pl, along_j, ni, nj, nk):
+    """THOMAS_3D (FN:3760-3876): a tridiagonal system per work-box line along j
+    (or i), first work cell to the halo cell past the last, every layer; the
+    answer goes to Pl.  Returns True on a zero pivot."""
+    n, m = (nj, ni) if along_j else (ni, nj)
+    zero = False
+
+    def at(arr, x, l, k):
+        return arr[k][x][l] if along_j else arr[k][l][x]
+
+    for k in range(1, nk + 1):
+        for l in range(1, m + 1):
+            W = [0.0] * (n + 2)
+            G = [0.0] * (n + 2)
+            W[1] = -at(F, 1, l, k) / at(E, 1, l, k)
+            G[1] = at(TI, 1, l, k) / at(E, 1, l, k)
+            for x in range(2, n + 2):
+                aux = at(E, x, l, k) + at(D, x, l, k) * W[x - 1]
+                if abs(aux) > 0:
+                    W[x] = -at(F, x, l, k) / aux
+                    G[x] = (at(TI, x, l, k) - at(D, x, l, k) * G[x - 1]) / aux
+                else:
+                    W[x], G[x], zero = 0.0, 0.0, True
+            ans = [0.0] * (n + 2)
+            ans[n + 1] = G[n + 1]
+            for x in range(n, 0, -1):
+                ans[x] = W[x] * ans[x + 1] + G[x]
+            for x in range(1, n + 2):
+                if along_j:
+                    Pl[k][x][l] = ans[x]
+                else:
+                    Pl[k][l][x] = ans[x]
+    return zero
+
+
 def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
     `p` is a dict of AdvectionDiffusion scalar arguments."""
@@ -212,11 +247,19 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
         for k in range(1, nk + 1):
             for j in range(1, nj + 1):
                 for i in range(1, ni + 1):
-                    if CU[k][j][i] == 1:
+                    if CU[k][j][i] != 1:
+                        continue
+                    if p["ImpExp_AdvXX"] == 0.0:
                         fl = XC[k][j][i] * Pl[k][j - 2][i] + XD[k][j][i] * Pl[k][j - 1][i] + \
                             XE[k][j][i] * Pl[k][j][i] + XF[k][j][i] * Pl[k][j + 1][i]
                         TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
                         TI[k][j - 1][i] = TI[k][j - 1][i] - fl * DT / V[k][j - 1][i]
+                    else:                                  # implicit, AD:4490-4515
+                        dt2, dt1 = DT / V[k][j][i], DT / V[k][j - 1][i]
+                        D[k][j][i] = D[k][j][i] - XD[k][j][i] * dt2
+                        E[k][j][i] = E[k][j][i] - XE[k][j][i] * dt2
+                        E[k][j - 1][i] = E[k][j - 1][i] + XD[k][j][i] * dt1
+                        F[k][j - 1][i] = F[k][j - 1][i] + XE[k][j][i] * dt1
         if not p["XZFlow"]:
             for k in range(1, nk + 1):
                 for j in range(1, nj + 1):
@@ -232,11 +275,25 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
             for k in range(1, nk + 1):
                 for j in range(1, nj + 1):
                     for i in range(1, ni + 1):
-                        if CV[k][j][i] == 1:
+                        if CV[k][j][i] != 1:
+                            continue
+                        if p["ImpExp_AdvYY"] == 0.0:
                             fl = YC[k][j][i] * Pl[k][j][i - 2] + YD[k][j][i] * Pl[k][j][i - 1] + \
                                 YE[k][j][i] * Pl[k][j][i] + YF[k][j][i] * Pl[k][j][i + 1]
                             TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
                             TI[k][j][i - 1] = TI[k][j][i - 1] - fl * DT / V[k][j][i - 1]
+                        else:                              # implicit, AD:4855-4880
+                            dt2, dt1 = DT / V[k][j][i], DT / V[k][j][i - 1]
+                            D[k][j][i] = D[k][j][i] - YD[k][j][i] * dt2
+                            E[k][j][i] = E[k][j][i] - YE[k][j][i] * dt2
+                            E[k][j][i - 1] = E[k][j][i - 1] + YD[k][j][i] * dt1
+                            F[k][j][i - 1] = F[k][j][i - 1] + YE[k][j][i] * dt1
+        # 3-D: the implicit direction is solved now, the vertical step starts
+        # again from D = 0, E = 1, F = 0, TI = PROP (AD:4167-4254)
+        if (p["ImpExp_AdvXX"] == 1.0 or p["ImpExp_AdvYY"] == 1.0) and nk > 1:
+            zero_h = _thomas_lines(D, E, F, TI, Pl, p["ImpExp_AdvXX"] == 1.0, ni, nj, nk)
+            D, E, F = z3(0.0), z3(1.0), z3(0.0)
+            TI = [[row[:] for row in layer] for layer in Pl]
 
     if nk > 1:
         ie = p["ImpExp_DifV"]
@@ -359,10 +416,16 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                 if LP[k][j][i] == 1:
                     TI[k][j][i] = NULL_REAL
 
+    # a one-layer domain solves the implicit direction instead (AD:1758-1858)
+    if nk == 1 and (p["ImpExp_AdvXX"] == 1.0 or p["ImpExp_AdvYY"] == 1.0):
+        _thomas_lines(D, E, F, TI, Pl, p["ImpExp_AdvXX"] == 1.0, ni, nj, nk)
+        solve_columns = False
+    else:
+        solve_columns = True
     # THOMASZ_NewType2
     W = [0.0] * (nk + 2)
     G = [0.0] * (nk + 2)
-    for j in range(1, nj + 1):
+    for j in range(1, nj + 1) if solve_columns else ():
         for i in range(1, ni + 1):
             if WP[nk][j][i] != 1:
                 continue

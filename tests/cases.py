@@ -38,6 +38,9 @@ OPTIONS = {
     "vertical1d": dict(Vertical1D=1),
     "xzflow": dict(XZFlow=1),
     "background": dict(SchmidtBackground_V=1e-3, schmidt_H=0.7, SchmidtCoef_V=2.0),
+    "implicit_xx": dict(ImpExp_AdvXX=1.0),
+    "implicit_yy_tvd": dict(ImpExp_AdvYY=1.0, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+    "implicit_xx_central": dict(ImpExp_AdvXX=1.0, AdvMethodH=5),
 }
 
 

@@ -21,7 +21,7 @@ def test_c_oracle_equals_python_restatement(built, grid, opt):
 @pytest.mark.parametrize("grid", ["open", "nsopen"])
 @pytest.mark.parametrize("bc,decay", [(1, 0.0), (1, 600.0), (2, 0.0), (2, 300.0), (5, 0.0), (4, 0.0), (7, 0.0),
                                       (8, 0.0)])
-@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod", "implicit_xx", "implicit_yy_tvd"])
 def test_open_boundaries_c_equals_python(built, grid, bc, decay, opt):
     d = domain(grid)
     P0 = d.tracer(3, 1.0, 0.5, seed=1)
