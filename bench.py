@@ -686,7 +686,7 @@ def main():
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # dominant kernel, from one ncu capture of the workload (profiles/).
 TRAFFIC: dict = {
-    ("cfg2", "batched_kernel<2>"): 710.452224e6 + 124.254208e6,
+    ("cfg2", "batched_kernel<2>"): 628.752640e6 + 123.641856e6,
 }
 
 if __name__ == "__main__":
