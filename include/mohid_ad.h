@@ -107,7 +107,7 @@ typedef struct mohid_ad_params {
     double DecayTime;             /* [s]                                              */
     int    AdvectionNudging;      /* LOGICAL, must be .false. in this build           */
     int    AdvectionNudgingCells;
-    int    CellFluxes;            /* LOGICAL, must be .false. in this build           */
+    int    CellFluxes;            /* LOGICAL: record the face fluxes (plain form)     */
     int    NoAdvFlux, NoDifFlux;  /* LOGICAL, must be .false. in this build           */
     int    Optimize, FirstProperty; /* LOGICAL; accepted, results follow the general path */
     int    Vertical1D, XZFlow;    /* LOGICAL, StartAdvectionDiffusion options          */
@@ -180,6 +180,21 @@ int mohid_ad_set_hydro(const int* id,
  */
 int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
                            const mohid_ad_params* p, int* stat);
+
+/*
+ * GetAdvFlux / GetDifFlux (ModuleAdvectionDiffusion.F90:697-860): the face
+ * fluxes of the instance's last step, which must have been made with
+ * p->CellFluxes (MOHID_AD_ERR_OPTION otherwise).  Size-box arrays: the flux
+ * through the west (X: between j-1 and j), south (Y: between i-1 and i) and
+ * bottom (Z: between k-1 and k) face of each cell, positive towards the cell;
+ * zero away from compute faces.  Explicit parts use the field as the
+ * explicit term saw it, implicit parts the new field (AD:1882-1916).  Any of
+ * the three pointers may be NULL; host (*on_device == 0) or device arrays.
+ */
+int mohid_ad_get_adv_flux(const int* id, double* AdvFluxX, double* AdvFluxY, double* AdvFluxZ,
+                          const int* on_device, int* stat);
+int mohid_ad_get_dif_flux(const int* id, double* DifFluxX, double* DifFluxY, double* DifFluxZ,
+                          const int* on_device, int* stat);
 
 /*
  * All-in-one drop-in with the argument surface of AdvectionDiffusion:

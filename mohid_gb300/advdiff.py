@@ -94,6 +94,20 @@ class AdvectionDiffusion:
             C.c_void_p(Ref.data_ptr()) if Ref is not None else None, C.byref(p), C.byref(st))
         N.check(rc, "mohid_ad_step_prop_f64_dev")
 
+    def cell_fluxes(self) -> dict:
+        """The face fluxes of the last step (made with CellFluxes=1): AdvFluxX/Y/Z,
+        DifFluxX/Y/Z as Size-box float64 arrays (mohid_ad_get_adv_flux / _dif_flux)."""
+        out = {n: np.empty(self.domain.shape3) for n in ("AdvFluxX", "AdvFluxY", "AdvFluxZ", "DifFluxX",
+                                                          "DifFluxY", "DifFluxZ")}
+        st = C.c_int(0)
+        host = C.c_int(0)
+        for fn, names in (("mohid_ad_get_adv_flux", ("AdvFluxX", "AdvFluxY", "AdvFluxZ")),
+                          ("mohid_ad_get_dif_flux", ("DifFluxX", "DifFluxY", "DifFluxZ"))):
+            rc = getattr(self.lib, fn)(C.byref(self._id), *(out[n].ctypes.data_as(C.c_void_p) for n in names),
+                                       C.byref(host), C.byref(st))
+            N.check(rc, fn)
+        return out
+
     @property
     def stream(self) -> int:
         return self.lib.mohid_ad_stream(C.byref(self._id)) or 0

@@ -43,7 +43,7 @@ int ok(int* stat)
 void Instance::release()
 {
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
-                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid};
+                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid, &flux};
     for (auto* b : d) b->release();
     DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl};
     for (auto* b : i) b->release();
@@ -110,7 +110,6 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
         return MOHID_AD_ERR_OPTION;
     }
     if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
-    if (p->CellFluxes) { why = "CellFluxes not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->NoAdvFlux || p->NoDifFlux) { why = "NoAdvFlux/NoDifFlux not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (nk > 200) { why = "KUB > 200 layers not supported"; return MOHID_AD_ERR_UNSUPPORTED; }
     return MOHID_AD_SUCCESS;
@@ -133,42 +132,76 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
 // AD:1758-1858): in 3-D the rows of the horizontal system, its line solve into
 // Pmid, then the column step from Pmid; with one layer the rows (open
 // boundaries and land included) and the line solve instead of the columns.
+cudaError_t post_solve(Instance* in, double* P, const double* Ref, const mohid_ad_params* p);
+
+// One step of one property, P_in -> P_out (device, Size box), on the
+// instance's stream: the solve (below), the boundary conditions applied after
+// it, and with CellFluxes the face fluxes (zeroed first, explicit parts
+// recorded by the step, implicit parts added after the solve, AD:1458-1468,
+// AD:1882-1916).  Implicit horizontal advection (AD:4167-4254, AD:1758-1858):
+// in 3-D the rows of the horizontal system, its line solve into Pmid, then the
+// column step from Pmid; with one layer the rows (open boundaries and land
+// included) and the line solve instead of the columns.
 int run_step(Instance* in, const double* Pin, double* Pout, const double* Ref, const mohid_ad_params* p,
              int* stat)
 {
     cudaStream_t s = in->stream;
-    mohid::PlainArgs a = make_args(in, Pin, Pout, Ref, p);
+    const bool cflux = p->CellFluxes != 0;
+    auto bad_alloc = [&](cudaError_t e) {
+        return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat,
+                    cuda_msg("cudaMalloc", e));
+    };
+    in->fluxLast = false;
+    if (cflux) {
+        if (!in->flux.p) {
+            cudaError_t e = in->flux.alloc(6 * in->n3);
+            if (e != cudaSuccess) { in->flux.release(); return bad_alloc(e); }
+        }
+        CK(cudaMemsetAsync(in->flux.p, 0, sizeof(double) * 6 * in->n3, s));
+    }
+    auto args = [&](const double* Pi, double* Po) {
+        mohid::PlainArgs x = make_args(in, Pi, Po, Ref, p);
+        if (cflux) {
+            double* f = in->flux.p;
+            x.fAX = f; x.fAY = f + in->n3; x.fAZ = f + 2 * in->n3;
+            x.fDX = f + 3 * in->n3; x.fDY = f + 4 * in->n3; x.fDZ = f + 5 * in->n3;
+        }
+        return x;
+    };
+    mohid::PlainArgs a = args(Pin, Pout);
     const bool imp = a.impXX || a.impYY;
     const bool lines3D = imp && in->nk > 1 && !a.vertical1D;
     const bool lines2D = imp && in->nk == 1;
+    mohid::PlainArgs v = a;                      // the field the vertical terms see
     if (!lines3D && !lines2D) {
         CK(mohid::launch_plain_f64(a, s));
-        return ok(stat);
-    }
-    if (!in->sys.p) {
-        cudaError_t e = in->sys.alloc(4 * in->n3);
-        if (e == cudaSuccess) e = in->Wl.alloc(in->n3);
-        if (e == cudaSuccess) e = in->Pmid.alloc(in->n3);
-        if (e != cudaSuccess) {
-            in->sys.release(); in->Wl.release(); in->Pmid.release();
-            return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat,
-                        cuda_msg("cudaMalloc", e));
+    } else {
+        if (!in->sys.p) {
+            cudaError_t e = in->sys.alloc(4 * in->n3);
+            if (e == cudaSuccess) e = in->Wl.alloc(in->n3);
+            if (e == cudaSuccess) e = in->Pmid.alloc(in->n3);
+            if (e != cudaSuccess) { in->sys.release(); in->Wl.release(); in->Pmid.release(); return bad_alloc(e); }
+        }
+        a.sD = in->sys.p; a.sE = a.sD + in->n3; a.sF = a.sE + in->n3; a.sTI = a.sF + in->n3;
+        const size_t bd = sizeof(double) * in->n3;
+        if (lines3D) {
+            CK(mohid::launch_plain_f64(a, s, mohid::kPlainHorizRows));
+            CK(cudaMemcpyAsync(in->Pmid.p, Pin, bd, cudaMemcpyDeviceToDevice, s));
+            CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p,
+                                        false, in->Wl.p, in->Pmid.p, in->status.p, s));
+            v = args(in->Pmid.p, Pout);
+            CK(mohid::launch_plain_f64(v, s, mohid::kPlainVertical));
+        } else {
+            CK(mohid::launch_plain_f64(a, s, mohid::kPlainRows2D));
+            CK(cudaMemcpyAsync(Pout, Pin, bd, cudaMemcpyDeviceToDevice, s));
+            CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p,
+                                        true, in->Wl.p, Pout, in->status.p, s));
         }
     }
-    a.sD = in->sys.p; a.sE = a.sD + in->n3; a.sF = a.sE + in->n3; a.sTI = a.sF + in->n3;
-    const size_t bd = sizeof(double) * in->n3;
-    if (lines3D) {
-        CK(mohid::launch_plain_f64(a, s, mohid::kPlainHorizRows));
-        CK(cudaMemcpyAsync(in->Pmid.p, Pin, bd, cudaMemcpyDeviceToDevice, s));
-        CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p, false,
-                                    in->Wl.p, in->Pmid.p, in->status.p, s));
-        mohid::PlainArgs v = make_args(in, in->Pmid.p, Pout, Ref, p);
-        CK(mohid::launch_plain_f64(v, s, mohid::kPlainVertical));
-    } else {
-        CK(mohid::launch_plain_f64(a, s, mohid::kPlainRows2D));
-        CK(cudaMemcpyAsync(Pout, Pin, bd, cudaMemcpyDeviceToDevice, s));
-        CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p, true,
-                                    in->Wl.p, Pout, in->status.p, s));
+    CK(post_solve(in, Pout, Ref, p));
+    if (cflux) {
+        CK(mohid::launch_cell_fluxes(a, v, Pout, p->ImpExp_AdvV, p->ImpExp_DifV, s));
+        in->fluxLast = true;
     }
     return ok(stat);
 }
@@ -218,6 +251,7 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.impXX = p->ImpExp_AdvXX == 1.0;
     a.impYY = p->ImpExp_AdvYY == 1.0;
     a.sD = a.sE = a.sF = a.sTI = nullptr;
+    a.fAX = a.fAY = a.fAZ = a.fDX = a.fDY = a.fDZ = nullptr;
     a.status = in->status.p;
     return a;
 }
@@ -410,10 +444,7 @@ int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PRO
     int code = check_params(p, ReferenceProp != nullptr, in->nk, why);
     if (code) return fail(code, stat, why);
     CK(cudaSetDevice(in->device));
-    code = run_step(in, PROP_in, PROP_out, ReferenceProp, p, stat);
-    if (code) return code;
-    CK(post_solve(in, PROP_out, ReferenceProp, p));
-    return ok(stat);
+    return run_step(in, PROP_in, PROP_out, ReferenceProp, p, stat);
 }
 
 int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
@@ -433,7 +464,6 @@ int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceP
     CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
     code = run_step(in, in->Pin.p, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p, stat);
     if (code) return code;
-    CK(post_solve(in, in->Pout.p, ReferenceProp ? in->Ref.p : nullptr, p));
     CK(cudaMemcpyAsync(in->hstatus, in->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, in->stream));
     CK(cudaMemcpyAsync(PROP, in->Pout.p, bd, cudaMemcpyDeviceToHost, in->stream));
     CK(cudaStreamSynchronize(in->stream));
@@ -477,6 +507,38 @@ void* mohid_ad_stream(const int* id)
 {
     Instance* in = lookup(id);
     return in ? (void*)in->stream : nullptr;
+}
+
+// GetAdvFlux / GetDifFlux (AD:697-860): copies of the face fluxes of the
+// last step, which must have been made with CellFluxes
+static int get_fluxes(const int* id, int first, double* X, double* Y, double* Z, const int* on_device, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (!in->fluxLast || !in->flux.p)
+        return fail(MOHID_AD_ERR_OPTION, stat, "the last step was not made with CellFluxes");
+    CK(cudaSetDevice(in->device));
+    const cudaMemcpyKind kind = *on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    double* dst[3] = {X, Y, Z};
+    for (int q = 0; q < 3; ++q)
+        if (dst[q])
+            CK(cudaMemcpyAsync(dst[q], in->flux.p + (size_t)(first + q) * in->n3, sizeof(double) * in->n3, kind,
+                               in->stream));
+    CK(cudaStreamSynchronize(in->stream));
+    return ok(stat);
+}
+
+int mohid_ad_get_adv_flux(const int* id, double* AdvFluxX, double* AdvFluxY, double* AdvFluxZ,
+                          const int* on_device, int* stat)
+{
+    return get_fluxes(id, 0, AdvFluxX, AdvFluxY, AdvFluxZ, on_device, stat);
+}
+
+int mohid_ad_get_dif_flux(const int* id, double* DifFluxX, double* DifFluxY, double* DifFluxZ,
+                          const int* on_device, int* stat)
+{
+    return get_fluxes(id, 3, DifFluxX, DifFluxY, DifFluxZ, on_device, stat);
 }
 
 int mohid_ad_kill(int* id, int* stat)

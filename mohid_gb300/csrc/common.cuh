@@ -31,6 +31,10 @@ struct PlainArgs {
     int nullDif, explicitV, docycle, vertical1D, xzflow, bc;
     int impXX, impYY;           // implicit horizontal advection along j (XX) or i (YY)
     double *sD, *sE, *sF, *sTI; // rows of the implicit horizontal system (Size box), or null
+    // CellFluxes (or null): AdvFluxX/Y/Z and DifFluxX/Y/Z at the west, south and
+    // bottom face of each cell, zeroed before the step; the step records the
+    // explicit parts, cell_flux_kernel adds the implicit ones after the solve
+    double *fAX, *fAY, *fAZ, *fDX, *fDY, *fDZ;
     unsigned int* status;
 };
 
@@ -57,6 +61,11 @@ cudaError_t launch_thomasz_f64(int ni, int nj, int nk, const double* D, const do
                                unsigned int* status, cudaStream_t s);
 cudaError_t launch_check_faces(int ni, int nj, int nk, const int* CFU, const int* CFV,
                                const int* CFW, unsigned int* status, cudaStream_t s);
+// CellFluxes, implicit parts (AD:1882-1916): with the new field Pnew and the
+// face coefficients of the step (horizontal ones from h.P, vertical ones from
+// v.P), into h's flux arrays
+cudaError_t launch_cell_fluxes(const PlainArgs& h, const PlainArgs& v, const double* Pnew, double impAdvV,
+                               double impDifV, cudaStream_t s);
 // Boundary conditions applied after the solve (AD:1874-1880), in place on P
 // (Fortran layout).  cols: the 2-D offsets i + sj*j of the boundary columns in
 // the reference's sweep order (j outer, i inner), ncols of them.

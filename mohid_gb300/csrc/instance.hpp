@@ -55,6 +55,10 @@ struct Instance {
     // implicit horizontal advection (allocated on first use): the rows of the
     // horizontal system (4 x Size box), the line solver's W, the line solution
     DevBuf<double> sys, Wl, Pmid;
+    // CellFluxes of the last step (6 x Size box: AdvFluxX/Y/Z, DifFluxX/Y/Z),
+    // allocated on first use; fluxLast: the last step computed them
+    DevBuf<double> flux;
+    bool fluxLast = false;
     DevBuf<unsigned int> status;
     unsigned int* hstatus = nullptr;   // pinned
 

@@ -257,6 +257,7 @@ plain_f64_kernel(const PlainArgs A)
                 if (A.nullDif && __ldg(A.Qx + a) == 0.) Kx = 0.;
                 double AuxJ = Kx * __ldg(A.AreaU + a) / __ldg(A.DZX + c - sj);
                 TI = TI - AuxJ * DT / Vk * (Pk - __ldg(P + am));
+                if (A.fDX) A.fDX[a] = 0.0 - AuxJ * (Pk - __ldg(P + am));       // AD:3784-3825
             }
             if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
                 size_t ap = a + sj;
@@ -277,6 +278,7 @@ plain_f64_kernel(const PlainArgs A)
                     if (A.nullDif && __ldg(A.Qy + a) == 0.) Ky = 0.;
                     double AuxI = Ky * __ldg(A.AreaV + a) / __ldg(A.DZY + c - 1);
                     TI = TI - AuxI * DT / Vk * (Pk - __ldg(P + am));
+                    if (A.fDY) A.fDY[a] = 0.0 - AuxI * (Pk - __ldg(P + am));   // AD:3871-3911
                 }
                 if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
                     size_t ap = a + 1;
@@ -297,6 +299,7 @@ plain_f64_kernel(const PlainArgs A)
                 if (!A.impXX) {
                     double Fx = adv_flux(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW);
                     TI = TI + Fx * DT / Vk;
+                    if (A.fAX) A.fAX[a] = 0.0 + 1.0 * Fx;                       // AD:4531-4537
                 } else {
                     double C[4];
                     adv_coef(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW, C);
@@ -325,6 +328,7 @@ plain_f64_kernel(const PlainArgs A)
                     if (!A.impYY) {
                         double Fy = adv_flux(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS);
                         TI = TI + Fy * DT / Vk;
+                        if (A.fAY) A.fAY[a] = 0.0 + 1.0 * Fy;                   // AD:4900-4906
                     } else {
                         double C[4];
                         adv_coef(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS, C);
@@ -356,6 +360,11 @@ plain_f64_kernel(const PlainArgs A)
         }
 
         if (doVert) {
+            // CellFluxes, explicit part of the diffusion through face k (the
+            // reference records it at every W compute face, AD:2776-2777, 3668-3711)
+            if (A.fDZ && ie < 1. && __ldg(A.CFW + a) == 1)
+                A.fDZ[a] = 0.0 - (1. - ie) * Kz(a) * DUXc * DVYc / __ldg(A.DZZ + a - sk) *
+                                     (Pk - __ldg(P + a - sk));
             // VerticalDiffusion: face k (below) then face k+1 (above)
             const bool fk = __ldg(A.CFW + a) == 1 && !sd;
             const bool fk1 = k + 1 <= nk && __ldg(A.CFW + a + sk) == 1 && !sd;
@@ -381,6 +390,7 @@ plain_f64_kernel(const PlainArgs A)
                         double Fz = C[0] * __ldg(P + a - 2 * sk) + C[1] * __ldg(P + a - sk) +
                                     C[2] * Pk + C[3] * Pkp1;
                         TI = TI + Fz * DT / Vk;
+                        if (A.fAZ) A.fAZ[a] = 0.0 + 1.0 * Fz;                   // AD:3128-3135
                     }
                     if (k + 1 <= nk && __ldg(A.CFW + a + sk) == 1) {
                         double C[4];
@@ -573,6 +583,77 @@ __global__ void check_faces_kernel(int ni, int nj, int nk, const int* __restrict
     if (bad) atomicOr(status, MOHID_DEV_BAD_FACE);
 }
 
+// Vertical advection coefficients of face k of column c (AD:2986-3001), from
+// A.P: columns with OpenPoints3D(KUB) == 1, faces between open cells.
+__device__ void vcoef_at(const PlainArgs& A, size_t c, int k, double C[4])
+{
+    C[0] = C[1] = C[2] = C[3] = 0.;
+    const long long sk = A.sk;
+    if (__ldg(A.OP + c + (size_t)sk * A.nk) != 1) return;
+    const size_t a = c + (size_t)sk * k;
+    if (__ldg(A.OP + a - sk) == 1 && __ldg(A.OP + a) == 1) {
+        const double QF = __ldg(A.Qz + a);
+        const bool nb = (QF > 0) ? (__ldg(A.OP + a - 2 * sk) != 1) : (__ldg(A.OP + a + sk) != 1);
+        double CF[4];
+        face_coef(QF, A.DT, A.volumeRelMax, A.methodV, A.limiterV, nb, A.upwind2V != 0,
+                  [&](int n) { return __ldg(A.P + a + (long long)(n - 2) * sk); },
+                  [&](int n) { return __ldg(A.V + a + (long long)(n - 2) * sk); },
+                  [&](int n) { return __ldg(A.DWZ + a + (long long)(n - 2) * sk); }, CF);
+        for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
+    }
+}
+
+// CellFluxes, the implicit parts (AD:1882-1916, with CalcVerticalAdvFlux
+// AD:3356, CalcVerticalDifFlux AD:3668, CalcHorizontalAdvFluxXX/YY
+// AD:3479/3571): the step's face coefficients applied to the new field Pn, at
+// the compute faces of the work box, added to what the step recorded.  The
+// horizontal coefficients come from H.P (the field the horizontal terms saw),
+// the vertical ones from V.P; coefficients the step did not form
+// (Vertical1D, XZFlow) are zero, as the reference's arrays.
+__global__ void __launch_bounds__(kThreads)
+cell_flux_kernel(const PlainArgs H, const PlainArgs Vv, const double* __restrict__ Pn, double impAdvV,
+                 double impDifV)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    const int ni = H.ni, nj = H.nj, nk = H.nk;
+    if (i < 1 || i > ni || j < 1 || j > nj) return;
+    const long long sj = H.sj, sk = H.sk;
+    const size_t c = (size_t)i + (size_t)sj * (size_t)j;
+    const bool up2H = H.upwind2H != 0;
+    for (int k = 1; k <= nk; ++k) {
+        const size_t a = c + (size_t)sk * k;
+        if (nk > 1 && __ldg(H.CFW + a) == 1) {
+            if (impAdvV > 0.) {
+                double C[4] = {0., 0., 0., 0.};
+                if (!H.vertical1D) vcoef_at(Vv, c, k, C);
+                H.fAZ[a] = H.fAZ[a] + impAdvV * (C[0] * Pn[a - 2 * sk] + C[1] * Pn[a - sk] + C[2] * Pn[a] +
+                                                 C[3] * Pn[a + sk]);
+            }
+            if (impDifV > 0.) {
+                double kz = H.schmidtCoefV * __ldg(H.DiffV + a) + H.schmidtBackV;
+                if (H.nullDif && __ldg(H.Qz + a) == 0.) kz = 0.;
+                H.fDZ[a] = H.fDZ[a] - impDifV * kz * __ldg(H.DUX + c) * __ldg(H.DVY + c) / __ldg(H.DZZ + a - sk) *
+                                          (Pn[a] - Pn[a - sk]);
+            }
+        }
+        if (H.impXX && __ldg(H.CFU + a) == 1) {
+            double C[4] = {0., 0., 0., 0.};
+            if (!H.vertical1D)
+                adv_coef(H, a, sj, H.Qx, H.methodH, H.limiterH, up2H, [&](int n) {
+                    return __ldg(H.DUX + c + (long long)(n - 2) * sj); }, C);
+            H.fAX[a] = H.fAX[a] + 1.0 * (C[0] * Pn[a - 2 * sj] + C[1] * Pn[a - sj] + C[2] * Pn[a] +
+                                         C[3] * Pn[a + sj]);
+        }
+        if (H.impYY && __ldg(H.CFV + a) == 1) {
+            double C[4] = {0., 0., 0., 0.};
+            if (!H.vertical1D && !H.xzflow)
+                adv_coef(H, a, 1, H.Qy, H.methodH, H.limiterH, up2H, [&](int n) {
+                    return __ldg(H.DVY + c + (n - 2)); }, C);
+            H.fAY[a] = H.fAY[a] + 1.0 * (C[0] * Pn[a - 2] + C[1] * Pn[a - 1] + C[2] * Pn[a] + C[3] * Pn[a + 1]);
+        }
+    }
+}
+
 // THOMAS_3D_i0_j1_NewType / _i1_j0_NewType (FN:3760-3876): thread e solves
 // line (l, k), l = 1 + e % m over i (lines along j) or j (lines along i), in
 // the reference's arithmetic; W to the scratch, G parked in P, then the
@@ -726,6 +807,16 @@ cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s, int mode)
     case kPlainVertical: return launch_plain_mode<kPlainVertical>(a, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_cell_fluxes(const PlainArgs& h, const PlainArgs& v, const double* Pnew, double impAdvV,
+                               double impDifV, cudaStream_t s)
+{
+    if (!h.fAX || !h.fAY || !h.fAZ || !h.fDX || !h.fDY || !h.fDZ) return cudaErrorInvalidValue;
+    dim3 blk(kBX, kBY);
+    dim3 grd((unsigned)((h.ni + 2 + kBX - 1) / kBX), (unsigned)((h.nj + 2 + kBY - 1) / kBY));
+    cell_flux_kernel<<<grd, blk, 0, s>>>(h, v, Pnew, impAdvV, impDifV);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_line_solve(int ni, int nj, int nk, bool alongJ, const double* D, const double* E,

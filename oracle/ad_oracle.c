@@ -194,7 +194,7 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     /* HorizontalAdvectionXX / YY ERR01: explicit (0) or implicit (1) only */
     if ((p->ImpExp_AdvXX != 0. && p->ImpExp_AdvXX != 1.) || (p->ImpExp_AdvYY != 0. && p->ImpExp_AdvYY != 1.))
         return MOHID_AD_ERR_OPTION;
-    if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux)
+    if (p->AdvectionNudging || p->NoAdvFlux || p->NoDifFlux)
         return MOHID_AD_ERR_UNSUPPORTED;
     if (p->Docycle_method != 1 && p->Docycle_method != 2) return MOHID_AD_ERR_OPTION;
     /* methods 2..4 reach `stop` at the first near-boundary face unless Upwind2 */
@@ -235,6 +235,9 @@ struct ora_work {
     double *D, *E, *F, *TI;
     double *XC, *XD, *XE, *XF, *YC, *YD, *YE, *YF, *VC, *VD, *VE, *VF;
     double *WFOB;
+    /* CellFluxes (allocated on first use): AdvFluxX/Y/Z, DifFluxX/Y/Z */
+    double* fpool;
+    double *FAX, *FAY, *FAZ, *FDX, *FDY, *FDZ;
 };
 
 /* AllocateVariables, AD:537-684: work arrays live for the instance's life and
@@ -258,7 +261,29 @@ ora_work* ora_work_new(int ni, int nj, int nk)
 
 void ora_work_free(ora_work* w)
 {
-    if (w) { free(w->pool); free(w); }
+    if (w) { free(w->pool); free(w->fpool); free(w); }
+}
+
+/* AllocateVariables AD:567-573 (the cell-flux arrays) */
+static int ora_work_fluxes(ora_work* w)
+{
+    if (w->fpool) return 1;
+    size_t n3 = (size_t)(w->ni + 2) * (size_t)(w->nj + 2) * (size_t)(w->nk + 2);
+    w->fpool = (double*)malloc(sizeof(double) * n3 * 6);
+    if (!w->fpool) return 0;
+    double** slots[6] = {&w->FAX, &w->FAY, &w->FAZ, &w->FDX, &w->FDY, &w->FDZ};
+    for (int s = 0; s < 6; ++s) *slots[s] = w->fpool + (size_t)s * n3;
+    return 1;
+}
+
+/* GetAdvFlux / GetDifFlux, AD:697-860: the fluxes of the last step made with
+ * CellFluxes (which = 0..5: AdvFluxX, AdvFluxY, AdvFluxZ, DifFluxX, DifFluxY,
+ * DifFluxZ), or NULL */
+const double* ora_cell_flux(const ora_work* w, int which)
+{
+    if (!w || !w->fpool || which < 0 || which > 5) return NULL;
+    const double* f[6] = {w->FAX, w->FAY, w->FAZ, w->FDX, w->FDY, w->FDZ};
+    return f[which];
 }
 
 /* SetMatrixValue over the Size box (FN:1599-1645: OpenMP over k, static). */
@@ -372,6 +397,37 @@ static void cyclic_boundary(const ora_domain* d, double* P, const double* Ref)
     }
 }
 
+/* CalcHorizontalAdvFluxXX / YY, AD:3479-3526, AD:3571-3619: over the work
+ * box, at compute faces, Flux += Weigth * (C P(-2) + D P(-1) + E P(0) + F P(+1))
+ * along the face's direction (s: the stride) */
+static void cell_adv_flux(const ora_domain* d, const int* CF, long long s, double wgt, const double* Cc,
+                          const double* Cd, const double* Ce, const double* Cf, const double* P, double* Flux)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    for (int k = 1; k <= d->nk; ++k)
+        for (int j = 1; j <= d->nj; ++j)
+            for (int i = 1; i <= d->ni; ++i) {
+                size_t a = I3(i, j, k);
+                if (CF[a] == 1)
+                    Flux[a] = Flux[a] + wgt * (Cc[a] * P[a - 2 * s] + Cd[a] * P[a - s] + Ce[a] * P[a] +
+                                               Cf[a] * P[a + s]);
+            }
+}
+
+/* CalcVerticalDifFlux, AD:3668-3711 */
+static void cell_dif_flux_z(const ora_domain* d, double wgt, const double* Kz, const double* P, double* Flux)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    for (int k = 1; k <= d->nk; ++k)
+        for (int j = 1; j <= d->nj; ++j)
+            for (int i = 1; i <= d->ni; ++i) {
+                size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                if (d->ComputeFacesW3D[a] == 1)
+                    Flux[a] = Flux[a] - wgt * Kz[a] * d->DUX[I2(i, j)] * d->DVY[I2(i, j)] / d->DZZ[am] *
+                                            (P[a] - P[am]);
+            }
+}
+
 int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                  const mohid_ad_params* p, ora_work* work, int nthreads)
 {
@@ -394,6 +450,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
     ora_work* own = NULL;
     if (!work) { own = work = ora_work_new(ni, nj, nk); if (!work) return MOHID_AD_ERR_ALLOC; }
     if (work->ni != ni || work->nj != nj || work->nk != nk) return MOHID_AD_ERR_BOUNDS;
+    const int cflux = p->CellFluxes != 0;
+    if (cflux && !ora_work_fluxes(work)) { ora_work_free(own); return MOHID_AD_ERR_ALLOC; }
     ora_work w = *work;
     int err = 0, zeroH = 0;
 
@@ -464,6 +522,10 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
         double* c12[12] = {w.XC, w.XD, w.XE, w.XF, w.YC, w.YD, w.YE, w.YF, w.VC, w.VD, w.VE, w.VF};
         for (int s = 0; s < 12; ++s) fill3(X, c12[s], 0.);
     }
+    if (cflux) {                                 /* AD:1458-1468 */
+        double* f6[6] = {w.FAX, w.FAY, w.FAZ, w.FDX, w.FDY, w.FDZ};
+        for (int s = 0; s < 6; ++s) fill3(X, f6[s], 0.);
+    }
 
     /* VolumeVariation, AD:3966-4021: do k / OMP DO j / do i */
     #pragma omp parallel
@@ -497,6 +559,14 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         w.TI[a] = w.TI[a] - AuxJ * DT / V[a] * (P[a] - P[am]);
                     }
                 }
+        if (cflux)                               /* CalcHorizontalDifFluxXX, AD:3784-3825 */
+            for (int k = 1; k <= nk; ++k)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k), am = I3(i, j - 1, k);
+                        if (CFU[a] == 1)
+                            w.FDX[a] = w.FDX[a] - w.Kx[a] * d->AreaU[a] / d->DZX[I2(i, j - 1)] * (P[a] - P[am]);
+                    }
         /* HorizontalDiffusionYY, AD:5313-5365: do k / OMP DO j / do i */
         if (!p->XZFlow) {
             #pragma omp parallel
@@ -512,6 +582,14 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                     }
             }
+            if (cflux)                           /* CalcHorizontalDifFluxYY, AD:3871-3911 */
+                for (int k = 1; k <= nk; ++k)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            size_t a = I3(i, j, k), am = I3(i - 1, j, k);
+                            if (CFV[a] == 1)
+                                w.FDY[a] = w.FDY[a] - w.Ky[a] * d->AreaV[a] / d->DZY[I2(i - 1, j)] * (P[a] - P[am]);
+                        }
         }
 
         /* HorizontalAdvectionXX, AD:4368-4540: coefficients per line (i,:,k)
@@ -541,6 +619,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         w.TI[am] = w.TI[am] - Fx * DT / V[am];
                     }
                 }
+        if (cflux)                               /* AD:4531-4537 */
+            cell_adv_flux(d, CFU, X.NI, 1. - p->ImpExp_AdvXX, w.XC, w.XD, w.XE, w.XF, P, w.FAX);
         } else {
             /* implicit, AD:4490-4515: OMP DO k / do j / do i */
             #pragma omp parallel for schedule(dynamic, 1)
@@ -586,6 +666,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                     }
             }
+            if (cflux)                           /* AD:4900-4906 */
+                cell_adv_flux(d, CFV, 1, 1. - p->ImpExp_AdvYY, w.YC, w.YD, w.YE, w.YF, P, w.FAY);
             } else {
                 /* implicit, AD:4855-4880: do k / do j / do i */
                 for (int k = 1; k <= nk; ++k)
@@ -638,6 +720,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                     }
                 }
         }
+        if (cflux && ie < 1.) cell_dif_flux_z(d, 1. - ie, w.Kz, P, w.FDZ);   /* AD:2776-2777 */
 
         if (!p->Vertical1D) {
             /* VerticalAdvection, AD:2941-3140: coefficients per column with
@@ -707,6 +790,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                 }
             }
+            if (cflux && p->ImpExp_AdvV < 1.)    /* AD:3128-3135 */
+                cell_adv_flux(d, CFW, (long long)X.n2, 1. - p->ImpExp_AdvV, w.VC, w.VD, w.VE, w.VF, P, w.FAZ);
         }
     }
 
@@ -800,6 +885,16 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
     /* AD:1874-1880: whether or not a reference is given */
     if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT) impose_null_gradient(d, PROP);
     else if (p->BoundaryCondition == MOHID_BC_CYCLIC) cyclic_boundary(d, PROP, ReferenceProp);
+    if (cflux) {
+        /* implicit parts with the new field, AD:1882-1916 */
+        if (p->ImpExp_AdvV > 0. && nk > 1)
+            cell_adv_flux(d, CFW, (long long)X.n2, p->ImpExp_AdvV, w.VC, w.VD, w.VE, w.VF, PROP, w.FAZ);
+        if (p->ImpExp_DifV > 0. && nk > 1) cell_dif_flux_z(d, p->ImpExp_DifV, w.Kz, PROP, w.FDZ);
+        if (p->ImpExp_AdvXX == 1.)
+            cell_adv_flux(d, CFU, X.NI, p->ImpExp_AdvXX, w.XC, w.XD, w.XE, w.XF, PROP, w.FAX);
+        if (p->ImpExp_AdvYY == 1.)
+            cell_adv_flux(d, CFV, 1, p->ImpExp_AdvYY, w.YC, w.YD, w.YE, w.YF, PROP, w.FAY);
+    }
     ora_work_free(own);
     return st;
 fail:

@@ -64,6 +64,11 @@ int ora_advection_face(const double P[4], const double V[4], const double du[4],
                        double Q, double VolumeRelMax, int method, int limiter,
                        int nearBoundary, int upwind2, double CFace[4]);
 
+/* GetAdvFlux / GetDifFlux (ModuleAdvectionDiffusion.F90:697-860): the face
+ * fluxes of the last step made with CellFluxes, which = 0..5 for AdvFluxX,
+ * AdvFluxY, AdvFluxZ, DifFluxX, DifFluxY, DifFluxZ (Size box); NULL if none. */
+const double* ora_cell_flux(const ora_work* w, int which);
+
 /* Compensated (Neumaier) FP64 sum of VolumeZ*PROP over water cells of the work box. */
 double ora_mass(const ora_domain* d, const double* PROP);
 double ora_mass_f32(const ora_domain* d, const float* PROP);

@@ -96,6 +96,8 @@ def lib():
         L.ora_advection_face.restype = C.c_int
         L.ora_advection_face.argtypes = [_dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_int,
                                          C.c_int, C.c_int, C.c_int, _dp]
+        L.ora_cell_flux.restype = _dp
+        L.ora_cell_flux.argtypes = [C.c_void_p, C.c_int]
         L.ora_mass.restype = C.c_double
         L.ora_mass.argtypes = [C.POINTER(OraDomain), _dp]
         L.ora_mass_f32.restype = C.c_double
@@ -144,6 +146,20 @@ def step(dom, P: np.ndarray, p: Params, ReferenceProp=None, work: Work | None = 
     cd = cdomain(dom, SmallDepths)
     return lib().ora_step_f64(C.byref(cd), _p(P), _p(ReferenceProp), C.byref(p),
                               work.ptr if work is not None else None, nthreads)
+
+
+FLUX_NAMES = ("AdvFluxX", "AdvFluxY", "AdvFluxZ", "DifFluxX", "DifFluxY", "DifFluxZ")
+
+
+def cell_fluxes(dom, work: Work) -> dict:
+    """Copies of the face fluxes of the last step made with CellFluxes on `work`."""
+    out = {}
+    for q, n in enumerate(FLUX_NAMES):
+        ptr = lib().ora_cell_flux(work.ptr, q)
+        if not ptr:
+            raise ValueError("no cell fluxes: step with CellFluxes=1 on this work first")
+        out[n] = np.ctypeslib.as_array(ptr, shape=(int(np.prod(dom.shape3)),)).reshape(dom.shape3).copy()
+    return out
 
 
 def thomasz(D, E, F, TI, RES, WP) -> int:

@@ -21,6 +21,8 @@ cells.  tests/ require it to agree bit for bit with the C oracle
 """
 from __future__ import annotations
 
+import numpy as np
+
 NULL_REAL = -9.9e15
 MIN_VALUE = 1.0e-16
 
@@ -156,9 +158,38 @@ def _thomas_lines(D, E, F, TI, Pl, along_j, ni, nj, nk):
     return zero
 
 
-def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
+def _adv_flux(Fl, Cc, Cd, Ce, Cf, Pl, CF, wgt, ni, nj, nk, axis):
+    """CalcHorizontalAdvFluxXX / YY, CalcVerticalAdvFlux (AD:3356-3619): Flux +=
+    Weigth * (C P(-2) + D P(-1) + E P(0) + F P(+1)) at the compute faces."""
+    for k in range(1, nk + 1):
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if CF[k][j][i] != 1:
+                    continue
+                if axis == 0:
+                    pm2, pm1, p0, pp1 = Pl[k][j - 2][i], Pl[k][j - 1][i], Pl[k][j][i], Pl[k][j + 1][i]
+                elif axis == 1:
+                    pm2, pm1, p0, pp1 = Pl[k][j][i - 2], Pl[k][j][i - 1], Pl[k][j][i], Pl[k][j][i + 1]
+                else:
+                    pm2, pm1, p0, pp1 = Pl[k - 2][j][i], Pl[k - 1][j][i], Pl[k][j][i], Pl[k + 1][j][i]
+                Fl[k][j][i] = Fl[k][j][i] + wgt * (Cc[k][j][i] * pm2 + Cd[k][j][i] * pm1 + Ce[k][j][i] * p0 +
+                                                   Cf[k][j][i] * pp1)
+
+
+def _dif_flux_z(Fl, Kz, DUX, DVY, DZZ, Pl, CW, wgt, ni, nj, nk):
+    """CalcVerticalDifFlux (AD:3668-3711)."""
+    for k in range(1, nk + 1):
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                if CW[k][j][i] == 1:
+                    Fl[k][j][i] = Fl[k][j][i] - wgt * Kz[k][j][i] * DUX[j][i] * DVY[j][i] / DZZ[k - 1][j][i] * \
+                        (Pl[k][j][i] - Pl[k - 1][j][i])
+
+
+def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
-    `p` is a dict of AdvectionDiffusion scalar arguments."""
+    `p` is a dict of AdvectionDiffusion scalar arguments.  With CellFluxes set
+    and a dict `fluxes`, the six face-flux arrays are stored in it."""
     ni, nj, nk = dom.ni, dom.nj, dom.nk
     A = dom.arrays
     f3 = lambda n: A[n].tolist()           # [k][j][i]
@@ -201,6 +232,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
     XC, XD, XE, XF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
     YC, YD, YE, YF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
     ZC, ZD, ZE, ZF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
+    cflux = bool(p.get("CellFluxes", 0))
+    FAX, FAY, FAZ, FDX, FDY, FDZ = (z3(0.0) for _ in range(6))
 
     # VolumeVariation
     for k in range(1, nk + 1):
@@ -223,6 +256,13 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                         dP = Pl[k][j][i] - Pl[k][j - 1][i]
                         TI[k][j - 1][i] = TI[k][j - 1][i] + aux * DT / V[k][j - 1][i] * dP
                         TI[k][j][i] = TI[k][j][i] - aux * DT / V[k][j][i] * dP
+        if cflux:                                          # CalcHorizontalDifFluxXX
+            for k in range(1, nk + 1):
+                for j in range(1, nj + 1):
+                    for i in range(1, ni + 1):
+                        if CU[k][j][i] == 1:
+                            FDX[k][j][i] = FDX[k][j][i] - Kx[k][j][i] * AU[k][j][i] / DZX[j - 1][i] * \
+                                (Pl[k][j][i] - Pl[k][j - 1][i])
         if not p["XZFlow"]:
             for k in range(1, nk + 1):
                 for j in range(1, nj + 1):
@@ -232,6 +272,13 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                             dP = Pl[k][j][i] - Pl[k][j][i - 1]
                             TI[k][j][i - 1] = TI[k][j][i - 1] + aux * DT / V[k][j][i - 1] * dP
                             TI[k][j][i] = TI[k][j][i] - aux * DT / V[k][j][i] * dP
+            if cflux:                                      # CalcHorizontalDifFluxYY
+                for k in range(1, nk + 1):
+                    for j in range(1, nj + 1):
+                        for i in range(1, ni + 1):
+                            if CV[k][j][i] == 1:
+                                FDY[k][j][i] = FDY[k][j][i] - Ky[k][j][i] * AV[k][j][i] / DZY[j][i - 1] * \
+                                    (Pl[k][j][i] - Pl[k][j][i - 1])
         # XX: faces j = 1..nj of every line (i, :, k)
         for k in range(1, nk + 1):
             for i in range(1, ni + 1):
@@ -260,6 +307,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                         E[k][j][i] = E[k][j][i] - XE[k][j][i] * dt2
                         E[k][j - 1][i] = E[k][j - 1][i] + XD[k][j][i] * dt1
                         F[k][j - 1][i] = F[k][j - 1][i] + XE[k][j][i] * dt1
+        if cflux and p["ImpExp_AdvXX"] == 0.0:
+            _adv_flux(FAX, XC, XD, XE, XF, Pl, CU, 1.0 - p["ImpExp_AdvXX"], ni, nj, nk, 0)
         if not p["XZFlow"]:
             for k in range(1, nk + 1):
                 for j in range(1, nj + 1):
@@ -288,6 +337,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                             E[k][j][i] = E[k][j][i] - YE[k][j][i] * dt2
                             E[k][j][i - 1] = E[k][j][i - 1] + YD[k][j][i] * dt1
                             F[k][j][i - 1] = F[k][j][i - 1] + YE[k][j][i] * dt1
+            if cflux and p["ImpExp_AdvYY"] == 0.0:
+                _adv_flux(FAY, YC, YD, YE, YF, Pl, CV, 1.0 - p["ImpExp_AdvYY"], ni, nj, nk, 1)
         # 3-D: the implicit direction is solved now, the vertical step starts
         # again from D = 0, E = 1, F = 0, TI = PROP (AD:4167-4254)
         if (p["ImpExp_AdvXX"] == 1.0 or p["ImpExp_AdvYY"] == 1.0) and nk > 1:
@@ -312,6 +363,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                         D[k][j][i] = D[k][j][i] - a2 * ie
                         E[k][j][i] = E[k][j][i] + a2 * ie
                         TI[k][j][i] = TI[k][j][i] - a2 * dP * (1.0 - ie)
+        if cflux and ie < 1.0:
+            _dif_flux_z(FDZ, Kz, DUX, DVY, DZZ, Pl, CW, 1.0 - ie, ni, nj, nk)
         if not p["Vertical1D"]:
             mV, lV, u2V = p["AdvMethodV"], p["TVDLimitationV"], bool(p["Upwind2V"])
             for j in range(1, nj + 1):
@@ -359,6 +412,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                             for i in range(1, ni + 1):
                                 if CW[k][j][i] == 1:
                                     upd(k, j, i, DT / V[k - 1][j][i], DT / V[k][j][i])
+            if cflux and p["ImpExp_AdvV"] < 1.0:
+                _adv_flux(FAZ, ZC, ZD, ZE, ZF, Pl, CW, 1.0 - p["ImpExp_AdvV"], ni, nj, nk, 2)
 
     if R is not None:
         bc = p["BoundaryCondition"]
@@ -471,4 +526,17 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None):
                     Pl[k][j][1] = Pl[k][j][ni - 1]
                 for k in range(max(KF[j][2], 0), nk + 1):
                     Pl[k][j][ni] = Pl[k][j][2]
+    if cflux:                                        # implicit parts, new field (AD:1882-1916)
+        if p["ImpExp_AdvV"] > 0.0 and nk > 1:
+            _adv_flux(FAZ, ZC, ZD, ZE, ZF, Pl, CW, p["ImpExp_AdvV"], ni, nj, nk, 2)
+        if p["ImpExp_DifV"] > 0.0 and nk > 1:
+            _dif_flux_z(FDZ, Kz, DUX, DVY, DZZ, Pl, CW, p["ImpExp_DifV"], ni, nj, nk)
+        if p["ImpExp_AdvXX"] == 1.0:
+            _adv_flux(FAX, XC, XD, XE, XF, Pl, CU, p["ImpExp_AdvXX"], ni, nj, nk, 0)
+        if p["ImpExp_AdvYY"] == 1.0:
+            _adv_flux(FAY, YC, YD, YE, YF, Pl, CV, p["ImpExp_AdvYY"], ni, nj, nk, 1)
+        if fluxes is not None:
+            for n, a in zip(("AdvFluxX", "AdvFluxY", "AdvFluxZ", "DifFluxX", "DifFluxY", "DifFluxZ"),
+                            (FAX, FAY, FAZ, FDX, FDY, FDZ)):
+                fluxes[n] = np.array(a)
     P[...] = Pl

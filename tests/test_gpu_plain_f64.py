@@ -131,6 +131,35 @@ def test_gpu_implicit_horizontal_many_steps(gpu, opt, nk):
     assert np.array_equal(a.cpu().numpy(), Po)
 
 
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "layer1"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "explicit_v_tvd", "theta_difv", "implicit_xx",
+                                 "implicit_yy_tvd", "docycle2", "tvd_vertical", "vertical1d", "xzflow", "nulldif"])
+def test_gpu_cell_fluxes_match_oracle(gpu, grid, opt):
+    # CellFluxes: the six face-flux arrays of the step, bit for bit
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=2)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    pd = dict(DTProp=30.0, CellFluxes=1, **OPTIONS[opt])
+    Po = P0.copy()
+    work = O.Work(d)
+    assert O.step(d, Po, O.params(**pd), ReferenceProp=R, work=work) == 0
+    fo = O.cell_fluxes(d, work)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(**pd), R)
+    fg = ad.cell_fluxes()
+    assert np.array_equal(Pg, Po)
+    for n in O.FLUX_NAMES:
+        assert np.array_equal(fg[n], fo[n]), n
+    # a step without CellFluxes leaves none to read
+    ad.step(Pg, advdiff.params(DTProp=30.0), R)
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        ad.cell_fluxes()
+    assert ei.value.code == 3
+    ad.kill()
+
+
 def test_gpu_boundary_condition_rules(gpu):
     d = domain("open")
     P = d.tracer(4, 1.0, 0.0, seed=1)
@@ -236,7 +265,7 @@ def test_gpu_zero_pivot_reported(gpu):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(CellFluxes=1), 4), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 4), (dict(AdvectionNudging=1), 4),
 ])
 def test_gpu_rejects_options_like_oracle(gpu, bad, code):
     d = domain("coast")

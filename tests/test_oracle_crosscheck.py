@@ -58,3 +58,23 @@ def test_small_depths_c_equals_python(built):
     assert O.step(d, Pc, O.params(**pd), SmallDepths=sd) == 0
     ref_py.step(d, Pp, pd, SmallDepths=sd)
     assert np.array_equal(Pc, Pp)
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "layer1"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "explicit_v_tvd", "theta_difv", "implicit_xx",
+                                 "implicit_yy_tvd", "docycle2", "tvd_vertical", "vertical1d", "xzflow", "nulldif"])
+def test_cell_fluxes_c_equals_python(built, grid, opt):
+    # CellFluxes (AD:1458-1468, 1882-1916, 3356-3954): the six face-flux arrays
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=2)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    pd = dict(O.DEFAULTS, DTProp=30.0, CellFluxes=1, **OPTIONS[opt])
+    Pc, Pp = P0.copy(), P0.copy()
+    work = O.Work(d)
+    assert O.step(d, Pc, O.params(**pd), ReferenceProp=R, work=work) == 0
+    fc = O.cell_fluxes(d, work)
+    fp = {}
+    ref_py.step(d, Pp, pd, ReferenceProp=R, fluxes=fp)
+    assert np.array_equal(Pc, Pp)
+    for n in O.FLUX_NAMES:
+        assert np.array_equal(fc[n], fp[n]), n

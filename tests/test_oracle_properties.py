@@ -118,6 +118,31 @@ def test_mass_budget_open_boundaries(built, spec, opt, decay):
     assert moved > 1e-6 * scale                  # the boundaries do move mass
 
 
+@pytest.mark.parametrize("opt", [dict(), dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1), dict(ImpExp_DifV=0.5),
+                                 dict(ImpExp_AdvV=0.0, AdvMethodV=4, TVDLimitationV=1, Upwind2V=1),
+                                 dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1), dict(Docycle_method=2)])
+@pytest.mark.parametrize("grid", ["coast", "zlevel"])
+def test_cell_fluxes_close_each_cell_budget(built, grid, opt):
+    # closed domain, static volumes: in every water cell
+    # V * P_new - VOld * P_old = DT * (net advective + diffusive flux in)
+    d = domain(grid)
+    P = d.tracer(3, 1.0, 0.6, seed=8)
+    P0 = P.copy()
+    work = O.Work(d)
+    assert O.step(d, P, O.params(DTProp=30.0, CellFluxes=1, **opt), work=work) == 0
+    f = O.cell_fluxes(d, work)
+    FX, FY, FZ = (f["AdvFlux" + c] + f["DifFlux" + c] for c in "XYZ")
+    nk, nj, ni = d.nk, d.nj, d.ni
+    c = (slice(1, nk + 1), slice(1, nj + 1), slice(1, ni + 1))
+    net = (FX[c] - FX[1:nk + 1, 2:nj + 2, 1:ni + 1] + FY[c] - FY[1:nk + 1, 1:nj + 1, 2:ni + 2] + FZ[c] -
+           FZ[2:nk + 2, 1:nj + 1, 1:ni + 1])
+    wp = d.water_mask()[c]
+    lhs = d.VolumeZ[c] * P[c] - d.VolumeZOld[c] * P0[c]
+    scale = np.max(np.abs(d.VolumeZ[c] * P[c]))
+    assert np.max(np.abs((lhs - 30.0 * net)[wp])) <= 1e-12 * scale
+    assert np.abs(net[wp]).max() > 1e-6 * scale / 30.0         # the fluxes are not all zero
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
@@ -189,7 +214,7 @@ def test_land_and_halo_handling(built):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(CellFluxes=1), 4), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 4), (dict(AdvectionNudging=1), 4),
 ])
 def test_rejected_options(built, bad, code):
     d = domain("coast")
