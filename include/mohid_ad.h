@@ -108,7 +108,7 @@ typedef struct mohid_ad_params {
     int    AdvectionNudging;      /* LOGICAL, must be .false. in this build           */
     int    AdvectionNudgingCells;
     int    CellFluxes;            /* LOGICAL: record the face fluxes (plain form)     */
-    int    NoAdvFlux, NoDifFlux;  /* LOGICAL, must be .false. in this build           */
+    int    NoAdvFlux, NoDifFlux;  /* LOGICAL: use the NoFlux masks (plain form)        */
     int    Optimize, FirstProperty; /* LOGICAL; accepted, results follow the general path */
     int    Vertical1D, XZFlow;    /* LOGICAL, StartAdvectionDiffusion options          */
     int    Docycle_method;        /* 1 (default) or 2, ModuleModel.F90:641-646        */
@@ -180,6 +180,16 @@ int mohid_ad_set_hydro(const int* id,
  */
 int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
                            const mohid_ad_params* p, int* stat);
+
+/*
+ * The NoFluxU / NoFluxV / NoFluxW masks of AdvectionDiffusion's optional
+ * arguments (Size-box int arrays, host).  Steps with p->NoAdvFlux zero the
+ * advection coefficients of masked faces, and steps with p->NoDifFlux their
+ * horizontal diffusivities and vertical diffusion conductances (AD:2496,
+ * 2527, 2741, 3004, 4434, 4804).  They need all three masks
+ * (MOHID_AD_ERR_NULLPTR otherwise).  All three NULL clears them.
+ */
+int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, const int* NoFluxW, int* stat);
 
 /*
  * GetAdvFlux / GetDifFlux (ModuleAdvectionDiffusion.F90:697-860): the face

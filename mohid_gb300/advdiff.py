@@ -94,6 +94,17 @@ class AdvectionDiffusion:
             C.c_void_p(Ref.data_ptr()) if Ref is not None else None, C.byref(p), C.byref(st))
         N.check(rc, "mohid_ad_step_prop_f64_dev")
 
+    def set_noflux(self, masks):
+        """NoFluxU/V/W masks (int32 Size-box arrays) for NoAdvFlux / NoDifFlux, or None to clear."""
+        st = C.c_int(0)
+        if masks is None:
+            rc = self.lib.mohid_ad_set_noflux(C.byref(self._id), None, None, None, C.byref(st))
+        else:
+            ms = [np.ascontiguousarray(m, dtype=np.int32) for m in masks]
+            rc = self.lib.mohid_ad_set_noflux(C.byref(self._id), *(m.ctypes.data_as(C.c_void_p) for m in ms),
+                                              C.byref(st))
+        N.check(rc, "mohid_ad_set_noflux")
+
     def cell_fluxes(self) -> dict:
         """The face fluxes of the last step (made with CellFluxes=1): AdvFluxX/Y/Z,
         DifFluxX/Y/Z as Size-box float64 arrays (mohid_ad_get_adv_flux / _dif_flux)."""

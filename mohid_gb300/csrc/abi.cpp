@@ -45,7 +45,7 @@ void Instance::release()
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
                            &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid, &flux};
     for (auto* b : d) b->release();
-    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl};
+    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl, &NFU, &NFV, &NFW};
     for (auto* b : i) b->release();
     status.release();
     if (hstatus) cudaFreeHost(hstatus);
@@ -110,7 +110,6 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
         return MOHID_AD_ERR_OPTION;
     }
     if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
-    if (p->NoAdvFlux || p->NoDifFlux) { why = "NoAdvFlux/NoDifFlux not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (nk > 200) { why = "KUB > 200 layers not supported"; return MOHID_AD_ERR_UNSUPPORTED; }
     return MOHID_AD_SUCCESS;
 }
@@ -146,6 +145,8 @@ int run_step(Instance* in, const double* Pin, double* Pout, const double* Ref, c
              int* stat)
 {
     cudaStream_t s = in->stream;
+    if ((p->NoAdvFlux || p->NoDifFlux) && !in->hasNoFlux)
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "NoAdvFlux / NoDifFlux need the NoFluxU/V/W masks (mohid_ad_set_noflux)");
     const bool cflux = p->CellFluxes != 0;
     auto bad_alloc = [&](cudaError_t e) {
         return fail(e == cudaErrorMemoryAllocation ? MOHID_AD_ERR_ALLOC : MOHID_AD_ERR_CUDA, stat,
@@ -252,6 +253,11 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.impYY = p->ImpExp_AdvYY == 1.0;
     a.sD = a.sE = a.sF = a.sTI = nullptr;
     a.fAX = a.fAY = a.fAZ = a.fDX = a.fDY = a.fDZ = nullptr;
+    a.noAdv = p->NoAdvFlux != 0;
+    a.noDif = p->NoDifFlux != 0;
+    a.NFU = in->hasNoFlux ? in->NFU.p : nullptr;
+    a.NFV = in->hasNoFlux ? in->NFV.p : nullptr;
+    a.NFW = in->hasNoFlux ? in->NFW.p : nullptr;
     a.status = in->status.p;
     return a;
 }
@@ -507,6 +513,30 @@ void* mohid_ad_stream(const int* id)
 {
     Instance* in = lookup(id);
     return in ? (void*)in->stream : nullptr;
+}
+
+int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, const int* NoFluxW, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!NoFluxU && !NoFluxV && !NoFluxW) {
+        in->hasNoFlux = false;
+        return ok(stat);
+    }
+    if (!NoFluxU || !NoFluxV || !NoFluxW) return fail(MOHID_AD_ERR_NULLPTR, stat, "give all three masks or none");
+    CK(cudaSetDevice(in->device));
+    DevBuf<int>* d[3] = {&in->NFU, &in->NFV, &in->NFW};
+    const int* src[3] = {NoFluxU, NoFluxV, NoFluxW};
+    for (int q = 0; q < 3; ++q) {
+        if (!d[q]->p) {
+            cudaError_t e = d[q]->alloc(in->n3);
+            if (e != cudaSuccess) return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
+        }
+        CK(cudaMemcpyAsync(d[q]->p, src[q], sizeof(int) * in->n3, cudaMemcpyHostToDevice, in->stream));
+    }
+    CK(cudaStreamSynchronize(in->stream));
+    in->hasNoFlux = true;
+    return ok(stat);
 }
 
 // GetAdvFlux / GetDifFlux (AD:697-860): copies of the face fluxes of the

@@ -30,6 +30,8 @@ struct PlainArgs {
     int methodH, limiterH, methodV, limiterV, upwind2H, upwind2V;
     int nullDif, explicitV, docycle, vertical1D, xzflow, bc;
     int impXX, impYY;           // implicit horizontal advection along j (XX) or i (YY)
+    int noAdv, noDif;           // NoAdvFlux / NoDifFlux with the masks below
+    const int *NFU, *NFV, *NFW; // NoFluxU/V/W (Size box), or null
     double *sD, *sE, *sF, *sTI; // rows of the implicit horizontal system (Size box), or null
     // CellFluxes (or null): AdvFluxX/Y/Z and DifFluxX/Y/Z at the west, south and
     // bottom face of each cell, zeroed before the step; the step records the

@@ -59,6 +59,9 @@ struct Instance {
     // allocated on first use; fluxLast: the last step computed them
     DevBuf<double> flux;
     bool fluxLast = false;
+    // NoFluxU/V/W masks (mohid_ad_set_noflux), used by NoAdvFlux / NoDifFlux
+    DevBuf<int> NFU, NFV, NFW;
+    bool hasNoFlux = false;
     DevBuf<unsigned int> status;
     unsigned int* hstatus = nullptr;   // pinned
 

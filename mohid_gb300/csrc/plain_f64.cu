@@ -131,9 +131,11 @@ __device__ __forceinline__ bool null_grad(const double* P, const int* CFU, const
 // along stride `s`; `f` is the face index along that axis (1..N), du indexed
 // by du(f + n - 2).  Coefficients are computed only where both cells are
 // OpenPoints (FN:10559); elsewhere they stay zero, as the reference's arrays.
+// nf: the NoFlux mask of these faces when NoAdvFlux is set (AD:4434-4443,
+// AD:4804-4813: the face's coefficients are zeroed), else null
 template <class DU>
 __device__ __forceinline__ void adv_coef(const PlainArgs& A, size_t a, long long s, const double* Q,
-                                         int method, int limiter, bool up2, DU du, double C[4])
+                                         const int* nf, int method, int limiter, bool up2, DU du, double C[4])
 {
     const double* P = A.P;
     const int* OP = A.OP;
@@ -148,15 +150,16 @@ __device__ __forceinline__ void adv_coef(const PlainArgs& A, size_t a, long long
                   [&](int n) { return du(n); }, CF);
         for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
     }
+    if (nf && __ldg(nf + a) == 1) C[0] = C[1] = C[2] = C[3] = 0.;
 }
 
 template <class DU>
 __device__ __forceinline__ double adv_flux(const PlainArgs& A, size_t a, long long s, const double* Q,
-                                           int method, int limiter, bool up2, DU du)
+                                           const int* nf, int method, int limiter, bool up2, DU du)
 {
     const double* P = A.P;
     double C[4];
-    adv_coef(A, a, s, Q, method, limiter, up2, du, C);
+    adv_coef(A, a, s, Q, nf, method, limiter, up2, du, C);
     return C[0] * __ldg(P + a - 2 * s) + C[1] * __ldg(P + a - s) + C[2] * __ldg(P + a) +
            C[3] * __ldg(P + a + s);
 }
@@ -220,6 +223,7 @@ plain_f64_kernel(const PlainArgs A)
                       [&](int n) { return __ldg(A.V + a + (long long)(n - 2) * sk); },
                       [&](int n) { return __ldg(A.DWZ + a + (long long)(n - 2) * sk); }, CF);
             for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
+            if (A.noAdv && __ldg(A.NFW + a) == 1) C[0] = C[1] = C[2] = C[3] = 0.;   // AD:3004-3013
         }
     };
 
@@ -255,6 +259,7 @@ plain_f64_kernel(const PlainArgs A)
                                           __ldg(A.ViscH + am) * __ldg(A.DUX + c)) /
                             (__ldg(A.DUX + c) + __ldg(A.DUX + c - sj));
                 if (A.nullDif && __ldg(A.Qx + a) == 0.) Kx = 0.;
+                if (A.noDif && __ldg(A.NFU + a) == 1) Kx = 0.;              // AD:2496-2500
                 double AuxJ = Kx * __ldg(A.AreaU + a) / __ldg(A.DZX + c - sj);
                 TI = TI - AuxJ * DT / Vk * (Pk - __ldg(P + am));
                 if (A.fDX) A.fDX[a] = 0.0 - AuxJ * (Pk - __ldg(P + am));       // AD:3784-3825
@@ -265,6 +270,7 @@ plain_f64_kernel(const PlainArgs A)
                                           __ldg(A.ViscH + a) * __ldg(A.DUX + c + sj)) /
                             (__ldg(A.DUX + c + sj) + __ldg(A.DUX + c));
                 if (A.nullDif && __ldg(A.Qx + ap) == 0.) Kx = 0.;
+                if (A.noDif && __ldg(A.NFU + ap) == 1) Kx = 0.;
                 double AuxJ = Kx * __ldg(A.AreaU + ap) / __ldg(A.DZX + c);
                 TI = TI + AuxJ * DT / Vk * (__ldg(P + ap) - Pk);
             }
@@ -276,6 +282,7 @@ plain_f64_kernel(const PlainArgs A)
                                               __ldg(A.ViscH + am) * __ldg(A.DVY + c)) /
                                 (__ldg(A.DVY + c) + __ldg(A.DVY + c - 1));
                     if (A.nullDif && __ldg(A.Qy + a) == 0.) Ky = 0.;
+                    if (A.noDif && __ldg(A.NFV + a) == 1) Ky = 0.;          // AD:2527-2531
                     double AuxI = Ky * __ldg(A.AreaV + a) / __ldg(A.DZY + c - 1);
                     TI = TI - AuxI * DT / Vk * (Pk - __ldg(P + am));
                     if (A.fDY) A.fDY[a] = 0.0 - AuxI * (Pk - __ldg(P + am));   // AD:3871-3911
@@ -286,6 +293,7 @@ plain_f64_kernel(const PlainArgs A)
                                               __ldg(A.ViscH + a) * __ldg(A.DVY + c + 1)) /
                                 (__ldg(A.DVY + c + 1) + __ldg(A.DVY + c));
                     if (A.nullDif && __ldg(A.Qy + ap) == 0.) Ky = 0.;
+                    if (A.noDif && __ldg(A.NFV + ap) == 1) Ky = 0.;
                     double AuxI = Ky * __ldg(A.AreaV + ap) / __ldg(A.DZY + c);
                     TI = TI + AuxI * DT / Vk * (__ldg(P + ap) - Pk);
                 }
@@ -293,16 +301,18 @@ plain_f64_kernel(const PlainArgs A)
             // HorizontalAdvectionXX: explicit (AD:4454-4488), or implicit
             // (AD:4490-4515: west face j into D, E; east face j+1 into E, F)
             const bool up2H = A.upwind2H != 0;
+            const int* nfU = A.noAdv ? A.NFU : nullptr;
+            const int* nfV = A.noAdv ? A.NFV : nullptr;
             auto duW = [&](int n) { return __ldg(A.DUX + c + (long long)(n - 2) * sj); };
             auto duE = [&](int n) { return __ldg(A.DUX + c + (long long)(n - 1) * sj); };
             if (__ldg(A.CFU + a) == 1) {
                 if (!A.impXX) {
-                    double Fx = adv_flux(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW);
+                    double Fx = adv_flux(A, a, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duW);
                     TI = TI + Fx * DT / Vk;
                     if (A.fAX) A.fAX[a] = 0.0 + 1.0 * Fx;                       // AD:4531-4537
                 } else {
                     double C[4];
-                    adv_coef(A, a, sj, A.Qx, A.methodH, A.limiterH, up2H, duW, C);
+                    adv_coef(A, a, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duW, C);
                     double DT2 = DT / Vk;
                     D = D - C[1] * DT2;
                     E = E - C[2] * DT2;
@@ -310,11 +320,11 @@ plain_f64_kernel(const PlainArgs A)
             }
             if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
                 if (!A.impXX) {
-                    double Fx = adv_flux(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H, duE);
+                    double Fx = adv_flux(A, a + sj, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duE);
                     TI = TI - Fx * DT / Vk;
                 } else {
                     double C[4];
-                    adv_coef(A, a + sj, sj, A.Qx, A.methodH, A.limiterH, up2H, duE, C);
+                    adv_coef(A, a + sj, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duE, C);
                     double DT1 = DT / Vk;
                     E = E + C[1] * DT1;
                     F = F + C[2] * DT1;
@@ -326,12 +336,12 @@ plain_f64_kernel(const PlainArgs A)
                 auto dvN = [&](int n) { return __ldg(A.DVY + c + (n - 1)); };
                 if (__ldg(A.CFV + a) == 1) {
                     if (!A.impYY) {
-                        double Fy = adv_flux(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS);
+                        double Fy = adv_flux(A, a, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvS);
                         TI = TI + Fy * DT / Vk;
                         if (A.fAY) A.fAY[a] = 0.0 + 1.0 * Fy;                   // AD:4900-4906
                     } else {
                         double C[4];
-                        adv_coef(A, a, 1, A.Qy, A.methodH, A.limiterH, up2H, dvS, C);
+                        adv_coef(A, a, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvS, C);
                         double DT2 = DT / Vk;
                         D = D - C[1] * DT2;
                         E = E - C[2] * DT2;
@@ -339,11 +349,11 @@ plain_f64_kernel(const PlainArgs A)
                 }
                 if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
                     if (!A.impYY) {
-                        double Fy = adv_flux(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H, dvN);
+                        double Fy = adv_flux(A, a + 1, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvN);
                         TI = TI - Fy * DT / Vk;
                     } else {
                         double C[4];
-                        adv_coef(A, a + 1, 1, A.Qy, A.methodH, A.limiterH, up2H, dvN, C);
+                        adv_coef(A, a + 1, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvN, C);
                         double DT1 = DT / Vk;
                         E = E + C[1] * DT1;
                         F = F + C[2] * DT1;
@@ -370,6 +380,7 @@ plain_f64_kernel(const PlainArgs A)
             const bool fk1 = k + 1 <= nk && __ldg(A.CFW + a + sk) == 1 && !sd;
             if (fk) {
                 double AuxK = Kz(a) * DUXc * DVYc / __ldg(A.DZZ + a - sk);
+                if (A.noDif && __ldg(A.NFW + a) == 1) AuxK = 0.;            // AD:2741-2745
                 double Aux2 = AuxK * DT / Vk;
                 D = D - Aux2 * ie;
                 E = E + Aux2 * ie;
@@ -377,6 +388,7 @@ plain_f64_kernel(const PlainArgs A)
             }
             if (fk1) {
                 double AuxK = Kz(a + sk) * DUXc * DVYc / __ldg(A.DZZ + a);
+                if (A.noDif && __ldg(A.NFW + a + sk) == 1) AuxK = 0.;
                 double Aux1 = AuxK * DT / Vk;
                 E = E + Aux1 * ie;
                 F = F - Aux1 * ie;
@@ -600,6 +612,7 @@ __device__ void vcoef_at(const PlainArgs& A, size_t c, int k, double C[4])
                   [&](int n) { return __ldg(A.V + a + (long long)(n - 2) * sk); },
                   [&](int n) { return __ldg(A.DWZ + a + (long long)(n - 2) * sk); }, CF);
         for (int n = 0; n < 4; ++n) C[n] = QF * CF[n];
+        if (A.noAdv && __ldg(A.NFW + a) == 1) C[0] = C[1] = C[2] = C[3] = 0.;
     }
 }
 
@@ -639,7 +652,7 @@ cell_flux_kernel(const PlainArgs H, const PlainArgs Vv, const double* __restrict
         if (H.impXX && __ldg(H.CFU + a) == 1) {
             double C[4] = {0., 0., 0., 0.};
             if (!H.vertical1D)
-                adv_coef(H, a, sj, H.Qx, H.methodH, H.limiterH, up2H, [&](int n) {
+                adv_coef(H, a, sj, H.Qx, H.noAdv ? H.NFU : nullptr, H.methodH, H.limiterH, up2H, [&](int n) {
                     return __ldg(H.DUX + c + (long long)(n - 2) * sj); }, C);
             H.fAX[a] = H.fAX[a] + 1.0 * (C[0] * Pn[a - 2 * sj] + C[1] * Pn[a - sj] + C[2] * Pn[a] +
                                          C[3] * Pn[a + sj]);
@@ -647,7 +660,7 @@ cell_flux_kernel(const PlainArgs H, const PlainArgs Vv, const double* __restrict
         if (H.impYY && __ldg(H.CFV + a) == 1) {
             double C[4] = {0., 0., 0., 0.};
             if (!H.vertical1D && !H.xzflow)
-                adv_coef(H, a, 1, H.Qy, H.methodH, H.limiterH, up2H, [&](int n) {
+                adv_coef(H, a, 1, H.Qy, H.noAdv ? H.NFV : nullptr, H.methodH, H.limiterH, up2H, [&](int n) {
                     return __ldg(H.DVY + c + (n - 2)); }, C);
             H.fAY[a] = H.fAY[a] + 1.0 * (C[0] * Pn[a - 2] + C[1] * Pn[a - 1] + C[2] * Pn[a] + C[3] * Pn[a + 1]);
         }

@@ -194,8 +194,9 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     /* HorizontalAdvectionXX / YY ERR01: explicit (0) or implicit (1) only */
     if ((p->ImpExp_AdvXX != 0. && p->ImpExp_AdvXX != 1.) || (p->ImpExp_AdvYY != 0. && p->ImpExp_AdvYY != 1.))
         return MOHID_AD_ERR_OPTION;
-    if (p->AdvectionNudging || p->NoAdvFlux || p->NoDifFlux)
-        return MOHID_AD_ERR_UNSUPPORTED;
+    if (p->AdvectionNudging) return MOHID_AD_ERR_UNSUPPORTED;
+    /* the reference reads NoFluxU/V/W whenever NoAdvFlux or NoDifFlux is set */
+    if ((p->NoAdvFlux || p->NoDifFlux) && (!d->NoFluxU || !d->NoFluxV || !d->NoFluxW)) return MOHID_AD_ERR_NULLPTR;
     if (p->Docycle_method != 1 && p->Docycle_method != 2) return MOHID_AD_ERR_OPTION;
     /* methods 2..4 reach `stop` at the first near-boundary face unless Upwind2 */
     int mH = p->AdvMethodH, mV = p->AdvMethodV;
@@ -428,6 +429,27 @@ static void cell_dif_flux_z(const ora_domain* d, double wgt, const double* Kz, c
             }
 }
 
+/* NoAdvFlux: the face coefficients of the masked faces of the work box are
+ * zeroed after their lines are formed (AD:4434-4443, AD:4804-4813); from
+ * KFloorZ for the vertical ones, on columns open at KUB (AD:3004-3013) */
+static void noflux_zero(const ora_domain* d, const int* NF, int vertical, double* C, double* D, double* E,
+                        double* F)
+{
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    for (int j = 1; j <= d->nj; ++j)
+        for (int i = 1; i <= d->ni; ++i) {
+            int k0 = 1;
+            if (vertical) {
+                if (d->OpenPoints3D[I3(i, j, d->nk)] != 1) continue;
+                k0 = d->KFloorZ[I2(i, j)] < 0 ? 0 : d->KFloorZ[I2(i, j)];
+            }
+            for (int k = k0; k <= d->nk; ++k) {
+                size_t a = I3(i, j, k);
+                if (NF[a] == 1) C[a] = D[a] = E[a] = F[a] = 0.;
+            }
+        }
+}
+
 int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                  const mohid_ad_params* p, ora_work* work, int nthreads)
 {
@@ -500,6 +522,17 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                                   d->Visc_H[I3(i - 1, j, k)] * d->DVY[I2(i, j)]) /
                                   (d->DVY[I2(i, j)] + d->DVY[I2(i - 1, j)]);
                 }
+        }
+        if (p->NoDifFlux) {                      /* AD:2496-2500, AD:2527-2531 */
+            for (int k = 1; k <= nk; ++k) {
+                #pragma omp for schedule(dynamic, 1)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        size_t a = I3(i, j, k);
+                        if (CFU[a] == 1 && d->NoFluxU[a] == 1) w.Kx[a] = 0.;
+                        if (CFV[a] == 1 && d->NoFluxV[a] == 1) w.Ky[a] = 0.;
+                    }
+            }
         }
         if (p->NullDif) {
             for (int k = 1; k <= nk; ++k) {
@@ -605,6 +638,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                       p->Upwind2H);
         }
         if (err) goto fail;
+        if (p->NoAdvFlux) noflux_zero(d, d->NoFluxU, 0, w.XC, w.XD, w.XE, w.XF);
         if (p->ImpExp_AdvXX == 0.) {
         #pragma omp parallel for schedule(dynamic, 1)
         for (int k = 1; k <= nk; ++k)
@@ -650,6 +684,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                           p->Upwind2H);
             }
             if (err) goto fail;
+            if (p->NoAdvFlux) noflux_zero(d, d->NoFluxV, 0, w.YC, w.YD, w.YE, w.YF);
             if (p->ImpExp_AdvYY == 0.) {
             #pragma omp parallel
             for (int k = 1; k <= nk; ++k) {
@@ -709,6 +744,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                     int sd = d->SmallDepths ? d->SmallDepths[I2(i, j)] : 0;
                     if (CFW[a] == 1 && !sd) {
                         double AuxK = w.Kz[a] * d->DUX[I2(i, j)] * d->DVY[I2(i, j)] / d->DZZ[am];
+                        if (p->NoDifFlux && d->NoFluxW[a] == 1) AuxK = 0.;   /* AD:2741-2745 */
                         double Aux1 = AuxK * DT / V[am];
                         double Aux2 = AuxK * DT / V[a];
                         w.E[am] = w.E[am] + Aux1 * ie;
@@ -735,6 +771,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                               w.VC, w.VD, w.VE, w.VF, p->AdvMethodV,
                                               p->TVDLimitationV, p->VolumeRelMax, p->Upwind2V);
             if (err) goto fail;
+            if (p->NoAdvFlux) noflux_zero(d, d->NoFluxW, 1, w.VC, w.VD, w.VE, w.VF);
 
             if (p->ImpExp_AdvV == 0.) {
                 /* explicit, AD:3036-3063: do k / OMP DO j / do i */

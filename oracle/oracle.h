@@ -41,6 +41,7 @@ typedef struct ora_domain {
     const int *OpenPoints3D, *LandPoints3D, *WaterPoints3D;
     const int *ComputeFacesU3D, *ComputeFacesV3D, *ComputeFacesW3D;
     const int *SmallDepths;            /* 2-D, may be NULL */
+    const int *NoFluxU, *NoFluxV, *NoFluxW;   /* 3-D, may be NULL (NoAdvFlux / NoDifFlux) */
 } ora_domain;
 
 /* Work arrays of one instance (AllocateVariables, AD:537-684). */

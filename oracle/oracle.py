@@ -32,7 +32,8 @@ class OraDomain(C.Structure):
         [(n, _dp) for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "VolumeZOld", "VolumeZ", "Visc_H",
                             "Diff_V", "AreaU", "AreaV", "DZZ", "DWZ")] + \
         [(n, _ip) for n in ("OpenPoints3D", "LandPoints3D", "WaterPoints3D", "ComputeFacesU3D",
-                            "ComputeFacesV3D", "ComputeFacesW3D", "SmallDepths")]
+                            "ComputeFacesV3D", "ComputeFacesW3D", "SmallDepths", "NoFluxU", "NoFluxV",
+                            "NoFluxW")]
 
 
 class Params(C.Structure):
@@ -110,7 +111,7 @@ def _p(a, t=_dp):
     return None if a is None else a.ctypes.data_as(t)
 
 
-def cdomain(dom, SmallDepths=None) -> OraDomain:
+def cdomain(dom, SmallDepths=None, NoFlux=None) -> OraDomain:
     a = dom.arrays
     d = OraDomain()
     d.ni, d.nj, d.nk = dom.ni, dom.nj, dom.nk
@@ -121,7 +122,9 @@ def cdomain(dom, SmallDepths=None) -> OraDomain:
               "ComputeFacesU3D", "ComputeFacesV3D", "ComputeFacesW3D"):
         setattr(d, n, _p(a[n], _ip))
     d.SmallDepths = _p(SmallDepths, _ip)
-    d._keep = (dom, SmallDepths)
+    nf = NoFlux if NoFlux is not None else (None, None, None)
+    d.NoFluxU, d.NoFluxV, d.NoFluxW = (_p(m, _ip) for m in nf)
+    d._keep = (dom, SmallDepths, NoFlux)
     return d
 
 
@@ -140,10 +143,11 @@ class Work:
 
 
 def step(dom, P: np.ndarray, p: Params, ReferenceProp=None, work: Work | None = None,
-         nthreads: int = 0, SmallDepths=None) -> int:
-    """One FP64 oracle step of one property, in place.  Returns the status code."""
+         nthreads: int = 0, SmallDepths=None, NoFlux=None) -> int:
+    """One FP64 oracle step of one property, in place.  Returns the status code.
+    NoFlux: (NoFluxU, NoFluxV, NoFluxW) int32 Size-box masks, or None."""
     assert P.dtype == np.float64 and P.flags.c_contiguous and P.shape == dom.shape3
-    cd = cdomain(dom, SmallDepths)
+    cd = cdomain(dom, SmallDepths, NoFlux)
     return lib().ora_step_f64(C.byref(cd), _p(P), _p(ReferenceProp), C.byref(p),
                               work.ptr if work is not None else None, nthreads)
 

@@ -186,7 +186,7 @@ def _dif_flux_z(Fl, Kz, DUX, DVY, DZZ, Pl, CW, wgt, ni, nj, nk):
                         (Pl[k][j][i] - Pl[k - 1][j][i])
 
 
-def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
+def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
     `p` is a dict of AdvectionDiffusion scalar arguments.  With CellFluxes set
     and a dict `fluxes`, the six face-flux arrays are stored in it."""
@@ -208,6 +208,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
     K, J, I = nk + 2, nj + 2, ni + 2
     z3 = lambda v: [[[v] * I for _ in range(J)] for _ in range(K)]
     Kx, Ky, Kz = z3(NULL_REAL), z3(NULL_REAL), z3(NULL_REAL)
+    NFU, NFV, NFW = (m.tolist() for m in NoFlux) if NoFlux is not None else (None, None, None)
+    no_adv = bool(p.get("NoAdvFlux"))
     for k in range(2, nk + 1):
         for j in range(1, nj + 1):
             for i in range(1, ni + 1):
@@ -221,11 +223,15 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
                 if CU[k][j][i] == 1:
                     Kx[k][j][i] = p["schmidt_H"] * (VH[k][j][i] * DUX[j - 1][i] + VH[k][j - 1][i] * DUX[j][i]) \
                         / (DUX[j][i] + DUX[j - 1][i])
+                    if p.get("NoDifFlux") and NFU[k][j][i] == 1:
+                        Kx[k][j][i] = 0.0
                     if p["NullDif"] and Qx[k][j][i] == 0.0:
                         Kx[k][j][i] = 0.0
                 if CV[k][j][i] == 1:
                     Ky[k][j][i] = p["schmidt_H"] * (VH[k][j][i] * DVY[j][i - 1] + VH[k][j][i - 1] * DVY[j][i]) \
                         / (DVY[j][i] + DVY[j][i - 1])
+                    if p.get("NoDifFlux") and NFV[k][j][i] == 1:
+                        Ky[k][j][i] = 0.0
                     if p["NullDif"] and Qy[k][j][i] == 0.0:
                         Ky[k][j][i] = 0.0
     D, E, F, TI = z3(0.0), z3(1.0), z3(0.0), z3(0.0)
@@ -291,6 +297,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
                                   [DUX[j + n][i] for n in (-2, -1, 0, 1)], DT, q,
                                   p["VolumeRelMax"], mH, lH, nb, u2H)
                         XC[k][j][i], XD[k][j][i], XE[k][j][i], XF[k][j][i] = (q * c for c in cf)
+                    if no_adv and NFU[k][j][i] == 1:             # AD:4434-4443
+                        XC[k][j][i] = XD[k][j][i] = XE[k][j][i] = XF[k][j][i] = 0.0
         for k in range(1, nk + 1):
             for j in range(1, nj + 1):
                 for i in range(1, ni + 1):
@@ -321,6 +329,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
                                       [DVY[j][i + n] for n in (-2, -1, 0, 1)], DT, q,
                                       p["VolumeRelMax"], mH, lH, nb, u2H)
                             YC[k][j][i], YD[k][j][i], YE[k][j][i], YF[k][j][i] = (q * c for c in cf)
+                        if no_adv and NFV[k][j][i] == 1:         # AD:4804-4813
+                            YC[k][j][i] = YD[k][j][i] = YE[k][j][i] = YF[k][j][i] = 0.0
             for k in range(1, nk + 1):
                 for j in range(1, nj + 1):
                     for i in range(1, ni + 1):
@@ -354,6 +364,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
                     sd = SD is not None and SD[j][i] != 0
                     if CW[k][j][i] == 1 and not sd:
                         auxk = Kz[k][j][i] * DUX[j][i] * DVY[j][i] / DZZ[k - 1][j][i]
+                        if p.get("NoDifFlux") and NFW[k][j][i] == 1:   # AD:2741-2745
+                            auxk = 0.0
                         a1 = auxk * DT / V[k - 1][j][i]
                         a2 = auxk * DT / V[k][j][i]
                         dP = Pl[k][j][i] - Pl[k - 1][j][i]
@@ -380,6 +392,10 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None):
                                       [DWZ[k + n][j][i] for n in (-2, -1, 0, 1)], DT, q,
                                       p["VolumeRelMax"], mV, lV, nb, u2V)
                             ZC[k][j][i], ZD[k][j][i], ZE[k][j][i], ZF[k][j][i] = (q * c for c in cf)
+                    if no_adv:                                     # AD:3004-3013
+                        for k in range(max(KF[j][i], 0), nk + 1):
+                            if NFW[k][j][i] == 1:
+                                ZC[k][j][i] = ZD[k][j][i] = ZE[k][j][i] = ZF[k][j][i] = 0.0
             if p["ImpExp_AdvV"] == 0.0:
                 for k in range(1, nk + 1):
                     for j in range(1, nj + 1):

@@ -73,3 +73,13 @@ def boundary_flux(d, P_old, P_new, ref, DT, decay_time=0.0, gross=False):
     if gross:
         return float(np.sum(gain[sel])), float(np.sum(np.abs(gain[sel])))
     return float(np.sum(gain[sel]))
+
+
+def noflux_masks(d, frac=0.3, seed=0):
+    """Seeded NoFluxU/V/W masks (int32, Size box) over a fraction of the compute faces."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in ("ComputeFacesU3D", "ComputeFacesV3D", "ComputeFacesW3D"):
+        cf = d.arrays[n]
+        out.append(((cf == 1) & (rng.random(cf.shape) < frac)).astype(np.int32))
+    return tuple(out)

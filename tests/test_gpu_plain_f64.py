@@ -160,6 +160,35 @@ def test_gpu_cell_fluxes_match_oracle(gpu, grid, opt):
     ad.kill()
 
 
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open"])
+@pytest.mark.parametrize("flags", [dict(NoAdvFlux=1), dict(NoDifFlux=1), dict(NoAdvFlux=1, NoDifFlux=1)])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "explicit_v_tvd", "theta_difv", "implicit_xx"])
+def test_gpu_noflux_masks(gpu, grid, flags, opt):
+    from tests.cases import noflux_masks
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=4)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    nf = noflux_masks(d, seed=5)
+    pd = dict(DTProp=30.0, CellFluxes=1, **flags, **OPTIONS[opt])
+    Po = P0.copy()
+    work = O.Work(d)
+    assert O.step(d, Po, O.params(**pd), ReferenceProp=R, work=work, NoFlux=nf) == 0
+    fo = O.cell_fluxes(d, work)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    with pytest.raises(advdiff.N.MohidAdError) as ei:        # the masks are required
+        ad.step(P0.copy(), advdiff.params(**pd), R)
+    assert ei.value.code == 9
+    ad.set_noflux(nf)
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(**pd), R)
+    fg = ad.cell_fluxes()
+    ad.kill()
+    assert np.array_equal(Pg, Po)
+    for n in O.FLUX_NAMES:
+        assert np.array_equal(fg[n], fo[n]), n
+
+
 def test_gpu_boundary_condition_rules(gpu):
     d = domain("open")
     P = d.tracer(4, 1.0, 0.0, seed=1)
@@ -265,7 +294,7 @@ def test_gpu_zero_pivot_reported(gpu):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 4), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9), (dict(AdvectionNudging=1), 4),
 ])
 def test_gpu_rejects_options_like_oracle(gpu, bad, code):
     d = domain("coast")

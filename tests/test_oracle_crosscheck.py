@@ -78,3 +78,27 @@ def test_cell_fluxes_c_equals_python(built, grid, opt):
     assert np.array_equal(Pc, Pp)
     for n in O.FLUX_NAMES:
         assert np.array_equal(fc[n], fp[n]), n
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open"])
+@pytest.mark.parametrize("flags", [dict(NoAdvFlux=1), dict(NoDifFlux=1), dict(NoAdvFlux=1, NoDifFlux=1)])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "explicit_v_tvd", "theta_difv"])
+def test_noflux_c_equals_python(built, grid, flags, opt):
+    from tests.cases import noflux_masks
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=4)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    nf = noflux_masks(d, seed=5)
+    pd = dict(O.DEFAULTS, DTProp=30.0, CellFluxes=1, **flags, **OPTIONS[opt])
+    Pc, Pp = P0.copy(), P0.copy()
+    work = O.Work(d)
+    assert O.step(d, Pc, O.params(**pd), ReferenceProp=R, work=work, NoFlux=nf) == 0
+    fp = {}
+    ref_py.step(d, Pp, pd, ReferenceProp=R, fluxes=fp, NoFlux=nf)
+    assert np.array_equal(Pc, Pp)
+    fc = O.cell_fluxes(d, work)
+    for n in O.FLUX_NAMES:
+        assert np.array_equal(fc[n], fp[n]), n
+    Q = P0.copy()                                   # the masks change the step
+    assert O.step(d, Q, O.params(**dict(pd, NoAdvFlux=0, NoDifFlux=0)), ReferenceProp=R) == 0
+    assert not np.array_equal(Q, Pc)

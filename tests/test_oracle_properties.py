@@ -143,6 +143,21 @@ def test_cell_fluxes_close_each_cell_budget(built, grid, opt):
     assert np.abs(net[wp]).max() > 1e-6 * scale / 30.0         # the fluxes are not all zero
 
 
+def test_noflux_everywhere_freezes_static_field(built):
+    # every face masked for advection and diffusion, static volumes: the step
+    # is VolumeVariation alone, P * VOld / V = P
+    d = domain("coast")
+    P = d.tracer(3, 1.0, 0.5, seed=6)
+    P0 = P.copy()
+    ones = tuple(np.ones(d.shape3, dtype=np.int32) for _ in range(3))
+    p = O.params(DTProp=30.0, NoAdvFlux=1, NoDifFlux=1, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1)
+    assert O.step(d, P, p, NoFlux=ones) == 0
+    wp = d.water_mask()
+    assert np.array_equal(P[wp], P0[wp])
+    # the masks are required when the flags are set
+    assert O.step(d, P.copy(), p) == 9
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
@@ -214,7 +229,7 @@ def test_land_and_halo_handling(built):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 4), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9), (dict(AdvectionNudging=1), 4),
 ])
 def test_rejected_options(built, bad, code):
     d = domain("coast")
