@@ -363,6 +363,19 @@ int mohid_ad_batched_sync(const int* bid, int* stat);
 
 int mohid_ad_batched_destroy(int* bid, int* stat);
 
+/* ---- test hooks (no counterpart in the reference; failure detection is
+ * tested by injecting on the host and by waits that run out, never by a GPU
+ * fault) */
+
+/* The *after-th device allocation from now fails with MOHID_AD_ERR_ALLOC
+ * (0: off), to exercise the cleanup of every allocating entry point. */
+int mohid_ad_debug_fail_alloc(const int* after, int* stat);
+
+/* Runs the step kernels' bounded stage wait on a barrier that nothing
+ * completes, for *polls polls: returns MOHID_AD_ERR_TIMEOUT, the status a
+ * step reports when a stage never arrives. */
+int mohid_ad_debug_wait_probe(const int* polls, int* stat);
+
 /* ======================================================================== */
 /* Ensemble: many independent batched domains in one launch                  */
 /* ======================================================================== */

@@ -40,6 +40,8 @@ int ok(int* stat)
     return MOHID_AD_SUCCESS;
 }
 
+int g_fail_alloc = 0;
+
 void Instance::release()
 {
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
@@ -569,6 +571,14 @@ int mohid_ad_get_dif_flux(const int* id, double* DifFluxX, double* DifFluxY, dou
                           const int* on_device, int* stat)
 {
     return get_fluxes(id, 3, DifFluxX, DifFluxY, DifFluxZ, on_device, stat);
+}
+
+int mohid_ad_debug_fail_alloc(const int* after, int* stat)
+{
+    if (!after) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*after < 0) return fail(MOHID_AD_ERR_BOUNDS, stat, "after must be >= 0");
+    g_fail_alloc = *after;
+    return ok(stat);
 }
 
 int mohid_ad_kill(int* id, int* stat)

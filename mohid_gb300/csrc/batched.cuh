@@ -127,6 +127,8 @@ size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
 // open: some member has reference concentrations (open-boundary instantiation)
 cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
                             int nt, int method, int limiter, bool open, cudaStream_t s);
+// test hook: a bounded stage wait that nothing completes (status: MOHID_DEV_TIMEOUT)
+cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s);
 // resident CTAs of the ensemble kernel on `device` (0 on error)
 int ensemble_slots(int nt, int method, int limiter, int device);
 // box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order

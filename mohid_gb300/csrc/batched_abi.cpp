@@ -1021,6 +1021,23 @@ int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
     return ok(stat);
 }
 
+int mohid_ad_debug_wait_probe(const int* polls, int* stat)
+{
+    if (!polls) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*polls < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "polls must be >= 1");
+    unsigned* d = nullptr;
+    unsigned h = 0;
+    cudaError_t e = cudaMalloc((void**)&d, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = mohid::wait_probe((unsigned)*polls, d, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("wait probe", e));
+    std::string why;
+    const int code = status_to_code(h, why);
+    return code ? fail(code, stat, why) : ok(stat);
+}
+
 int mohid_ad_batched_boundary_flux(const int* bid, const int* t, double* flux, int* stat)
 {
     Batch* b = blookup(bid);

@@ -24,6 +24,21 @@ __global__ void k_tile_cost(const uint8_t* cflag, const int* kfloor, BLayout L, 
     cost[tile] = kmin <= L.nk ? L.nk - kmin + 1 : 0;
 }
 
+// The step kernels' bounded stage wait, on a barrier that nothing completes:
+// it gives up after `polls` polls, and the CTA reports MOHID_DEV_TIMEOUT as
+// the step's exit path does when a stage never arrives.
+__global__ void k_wait_probe(uint32_t polls, unsigned* status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0, polls);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(status, MOHID_DEV_TIMEOUT);
+}
+
 template <int NT>
 size_t smem_n(bool halfQ, bool halfK, int nk)
 {
@@ -33,6 +48,12 @@ size_t smem_n(bool halfQ, bool halfK, int nk)
 }
 
 }  // namespace
+
+cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s)
+{
+    k_wait_probe<<<1, 32, 0, s>>>(polls, status);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_batched_closed(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
                                   bool halfK, const int2* tiles, int ntl, cudaStream_t s)

@@ -15,6 +15,10 @@ int fail(int code, int* stat, const std::string& msg);
 int ok(int* stat);
 std::string cuda_msg(const char* what, cudaError_t e);
 
+// test hook (mohid_ad_debug_fail_alloc): when > 0, counts device
+// allocations down and fails the one that reaches zero
+extern int g_fail_alloc;
+
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -22,6 +26,7 @@ struct DevBuf {
     cudaError_t alloc(size_t count)
     {
         n = count;
+        if (g_fail_alloc > 0 && --g_fail_alloc == 0) { p = nullptr; return cudaErrorMemoryAllocation; }
         cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
         if (e == cudaSuccess) e = cudaMemset(p, 0, sizeof(T) * (count ? count : 1));
         return e;
