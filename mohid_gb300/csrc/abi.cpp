@@ -336,6 +336,7 @@ int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize, const
                   const double* DVY, const double* DZX, const double* DZY, const int* KFloorZ,
                   const int* BoundaryPoints2D, int* stat)
 {
+    TraceRange trace_("mohid_ad_init");
     if (!id || !size || !worksize || !DUX || !DVY || !DZX || !DZY || !KFloorZ || !BoundaryPoints2D)
         return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_ad_init: NULL argument");
     const T_Size3D& s = *size;
@@ -417,6 +418,7 @@ int mohid_ad_set_hydro(const int* id, const double* Wflux_X, const double* Wflux
                        const int* ComputeFacesU3D, const int* ComputeFacesV3D,
                        const int* ComputeFacesW3D, const int* SmallDepths, int* stat)
 {
+    TraceRange trace_("mohid_ad_set_hydro");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     return upload_hydro(in, false, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
@@ -433,6 +435,7 @@ int mohid_ad_set_hydro_dev(const int* id, const double* Wflux_X, const double* W
                            const int* ComputeFacesV3D, const int* ComputeFacesW3D,
                            const int* SmallDepths, int* stat)
 {
+    TraceRange trace_("mohid_ad_set_hydro_dev");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     return upload_hydro(in, true, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
@@ -443,6 +446,7 @@ int mohid_ad_set_hydro_dev(const int* id, const double* Wflux_X, const double* W
 int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PROP_out,
                                const double* ReferenceProp, const mohid_ad_params* p, int* stat)
 {
+    TraceRange trace_("mohid_ad_step_prop_f64_dev");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     if (!PROP_in || !PROP_out) return fail(MOHID_AD_ERR_NULLPTR, stat, "PROP pointer is NULL");
@@ -458,6 +462,7 @@ int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PRO
 int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceProp,
                            const mohid_ad_params* p, int* stat)
 {
+    TraceRange trace_("mohid_ad_step_prop_f64");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     if (!PROP) return fail(MOHID_AD_ERR_NULLPTR, stat, "PROP is NULL");
@@ -489,6 +494,7 @@ int mohid_ad_step_f64(const int* id, double* PROP, const mohid_ad_params* p, con
                       const int* ComputeFacesV3D, const int* ComputeFacesW3D,
                       const int* SmallDepths, const double* ReferenceProp, int* stat)
 {
+    TraceRange trace_("mohid_ad_step_f64");
     int code = mohid_ad_set_hydro(id, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H,
                                   Diff_V, AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D,
                                   WaterPoints3D, ComputeFacesU3D, ComputeFacesV3D,
@@ -499,6 +505,7 @@ int mohid_ad_step_f64(const int* id, double* PROP, const mohid_ad_params* p, con
 
 int mohid_ad_sync(const int* id, int* stat)
 {
+    TraceRange trace_("mohid_ad_sync");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     CK(cudaSetDevice(in->device));
@@ -583,6 +590,7 @@ int mohid_ad_debug_fail_alloc(const int* after, int* stat)
 
 int mohid_ad_kill(int* id, int* stat)
 {
+    TraceRange trace_("mohid_ad_kill");
     Instance* in = nullptr;
     if (id) {
         std::lock_guard<std::mutex> lk(g_mu);

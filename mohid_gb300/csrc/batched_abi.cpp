@@ -677,6 +677,7 @@ extern "C" {
 
 int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_create");
     if (!bid || !ntracers || !storage) return fail(MOHID_AD_ERR_NULLPTR, stat, "mohid_ad_batched_create: NULL argument");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown plain instance id");
@@ -765,6 +766,7 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
 
 int mohid_ad_batched_pack_hydro(const int* bid, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_pack_hydro");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     CK(cudaSetDevice(b->in->device));
@@ -773,6 +775,7 @@ int mohid_ad_batched_pack_hydro(const int* bid, int* stat)
 
 int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP, const int* on_device, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_set_tracer");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -823,6 +826,7 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
 
 int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, const int* on_device, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_get_tracer");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -844,6 +848,7 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
 int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
                                    const int* on_device, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_set_reference");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !ReferenceProp || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -873,6 +878,7 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
 int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
                           int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_step");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!nsteps || !use_graph) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -947,6 +953,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
 
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_autotune");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!p) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -1000,6 +1007,7 @@ int mohid_ad_batched_set_mass_fix(const int* bid, const int* on, int* stat)
 
 int mohid_ad_batched_mass(const int* bid, const int* t, double* mass, int* stat)
 {
+    TraceRange trace_("mohid_ad_batched_mass");
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !mass) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
@@ -1142,6 +1150,7 @@ int mohid_ad_ensemble_create(int* eid, const int* nmembers, const int* bids, int
 int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* nsteps, const int* use_graph,
                            int* stat)
 {
+    TraceRange trace_("mohid_ad_ensemble_step");
     Ensemble* E = elookup(eid);
     if (!E) return fail(MOHID_AD_ERR_ID, stat, "unknown ensemble id");
     if (!p || !nsteps || !use_graph) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");

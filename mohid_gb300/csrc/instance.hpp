@@ -1,6 +1,7 @@
 // instance.hpp -- internal state shared by the C-ABI translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <map>
 #include <mutex>
@@ -74,6 +75,15 @@ struct Instance {
 };
 
 Instance* lookup(const int* id);
+
+// NVTX range around one C-ABI call (a profiler shows each entry point's span;
+// without a tool attached the calls do nothing)
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 #define CK(call)                                                                  \
     do {                                                                          \
