@@ -68,6 +68,8 @@ struct Batch {
     int graphSched = -1, graphSplit = -1;
     int graphFix = -1;                   // fixer / open-boundary launches the graph holds
     bool graphLast = false;              // the graph ends with the call's last step
+    unsigned graphPack = ~0u;            // packed hydrodynamics the graph's arguments hold
+                                         // (FP16 scales, tile count)
     // asynchronous repack of a new hydrodynamic state (on the instance's
     // stream) and tracer loads (on their own stream, with their own scratch),
     // so that the two overlap; the host-side results of the repack are read
@@ -921,6 +923,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
                            b->graphSched == b->sched && b->graphSplit == b->split &&
                            b->graphFix == fix_key(b) && b->graphLast == glast &&
+                           b->graphPack == b->packedVersion &&
                            std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
         if (!reuse) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -944,6 +947,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphSplit = b->split;
             b->graphFix = fix_key(b);
             b->graphLast = glast;
+            b->graphPack = b->packedVersion;
         }
         CK(cudaGraphLaunch(b->graph, s));
     }

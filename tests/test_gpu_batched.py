@@ -161,3 +161,34 @@ def test_batched_rejects_unsupported(gpu, bad):
         b.step(advdiff.params(DTProp=30.0, **bad))
     assert ei.value.code == 4
     b.destroy(); ad.kill()
+
+
+@pytest.mark.parametrize("storage", [0, 1, 2])
+def test_graph_rebuilt_after_new_hydrodynamics(gpu, storage):
+    """A graph captured under one hydrodynamic state is not reused under the
+    next (its arguments hold the FP16 scales and the tile count): graph and
+    direct stepping agree bit for bit across a change of state."""
+    from mohid_gb300 import synth
+    d = domain("coast")
+    arrays = dict(d.arrays)
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z"):
+        arrays[n] = d.arrays[n] * 0.5                    # divergence-free still
+    d2 = synth.Domain(spec=d.spec, arrays=arrays)
+    P = d.tracer(3, 1.0, 0.5, seed=1)
+    pd = advdiff.params(DTProp=30.0, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1)
+    out = {}
+    for graph in (True, False):
+        ad = advdiff.AdvectionDiffusion(d)
+        ad.set_hydro()
+        b = batched.Batch(ad, 1, storage)
+        b.set_tracer(0, P)
+        b.step(pd, nsteps=4, graph=graph)
+        ad.set_hydro(d2)
+        b.step(pd, nsteps=4, graph=graph)
+        ad.set_hydro(d)
+        b.step(pd, nsteps=4, graph=graph)
+        b.sync()
+        out[graph] = b.get_tracer(0)
+        b.destroy()
+        ad.kill()
+    assert np.array_equal(out[True], out[False])
