@@ -44,7 +44,7 @@ extern "C" {
 #define MOHID_AD_ERR_BOUNDS       1   /* inconsistent Size/WorkSize bounds or array extents      */
 #define MOHID_AD_ERR_ID           2   /* unknown / dead instance id (reference: ready_ /= IDLE)  */
 #define MOHID_AD_ERR_OPTION       3   /* option combination the reference rejects with `stop`   */
-#define MOHID_AD_ERR_UNSUPPORTED  4   /* option of the reference this build does not implement  */
+#define MOHID_AD_ERR_UNSUPPORTED  4   /* option of the reference this library does not implement */
 #define MOHID_AD_ERR_CUDA         5   /* CUDA runtime error (message via mohid_ad_last_error)    */
 #define MOHID_AD_ERR_ZERO_PIVOT   6   /* THOMASZ pivot |E + D*W| == 0 in some water column       */
 #define MOHID_AD_ERR_NONFINITE    7   /* a solved concentration is Inf/NaN                       */
@@ -105,7 +105,7 @@ typedef struct mohid_ad_params {
     int    NullDif;               /* LOGICAL                                          */
     int    BoundaryCondition;     /* MOHID_BC_*; 4 and 8 also act without a reference */
     double DecayTime;             /* [s]                                              */
-    int    AdvectionNudging;      /* LOGICAL, must be .false. in this build           */
+    int    AdvectionNudging;      /* LOGICAL, must be .false. (not implemented)       */
     int    AdvectionNudgingCells;
     int    CellFluxes;            /* LOGICAL: record the face fluxes (plain form)     */
     int    NoAdvFlux, NoDifFlux;  /* LOGICAL: use the NoFlux masks (plain form)        */

@@ -75,7 +75,7 @@ std::string cuda_msg(const char* what, cudaError_t e)
 
 
 // Option checks of AdvectionDiffusion (AD:1231-1239, AD:1340-1349,
-// Set_Internal_State AD:5816-5830) plus the options this build leaves out.
+// Set_Internal_State AD:5816-5830) plus the options this library leaves out.
 int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why)
 {
     if (!p) { why = "params is NULL"; return MOHID_AD_ERR_NULLPTR; }
