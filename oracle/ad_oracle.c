@@ -176,6 +176,8 @@ static int advection_line(int flo, int fhi, double dt, const double* du, size_t 
     return 0;
 }
 
+static int disch_valid(const ora_domain* d);
+
 static int validate(const ora_domain* d, const double* PROP, const mohid_ad_params* p,
                     const double* ReferenceProp)
 {
@@ -195,6 +197,7 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     if ((p->ImpExp_AdvXX != 0. && p->ImpExp_AdvXX != 1.) || (p->ImpExp_AdvYY != 0. && p->ImpExp_AdvYY != 1.))
         return MOHID_AD_ERR_OPTION;
     if (p->AdvectionNudging) return MOHID_AD_ERR_UNSUPPORTED;
+    if (!disch_valid(d)) return MOHID_AD_ERR_BOUNDS;
     /* the reference reads NoFluxU/V/W whenever NoAdvFlux or NoDifFlux is set */
     if ((p->NoAdvFlux || p->NoDifFlux) && (!d->NoFluxU || !d->NoFluxV || !d->NoFluxW)) return MOHID_AD_ERR_NULLPTR;
     if (p->Docycle_method != 1 && p->Docycle_method != 2) return MOHID_AD_ERR_OPTION;
@@ -429,6 +432,76 @@ static void cell_dif_flux_z(const ora_domain* d, double wgt, const double* Kz, c
             }
 }
 
+#define ORA_FILL_INT (-9999999)   /* FillValueInt, ModuleGlobalData.F90:131 */
+#define ORA_DISCH_UNIFORM 5       /* DischUniform_, ModuleGlobalData.F90:1006 */
+
+/* the discharge cells' layer range: the given layer, or for a uniform
+ * vertical distribution Kmin..Kmax with "not given" read as KFloorZ and KUB */
+static void disch_layers(const ora_domain* d, int dis, int n, int* kmin, int* kmax)
+{
+    const ora_discharges* q = d->Disch;
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    if (q->vert[dis] == ORA_DISCH_UNIFORM) {
+        *kmin = q->Kmin[n] == ORA_FILL_INT ? d->KFloorZ[I2(q->I[n], q->J[n])] : q->Kmin[n];
+        *kmax = q->Kmax[n] == ORA_FILL_INT ? d->nk : q->Kmax[n];
+    } else {
+        *kmin = *kmax = q->K[n];
+    }
+}
+
+/* cells of the work box, layers 1..KUB (the reference does not check) */
+static int disch_valid(const ora_domain* d)
+{
+    const ora_discharges* q = d->Disch;
+    if (!q) return 1;
+    if (q->number < 0 || (q->number > 0 && (!q->nCells || !q->ignore || !q->bypass || !q->vert))) return 0;
+    int n = 0;
+    for (int dis = 0; dis < q->number; ++dis) {
+        if (q->ignore[dis]) continue;
+        for (int nc = 0; nc < q->nCells[dis]; ++nc, ++n) {
+            if (q->I[n] < 1 || q->I[n] > d->ni || q->J[n] < 1 || q->J[n] > d->nj) return 0;
+            int kmin, kmax;
+            disch_layers(d, dis, n, &kmin, &kmax);
+            if (kmin < 1 || kmax > d->nk) return 0;
+        }
+    }
+    return 1;
+}
+
+/* Discharges, AD:4025-4128: after VolumeVariation, each discharge cell adds
+ * its inflow to TI, or a withdrawal to E (times DischConcMF); a uniform
+ * discharge spreads its flow over Kmin..Kmax by layer thickness.  A closed
+ * cell takes the inflow over the old mass.  In the reference's order. */
+static void discharges(const ora_domain* d, const double* P, double* TI, double* E, double DT)
+{
+    const ora_discharges* q = d->Disch;
+    ora_ext X = {d->ni + 2, d->nj + 2, d->nk + 2, 0, 0};
+    int n = 0;
+    for (int dis = 0; dis < q->number; ++dis) {
+        if (q->ignore[dis]) continue;
+        const int uniform = q->vert[dis] == ORA_DISCH_UNIFORM;
+        for (int nc = 0; nc < q->nCells[dis]; ++nc, ++n) {
+            const int i = q->I[n], j = q->J[n];
+            int kmin, kmax;
+            disch_layers(d, dis, n, &kmin, &kmax);
+            double WaterColumn = 0.0;
+            for (int k = kmin; k <= kmax; ++k) WaterColumn = WaterColumn + d->DWZ[I3(i, j, k)];
+            for (int k = kmin; k <= kmax; ++k) {
+                const size_t a = I3(i, j, k);
+                const double DT_V = DT / d->VolumeZ[a];
+                const double Flow = uniform ? q->Flow[n] * d->DWZ[a] / WaterColumn : q->Flow[n];
+                if (d->OpenPoints3D[a] == 1) {
+                    if (q->bypass[dis]) TI[a] = TI[a] + Flow * DT_V * q->Conc[n];
+                    else if (Flow > 0.) TI[a] = TI[a] + Flow * DT_V * q->Conc[n];
+                    else E[a] = E[a] - Flow * DT_V * q->ConcMF[n];
+                } else if (Flow > 0.) {
+                    TI[a] = P[a] * d->VolumeZOld[a] / d->VolumeZ[a] + Flow * DT_V * q->Conc[n];
+                }
+            }
+        }
+    }
+}
+
 /* NoAdvFlux: the face coefficients of the masked faces of the work box are
  * zeroed after their lines are formed (AD:4434-4443, AD:4804-4813); from
  * KFloorZ for the vertical ones, on columns open at KUB (AD:3004-3013) */
@@ -578,6 +651,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                 }
             }
     }
+    if (d->Disch) discharges(d, P, w.TI, w.E, DT);   /* AD:1702 */
 
     if (!p->Vertical1D) {
         /* HorizontalDiffusionXX, AD:5156-5214: OMP DO k / do j / do i */

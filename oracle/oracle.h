@@ -28,6 +28,18 @@
 extern "C" {
 #endif
 
+/* SetDischarges (ModuleAdvectionDiffusion.F90:978-1030): per discharge
+ * (number of them) its cell count, IgnoreDisch, ByPass and DischVert; per
+ * discharge cell of the discharges not ignored, in order, its work-box
+ * indices I, J, K, Kmin, Kmax (FillValueInt = -9999999 for "not given"),
+ * DischFlow, DischConc and DischConcMF. */
+typedef struct ora_discharges {
+    int number;
+    const int *nCells, *ignore, *bypass, *vert;
+    const int *I, *J, *K, *Kmin, *Kmax;
+    const double *Flow, *Conc, *ConcMF;
+} ora_discharges;
+
 typedef struct ora_domain {
     int ni, nj, nk;                    /* WorkSize upper bounds; lower bounds are 1 */
     /* 2-D, Size box (ni+2)*(nj+2) */
@@ -42,6 +54,7 @@ typedef struct ora_domain {
     const int *ComputeFacesU3D, *ComputeFacesV3D, *ComputeFacesW3D;
     const int *SmallDepths;            /* 2-D, may be NULL */
     const int *NoFluxU, *NoFluxV, *NoFluxW;   /* 3-D, may be NULL (NoAdvFlux / NoDifFlux) */
+    const ora_discharges* Disch;              /* may be NULL (no discharges) */
 } ora_domain;
 
 /* Work arrays of one instance (AllocateVariables, AD:537-684). */

@@ -25,6 +25,32 @@ _ip = C.POINTER(C.c_int)
 _fp = C.POINTER(C.c_float)
 
 
+class OraDischarges(C.Structure):
+    _fields_ = [("number", C.c_int)] + [(n, _ip) for n in ("nCells", "ignore", "bypass", "vert", "I", "J", "K",
+                                                          "Kmin", "Kmax")] + \
+        [(n, _dp) for n in ("Flow", "Conc", "ConcMF")]
+
+
+DISCH_FIELDS_INT = ("nCells", "ignore", "bypass", "vert", "I", "J", "K", "Kmin", "Kmax")
+DISCH_FIELDS_F64 = ("Flow", "Conc", "ConcMF")
+
+
+def discharges_struct(disch: dict) -> OraDischarges:
+    """SetDischarges arguments as numpy arrays: nCells, ignore, bypass, vert (per
+    discharge), I, J, K, Kmin, Kmax, Flow, Conc, ConcMF (per discharge cell)."""
+    q = OraDischarges()
+    q.number = len(disch["nCells"])
+    keep = {}
+    for n in DISCH_FIELDS_INT:
+        keep[n] = np.ascontiguousarray(disch[n], dtype=np.int32)
+        setattr(q, n, _p(keep[n], _ip))
+    for n in DISCH_FIELDS_F64:
+        keep[n] = np.ascontiguousarray(disch[n], dtype=np.float64)
+        setattr(q, n, _p(keep[n]))
+    q._keep = keep
+    return q
+
+
 class OraDomain(C.Structure):
     _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int)] + \
         [(n, _dp) for n in ("DUX", "DVY", "DZX", "DZY")] + \
@@ -33,7 +59,7 @@ class OraDomain(C.Structure):
                             "Diff_V", "AreaU", "AreaV", "DZZ", "DWZ")] + \
         [(n, _ip) for n in ("OpenPoints3D", "LandPoints3D", "WaterPoints3D", "ComputeFacesU3D",
                             "ComputeFacesV3D", "ComputeFacesW3D", "SmallDepths", "NoFluxU", "NoFluxV",
-                            "NoFluxW")]
+                            "NoFluxW")] + [("Disch", C.POINTER(OraDischarges))]
 
 
 class Params(C.Structure):
@@ -111,7 +137,7 @@ def _p(a, t=_dp):
     return None if a is None else a.ctypes.data_as(t)
 
 
-def cdomain(dom, SmallDepths=None, NoFlux=None) -> OraDomain:
+def cdomain(dom, SmallDepths=None, NoFlux=None, Disch=None) -> OraDomain:
     a = dom.arrays
     d = OraDomain()
     d.ni, d.nj, d.nk = dom.ni, dom.nj, dom.nk
@@ -124,7 +150,9 @@ def cdomain(dom, SmallDepths=None, NoFlux=None) -> OraDomain:
     d.SmallDepths = _p(SmallDepths, _ip)
     nf = NoFlux if NoFlux is not None else (None, None, None)
     d.NoFluxU, d.NoFluxV, d.NoFluxW = (_p(m, _ip) for m in nf)
-    d._keep = (dom, SmallDepths, NoFlux)
+    q = discharges_struct(Disch) if Disch is not None else None
+    d.Disch = C.pointer(q) if q is not None else None
+    d._keep = (dom, SmallDepths, NoFlux, q)
     return d
 
 
@@ -143,11 +171,11 @@ class Work:
 
 
 def step(dom, P: np.ndarray, p: Params, ReferenceProp=None, work: Work | None = None,
-         nthreads: int = 0, SmallDepths=None, NoFlux=None) -> int:
+         nthreads: int = 0, SmallDepths=None, NoFlux=None, Disch=None) -> int:
     """One FP64 oracle step of one property, in place.  Returns the status code.
     NoFlux: (NoFluxU, NoFluxV, NoFluxW) int32 Size-box masks, or None."""
     assert P.dtype == np.float64 and P.flags.c_contiguous and P.shape == dom.shape3
-    cd = cdomain(dom, SmallDepths, NoFlux)
+    cd = cdomain(dom, SmallDepths, NoFlux, Disch)
     return lib().ora_step_f64(C.byref(cd), _p(P), _p(ReferenceProp), C.byref(p),
                               work.ptr if work is not None else None, nthreads)
 

@@ -186,7 +186,7 @@ def _dif_flux_z(Fl, Kz, DUX, DVY, DZZ, Pl, CW, wgt, ni, nj, nk):
                         (Pl[k][j][i] - Pl[k - 1][j][i])
 
 
-def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=None):
+def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=None, Disch=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
     `p` is a dict of AdvectionDiffusion scalar arguments.  With CellFluxes set
     and a dict `fluxes`, the six face-flux arrays are stored in it."""
@@ -251,6 +251,36 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                         E[k][j][i] = 1.0 + (DT / V[k][j][i]) * Qz[k + 1][j][i]
                 else:
                     TI[k][j][i] = Pl[k][j][i]
+
+    # Discharges (AD:4025-4128)
+    if Disch is not None:
+        n = 0
+        for dis in range(len(Disch["nCells"])):
+            if Disch["ignore"][dis]:
+                continue
+            uniform = int(Disch["vert"][dis]) == 5
+            for _ in range(int(Disch["nCells"][dis])):
+                i, j = int(Disch["I"][n]), int(Disch["J"][n])
+                if uniform:
+                    kmin = KF[j][i] if int(Disch["Kmin"][n]) == -9999999 else int(Disch["Kmin"][n])
+                    kmax = nk if int(Disch["Kmax"][n]) == -9999999 else int(Disch["Kmax"][n])
+                else:
+                    kmin = kmax = int(Disch["K"][n])
+                wc = 0.0
+                for k in range(kmin, kmax + 1):
+                    wc = wc + DWZ[k][j][i]
+                flow0, conc, cmf = float(Disch["Flow"][n]), float(Disch["Conc"][n]), float(Disch["ConcMF"][n])
+                for k in range(kmin, kmax + 1):
+                    dtv = DT / V[k][j][i]
+                    flow = flow0 * DWZ[k][j][i] / wc if uniform else flow0
+                    if OP[k][j][i] == 1:
+                        if Disch["bypass"][dis] or flow > 0.0:
+                            TI[k][j][i] = TI[k][j][i] + flow * dtv * conc
+                        else:
+                            E[k][j][i] = E[k][j][i] - flow * dtv * cmf
+                    elif flow > 0.0:
+                        TI[k][j][i] = Pl[k][j][i] * Vo[k][j][i] / V[k][j][i] + flow * dtv * conc
+                n += 1
 
     mH, lH, u2H = p["AdvMethodH"], p["TVDLimitationH"], bool(p["Upwind2H"])
     if not p["Vertical1D"]:

@@ -83,3 +83,43 @@ def noflux_masks(d, frac=0.3, seed=0):
         cf = d.arrays[n]
         out.append(((cf == 1) & (rng.random(cf.shape) < frac)).astype(np.int32))
     return tuple(out)
+
+
+def discharges(d, seed=0, ndis=4, uniform=True, ignore_one=True):
+    """Seeded SetDischarges arguments over water columns: point discharges at a
+    layer, uniform ones over a layer range or the whole column (Kmin / Kmax not
+    given), inflows and withdrawals, a bypass, and an ignored discharge."""
+    rng = np.random.default_rng(seed)
+    a = d.arrays
+    cols = [(j, i) for j in range(1, d.nj + 1) for i in range(1, d.ni + 1)
+            if a["WaterPoints3D"][d.nk, j, i] == 1]
+    nCells, ignore, bypass, vert = [], [], [], []
+    I, J, K, Kmin, Kmax, Flow, Conc, CMF = ([] for _ in range(8))
+    for dis in range(ndis):
+        nc = int(rng.integers(1, 3))
+        ign = 1 if (ignore_one and dis == 1) else 0
+        nCells.append(nc)
+        ignore.append(ign)
+        bypass.append(1 if dis == 2 else 0)
+        vert.append(5 if (uniform and dis % 2 == 0) else 1)
+        if ign:
+            continue                         # the cells of an ignored discharge are not listed
+        for _ in range(nc):
+            j, i = cols[int(rng.integers(len(cols)))]
+            kf = int(a["KFloorZ"][j, i])
+            I.append(i)
+            J.append(j)
+            K.append(int(rng.integers(kf, d.nk + 1)))
+            if dis == 0:
+                Kmin.append(-9999999)
+                Kmax.append(-9999999)
+            else:
+                k0 = int(rng.integers(kf, d.nk + 1))
+                Kmin.append(k0)
+                Kmax.append(int(rng.integers(k0, d.nk + 1)))
+            Flow.append(float(rng.uniform(-2.0, 6.0)))
+            Conc.append(float(rng.uniform(0.5, 8.0)))
+            CMF.append(float(rng.uniform(0.5, 1.5)))
+    return dict(nCells=np.array(nCells), ignore=np.array(ignore), bypass=np.array(bypass), vert=np.array(vert),
+                I=np.array(I), J=np.array(J), K=np.array(K), Kmin=np.array(Kmin), Kmax=np.array(Kmax),
+                Flow=np.array(Flow), Conc=np.array(Conc), ConcMF=np.array(CMF))

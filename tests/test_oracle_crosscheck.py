@@ -102,3 +102,19 @@ def test_noflux_c_equals_python(built, grid, flags, opt):
     Q = P0.copy()                                   # the masks change the step
     assert O.step(d, Q, O.params(**dict(pd, NoAdvFlux=0, NoDifFlux=0)), ReferenceProp=R) == 0
     assert not np.array_equal(Q, Pc)
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "layer1"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "theta_difv", "implicit_xx"])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_discharges_c_equals_python(built, grid, opt, seed):
+    from tests.cases import discharges
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=2)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    ds = discharges(d, seed=seed)
+    pd = dict(O.DEFAULTS, DTProp=30.0, CellFluxes=1, **OPTIONS[opt])
+    Pc, Pp = P0.copy(), P0.copy()
+    assert O.step(d, Pc, O.params(**pd), ReferenceProp=R, Disch=ds) == 0
+    ref_py.step(d, Pp, pd, ReferenceProp=R, Disch=ds)
+    assert np.array_equal(Pc, Pp)

@@ -158,6 +158,47 @@ def test_noflux_everywhere_freezes_static_field(built):
     assert O.step(d, P.copy(), p) == 9
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_discharge_mass_budget(built, seed):
+    # closed domain, static volumes, discharges into open cells: the mass
+    # changes by the inflows (flow * DT * concentration, bypasses included) and
+    # the withdrawals (flow * DT * DischConcMF * new value)
+    from tests.cases import discharges
+    d = domain("zlevel")
+    ds = discharges(d, seed=seed)
+    P = d.tracer(3, 1.0, 0.5, seed=7)
+    P0 = P.copy()
+    assert O.step(d, P, O.params(DTProp=30.0, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1), Disch=ds) == 0
+    a = d.arrays
+    dm, n = 0.0, 0
+    for dis in range(len(ds["nCells"])):
+        if ds["ignore"][dis]:
+            continue
+        for _ in range(ds["nCells"][dis]):
+            i, j = ds["I"][n], ds["J"][n]
+            if ds["vert"][dis] == 5:
+                k0 = a["KFloorZ"][j, i] if ds["Kmin"][n] == -9999999 else ds["Kmin"][n]
+                k1 = d.nk if ds["Kmax"][n] == -9999999 else ds["Kmax"][n]
+            else:
+                k0 = k1 = ds["K"][n]
+            wc = sum(a["DWZ"][k, j, i] for k in range(k0, k1 + 1))
+            for k in range(k0, k1 + 1):
+                assert a["OpenPoints3D"][k, j, i] == 1
+                flow = ds["Flow"][n] * (a["DWZ"][k, j, i] / wc if ds["vert"][dis] == 5 else 1.0)
+                if ds["bypass"][dis] or flow > 0:
+                    dm += flow * 30.0 * ds["Conc"][n]
+                else:
+                    dm += flow * 30.0 * ds["ConcMF"][n] * P[k, j, i]
+            n += 1
+    m0, m1 = O.mass(d, P0), O.mass(d, P)
+    assert abs((m1 - m0) - dm) <= 1e-12 * abs(m0)
+    assert abs(dm) > 1e-9 * abs(m0)
+    # discharge cells outside the work box are rejected
+    bad = dict(ds, I=ds["I"].copy())
+    bad["I"][0] = d.ni + 1
+    assert O.step(d, P0.copy(), O.params(DTProp=30.0), Disch=bad) == 1
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
