@@ -182,6 +182,25 @@ int mohid_ad_step_prop_f64(const int* id, double* PROP, const double* ReferenceP
                            const mohid_ad_params* p, int* stat);
 
 /*
+ * SetDischarges / UnSetDischarges (ModuleAdvectionDiffusion.F90:978-1075):
+ * point sources applied by the following steps right after VolumeVariation
+ * (AD:4025-4128).  Per discharge (*DischNumber of them): DischnCells,
+ * IgnoreDisch, ByPass (LOGICAL as int) and DischVert (5 = DischUniform_:
+ * the flow is spread over layers Kmin..Kmax by thickness, -9999999 =
+ * FillValueInt reads as KFloorZ / KUB; any other value: layer DischK).  Per
+ * cell of the discharges not ignored, in order: DischI, DischJ, DischK,
+ * DischKmin, DischKmax (work-box indices), DischFlow, DischConc, DischConcMF.
+ * The arguments are copied.  Cells outside the work box or layers outside
+ * 1..KUB return MOHID_AD_ERR_BOUNDS.  DischConc is per property, so call it
+ * before each property's step as WP does.
+ */
+int mohid_ad_set_discharges(const int* id, const int* DischNumber, const int* DischnCells, const int* IgnoreDisch,
+                            const int* ByPass, const int* DischVert, const int* DischI, const int* DischJ,
+                            const int* DischK, const int* DischKmin, const int* DischKmax, const double* DischFlow,
+                            const double* DischConc, const double* DischConcMF, int* stat);
+int mohid_ad_unset_discharges(const int* id, int* stat);
+
+/*
  * The NoFluxU / NoFluxV / NoFluxW masks of AdvectionDiffusion's optional
  * arguments (Size-box int arrays, host).  Steps with p->NoAdvFlux zero the
  * advection coefficients of masked faces, and steps with p->NoDifFlux their

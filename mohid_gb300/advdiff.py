@@ -94,6 +94,21 @@ class AdvectionDiffusion:
             C.c_void_p(Ref.data_ptr()) if Ref is not None else None, C.byref(p), C.byref(st))
         N.check(rc, "mohid_ad_step_prop_f64_dev")
 
+    def set_discharges(self, disch: dict | None):
+        """SetDischarges (mohid_ad_set_discharges) from numpy arrays: nCells, ignore,
+        bypass, vert per discharge; I, J, K, Kmin, Kmax, Flow, Conc, ConcMF per
+        discharge cell.  None: UnSetDischarges."""
+        st = C.c_int(0)
+        if disch is None:
+            N.check(self.lib.mohid_ad_unset_discharges(C.byref(self._id), C.byref(st)), "mohid_ad_unset_discharges")
+            return
+        ints = [np.ascontiguousarray(disch[n], dtype=np.int32)
+                for n in ("nCells", "ignore", "bypass", "vert", "I", "J", "K", "Kmin", "Kmax")]
+        dbls = [np.ascontiguousarray(disch[n], dtype=np.float64) for n in ("Flow", "Conc", "ConcMF")]
+        rc = self.lib.mohid_ad_set_discharges(C.byref(self._id), C.byref(C.c_int(len(ints[0]))),
+                                              *(a.ctypes.data_as(C.c_void_p) for a in ints + dbls), C.byref(st))
+        N.check(rc, "mohid_ad_set_discharges")
+
     def set_noflux(self, masks):
         """NoFluxU/V/W masks (int32 Size-box arrays) for NoAdvFlux / NoDifFlux, or None to clear."""
         st = C.c_int(0)

@@ -11,6 +11,7 @@
 // the process: every failure becomes a status code.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -47,8 +48,11 @@ void Instance::release()
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
                            &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid, &flux};
     for (auto* b : d) b->release();
-    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl, &NFU, &NFV, &NFW};
+    DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl, &NFU, &NFV, &NFW,
+                        &dStart};
     for (auto* b : i) b->release();
+    dTerms.release();
+    hasDisch = false;
     status.release();
     if (hstatus) cudaFreeHost(hstatus);
     hstatus = nullptr;
@@ -260,6 +264,8 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.NFU = in->hasNoFlux ? in->NFU.p : nullptr;
     a.NFV = in->hasNoFlux ? in->NFV.p : nullptr;
     a.NFW = in->hasNoFlux ? in->NFW.p : nullptr;
+    a.dStart = in->hasDisch ? in->dStart.p : nullptr;
+    a.dTerms = in->hasDisch ? in->dTerms.p : nullptr;
     a.status = in->status.p;
     return a;
 }
@@ -376,6 +382,7 @@ int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize, const
         if ((e = cudaMemcpy(d2[q]->p, s2[q], sizeof(double) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess)
             return bad(e, "cudaMemcpy");
     if ((e = cudaMemcpy(in->KFloor.p, KFloorZ, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
+    in->hKFloor.assign(KFloorZ, KFloorZ + in->n2);
     if ((e = cudaMemcpy(in->BP2D.p, BoundaryPoints2D, sizeof(int) * in->n2, cudaMemcpyHostToDevice)) != cudaSuccess) return bad(e, "cudaMemcpy");
     {
         // boundary columns in the reference's sweep order (j outer, i inner);
@@ -522,6 +529,87 @@ void* mohid_ad_stream(const int* id)
 {
     Instance* in = lookup(id);
     return in ? (void*)in->stream : nullptr;
+}
+
+int mohid_ad_set_discharges(const int* id, const int* DischNumber, const int* DischnCells, const int* IgnoreDisch,
+                            const int* ByPass, const int* DischVert, const int* DischI, const int* DischJ,
+                            const int* DischK, const int* DischKmin, const int* DischKmax, const double* DischFlow,
+                            const double* DischConc, const double* DischConcMF, int* stat)
+{
+    TraceRange trace_("mohid_ad_set_discharges");
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!DischNumber) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    const int nd = *DischNumber;
+    if (nd < 0) return fail(MOHID_AD_ERR_BOUNDS, stat, "DischNumber must be >= 0");
+    if (nd > 0 && (!DischnCells || !IgnoreDisch || !ByPass || !DischVert))
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    // the terms in the reference's order (AD:4040-4125): discharges not
+    // ignored, their cells, the layers of each cell
+    const int fillInt = -9999999, uniformVert = 5;   // FillValueInt, DischUniform_
+    const int ni = in->ni, nj = in->nj, nk = in->nk, sj = ni + 2;
+    std::vector<std::pair<int, mohid::DischTerm>> terms;   // (column, term)
+    int n = 0;
+    for (int dis = 0; dis < nd; ++dis) {
+        if (IgnoreDisch[dis]) continue;
+        if (DischnCells[dis] < 0) return fail(MOHID_AD_ERR_BOUNDS, stat, "DischnCells must be >= 0");
+        const bool uniform = DischVert[dis] == uniformVert;
+        for (int nc = 0; nc < DischnCells[dis]; ++nc, ++n) {
+            if (!DischI || !DischJ || !DischK || !DischKmin || !DischKmax || !DischFlow || !DischConc || !DischConcMF)
+                return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+            const int i = DischI[n], j = DischJ[n];
+            if (i < 1 || i > ni || j < 1 || j > nj) return fail(MOHID_AD_ERR_BOUNDS, stat, "discharge cell outside the work box");
+            int kmin, kmax;
+            if (uniform) {
+                kmin = DischKmin[n] == fillInt ? in->hKFloor[(size_t)i + (size_t)sj * j] : DischKmin[n];
+                kmax = DischKmax[n] == fillInt ? nk : DischKmax[n];
+            } else {
+                kmin = kmax = DischK[n];
+            }
+            if (kmin < 1 || kmax > nk) return fail(MOHID_AD_ERR_BOUNDS, stat, "discharge layers outside 1..KUB");
+            for (int k = kmin; k <= kmax; ++k) {
+                mohid::DischTerm t;
+                t.k = k; t.kmin = kmin; t.kmax = kmax;
+                t.flags = (uniform ? 1 : 0) | (ByPass[dis] ? 2 : 0);
+                t.flow = DischFlow[n]; t.conc = DischConc[n]; t.concMF = DischConcMF[n];
+                terms.emplace_back(i + sj * j, t);
+            }
+        }
+    }
+    // by column, then layer, keeping the reference's order among equal cells
+    std::stable_sort(terms.begin(), terms.end(), [](const auto& x, const auto& y) {
+        return x.first != y.first ? x.first < y.first : x.second.k < y.second.k;
+    });
+    std::vector<int> start(in->n2 + 1, 0);
+    for (const auto& t : terms) ++start[(size_t)t.first + 1];
+    for (size_t c = 0; c < in->n2; ++c) start[c + 1] += start[c];
+    std::vector<mohid::DischTerm> tv(terms.size());
+    for (size_t q = 0; q < terms.size(); ++q) tv[q] = terms[q].second;
+    CK(cudaSetDevice(in->device));
+    CK(cudaStreamSynchronize(in->stream));              // no step still reads the old lists
+    if (!in->dStart.p) {
+        cudaError_t e = in->dStart.alloc(in->n2 + 1);
+        if (e != cudaSuccess) return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
+    }
+    in->dTerms.release();
+    if (!tv.empty()) {
+        cudaError_t e = in->dTerms.alloc(tv.size());
+        if (e != cudaSuccess) { in->hasDisch = false; return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e)); }
+        CK(cudaMemcpy(in->dTerms.p, tv.data(), sizeof(mohid::DischTerm) * tv.size(), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(in->dStart.p, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+    in->hasDisch = !tv.empty();
+    return ok(stat);
+}
+
+int mohid_ad_unset_discharges(const int* id, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    CK(cudaSetDevice(in->device));
+    CK(cudaStreamSynchronize(in->stream));
+    in->hasDisch = false;
+    return ok(stat);
 }
 
 int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, const int* NoFluxW, int* stat)

@@ -14,6 +14,14 @@
 
 namespace mohid {
 
+// One discharge term at one cell (SetDischarges, AD:4025-4128): its layer, the
+// layer range of a uniform discharge (for the water column), flags (1: uniform
+// vertical distribution, 2: bypass), DischFlow, DischConc, DischConcMF.
+struct DischTerm {
+    int k, kmin, kmax, flags;
+    double flow, conc, concMF;
+};
+
 // Arguments of the plain FP64 step: Fortran layout over the Size box
 // (0:ni+1, 0:nj+1, 0:nk+1), i fastest, strides sj = ni+2, sk = (ni+2)(nj+2).
 struct PlainArgs {
@@ -32,6 +40,10 @@ struct PlainArgs {
     int impXX, impYY;           // implicit horizontal advection along j (XX) or i (YY)
     int noAdv, noDif;           // NoAdvFlux / NoDifFlux with the masks below
     const int *NFU, *NFV, *NFW; // NoFluxU/V/W (Size box), or null
+    // discharges, or null: terms of column c at dTerms[dStart[c] .. dStart[c+1]),
+    // by layer and then in the reference's order (c = i + sj * j)
+    const int* dStart;
+    const DischTerm* dTerms;
     double *sD, *sE, *sF, *sTI; // rows of the implicit horizontal system (Size box), or null
     // CellFluxes (or null): AdvFluxX/Y/Z and DifFluxX/Y/Z at the west, south and
     // bottom face of each cell, zeroed before the step; the step records the

@@ -6,6 +6,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/mohid_ad.h"
 #include "common.cuh"
@@ -68,6 +69,11 @@ struct Instance {
     // NoFluxU/V/W masks (mohid_ad_set_noflux), used by NoAdvFlux / NoDifFlux
     DevBuf<int> NFU, NFV, NFW;
     bool hasNoFlux = false;
+    // discharges (mohid_ad_set_discharges): per-column term lists
+    std::vector<int> hKFloor;          // KFloorZ (host copy, Size box 2-D)
+    DevBuf<int> dStart;
+    DevBuf<mohid::DischTerm> dTerms;
+    bool hasDisch = false;
     DevBuf<unsigned int> status;
     unsigned int* hstatus = nullptr;   // pinned
 

@@ -250,6 +250,27 @@ plain_f64_kernel(const PlainArgs A)
         } else {
             TI = Pk;
         }
+        // Discharges (AD:4025-4128): this row's terms, in the reference's order
+        if (A.dStart) {
+            const int q1 = __ldg(A.dStart + c + 1);
+            for (int q = __ldg(A.dStart + c); q < q1; ++q) {
+                const DischTerm T = A.dTerms[q];
+                if (T.k != k) continue;
+                const double DT_V = DT / Vk;
+                double Flow = T.flow;
+                if (T.flags & 1) {                   // uniform: by layer thickness
+                    double WaterColumn = 0.0;
+                    for (int kk = T.kmin; kk <= T.kmax; ++kk) WaterColumn = WaterColumn + __ldg(A.DWZ + c + (size_t)sk * kk);
+                    Flow = T.flow * __ldg(A.DWZ + a) / WaterColumn;
+                }
+                if (opk == 1) {
+                    if ((T.flags & 2) || Flow > 0.) TI = TI + Flow * DT_V * T.conc;
+                    else E = E - Flow * DT_V * T.concMF;
+                } else if (Flow > 0.) {
+                    TI = Pk * __ldg(A.Vold + a) / Vk + Flow * DT_V * T.conc;
+                }
+            }
+        }
 
         if (!A.vertical1D) {
             // HorizontalDiffusionXX: west face j, east face j+1 (loop runs j = JLB..JUB)

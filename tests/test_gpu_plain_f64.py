@@ -189,6 +189,53 @@ def test_gpu_noflux_masks(gpu, grid, flags, opt):
         assert np.array_equal(fg[n], fo[n]), n
 
 
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "layer1"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "theta_difv", "implicit_xx"])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_gpu_discharges(gpu, grid, opt, seed):
+    # SetDischarges: point and uniform discharges, inflows, withdrawals,
+    # a bypass and an ignored discharge; three steps through the host entry
+    # point, then the same through the device one; bit for bit
+    from tests.cases import discharges
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=2)
+    R = d.reference(2.0, 0.3, seed=3) if d.spec.open_sides else None
+    ds = discharges(d, seed=seed)
+    pd = dict(DTProp=30.0, **OPTIONS[opt])
+    Po = P0.copy()
+    for _ in range(3):
+        assert O.step(d, Po, O.params(**pd), ReferenceProp=R, Disch=ds) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    ad.set_discharges(ds)
+    Pg = P0.copy()
+    for _ in range(3):
+        ad.step(Pg, advdiff.params(**pd), R)
+    assert np.array_equal(Pg, Po)
+    import torch
+    a = torch.from_numpy(P0.copy()).cuda()
+    b = torch.empty_like(a)
+    Rd = torch.from_numpy(R).cuda() if R is not None else None
+    for _ in range(3):
+        ad.step_device(a, b, advdiff.params(**pd), Rd)
+        a, b = b, a
+    ad.sync()
+    assert np.array_equal(a.cpu().numpy(), Po)
+    # unset: the step without discharges again
+    ad.set_discharges(None)
+    Pq, Pr = P0.copy(), P0.copy()
+    ad.step(Pq, advdiff.params(**pd), R)
+    assert O.step(d, Pr, O.params(**pd), ReferenceProp=R) == 0
+    assert np.array_equal(Pq, Pr)
+    # cells outside the work box are rejected
+    bad = dict(ds, J=ds["J"].copy())
+    bad["J"][0] = d.nj + 1
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        ad.set_discharges(bad)
+    assert ei.value.code == 1
+    ad.kill()
+
+
 def test_gpu_boundary_condition_rules(gpu):
     d = domain("open")
     P = d.tracer(4, 1.0, 0.0, seed=1)
