@@ -199,6 +199,47 @@ def test_discharge_mass_budget(built, seed):
     assert O.step(d, P0.copy(), O.params(DTProp=30.0), Disch=bad) == 1
 
 
+def test_upwind_one_layer_matches_textbook_update(built):
+    # one layer, no diffusion, no surface flux: the step is the first-order
+    # upwind finite-volume update
+    #   V P_new = VOld P + DT * (sum over U and V faces of Q * P_upstream, signed)
+    # with fluxes only where both cells are open and the face computes
+    d = domain("layer1")
+    a = d.arrays
+    rng = np.random.default_rng(3)
+    a["Visc_H"][:] = 0.0
+    a["Diff_V"][:] = 0.0
+    a["Wflux_Z"][:] = 0.0
+    a["Wflux_X"][:] = rng.uniform(-2.0, 2.0, a["Wflux_X"].shape) * a["ComputeFacesU3D"]
+    a["Wflux_Y"][:] = rng.uniform(-2.0, 2.0, a["Wflux_Y"].shape) * a["ComputeFacesV3D"]
+    P = d.tracer(3, 1.0, 0.5, seed=9)
+    P0 = P.copy()
+    DT = 30.0
+    assert O.step(d, P, O.params(DTProp=DT, SchmidtBackground_V=0.0)) == 0
+    OP, CU, CV = a["OpenPoints3D"], a["ComputeFacesU3D"], a["ComputeFacesV3D"]
+    V, Vo = a["VolumeZ"], a["VolumeZOld"]
+    k = 1
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            if a["WaterPoints3D"][k, j, i] != 1:
+                continue
+            net = 0.0
+            for (jj, ii, sign, q, cf) in ((j, i, 1, a["Wflux_X"], CU), (j + 1, i, -1, a["Wflux_X"], CU),
+                                          (j, i, 1, a["Wflux_Y"], CV), (j, i + 1, -1, a["Wflux_Y"], CV)):
+                if cf[k, jj, ii] != 1:
+                    continue
+                up = (jj - 1, ii) if q is a["Wflux_X"] else (jj, ii - 1)
+                if OP[k, jj, ii] != 1 or OP[k, up[0], up[1]] != 1:
+                    continue
+                qf = q[k, jj, ii]
+                pu = P0[k, up[0], up[1]] if qf > 0 else P0[k, jj, ii]
+                net += sign * qf * pu
+            want = (Vo[k, j, i] * P0[k, j, i] + DT * net) / V[k, j, i]
+            if OP[k, j, i] != 1:
+                want = P0[k, j, i]
+            assert P[k, j, i] == pytest.approx(want, rel=1e-13, abs=1e-13)
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
