@@ -240,6 +240,38 @@ def test_upwind_one_layer_matches_textbook_update(built):
             assert P[k, j, i] == pytest.approx(want, rel=1e-13, abs=1e-13)
 
 
+@pytest.mark.parametrize("limiter", [1, 2, 3, 4])
+def test_tvd_face_value_matches_textbook(built, limiter):
+    # uniform cells: ComputeAdvectionFace's P2_TVD face value is the textbook
+    # limited upwind value  P_up + 0.5 * psi(r) * w * (P_down - P_up),
+    # r = (P_up - P_farup) / (P_down - P_up), with the reference's signed
+    # Courant number Cr = Q dt / V_up (FN:11045-11052): w = 1 - Cr, which is
+    # 1 - |Cr| for Q > 0 and 1 + |Cr| for Q < 0
+    psi = {1: lambda r: max(0.0, min(1.0, r)),                             # MinMod
+           2: lambda r: 0.0 if r < 0 else 2.0 * r / (1.0 + r),             # VanLeer
+           3: lambda r: max(0.0, min(2.0, 2.0 * r, (1.0 + r) / 2.0)),      # MUSCL
+           4: lambda r: max(0.0, min(1.0, 2.0 * r), min(r, 2.0))}[limiter]  # SuperBee
+    rng = np.random.default_rng(limiter)
+    V4, du4, dt = np.full(4, 50.0), np.full(4, 10.0), 5.0
+    n = 0
+    for _ in range(200):
+        P4 = rng.uniform(0.0, 10.0, 4)
+        Q = float(rng.uniform(-3.0, 3.0))
+        if abs(Q) < 0.1:
+            continue
+        up, down, far = (1, 2, 0) if Q > 0 else (2, 1, 3)
+        if abs(P4[down] - P4[up]) < 1e-3:
+            continue
+        rc, CF = O.advection_face(P4, V4, du4, dt, Q, 1.5, 4, limiter, False, True)
+        assert rc == 0
+        r = (P4[up] - P4[far]) / (P4[down] - P4[up])
+        Cr = Q * dt / V4[up]
+        want = P4[up] + 0.5 * psi(r) * (1.0 - Cr) * (P4[down] - P4[up])
+        assert float(np.dot(CF, P4)) == pytest.approx(want, rel=1e-12, abs=1e-12)
+        n += 1
+    assert n > 150
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
