@@ -272,6 +272,29 @@ def test_tvd_face_value_matches_textbook(built, limiter):
     assert n > 150
 
 
+def test_quick_and_central_face_values_match_textbook(built):
+    # UpwindOrder2 (FaceConcUpSecondOrder FN:11055) is the QUICK face value
+    # 6/8 P_up + 3/8 P_down - 1/8 P_farup where the volumes vary by less than
+    # VolumeRelMax (first order beyond); CentralDif is the distance-weighted mean
+    rng = np.random.default_rng(11)
+    du4, dt = np.array([10.0, 12.0, 9.0, 11.0]), 5.0
+    for _ in range(100):
+        P4 = rng.uniform(0.0, 10.0, 4)
+        Q = float(rng.choice([-1.0, 1.0]) * rng.uniform(0.1, 3.0))
+        up, down, far = (1, 2, 0) if Q > 0 else (2, 1, 3)
+        V4 = np.full(4, 50.0)
+        rc, CF = O.advection_face(P4, V4, du4, dt, Q, 1.5, 2, 4, False, True)
+        assert rc == 0
+        quick = 6.0 / 8.0 * P4[up] + 3.0 / 8.0 * P4[down] - 1.0 / 8.0 * P4[far]
+        assert float(np.dot(CF, P4)) == pytest.approx(quick, rel=1e-13, abs=1e-13)
+        V4[up] = 100.0                                    # VolumeRel 2 > 1.5: first order
+        rc, CF = O.advection_face(P4, V4, du4, dt, Q, 1.5, 2, 4, False, True)
+        assert float(np.dot(CF, P4)) == pytest.approx(P4[up], rel=1e-13, abs=1e-13)
+        rc, CF = O.advection_face(P4, np.full(4, 50.0), du4, dt, Q, 1.5, 5, 4, False, True)
+        central = (du4[2] * P4[1] + du4[1] * P4[2]) / (du4[1] + du4[2])
+        assert float(np.dot(CF, P4)) == pytest.approx(central, rel=1e-13, abs=1e-13)
+
+
 def test_pure_vertical_diffusion_matches_discrete_solve(built):
     d = synth.generate(synth.GenSpec(ni=1, nj=1, nk=9, land_frac=0.0, seed=2, dt=600.0,
                                      kz_median=1e-2, kz_logsigma=0.8))
