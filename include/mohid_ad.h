@@ -457,13 +457,17 @@ int mohid_thomasz_f64(const int* ILB, const int* IUB, const int* JLB, const int*
  * allocator that already holds the GPU, or a fixed budget reserved at start-up)
  * or one that must not synchronise the device inside its time step -- this
  * entry point allocates nothing: its scratch is a file-scope device array of
- * 2 x 8192 doubles (128 KiB) that every GPU loading the library holds until the
- * process exits.  Limit: at most 8192 work-box rows (JUB - 1 <= 8192); larger
- * grids return MOHID_AD_ERR_BOUNDS.  The first call on a device looks the array
- * up (cudaGetSymbolAddress); make that first call before any stream capture.
- * Calls share the array, so calls that overlap on the GPU (other streams or
- * other host threads) race; every call overwrites the part it reads, so
- * nothing needs clearing between calls.
+ * 2 x 8192 doubles (128 KiB).  A GPU holds it from the first call on that
+ * device (which loads the library's CUDA module, lazily, and looks the array
+ * up with cudaGetSymbolAddress) until the process exits.  That first call can
+ * synchronise, or fail under memory pressure, as any module load can: make it
+ * at start-up (a warm-up call), before any stream capture and outside the time
+ * step.  The lookup is repeated only when the calling thread's CUDA context
+ * changes (a reset primary context, another context on the device).
+ * Limit: at most 8192 work-box rows (JUB - 1 <= 8192); larger grids return
+ * MOHID_AD_ERR_BOUNDS.  Calls share the array, so calls that overlap on the
+ * GPU (other streams or other host threads) race; every call overwrites the
+ * part it reads, so nothing needs clearing between calls.
  */
 int mohid_ad_mass_f64_noalloc(const T_Size3D* size, const double* PROP, const double* VolumeZ,
                               const int* WaterPoints3D, double* mass, void* stream, int* stat);

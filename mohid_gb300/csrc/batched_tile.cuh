@@ -188,6 +188,15 @@ __device__ __forceinline__ float ld_l2hint(const float* a, uint64_t pol)
 
 constexpr uint32_t kWaitLimit = 1u << 24;
 
+// fetch-add on a shared-memory counter with acquire-release semantics at CTA scope
+__device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+                 : "=r"(old) : "r"(smem_u32(p)), "r"(v) : "memory");
+    return old;
+}
+
 // psi(r) * d for r = n / d, psi one of the ComputeAdvectionFace limiters
 // (FN:10823-10856).  Each min/max of psi(r) is multiplied through by |d|, so
 // with a = |d| and b = n * sign(d) no division is needed (VanLeer keeps one);
@@ -560,10 +569,15 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
         }
         // buffer s is free once every warp has finished row k: the last warp
         // to get here refills it with layer k + 2 (all warps pass the barrier
-        // of layer k + 1 only after all of them got here for layer k)
+        // of layer k + 1 only after all of them got here for layer k).  The
+        // counter is an acquire-release fetch-add at CTA scope: each warp's
+        // reads of buffer s (ordered before its lane 0 by __syncwarp) happen
+        // before its release, the last warp's acquire sees all of them, and
+        // the proxy fence in issue() then orders them before the bulk copy's
+        // async-proxy writes.
         __syncwarp();
         if (tx == 0) {
-            const unsigned n = atomicAdd(done, 1u);
+            const unsigned n = atom_add_acq_rel_cta(done, 1u);
             if ((n & (TY - 1)) == TY - 1 && k + 2 <= L.nk) issue(k + 2, s);
         }
     }

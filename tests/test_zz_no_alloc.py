@@ -43,12 +43,28 @@ def test_noalloc_mass_matches_existing_budget_twice(gpu, grid):
     WP = torch.from_numpy(d.arrays["WaterPoints3D"]).cuda()
     b.destroy()
     ad.kill()
+    outs = [torch.full((1,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    lib = N.ad_lib()
+    st0 = C.c_int(0)
     for call in range(2):                              # two calls sharing the scratch
-        out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
-        rc, st = _noalloc(d, P, V, WP, out)
-        assert rc == 0 and st == 0
-        torch.cuda.synchronize()
-        got = float(out.item())
+        if call == 1:
+            # the first (warm-up) call loaded the module holding the scratch;
+            # the second must allocate nothing: every allocation of this
+            # library fails from here on, and the device's free memory must
+            # not change across the call
+            N.check(lib.mohid_ad_debug_fail_alloc(C.byref(C.c_int(1)), C.byref(st0)), "fail_alloc")
+            free0 = torch.cuda.mem_get_info()[0]
+        try:
+            rc, st = _noalloc(d, P, V, WP, outs[call])
+            assert rc == 0 and st == 0
+            torch.cuda.synchronize()
+            if call == 1:
+                assert torch.cuda.mem_get_info()[0] == free0
+        finally:
+            if call == 1:
+                N.check(lib.mohid_ad_debug_fail_alloc(C.byref(C.c_int(0)), C.byref(st0)), "fail_alloc")
+        got = float(outs[call].item())
         assert abs(got - want) <= RTOL * abs(want), (call, got, want)
 
 
