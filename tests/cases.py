@@ -123,3 +123,17 @@ def discharges(d, seed=0, ndis=4, uniform=True, ignore_one=True):
     return dict(nCells=np.array(nCells), ignore=np.array(ignore), bypass=np.array(bypass), vert=np.array(vert),
                 I=np.array(I), J=np.array(J), K=np.array(K), Kmin=np.array(Kmin), Kmax=np.array(Kmax),
                 Flow=np.array(Flow), Conc=np.array(Conc), ConcMF=np.array(CMF))
+
+
+def fp16_round_fields(d, storage):
+    """Round the domain's transports (and, with FP16_QK storage, Visc_H and
+    Diff_V) in place to what the batched form stores: FP16 times a per-field
+    FP32 scale absmax / 16384.  The oracle then runs on the same inputs as the
+    batched kernel, so a comparison measures the arithmetic alone."""
+    a = d.arrays
+    names = ["Wflux_X", "Wflux_Y", "Wflux_Z"] + (["Visc_H", "Diff_V"] if storage == 2 else [])
+    for n in names:
+        m = float(np.abs(a[n]).max())
+        s = np.float32(m / 16384.0) if m > 0 else np.float32(1.0)
+        q = (a[n] * np.float64(np.float32(1.0) / s)).astype(np.float32).astype(np.float16)
+        a[n][...] = (s * q.astype(np.float32)).astype(np.float64)

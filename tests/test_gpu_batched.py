@@ -10,7 +10,7 @@ import pytest
 
 from mohid_gb300 import advdiff, batched, configs, synth
 from oracle import oracle as O
-from tests.cases import domain
+from tests.cases import domain, fp16_round_fields
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
@@ -120,13 +120,7 @@ def test_batched_fp16_storage(gpu, storage):
     import torch
     w = configs.cfg3().scaled(ni=96, nj=64, nk=20)
     d = synth.generate(w.spec)
-    a = d.arrays
-    names = ["Wflux_X", "Wflux_Y", "Wflux_Z"] + (["Visc_H", "Diff_V"] if storage == batched.FP16_QK else [])
-    for n in names:     # the same per-field scaling the library applies
-        m = float(np.abs(a[n]).max())
-        s = np.float32(m / 16384.0) if m > 0 else np.float32(1.0)
-        q = (a[n] * np.float64(np.float32(1.0) / s)).astype(np.float32).astype(np.float16)
-        a[n][...] = (s * q.astype(np.float32)).astype(np.float64)
+    fp16_round_fields(d, storage)      # the same per-field scaling the library applies
     tr = [d.tracer(k, a_, b_, seed=7 + t) for t, (k, a_, b_) in enumerate(w.tracers[:4])]
     want, got = run_pair(d, tr, w.params(), 20, storage=storage)
     for g_, w_ in zip(got, want):
