@@ -81,6 +81,8 @@ struct BatchArgs {
     int nt;
     const float* Ref;                   // same layout as tracers (boundary cells read), or null
     float* W;                           // scratch: THOMASZ W per cell (batched layout)
+    float* G;                           // scratch: THOMASZ G of the launch's tracers per cell, nt
+                                        // floats per cell (cell c at G + c * nt)
     // mass budget of the fixer (closed domains), or mpart == null: VolumeZ as
     // an FP32 pair hi + lo (batched layout), and per tile and tracer of the
     // batch the sum of VolumeZ * stored value written to

@@ -42,7 +42,7 @@ struct Batch {
     DevBuf<float> areaCol;
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;
-    DevBuf<float> Wsc;                   // THOMASZ W per cell, scratch of the step kernel
+    DevBuf<float> Wsc, Gsc;              // THOMASZ W and G per cell, scratch of the step kernel
     // mass fixer (static volumes): VolumeZ as an FP32 pair, the fixer state
     // (volume, targets, constants, corrections, boundary fluxes), per-tile
     // sums; with open boundaries the boundary columns and the per-block
@@ -118,7 +118,7 @@ struct Batch {
     void release()
     {
         DevBuf<float>* f[] = {&Qx32, &Qy32, &Qz32, &Vis32, &Dif32, &AreaU, &AreaV, &DZZ,
-                              &areaCol, &PA, &PB, &Ref, &Wsc, &Vhi, &Vlo};
+                              &areaCol, &PA, &PB, &Ref, &Wsc, &Gsc, &Vhi, &Vlo};
         for (auto* b : f) b->release();
         DevBuf<__half>* h[] = {&Qx16, &Qy16, &Qz16, &Vis16, &Dif16};
         for (auto* b : h) b->release();
@@ -433,6 +433,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.t0 = t0;
     a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
     a.W = b->Wsc.p;
+    a.G = b->Gsc.p;
     a.Vhi = b->Vhi.p;
     a.Vlo = b->Vlo.p;
     a.mfix = b->mfix.p;
@@ -728,6 +729,10 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->PA.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->PB.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Wsc.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
+    {
+        const int gmax = b->nt >= 8 ? 8 : (b->nt >= 4 ? 4 : (b->nt >= 2 ? 2 : 1));   // largest tracer group
+        if ((e = b->Gsc.alloc(n3 * (size_t)gmax)) != cudaSuccess) return bad(e, "cudaMalloc");
+    }
     b->tilesX = (in->ni + mohid::kTX - 1) / mohid::kTX;
     b->ntiles = b->tilesX * ((in->nj + mohid::kTY - 1) / mohid::kTY);
     if ((e = b->Vhi.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");

@@ -101,9 +101,10 @@ struct Smem {
     static constexpr int FXYStride = al128(NT * NWF * 4) + al128(NT * NSF * 4);
     static constexpr int oFX = 2 * SL::size;
     static constexpr int oFY = oFX + al128(NT * NWF * 4);
-    static constexpr int oCX = oFX + 2 * FXYStride;
+    static constexpr int oCX = oFX + 2 * FXYStride;        // face constants (west, south faces)
     static constexpr int oCY = oCX + al128(NWF * 16);
-    static constexpr int oBar = oCY + al128(NSF * 16);
+    static constexpr int oRed = oCY + al128(NSF * 16);      // the mass fixer's per-warp sums
+    static constexpr int oBar = oRed + al128(TY * NT * 2 * 4);
     static constexpr int oEnd = oBar + 128;
     static size_t bytes(int) { return (size_t)oEnd; }
 };
@@ -241,55 +242,113 @@ __device__ __forceinline__ float obc_wfob(float qw, float qe, float qs, float qn
     return (float)((double)h - (double)dvr / ((double)rV * (double)DT));
 }
 
-// One face of the tile at one layer.  WEST: the face between cells
-// (i0+b, j0+a-1) and (i0+b, j0+a), a = 0..TY; otherwise the face between
-// (i0+b-1, j0+a) and (i0+b, j0+a), b = 0..TX.  Tracer-independent part first
-// (upwind side, Courant number, diffusive conductance), then for every tracer
+// THOMASZ scratch of the walk, per cell of the batched layout: W in its own
+// plane (A.W) and G of the launch's tracers together (A.G, NT floats per
+// cell), so that a row's scratch is one scalar and one vector store on the
+// way up and the same two loads on the way down.  The lines are discarded
+// from L2 once read (they are dead), so they are never written back.
+template <int NT> struct GVec;
+template <> struct GVec<1> {
+    static __device__ __forceinline__ void st(float* a, const float* g, uint64_t pol)
+    {
+        asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(g[0]), "l"(pol));
+    }
+    static __device__ __forceinline__ void ld(const float* a, float* g, uint64_t pol)
+    {
+        asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(g[0]) : "l"(a), "l"(pol));
+    }
+};
+template <> struct GVec<2> {
+    static __device__ __forceinline__ void st(float* a, const float* g, uint64_t pol)
+    {
+        asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(a), "f"(g[0]), "f"(g[1]), "l"(pol));
+    }
+    static __device__ __forceinline__ void ld(const float* a, float* g, uint64_t pol)
+    {
+        asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+                     : "=f"(g[0]), "=f"(g[1]) : "l"(a), "l"(pol));
+    }
+};
+template <> struct GVec<4> {
+    static __device__ __forceinline__ void st(float* a, const float* g, uint64_t pol)
+    {
+        asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "f"(g[0]), "f"(g[1]),
+                     "f"(g[2]), "f"(g[3]), "l"(pol));
+    }
+    static __device__ __forceinline__ void ld(const float* a, float* g, uint64_t pol)
+    {
+        asm volatile("ld.global.cg.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                     : "=f"(g[0]), "=f"(g[1]), "=f"(g[2]), "=f"(g[3]) : "l"(a), "l"(pol));
+    }
+};
+template <> struct GVec<8> {
+    static __device__ __forceinline__ void st(float* a, const float* g, uint64_t pol)
+    {
+        GVec<4>::st(a, g, pol);
+        GVec<4>::st(a + 4, g + 4, pol);
+    }
+    static __device__ __forceinline__ void ld(const float* a, float* g, uint64_t pol)
+    {
+        GVec<4>::ld(a, g, pol);
+        GVec<4>::ld(a + 4, g + 4, pol);
+    }
+};
+
+// the 128-byte L2 line at a holds only dead data: drop it without a write-back
+__device__ __forceinline__ void l2_discard(const void* a)
+{
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+}
+
+// One face of the tile at one layer.  WEST: the face between the cells at P
+// offsets pb - PBX and pb (j - 1 and j); otherwise between pb - 1 and pb (i - 1
+// and i).  The offsets into the stage (elements): pb into the tracer tile, vb
+// into 1/V, visb into Visc_H, qo / ao into the face transports and areas, fo
+// into the face-flag bytes; out: the face's flux slot (tracer stride cs).  cf:
+// the face's constants (Visc weights with Schmidt and 1/DZ folded in, TVD
+// slope ratios).  Tracer-independent part first (upwind side, Courant number,
+// diffusive conductance), then for every tracer
 // F = q*P_up + kd*(P_dn - P_up) + q*c*psi(r)*(P_dn - P_up) into shared memory.
 // Reference face coefficients: ComputeAdvectionFace FN:10702-10894 (upwind,
 // P2_TVD limiters, theta = psi*(1-Cr)/2); diffusive flux
 // HorizontalDiffusionXX/YY AD:5185-5196 with Kx from
 // Convert_Visc_Dif_Horizontal AD:2487-2494.
 template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT>
-__device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, const float4* CXY,
-                                          const BatchArgs& A, int a, int b)
+__device__ __forceinline__ void face_flux(const unsigned char* st, float* out, const float4 cf, const BatchArgs& A,
+                                          int pb, int vb, int visb, int qo, int ao, int fo)
 {
     using SL = StageLayout<NT, QT, KT>;
     constexpr int pst = WEST ? PBX : 1, vst = WEST ? VBX : 1;
     constexpr int visst = WEST ? Box<KT>::visX : 1;
     constexpr int cs = WEST ? NWF : NSF;
+    constexpr int tst = (TY + 4) * PBX;              // tracer stride of the stage's tracer tile
     constexpr uint8_t ACT = WEST ? FU_ACT : FV_ACT, ADV = WEST ? FU_ADV : FV_ADV;
     constexpr uint8_t TVDP = WEST ? FU_TVDP : FV_TVDP, TVDN = WEST ? FU_TVDN : FV_TVDN;
     const float* P = reinterpret_cast<const float*>(st + SL::oP);
-    const float* RVt = reinterpret_cast<const float*>(st + SL::oV);
     const KT* Vis = reinterpret_cast<const KT*>(st + SL::oVis);
-    const int pb = (a + 2) * PBX + b + 4;
-    const int vb = (a + 1) * VBX + b + 4;
-    const int visb = (a + 1) * Box<KT>::visX + b + Box<KT>::visOff;
-    const int fi = WEST ? a * TX + b : a * (TX + 1) + b;
     float q, area;
     if (WEST) {
-        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQX)[a * TX + b], A.qsx);
-        area = reinterpret_cast<const float*>(st + SL::oAU)[a * TX + b];
+        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQX)[qo], A.qsx);
+        area = reinterpret_cast<const float*>(st + SL::oAU)[ao];
     } else {
-        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQY)[a * SL::qyX + b], A.qsy);
-        area = reinterpret_cast<const float*>(st + SL::oAV)[a * AVX + b];
+        q = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQY)[qo], A.qsy);
+        area = reinterpret_cast<const float*>(st + SL::oAV)[ao];
     }
-    const uint8_t ff = (WEST || !A.xzflow) ? st[SL::oF + a * FBX + b] : 0;
+    const uint8_t ff = (WEST || !A.xzflow) ? st[SL::oF + fo] : 0;
     const bool pos = q > 0.f;
-    const float4 cf = CXY[fi];                     // Visc weights (Schmidt and 1/DZ folded in), TVD ratios
     float K = tofl<KT>(Vis[visb], A.ksh) * cf.x + tofl<KT>(Vis[visb - visst], A.ksh) * cf.y;
     if (A.nullDif && q == 0.f) K = 0.f;
     const float auxK = (ff & ACT) ? K * area : 0.f;
     const float kd = pos ? -auxK : auxK;
     const float qv = (ff & ADV) ? q : 0.f;
-    const int pa = pb - pst;
-    const int iup = pos ? pa : pb, idn = pos ? pb : pa;
-    const int iuu = pos ? pa - pst : pb + pst;
+    const float* pup = P + (pos ? pb - pst : pb);
+    const float* pdn = P + (pos ? pb : pb - pst);
+    const float* puu = P + (pos ? pb - 2 * pst : pb + pst);
     float gr = 0.f, qvc = 0.f, pa5 = 0.f, pb5 = 0.f, p2 = 0.f, pcr = 0.f;
     if (METHOD == 4) {
         const bool tvd = (ff & ADV) && (ff & (pos ? TVDP : TVDN));   // not NearBoundary
         gr = pos ? cf.z : cf.w;
+        const float* RVt = reinterpret_cast<const float*>(st + SL::oV);
         float Cr = q * A.DT * RVt[pos ? vb - vst : vb];
         if (LIM == 5) {
             const float t6 = (1.f - 2.f * fabsf(Cr)) / 6.f;
@@ -301,14 +360,12 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* FXY, c
         }
         qvc = tvd ? q * (0.5f - 0.5f * Cr) : 0.f;
     }
-    float* out = FXY + fi;
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
-        const float* Pt = P + t * (TY + 4) * PBX;
-        const float Pup = Pt[iup];
-        const float dd = Pt[idn] - Pup;
+        const float Pup = pup[t * tst];
+        const float dd = pdn[t * tst] - Pup;
         float o = fmaf(kd, dd, qv * Pup);
-        if (METHOD == 4) o = fmaf(qvc, limited_slope<LIM>((Pup - Pt[iuu]) * gr, dd, pa5, pb5, p2, pcr), o);
+        if (METHOD == 4) o = fmaf(qvc, limited_slope<LIM>((Pup - puu[t * tst]) * gr, dd, pa5, pb5, p2, pcr), o);
         out[t * cs] = o;
     }
 }
@@ -358,14 +415,17 @@ __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
 // next in the same CTA.  Returns false when a stage never arrived (the status
 // word then holds MOHID_DEV_TIMEOUT).  The caller must have every warp of the
 // CTA past its previous walk before calling (a barrier between walks).
+//
+// The layer body is compiled once per stage buffer (the walk advances two
+// layers per iteration), so every shared-memory access is a per-thread offset
+// computed once per tile plus a constant.
 template <int NT, int METHOD, int LIM, typename QT, typename KT, bool OBC>
 __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, int bx, int by,
                                           unsigned char* smem_raw, uint32_t& phase)
 {
     using SL = StageLayout<NT, QT, KT>;
     using SM = Smem<NT, QT, KT>;
-    float4* CX = reinterpret_cast<float4*>(smem_raw + SM::oCX);
-    float4* CY = reinterpret_cast<float4*>(smem_raw + SM::oCY);
+    constexpr int visX = Box<KT>::visX, visOff = Box<KT>::visOff;
     WalkWords* ww = reinterpret_cast<WalkWords*>(smem_raw + SM::oBar);
     uint64_t* bar = ww->bar;
     int* kminp = &ww->kmin;
@@ -382,6 +442,10 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     const int kb = solve ? A.kfloor[c2] : L.nk + 1;
 
     if (tid == 0) *kminp = L.nk + 1;
+    // face constants of the tile's faces (Visc weights with Schmidt folded in,
+    // TVD slope ratios), tile-invariant, into shared memory
+    float4* CX = reinterpret_cast<float4*>(smem_raw + SM::oCX);
+    float4* CY = reinterpret_cast<float4*>(smem_raw + SM::oCY);
     for (int e = tid; e < NWF; e += NTH) {
         float4 c = A.fc[L.at2(i0 + e % TX, j0 + e / TX)];
         c.x *= A.schmidtH; c.y *= A.schmidtH;
@@ -392,6 +456,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
         c.x *= A.schmidtH; c.y *= A.schmidtH;
         CY[e] = c;
     }
+    const bool xW = ty == 0, xS = ty == 1 && tx < TY;
     __syncthreads();
     if (solve) atomicMin(kminp, kb);
     __syncthreads();
@@ -404,7 +469,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
 
     // TMA box origins (x on 16-byte boundaries of the batched layout)
     const int xP = i0 + kXOff - 4, xV = i0 + kXOff - 4;
-    const int xVis = i0 + kXOff - Box<KT>::visOff, xO = i0 + kXOff;
+    const int xVis = i0 + kXOff - visOff, xO = i0 + kXOff;
     const int yP = j0 + kYOff - 2, yV = j0 + kYOff - 1, yO = j0 + kYOff;
     auto issue = [&](int k, int s) {               // one thread: stage layer k into buffer s
         unsigned char* d = smem_raw + (s ? SM::oStage1 : SM::oStage0);
@@ -460,42 +525,56 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     for (int t = 0; t < NT; ++t) Gp[t] = 0.f;
     float Wp = 0.f;
     unsigned bad = 0;
-    const int own = ty * OWN + tx;
-    const int fw = ty * TX + tx, fs = ty * (TX + 1) + tx;
-    float* const Wc = A.W + cb;
-    float* const Po = A.Pout + cb;
+    // per-thread offsets into a stage (elements), the same for both buffers
+    const int pbO = (ty + 2) * PBX + tx + 4;       // tracer tile, own cell
+    const int vbO = (ty + 1) * VBX + tx + 4;       // 1/V, own cell
+    const int visO = (ty + 1) * visX + tx + visOff;
+    const int own = ty * OWN + tx;                 // own-cell boxes, west-face boxes (pitch TX)
+    const int qyO = ty * SL::qyX + tx, avO = ty * AVX + tx, fO = ty * FBX + tx;
+    const int fs = ty * (TX + 1) + tx;             // own south face in FY
+    // closing faces: warp 0 the west faces of row TY, warp 1 the south faces of column TX
+    const int xa = xW ? TY : tx, xb = xW ? tx : TX;
+    const int pbX = (xa + 2) * PBX + xb + 4, vbX = (xa + 1) * VBX + xb + 4;
+    const int visXo = (xa + 1) * visX + xb + visOff;
+    const int qoX = xW ? xa * TX + xb : xa * SL::qyX + xb, aoX = xW ? xa * TX + xb : xa * AVX + xb;
+    const int foX = xa * FBX + xb, fiX = xW ? xa * TX + xb : xa * (TX + 1) + xb;
+    // THOMASZ scratch of row k of this column: W at A.W + cb + k * sl, G at
+    // A.G + (cb + k * sl) * NT
+    float* wr = A.W + cb + (long long)kmin * L.sl;
+    float* gr = A.G + (cb + (long long)kmin * L.sl) * NT;
+    const long long wStep = L.sl, gStep = L.sl * NT;
     const uint64_t keep = l2_policy_evict_last(), drop = l2_policy_evict_first();
 
-    for (int k = kmin; k <= L.nk; ++k) {
-        const int s = k & 1;
-        const unsigned char* st = smem_raw + (s ? SM::oStage1 : SM::oStage0);
-        float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX + s * SM::FXYStride);
-        float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY + s * SM::FXYStride);
-        const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
-        phase ^= 1u << s;
+    // one layer with the stage buffer S; false: a stage never arrived
+    auto layer = [&](auto SC, const int k) -> bool {
+        constexpr int S = decltype(SC)::value;
+        const unsigned char* st = smem_raw + (S ? SM::oStage1 : SM::oStage0);
+        float* FX = reinterpret_cast<float*>(smem_raw + SM::oFX + S * SM::FXYStride);
+        float* FY = reinterpret_cast<float*>(smem_raw + SM::oFY + S * SM::FXYStride);
+        const bool ok = mbar_wait_bounded(&bar[S], (phase >> S) & 1u, kWaitLimit);
+        phase ^= 1u << S;
 
         // ---- faces of the tile at layer k: own west and south faces; the
         //      east row (warp 0) and north column (warp 1) close the tile
         if (horiz && ok) {
-            face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, ty, tx);
-            face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, ty, tx);
-            if (ty == 0) face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX, CX, A, TY, tx);
-            else if (ty == 1 && tx < TY) face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY, CY, A, tx, TX);
+            face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX + own, CX[own], A, pbO, vbO, visO, own, own, fO);
+            face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY + fs, CY[fs], A, pbO, vbO, visO, qyO, avO, fO);
+            if (xW) face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX + fiX, CX[fiX], A, pbX, vbX, visXo, qoX, aoX, foX);
+            else if (xS) face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY + fiX, CY[fiX], A, pbX, vbX, visXo, qoX, aoX, foX);
         }
         if (__syncthreads_or(!ok)) {               // a stage never arrived: leave cleanly
             if (tid == 0) {
                 atomicOr(A.status, MOHID_DEV_TIMEOUT);
-                mbar_wait_bounded(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u, kWaitLimit);
+                mbar_wait_bounded(&bar[S ^ 1], (phase >> (S ^ 1)) & 1u, kWaitLimit);
             }
             return false;
         }
 
         if (solve && k >= kb) {
             // ---- row k of column (i,j): tracer-independent matrix
-            const long long ko = (long long)k * L.sl;
             const bool top = k == L.nk;
             const uint8_t flp = top ? 0 : (st + SL::oFn)[own];
-            const float rVk = reinterpret_cast<const float*>(st + SL::oV)[(ty + 1) * VBX + tx + 4];
+            const float rVk = reinterpret_cast<const float*>(st + SL::oV)[vbO];
             const float dvr = reinterpret_cast<const float*>(st + SL::oVo)[own];   // (V - Vold)/V
             const float qzp = tofl<QT>(reinterpret_cast<const QT*>(st + SL::oQz)[own], A.qsz);
             const float dtv = DT * rVk;
@@ -529,11 +608,11 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             if (obc) {
                 const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
                 const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
-                const uint8_t* ffl = st + SL::oF + ty * FBX + tx;
-                wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[fw], A.qsx) : 0.f,
-                                (ffl[FBX] & FU_ACT) ? tofl<QT>(qx[fw + TX], A.qsx) : 0.f,
-                                (ffl[0] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx], A.qsy) : 0.f,
-                                (ffl[1] & FV_ACT) ? tofl<QT>(qy[ty * SL::qyX + tx + 1], A.qsy) : 0.f,
+                const uint8_t* ffl = st + SL::oF + fO;
+                wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[own], A.qsx) : 0.f,
+                                (ffl[FBX] & FU_ACT) ? tofl<QT>(qx[own + TX], A.qsx) : 0.f,
+                                (ffl[0] & FV_ACT) ? tofl<QT>(qy[qyO], A.qsy) : 0.f,
+                                (ffl[1] & FV_ACT) ? tofl<QT>(qy[qyO + 1], A.qsy) : 0.f,
                                 (fl & F_CFW) ? qz : 0.f, (flp & F_CFW) ? qzp : 0.f, dvr, rVk, DT);
                 if (wfob >= 0.f) E += wfob * dtv;
             }
@@ -542,50 +621,63 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             float inv = rcp_approx(aux);
             if (aux == 0.f) { inv = 0.f; bad |= MOHID_DEV_ZERO_PIVOT; }
             const float W = -Fc * inv;
-            st_l2hint(Wc + ko, W, keep);                 // read back by the back-substitution
             Wp = W;
+            st_l2hint(wr, W, keep);                      // read back by the back-substitution
             const float* P = reinterpret_cast<const float*>(st + SL::oP);
-            const int po = (ty + 2) * PBX + tx + 4;
 #pragma unroll
             for (int t = 0; t < NT; ++t) {
-                const float Pc = P[t * (TY + 4) * PBX + po];
+                const float Pc = P[t * (TY + 4) * PBX + pbO];
                 float TI = Pc * ratio;
                 if (horiz)
-                    TI = fmaf(dtv, (FX[t * NWF + fw] - FX[t * NWF + fw + TX]) +
+                    TI = fmaf(dtv, (FX[t * NWF + own] - FX[t * NWF + own + TX]) +
                                    (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
                 if (obc && wfob < 0.f) {
                     // the reference is stored relative to the tracer's loaded
                     // constant; the fixer's correction moves it with the field
-                    const float ref = A.Ref[(long long)t * A.ts + cb + ko] -
+                    const float ref = A.Ref[(long long)t * A.ts + cb + (long long)k * L.sl] -
                                       (float)A.mfix[1 + 2 * A.ntAll + A.t0 + t];
                     const float ext = Pc * (1.f - A.tdec) + ref * A.tdec;
                     TI -= wfob * ext * dtv;
                 }
-                const float G = (TI - D * Gp[t]) * inv;
-                Gp[t] = G;
-                st_l2hint(Po + (long long)t * A.ts + ko, G, keep);
+                Gp[t] = (TI - D * Gp[t]) * inv;
             }
+            GVec<NT>::st(gr, Gp, keep);
             qz = qzp; kzb = kza; flm = fl; fl = flp;
         }
-        // buffer s is free once every warp has finished row k: the last warp
+        wr += wStep;
+        gr += gStep;
+        // buffer S is free once every warp has finished row k: the last warp
         // to get here refills it with layer k + 2 (all warps pass the barrier
         // of layer k + 1 only after all of them got here for layer k).  The
         // counter is an acquire-release fetch-add at CTA scope: each warp's
-        // reads of buffer s (ordered before its lane 0 by __syncwarp) happen
+        // reads of buffer S (ordered before its lane 0 by __syncwarp) happen
         // before its release, the last warp's acquire sees all of them, and
         // the proxy fence in issue() then orders them before the bulk copy's
         // async-proxy writes.
         __syncwarp();
         if (tx == 0) {
             const unsigned n = atom_add_acq_rel_cta(done, 1u);
-            if ((n & (TY - 1)) == TY - 1 && k + 2 <= L.nk) issue(k + 2, s);
+            if ((n & (TY - 1)) == TY - 1 && k + 2 <= L.nk) issue(k + 2, S);
         }
+        return true;
+    };
+
+    int k = kmin;
+    if (k & 1) {
+        if (!layer(std::integral_constant<int, 1>{}, k)) return false;
+        ++k;
+    }
+    for (; k <= L.nk; k += 2) {
+        if (!layer(std::integral_constant<int, 0>{}, k)) return false;
+        if (k + 1 > L.nk) break;
+        if (!layer(std::integral_constant<int, 1>{}, k + 1)) return false;
     }
 
-    // ---- back-substitution (row KUB+1 solves to 0); W and G loads are issued
-    //      RB rows at a time, all tracers of the column together.  With the mass
-    //      fixer on, the column's sum of VolumeZ * value is accumulated as an
-    //      FP32 pair per tracer from VolumeZ = hi + lo (about 2^-44 relative).
+    // ---- back-substitution (row KUB+1 solves to 0); the scratch rows are
+    //      loaded RB rows at a time, all tracers of the column together.  With
+    //      the mass fixer on, the column's sum of VolumeZ * value is
+    //      accumulated as an FP32 pair per tracer from VolumeZ = hi + lo (about
+    //      2^-44 relative).
     const bool mf = A.mpart != nullptr;
     constexpr int RB = NT >= 8 ? 2 : 4;            // rows per batch of loads (registers)
     float mh[NT], ml[NT];
@@ -596,15 +688,15 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
 #pragma unroll
         for (int t = 0; t < NT; ++t) x[t] = 0.f;
         float chk = 0.f;                           // NaN / Inf anywhere in the column shows here
+        float* const Po = A.Pout + cb;
         for (int k = L.nk; k >= kb; k -= RB) {
-            float w[RB], g[NT][RB], vh[RB], vl[RB];
+            float w[RB], g[RB][NT], vh[RB], vl[RB];
 #pragma unroll
             for (int q = 0; q < RB; ++q)
                 if (k - q >= kb) {
                     const long long o = (long long)(k - q) * L.sl;
-                    w[q] = ld_l2hint(Wc + o, drop);
-#pragma unroll
-                    for (int t = 0; t < NT; ++t) g[t][q] = ld_l2hint(Po + (long long)t * A.ts + o, drop);
+                    w[q] = ld_l2hint(A.W + cb + o, drop);
+                    GVec<NT>::ld(A.G + (cb + o) * NT, g[q], drop);
                     if (mf) {
                         vh[q] = ld_l2hint(A.Vhi + cb + o, drop);
                         vl[q] = ld_l2hint(A.Vlo + cb + o, drop);
@@ -616,7 +708,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                     const long long o = (long long)(k - q) * L.sl;
 #pragma unroll
                     for (int t = 0; t < NT; ++t) {
-                        x[t] = fmaf(w[q], x[t], g[t][q]);
+                        x[t] = fmaf(w[q], x[t], g[q][t]);
                         Po[(long long)t * A.ts + o] = x[t];
                         chk += x[t];
                         if (mf) {
@@ -629,6 +721,21 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
         }
         if (!isfinite(chk)) bad |= MOHID_DEV_NONFINITE;
     }
+    // the scratch rows kmin..nk of this warp's 32 cells are dead now: drop
+    // their L2 lines (one W line and NT G lines per row) without a write-back.
+    // The warp's cells start on a 32-cell boundary of the layout, so these
+    // lines hold no other cells.
+    __syncwarp();
+    {
+        const long long c0 = cb - tx;                // the warp's first cell
+        const int nl = 1 + NT;                       // lines per row
+        const int nrow = L.nk - kmin + 1;
+        for (int e = tx; e < nrow * nl; e += TX) {
+            const int r = e / nl, q = e - r * nl;
+            const long long c = c0 + (long long)(kmin + r) * L.sl;
+            l2_discard(q == 0 ? (const void*)(A.W + c) : (const void*)(A.G + c * NT + (q - 1) * 32));
+        }
+    }
     if (mf) {
         // fixed-order reduction: lanes by a shuffle tree, warps in order
 #pragma unroll
@@ -640,7 +747,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                 two_sum_acc(mh[t], ml[t], oh);
                 ml[t] = __fadd_rn(ml[t], ol);
             }
-        float* red = reinterpret_cast<float*>(CX);   // the face constants are no longer needed
+        float* red = reinterpret_cast<float*>(smem_raw + SM::oRed);
         if (tx == 0)
 #pragma unroll
             for (int t = 0; t < NT; ++t) {
