@@ -75,6 +75,9 @@ extern "C" {
 #define MOHID_BC_CYCLIC              8
 /* ModuleGlobalData.F90:143 */
 #define MOHID_NULL_REAL (-9.9e15)
+/* face thickness options of ModuleGeometry (ModuleGeometry.F90:231-232) */
+#define MOHID_FACES_AVERAGE_THICKNESS 2
+#define MOHID_FACES_MIN_THICKNESS     3
 
 /* T_Size3D, ModuleGlobalData.F90:2042-2052 (bind(c) under _USE_CUDA). */
 typedef struct T_Size3D {
@@ -152,6 +155,12 @@ int mohid_ad_init(int* id, const T_Size3D* size, const T_Size3D* worksize,
  * are over the Size box.  `SmallDepths` (int, 2-D) may be NULL.
  * Equivalent to the pointer-binding part of the reference call; lets a caller that
  * transports N properties per step send the hydrodynamics once instead of N times.
+ * After the first call any of the eleven FP64 arrays may be NULL: the instance
+ * keeps its copy (unchanged since the last call, or made on the device by
+ * mohid_ad_geometry_dev / mohid_ad_vertical_flux).  The six 3-D masks are given
+ * all together (then checked, and SmallDepths replaced) or all NULL (kept,
+ * SmallDepths ignored); a call that keeps the masks does not wait for the
+ * device beyond consuming the host buffers.
  */
 int mohid_ad_set_hydro(const int* id,
                        const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
@@ -255,8 +264,9 @@ int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PRO
                                const double* ReferenceProp,
                                const mohid_ad_params* p, int* stat);
 
-/* Upload hydrodynamics that already live on the device (same layout as
- * mohid_ad_set_hydro, device pointers; copied device-to-device, async). */
+/* Upload hydrodynamics that already live on the device (same layout and
+ * NULL rules as mohid_ad_set_hydro, device pointers; copied device-to-device,
+ * asynchronous when the masks are kept). */
 int mohid_ad_set_hydro_dev(const int* id,
                            const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
                            const double* VolumeZOld, const double* VolumeZ,
@@ -268,6 +278,15 @@ int mohid_ad_set_hydro_dev(const int* id,
                            const int* ComputeFacesU3D, const int* ComputeFacesV3D,
                            const int* ComputeFacesW3D,
                            const int* SmallDepths, int* stat);
+
+/* Copy the instance's current FP64 hydrodynamic fields (those of the last
+ * mohid_ad_set_hydro*, as changed since by the device producers) to the
+ * caller's Size-box arrays; any pointer may be NULL (not copied).  Host
+ * pointers when *on_device == 0, device pointers otherwise.  Synchronous. */
+int mohid_ad_get_hydro(const int* id, double* Wflux_X, double* Wflux_Y, double* Wflux_Z,
+                       double* VolumeZOld, double* VolumeZ, double* Visc_H, double* Diff_V,
+                       double* AreaU, double* AreaV, double* DZZ, double* DWZ,
+                       const int* on_device, int* stat);
 
 /* Wait for the instance's stream and report latched device errors. */
 int mohid_ad_sync(const int* id, int* stat);
@@ -420,6 +439,39 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
 
 /* Release the ensemble (the member batches are not destroyed). */
 int mohid_ad_ensemble_destroy(int* eid, int* stat);
+
+/* ======================================================================== */
+/* Device producers of the step's geometry and vertical water flux           */
+/* ======================================================================== */
+
+/*
+ * The geometry of a new water level on the instance's device arrays, as
+ * ModuleGeometry computes it before the transport call
+ * (Software/MOHIDBase2/ModuleGeometry.F90): StoreVolumeZOld (GEO:4335-4370)
+ * when *store_old != 0, then ComputeDistances (GEO:3798-4103: DWZ = SZZ(k-1) -
+ * SZZ(k) on water points, the face thicknesses DUZ / DVZ between water points,
+ * minimum or DUX/DVY-weighted by *faces_option, DZZ = (DWZ(k+1) + DWZ(k)) / 2),
+ * ComputeVolumes (GEO:4108-4163: VolumeZ = DWZ * DUX * DVY) and ComputeAreas
+ * (GEO:4238-4288: AreaU = DUZ * DYY, AreaV = DVZ * DXX; without
+ * impermeability).  SZZ: layer interface depths (Size box), DXX, DYY (2-D Size
+ * box), all device pointers; WaterPoints3D is the one of the last
+ * mohid_ad_set_hydro*, DUX / DVY those of mohid_ad_init.  Every value is the
+ * reference's, bit for bit; arrays keep their values where the reference does
+ * not write them.  Asynchronous on the instance's stream.
+ */
+int mohid_ad_geometry_dev(const int* id, const double* SZZ, const double* DXX, const double* DYY,
+                          const int* faces_option, const int* store_old, int* stat);
+
+/*
+ * The vertical water flux of the instance from continuity, in place
+ * (ModuleHydrodynamic.F90 WaterFlux_Z_VarGrid HD:43270-43308 when
+ * *var_grid != 0, WaterFlux_Z_FixGrid HD:43315-43349 otherwise): on every
+ * water point, Wflux_Z(k+1) = Wflux_Z(k) + West - East + South - North
+ * [- (VolumeZ - VolumeZOld) / DT], from the instance's horizontal fluxes,
+ * volumes and compute-face masks.  Wflux_Z at each column's floor is kept.
+ * Asynchronous on the instance's stream.
+ */
+int mohid_ad_vertical_flux(const int* id, const double* DT, const int* var_grid, int* stat);
 
 /* ======================================================================== */
 /* Stand-alone THOMASZ (replaces SolveThomas_C with dim = 2 = Z)             */

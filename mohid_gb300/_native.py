@@ -112,6 +112,9 @@ _AD_SIGS = {
     "mohid_ad_ensemble_create": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p]),
     "mohid_ad_ensemble_step": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p, c_int_p, c_int_p]),
     "mohid_ad_ensemble_destroy": (C.c_int, [c_int_p, c_int_p]),
+    "mohid_ad_get_hydro": (C.c_int, [c_int_p] + [c_double_p] * 11 + [c_int_p, c_int_p]),
+    "mohid_ad_geometry_dev": (C.c_int, [c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_vertical_flux": (C.c_int, [c_int_p, c_double_p, c_int_p, c_int_p]),
     "mohid_ad_mass_f64_noalloc": (C.c_int, [C.POINTER(T_Size3D), C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, c_int_p]),
 }

@@ -77,6 +77,45 @@ class AdvectionDiffusion:
             C.byref(st))
         N.check(rc, "mohid_ad_set_hydro_dev")
 
+    def set_fields(self, fields: dict, device: bool = False):
+        """Update some FP64 hydrodynamic fields and keep the rest and the masks
+        (mohid_ad_set_hydro[_dev] with NULL for what is kept).  `fields` maps F3
+        names to float64 Size-box numpy arrays, or torch CUDA tensors when device."""
+        if device:
+            args = [C.cast(C.c_void_p(fields[n].data_ptr()), N.c_double_p) if n in fields else None for n in F3]
+        else:
+            args = [N.ptr(fields[n]) if n in fields else None for n in F3]
+        st = C.c_int(0)
+        fn = "mohid_ad_set_hydro_dev" if device else "mohid_ad_set_hydro"
+        rc = getattr(self.lib, fn)(C.byref(self._id), *args, *([None] * len(I3)), None, C.byref(st))
+        N.check(rc, fn)
+
+    def get_fields(self, names=F3) -> dict:
+        """The instance's current FP64 hydrodynamic fields (mohid_ad_get_hydro) as numpy arrays."""
+        out = {n: np.empty(self.domain.shape3) for n in names}
+        args = [N.ptr(out[n]) if n in out else None for n in F3]
+        st = C.c_int(0)
+        N.check(self.lib.mohid_ad_get_hydro(C.byref(self._id), *args, C.byref(C.c_int(0)), C.byref(st)),
+                "mohid_ad_get_hydro")
+        return out
+
+    def geometry(self, SZZ, DXX, DYY, faces_option: int = 3, store_old: bool = True):
+        """Geometry of a new water level on the device (mohid_ad_geometry_dev): SZZ,
+        DXX, DYY torch CUDA float64 tensors (Size box / 2-D Size box)."""
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_geometry_dev(C.byref(self._id), C.c_void_p(SZZ.data_ptr()),
+                                            C.c_void_p(DXX.data_ptr()), C.c_void_p(DYY.data_ptr()),
+                                            C.byref(C.c_int(int(faces_option))), C.byref(C.c_int(int(store_old))),
+                                            C.byref(st))
+        N.check(rc, "mohid_ad_geometry_dev")
+
+    def vertical_flux(self, dt: float, var_grid: bool = True):
+        """Vertical water flux from continuity on the device (mohid_ad_vertical_flux)."""
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_vertical_flux(C.byref(self._id), C.byref(C.c_double(dt)),
+                                             C.byref(C.c_int(int(var_grid))), C.byref(st))
+        N.check(rc, "mohid_ad_vertical_flux")
+
     def step(self, PROP: np.ndarray, p: N.MohidAdParams, ReferenceProp: np.ndarray | None = None):
         """AdvectionDiffusion for one property: PROP (float64, Size box) updated in place."""
         if PROP.dtype != np.float64 or not PROP.flags.c_contiguous or PROP.shape != self.domain.shape3:

@@ -30,6 +30,7 @@ CUDA_UNITS = [
     ("ensemble_kernel.cu", []),
     ("batched_pack.cu", []),
     ("mass_noalloc.cu", []),
+    ("producers.cu", ["--fmad=false"]),
     ("abi.cpp", []),
     ("batched_abi.cpp", []),
 ]

@@ -46,7 +46,8 @@ int g_fail_alloc = 0;
 void Instance::release()
 {
     DevBuf<double>* d[] = {&DUX, &DVY, &DZX, &DZY, &Qx, &Qy, &Qz, &Vold, &V, &ViscH,
-                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid, &flux};
+                           &DiffV, &AreaU, &AreaV, &DZZ, &DWZ, &Pin, &Pout, &Ref, &sys, &Wl, &Pmid, &flux,
+                           &DUZ, &DVZ};
     for (auto* b : d) b->release();
     DevBuf<int>* i[] = {&KFloor, &BP2D, &OP, &LP, &WP, &CFU, &CFV, &CFW, &SD, &bcols, &cycl, &NFU, &NFV, &NFW,
                         &dStart};
@@ -278,23 +279,38 @@ int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const dou
                  const int* ComputeFacesV3D, const int* ComputeFacesW3D, const int* SmallDepths,
                  int* stat)
 {
-    const void* src[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU,
-                         AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
-                         ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D};
-    for (const void* s : src)
-        if (!s) return fail(MOHID_AD_ERR_NULLPTR, stat, "a required hydrodynamic array is NULL");
+    const double* ds[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU, AreaV, DZZ, DWZ};
+    const int* is[] = {OpenPoints3D, LandPoints3D, WaterPoints3D, ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D};
+    // After the first complete call, a NULL array keeps the instance's copy
+    // (unchanged since the last call, or produced on the device); the six
+    // masks are given all together or not at all.
+    int nmask = 0;
+    for (const int* m : is) nmask += m != nullptr;
+    if (!in->hydro) {
+        for (const double* d : ds)
+            if (!d) return fail(MOHID_AD_ERR_NULLPTR, stat, "a required hydrodynamic array is NULL");
+        if (nmask != 6) return fail(MOHID_AD_ERR_NULLPTR, stat, "a required mask array is NULL");
+    } else if (nmask != 0 && nmask != 6) {
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "give the six 3-D masks together, or none to keep them");
+    }
     const cudaMemcpyKind kind = fromDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     CK(cudaSetDevice(in->device));
     const size_t bd = sizeof(double) * in->n3, bi = sizeof(int) * in->n3;
     DevBuf<double>* dd[] = {&in->Qx, &in->Qy, &in->Qz, &in->Vold, &in->V, &in->ViscH, &in->DiffV,
                             &in->AreaU, &in->AreaV, &in->DZZ, &in->DWZ};
-    const double* ds[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU, AreaV, DZZ, DWZ};
-    for (int q = 0; q < 11; ++q) CK(cudaMemcpyAsync(dd[q]->p, ds[q], bd, kind, in->stream));
+    for (int q = 0; q < 11; ++q)
+        if (ds[q]) CK(cudaMemcpyAsync(dd[q]->p, ds[q], bd, kind, in->stream));
+    ++in->hydroVersion;
+    if (nmask == 0) {
+        // the masks stay; host buffers are consumed before returning
+        if (!fromDevice) CK(cudaStreamSynchronize(in->stream));
+        return ok(stat);
+    }
     DevBuf<int>* di[] = {&in->OP, &in->LP, &in->WP, &in->CFU, &in->CFV, &in->CFW};
-    const int* is[] = {OpenPoints3D, LandPoints3D, WaterPoints3D, ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D};
     for (int q = 0; q < 6; ++q) CK(cudaMemcpyAsync(di[q]->p, is[q], bi, kind, in->stream));
     in->hasSD = SmallDepths != nullptr;
     if (SmallDepths) CK(cudaMemcpyAsync(in->SD.p, SmallDepths, sizeof(int) * in->n2, kind, in->stream));
+    ++in->maskVersion;
     CK(cudaMemsetAsync(in->status.p, 0, sizeof(unsigned int), in->stream));
     CK(mohid::launch_check_faces(in->ni, in->nj, in->nk, in->CFU.p, in->CFV.p, in->CFW.p,
                                  in->status.p, in->stream));
@@ -303,7 +319,6 @@ int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const dou
     std::string why;
     int code = status_to_code(*in->hstatus, why);
     in->hydro = code == MOHID_AD_SUCCESS;
-    ++in->hydroVersion;
     if (code) return fail(code, stat, why);
     return ok(stat);
 }
@@ -448,6 +463,26 @@ int mohid_ad_set_hydro_dev(const int* id, const double* Wflux_X, const double* W
     return upload_hydro(in, true, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
                         AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
                         ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
+}
+
+int mohid_ad_get_hydro(const int* id, double* Wflux_X, double* Wflux_Y, double* Wflux_Z, double* VolumeZOld,
+                       double* VolumeZ, double* Visc_H, double* Diff_V, double* AreaU, double* AreaV, double* DZZ,
+                       double* DWZ, const int* on_device, int* stat)
+{
+    TraceRange trace_("mohid_ad_get_hydro");
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (!on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "the instance has no hydrodynamics set");
+    CK(cudaSetDevice(in->device));
+    double* dst[] = {Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V, AreaU, AreaV, DZZ, DWZ};
+    DevBuf<double>* src[] = {&in->Qx, &in->Qy, &in->Qz, &in->Vold, &in->V, &in->ViscH, &in->DiffV,
+                             &in->AreaU, &in->AreaV, &in->DZZ, &in->DWZ};
+    const cudaMemcpyKind kind = *on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    for (int q = 0; q < 11; ++q)
+        if (dst[q]) CK(cudaMemcpyAsync(dst[q], src[q]->p, sizeof(double) * in->n3, kind, in->stream));
+    CK(cudaStreamSynchronize(in->stream));
+    return ok(stat);
 }
 
 int mohid_ad_step_prop_f64_dev(const int* id, const double* PROP_in, double* PROP_out,

@@ -208,7 +208,9 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s);
-// *out = max(0, max over open non-boundary water cells of |R| - tol * sum |terms|)
+// *out = max(0, max over open non-boundary water cells of |R| - tol * sum |terms|),
+// R the cell's water budget, and on the top cell of open boundary columns R =
+// the surface flux (the step maps constants onto themselves when *out == 0)
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
                                 const int* CFW, const int* BP2D, double DT, double tol, const BLayout& L,

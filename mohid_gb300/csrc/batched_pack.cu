@@ -227,7 +227,8 @@ __global__ void k_water_mean(const double* partial, int nb, double* out)
 // Continuity over open, non-boundary water cells, with the fluxes the step
 // applies (Fortran-layout FP64 inputs):
 //   R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT
-// over compute faces; the result is max(0, max over cells of |R| - tol * sum of
+// over compute faces, and on the top cell of each open boundary column
+// R = Qz(KUB+1); the result is max(0, max over cells of |R| - tol * sum of
 // the terms' magnitudes).  When it is 0 the step maps a constant field onto
 // itself to round-off.
 __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, const double* Qy, const double* Qz,
@@ -241,7 +242,13 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
     double m = 0.0;
     for_rows(L, 1, nk, [&](long long a, long long, int i, int j, int k) {
         if (i < 1 || i > L.ni || j < 1 || j > L.nj) return;
-        if (OP[a] != 1 || BP2D[i + (long long)NI * j] == 1) return;
+        if (OP[a] != 1) return;
+        // an open boundary cell maps constants onto themselves (its reference
+        // shifted with them) when its exterior-face balance WFOB takes up the
+        // rest, except for the surface face, which the step applies at the
+        // top cell but WFOB leaves out: that flux must vanish there
+        const bool bp = BP2D[i + (long long)NI * j] == 1;
+        if (bp && k != nk) return;
         double r = 0.0, s = 0.0, f;
         f = CFU[a] == 1 ? Qx[a] : 0.0; r += f; s += fabs(f);
         f = CFU[a + NI] == 1 ? Qx[a + NI] : 0.0; r -= f; s += fabs(f);
@@ -250,6 +257,7 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
         f = CFW[a] == 1 ? Qz[a] : 0.0; r += f; s += fabs(f);
         f = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0); r -= f; s += fabs(f);
         f = (V[a] - Vold[a]) * rDT; r -= f; s += fabs(f);
+        if (bp) r = Qz[a + sk];                    // the surface flux of the boundary column
         m = fmax(m, fma(-tol, s, fabs(r)));       // > 0 where |R| exceeds tol * sum |terms|
     });
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));

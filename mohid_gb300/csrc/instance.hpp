@@ -55,8 +55,11 @@ struct Instance {
     // per-step hydrodynamics
     DevBuf<double> Qx, Qy, Qz, Vold, V, ViscH, DiffV, AreaU, AreaV, DZZ, DWZ;
     DevBuf<int> OP, LP, WP, CFU, CFV, CFW, SD;
+    // face thicknesses DUZ, DVZ of the geometry producer (allocated on first use)
+    DevBuf<double> DUZ, DVZ;
     bool hydro = false, hasSD = false;
-    unsigned hydroVersion = 0;
+    unsigned hydroVersion = 0;         // bumped by every change of the per-step hydrodynamics
+    unsigned maskVersion = 0;          // bumped by every upload of the 3-D masks
     // per-property staging for the host-pointer entry points
     DevBuf<double> Pin, Pout, Ref;
     // implicit horizontal advection (allocated on first use): the rows of the

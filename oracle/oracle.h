@@ -83,6 +83,16 @@ int ora_advection_face(const double P[4], const double V[4], const double du[4],
  * AdvFluxY, AdvFluxZ, DifFluxX, DifFluxY, DifFluxZ (Size box); NULL if none. */
 const double* ora_cell_flux(const ora_work* w, int which);
 
+/* Producers (producers.c): ComputeDistances / ComputeVolumes / ComputeAreas /
+ * StoreVolumeZOld of ModuleGeometry, in place, and WaterFlux_Z_VarGrid
+ * (var_grid != 0) / _FixGrid of ModuleHydrodynamic, in place on Qz. */
+void ora_geometry(int ni, int nj, int nk, const double* SZZ, const int* WP, const double* DUX,
+                  const double* DVY, const double* DXX, const double* DYY, int faces_option,
+                  int store_old, double* DWZ, double* DUZ, double* DVZ, double* DZZ, double* VolumeZ,
+                  double* VolumeZOld, double* AreaU, double* AreaV);
+void ora_vertical_flux(int ni, int nj, int nk, const double* Qx, const double* Qy, double* Qz, const double* Vnew,
+                       const double* Vold, const int* CFU, const int* CFV, const int* WP, double dt, int var_grid);
+
 /* Compensated (Neumaier) FP64 sum of VolumeZ*PROP over water cells of the work box. */
 double ora_mass(const ora_domain* d, const double* PROP);
 double ora_mass_f32(const ora_domain* d, const float* PROP);

@@ -129,6 +129,12 @@ def lib():
         L.ora_mass.argtypes = [C.POINTER(OraDomain), _dp]
         L.ora_mass_f32.restype = C.c_double
         L.ora_mass_f32.argtypes = [C.POINTER(OraDomain), _fp]
+        L.ora_geometry.restype = None
+        L.ora_geometry.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _ip, _dp, _dp, _dp, _dp, C.c_int, C.c_int] + \
+            [_dp] * 8
+        L.ora_vertical_flux.restype = None
+        L.ora_vertical_flux.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
+                                        C.c_double, C.c_int]
         _lib = L
     return _lib
 
@@ -212,3 +218,26 @@ def mass(dom, P) -> float:
     if P.dtype == np.float32:
         return lib().ora_mass_f32(C.byref(cd), _p(P, _fp))
     return lib().ora_mass(C.byref(cd), _p(P))
+
+
+GEOMETRY_OUT = ("DWZ", "DUZ", "DVZ", "DZZ", "VolumeZ", "VolumeZOld", "AreaU", "AreaV")
+
+
+def geometry(ni, nj, nk, SZZ, WP, DUX, DVY, DXX, DYY, faces_option, store_old, out: dict) -> None:
+    """ComputeDistances / ComputeVolumes / ComputeAreas (and StoreVolumeZOld when
+    store_old) of ModuleGeometry, in place on the arrays of `out` (keys
+    GEOMETRY_OUT, float64 Size box)."""
+    for n in GEOMETRY_OUT:
+        assert out[n].dtype == np.float64 and out[n].flags.c_contiguous
+    lib().ora_geometry(ni, nj, nk, _p(SZZ), _p(WP, _ip), _p(DUX), _p(DVY), _p(DXX), _p(DYY),
+                       int(faces_option), int(store_old), *[_p(out[n]) for n in GEOMETRY_OUT])
+
+
+def vertical_flux(dom, Qz: np.ndarray, dt: float, var_grid: bool) -> None:
+    """WaterFlux_Z_VarGrid (var_grid) / WaterFlux_Z_FixGrid of ModuleHydrodynamic,
+    in place on Qz, from the domain's horizontal fluxes, volumes and masks."""
+    a = dom.arrays
+    assert Qz.dtype == np.float64 and Qz.flags.c_contiguous
+    lib().ora_vertical_flux(dom.ni, dom.nj, dom.nk, _p(a["Wflux_X"]), _p(a["Wflux_Y"]), _p(Qz), _p(a["VolumeZ"]),
+                            _p(a["VolumeZOld"]), _p(a["ComputeFacesU3D"], _ip), _p(a["ComputeFacesV3D"], _ip),
+                            _p(a["WaterPoints3D"], _ip), float(dt), int(bool(var_grid)))
