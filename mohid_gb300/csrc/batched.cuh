@@ -191,6 +191,19 @@ cudaError_t obc_flux(const BatchArgs& a, const int* list, bool halfQ, cudaStream
 // the same for `nb` batches from their argument records (device): mpart and
 // obpart of each record select what runs for that batch
 cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s);
+// pack_fields, vol_changed, water_volume and (DT > 0) the constant-preservation
+// check of continuity_residual in one pass, into *cont (m: the largest
+// magnitude among each cell's terms in place of their sum); masks: the flag
+// bytes are formed from the masks (they changed), else the stored ones are
+// read.  vpart: 2 * nvblocks doubles of scratch (nvblocks <= 16384).
+cudaError_t pack_state(const double* Qx, const double* Qy, const double* Qz, const double* V, const double* Vold,
+                       const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
+                       const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
+                       const int* BP2D, bool masks, void* oQx, void* oQy, void* oQz, void* oVis, void* oDif,
+                       bool halfQ, bool halfK, const float* dinv, float* oAU, float* oAV, float* orDZZ, float* oRV,
+                       float* oDVR, float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
+                       double* Vprev, unsigned* vchanged, double* vpart, int nvblocks, double* mfix, double DT,
+                       double tol, double* cont, const BLayout& L, cudaStream_t s);
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
                          const int* KFloor, const int* BP2D, const int* WP, const int* OP,
                          const int* CFW, const int* SD, float4* fc, float* areaCol,
@@ -208,7 +221,7 @@ cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double 
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s);
-// *out = max(0, max over open non-boundary water cells of |R| - tol * sum |terms|),
+// *out = max(0, max over open non-boundary water cells of |R| - tol * max |term|),
 // R the cell's water budget, and on the top cell of open boundary columns R =
 // the surface flux (the step maps constants onto themselves when *out == 0)
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,

@@ -55,6 +55,10 @@ struct Batch {
     bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
     bool staticVol = false;              // the packed hydrodynamics have VolumeZ == VolumeZOld
     bool packedOnce = false;
+    unsigned packedMask = 0;             // mask version of the last completed pack
+    unsigned packingMask = 0;            // ... and of the pack in flight
+    bool packingMasks = true;            // the pack in flight formed flags and schedule from the masks
+    DevBuf<double> vpart;                // per-block water-volume sums of the pack
     bool fixDirty = false;               // the device constants / corrections differ from `shift`
     int tilesX = 0, ntiles = 0;
     // launch schedule: one CTA per tile, or a persistent grid over the tiles
@@ -125,7 +129,7 @@ struct Batch {
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
         partial.release(); scratch.release(); stage.release();
-        mfix.release(); mpart.release(); moving.release(); Vprev.release();
+        mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release();
         obpart.release(); obcol.release(); obcnt.release();
         tl.release(); tcost.release();
         dscale.release(); dinv.release(); vchanged.release(); tpartial.release(); tscratch.release();
@@ -150,6 +154,7 @@ std::mutex g_bmu;
 std::map<int, Batch*> g_batch;
 int g_next_bid = 1;
 constexpr int kMassBlocks = 1024;
+constexpr int kPackBlocks = 2048;            // blocks of the per-cell repack pass
 
 Batch* blookup(const int* bid)
 {
@@ -276,34 +281,39 @@ int pack_enqueue(Batch* b, int* stat)
         CK(mohid::fp16_scales(f, 5, (long long)in->n3, b->scratch.p, b->dscale.p, b->dinv.p, s));
         CK(cudaMemcpyAsync(b->hp->scale, b->dscale.p, 5 * sizeof(float), cudaMemcpyDeviceToHost, s));
     }
-    CK(mohid::vol_changed(in->V.p, b->Vprev.p, (long long)in->n3, b->vchanged.p, s));
-    CK(mohid::pack_fields(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
-                          in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
-                          in->CFV.p, in->CFW.p,
-                          hq ? (void*)b->Qx16.p : (void*)b->Qx32.p, hq ? (void*)b->Qy16.p : (void*)b->Qy32.p,
-                          hq ? (void*)b->Qz16.p : (void*)b->Qz32.p, hk ? (void*)b->Vis16.p : (void*)b->Vis32.p,
-                          hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, (hq || hk) ? b->dinv.p : nullptr,
-                          b->AreaU.p, b->AreaV.p, b->DZZ.p, b->RV.p, b->DVR.p, b->Vhi.p, b->Vlo.p, b->flag.p,
-                          b->fflag.p, b->moving.p, L, s));
-    CK(mohid::water_volume(in->V.p, in->WP.p, L, b->partial.p, kMassBlocks, b->mfix.p, s));
-    CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
-                           in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
-                           b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
-    CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
-    CK(mohid::obc_columns(b->cflag.p, L, b->obcnt.p, b->obcol.p, s));
-    // tiles left out of a schedule keep no stale mass-fixer sums
-    CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
-    CK(cudaMemcpyAsync(b->hcost, b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
+    // the per-cell pass (fields, flag bytes when the masks changed, volume
+    // change, water volume, and the constant-preservation check for the DT of
+    // the last step); the per-column data and the tile schedule only when the
+    // masks changed
+    const bool masks = !b->packedOnce || b->packedMask != in->maskVersion;
+    const double cdt = (b->checkedDT > 0.0 && b->checkedFlags == 0) ? b->checkedDT : 0.0;
+    CK(mohid::pack_state(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
+                         in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
+                         in->CFV.p, in->CFW.p, in->BP2D.p, masks,
+                         hq ? (void*)b->Qx16.p : (void*)b->Qx32.p, hq ? (void*)b->Qy16.p : (void*)b->Qy32.p,
+                         hq ? (void*)b->Qz16.p : (void*)b->Qz32.p, hk ? (void*)b->Vis16.p : (void*)b->Vis32.p,
+                         hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, (hq || hk) ? b->dinv.p : nullptr,
+                         b->AreaU.p, b->AreaV.p, b->DZZ.p, b->RV.p, b->DVR.p, b->Vhi.p, b->Vlo.p, b->flag.p,
+                         b->fflag.p, b->moving.p, b->Vprev.p, b->vchanged.p, b->vpart.p, kPackBlocks, b->mfix.p,
+                         cdt, kContinuityTol, b->scratch.p + 5, L, s));
+    if (masks) {
+        CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
+                               in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
+                               b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
+        CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
+        CK(mohid::obc_columns(b->cflag.p, L, b->obcnt.p, b->obcol.p, s));
+        // tiles left out of a schedule keep no stale mass-fixer sums
+        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
+        CK(cudaMemcpyAsync(b->hcost, b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
+    }
+    b->packingMasks = masks;
+    b->packingMask = in->maskVersion;
     CK(cudaMemcpyAsync(&b->hp->moving, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(&b->hp->vchanged, b->vchanged.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     b->hp->cont = -1.0;
     b->hp->contDT = b->checkedDT;
-    if (b->checkedDT > 0.0 && b->checkedFlags == 0) {   // continuity for the DT of the last step
-        CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p, in->CFU.p,
-                                      in->CFV.p, in->CFW.p, in->BP2D.p, b->checkedDT, kContinuityTol, L,
-                                      b->scratch.p + 5, s));
+    if (cdt > 0.0)                                      // continuity for the DT of the last step
         CK(cudaMemcpyAsync(&b->hp->cont, b->scratch.p + 5, sizeof(double), cudaMemcpyDeviceToHost, s));
-    }
     CK(cudaEventRecord(b->packEv, s));
     // tensor maps of the shared fields and of the tracer buffers (host only)
     {
@@ -372,6 +382,15 @@ int pack_finalize(Batch* b, int* stat)
                 CK(cudaStreamSynchronize(s));
             }
     b->packedOnce = true;
+    b->packedMask = b->packingMask;
+    if (!b->packingMasks) {                      // the masks, and with them the schedule, are unchanged
+        b->preCont = h.cont;
+        b->preContDT = h.contDT;
+        b->preContVersion = b->packingVersion;
+        b->packed = true;
+        b->packedVersion = b->packingVersion;
+        return ok(stat);
+    }
     // tile schedule: tiles holding water, most layers first (stable by tile index)
     std::vector<int> order;
     for (int q = 0; q < b->ntiles; ++q)
@@ -749,6 +768,7 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->tl.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->tcost.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = b->vpart.alloc(2 * kPackBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(8)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->tscratch.alloc(4)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->tpartial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");

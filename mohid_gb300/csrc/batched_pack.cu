@@ -61,6 +61,12 @@ __device__ __forceinline__ bool same_bits(double a, double b)
     return __double_as_longlong(a) == __double_as_longlong(b);
 }
 
+// |x| as its bit pattern (orders like |x| for non-NaN values, no FP64 instruction)
+__device__ __forceinline__ unsigned long long abs_bits(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
 // Neumaier-compensated accumulation s + c += x
 __device__ __forceinline__ void neu_add(double& s, double& c, double x)
 {
@@ -176,6 +182,132 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_fields(PackIn in, PackOut 
     });
 }
 
+// The repack of a new hydrodynamic state in one pass over the Fortran-layout
+// FP64 fields (k_pack_fields' conversions) that also
+//  * flags a bit-level change of VolumeZ against the last pack (Vprev, updated
+//    where it changed);
+//  * sums VolumeZ over water cells of the work box (per-thread FP64, blocks
+//    by a fixed-order compensated tree; partials to vpart[2 b], vpart[2 b + 1] = 0);
+//  * when rDT > 0, checks that the step maps constants onto themselves (the
+//    check of k_continuity): on open non-boundary water cells
+//    R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT over
+//    the faces the step applies, on the top cell of open boundary columns R =
+//    Qz(KUB+1); *cont = max(0, max of |R| - tol * m), m the largest magnitude
+//    among the cell's terms (compared on the bit patterns, no FP64 work).
+// MASKS: the masks changed since the last pack and the flag bytes are formed
+// from them; otherwise the stored flag bytes are kept and read instead.
+struct FuseArgs {
+    double* Vprev;
+    unsigned* vchanged;
+    double* vpart;
+    const int* BP2D;
+    double rDT, tol;
+    unsigned long long* cont;
+};
+
+template <bool MASKS>
+__global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut out, BLayout L, FuseArgs f)
+{
+    const int NI = L.ni + 2, NJ = L.nj + 2, nk = L.nk;
+    const long long sk = (long long)NI * NJ;
+    float iv[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
+    if (out.inv)
+        for (int q = 0; q < 5; ++q) iv[q] = out.inv[q];
+    double vs = 0.0, cm = 0.0;
+    bool changed = false;
+    for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
+        put(out.Qx, out.halfQ, iv[0], g, in.Qx[e]);
+        put(out.Qy, out.halfQ, iv[1], g, in.Qy[e]);
+        put(out.Qz, out.halfQ, iv[2], g, in.Qz[e]);
+        put(out.Vis, out.halfK, iv[3], g, in.Vis[e]);
+        put(out.Dif, out.halfK, iv[4], g, in.Dif[e]);
+        out.AU[g] = f64_to_f32(in.AU[e]);
+        out.AV[g] = f64_to_f32(in.AV[e]);
+        const float dz = f64_to_f32(in.DZZ[e]);
+        out.rDZZ[g] = dz != 0.f ? __frcp_rn(dz) : 0.f;
+        const double v = in.V[e], vo = in.Vold[e];
+        const float vh = f64_to_f32(v);
+        out.Vhi[g] = vh;
+        out.Vlo[g] = f64_to_f32(v - (double)vh);
+        const float rv = vh != 0.f ? __frcp_rn(vh) : 0.f;
+        out.RV[g] = rv;
+        const bool still = same_bits(v, vo);
+        if (still) {
+            out.DVR[g] = 0.f;
+        } else {
+            *out.moving = 1u;
+            out.DVR[g] = f64_to_f32(v - vo) * rv;
+        }
+        if (!same_bits(v, f.Vprev[e])) { changed = true; f.Vprev[e] = v; }
+        uint8_t fl;
+        if (MASKS) {
+            const bool cfu = in.CFU[e] == 1 && j != L.nj + 1, cfv = in.CFV[e] == 1 && i != L.ni + 1;
+            const bool op = in.OP[e] == 1;
+            fl = 0;
+            if (in.WP[e] == 1) fl |= F_WP;
+            if (op) fl |= F_OP;
+            if (cfu) fl |= F_CFU;
+            if (cfv) fl |= F_CFV;
+            if (in.CFW[e] == 1) fl |= F_CFW;
+            if (in.LP[e] == 1) fl |= F_LP;
+            out.flag[g] = fl;
+            auto opn = [&](int di, int dj) -> bool {
+                const int ii = i + di, jj = j + dj;
+                return ii >= 0 && ii < NI && jj >= 0 && jj < NJ && in.OP[e + di + (long long)NI * dj] == 1;
+            };
+            uint8_t ff = 0;
+            if (cfu) { ff |= FU_ACT; if (op && opn(0, -1)) ff |= FU_ADV; }
+            if (opn(0, -2)) ff |= FU_TVDP;
+            if (opn(0, 1)) ff |= FU_TVDN;
+            if (cfv) { ff |= FV_ACT; if (op && opn(-1, 0)) ff |= FV_ADV; }
+            if (opn(-2, 0)) ff |= FV_TVDP;
+            if (opn(1, 0)) ff |= FV_TVDN;
+            out.fflag[g] = ff;
+        } else {
+            fl = out.flag[g];
+        }
+        const bool work = i >= 1 && i <= L.ni && j >= 1 && j <= L.nj && k >= 1 && k <= nk;
+        if (!work) return;
+        if (fl & F_WP) vs += v;
+        if (f.rDT > 0.0 && (fl & F_OP)) {
+            // the east / north / top neighbours' flags: written by other
+            // threads in MASKS mode, so formed here from the masks
+            bool cfe, cfn, cft;
+            if (MASKS) {
+                cfe = in.CFU[e + NI] == 1 && j + 1 != L.nj + 1;
+                cfn = in.CFV[e + 1] == 1 && i + 1 != L.ni + 1;
+                cft = in.CFW[e + sk] == 1;
+            } else {
+                cfe = out.flag[g + L.px] & F_CFU;
+                cfn = out.flag[g + 1] & F_CFV;
+                cft = out.flag[g + L.sl] & F_CFW;
+            }
+            const bool bp = f.BP2D[i + (long long)NI * j] == 1;
+            if (bp && k != nk) return;
+            const double qw = (fl & F_CFU) ? in.Qx[e] : 0.0, qe = cfe ? in.Qx[e + NI] : 0.0;
+            const double qs = (fl & F_CFV) ? in.Qy[e] : 0.0, qn = cfn ? in.Qy[e + 1] : 0.0;
+            const double qb = (fl & F_CFW) ? in.Qz[e] : 0.0;
+            const double qt = (k < nk) ? (cft ? in.Qz[e + sk] : 0.0) : in.Qz[e + sk];
+            const double dv = still ? 0.0 : (v - vo) * f.rDT;
+            unsigned long long m = abs_bits(qw);
+            m = max(m, abs_bits(qe)); m = max(m, abs_bits(qs)); m = max(m, abs_bits(qn));
+            m = max(m, abs_bits(qb)); m = max(m, abs_bits(qt)); m = max(m, abs_bits(dv));
+            const double r = bp ? qt : qw - qe + qs - qn + qb - qt - dv;
+            cm = fmax(cm, fma(-f.tol, __longlong_as_double((long long)m), fabs(r)));
+        }
+    });
+    if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) *f.vchanged = 1u;
+    if (f.rDT > 0.0) {
+        for (int o = 16; o > 0; o >>= 1) cm = fmax(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+        if ((threadIdx.x & 31) == 0 && cm > 0.0) atomicMax(f.cont, (unsigned long long)__double_as_longlong(cm));
+    }
+    const double S = block_neu(vs, 0.0);
+    if (threadIdx.x == 0) {
+        f.vpart[2 * blockIdx.x] = S;
+        f.vpart[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
 __global__ void __launch_bounds__(kRowThreads) k_pack_shift_f32(const double* __restrict__ src, float* __restrict__ dst,
                                                                const int* __restrict__ WP, double shift, BLayout L)
 {
@@ -227,10 +359,10 @@ __global__ void k_water_mean(const double* partial, int nb, double* out)
 // Continuity over open, non-boundary water cells, with the fluxes the step
 // applies (Fortran-layout FP64 inputs):
 //   R = Qx(w) - Qx(e) + Qy(s) - Qy(n) + Qz(k) - Qz(k+1) - (V - Vold)/DT
-// over compute faces, and on the top cell of each open boundary column
-// R = Qz(KUB+1); the result is max(0, max over cells of |R| - tol * sum of
-// the terms' magnitudes).  When it is 0 the step maps a constant field onto
-// itself to round-off.
+// over the faces the step applies, and on the top cell of each open boundary
+// column R = Qz(KUB+1); the result is max(0, max over cells of |R| - tol *
+// the largest magnitude among the terms).  When it is 0 the step maps a
+// constant field onto itself to round-off.
 __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, const double* Qy, const double* Qz,
                                                           const double* V, const double* Vold, const int* OP,
                                                           const int* CFU, const int* CFV, const int* CFW,
@@ -249,16 +381,20 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
         // top cell but WFOB leaves out: that flux must vanish there
         const bool bp = BP2D[i + (long long)NI * j] == 1;
         if (bp && k != nk) return;
-        double r = 0.0, s = 0.0, f;
-        f = CFU[a] == 1 ? Qx[a] : 0.0; r += f; s += fabs(f);
-        f = CFU[a + NI] == 1 ? Qx[a + NI] : 0.0; r -= f; s += fabs(f);
-        f = CFV[a] == 1 ? Qy[a] : 0.0; r += f; s += fabs(f);
-        f = CFV[a + 1] == 1 ? Qy[a + 1] : 0.0; r -= f; s += fabs(f);
-        f = CFW[a] == 1 ? Qz[a] : 0.0; r += f; s += fabs(f);
-        f = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0); r -= f; s += fabs(f);
-        f = (V[a] - Vold[a]) * rDT; r -= f; s += fabs(f);
-        if (bp) r = Qz[a + sk];                    // the surface flux of the boundary column
-        m = fmax(m, fma(-tol, s, fabs(r)));       // > 0 where |R| exceeds tol * sum |terms|
+        // the faces the step applies: compute faces, those on the j = JUB+1 /
+        // i = IUB+1 planes excepted
+        const double qw = CFU[a] == 1 ? Qx[a] : 0.0;
+        const double qe = (CFU[a + NI] == 1 && j + 1 != L.nj + 1) ? Qx[a + NI] : 0.0;
+        const double qs = CFV[a] == 1 ? Qy[a] : 0.0;
+        const double qn = (CFV[a + 1] == 1 && i + 1 != L.ni + 1) ? Qy[a + 1] : 0.0;
+        const double qb = CFW[a] == 1 ? Qz[a] : 0.0;
+        const double qt = (k < nk && CFW[a + sk] == 1) ? Qz[a + sk] : (k == nk ? Qz[a + sk] : 0.0);
+        const double dv = (V[a] - Vold[a]) * rDT;
+        unsigned long long mb = abs_bits(qw);
+        mb = max(mb, abs_bits(qe)); mb = max(mb, abs_bits(qs)); mb = max(mb, abs_bits(qn));
+        mb = max(mb, abs_bits(qb)); mb = max(mb, abs_bits(qt)); mb = max(mb, abs_bits(dv));
+        const double r = bp ? qt : qw - qe + qs - qn + qb - qt - dv;   // bp: the boundary column's surface flux
+        m = fmax(m, fma(-tol, __longlong_as_double((long long)mb), fabs(r)));   // > 0 where |R| > tol * max |term|
     });
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
@@ -607,6 +743,31 @@ cudaError_t pack_fields(const double* Qx, const double* Qy, const double* Qz, co
     cudaError_t e = cudaMemsetAsync(moving, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     k_pack_fields<<<row_blocks(L, L.nk + 2), kRowThreads, 0, s>>>(in, out, L);
+    return cudaGetLastError();
+}
+cudaError_t pack_state(const double* Qx, const double* Qy, const double* Qz, const double* V, const double* Vold,
+                       const double* Vis, const double* Dif, const double* AU, const double* AV, const double* DZZ,
+                       const int* WP, const int* OP, const int* LP, const int* CFU, const int* CFV, const int* CFW,
+                       const int* BP2D, bool masks, void* oQx, void* oQy, void* oQz, void* oVis, void* oDif,
+                       bool halfQ, bool halfK, const float* dinv, float* oAU, float* oAV, float* orDZZ, float* oRV,
+                       float* oDVR, float* oVhi, float* oVlo, uint8_t* oflag, uint8_t* offlag, unsigned* moving,
+                       double* Vprev, unsigned* vchanged, double* vpart, int nvblocks, double* mfix, double DT,
+                       double tol, double* cont, const BLayout& L, cudaStream_t s)
+{
+    PackIn in{Qx, Qy, Qz, V, Vold, Vis, Dif, AU, AV, DZZ, WP, OP, LP, CFU, CFV, CFW};
+    PackOut out{oQx, oQy, oQz, oVis, oDif, dinv, halfQ ? 1 : 0, halfK ? 1 : 0,
+                oAU, oAV, orDZZ, oRV, oDVR, oVhi, oVlo, oflag, offlag, moving};
+    FuseArgs f{Vprev, vchanged, vpart, BP2D, DT > 0.0 ? 1.0 / DT : 0.0, tol,
+               reinterpret_cast<unsigned long long*>(cont)};
+    cudaError_t e = cudaMemsetAsync(moving, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(vchanged, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess && DT > 0.0) e = cudaMemsetAsync(cont, 0, sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    const unsigned nb = (unsigned)nvblocks;
+    if (masks) k_pack_state<true><<<nb, kRowThreads, 0, s>>>(in, out, L, f);
+    else k_pack_state<false><<<nb, kRowThreads, 0, s>>>(in, out, L, f);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_fix_set<<<1, 32, 0, s>>>(vpart, nvblocks, mfix, 0, 0, 0, 0.0);
     return cudaGetLastError();
 }
 cudaError_t pack_columns(const double* DUX, const double* DVY, const double* DZX, const double* DZY,
