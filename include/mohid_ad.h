@@ -181,8 +181,14 @@ int mohid_ad_set_hydro(const int* id,
  * ModuleFunctions.F90:4026-4123).  ReferenceProp may be NULL (closed
  * boundaries); when given, `p->BoundaryCondition` selects the open-boundary
  * treatment (ModuleAdvectionDiffusion.F90:5369-5742): MassConservation,
- * ImposedValue, SubModel, NullGradient, MassConservNullGrad or Cyclic
- * (Orlanski returns MOHID_AD_ERR_UNSUPPORTED).  As in the reference,
+ * ImposedValue, SubModel, Orlanski, NullGradient, MassConservNullGrad or
+ * Cyclic.  Orlanski radiates the field outwards (OrlanskiCelerity2D,
+ * ModuleFunctions.F90:4129-4490): the exterior point of each open boundary
+ * cell (a halo cell, or for the corner i = IUB, j = JLB the interior point
+ * IUB-1) takes the radiated value, which the boundary cell's inflow carries
+ * in; a boundary point off the work box's edges returns MOHID_AD_ERR_OPTION
+ * (the reference stops), a grid under 3 cells wide whose radiation would read
+ * outside the layer plane MOHID_AD_ERR_BOUNDS.  As in the reference,
  * NullGradient sets the boundary columns to their neighbours' mean after the
  * solve whether or not ReferenceProp is given (AD:1874-1987), and Cyclic
  * (AD:2121-2224) needs ReferenceProp (MOHID_AD_ERR_OPTION without it).
@@ -218,6 +224,18 @@ int mohid_ad_unset_discharges(const int* id, int* stat);
  * (MOHID_AD_ERR_NULLPTR otherwise).  All three NULL clears them.
  */
 int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, const int* NoFluxW, int* stat);
+
+/*
+ * The PropOld argument of AdvectionDiffusion (ModuleAdvectionDiffusion.F90:1139,
+ * 1253-1260).  Steps with Orlanski boundaries (BoundaryCondition 6 and a
+ * ReferenceProp) write into it the field as OpenBoundaryCondition saw it,
+ * PROPOld(:,:,:) = PROP(:,:,:) (AD:5428-5429): the step's input, or with
+ * implicit horizontal advection the line solution.  OrlanskiCelerity2D reads
+ * it as the previous time level.  Host (*on_device == 0) or device array over
+ * the Size box, kept by pointer: it must stay valid while steps run.  NULL
+ * detaches it; other boundary conditions leave it untouched.
+ */
+int mohid_ad_set_prop_old(const int* id, double* PropOld, const int* on_device, int* stat);
 
 /*
  * GetAdvFlux / GetDifFlux (ModuleAdvectionDiffusion.F90:697-860): the face

@@ -99,6 +99,7 @@ _AD_SIGS = {
     "mohid_ad_set_discharges": (C.c_int, [c_int_p, c_int_p] + [C.c_void_p] * 12 + [c_int_p]),
     "mohid_ad_unset_discharges": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_set_noflux": (C.c_int, [c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p]),
+    "mohid_ad_set_prop_old": (C.c_int, [c_int_p, C.c_void_p, c_int_p, c_int_p]),
     "mohid_ad_debug_fail_alloc": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_debug_wait_probe": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_get_adv_flux": (C.c_int, [c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p, c_int_p]),

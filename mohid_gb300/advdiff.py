@@ -159,6 +159,23 @@ class AdvectionDiffusion:
                                               C.byref(st))
         N.check(rc, "mohid_ad_set_noflux")
 
+    def set_prop_old(self, PropOld, device: bool = False):
+        """The PropOld array that steps with Orlanski boundaries write (the field as
+        OpenBoundaryCondition saw it): a float64 Size-box numpy array, or a device
+        tensor / pointer with device=True; kept by reference (None detaches)."""
+        st = C.c_int(0)
+        if PropOld is None:
+            ptr_, self._prop_old = None, None
+        elif device:
+            ptr_ = C.c_void_p(PropOld.data_ptr() if hasattr(PropOld, "data_ptr") else int(PropOld))
+            self._prop_old = PropOld
+        else:
+            assert PropOld.dtype == np.float64 and PropOld.flags.c_contiguous and PropOld.shape == self.domain.shape3
+            ptr_, self._prop_old = PropOld.ctypes.data_as(C.c_void_p), PropOld
+        rc = self.lib.mohid_ad_set_prop_old(C.byref(self._id), ptr_, C.byref(C.c_int(1 if device else 0)),
+                                            C.byref(st))
+        N.check(rc, "mohid_ad_set_prop_old")
+
     def cell_fluxes(self) -> dict:
         """The face fluxes of the last step (made with CellFluxes=1): AdvFluxX/Y/Z,
         DifFluxX/Y/Z as Size-box float64 arrays (mohid_ad_get_adv_flux / _dif_flux)."""

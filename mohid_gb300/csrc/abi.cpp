@@ -107,7 +107,6 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
             if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
                 why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
             }
-            if (bc == MOHID_BC_ORLANSKI) { why = "Orlanski open boundaries not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
         } else if (bc == MOHID_BC_CYCLIC) {
             why = "cyclic boundaries read ReferenceProp (reference Prop_CyclicBoundary)"; return MOHID_AD_ERR_OPTION;
         }
@@ -116,7 +115,13 @@ int check_params(const mohid_ad_params* p, bool hasRef, int nk, std::string& why
         why = "ImpExp_AdvXX / ImpExp_AdvYY must be 0 or 1 (reference HorizontalAdvectionXX/YY ERR01)";
         return MOHID_AD_ERR_OPTION;
     }
-    if (p->AdvectionNudging) { why = "AdvectionNudging not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->AdvectionNudging && (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0 || p->Vertical1D)) {
+        // the _Nudge routines put implicit horizontal coefficients into the
+        // vertical system (AD:4692-4696), and with Vertical1D AdvectionNudging
+        // reads arrays nothing set in the call (AD:1704, AD:4151-4157)
+        why = "AdvectionNudging with implicit horizontal advection or Vertical1D";
+        return MOHID_AD_ERR_UNSUPPORTED;
+    }
     if (nk > 200) { why = "KUB > 200 layers not supported"; return MOHID_AD_ERR_UNSUPPORTED; }
     return MOHID_AD_SUCCESS;
 }
@@ -127,6 +132,11 @@ int status_to_code(unsigned int s, std::string& why)
     if (s & MOHID_DEV_ZERO_PIVOT) { why = "THOMASZ zero pivot in a water column"; return MOHID_AD_ERR_ZERO_PIVOT; }
     if (s & MOHID_DEV_NONFINITE) { why = "non-finite concentration after the solve"; return MOHID_AD_ERR_NONFINITE; }
     if (s & MOHID_DEV_TIMEOUT) { why = "bounded device wait expired"; return MOHID_AD_ERR_TIMEOUT; }
+    if (s & MOHID_DEV_OBC_EDGE) {
+        why = "Orlanski: an open boundary point off the work box's edges (reference 'Orlanski Advection 2')";
+        return MOHID_AD_ERR_OPTION;
+    }
+    if (s & MOHID_DEV_OBC_READ) { why = "Orlanski: a read outside the layer plane (grid under 3 cells wide)"; return MOHID_AD_ERR_BOUNDS; }
     return MOHID_AD_SUCCESS;
 }
 
@@ -176,12 +186,31 @@ int run_step(Instance* in, const double* Pin, double* Pout, const double* Ref, c
         }
         return x;
     };
+    // Orlanski boundaries: the caller's PropOld and the radiated exterior
+    // values of the field the boundary condition sees (AD:5428-5429, 5496-5569)
+    const bool orl = Ref && p->BoundaryCondition == MOHID_BC_ORLANSKI;
+    const size_t bd = sizeof(double) * in->n3;
+    if (orl && !in->Pobc.p) {
+        cudaError_t e = in->Pobc.alloc(in->n3);
+        if (e != cudaSuccess) { in->Pobc.release(); return bad_alloc(e); }
+    }
+    auto orlanski = [&](mohid::PlainArgs& x) -> cudaError_t {
+        if (!orl) return cudaSuccess;
+        cudaError_t e = cudaMemcpyAsync(in->Pobc.p, x.P, bd, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess && in->propOld)
+            e = cudaMemcpyAsync(in->propOld, x.P, bd, in->propOldDev ? cudaMemcpyDeviceToDevice
+                                                                      : cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = mohid::launch_orlanski(x, in->Pobc.p, in->bcols.p, in->nbcols, s);
+        x.Pobc = in->Pobc.p;
+        return e;
+    };
     mohid::PlainArgs a = args(Pin, Pout);
     const bool imp = a.impXX || a.impYY;
     const bool lines3D = imp && in->nk > 1 && !a.vertical1D;
     const bool lines2D = imp && in->nk == 1;
     mohid::PlainArgs v = a;                      // the field the vertical terms see
     if (!lines3D && !lines2D) {
+        CK(orlanski(a));
         CK(mohid::launch_plain_f64(a, s));
     } else {
         if (!in->sys.p) {
@@ -191,17 +220,18 @@ int run_step(Instance* in, const double* Pin, double* Pout, const double* Ref, c
             if (e != cudaSuccess) { in->sys.release(); in->Wl.release(); in->Pmid.release(); return bad_alloc(e); }
         }
         a.sD = in->sys.p; a.sE = a.sD + in->n3; a.sF = a.sE + in->n3; a.sTI = a.sF + in->n3;
-        const size_t bd = sizeof(double) * in->n3;
         if (lines3D) {
             CK(mohid::launch_plain_f64(a, s, mohid::kPlainHorizRows));
             CK(cudaMemcpyAsync(in->Pmid.p, Pin, bd, cudaMemcpyDeviceToDevice, s));
             CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p,
                                         false, in->Wl.p, in->Pmid.p, in->status.p, s));
             v = args(in->Pmid.p, Pout);
+            CK(orlanski(v));
             CK(mohid::launch_plain_f64(v, s, mohid::kPlainVertical));
         } else {
+            CK(orlanski(a));
             CK(mohid::launch_plain_f64(a, s, mohid::kPlainRows2D));
-            CK(cudaMemcpyAsync(Pout, Pin, bd, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(Pout, orl ? in->Pobc.p : Pin, bd, cudaMemcpyDeviceToDevice, s));
             CK(mohid::launch_line_solve(in->ni, in->nj, in->nk, a.impXX != 0, a.sD, a.sE, a.sF, a.sTI, in->LP.p,
                                         true, in->Wl.p, Pout, in->status.p, s));
         }
@@ -243,6 +273,7 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.DUX = in->DUX.p; a.DVY = in->DVY.p; a.DZX = in->DZX.p; a.DZY = in->DZY.p;
     a.KFloor = in->KFloor.p; a.BP2D = in->BP2D.p;
     a.Ref = Ref;
+    a.Pobc = nullptr;
     a.DT = p->DTProp;
     a.schmidtH = p->schmidt_H; a.schmidtCoefV = p->SchmidtCoef_V; a.schmidtBackV = p->SchmidtBackground_V;
     a.volumeRelMax = p->VolumeRelMax; a.impExpDifV = p->ImpExp_DifV;
@@ -260,7 +291,9 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     a.impYY = p->ImpExp_AdvYY == 1.0;
     a.sD = a.sE = a.sF = a.sTI = nullptr;
     a.fAX = a.fAY = a.fAZ = a.fDX = a.fDY = a.fDZ = nullptr;
-    a.noAdv = p->NoAdvFlux != 0;
+    a.nudge = p->AdvectionNudging != 0;
+    a.nudgeCells = p->AdvectionNudgingCells;
+    a.noAdv = p->NoAdvFlux != 0 && !a.nudge;     // the _Nudge routines ignore the NoAdvFlux masks
     a.noDif = p->NoDifFlux != 0;
     a.NFU = in->hasNoFlux ? in->NFU.p : nullptr;
     a.NFV = in->hasNoFlux ? in->NFV.p : nullptr;
@@ -668,6 +701,19 @@ int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, c
     }
     CK(cudaStreamSynchronize(in->stream));
     in->hasNoFlux = true;
+    return ok(stat);
+}
+
+// The PropOld argument of AdvectionDiffusion (AD:1139, AD:1253-1260), kept by
+// pointer: steps with Orlanski boundaries write into it the field as
+// OpenBoundaryCondition saw it (AD:5428-5429)
+int mohid_ad_set_prop_old(const int* id, double* PropOld, const int* on_device, int* stat)
+{
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    if (PropOld && !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "on_device is NULL");
+    in->propOld = PropOld;
+    in->propOldDev = PropOld && *on_device != 0;
     return ok(stat);
 }
 

@@ -11,6 +11,8 @@
 #define MOHID_DEV_NONFINITE  2u
 #define MOHID_DEV_BAD_FACE   4u
 #define MOHID_DEV_TIMEOUT    8u
+#define MOHID_DEV_OBC_EDGE   16u  // Orlanski: an open boundary point off the work box's edges
+#define MOHID_DEV_OBC_READ   32u  // Orlanski: a read outside the layer plane (grids under 3 cells wide)
 
 namespace mohid {
 
@@ -34,11 +36,19 @@ struct PlainArgs {
     const double *DUX, *DVY, *DZX, *DZY;
     const int *KFloor, *BP2D;
     const double* Ref;          // nullptr: closed boundaries
+    // Orlanski boundaries (bc 6): the field as OpenBoundaryCondition leaves it
+    // (P with the radiated values at the exterior points, orlanski_kernel);
+    // the boundary cells read their exterior value there and columns the
+    // solve leaves untouched are copied from it.  nullptr otherwise.
+    const double* Pobc;
     double DT, schmidtH, schmidtCoefV, schmidtBackV, volumeRelMax, impExpDifV, tdecAux;
     int methodH, limiterH, methodV, limiterV, upwind2H, upwind2V;
     int nullDif, explicitV, docycle, vertical1D, xzflow, bc;
     int impXX, impYY;           // implicit horizontal advection along j (XX) or i (YY)
     int noAdv, noDif;           // NoAdvFlux / NoDifFlux with the masks below
+    // AdvectionNudging (AD:1989-2068): the advective terms of a row gather
+    // apart and enter scaled by the column's edge factor; nudgeCells as given
+    int nudge, nudgeCells;
     const int *NFU, *NFV, *NFW; // NoFluxU/V/W (Size box), or null
     // discharges, or null: terms of column c at dTerms[dStart[c] .. dStart[c+1]),
     // by layer and then in the reference's order (c = i + sj * j)
@@ -61,6 +71,11 @@ enum PlainMode {
 };
 
 // Launchers (plain_f64.cu)
+// Orlanski open boundaries (OpenBoundaryCondition AD:5496-5569 with
+// OrlanskiCelerity2D FN:4129-4490): the radiated value at the exterior point
+// of each open boundary cell, written into S, which must hold a copy of a.P.
+// cols: the boundary columns in the reference's order (j outer, i inner).
+cudaError_t launch_orlanski(const PlainArgs& a, double* S, const int* cols, int ncols, cudaStream_t s);
 cudaError_t launch_plain_f64(const PlainArgs& a, cudaStream_t s, int mode = kPlainFull);
 // THOMAS_3D (FN:3760-3876): one tridiagonal system per work-box line along j
 // (alongJ) or i, from the first work cell to the halo cell past the last, at

@@ -65,6 +65,11 @@ struct Instance {
     // implicit horizontal advection (allocated on first use): the rows of the
     // horizontal system (4 x Size box), the line solver's W, the line solution
     DevBuf<double> sys, Wl, Pmid;
+    // Orlanski boundaries (allocated on first use): the field with the
+    // radiated exterior values; the caller's PropOld (mohid_ad_set_prop_old)
+    DevBuf<double> Pobc;
+    double* propOld = nullptr;
+    bool propOldDev = false;
     // CellFluxes of the last step (6 x Size box: AdvFluxX/Y/Z, DifFluxX/Y/Z),
     // allocated on first use; fluxLast: the last step computed them
     DevBuf<double> flux;

@@ -127,6 +127,104 @@ __device__ __forceinline__ bool null_grad(const double* P, const int* CFU, const
     return true;
 }
 
+// WaterFluxOBoundary of open boundary cell `a` (FluxAtOpenBoundary,
+// AD:5680-5742): transport in through its compute faces less its volume change.
+__device__ __forceinline__ double obc_flux(const PlainArgs& A, size_t a, double Vk)
+{
+    const long long sj = A.sj, sk = A.sk;
+    return __ldg(A.Qx + a) * (double)__ldg(A.CFU + a) - __ldg(A.Qx + a + sj) * (double)__ldg(A.CFU + a + sj) +
+           __ldg(A.Qy + a) * (double)__ldg(A.CFV + a) - __ldg(A.Qy + a + 1) * (double)__ldg(A.CFV + a + 1) +
+           __ldg(A.Qz + a) * (double)__ldg(A.CFW + a) - __ldg(A.Qz + a + sk) * (double)__ldg(A.CFW + a + sk) -
+           (Vk - __ldg(A.Vold + a)) / A.DT;
+}
+
+// The normal of boundary point (i, j) and its exterior point (ie, je)
+// (OpenBoundaryCondition AD:5504-5540): along i on the i = ILB / IUB edges,
+// else along j on the j = JLB / JUB edges.  The exterior point is the point at
+// -(di, dj) when i = ILB or j = JLB, else at +(di, dj): the corner i = IUB,
+// j = JLB therefore takes the interior point (IUB-1, JLB).  false where the
+// reference stops ('Orlanski Advection 2').
+__device__ __forceinline__ bool orl_normal(int ni, int nj, int i, int j, int& di, int& dj, bool& en, int& ie,
+                                           int& je)
+{
+    if (i == 1 || i == ni) { di = 1; dj = 0; }
+    else if (j == 1 || j == nj) { di = 0; dj = 1; }
+    else return false;
+    en = !(i == 1 || j == 1);
+    ie = en ? i + di : i - di;
+    je = en ? j + dj : j - dj;
+    return true;
+}
+
+// OrlanskiCelerity2D (FN:4129-4490) at exterior point (i, j) of the layer
+// starting at `lay`, with the arguments OpenBoundaryCondition passes
+// (AD:5551-5567): implicit, oblique, computed celerity, the default relaxation
+// times (86400 * 300 s), the work box as compute box.  NewField is read from
+// NF, OldField from OF and ComputePoints from CP, each at the column-major
+// plane offset i + sj * j as the Fortran addresses them (the caller has
+// checked that the six unguarded points lie in the plane).  Returns the new
+// value at the exterior point.
+__device__ double orlanski_value(const double* NF, const double* OF, const double* Ref, const int* CP,
+                                 long long sj, long long lay, int ni, int nj, int di, int dj, int i, int j,
+                                 bool en, double LimitMax, double DT, double FlowVelX)
+{
+    auto at = [&](int x, int y) { return (size_t)(lay + x + sj * y); };
+    const int s = en ? -1 : 1;                   // from the exterior point into the domain
+    const int bi = i + s * di, bj = j + s * dj;  // the first interior point
+    const double I1N = NF[at(bi, bj)], I1O = OF[at(bi, bj)];
+    const double I2N = NF[at(i + 2 * s * di, j + 2 * s * dj)];
+    const double I3N = NF[at(i + 3 * s * di, j + 3 * s * dj)];
+    const double I6O = OF[at(bi + dj, bj + di)], I7O = OF[at(bi - dj, bj - di)];
+    bool noNE = false, noSW = false;
+    if (bi + 3 * dj > ni || bj + 3 * di > nj) noNE = true;
+    else if (CP[at(bi + dj, bj + di)] * CP[at(bi + 2 * dj, bj + 2 * di)] * CP[at(bi + 3 * dj, bj + 3 * di)] == 0)
+        noNE = true;
+    if (bi - 3 * dj < 1 || bj - 3 * di < 1) noSW = true;
+    else if (CP[at(bi - dj, bj - di)] * CP[at(bi - 2 * dj, bj - 2 * di)] * CP[at(bi - 3 * dj, bj - 3 * di)] == 0)
+        noSW = true;
+    const double B5 = OF[at(i, j)];
+    // the scheme of Marchesiello et al. (2000), FN:4316-4354
+    const double tv = I1N - I1O;
+    const double svx = I1N - I2N;
+    double svy;
+    if ((I6O - I7O) * tv > 0) svy = noSW ? 0. : I1O - I7O;
+    else svy = noNE ? 0. : I6O - I1O;
+    const double ss = svx * svx + svy * svy;
+    double cx = 0., cy = 0.;
+    if (ss > 0.) {
+        cx = -((tv * svx) / ss);
+        cy = -((tv * svy) / ss);
+        if (fabs(cx) > LimitMax) cx = LimitMax * cx / fabs(cx);
+        if (fabs(cy) > LimitMax) cy = LimitMax * cy / fabs(cy);
+    }
+    const double refv = Ref[at(i, j)];
+    const double trelax = 86400.0 * 300.0;
+    cx = cx + FlowVelX;
+    double adjx;
+    if (cx > 0) {
+        cx = 4 * cx;
+        adjx = 0.0546875 * I3N - 0.2578125 * I2N + 0.6015625 * I1N;
+    } else {
+        adjx = refv; cx = 0.; cy = 0.;
+    }
+    double auxInt = cx * adjx;
+    if (cy >= 0 && !noSW) {
+        const double B4 = OF[at(i - dj, j - di)], B42 = OF[at(i - 2 * dj, j - 2 * di)];
+        const double B43 = OF[at(i - 3 * dj, j - 3 * di)];
+        const double adjy = 0.0546875 * B43 - 0.2578125 * B42 + 0.6015625 * B4 + 0.6015625 * B5;
+        auxInt = auxInt - 4 * cy * (B5 - adjy);
+    } else if (cy < 0 && !noNE) {
+        const double B3 = OF[at(i + dj, j + di)], B32 = OF[at(i + 2 * dj, j + 2 * di)];
+        const double B33 = OF[at(i + 3 * dj, j + 3 * di)];
+        const double adjy = 0.0546875 * B33 - 0.2578125 * B32 + 0.6015625 * B3 + 0.6015625 * B5;
+        auxInt = auxInt - 4 * cy * (adjy - B5);
+    }
+    // OldField(i, j) = NewField(i, j): the exterior point's value as the call found it
+    const double old = NF[at(i, j)];
+    const double auxBound = 1. + cx * (1 - 0.6015625) + DT / trelax;
+    return (old + auxInt + refv * DT / trelax) / auxBound;
+}
+
 // Explicit advective flux through the face between cells `m` (= a - s) and `a`
 // along stride `s`; `f` is the face index along that axis (1..N), du indexed
 // by du(f + n - 2).  Coefficients are computed only where both cells are
@@ -187,7 +285,8 @@ plain_f64_kernel(const PlainArgs A)
     if (kRows && !interior) return;               // every work-box cell has a row
     const bool solve = interior && (kRows || __ldg(A.WP + c + (size_t)sk * nk) == 1);
     if (!solve) {                                 // THOMASZ leaves the column untouched
-        for (int k = 0; k <= nk + 1; ++k) Po[c + (size_t)sk * k] = __ldg(P + c + (size_t)sk * k);
+        const double* Pc = A.Pobc ? A.Pobc : P;   // (with the radiated exterior values)
+        for (int k = 0; k <= nk + 1; ++k) Po[c + (size_t)sk * k] = __ldg(Pc + c + (size_t)sk * k);
         return;
     }
     if (!kRows) Po[c] = __ldg(P + c);             // row 0 is never solved
@@ -203,6 +302,18 @@ plain_f64_kernel(const PlainArgs A)
     const double ie = A.impExpDifV;
     const bool doVert = nk > 1;
     const bool doVAdv = doVert && !A.vertical1D;
+    // AdvectionNudging's factor n of this column: min(in, jn) / nCells, in (jn)
+    // = i (j) within nCells of the low edge, IUB - i + 1 (JUB - j + 1) within
+    // nCells of the high edge, else nCells, which is what the reference's
+    // loop leaves in the distance it does not set when it runs in order
+    const bool nud = A.nudge != 0;
+    double nudN = 1.0;
+    if (nud && A.nudgeCells >= 1) {
+        const int nc = A.nudgeCells;
+        const int di = i < nc + 1 ? i : (i > ni - nc ? ni - i + 1 : nc);
+        const int dj = j < nc + 1 ? j : (j > nj - nc ? nj - j + 1 : nc);
+        nudN = (double)(di < dj ? di : dj) / (double)nc;
+    }
 
     // vertical face helpers -------------------------------------------------
     auto Kz = [&](size_t a) {                    // Convert_Dif_Vertical AD:2397-2424
@@ -236,6 +347,7 @@ plain_f64_kernel(const PlainArgs A)
         const int opk = __ldg(A.OP + a);
         const double Pkp1 = __ldg(P + a + sk);
         double D = 0., E = 1., F = 0., TI;
+        double aTi = 0., aD = 0., aE = 0., aF = 0.;   // AdvectionTi/D/E/F (nudging)
 
         if (MODE == kPlainVertical) {
             TI = Pk;                              // the step restarts from the line solution
@@ -329,7 +441,8 @@ plain_f64_kernel(const PlainArgs A)
             if (__ldg(A.CFU + a) == 1) {
                 if (!A.impXX) {
                     double Fx = adv_flux(A, a, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duW);
-                    TI = TI + Fx * DT / Vk;
+                    if (nud) aTi = aTi + Fx * DT / Vk;
+                    else TI = TI + Fx * DT / Vk;
                     if (A.fAX) A.fAX[a] = 0.0 + 1.0 * Fx;                       // AD:4531-4537
                 } else {
                     double C[4];
@@ -342,7 +455,8 @@ plain_f64_kernel(const PlainArgs A)
             if (j + 1 <= nj && __ldg(A.CFU + a + sj) == 1) {
                 if (!A.impXX) {
                     double Fx = adv_flux(A, a + sj, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duE);
-                    TI = TI - Fx * DT / Vk;
+                    if (nud) aTi = aTi - Fx * DT / Vk;
+                    else TI = TI - Fx * DT / Vk;
                 } else {
                     double C[4];
                     adv_coef(A, a + sj, sj, A.Qx, nfU, A.methodH, A.limiterH, up2H, duE, C);
@@ -358,7 +472,8 @@ plain_f64_kernel(const PlainArgs A)
                 if (__ldg(A.CFV + a) == 1) {
                     if (!A.impYY) {
                         double Fy = adv_flux(A, a, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvS);
-                        TI = TI + Fy * DT / Vk;
+                        if (nud) aTi = aTi + Fy * DT / Vk;
+                        else TI = TI + Fy * DT / Vk;
                         if (A.fAY) A.fAY[a] = 0.0 + 1.0 * Fy;                   // AD:4900-4906
                     } else {
                         double C[4];
@@ -371,7 +486,8 @@ plain_f64_kernel(const PlainArgs A)
                 if (i + 1 <= ni && __ldg(A.CFV + a + 1) == 1) {
                     if (!A.impYY) {
                         double Fy = adv_flux(A, a + 1, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvN);
-                        TI = TI - Fy * DT / Vk;
+                        if (nud) aTi = aTi - Fy * DT / Vk;
+                        else TI = TI - Fy * DT / Vk;
                     } else {
                         double C[4];
                         adv_coef(A, a + 1, 1, A.Qy, nfV, A.methodH, A.limiterH, up2H, dvN, C);
@@ -422,7 +538,8 @@ plain_f64_kernel(const PlainArgs A)
                         vcoef(k, C);
                         double Fz = C[0] * __ldg(P + a - 2 * sk) + C[1] * __ldg(P + a - sk) +
                                     C[2] * Pk + C[3] * Pkp1;
-                        TI = TI + Fz * DT / Vk;
+                        if (nud) aTi = aTi + Fz * DT / Vk;
+                        else TI = TI + Fz * DT / Vk;
                         if (A.fAZ) A.fAZ[a] = 0.0 + 1.0 * Fz;                   // AD:3128-3135
                     }
                     if (k + 1 <= nk && __ldg(A.CFW + a + sk) == 1) {
@@ -430,7 +547,23 @@ plain_f64_kernel(const PlainArgs A)
                         vcoef(k + 1, C);
                         double Fz = C[0] * __ldg(P + a - sk) + C[1] * Pk + C[2] * Pkp1 +
                                     C[3] * __ldg(P + a + 2 * sk);
-                        TI = TI - Fz * DT / Vk;
+                        if (nud) aTi = aTi - Fz * DT / Vk;
+                        else TI = TI - Fz * DT / Vk;
+                    }
+                } else if (nud) {                 // VerticalAdvection_Nudge AD:3302-3331: by layers
+                    if (__ldg(A.CFW + a) == 1) {
+                        double C[4];
+                        vcoef(k, C);
+                        double DT2 = DT / Vk;
+                        aD = aD - C[1] * DT2;
+                        aE = aE - C[2] * DT2;
+                    }
+                    if (k + 1 <= nk && __ldg(A.CFW + a + sk) == 1) {
+                        double C[4];
+                        vcoef(k + 1, C);
+                        double DT1 = DT / Vk;
+                        aE = aE + C[1] * DT1;
+                        aF = aF + C[2] * DT1;
                     }
                 } else {
                     bool gk, gk1;
@@ -459,20 +592,30 @@ plain_f64_kernel(const PlainArgs A)
             }
         }
 
+        // AdvectionNudging (AD:2051-2060): the advective terms, scaled, at open cells
+        if (nud && opk == 1) {
+            TI = TI + nudN * aTi;
+            D = D + nudN * aD;
+            E = E + nudN * aE;
+            F = F + nudN * aF;
+        }
+
         // OpenBoundaryCondition (boundary columns, open cells, k >= |KFloor|)
         if (bp && k >= kbp && opk == 1) {
             double DT_V = DT / Vk;
             const double Rf = __ldg(A.Ref + a);
-            if (A.bc == 1 || A.bc == 7) {         // MassConservation, MassConservNullGrad
-                double WF = __ldg(A.Qx + a) * (double)__ldg(A.CFU + a) -
-                            __ldg(A.Qx + a + sj) * (double)__ldg(A.CFU + a + sj) +
-                            __ldg(A.Qy + a) * (double)__ldg(A.CFV + a) -
-                            __ldg(A.Qy + a + 1) * (double)__ldg(A.CFV + a + 1) +
-                            __ldg(A.Qz + a) * (double)__ldg(A.CFW + a) -
-                            __ldg(A.Qz + a + sk) * (double)__ldg(A.CFW + a + sk) -
-                            (Vk - __ldg(A.Vold + a)) / DT;
-                if (A.bc == 1) {
-                    double Ext = Pk * (1.0 - A.tdecAux) + Rf * A.tdecAux;
+            if (A.bc == 1 || A.bc == 6 || A.bc == 7) {   // MassConservation, Orlanski, MassConservNullGrad
+                const double WF = obc_flux(A, a, Vk);
+                if (A.bc != 7) {
+                    double Ext;
+                    if (A.bc == 1) {
+                        Ext = Pk * (1.0 - A.tdecAux) + Rf * A.tdecAux;
+                    } else {                      // the radiated value at the exterior point
+                        int di, dj, ie, je;
+                        bool en;
+                        Ext = orl_normal(ni, nj, i, j, di, dj, en, ie, je)
+                                  ? __ldg(A.Pobc + (size_t)ie + (size_t)sj * je + (size_t)sk * k) : 0.;
+                    }
                     if (WF < 0.0) TI = TI - WF * Ext * DT_V;
                     else E = E + WF * DT_V;
                 } else if (WF < 0.0) {            // inflow: interior mean of the old field
@@ -789,7 +932,77 @@ __global__ void cyclic_copy_kernel(int ni, int nj, int nk, long long sj, long lo
     }
 }
 
+// Orlanski radiation (OpenBoundaryCondition AD:5496-5569) at every open cell
+// of the boundary columns: the new value at the cell's exterior point, into S
+// (a copy of A.P).  The reference calls OrlanskiCelerity2D point by point (j
+// outer, i inner, then k), each call reading NewField at three interior points
+// and writing it at the exterior point.  Layers never mix.  On grids at least
+// 4 cells wide in i and j every such read precedes (in the reference's order)
+// any write to the same point, so each (column, layer) is one thread reading
+// A.P (seq false); on narrower grids thread k walks layer k in order, reading
+// and writing S (seq true).  OldField is the reference's PROPOld, a copy of
+// PROP whose values the calls never change: A.P.  Points off the work box's
+// edges, and reads outside the layer plane, set a status bit instead.
+__global__ void orlanski_kernel(const PlainArgs A, double* S, const int* __restrict__ cols, int ncols, bool seq)
+{
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int ni = A.ni, nj = A.nj, nk = A.nk;
+    int q0, q1, k;
+    if (seq) {
+        k = 1 + (int)e;
+        if (k > nk) return;
+        q0 = 0; q1 = ncols;
+    } else {
+        if (e >= (long long)ncols * nk) return;
+        q0 = (int)(e / nk); q1 = q0 + 1;
+        k = 1 + (int)(e % nk);
+    }
+    const long long sj = A.sj, sk = A.sk, plane = sj * (nj + 2), lay = sk * k;
+    const double* NF = seq ? S : A.P;
+    unsigned flags = 0;
+    for (int q = q0; q < q1; ++q) {
+        const size_t c = (size_t)cols[q];
+        const int i = (int)(c % (size_t)sj), j = (int)(c / (size_t)sj);
+        const int kf = __ldg(A.KFloor + c);
+        if (k < (kf < 0 ? -kf : kf)) continue;
+        const size_t a = c + (size_t)lay;
+        if (__ldg(A.OP + a) != 1) continue;
+        int di, dj, ie, je;
+        bool en;
+        if (!orl_normal(ni, nj, i, j, di, dj, en, ie, je)) { flags |= MOHID_DEV_OBC_EDGE; continue; }
+        // the exterior point, the three interior points along the normal and
+        // the two beside the first are read without a bounds test
+        const int sgn = en ? -1 : 1;
+        bool inside = true;
+        const int px[6] = {ie, ie + sgn * di, ie + 2 * sgn * di, ie + 3 * sgn * di, ie + sgn * di + dj,
+                           ie + sgn * di - dj};
+        const int py[6] = {je, je + sgn * dj, je + 2 * sgn * dj, je + 3 * sgn * dj, je + sgn * dj + di,
+                           je + sgn * dj - di};
+        for (int n = 0; n < 6; ++n) {
+            const long long o = px[n] + sj * py[n];
+            inside = inside && o >= 0 && o < plane;
+        }
+        if (!inside) { flags |= MOHID_DEV_OBC_READ; continue; }
+        const double Vk = __ldg(A.V + a);
+        const double DT_V = A.DT / Vk;
+        const double VelBound = obc_flux(A, a, Vk) * DT_V;
+        const double LimitMax = 10. * A.DT / (__ldg(A.DUX + c) + __ldg(A.DVY + c)) * 2;
+        S[(size_t)(lay + ie + sj * je)] = orlanski_value(NF, A.P, A.Ref, A.OP, sj, lay, ni, nj, di, dj, ie, je,
+                                                         en, LimitMax, A.DT, VelBound);
+    }
+    if (flags) atomicOr(A.status, flags);
+}
+
 }  // namespace
+
+cudaError_t launch_orlanski(const PlainArgs& a, double* S, const int* cols, int ncols, cudaStream_t s)
+{
+    if (ncols <= 0 || a.nk <= 0) return cudaSuccess;
+    const bool seq = a.ni < 4 || a.nj < 4;
+    const long long n = seq ? a.nk : (long long)ncols * a.nk;
+    orlanski_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a, S, cols, ncols, seq);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_null_gradient(int ni, int nj, int nk, double* P, const int* CFU, const int* CFV,
                                  const int* KFloor, const int* cols, int ncols, cudaStream_t s)

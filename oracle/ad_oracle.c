@@ -178,6 +178,148 @@ static int advection_line(int flo, int fhi, double dt, const double* du, size_t 
 
 static int disch_valid(const ora_domain* d);
 
+/* Orlanski boundaries (OpenBoundaryCondition AD:5496-5569): the normal of a
+ * boundary point and the exterior point OrlanskiCelerity2D works on.  di = 1
+ * on the i = ILB / IUB edges, else dj = 1 on the j = JLB / JUB edges, else the
+ * reference stops ('Orlanski Advection 2'); the exterior point lies at -(di,
+ * dj) when i = ILB or j = JLB, else at +(di, dj).  Returns 0, or 1 where the
+ * reference stops. */
+static int orlanski_normal(int ni, int nj, int i, int j, int* di, int* dj, int* en, int* iext, int* jext)
+{
+    if (i == 1 || i == ni) { *di = 1; *dj = 0; }
+    else if (j == 1 || j == nj) { *di = 0; *dj = 1; }
+    else return 1;
+    if (i == 1 || j == 1) { *en = 0; *iext = i - *di; *jext = j - *dj; }
+    else { *en = 1; *iext = i + *di; *jext = j + *dj; }
+    return 0;
+}
+
+/* Every boundary point with an open cell must have a normal (else the
+ * reference stops: MOHID_AD_ERR_OPTION).  The corner i = IUB, j = JLB takes
+ * the interior point (IUB-1, JLB) as its exterior point and reads two cells
+ * along i past it, (IUB+2, JLB): in the Size-box array, column-major, that
+ * element is (ILB-1, JLB+1), which the reference reads (it does not check
+ * bounds) and this restatement, indexing the same contiguous array, reads
+ * too.  Reads whose element lies outside the whole layer plane are rejected
+ * (MOHID_AD_ERR_BOUNDS): they only occur on grids under three cells wide. */
+static int orlanski_geometry_ok(const ora_domain* d)
+{
+    const int ni = d->ni, nj = d->nj, nk = d->nk;
+    ora_ext X = {ni + 2, nj + 2, nk + 2, 0, 0};
+    const long long n2 = (long long)X.NI * X.NJ;
+    for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+            if (d->BoundaryPoints2D[I2(i, j)] != 1) continue;
+            int open = 0;
+            for (int k = abs(d->KFloorZ[I2(i, j)]); k <= nk; ++k) open |= d->OpenPoints3D[I3(i, j, k)] == 1;
+            if (!open) continue;
+            int di = 0, dj = 0, en = 0, ie = 0, je = 0;
+            if (orlanski_normal(ni, nj, i, j, &di, &dj, &en, &ie, &je)) return MOHID_AD_ERR_OPTION;
+            const int s = en ? -1 : 1;               /* towards the interior */
+            const int pts[6][2] = {{ie, je}, {ie + s * di, je + s * dj}, {ie + 2 * s * di, je + 2 * s * dj},
+                                   {ie + 3 * s * di, je + 3 * s * dj},
+                                   {ie + s * di + dj, je + s * dj + di}, {ie + s * di - dj, je + s * dj - di}};
+            for (int q = 0; q < 6; ++q) {
+                const long long lin = (long long)pts[q][0] + (long long)X.NI * pts[q][1];
+                if (lin < 0 || lin >= n2) return MOHID_AD_ERR_BOUNDS;
+            }
+        }
+    return 0;
+}
+
+/* OrlanskiCelerity2D (ModuleFunctions.F90:4129-4490) with the arguments
+ * OpenBoundaryCondition passes (AD:5551-5567): NewField = PROP, OldField =
+ * PROPOld, ComputePoints = OpenPoints3D, ReferenceField = ReferenceProp,
+ * Imin..Jmax = the work box, FlowVelX = the boundary flux times DT/V, no
+ * relaxation times (86400 * 300 s), the implicit, non-constant-celerity,
+ * oblique form.  Writes OldField and NewField at the exterior point (i, j, k)
+ * and returns the new value there. */
+static double orlanski_celerity_2d(ora_ext X, double* NewF, double* OldF, const double* Ref, const int* CP,
+                                   int Imin, int Imax, int Jmin, int Jmax, int di, int dj, int i, int j, int k,
+                                   int en, double LimitMax, double DT, double FlowVelX)
+{
+#define NF(a, b) NewF[I3((a), (b), k)]
+#define OF(a, b) OldF[I3((a), (b), k)]
+#define CPT(a, b) CP[I3((a), (b), k)]
+    int noSW = 0, noNE = 0;
+    double I1N, I1O, I2N, I2O, I3N, I3O, I6O, I7O;
+    double B3 = 0, B32 = 0, B33 = 0, B4 = 0, B42 = 0, B43 = 0, B5;
+    if (en) {
+        I1N = NF(i - di, j - dj); I1O = OF(i - di, j - dj);
+        I2N = NF(i - 2 * di, j - 2 * dj); I3N = NF(i - 3 * di, j - 3 * dj);
+        I2O = OF(i - 2 * di, j - 2 * dj); I3O = OF(i - 3 * di, j - 3 * dj);
+        I6O = OF(i - di + dj, j - dj + di); I7O = OF(i - di - dj, j - dj - di);
+        if ((i - di + 3 * dj) > Imax || (j - dj + 3 * di) > Jmax) noNE = 1;
+        else if (CPT(i - di + dj, j - dj + di) * CPT(i - di + 2 * dj, j - dj + 2 * di) *
+                 CPT(i - di + 3 * dj, j - dj + 3 * di) == 0) noNE = 1;
+        if ((i - di - 3 * dj) < Imin || (j - dj - 3 * di) < Jmin) noSW = 1;
+        else if (CPT(i - di - dj, j - dj - di) * CPT(i - di - 2 * dj, j - dj - 2 * di) *
+                 CPT(i - di - 3 * dj, j - dj - 3 * di) == 0) noSW = 1;
+    } else {
+        I1N = NF(i + di, j + dj); I1O = OF(i + di, j + dj);
+        I2N = NF(i + 2 * di, j + 2 * dj); I3N = NF(i + 3 * di, j + 3 * dj);
+        I2O = OF(i + 2 * di, j + 2 * dj); I3O = OF(i + 3 * di, j + 3 * dj);
+        I6O = OF(i + di + dj, j + dj + di); I7O = OF(i + di - dj, j + dj - di);
+        if ((i + di + 3 * dj) > Imax || (j + dj + 3 * di) > Jmax) noNE = 1;
+        else if (CPT(i + di + dj, j + dj + di) * CPT(i + di + 2 * dj, j + dj + 2 * di) *
+                 CPT(i + di + 3 * dj, j + dj + 3 * di) == 0) noNE = 1;
+        if ((i + di - 3 * dj) < Imin || (j + dj - 3 * di) < Jmin) noSW = 1;
+        else if (CPT(i + di - dj, j + dj - di) * CPT(i + di - 2 * dj, j + dj - 2 * di) *
+                 CPT(i + di - 3 * dj, j + dj - 3 * di) == 0) noSW = 1;
+    }
+    (void)I2O; (void)I3O;                    /* read by the explicit form only */
+    if (!noNE) { B3 = OF(i + dj, j + di); B32 = OF(i + 2 * dj, j + 2 * di); B33 = OF(i + 3 * dj, j + 3 * di); }
+    if (!noSW) { B4 = OF(i - dj, j - di); B42 = OF(i - 2 * dj, j - 2 * di); B43 = OF(i - 3 * dj, j - 3 * di); }
+    B5 = OF(i, j);
+    /* the scheme of Marchesiello et al. (2000), FN:4316-4354 */
+    const double tv = I1N - I1O;
+    const double svx = I1N - I2N;
+    const double auxIntY = I6O - I7O;
+    double svy;
+    if (auxIntY * tv > 0) { svy = I1O - I7O; if (noSW) svy = 0.; }
+    else { svy = I6O - I1O; if (noNE) svy = 0.; }
+    const double ss = svx * svx + svy * svy;
+    double wcx, wcy;
+    if (ss > 0.) {
+        wcx = -((tv * svx) / ss);
+        wcy = -((tv * svy) / ss);
+        if (fabs(wcx) > LimitMax) wcx = LimitMax * wcx / fabs(wcx);
+        if (fabs(wcy) > LimitMax) wcy = LimitMax * wcy / fabs(wcy);
+    } else {
+        wcx = 0.; wcy = 0.;
+    }
+    const double refv = Ref[I3(i, j, k)];
+    const double trelax_out = 86400 * 300, trelax_in = 86400 * 300;
+    wcx = wcx + FlowVelX;
+    double adjx, trelax;
+    if (wcx > 0) {
+        wcx = 4 * wcx;
+        adjx = 0.0546875 * I3N - 0.2578125 * I2N + 0.6015625 * I1N;
+        trelax = trelax_out;
+    } else {
+        adjx = refv;
+        wcx = 0.;
+        wcy = 0.;
+        trelax = trelax_in;
+    }
+    double auxInt = wcx * adjx;
+    if (wcy >= 0 && !noSW) {
+        const double adjy = 0.0546875 * B43 - 0.2578125 * B42 + 0.6015625 * B4 + 0.6015625 * B5;
+        auxInt = auxInt - 4 * wcy * (B5 - adjy);
+    } else if (wcy < 0 && !noNE) {
+        const double adjy = 0.0546875 * B33 - 0.2578125 * B32 + 0.6015625 * B3 + 0.6015625 * B5;
+        auxInt = auxInt - 4 * wcy * (adjy - B5);
+    }
+    OF(i, j) = NF(i, j);
+    double auxBound = 1;
+    auxBound = auxBound + wcx * (1 - 0.6015625) + DT / trelax;
+    NF(i, j) = (OF(i, j) + auxInt + refv * DT / trelax) / auxBound;
+    return NF(i, j);
+#undef NF
+#undef OF
+#undef CPT
+}
+
 static int validate(const ora_domain* d, const double* PROP, const mohid_ad_params* p,
                     const double* ReferenceProp)
 {
@@ -196,7 +338,13 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
     /* HorizontalAdvectionXX / YY ERR01: explicit (0) or implicit (1) only */
     if ((p->ImpExp_AdvXX != 0. && p->ImpExp_AdvXX != 1.) || (p->ImpExp_AdvYY != 0. && p->ImpExp_AdvYY != 1.))
         return MOHID_AD_ERR_OPTION;
-    if (p->AdvectionNudging) return MOHID_AD_ERR_UNSUPPORTED;
+    /* AdvectionNudging: HorizontalAdvectionXX/YY_Nudge add their implicit
+     * coefficients (cells j-1, j or i-1, i) into the vertical system's D, E, F
+     * (AD:4692-4696, 5076-5080), and with Vertical1D AdvectionNudging reads
+     * AdvectionTi/D/E/F that nothing set in the call (AD:1704, 4151-4157);
+     * neither is restated */
+    if (p->AdvectionNudging && (p->ImpExp_AdvXX != 0. || p->ImpExp_AdvYY != 0. || p->Vertical1D))
+        return MOHID_AD_ERR_UNSUPPORTED;
     if (!disch_valid(d)) return MOHID_AD_ERR_BOUNDS;
     /* the reference reads NoFluxU/V/W whenever NoAdvFlux or NoDifFlux is set */
     if ((p->NoAdvFlux || p->NoDifFlux) && (!d->NoFluxU || !d->NoFluxV || !d->NoFluxW)) return MOHID_AD_ERR_NULLPTR;
@@ -213,7 +361,10 @@ static int validate(const ora_domain* d, const double* PROP, const mohid_ad_para
         if (ReferenceProp) {
             if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8)
                 return MOHID_AD_ERR_OPTION;          /* Set_Internal_State ERR01, AD:5816-5830 */
-            if (bc == MOHID_BC_ORLANSKI) return MOHID_AD_ERR_UNSUPPORTED;
+            if (bc == MOHID_BC_ORLANSKI) {
+                int e = orlanski_geometry_ok(d);
+                if (e) return e;
+            }
         } else if (bc == MOHID_BC_CYCLIC) {
             return MOHID_AD_ERR_OPTION;              /* Prop_CyclicBoundary reads ReferenceProp, AD:2150 */
         }
@@ -242,6 +393,9 @@ struct ora_work {
     /* CellFluxes (allocated on first use): AdvFluxX/Y/Z, DifFluxX/Y/Z */
     double* fpool;
     double *FAX, *FAY, *FAZ, *FDX, *FDY, *FDZ;
+    /* AdvectionNudging (allocated on first use): AdvectionTi/D/E/F */
+    double* npool;
+    double *ATi, *AD, *AE, *AF;
 };
 
 /* AllocateVariables, AD:537-684: work arrays live for the instance's life and
@@ -265,7 +419,19 @@ ora_work* ora_work_new(int ni, int nj, int nk)
 
 void ora_work_free(ora_work* w)
 {
-    if (w) { free(w->pool); free(w->fpool); free(w); }
+    if (w) { free(w->pool); free(w->fpool); free(w->npool); free(w); }
+}
+
+/* AllocateVariables AD:608-612 (AdvectionTi/D/E/F) */
+static int ora_work_nudge(ora_work* w)
+{
+    if (w->npool) return 1;
+    size_t n3 = (size_t)(w->ni + 2) * (size_t)(w->nj + 2) * (size_t)(w->nk + 2);
+    w->npool = (double*)malloc(sizeof(double) * n3 * 4);
+    if (!w->npool) return 0;
+    double** slots[4] = {&w->ATi, &w->AD, &w->AE, &w->AF};
+    for (int s = 0; s < 4; ++s) *slots[s] = w->npool + (size_t)s * n3;
+    return 1;
 }
 
 /* AllocateVariables AD:567-573 (the cell-flux arrays) */
@@ -547,7 +713,12 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
     if (work->ni != ni || work->nj != nj || work->nk != nk) return MOHID_AD_ERR_BOUNDS;
     const int cflux = p->CellFluxes != 0;
     if (cflux && !ora_work_fluxes(work)) { ora_work_free(own); return MOHID_AD_ERR_ALLOC; }
+    /* AdvectionNudging: the advective terms go to AdvectionTi/D/E/F first */
+    const int nudge = p->AdvectionNudging != 0;
+    if (nudge && !ora_work_nudge(work)) { ora_work_free(own); return MOHID_AD_ERR_ALLOC; }
     ora_work w = *work;
+    /* the Nudge routines ignore the NoAdvFlux masks (AD:4586-4733, 4957-5118, 3211-3350) */
+    const int noAdv = p->NoAdvFlux && !nudge;
     int err = 0, zeroH = 0;
 
     /* Convert_Dif_Vertical, AD:2364-2443: do k = KLB+1,KUB / OMP DO j / do i */
@@ -699,6 +870,11 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
         }
 
+        /* HorizontalAdvection AD:4151-4165: with AdvectionNudging the
+         * explicit updates go to AdvectionTi, zeroed first (the _Nudge
+         * variants of XX and YY, AD:4586-4733 and AD:4957-5118) */
+        double* TIa = nudge ? w.ATi : w.TI;
+        if (nudge) { fill3(X, w.ATi, 0.); fill3(X, w.AD, 0.); fill3(X, w.AE, 0.); fill3(X, w.AF, 0.); }
         /* HorizontalAdvectionXX, AD:4368-4540: coefficients per line (i,:,k)
          * (do k / OMP DO i), faces j = JLB..JUB after the dummy-index shift;
          * explicit update OMP DO k / do j / do i. */
@@ -712,7 +888,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                       p->Upwind2H);
         }
         if (err) goto fail;
-        if (p->NoAdvFlux) noflux_zero(d, d->NoFluxU, 0, w.XC, w.XD, w.XE, w.XF);
+        if (noAdv) noflux_zero(d, d->NoFluxU, 0, w.XC, w.XD, w.XE, w.XF);
         if (p->ImpExp_AdvXX == 0.) {
         #pragma omp parallel for schedule(dynamic, 1)
         for (int k = 1; k <= nk; ++k)
@@ -723,8 +899,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         size_t am = I3(i, j - 1, k);
                         double Fx = w.XC[a] * P[I3(i, j - 2, k)] + w.XD[a] * P[am] +
                                     w.XE[a] * P[a] + w.XF[a] * P[I3(i, j + 1, k)];
-                        w.TI[a] = w.TI[a] + Fx * DT / V[a];
-                        w.TI[am] = w.TI[am] - Fx * DT / V[am];
+                        TIa[a] = TIa[a] + Fx * DT / V[a];
+                        TIa[am] = TIa[am] - Fx * DT / V[am];
                     }
                 }
         if (cflux)                               /* AD:4531-4537 */
@@ -758,7 +934,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                           p->Upwind2H);
             }
             if (err) goto fail;
-            if (p->NoAdvFlux) noflux_zero(d, d->NoFluxV, 0, w.YC, w.YD, w.YE, w.YF);
+            if (noAdv) noflux_zero(d, d->NoFluxV, 0, w.YC, w.YD, w.YE, w.YF);
             if (p->ImpExp_AdvYY == 0.) {
             #pragma omp parallel
             for (int k = 1; k <= nk; ++k) {
@@ -770,8 +946,8 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                             size_t am = I3(i - 1, j, k);
                             double Fy = w.YC[a] * P[I3(i - 2, j, k)] + w.YD[a] * P[am] +
                                         w.YE[a] * P[a] + w.YF[a] * P[I3(i + 1, j, k)];
-                            w.TI[a] = w.TI[a] + Fy * DT / V[a];
-                            w.TI[am] = w.TI[am] - Fy * DT / V[am];
+                            TIa[a] = TIa[a] + Fy * DT / V[a];
+                            TIa[am] = TIa[am] - Fy * DT / V[am];
                         }
                     }
             }
@@ -845,7 +1021,10 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                                               w.VC, w.VD, w.VE, w.VF, p->AdvMethodV,
                                               p->TVDLimitationV, p->VolumeRelMax, p->Upwind2V);
             if (err) goto fail;
-            if (p->NoAdvFlux) noflux_zero(d, d->NoFluxW, 1, w.VC, w.VD, w.VE, w.VF);
+            if (noAdv) noflux_zero(d, d->NoFluxW, 1, w.VC, w.VD, w.VE, w.VF);
+            /* VerticalAdvection_Nudge (AD:3211-3350): explicit to AdvectionTi,
+             * implicit to AdvectionD/E/F by layers whatever Docycle_method */
+            double* TIv = nudge ? w.ATi : w.TI;
 
             if (p->ImpExp_AdvV == 0.) {
                 /* explicit, AD:3036-3063: do k / OMP DO j / do i */
@@ -858,11 +1037,26 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                             if (CFW[a] == 1) {
                                 double Fz = w.VC[a] * P[I3(i, j, k - 2)] + w.VD[a] * P[am] +
                                             w.VE[a] * P[a] + w.VF[a] * P[I3(i, j, k + 1)];
-                                w.TI[am] = w.TI[am] - Fz * DT / V[am];
-                                w.TI[a] = w.TI[a] + Fz * DT / V[a];
+                                TIv[am] = TIv[am] - Fz * DT / V[am];
+                                TIv[a] = TIv[a] + Fz * DT / V[a];
                             }
                         }
                 }
+            } else if (nudge) {
+                /* implicit, AD:3302-3331: do k / OMP DO j / do i */
+                for (int k = 1; k <= nk; ++k)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            size_t a = I3(i, j, k), am = I3(i, j, k - 1);
+                            if (CFW[a] == 1) {
+                                double DT1 = DT / V[am];
+                                double DT2 = DT / V[a];
+                                w.AD[a] = w.AD[a] - w.VD[a] * DT2;
+                                w.AE[a] = w.AE[a] - w.VE[a] * DT2;
+                                w.AE[am] = w.AE[am] + w.VD[a] * DT1;
+                                w.AF[am] = w.AF[am] + w.VE[a] * DT1;
+                            }
+                        }
             } else if (p->Docycle_method == 1) {
                 /* implicit, column cycle, AD:3070-3093: OMP DO j / do i / do k */
                 #pragma omp parallel for schedule(dynamic, 1)
@@ -906,12 +1100,45 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
         }
     }
 
+    if (nudge) {
+        /* AdvectionNudging, AD:1989-2068: the advective terms enter scaled
+         * by n = min(in, jn) / nCells near the edges, in / jn the distance in
+         * cells to the nearer i / j edge.  A cell near only one pair of edges
+         * reads the other distance from the last cell that set it: the
+         * reference keeps in / jn as OpenMP-private variables across the loop,
+         * so its result there depends on which cells a thread ran before.
+         * This restatement runs the loop in order on one thread, where that
+         * value is always nCells. */
+        const int nc = p->AdvectionNudgingCells;
+        int in_ = 0, jn_ = 0;                    /* max(0, i - ILB + 1) etc., ILB = JLB = 1 */
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                int cell = 0;
+                if (i < nc + 1) { cell = 1; in_ = i > 0 ? i : 0; }
+                else if (i > ni - nc) { cell = 1; in_ = ni - i + 1 > 0 ? ni - i + 1 : 0; }
+                if (j < nc + 1) { cell = 1; jn_ = j > 0 ? j : 0; }
+                else if (j > nj - nc) { cell = 1; jn_ = nj - j + 1 > 0 ? nj - j + 1 : 0; }
+                double n;
+                if (cell) { n = (double)(in_ < jn_ ? in_ : jn_); n = n / nc; }
+                else n = 1.0;
+                for (int k = 1; k <= nk; ++k) {
+                    size_t a = I3(i, j, k);
+                    if (OP[a] == 1) {
+                        w.TI[a] = w.TI[a] + n * w.ATi[a];
+                        w.D[a] = w.D[a] + n * w.AD[a];
+                        w.E[a] = w.E[a] + n * w.AE[a];
+                        w.F[a] = w.F[a] + n * w.AF[a];
+                    }
+                }
+            }
+    }
+
     if (ReferenceProp) {
         /* OpenBoundaryCondition, AD:5369-5672 (serial); FluxAtOpenBoundary,
          * AD:5680-5742 (OMP DO j / do i / do k). */
         const int bc = p->BoundaryCondition;
         const double TdecAux = 1.0 / (1.0 + p->DecayTime / DT);
-        if (bc == MOHID_BC_MASS_CONSERVATION || bc == MOHID_BC_MASS_CONSERV_NULLGRAD) {
+        if (bc == MOHID_BC_MASS_CONSERVATION || bc == MOHID_BC_MASS_CONSERV_NULLGRAD || bc == MOHID_BC_ORLANSKI) {
             #pragma omp parallel for schedule(dynamic, 1)
             for (int j = 1; j <= nj; ++j)
                 for (int i = 1; i <= ni; ++i)
@@ -929,6 +1156,16 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                         }
                     }
         }
+        /* Orlanski: PROPOld(:,:,:) = PROP(:,:,:) (AD:5428-5429); the field
+         * itself is updated in place at the exterior points */
+        double* PROPOld = NULL;
+        double* ownOld = NULL;
+        if (bc == MOHID_BC_ORLANSKI) {
+            PROPOld = d->PROPOld;
+            if (!PROPOld) PROPOld = ownOld = (double*)malloc(sizeof(double) * X.n3);
+            if (!PROPOld) { ora_work_free(own); return MOHID_AD_ERR_ALLOC; }
+            memcpy(PROPOld, PROP, sizeof(double) * X.n3);
+        }
         for (int j = 1; j <= nj; ++j)
             for (int i = 1; i <= ni; ++i) {
                 if (d->BoundaryPoints2D[I2(i, j)] != 1) continue;
@@ -938,6 +1175,18 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                     if (OP[a] != 1) continue;
                     double DT_V = DT / V[a];
                     double Ext;
+                    if (bc == MOHID_BC_ORLANSKI) {
+                        /* AD:5504-5567, then the inflow / outflow terms of MassConservation */
+                        const double VelBound = w.WFOB[a] * DT_V;
+                        int di = 0, dj = 0, en = 0, ie = 0, je = 0;
+                        orlanski_normal(ni, nj, i, j, &di, &dj, &en, &ie, &je);   /* checked in validate */
+                        const double LimitMax = 10. * DT / (d->DUX[I2(i, j)] + d->DVY[I2(i, j)]) * 2;
+                        Ext = orlanski_celerity_2d(X, PROP, PROPOld, ReferenceProp, OP, 1, ni, 1, nj, di, dj, ie, je,
+                                                   k, en, LimitMax, DT, VelBound);
+                        if (w.WFOB[a] < 0.0) w.TI[a] = w.TI[a] - w.WFOB[a] * Ext * DT_V;
+                        else w.E[a] = w.E[a] + w.WFOB[a] * DT_V;
+                        continue;
+                    }
                     if (bc == MOHID_BC_IMPOSED_VALUE || bc == MOHID_BC_SUBMODEL) {
                         double A1 = OP[I3(i + 1, j, k)] * (1 - d->BoundaryPoints2D[I2(i + 1, j)]);
                         double A2 = OP[I3(i - 1, j, k)] * (1 - d->BoundaryPoints2D[I2(i - 1, j)]);
@@ -977,6 +1226,7 @@ int ora_step_f64(const ora_domain* d, double* PROP, const double* ReferenceProp,
                     }
                 }
             }
+        free(ownOld);
     }
 
     /* SetMatrixValue(TICOEF3, Size, Null_Real, LandPoints3D), AD:1753 */

@@ -55,6 +55,8 @@ typedef struct ora_domain {
     const int *SmallDepths;            /* 2-D, may be NULL */
     const int *NoFluxU, *NoFluxV, *NoFluxW;   /* 3-D, may be NULL (NoAdvFlux / NoDifFlux) */
     const ora_discharges* Disch;              /* may be NULL (no discharges) */
+    double* PROPOld;                   /* 3-D, may be NULL: with Orlanski boundaries it receives
+                                        * the field as OpenBoundaryCondition saw it (AD:5428-5429) */
 } ora_domain;
 
 /* Work arrays of one instance (AllocateVariables, AD:537-684). */

@@ -59,7 +59,7 @@ class OraDomain(C.Structure):
                             "Diff_V", "AreaU", "AreaV", "DZZ", "DWZ")] + \
         [(n, _ip) for n in ("OpenPoints3D", "LandPoints3D", "WaterPoints3D", "ComputeFacesU3D",
                             "ComputeFacesV3D", "ComputeFacesW3D", "SmallDepths", "NoFluxU", "NoFluxV",
-                            "NoFluxW")] + [("Disch", C.POINTER(OraDischarges))]
+                            "NoFluxW")] + [("Disch", C.POINTER(OraDischarges)), ("PROPOld", _dp)]
 
 
 class Params(C.Structure):
@@ -143,7 +143,7 @@ def _p(a, t=_dp):
     return None if a is None else a.ctypes.data_as(t)
 
 
-def cdomain(dom, SmallDepths=None, NoFlux=None, Disch=None) -> OraDomain:
+def cdomain(dom, SmallDepths=None, NoFlux=None, Disch=None, PropOld=None) -> OraDomain:
     a = dom.arrays
     d = OraDomain()
     d.ni, d.nj, d.nk = dom.ni, dom.nj, dom.nk
@@ -158,7 +158,8 @@ def cdomain(dom, SmallDepths=None, NoFlux=None, Disch=None) -> OraDomain:
     d.NoFluxU, d.NoFluxV, d.NoFluxW = (_p(m, _ip) for m in nf)
     q = discharges_struct(Disch) if Disch is not None else None
     d.Disch = C.pointer(q) if q is not None else None
-    d._keep = (dom, SmallDepths, NoFlux, q)
+    d.PROPOld = _p(PropOld)
+    d._keep = (dom, SmallDepths, NoFlux, q, PropOld)
     return d
 
 
@@ -177,11 +178,14 @@ class Work:
 
 
 def step(dom, P: np.ndarray, p: Params, ReferenceProp=None, work: Work | None = None,
-         nthreads: int = 0, SmallDepths=None, NoFlux=None, Disch=None) -> int:
+         nthreads: int = 0, SmallDepths=None, NoFlux=None, Disch=None, PropOld=None) -> int:
     """One FP64 oracle step of one property, in place.  Returns the status code.
-    NoFlux: (NoFluxU, NoFluxV, NoFluxW) int32 Size-box masks, or None."""
+    NoFlux: (NoFluxU, NoFluxV, NoFluxW) int32 Size-box masks, or None.
+    PropOld: float64 Size-box array written with Orlanski boundaries, or None."""
     assert P.dtype == np.float64 and P.flags.c_contiguous and P.shape == dom.shape3
-    cd = cdomain(dom, SmallDepths, NoFlux, Disch)
+    if PropOld is not None:
+        assert PropOld.dtype == np.float64 and PropOld.flags.c_contiguous and PropOld.shape == dom.shape3
+    cd = cdomain(dom, SmallDepths, NoFlux, Disch, PropOld)
     return lib().ora_step_f64(C.byref(cd), _p(P), _p(ReferenceProp), C.byref(p),
                               work.ptr if work is not None else None, nthreads)
 

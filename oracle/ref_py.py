@@ -16,6 +16,7 @@ cells.  tests/ require it to agree bit for bit with the C oracle
     VerticalDiffusion         ModuleAdvectionDiffusion.F90:2708-2784
     VerticalAdvection         :2941-3140
     OpenBoundaryCondition     :5369-5742
+      OrlanskiCelerity2D      ModuleFunctions.F90:4129-4490
     SetMatrixValue(TI, null)  :1753
     THOMASZ_NewType2          ModuleFunctions.F90:4026-4123
 """
@@ -123,6 +124,90 @@ def _null_grad(Pl, CU, CV, k, j, i):
             Pl[k][j + 1][i] * CU[k][j + 1][i] + Pl[k][j - 1][i] * CU[k][j][i]) / float(aux)
 
 
+def _orlanski_normal(ni, nj, i, j):
+    """The normal of boundary point (i, j) and its exterior point (AD:5504-5540):
+    (di, dj, east_north, iext, jext), or None where the reference stops."""
+    if i == 1 or i == ni:
+        di, dj = 1, 0
+    elif j == 1 or j == nj:
+        di, dj = 0, 1
+    else:
+        return None
+    if i == 1 or j == 1:
+        return di, dj, False, i - di, j - dj
+    return di, dj, True, i + di, j + dj
+
+
+def _orlanski(NF, OF, Ref, CP, k, ni, nj, di, dj, i, j, en, limit, dt, flow):
+    """OrlanskiCelerity2D (ModuleFunctions.F90:4129-4490) as OpenBoundaryCondition
+    calls it (AD:5551-5567): implicit, oblique, non-constant celerity, no
+    relaxation times given (86400 * 300 s), compute box 1..ni x 1..nj.  NF / OF
+    are [k][j][i] lists of the Size box; a point (a, b) is addressed through
+    the column-major plane offset a + (ni + 2) * b, as the Fortran does without
+    bounds checks.  Updates OF and NF at (i, j, k) and returns the new value."""
+    I = ni + 2
+
+    def at(arr, a, b):
+        q = a + I * b
+        return arr[k][q // I][q % I]
+
+    no_sw = no_ne = False
+    s = -1 if en else 1                        # from the exterior point into the domain
+    i1n, i1o = at(NF, i + s * di, j + s * dj), at(OF, i + s * di, j + s * dj)
+    i2n = at(NF, i + 2 * s * di, j + 2 * s * dj)
+    i3n = at(NF, i + 3 * s * di, j + 3 * s * dj)
+    i6o = at(OF, i + s * di + dj, j + s * dj + di)
+    i7o = at(OF, i + s * di - dj, j + s * dj - di)
+    bi, bj = i + s * di, j + s * dj            # the first interior point
+    if bi + 3 * dj > ni or bj + 3 * di > nj:
+        no_ne = True
+    elif at(CP, bi + dj, bj + di) * at(CP, bi + 2 * dj, bj + 2 * di) * at(CP, bi + 3 * dj, bj + 3 * di) == 0:
+        no_ne = True
+    if bi - 3 * dj < 1 or bj - 3 * di < 1:
+        no_sw = True
+    elif at(CP, bi - dj, bj - di) * at(CP, bi - 2 * dj, bj - 2 * di) * at(CP, bi - 3 * dj, bj - 3 * di) == 0:
+        no_sw = True
+    b5 = at(OF, i, j)
+    tv = i1n - i1o
+    svx = i1n - i2n
+    if (i6o - i7o) * tv > 0:
+        svy = 0.0 if no_sw else i1o - i7o
+    else:
+        svy = 0.0 if no_ne else i6o - i1o
+    ss = svx * svx + svy * svy
+    if ss > 0.0:
+        cx = -((tv * svx) / ss)
+        cy = -((tv * svy) / ss)
+        if abs(cx) > limit:
+            cx = limit * cx / abs(cx)
+        if abs(cy) > limit:
+            cy = limit * cy / abs(cy)
+    else:
+        cx = cy = 0.0
+    ref = at(Ref, i, j)
+    trelax = float(86400 * 300)
+    cx = cx + flow
+    if cx > 0:
+        cx = 4 * cx
+        adj = 0.0546875 * i3n - 0.2578125 * i2n + 0.6015625 * i1n
+    else:
+        adj, cx, cy = ref, 0.0, 0.0
+    aux = cx * adj
+    if cy >= 0 and not no_sw:
+        b4, b42, b43 = at(OF, i - dj, j - di), at(OF, i - 2 * dj, j - 2 * di), at(OF, i - 3 * dj, j - 3 * di)
+        adjy = 0.0546875 * b43 - 0.2578125 * b42 + 0.6015625 * b4 + 0.6015625 * b5
+        aux = aux - 4 * cy * (b5 - adjy)
+    elif cy < 0 and not no_ne:
+        b3, b32, b33 = at(OF, i + dj, j + di), at(OF, i + 2 * dj, j + 2 * di), at(OF, i + 3 * dj, j + 3 * di)
+        adjy = 0.0546875 * b33 - 0.2578125 * b32 + 0.6015625 * b3 + 0.6015625 * b5
+        aux = aux - 4 * cy * (adjy - b5)
+    q = i + I * j
+    OF[k][q // I][q % I] = NF[k][q // I][q % I]
+    bound = 1 + cx * (1 - 0.6015625) + dt / trelax
+    NF[k][q // I][q % I] = (OF[k][q // I][q % I] + aux + ref * dt / trelax) / bound
+    return NF[k][q // I][q % I]
+
+
 def _thomas_lines(D, E, F, TI, Pl, along_j, ni, nj, nk):
     """THOMAS_3D (FN:3760-3876): a tridiagonal system per work-box line along j
     (or i), first work cell to the halo cell past the last, every layer; the
@@ -186,10 +271,12 @@ def _dif_flux_z(Fl, Kz, DUX, DVY, DZZ, Pl, CW, wgt, ni, nj, nk):
                         (Pl[k][j][i] - Pl[k - 1][j][i])
 
 
-def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=None, Disch=None):
+def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=None, Disch=None, PropOld=None):
     """One step on numpy arrays of a tiny Domain; P (float64 Size box) updated in place.
     `p` is a dict of AdvectionDiffusion scalar arguments.  With CellFluxes set
-    and a dict `fluxes`, the six face-flux arrays are stored in it."""
+    and a dict `fluxes`, the six face-flux arrays are stored in it.  With
+    Orlanski boundaries the field as OpenBoundaryCondition saw it is written
+    to `PropOld` when given (AD:5428-5429)."""
     ni, nj, nk = dom.ni, dom.nj, dom.nk
     A = dom.arrays
     f3 = lambda n: A[n].tolist()           # [k][j][i]
@@ -209,7 +296,13 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
     z3 = lambda v: [[[v] * I for _ in range(J)] for _ in range(K)]
     Kx, Ky, Kz = z3(NULL_REAL), z3(NULL_REAL), z3(NULL_REAL)
     NFU, NFV, NFW = (m.tolist() for m in NoFlux) if NoFlux is not None else (None, None, None)
-    no_adv = bool(p.get("NoAdvFlux"))
+    # AdvectionNudging: the advective terms gather in AdvectionTi/D/E/F, the
+    # _Nudge routines ignore the NoAdvFlux masks (AD:4151-4165, 3211-3350)
+    nudge = bool(p.get("AdvectionNudging"))
+    if nudge and (p["ImpExp_AdvXX"] != 0.0 or p["ImpExp_AdvYY"] != 0.0 or p["Vertical1D"]):
+        raise ValueError("AdvectionNudging with implicit horizontal advection or Vertical1D")
+    no_adv = bool(p.get("NoAdvFlux")) and not nudge
+    ATi, AD, AE, AF = z3(0.0), z3(0.0), z3(0.0), z3(0.0)
     for k in range(2, nk + 1):
         for j in range(1, nj + 1):
             for i in range(1, ni + 1):
@@ -315,6 +408,7 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                             if CV[k][j][i] == 1:
                                 FDY[k][j][i] = FDY[k][j][i] - Ky[k][j][i] * AV[k][j][i] / DZY[j][i - 1] * \
                                     (Pl[k][j][i] - Pl[k][j][i - 1])
+        TIa = ATi if nudge else TI
         # XX: faces j = 1..nj of every line (i, :, k)
         for k in range(1, nk + 1):
             for i in range(1, ni + 1):
@@ -337,8 +431,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                     if p["ImpExp_AdvXX"] == 0.0:
                         fl = XC[k][j][i] * Pl[k][j - 2][i] + XD[k][j][i] * Pl[k][j - 1][i] + \
                             XE[k][j][i] * Pl[k][j][i] + XF[k][j][i] * Pl[k][j + 1][i]
-                        TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
-                        TI[k][j - 1][i] = TI[k][j - 1][i] - fl * DT / V[k][j - 1][i]
+                        TIa[k][j][i] = TIa[k][j][i] + fl * DT / V[k][j][i]
+                        TIa[k][j - 1][i] = TIa[k][j - 1][i] - fl * DT / V[k][j - 1][i]
                     else:                                  # implicit, AD:4490-4515
                         dt2, dt1 = DT / V[k][j][i], DT / V[k][j - 1][i]
                         D[k][j][i] = D[k][j][i] - XD[k][j][i] * dt2
@@ -369,8 +463,8 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                         if p["ImpExp_AdvYY"] == 0.0:
                             fl = YC[k][j][i] * Pl[k][j][i - 2] + YD[k][j][i] * Pl[k][j][i - 1] + \
                                 YE[k][j][i] * Pl[k][j][i] + YF[k][j][i] * Pl[k][j][i + 1]
-                            TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
-                            TI[k][j][i - 1] = TI[k][j][i - 1] - fl * DT / V[k][j][i - 1]
+                            TIa[k][j][i] = TIa[k][j][i] + fl * DT / V[k][j][i]
+                            TIa[k][j][i - 1] = TIa[k][j][i - 1] - fl * DT / V[k][j][i - 1]
                         else:                              # implicit, AD:4855-4880
                             dt2, dt1 = DT / V[k][j][i], DT / V[k][j][i - 1]
                             D[k][j][i] = D[k][j][i] - YD[k][j][i] * dt2
@@ -426,6 +520,7 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                         for k in range(max(KF[j][i], 0), nk + 1):
                             if NFW[k][j][i] == 1:
                                 ZC[k][j][i] = ZD[k][j][i] = ZE[k][j][i] = ZF[k][j][i] = 0.0
+            TIv = ATi if nudge else TI
             if p["ImpExp_AdvV"] == 0.0:
                 for k in range(1, nk + 1):
                     for j in range(1, nj + 1):
@@ -433,8 +528,18 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                             if CW[k][j][i] == 1:
                                 fl = ZC[k][j][i] * Pl[k - 2][j][i] + ZD[k][j][i] * Pl[k - 1][j][i] + \
                                     ZE[k][j][i] * Pl[k][j][i] + ZF[k][j][i] * Pl[k + 1][j][i]
-                                TI[k - 1][j][i] = TI[k - 1][j][i] - fl * DT / V[k - 1][j][i]
-                                TI[k][j][i] = TI[k][j][i] + fl * DT / V[k][j][i]
+                                TIv[k - 1][j][i] = TIv[k - 1][j][i] - fl * DT / V[k - 1][j][i]
+                                TIv[k][j][i] = TIv[k][j][i] + fl * DT / V[k][j][i]
+            elif nudge:                                # VerticalAdvection_Nudge, by layers
+                for k in range(1, nk + 1):
+                    for j in range(1, nj + 1):
+                        for i in range(1, ni + 1):
+                            if CW[k][j][i] == 1:
+                                dt1, dt2 = DT / V[k - 1][j][i], DT / V[k][j][i]
+                                AD[k][j][i] = AD[k][j][i] - ZD[k][j][i] * dt2
+                                AE[k][j][i] = AE[k][j][i] - ZE[k][j][i] * dt2
+                                AE[k - 1][j][i] = AE[k - 1][j][i] + ZD[k][j][i] * dt1
+                                AF[k - 1][j][i] = AF[k - 1][j][i] + ZE[k][j][i] * dt1
             else:
                 def upd(k, j, i, dt1, dt2):
                     D[k][j][i] = D[k][j][i] - ZD[k][j][i] * dt2
@@ -461,9 +566,32 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
             if cflux and p["ImpExp_AdvV"] < 1.0:
                 _adv_flux(FAZ, ZC, ZD, ZE, ZF, Pl, CW, 1.0 - p["ImpExp_AdvV"], ni, nj, nk, 2)
 
+    if nudge:                                          # AdvectionNudging AD:1989-2068
+        nc = p["AdvectionNudgingCells"]
+        in_ = jn_ = 0                                  # kept across cells, as in one OpenMP thread
+        for j in range(1, nj + 1):
+            for i in range(1, ni + 1):
+                cell = False
+                if i < nc + 1:
+                    cell, in_ = True, max(0, i)
+                elif i > ni - nc:
+                    cell, in_ = True, max(0, ni - i + 1)
+                if j < nc + 1:
+                    cell, jn_ = True, max(0, j)
+                elif j > nj - nc:
+                    cell, jn_ = True, max(0, nj - j + 1)
+                n = float(min(in_, jn_)) / nc if cell else 1.0
+                for k in range(1, nk + 1):
+                    if OP[k][j][i] == 1:
+                        TI[k][j][i] = TI[k][j][i] + n * ATi[k][j][i]
+                        D[k][j][i] = D[k][j][i] + n * AD[k][j][i]
+                        E[k][j][i] = E[k][j][i] + n * AE[k][j][i]
+                        F[k][j][i] = F[k][j][i] + n * AF[k][j][i]
+
     if R is not None:
         bc = p["BoundaryCondition"]
         tdec = 1.0 / (1.0 + p["DecayTime"] / DT)
+        PO = [[row[:] for row in lay] for lay in Pl] if bc == 6 else None
         for j in range(1, nj + 1):
             for i in range(1, ni + 1):
                 if BP[j][i] != 1:
@@ -505,11 +633,22 @@ def step(dom, P, p, ReferenceProp=None, SmallDepths=None, fluxes=None, NoFlux=No
                             Qy[k][j][i] * CV[k][j][i] - Qy[k][j][i + 1] * CV[k][j][i + 1] + \
                             Qz[k][j][i] * CW[k][j][i] - Qz[k + 1][j][i] * CW[k + 1][j][i] - \
                             (V[k][j][i] - Vo[k][j][i]) / DT
-                        ext = Pl[k][j][i] * (1.0 - tdec) + R[k][j][i] * tdec
+                        if bc == 6:                    # AD:5496-5569
+                            nrm = _orlanski_normal(ni, nj, i, j)
+                            if nrm is None:
+                                raise ValueError("Orlanski Advection 2")
+                            di, dj, en, ie, je = nrm
+                            limit = 10. * DT / (DUX[j][i] + DVY[j][i]) * 2
+                            ext = _orlanski(Pl, PO, R, OP, k, ni, nj, di, dj, ie, je, en, limit, DT, wf * dtv)
+                        else:
+                            ext = Pl[k][j][i] * (1.0 - tdec) + R[k][j][i] * tdec
                         if wf < 0.0:
                             TI[k][j][i] = TI[k][j][i] - wf * ext * dtv
                         else:
                             E[k][j][i] = E[k][j][i] + wf * dtv
+
+        if PO is not None and PropOld is not None:
+            PropOld[...] = PO
 
     for k in range(K):
         for j in range(J):

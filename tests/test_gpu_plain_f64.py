@@ -242,8 +242,7 @@ def test_gpu_boundary_condition_rules(gpu):
     R = d.reference(2.0, 0.3, seed=2)
     ad = advdiff.AdvectionDiffusion(d)
     ad.set_hydro()
-    for pd, ref, code in [(dict(BoundaryCondition=8), None, 3), (dict(BoundaryCondition=6), R, 4),
-                          (dict(BoundaryCondition=3), R, 3)]:
+    for pd, ref, code in [(dict(BoundaryCondition=8), None, 3), (dict(BoundaryCondition=3), R, 3)]:
         assert O.step(d, P.copy(), O.params(DTProp=30.0, **pd), ReferenceProp=ref) == code
         with pytest.raises(advdiff.N.MohidAdError) as ei:
             ad.step(P.copy(), advdiff.params(DTProp=30.0, **pd), ref)
@@ -341,7 +340,9 @@ def test_gpu_zero_pivot_reported(gpu):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9),
+    (dict(AdvectionNudging=1, AdvectionNudgingCells=2, ImpExp_AdvXX=1.0), 4),
+    (dict(AdvectionNudging=1, AdvectionNudgingCells=2, Vertical1D=1), 4),
 ])
 def test_gpu_rejects_options_like_oracle(gpu, bad, code):
     d = domain("coast")
@@ -380,3 +381,122 @@ def test_gpu_unknown_id_and_bad_bounds(gpu):
                            advdiff.N.ptr(z), advdiff.N.ptr(z), advdiff.N.ptr(z),
                            advdiff.N.iptr(zi), advdiff.N.iptr(zi), C.byref(st))
     assert rc == 1
+
+
+@pytest.mark.parametrize("grid", ["open", "nsopen", "allopen", "narrow", "flat", "wide"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_minmod", "implicit_xx", "theta_difv"])
+def test_gpu_orlanski(gpu, grid, opt):
+    # Orlanski open boundaries (AD:5496-5569, FN:4129-4490) over four steps:
+    # the field with its radiated exterior values and PropOld, through the host
+    # and the device entry points, bit for bit against the oracle
+    import torch
+    from tests.test_oracle_crosscheck import _orlanski_grids
+    if grid == "wide":
+        d = synth.generate(synth.GenSpec(ni=61, nj=47, nk=7, land_frac=0.1, land_kind=1, seed=13, open_sides=15,
+                                         bathy_kind=1, vol_var=0.01, dt=30.0))
+    else:
+        d = _orlanski_grids()[grid]
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    pd = dict(DTProp=30.0, BoundaryCondition=6, **OPTIONS[opt])
+    Po, oo = P0.copy(), np.zeros_like(P0)
+    olds = []
+    for _ in range(4):
+        assert O.step(d, Po, O.params(**pd), ReferenceProp=R, PropOld=oo) == 0
+        olds.append(oo.copy())
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg, og = P0.copy(), np.zeros_like(P0)
+    ad.set_prop_old(og)
+    for q in range(4):
+        ad.step(Pg, advdiff.params(**pd), R)
+        assert np.array_equal(og, olds[q])
+    assert np.array_equal(Pg, Po)
+    a = torch.from_numpy(P0.copy()).cuda()
+    b = torch.empty_like(a)
+    od = torch.zeros_like(a)
+    ad.set_prop_old(od, device=True)
+    Rd = torch.from_numpy(R).cuda()
+    for _ in range(4):
+        ad.step_device(a, b, advdiff.params(**pd), Rd)
+        a, b = b, a
+    ad.sync()
+    ad.set_prop_old(None)
+    ad.kill()
+    assert np.array_equal(a.cpu().numpy(), Po)
+    assert np.array_equal(od.cpu().numpy(), olds[-1])
+
+
+def test_gpu_orlanski_rejects_interior_boundary_points(gpu):
+    # a boundary point off the work box's edges: the reference stops, the
+    # drop-in returns MOHID_AD_ERR_OPTION like the oracle
+    from tests.test_oracle_crosscheck import _orlanski_grids
+    d = _orlanski_grids()["allopen"]
+    bp = d.arrays["BoundaryPoints2D"].copy()
+    bp[3, 4] = 1
+    d.arrays["BoundaryPoints2D"] = bp
+    P = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    pd = dict(DTProp=30.0, BoundaryCondition=6)
+    assert O.step(d, P.copy(), O.params(**pd), ReferenceProp=R) == 3
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        ad.step(P.copy(), advdiff.params(**pd), R)
+    assert ei.value.code == 3
+    Q = P.copy()                                     # the instance stays usable
+    ad.step(Q, advdiff.params(**dict(pd, BoundaryCondition=1)), R)
+    ad.kill()
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open", "layer1", "nsopen"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "explicit_v_tvd", "docycle2", "theta_difv", "xzflow"])
+@pytest.mark.parametrize("nc", [1, 3])
+def test_gpu_nudging(gpu, grid, opt, nc):
+    # AdvectionNudging (AD:1989-2068): the advective terms gathered apart and
+    # scaled by the edge factor, with the cell fluxes; bit for bit
+    d = domain(grid)
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2) if d.spec.open_sides else None
+    pd = dict(DTProp=30.0, AdvectionNudging=1, AdvectionNudgingCells=nc, CellFluxes=1, **OPTIONS[opt])
+    Po = P0.copy()
+    work = O.Work(d)
+    assert O.step(d, Po, O.params(**pd), ReferenceProp=R, work=work) == 0
+    fo = O.cell_fluxes(d, work)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    ad.step(Pg, advdiff.params(**pd), R)
+    fg = ad.cell_fluxes()
+    ad.kill()
+    assert np.array_equal(Pg, Po)
+    for n in O.FLUX_NAMES:
+        assert np.array_equal(fg[n], fo[n]), n
+
+
+def test_gpu_nudging_many_steps(gpu):
+    # a larger open grid, several steps, host and device entry points
+    import torch
+    d = synth.generate(synth.GenSpec(ni=61, nj=47, nk=7, land_frac=0.1, land_kind=1, seed=13, open_sides=15,
+                                     bathy_kind=1, dt=30.0))
+    P0 = d.tracer(3, 1.0, 0.5, seed=1)
+    R = d.reference(2.0, 0.3, seed=2)
+    pd = dict(DTProp=30.0, AdvectionNudging=1, AdvectionNudgingCells=5, **OPTIONS["tvd_superbee"])
+    Po = P0.copy()
+    for _ in range(4):
+        assert O.step(d, Po, O.params(**pd), ReferenceProp=R) == 0
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P0.copy()
+    for _ in range(4):
+        ad.step(Pg, advdiff.params(**pd), R)
+    assert np.array_equal(Pg, Po)
+    a = torch.from_numpy(P0.copy()).cuda()
+    b = torch.empty_like(a)
+    Rd = torch.from_numpy(R).cuda()
+    for _ in range(4):
+        ad.step_device(a, b, advdiff.params(**pd), Rd)
+        a, b = b, a
+    ad.sync()
+    ad.kill()
+    assert np.array_equal(a.cpu().numpy(), Po)

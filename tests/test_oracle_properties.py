@@ -366,7 +366,9 @@ def test_land_and_halo_handling(built):
     (dict(ImpExp_DifH=1.0), 3), (dict(ImpExp_AdvXX=1.0, ImpExp_AdvYY=1.0), 3),
     (dict(AdvMethodV=2, Upwind2V=1), 3), (dict(AdvMethodH=4, Upwind2H=0), 3),
     (dict(AdvMethodH=9), 3), (dict(ImpExp_AdvV=0.5), 3), (dict(Docycle_method=3), 3),
-    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9), (dict(AdvectionNudging=1), 4),
+    (dict(ImpExp_AdvXX=0.5), 3), (dict(NoAdvFlux=1), 9),
+    (dict(AdvectionNudging=1, AdvectionNudgingCells=2, ImpExp_AdvXX=1.0), 4),
+    (dict(AdvectionNudging=1, AdvectionNudgingCells=2, Vertical1D=1), 4),
 ])
 def test_rejected_options(built, bad, code):
     d = domain("coast")
@@ -380,9 +382,8 @@ def test_boundary_condition_rules(built):
     d = domain("open")
     P = d.tracer(4, 1.0, 0.0, seed=1)
     R = d.reference(2.0, 0.3, seed=2)
-    # cyclic boundaries read the reference (AD:2150); Orlanski is not built
+    # cyclic boundaries read the reference (AD:2150)
     assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=8)) == 3
-    assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=6), ReferenceProp=R) == 4
     assert O.step(d, P.copy(), O.params(DTProp=30.0, BoundaryCondition=3), ReferenceProp=R) == 3
     # without a reference a BC other than 4 and 8 changes nothing (AD:1874-1880, AD:5816)
     a, b = P.copy(), P.copy()
