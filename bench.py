@@ -460,7 +460,11 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
 
     ensemble = len(cases) > 1
     free, total = torch.cuda.mem_get_info()
-    need = sum(c.cells for c in cases) * (120 + 12 * cases[0].nt + (4 * cases[0].nt if cases[0].refs else 0))
+    # per cell: the FP64 hydrodynamics and masks, the packed fields, two FP32
+    # tracer buffers and the G scratch of the largest tracer group (the open
+    # boundaries' references are kept for the boundary columns only)
+    nt0 = cases[0].nt
+    need = sum(c.cells for c in cases) * (120 + 8 * nt0 + 4 * min(nt0, 10))
     if need > 0.9 * free:
         raise SystemExit(f"the workload needs about {need / 2**30:.0f} GiB of device memory, {free / 2**30:.0f} free")
     objs = [load_batch(c, storage) for c in cases]

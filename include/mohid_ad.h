@@ -353,7 +353,9 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
  * the tracer itself: a tracer is held as its anomaly from a per-tracer
  * constant (the mean over its water cells, chosen when it is loaded), and
  * its reference is stored relative to the same constant (the step subtracts
- * the mass fixer's correction to that constant). */
+ * the mass fixer's correction to that constant).  Only the boundary columns
+ * (BoundaryPoints2D == 1) read a reference, so only they are kept: (KUB + 2)
+ * FP32 values per boundary column and tracer. */
 int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
                                    const int* on_device, int* stat);
 
@@ -367,14 +369,15 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
  * the batch on the batch itself and keeps the fastest.  The schedules are one
  * CTA per 32 x 8 tile, or a persistent grid over the tiles that hold water with
  * the deepest first (the column-length-aware schedule for z-level domains);
- * with 4 or more tracers, 4 or 2 tracers per launch (with 8 or more also 8).
+ * with 4 or more tracers, 4 or 2 tracers per launch (with 8 or more also 8,
+ * with 10 or more also 10).
  * Each candidate runs a warm-up and two timed steps that leave the tracers
  * unchanged.  The first mohid_ad_batched_step of a batch runs it; call it
  * again after a change that
  * may favour another schedule. */
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat);
 
-/* Set the schedule by hand (*sched 0 or 1, *split 8, 4 or 2) instead of the autotuner. */
+/* Set the schedule by hand (*sched 0 or 1, *split 10, 8, 4 or 2) instead of the autotuner. */
 int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat);
 
 /* The schedule in use: kernel launches per step (the step kernels, and with

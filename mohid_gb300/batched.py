@@ -80,7 +80,7 @@ class Batch:
                 "mohid_ad_batched_set_schedule")
 
     def schedule(self) -> dict:
-        """{'launches': kernel launches per step, 'sched': 0 grid / 1 tile list, 'split': 8, 4 or 2,
+        """{'launches': kernel launches per step, 'sched': 0 grid / 1 tile list, 'split': 10, 8, 4 or 2,
         'per_call': launches made once per step() call (the closed-domain mass fixer's finish)}."""
         n, sc, sp, pc, st = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
         N.check(self.lib.mohid_ad_batched_schedule(C.byref(self._bid), C.byref(n), C.byref(sc), C.byref(sp),

@@ -22,11 +22,16 @@ LIB = PKG / "_lib"
 OBJ = PKG / "_build"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-# (source, extra nvcc flags)
+# (source, extra nvcc flags[, object name])
 CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
     ("batched_kernel.cu", []),
     ("batched_kernel_obc.cu", []),
+] + [
+    # the batched step's kernels: one unit per boundary form and storage
+    ("batched_inst.cu", [f"-DMOHID_INST_OBC={o}", f"-DMOHID_INST_STORAGE={st}"], f"batched_inst_{o}{st}")
+    for o in (0, 1) for st in (0, 1, 2)
+] + [
     ("ensemble_kernel.cu", []),
     ("batched_pack.cu", []),
     ("mass_noalloc.cu", []),
@@ -65,9 +70,10 @@ def build(verbose: bool = False, force: bool = False) -> dict:
               "-I", str(PKG.parent / "include")]
     jobs = []
     objs = []
-    for src, extra in CUDA_UNITS:
+    for unit in CUDA_UNITS:
+        src, extra = unit[0], unit[1]
         s = CSRC / src
-        o = OBJ / (Path(src).stem + ".o")
+        o = OBJ / ((unit[2] if len(unit) > 2 else Path(src).stem) + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             lang = ["-x", "cu"] if src.endswith(".cu") else []

@@ -79,7 +79,13 @@ struct BatchArgs {
     float* Pout;
     long long ts;
     int nt;
-    const float* Ref;                   // same layout as tracers (boundary cells read), or null
+    // open-boundary references of the boundary columns only (or null): tracer
+    // t, boundary column q, layer k at Ref[t * rts + q * rk + k]; refIdx holds
+    // q for each column of the layout (-1 away from the boundary)
+    const float* Ref;
+    const int* refIdx;
+    long long rts;
+    int rk;
     float* W;                           // scratch: THOMASZ W per cell (batched layout)
     float* G;                           // scratch: THOMASZ G of the launch's tracers per cell, nt
                                         // floats per cell (cell c at G + c * nt)
@@ -217,6 +223,14 @@ cudaError_t pack_tracer(const double* src, float* dstA, float* dstB, const int* 
 // shift: the stored values' constant; corr (device, may be null): a correction added to it
 cudaError_t unpack_tracer(const float* src, double* dst, const double* orig, const int* WP,
                           const int* KFloor, double shift, const double* corr, const BLayout& L, cudaStream_t s);
+// open-boundary references: column q of `cols` (Size-box 2-D offsets i + (ni+2) j)
+// at layer k to dst[q * (nk+2) + k], relative to the tracer's constant on water
+// cells; back to absolute values; and each boundary column's q in the layout
+cudaError_t pack_ref(const double* src, const int* WP, const int* cols, int ncols, int ni, int nj, int nk,
+                     double shift, float* dst, cudaStream_t s);
+cudaError_t unshift_ref(float* R, const int* WP, const int* cols, int ncols, int ni, int nj, int nk, double shift,
+                        cudaStream_t s);
+cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int* idx, cudaStream_t s);
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,

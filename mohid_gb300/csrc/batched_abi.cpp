@@ -41,7 +41,8 @@ struct Batch {
     DevBuf<float4> fc;
     DevBuf<float> areaCol;
     DevBuf<int> kfloor;
-    DevBuf<float> PA, PB, Ref;
+    DevBuf<float> PA, PB, Ref;           // tracers (ping-pong); references of the boundary columns
+    DevBuf<int> refIdx;                  // per column of the layout: its row in Ref, or -1
     DevBuf<float> Wsc, Gsc;              // THOMASZ W and G per cell, scratch of the step kernel
     // mass fixer (static volumes): VolumeZ as an FP32 pair, the fixer state
     // (volume, targets, constants, corrections, boundary fluxes), per-tile
@@ -67,7 +68,7 @@ struct Batch {
     DevBuf<int> tcost;
     int ntl = 0;
     int sched = 0;                       // 0 grid, 1 tile list
-    int split = 4;                       // largest tracer group per launch: 8, 4 or 2
+    int split = 4;                       // largest tracer group per launch: 10, 8, 4 or 2
     bool tuned = false;
     int graphSched = -1, graphSplit = -1;
     int graphFix = -1;                   // fixer / open-boundary launches the graph holds
@@ -112,7 +113,7 @@ struct Batch {
     DevBuf<double> partial, scratch, stage;
     double* hmass = nullptr;             // pinned
     mohid::TmaMaps maps{};               // shared-field maps (valid after a pack)
-    CUtensorMap mapP[2][4];              // tracer maps: input buffer (A/B) x group size (1, 2, 4, 8)
+    CUtensorMap mapP[2][5];              // tracer maps: input buffer (A/B) x group size (1, 2, 4, 8, 10)
     bool mapsOk = false;
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
@@ -128,7 +129,7 @@ struct Batch {
         for (auto* b : h) b->release();
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
-        partial.release(); scratch.release(); stage.release();
+        partial.release(); scratch.release(); stage.release(); refIdx.release();
         mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release();
         obpart.release(); obcol.release(); obcnt.release();
         tl.release(); tcost.release();
@@ -341,9 +342,9 @@ int pack_enqueue(Batch* b, int* stat)
         okm &= encode_map(&M.Dv, tk, ek, dif, L, 1, box[10]);
         okm &= encode_map(&M.Dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->DZZ.p, L, 1, box[11]);
         okm &= encode_map(&M.Fn, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->flag.p, L, 1, box[12]);
-        const int gs[4] = {1, 2, 4, 8};
+        const int gs[5] = {1, 2, 4, 8, 10};
         for (int buf = 0; buf < 2; ++buf)
-            for (int g = 0; g < 4; ++g) {
+            for (int g = 0; g < 5; ++g) {
                 if (gs[g] > b->nt) continue;
                 int bb[mohid::kNumMaps][4];
                 mohid::batched_boxes(hq, hk, gs[g], bb);
@@ -450,7 +451,10 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.Pout = Pout + (long long)t0 * a.ts;
     a.nt = nt;
     a.t0 = t0;
-    a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.ts : nullptr;
+    a.rk = b->L.nk + 2;
+    a.rts = (long long)b->in->nbcols * a.rk;
+    a.Ref = b->hasRef ? b->Ref.p + (long long)t0 * a.rts : nullptr;
+    a.refIdx = b->hasRef ? b->refIdx.p : nullptr;
     a.W = b->Wsc.p;
     a.G = b->Gsc.p;
     a.Vhi = b->Vhi.p;
@@ -506,7 +510,9 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
             CK(mohid::unshift(b->PA.p + off, b->flag.p, b->shift[t], b->L.n3, s));
             CK(mohid::unshift(b->PB.p + off, b->flag.p, b->shift[t], b->L.n3, s));
             if (b->hasRef && t < (int)b->refShift.size() && b->refShift[t] != 0.0) {
-                CK(mohid::unshift(b->Ref.p + off, b->flag.p, b->refShift[t], b->L.n3, s));
+                const long long rts = (long long)in->nbcols * (b->L.nk + 2);
+                CK(mohid::unshift_ref(b->Ref.p + (long long)t * rts, in->WP.p, in->bcols.p, in->nbcols, in->ni,
+                                      in->nj, in->nk, b->refShift[t], s));
                 b->refShift[t] = 0.0;
             }
             b->shift[t] = 0.0;
@@ -515,15 +521,16 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     return ok(stat);
 }
 
-// tracers of the next launch: groups of b->split (8, 4 or 2), then 4, 2, 1
+// tracers of the next launch: groups of b->split (10, 8, 4 or 2), then 8, 4, 2, 1
 inline int group_size(const Batch* b, int left)
 {
+    if (left >= 10 && b->split >= 10) return 10;
     if (left >= 8 && b->split >= 8) return 8;
     if (left >= 4 && b->split >= 4) return 4;
     return left >= 2 ? 2 : 1;
 }
 
-inline int map_index(int g) { return g == 8 ? 3 : (g == 4 ? 2 : (g == 2 ? 1 : 0)); }
+inline int map_index(int g) { return g == 10 ? 4 : (g == 8 ? 3 : (g == 4 ? 2 : (g == 2 ? 1 : 0))); }
 
 int launches_per_step(const Batch* b)
 {
@@ -598,8 +605,8 @@ int autotune(Batch* b, const mohid_ad_params* p, int* stat)
     int bestSched = 0, bestSplit = 4;
     float best = 1e30f;
     cudaError_t err = cudaSuccess;
-    for (int split : {8, 4, 2}) {
-        if ((split == 8 && b->nt < 8) || (split == 2 && b->nt < 4)) continue;
+    for (int split : {10, 8, 4, 2}) {
+        if ((split == 10 && b->nt < 10) || (split == 8 && b->nt < 8) || (split == 2 && b->nt < 4)) continue;
         for (int sched : {0, 1}) {
             if (sched == 1 && b->ntl == 0) continue;
             b->sched = sched;
@@ -749,7 +756,8 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
     if ((e = b->PB.alloc(n3 * b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Wsc.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     {
-        const int gmax = b->nt >= 8 ? 8 : (b->nt >= 4 ? 4 : (b->nt >= 2 ? 2 : 1));   // largest tracer group
+        // the largest tracer group a launch can hold (group_size): NT floats of G per cell
+        const int gmax = b->nt >= 10 ? 10 : (b->nt >= 8 ? 8 : (b->nt >= 4 ? 4 : (b->nt >= 2 ? 2 : 1)));
         if ((e = b->Gsc.alloc(n3 * (size_t)gmax)) != cudaSuccess) return bad(e, "cudaMalloc");
     }
     b->tilesX = (in->ni + mohid::kTX - 1) / mohid::kTX;
@@ -882,11 +890,19 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
     if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
-    if (!b->Ref.p) {
-        cudaError_t e = b->Ref.alloc((size_t)b->L.n3 * b->nt);
-        if (e != cudaSuccess) return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
-    }
     cudaStream_t s = in->stream;
+    // only the boundary columns read a reference: one row of nk + 2 layers
+    // per boundary column (the reference's sweep order) and tracer
+    const long long rts = (long long)in->nbcols * (b->L.nk + 2);
+    if (!b->Ref.p) {
+        cudaError_t e = b->Ref.alloc((size_t)std::max<long long>(1, rts * b->nt));
+        if (e == cudaSuccess) e = b->refIdx.alloc((size_t)b->L.n2);
+        if (e != cudaSuccess) {
+            b->Ref.release(); b->refIdx.release();
+            return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
+        }
+        CK(mohid::ref_index(in->bcols.p, in->nbcols, in->ni, b->L, b->refIdx.p, s));
+    }
     const double* src = ReferenceProp;
     if (!*on_device) {
         CK(cudaMemcpyAsync(b->stage.p, ReferenceProp, sizeof(double) * in->n3, cudaMemcpyHostToDevice, s));
@@ -894,7 +910,8 @@ int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* R
     }
     // stored relative to the tracer's loaded constant, like the tracer; the
     // step subtracts the mass fixer's correction to that constant
-    CK(mohid::pack_shift_f32(src, b->Ref.p + (long long)*t * b->L.n3, in->WP.p, b->shift[*t], b->L, s));
+    CK(mohid::pack_ref(src, in->WP.p, in->bcols.p, in->nbcols, in->ni, in->nj, in->nk, b->shift[*t],
+                       b->Ref.p + (long long)*t * rts, s));
     CK(cudaStreamSynchronize(s));
     b->hasRef = true;
     b->refShift.resize(b->nt, 0.0);
@@ -1006,8 +1023,8 @@ int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* s
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!sched || !split) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
-    if ((*sched != 0 && *sched != 1) || (*split != 8 && *split != 4 && *split != 2))
-        return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 8, 4 or 2");
+    if ((*sched != 0 && *sched != 1) || (*split != 10 && *split != 8 && *split != 4 && *split != 2))
+        return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 10, 8, 4 or 2");
     b->sched = *sched;
     b->split = *split;
     b->tuned = true;

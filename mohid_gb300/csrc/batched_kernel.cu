@@ -1,6 +1,6 @@
-// batched_kernel.cu -- closed-domain instantiation of the batched step
-// (batched_launch.cuh), the tile-cost kernel of the schedule, and the layout
-// queries of the batched form.
+// batched_kernel.cu -- the dispatch of the batched step to its instantiation
+// units (batched_inst.cu), the tile-cost kernel of the schedule, and the
+// layout queries of the batched form.
 #include "batched_launch.cuh"
 
 namespace mohid {
@@ -55,19 +55,20 @@ cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_batched_closed(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                                  bool halfK, const int2* tiles, int ntl, cudaStream_t s)
-{
-    return launch_detail::launch_batched_form<false>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-}
-
 // open boundaries (reference concentrations set) take the instantiation
 // that carries the MassConservation boundary terms
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
                            bool halfK, const int2* tiles, int ntl, cudaStream_t s)
 {
-    if (a.Ref) return launch_batched_open(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-    return launch_batched_closed(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
+    const int storage = halfQ ? (halfK ? 2 : 1) : 0;
+    if (a.Ref) {
+        if (storage == 2) return launch_batched_unit<true, 2>(a, m, method, limiter, tiles, ntl, s);
+        if (storage == 1) return launch_batched_unit<true, 1>(a, m, method, limiter, tiles, ntl, s);
+        return launch_batched_unit<true, 0>(a, m, method, limiter, tiles, ntl, s);
+    }
+    if (storage == 2) return launch_batched_unit<false, 2>(a, m, method, limiter, tiles, ntl, s);
+    if (storage == 1) return launch_batched_unit<false, 1>(a, m, method, limiter, tiles, ntl, s);
+    return launch_batched_unit<false, 0>(a, m, method, limiter, tiles, ntl, s);
 }
 
 cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int* cost,
@@ -79,6 +80,7 @@ cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L
 
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk)
 {
+    if (nt == 10) return smem_n<10>(halfQ, halfK, nk);
     if (nt == 8) return smem_n<8>(halfQ, halfK, nk);
     if (nt == 4) return smem_n<4>(halfQ, halfK, nk);
     if (nt == 2) return smem_n<2>(halfQ, halfK, nk);

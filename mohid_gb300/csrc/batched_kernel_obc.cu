@@ -1,6 +1,5 @@
-// batched_kernel_obc.cu -- open-boundary instantiation of the batched step
-// (batched_launch.cuh): MassConservation boundary terms compiled in; and the
-// boundary mass flux of a step, which the mass fixer's target follows.
+// batched_kernel_obc.cu -- the boundary mass flux of a batched step with
+// MassConservation open boundaries, which the mass fixer's target follows.
 #include "batched_launch.cuh"
 
 namespace mohid {
@@ -50,12 +49,13 @@ __global__ void __launch_bounds__(kFluxThreads) k_obc_flux(const BatchArgs A, co
          base += (long long)gridDim.x * kFluxThreads) {
         const long long e = base + threadIdx.x;
         double wd = 0.0;
-        long long a = 0;
+        long long a = 0, r = 0;
         bool act = false, in = false;
         if (e < ncell) {
             const long long c2 = list[1 + (int)(e % n)];
             const int k = 1 + (int)(e / n);
             a = c2 + (long long)k * L.sl;
+            r = (long long)A.refIdx[c2] * A.rk + k;   // the cell's reference (boundary columns only)
             if (k >= A.kfloor[c2] && (A.flag[a] & F_OP)) {
                 const uint8_t fl = A.flag[a];
                 const uint8_t flp = k == L.nk ? 0 : A.flag[a + L.sl];
@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(kFluxThreads) k_obc_flux(const BatchArgs A, co
             double v = 0.0;
             if (act) {
                 const long long ta = (long long)t * A.ts + a;
-                const float y = in ? A.Pin[ta] * (1.f - A.tdec) + (A.Ref[ta] - corr[t]) * A.tdec : A.Pout[ta];
+                const float y = in ? A.Pin[ta] * (1.f - A.tdec) + (A.Ref[(long long)t * A.rts + r] - corr[t]) * A.tdec
+                                   : A.Pout[ta];
                 v = wd * (double)y;
             }
             v = warp_sum_fixed(v);
@@ -109,12 +110,6 @@ cudaError_t obc_flux(const BatchArgs& a, const int* list, bool halfQ, cudaStream
     if (halfQ) k_obc_flux<__half><<<a.nob, kFluxThreads, smem, s>>>(a, list);
     else k_obc_flux<float><<<a.nob, kFluxThreads, smem, s>>>(a, list);
     return cudaGetLastError();
-}
-
-cudaError_t launch_batched_open(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                                bool halfK, const int2* tiles, int ntl, cudaStream_t s)
-{
-    return launch_detail::launch_batched_form<true>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
 }
 
 }  // namespace mohid

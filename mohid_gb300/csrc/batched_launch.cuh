@@ -3,8 +3,7 @@
 // tile of the grid, or a persistent grid walking a list of the tiles that hold
 // water, costliest (deepest) first -- the column-length-aware schedule for
 // z-level domains, whose shallow and land tiles would otherwise cost CTAs.
-// Instantiated for closed domains in batched_kernel.cu and for open
-// boundaries in batched_kernel_obc.cu (compiled in parallel).
+// Instantiated by batched_inst.cu, once per boundary form and storage.
 #pragma once
 #include "batched_tile.cuh"
 
@@ -73,32 +72,43 @@ cudaError_t launch_m(const BatchArgs& a, const TmaMaps& m, int method, int limit
     }
 }
 
-template <int NT, bool OBC>
-cudaError_t launch_n(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ, bool halfK,
-                     const int2* tiles, int ntl, cudaStream_t s)
+// the kernels of one storage (QT transports, KT diffusivities) for every
+// tracer group size and scheme
+template <bool OBC, typename QT, typename KT>
+cudaError_t launch_storage(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles, int ntl,
+                           cudaStream_t s)
 {
-    if (halfQ && halfK) return launch_m<NT, __half, __half, OBC>(a, m, method, limiter, tiles, ntl, s);
-    if (halfQ) return launch_m<NT, __half, float, OBC>(a, m, method, limiter, tiles, ntl, s);
-    return launch_m<NT, float, float, OBC>(a, m, method, limiter, tiles, ntl, s);
-}
-
-template <bool OBC>
-cudaError_t launch_batched_form(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                                bool halfK, const int2* tiles, int ntl, cudaStream_t s)
-{
-    if (a.nt == 8) return launch_n<8, OBC>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-    if (a.nt == 4) return launch_n<4, OBC>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-    if (a.nt == 2) return launch_n<2, OBC>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-    if (a.nt == 1) return launch_n<1, OBC>(a, m, method, limiter, halfQ, halfK, tiles, ntl, s);
-    return cudaErrorInvalidValue;
+    switch (a.nt) {
+    case 10: return launch_m<10, QT, KT, OBC>(a, m, method, limiter, tiles, ntl, s);
+    case 8: return launch_m<8, QT, KT, OBC>(a, m, method, limiter, tiles, ntl, s);
+    case 4: return launch_m<4, QT, KT, OBC>(a, m, method, limiter, tiles, ntl, s);
+    case 2: return launch_m<2, QT, KT, OBC>(a, m, method, limiter, tiles, ntl, s);
+    case 1: return launch_m<1, QT, KT, OBC>(a, m, method, limiter, tiles, ntl, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace launch_detail
 
-// the two instantiations (batched_kernel.cu, batched_kernel_obc.cu)
-cudaError_t launch_batched_closed(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                                  bool halfK, const int2* tiles, int ntl, cudaStream_t s);
-cudaError_t launch_batched_open(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                                bool halfK, const int2* tiles, int ntl, cudaStream_t s);
+// One instantiation unit per boundary form (OBC: the MassConservation terms
+// compiled in) and storage (0: FP32, 1: FP16 transports, 2: FP16 transports
+// and diffusivities): batched_inst.cu, compiled once per pair in parallel.
+template <bool OBC, int STORAGE>
+cudaError_t launch_batched_unit(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles,
+                                int ntl, cudaStream_t s)
+{
+    using QT = typename std::conditional<STORAGE >= 1, __half, float>::type;
+    using KT = typename std::conditional<STORAGE >= 2, __half, float>::type;
+    return launch_detail::launch_storage<OBC, QT, KT>(a, m, method, limiter, tiles, ntl, s);
+}
+#define MOHID_BATCHED_UNIT(OBC, STORAGE)                                                                   \
+    template cudaError_t launch_batched_unit<OBC, STORAGE>(const BatchArgs&, const TmaMaps&, int, int,     \
+                                                           const int2*, int, cudaStream_t)
+extern MOHID_BATCHED_UNIT(false, 0);
+extern MOHID_BATCHED_UNIT(false, 1);
+extern MOHID_BATCHED_UNIT(false, 2);
+extern MOHID_BATCHED_UNIT(true, 0);
+extern MOHID_BATCHED_UNIT(true, 1);
+extern MOHID_BATCHED_UNIT(true, 2);
 
 }  // namespace mohid

@@ -400,6 +400,31 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
+// open-boundary references of the boundary columns (element e = q * nk2 + k)
+__global__ void k_pack_ref(const double* __restrict__ src, const int* __restrict__ WP, const int* __restrict__ cols,
+                           long long n, int nk2, long long sk, double shift, float* __restrict__ dst)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long c = cols[e / nk2] + sk * (e % nk2);
+        dst[e] = (float)(src[c] - (WP[c] == 1 ? shift : 0.0));
+    }
+}
+__global__ void k_unshift_ref(float* R, const int* __restrict__ WP, const int* __restrict__ cols, long long n,
+                              int nk2, long long sk, double shift)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const long long c = cols[e / nk2] + sk * (e % nk2);
+        if (WP[c] == 1) R[e] = (float)((double)R[e] + shift);
+    }
+}
+__global__ void k_ref_index(const int* __restrict__ cols, int ncols, int sj, BLayout L, int* idx)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ncols) return;
+    const int c = cols[q];
+    idx[L.at2(c % sj, c / sj)] = q;
+}
+
 // add the stored constant back: anomaly -> absolute values (water cells)
 __global__ void k_unshift(float* P, const uint8_t* flag, double shift, long long n)
 {
@@ -806,6 +831,31 @@ cudaError_t continuity_residual(const double* Qx, const double* Qy, const double
     if (e != cudaSuccess) return e;
     k_continuity<<<row_blocks(L, L.nk), kRowThreads, 0, s>>>(Qx, Qy, Qz, V, Vold, OP, CFU, CFV, CFW, BP2D, 1.0 / DT, tol,
                                                               L, reinterpret_cast<unsigned long long*>(out));
+    return cudaGetLastError();
+}
+cudaError_t pack_ref(const double* src, const int* WP, const int* cols, int ncols, int ni, int nj, int nk,
+                     double shift, float* dst, cudaStream_t s)
+{
+    const long long n = (long long)ncols * (nk + 2);
+    if (n <= 0) return cudaSuccess;
+    const long long sk = (long long)(ni + 2) * (nj + 2);
+    k_pack_ref<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(src, WP, cols, n, nk + 2, sk, shift, dst);
+    return cudaGetLastError();
+}
+cudaError_t unshift_ref(float* R, const int* WP, const int* cols, int ncols, int ni, int nj, int nk, double shift,
+                        cudaStream_t s)
+{
+    const long long n = (long long)ncols * (nk + 2);
+    if (n <= 0) return cudaSuccess;
+    const long long sk = (long long)(ni + 2) * (nj + 2);
+    k_unshift_ref<<<blocks_for(n) > 4096 ? 4096 : blocks_for(n), 256, 0, s>>>(R, WP, cols, n, nk + 2, sk, shift);
+    return cudaGetLastError();
+}
+cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int* idx, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(idx, 0xff, sizeof(int) * (size_t)L.n2, s);
+    if (e != cudaSuccess || ncols <= 0) return e;
+    k_ref_index<<<(ncols + 255) / 256, 256, 0, s>>>(cols, ncols, ni + 2, L, idx);
     return cudaGetLastError();
 }
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s)

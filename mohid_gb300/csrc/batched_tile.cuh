@@ -294,6 +294,19 @@ template <> struct GVec<8> {
     }
 };
 
+template <> struct GVec<10> {                     // 40 B per cell: 8-byte aligned pairs
+    static __device__ __forceinline__ void st(float* a, const float* g, uint64_t pol)
+    {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) GVec<2>::st(a + 2 * q, g + 2 * q, pol);
+    }
+    static __device__ __forceinline__ void ld(const float* a, float* g, uint64_t pol)
+    {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) GVec<2>::ld(a + 2 * q, g + 2 * q, pol);
+    }
+};
+
 // the 128-byte L2 line at a holds only dead data: drop it without a write-back
 __device__ __forceinline__ void l2_discard(const void* a)
 {
@@ -504,6 +517,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     // open boundaries are compiled in only where the batch has reference
     // concentrations: the closed form carries none of their instructions
     const bool obcCol = OBC && (cf & C_BP) && A.Ref != nullptr;
+    const float* refc = obcCol ? A.Ref + (long long)A.refIdx[c2] * A.rk : nullptr;   // this column's row
     // own-column values of the face below row k slide up the walk: transport,
     // conductance Kz * area / DZZ (AD:2736-2765), cell flags of rows k-1 and k
     float qz = 0.f, kzb = 0.f;
@@ -634,7 +648,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                 if (obc && wfob < 0.f) {
                     // the reference is stored relative to the tracer's loaded
                     // constant; the fixer's correction moves it with the field
-                    const float ref = A.Ref[(long long)t * A.ts + cb + (long long)k * L.sl] -
+                    const float ref = refc[(long long)t * A.rts + k] -
                                       (float)A.mfix[1 + 2 * A.ntAll + A.t0 + t];
                     const float ext = Pc * (1.f - A.tdec) + ref * A.tdec;
                     TI -= wfob * ext * dtv;

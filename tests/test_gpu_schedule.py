@@ -1,7 +1,7 @@
 """Launch schedules of the batched form and the autotuner.
 
 The schedules (one CTA per tile, or a persistent grid over the tiles holding
-water with the deepest first; 4 or 2 tracers per launch) run the same tile walk
+water with the deepest first; 10, 8, 4 or 2 tracers per launch) run the same tile walk
 and must give the same result bit for bit; the autotuner must leave the tracers
 as they were and report what it chose.
 """
@@ -35,14 +35,15 @@ def _run(d, tr, sched, split, steps=6, graph=True):
     return got, info
 
 
-@pytest.mark.parametrize("nt", [1, 3, 5, 9])
+@pytest.mark.parametrize("nt", [1, 3, 5, 9, 12])
 def test_schedules_agree(gpu, nt):
     d = synth.generate(synth.GenSpec(**ZLEVEL))
     tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(nt)]
     ref, info = _run(d, tr, 0, 4)
-    groups4 = {1: 1, 3: 2, 5: 2, 9: 3}[nt]                 # 4-tracer groups, then 2, then 1
+    groups4 = {1: 1, 3: 2, 5: 2, 9: 3, 12: 3}[nt]          # 4-tracer groups, then 2, then 1
     assert info == {"launches": groups4, "sched": 0, "split": 4, "per_call": 1}
-    cands = [(1, 4), (0, 2), (1, 2)] + ([(0, 8), (1, 8)] if nt >= 8 else [])
+    cands = [(1, 4), (0, 2), (1, 2)] + ([(0, 8), (1, 8)] if nt >= 8 else []) + \
+        ([(0, 10), (1, 10)] if nt >= 10 else [])
     for sched, split in cands:
         got, info = _run(d, tr, sched, split)
         assert info["sched"] == sched and info["split"] == split
