@@ -73,7 +73,7 @@ class Batch:
                 "mohid_ad_batched_autotune")
 
     def set_schedule(self, sched: int, split: int = 4):
-        """Fix the launch schedule by hand (0 one CTA per tile, 1 tile list; 4 or 2 tracers per launch)."""
+        """Fix the launch schedule by hand (0 one CTA per tile, 1 tile list; 10, 8, 4 or 2 tracers per launch)."""
         st = C.c_int(0)
         N.check(self.lib.mohid_ad_batched_set_schedule(C.byref(self._bid), C.byref(C.c_int(sched)),
                                                        C.byref(C.c_int(split)), C.byref(st)),

@@ -106,6 +106,7 @@ struct BatchArgs {
     // scalars
     float DT, schmidtH, coefV, backV, tdec;
     int nullDif, vertical1D, xzflow;
+    int bc;                             // BoundaryCondition (with Ref): 1, 2, 5, 7 or 4
     int t0;                             // first tracer of this launch (TMA coordinate)
     unsigned* status;
 };
@@ -231,13 +232,21 @@ cudaError_t pack_ref(const double* src, const int* WP, const int* cols, int ncol
 cudaError_t unshift_ref(float* R, const int* WP, const int* cols, int ncols, int ni, int nj, int nk, double shift,
                         cudaStream_t s);
 cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int* idx, cudaStream_t s);
+// ImposeNullGradient (AD:1926-1987) on nt batched FP32 tracers (stride ts):
+// at each layer the boundary columns `cols` (Size-box 2-D offsets, the
+// reference's order) take in turn the mean of their neighbours across compute
+// faces; KFloor over the Size box
+cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* fflag, const int* cols, int ncols,
+                                  const int* KFloor, const BLayout& L, cudaStream_t s);
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,
                        double* out, cudaStream_t s);
 // *out = max(0, max over open non-boundary water cells of |R| - tol * max |term|),
 // R the cell's water budget, and on the top cell of open boundary columns R =
-// the surface flux (the step maps constants onto themselves when *out == 0)
+// the surface flux (the step maps constants onto themselves when *out == 0).
+// BP2D null: no open-boundary treatment, boundary columns are checked like
+// the others (pack_state likewise)
 cudaError_t continuity_residual(const double* Qx, const double* Qy, const double* Qz, const double* V,
                                 const double* Vold, const int* OP, const int* CFU, const int* CFV,
                                 const int* CFW, const int* BP2D, double DT, double tol, const BLayout& L,

@@ -54,6 +54,7 @@ struct Batch {
     DevBuf<double> Vprev;                // VolumeZ of the last pack (Fortran layout)
     DevBuf<unsigned> moving;
     bool massFix = true;                 // requested (mohid_ad_batched_set_mass_fix)
+    bool bcFix = true;                   // the step's boundary condition lets the fixer run (bc_fixable)
     bool staticVol = false;              // the packed hydrodynamics have VolumeZ == VolumeZOld
     bool packedOnce = false;
     unsigned packedMask = 0;             // mask version of the last completed pack
@@ -97,6 +98,9 @@ struct Batch {
     std::vector<unsigned> targetVersion; // hydro version each tracer's mass target was taken at
     double preCont = -1.0, preContDT = -1.0;
     unsigned preContVersion = ~0u;
+    // the repack's check treated the boundary columns as open boundaries
+    // (the batch had references) -- of the last completed pack, of the one in flight
+    bool preContRef = false, packingRef = false;
     std::vector<double> shift;           // per tracer: water cells hold P - shift
     std::vector<double> refShift;        // shift each stored reference was packed with
     // anomaly storage is exact only when the step preserves constants; this
@@ -198,7 +202,7 @@ bool encode_map(CUtensorMap* m, CUtensorMapDataType dt, int elt, const void* bas
     return r == CUDA_SUCCESS;
 }
 
-int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why)
+int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why, bool ensemble = false)
 {
     if (!p) { why = "params is NULL"; return MOHID_AD_ERR_NULLPTR; }
     if (!(p->DTProp > 0.0) || !std::isfinite(p->DTProp)) { why = "DTProp must be > 0"; return MOHID_AD_ERR_OPTION; }
@@ -215,12 +219,21 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->Docycle_method != 1) { why = "batched form follows Docycle_method 1"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
-    if (hasRef && p->BoundaryCondition != MOHID_BC_MASS_CONSERVATION) {
-        why = "batched form: only MassConservation open boundaries"; return MOHID_AD_ERR_UNSUPPORTED;
-    }
-    // applied after the solve even without a reference (AD:1874-1880)
-    if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT || p->BoundaryCondition == MOHID_BC_CYCLIC) {
-        why = "batched form: NullGradient / Cyclic boundaries (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
+    const int bc = p->BoundaryCondition;
+    if (hasRef) {
+        if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
+            why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
+        }
+        if (bc == MOHID_BC_ORLANSKI || bc == MOHID_BC_CYCLIC) {
+            why = "batched form: Orlanski and Cyclic boundaries (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
+        }
+        if (ensemble && bc != MOHID_BC_MASS_CONSERVATION) {
+            why = "ensembles: closed or MassConservation open boundaries"; return MOHID_AD_ERR_UNSUPPORTED;
+        }
+    } else if (bc == MOHID_BC_CYCLIC) {
+        why = "cyclic boundaries read ReferenceProp (reference Prop_CyclicBoundary)"; return MOHID_AD_ERR_OPTION;
+    } else if (ensemble && bc == MOHID_BC_NULL_GRADIENT) {
+        why = "ensembles: NullGradient boundaries (use a batch per domain)"; return MOHID_AD_ERR_UNSUPPORTED;
     }
     return MOHID_AD_SUCCESS;
 }
@@ -233,7 +246,16 @@ constexpr double kContinuityTol = 1e-9;
 // targets follow the boundary flux of every step
 bool fix_active(const Batch* b)
 {
-    return b->massFix && b->shiftOk && b->staticVol;
+    return b->massFix && b->shiftOk && b->staticVol && b->bcFix;
+}
+
+// the step's budget closes through the boundary flux the fixer follows:
+// closed domains (NullGradient excepted, whose sweep after the solve sets
+// the boundary cells) and MassConservation open boundaries
+bool bc_fixable(const Batch* b, const mohid_ad_params* p)
+{
+    const int bc = p->BoundaryCondition;
+    return b->hasRef ? bc == MOHID_BC_MASS_CONSERVATION : bc != MOHID_BC_NULL_GRADIENT;
 }
 
 // which of the fixer's launches a step makes (fixer, boundary flux, target drop)
@@ -287,10 +309,10 @@ int pack_enqueue(Batch* b, int* stat)
     // the last step); the per-column data and the tile schedule only when the
     // masks changed
     const bool masks = !b->packedOnce || b->packedMask != in->maskVersion;
-    const double cdt = (b->checkedDT > 0.0 && b->checkedFlags == 0) ? b->checkedDT : 0.0;
+    const double cdt = (b->checkedDT > 0.0 && (b->checkedFlags & 3) == 0) ? b->checkedDT : 0.0;
     CK(mohid::pack_state(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->ViscH.p, in->DiffV.p,
                          in->AreaU.p, in->AreaV.p, in->DZZ.p, in->WP.p, in->OP.p, in->LP.p, in->CFU.p,
-                         in->CFV.p, in->CFW.p, in->BP2D.p, masks,
+                         in->CFV.p, in->CFW.p, b->hasRef ? in->BP2D.p : nullptr, masks,
                          hq ? (void*)b->Qx16.p : (void*)b->Qx32.p, hq ? (void*)b->Qy16.p : (void*)b->Qy32.p,
                          hq ? (void*)b->Qz16.p : (void*)b->Qz32.p, hk ? (void*)b->Vis16.p : (void*)b->Vis32.p,
                          hk ? (void*)b->Dif16.p : (void*)b->Dif32.p, hq, hk, (hq || hk) ? b->dinv.p : nullptr,
@@ -309,6 +331,7 @@ int pack_enqueue(Batch* b, int* stat)
     }
     b->packingMasks = masks;
     b->packingMask = in->maskVersion;
+    b->packingRef = b->hasRef;
     CK(cudaMemcpyAsync(&b->hp->moving, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(&b->hp->vchanged, b->vchanged.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     b->hp->cont = -1.0;
@@ -388,6 +411,7 @@ int pack_finalize(Batch* b, int* stat)
         b->preCont = h.cont;
         b->preContDT = h.contDT;
         b->preContVersion = b->packingVersion;
+        b->preContRef = b->packingRef;
         b->packed = true;
         b->packedVersion = b->packingVersion;
         return ok(stat);
@@ -404,6 +428,7 @@ int pack_finalize(Batch* b, int* stat)
     b->preCont = h.cont;
     b->preContDT = h.contDT;
     b->preContVersion = b->packingVersion;
+    b->preContRef = b->packingRef;
     b->packed = true;
     b->packedVersion = b->packingVersion;
     return ok(stat);
@@ -475,6 +500,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.vertical1D = p->Vertical1D != 0;
     a.xzflow = p->XZFlow != 0;
     a.status = in->status.p;
+    a.bc = p->BoundaryCondition;
     return a;
 }
 
@@ -484,15 +510,18 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
 {
     Instance* in = b->in;
     cudaStream_t s = in->stream;
-    const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0);
+    // without references the boundary columns get ordinary rows, whose budget
+    // must close like any other cell's: the check then covers them in full
+    const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0) | (b->hasRef ? 4 : 0);
     if (b->checkedVersion != in->hydroVersion || b->checkedDT != p->DTProp || b->checkedFlags != flags) {
-        bool okc = flags == 0;
-        if (okc && b->preContVersion == in->hydroVersion && b->preContDT == p->DTProp && b->preCont >= 0.0) {
+        bool okc = (flags & 3) == 0;
+        if (okc && b->preContVersion == in->hydroVersion && b->preContDT == p->DTProp && b->preCont >= 0.0 &&
+            b->preContRef == b->hasRef) {
             okc = b->preCont <= 0.0;             // computed with the repack
         } else if (okc) {
             CK(mohid::continuity_residual(in->Qx.p, in->Qy.p, in->Qz.p, in->V.p, in->Vold.p, in->OP.p,
-                                          in->CFU.p, in->CFV.p, in->CFW.p, in->BP2D.p, p->DTProp, kContinuityTol,
-                                          b->L, b->scratch.p, s));
+                                          in->CFU.p, in->CFV.p, in->CFW.p, b->hasRef ? in->BP2D.p : nullptr,
+                                          p->DTProp, kContinuityTol, b->L, b->scratch.p, s));
             CK(cudaMemcpyAsync(b->hmass, b->scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             okc = *b->hmass <= 0.0;
@@ -573,6 +602,13 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
                                               b->storage >= 2, tiles, b->ntl, s);
         if (e != cudaSuccess) return e;
         t0 += g;
+    }
+    // ImposeNullGradient after the solve, whether or not a reference is given (AD:1874-1880)
+    if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT) {
+        Instance* in = b->in;
+        cudaError_t e = mohid::null_gradient_batched(Pout, b->L.n3, b->nt, b->fflag.p, in->bcols.p, in->nbcols,
+                                                     in->KFloor.p, b->L, s);
+        if (e != cudaSuccess) return e;
     }
     if (!real) return cudaSuccess;
     if (fix_active(b) && (sums || b->hasRef)) {
@@ -931,6 +967,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     int code = check_batched_params(p, b->hasRef, why);
     if (code) return fail(code, stat, why);
     if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
+    b->bcFix = bc_fixable(b, p);
     if (b->hasRef)
         for (int t = 0; t < b->nt; ++t)
             if (t >= (int)b->refShift.size() || b->refShift[t] != b->shift[t])
@@ -1207,8 +1244,9 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
     for (size_t q = 0; q < n; ++q) {
         Batch* b = E->m[q];
         std::string why;
-        int code = check_batched_params(&p[q], b->hasRef, why);
+        int code = check_batched_params(&p[q], b->hasRef, why, true);
         if (code) return fail(code, stat, "member " + std::to_string(q) + ": " + why);
+        b->bcFix = bc_fixable(b, &p[q]);
         if (p[q].AdvMethodH != method || (method != MOHID_UPWIND_ORDER1 && p[q].TVDLimitationH != limiter))
             return fail(MOHID_AD_ERR_OPTION, stat, "members must share AdvMethodH and TVDLimitationH");
         if (b->hasRef)

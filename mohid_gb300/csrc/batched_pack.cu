@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut o
                 cfn = out.flag[g + 1] & F_CFV;
                 cft = out.flag[g + L.sl] & F_CFW;
             }
-            const bool bp = f.BP2D[i + (long long)NI * j] == 1;
+            const bool bp = f.BP2D && f.BP2D[i + (long long)NI * j] == 1;
             if (bp && k != nk) return;
             const double qw = (fl & F_CFU) ? in.Qx[e] : 0.0, qe = cfe ? in.Qx[e + NI] : 0.0;
             const double qs = (fl & F_CFV) ? in.Qy[e] : 0.0, qn = cfn ? in.Qy[e + 1] : 0.0;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kRowThreads) k_continuity(const double* Qx, co
         // shifted with them) when its exterior-face balance WFOB takes up the
         // rest, except for the surface face, which the step applies at the
         // top cell but WFOB leaves out: that flux must vanish there
-        const bool bp = BP2D[i + (long long)NI * j] == 1;
+        const bool bp = BP2D && BP2D[i + (long long)NI * j] == 1;
         if (bp && k != nk) return;
         // the faces the step applies: compute faces, those on the j = JUB+1 /
         // i = IUB+1 planes excepted
@@ -423,6 +423,32 @@ __global__ void k_ref_index(const int* __restrict__ cols, int ncols, int sj, BLa
     if (q >= ncols) return;
     const int c = cols[q];
     idx[L.at2(c % sj, c / sj)] = q;
+}
+
+// ImposeNullGradient on the batched tracers: thread (k, t) walks the boundary
+// columns in the reference's order at layer k (k = 0..KUB from |KFloorZ|), so
+// a cell sees the new values of the boundary cells swept before it.  The
+// neighbours across compute faces are water cells, stored relative to the
+// same constant as the boundary cell, so their mean is taken as stored.
+__global__ void k_null_gradient_b(float* P, long long ts, int nt, const uint8_t* __restrict__ fflag,
+                                  const int* __restrict__ cols, int ncols, const int* __restrict__ KFloor, BLayout L)
+{
+    const int nk1 = L.nk + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nk1 * nt) return;
+    const int k = e % nk1, t = e / nk1, sj = L.ni + 2;
+    float* Pt = P + (long long)t * ts;
+    for (int q = 0; q < ncols; ++q) {
+        const int c = cols[q];
+        const int kf = KFloor[c];
+        if (k < (kf < 0 ? -kf : kf)) continue;
+        const long long a = L.at(c % sj, c / sj, k);
+        const float cv1 = (fflag[a + 1] & FV_ACT) ? 1.f : 0.f, cv0 = (fflag[a] & FV_ACT) ? 1.f : 0.f;
+        const float cu1 = (fflag[a + L.px] & FU_ACT) ? 1.f : 0.f, cu0 = (fflag[a] & FU_ACT) ? 1.f : 0.f;
+        const float aux = cv1 + cv0 + cu1 + cu0;
+        if (aux <= 0.f) continue;
+        Pt[a] = (Pt[a + 1] * cv1 + Pt[a - 1] * cv0 + Pt[a + L.px] * cu1 + Pt[a - L.px] * cu0) / aux;
+    }
 }
 
 // add the stored constant back: anomaly -> absolute values (water cells)
@@ -856,6 +882,14 @@ cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int*
     cudaError_t e = cudaMemsetAsync(idx, 0xff, sizeof(int) * (size_t)L.n2, s);
     if (e != cudaSuccess || ncols <= 0) return e;
     k_ref_index<<<(ncols + 255) / 256, 256, 0, s>>>(cols, ncols, ni + 2, L, idx);
+    return cudaGetLastError();
+}
+cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* fflag, const int* cols, int ncols,
+                                  const int* KFloor, const BLayout& L, cudaStream_t s)
+{
+    if (ncols <= 0 || nt <= 0) return cudaSuccess;
+    const int n = (L.nk + 1) * nt;
+    k_null_gradient_b<<<(n + 63) / 64, 64, 0, s>>>(P, ts, nt, fflag, cols, ncols, KFloor, L);
     return cudaGetLastError();
 }
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s)

@@ -616,20 +616,34 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                     Fc += fminf(qzp, 0.f) * dtv;
                 }
             }
-            // open boundary (MassConservation): net flux through the exterior faces
+            // open boundary cells (OpenBoundaryCondition AD:5369-5742).
+            // MassConservation (1) and MassConservNullGrad (7): the net flux
+            // through the exterior faces, outflow implicit in E; inflow carries
+            // the exterior value in (1) or takes the neighbours' mean across
+            // compute faces as an identity row (7).  ImposedValue (2), SubModel
+            // (5) and NullGradient (4, set after the solve): identity rows with
+            // the exterior value, or the old value.
             float wfob = 0.f;
             const bool obc = obcCol && open;
+            bool ident = false;
+            const uint8_t* ffl = st + SL::oF + fO;
             if (obc) {
-                const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
-                const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
-                const uint8_t* ffl = st + SL::oF + fO;
-                wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[own], A.qsx) : 0.f,
-                                (ffl[FBX] & FU_ACT) ? tofl<QT>(qx[own + TX], A.qsx) : 0.f,
-                                (ffl[0] & FV_ACT) ? tofl<QT>(qy[qyO], A.qsy) : 0.f,
-                                (ffl[1] & FV_ACT) ? tofl<QT>(qy[qyO + 1], A.qsy) : 0.f,
-                                (fl & F_CFW) ? qz : 0.f, (flp & F_CFW) ? qzp : 0.f, dvr, rVk, DT);
-                if (wfob >= 0.f) E += wfob * dtv;
+                if (A.bc == 1 || A.bc == 7) {
+                    const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
+                    const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
+                    wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[own], A.qsx) : 0.f,
+                                    (ffl[FBX] & FU_ACT) ? tofl<QT>(qx[own + TX], A.qsx) : 0.f,
+                                    (ffl[0] & FV_ACT) ? tofl<QT>(qy[qyO], A.qsy) : 0.f,
+                                    (ffl[1] & FV_ACT) ? tofl<QT>(qy[qyO + 1], A.qsy) : 0.f,
+                                    (fl & F_CFW) ? qz : 0.f, (flp & F_CFW) ? qzp : 0.f, dvr, rVk, DT);
+                    if (wfob >= 0.f) E += wfob * dtv;
+                    else ident = A.bc == 7;
+                } else {
+                    ident = true;
+                }
+                if (ident) { D = 0.f; E = 1.f; Fc = 0.f; }
             }
+
             // THOMASZ factorisation of row k
             const float aux = fmaf(D, Wp, E);
             float inv = rcp_approx(aux);
@@ -645,7 +659,36 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                 if (horiz)
                     TI = fmaf(dtv, (FX[t * NWF + own] - FX[t * NWF + own + TX]) +
                                    (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
-                if (obc && wfob < 0.f) {
+                if (OBC && ident) {
+                    const float* Pt = P + t * (TY + 4) * PBX + pbO;   // the neighbours: i +- 1, j +- PBX
+                    if (A.bc == 2 || A.bc == 5) {
+                        // the interior mean over the neighbours that are open
+                        // and not boundary points (AD:5458-5485)
+                        const long long a = cb + (long long)k * L.sl;
+                        const float w0 = ((A.flag[a + 1] & F_OP) && !(A.cflag[c2 + 1] & C_BP)) ? 1.f : 0.f;
+                        const float w1 = ((A.flag[a - 1] & F_OP) && !(A.cflag[c2 - 1] & C_BP)) ? 1.f : 0.f;
+                        const float w2 = ((A.flag[a + L.px] & F_OP) && !(A.cflag[c2 + L.px] & C_BP)) ? 1.f : 0.f;
+                        const float w3 = ((A.flag[a - L.px] & F_OP) && !(A.cflag[c2 - L.px] & C_BP)) ? 1.f : 0.f;
+                        const float ws = w0 + w1 + w2 + w3;
+                        const float ref = refc[(long long)t * A.rts + k] -
+                                          (float)A.mfix[1 + 2 * A.ntAll + A.t0 + t];
+                        if (ws > 0.f) {
+                            const float in = (Pt[1] * w0 + Pt[-1] * w1 + Pt[PBX] * w2 + Pt[-PBX] * w3) / ws;
+                            TI = in * (1.f - A.tdec) + ref * A.tdec;
+                        } else {
+                            TI = ref;
+                        }
+                    } else if (A.bc == 7) {
+                        // the mean across the compute faces north, south,
+                        // east and west (NullGradProp AD:2071-2110)
+                        const float c0 = (ffl[1] & FV_ACT) ? 1.f : 0.f, c1 = (ffl[0] & FV_ACT) ? 1.f : 0.f;
+                        const float c2f = (ffl[FBX] & FU_ACT) ? 1.f : 0.f, c3 = (ffl[0] & FU_ACT) ? 1.f : 0.f;
+                        const float cs = c0 + c1 + c2f + c3;
+                        TI = cs > 0.f ? (Pt[1] * c0 + Pt[-1] * c1 + Pt[PBX] * c2f + Pt[-PBX] * c3) / cs : Pc;
+                    } else {
+                        TI = Pc;                         // NullGradient: set after the solve
+                    }
+                } else if (obc && wfob < 0.f) {
                     // the reference is stored relative to the tracer's loaded
                     // constant; the fixer's correction moves it with the field
                     const float ref = refc[(long long)t * A.rts + k] -

@@ -24,6 +24,9 @@ def main():
     ap.add_argument("--nj", type=int, default=0)
     ap.add_argument("--tracers", type=int, default=0)
     ap.add_argument("--no-mass-fix", action="store_true", help="batched form without the mass fixer")
+    ap.add_argument("--sched", type=int, default=-1,
+                    help="batched schedule (0 one CTA per tile, 1 tile list) instead of the autotuner's choice")
+    ap.add_argument("--split", type=int, default=4, help="largest tracer group per launch with --sched")
     args = ap.parse_args()
     build.build()
     import torch
@@ -40,6 +43,8 @@ def main():
     if args.form == "batched":
         b = batched.Batch(ad, len(tr), args.storage)
         b.set_mass_fix(not args.no_mass_fix)
+        if args.sched >= 0:
+            b.set_schedule(args.sched, args.split)   # no autotuner launches before the profiled ones
         for t, P in enumerate(tr):
             b.set_tracer(t, P)
             if refs:

@@ -86,6 +86,64 @@ def test_batched_open_boundaries(gpu, grid, opt, decay):
         assert rel_l2(d, g, w) <= TOL
 
 
+@pytest.mark.parametrize("grid", ["open", "nsopen", "allopen"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee"])
+@pytest.mark.parametrize("bc,decay", [(2, 0.0), (2, 300.0), (5, 0.0), (7, 0.0), (4, 0.0)])
+def test_batched_other_open_boundaries(gpu, grid, opt, bc, decay):
+    # ImposedValue, SubModel (identity rows with the interior mean decayed
+    # towards the reference), MassConservNullGrad (inflow rows take the
+    # neighbours' mean) and NullGradient (the sweep after the solve), one step
+    # and five steps against the oracle
+    if grid == "allopen":
+        d = synth.generate(synth.GenSpec(ni=40, nj=33, nk=6, land_frac=0.1, land_kind=1, seed=11, open_sides=15,
+                                         bathy_kind=1, dt=30.0))
+    else:
+        d = domain(grid)
+    tr = [d.tracer(3, 1.0, 0.5, seed=1), d.tracer(1, 5.0, 20.0, seed=4)]
+    refs = [d.reference(2.0, 0.3, seed=2), d.reference(12.0, 0.2, seed=3)]
+    pd = dict(DTProp=30.0, BoundaryCondition=bc, DecayTime=decay, **BATCH_OPTIONS[opt])
+    for steps, tol in ((1, 1e-6), (5, TOL)):
+        want, got = run_pair(d, tr, pd, steps, refs=refs)
+        for w, g in zip(want, got):
+            assert rel_l2(d, g, w) <= tol
+
+
+@pytest.mark.parametrize("grid", ["nsopen", "allopen"])
+def test_batched_null_gradient_without_reference(gpu, grid):
+    # ImposeNullGradient runs after the solve whether or not a reference is given (AD:1874-1880)
+    if grid == "allopen":
+        d = synth.generate(synth.GenSpec(ni=40, nj=33, nk=6, land_frac=0.1, land_kind=1, seed=11, open_sides=15,
+                                         bathy_kind=1, dt=30.0))
+    else:
+        d = domain(grid)
+    tr = [d.tracer(3, 1.0, 0.5, seed=1), d.tracer(1, 5.0, 20.0, seed=4)]
+    pd = dict(DTProp=30.0, BoundaryCondition=4, **BATCH_OPTIONS["tvd_superbee"])
+    want, got = run_pair(d, tr, pd, 5)
+    for w, g in zip(want, got):
+        assert rel_l2(d, g, w) <= TOL
+
+
+def test_batched_rejects_boundary_conditions_like_the_plain_form(gpu):
+    # Orlanski and Cyclic stay with the plain form (MOHID_AD_ERR_UNSUPPORTED);
+    # codes the reference rejects give MOHID_AD_ERR_OPTION as there
+    d = domain("open")
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, d.tracer(3, 1.0, 0.5, seed=1))
+    for bc, code in ((8, 3),):                       # cyclic without a reference
+        with pytest.raises(advdiff.N.MohidAdError) as ei:
+            b.step(advdiff.params(DTProp=30.0, BoundaryCondition=bc))
+        assert ei.value.code == code
+    b.set_reference(0, d.reference(2.0, 0.3, seed=2))
+    for bc, code in ((6, 4), (8, 4), (3, 3)):
+        with pytest.raises(advdiff.N.MohidAdError) as ei:
+            b.step(advdiff.params(DTProp=30.0, BoundaryCondition=bc))
+        assert ei.value.code == code
+    b.destroy()
+    ad.kill()
+
+
 def test_batched_cfg1_100_steps(gpu):
     w = configs.cfg1()
     d = synth.generate(w.spec)
@@ -143,8 +201,7 @@ def test_batched_mass_budget_matches_oracle_sum(gpu):
 
 
 @pytest.mark.parametrize("bad", [dict(AdvMethodH=5), dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1),
-                                 dict(ImpExp_DifV=0.5), dict(Docycle_method=2), dict(ImpExp_AdvV=0.0),
-                                 dict(BoundaryCondition=4), dict(BoundaryCondition=8)])
+                                 dict(ImpExp_DifV=0.5), dict(Docycle_method=2), dict(ImpExp_AdvV=0.0)])
 def test_batched_rejects_unsupported(gpu, bad):
     d = domain("coast")
     ad = advdiff.AdvectionDiffusion(d)
