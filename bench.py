@@ -695,7 +695,8 @@ def main():
                          f"the packed fields and tracers > 129 MiB)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (committed ncu capture)",
                      "kernel": r["kernel"], "bytes_per_launch": r["bytes_per_launch"],
                      "bytes_per_update": r["bytes_per_update"],
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
@@ -723,9 +724,12 @@ def main():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# dominant kernel, from one ncu capture of the workload (profiles/).
+# dominant kernel, from one ncu capture of the workload's step launch (the
+# one-CTA-per-tile schedule the autotuner picks, no mass-fixer sums): not
+# measured by this run; the capture and its command are in
+# profiles/batched_kernel_512x512x40_2tracers.md.
 TRAFFIC: dict = {
-    ("cfg2", "batched_kernel<2>"): 628.752640e6 + 123.641856e6,
+    ("cfg2", "batched_kernel<2>"): 623.725568e6 + 112.851968e6,
 }
 
 if __name__ == "__main__":
