@@ -513,7 +513,7 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
         hsteps = max(3, min(steps, 20))
 
         def hydro_step():
-            ad0.set_fields(dev, device=True)
+            ad0.set_fields(dev, bind=True)         # borrowed in place, a new state each call
             stepper(1, False)
         hydro_step()
         hydro_step()
@@ -527,8 +527,10 @@ def run_batched(cases, storage, steps, warmup, world, e2e=True):
         hms = (time.perf_counter() - t0) / hsteps * 1e3
         hydro = {"ms_per_step": hms, "step_ms": ms, "update_ms": hms - ms, "steps": hsteps,
                  "value": cases[0].cells * cases[0].nt / (hms / 1e3),
-                 "definition": "every step: mohid_ad_set_hydro_dev of the 11 FP64 fields from device "
-                               "memory (masks kept), the batched repack and one step; wall clock"}
+                 "definition": "every step: mohid_ad_bind_hydro_dev of the 11 FP64 fields in device "
+                               "memory (borrowed in place, masks kept), the batched repack and one "
+                               "step; wall clock"}
+        ad0.set_fields(dev, device=True)           # back to the instance's own copies
         del dev
 
     e2e_s = h2d = d2h = None

@@ -297,6 +297,28 @@ int mohid_ad_set_hydro_dev(const int* id,
                            const int* ComputeFacesW3D,
                            const int* SmallDepths, int* stat);
 
+/* The eleven FP64 fields as borrowed device arrays, as AdvectionDiffusion
+ * binds its array arguments by pointer (ModuleAdvectionDiffusion.F90:1271-1292):
+ * the instance reads them in place, with no copy, until the next
+ * mohid_ad_set_hydro* or mohid_ad_bind_hydro_dev call gives that field
+ * again, and the device producers (mohid_ad_geometry_dev,
+ * mohid_ad_vertical_flux) write their results into them.  They must stay
+ * valid and must not change while a step that reads them runs; after
+ * changing their contents call this again (with the same pointers), which
+ * marks the hydrodynamic state as new.  NULL and mask rules as
+ * mohid_ad_set_hydro_dev; the masks are copied. */
+int mohid_ad_bind_hydro_dev(const int* id,
+                            const double* Wflux_X, const double* Wflux_Y, const double* Wflux_Z,
+                            const double* VolumeZOld, const double* VolumeZ,
+                            const double* Visc_H, const double* Diff_V,
+                            const double* AreaU, const double* AreaV,
+                            const double* DZZ, const double* DWZ,
+                            const int* OpenPoints3D, const int* LandPoints3D,
+                            const int* WaterPoints3D,
+                            const int* ComputeFacesU3D, const int* ComputeFacesV3D,
+                            const int* ComputeFacesW3D,
+                            const int* SmallDepths, int* stat);
+
 /* Copy the instance's current FP64 hydrodynamic fields (those of the last
  * mohid_ad_set_hydro*, as changed since by the device producers) to the
  * caller's Size-box arrays; any pointer may be NULL (not copied).  Host

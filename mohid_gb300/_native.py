@@ -77,6 +77,7 @@ _AD_SIGS = {
                       [c_double_p] * 4 + [c_int_p, c_int_p, c_int_p]),
     "mohid_ad_set_hydro": (C.c_int, [c_int_p] + [c_double_p] * 11 + [c_int_p] * 7 + [c_int_p]),
     "mohid_ad_set_hydro_dev": (C.c_int, [c_int_p] + [c_double_p] * 11 + [c_int_p] * 7 + [c_int_p]),
+    "mohid_ad_bind_hydro_dev": (C.c_int, [c_int_p] + [c_double_p] * 11 + [c_int_p] * 7 + [c_int_p]),
     "mohid_ad_step_prop_f64": (C.c_int, [c_int_p, c_double_p, c_double_p,
                                          C.POINTER(MohidAdParams), c_int_p]),
     "mohid_ad_step_prop_f64_dev": (C.c_int, [c_int_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -77,18 +77,22 @@ class AdvectionDiffusion:
             C.byref(st))
         N.check(rc, "mohid_ad_set_hydro_dev")
 
-    def set_fields(self, fields: dict, device: bool = False):
+    def set_fields(self, fields: dict, device: bool = False, bind: bool = False):
         """Update some FP64 hydrodynamic fields and keep the rest and the masks
         (mohid_ad_set_hydro[_dev] with NULL for what is kept).  `fields` maps F3
-        names to float64 Size-box numpy arrays, or torch CUDA tensors when device."""
-        if device:
+        names to float64 Size-box numpy arrays, or torch CUDA tensors when device.
+        bind (device tensors): borrow them in place instead of copying
+        (mohid_ad_bind_hydro_dev); the tensors must outlive their use."""
+        if device or bind:
             args = [C.cast(C.c_void_p(fields[n].data_ptr()), N.c_double_p) if n in fields else None for n in F3]
         else:
             args = [N.ptr(fields[n]) if n in fields else None for n in F3]
         st = C.c_int(0)
-        fn = "mohid_ad_set_hydro_dev" if device else "mohid_ad_set_hydro"
+        fn = "mohid_ad_bind_hydro_dev" if bind else ("mohid_ad_set_hydro_dev" if device else "mohid_ad_set_hydro")
         rc = getattr(self.lib, fn)(C.byref(self._id), *args, *([None] * len(I3)), None, C.byref(st))
         N.check(rc, fn)
+        if bind:
+            self._bound = dict(getattr(self, "_bound", {}), **fields)   # keep the borrowed tensors alive
 
     def get_fields(self, names=F3) -> dict:
         """The instance's current FP64 hydrodynamic fields (mohid_ad_get_hydro) as numpy arrays."""

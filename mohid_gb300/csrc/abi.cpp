@@ -304,7 +304,9 @@ mohid::PlainArgs make_args(Instance* in, const double* Pin, double* Pout, const 
     return a;
 }
 
-int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const double* Wflux_Y,
+// fromDevice: device arrays; bind: the FP64 device arrays are borrowed in
+// place (read, and written by the device producers) instead of copied
+int upload_hydro(Instance* in, bool fromDevice, bool bind, const double* Wflux_X, const double* Wflux_Y,
                  const double* Wflux_Z, const double* VolumeZOld, const double* VolumeZ,
                  const double* Visc_H, const double* Diff_V, const double* AreaU,
                  const double* AreaV, const double* DZZ, const double* DWZ, const int* OpenPoints3D,
@@ -331,8 +333,15 @@ int upload_hydro(Instance* in, bool fromDevice, const double* Wflux_X, const dou
     const size_t bd = sizeof(double) * in->n3, bi = sizeof(int) * in->n3;
     DevBuf<double>* dd[] = {&in->Qx, &in->Qy, &in->Qz, &in->Vold, &in->V, &in->ViscH, &in->DiffV,
                             &in->AreaU, &in->AreaV, &in->DZZ, &in->DWZ};
-    for (int q = 0; q < 11; ++q)
-        if (ds[q]) CK(cudaMemcpyAsync(dd[q]->p, ds[q], bd, kind, in->stream));
+    for (int q = 0; q < 11; ++q) {
+        if (!ds[q]) continue;
+        if (bind) {
+            dd[q]->borrow(const_cast<double*>(ds[q]));
+        } else {
+            dd[q]->unborrow();
+            CK(cudaMemcpyAsync(dd[q]->p, ds[q], bd, kind, in->stream));
+        }
+    }
     ++in->hydroVersion;
     if (nmask == 0) {
         // the masks stay; host buffers are consumed before returning
@@ -476,7 +485,7 @@ int mohid_ad_set_hydro(const int* id, const double* Wflux_X, const double* Wflux
     TraceRange trace_("mohid_ad_set_hydro");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
-    return upload_hydro(in, false, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
+    return upload_hydro(in, false, false, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
                         AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
                         ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
 }
@@ -493,7 +502,24 @@ int mohid_ad_set_hydro_dev(const int* id, const double* Wflux_X, const double* W
     TraceRange trace_("mohid_ad_set_hydro_dev");
     Instance* in = lookup(id);
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
-    return upload_hydro(in, true, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
+    return upload_hydro(in, true, false, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
+                        AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
+                        ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
+}
+
+int mohid_ad_bind_hydro_dev(const int* id, const double* Wflux_X, const double* Wflux_Y,
+                            const double* Wflux_Z, const double* VolumeZOld, const double* VolumeZ,
+                            const double* Visc_H, const double* Diff_V, const double* AreaU,
+                            const double* AreaV, const double* DZZ, const double* DWZ,
+                            const int* OpenPoints3D, const int* LandPoints3D,
+                            const int* WaterPoints3D, const int* ComputeFacesU3D,
+                            const int* ComputeFacesV3D, const int* ComputeFacesW3D,
+                            const int* SmallDepths, int* stat)
+{
+    TraceRange trace_("mohid_ad_bind_hydro_dev");
+    Instance* in = lookup(id);
+    if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
+    return upload_hydro(in, true, true, Wflux_X, Wflux_Y, Wflux_Z, VolumeZOld, VolumeZ, Visc_H, Diff_V,
                         AreaU, AreaV, DZZ, DWZ, OpenPoints3D, LandPoints3D, WaterPoints3D,
                         ComputeFacesU3D, ComputeFacesV3D, ComputeFacesW3D, SmallDepths, stat);
 }

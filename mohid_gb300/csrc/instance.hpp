@@ -23,21 +23,26 @@ extern int g_fail_alloc;
 
 template <class T>
 struct DevBuf {
-    T* p = nullptr;
+    T* p = nullptr;          // the array in use: the own allocation, or a borrowed device array
+    T* own = nullptr;
     size_t n = 0;
     cudaError_t alloc(size_t count)
     {
         n = count;
-        if (g_fail_alloc > 0 && --g_fail_alloc == 0) { p = nullptr; return cudaErrorMemoryAllocation; }
+        if (g_fail_alloc > 0 && --g_fail_alloc == 0) { p = own = nullptr; return cudaErrorMemoryAllocation; }
         cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
+        own = e == cudaSuccess ? p : nullptr;
         if (e == cudaSuccess) e = cudaMemset(p, 0, sizeof(T) * (count ? count : 1));
         return e;
     }
     void release()
     {
-        if (p) cudaFree(p);
-        p = nullptr;
+        if (own) cudaFree(own);
+        p = own = nullptr;
     }
+    // use the caller's device array in place of the own one (never freed here)
+    void borrow(T* x) { p = x; }
+    void unborrow() { p = own; }
 };
 
 struct Instance {

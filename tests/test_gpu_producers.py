@@ -170,3 +170,61 @@ def test_cfg2_cut_producers_match_oracle(gpu):
     for n in ("DWZ", "DZZ", "VolumeZ", "VolumeZOld", "AreaU", "AreaV"):
         assert np.array_equal(got[n], state[n]), n
     assert np.array_equal(got["Wflux_Z"], qz)
+
+
+def test_bound_device_arrays(gpu):
+    """mohid_ad_bind_hydro_dev: the instance reads the caller's device arrays in
+    place (no copy), the producers write into them, a new bind after a change
+    marks a new state for the batched form, and a later copy upload returns
+    the field to the instance's own storage."""
+    import torch
+    d = domain("open")
+    a = d.arrays
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    dev = {n: torch.from_numpy(a[n].copy()).cuda() for n in synth.F3}
+    ad.set_fields(dev, bind=True)
+    pd = dict(DTProp=d.spec.dt, AdvMethodH=4, TVDLimitationH=4, Upwind2H=1)
+    P = d.tracer(3, 2.0, 0.5, seed=3)
+    ref = d.reference(2.0, 0.2, seed=4)
+    Pg, Po = P.copy(), P.copy()
+    ad.step(Pg, advdiff.params(BoundaryCondition=1, **pd), ReferenceProp=ref)
+    assert O.step(d, Po, O.params(BoundaryCondition=1, **pd), ReferenceProp=ref) == 0
+    assert np.array_equal(Pg, Po)
+    # the producers write the bound arrays
+    dxx, dyy = grid_lengths(d)
+    szz = new_level(d, seed=7)
+    ad.geometry(torch.from_numpy(szz).cuda(), torch.from_numpy(dxx).cuda(), torch.from_numpy(dyy).cuda(), 3, True)
+    ad.vertical_flux(d.spec.dt, True)
+    torch.cuda.synchronize()
+    prod = ad.get_fields()
+    for n in ("VolumeZ", "VolumeZOld", "Wflux_Z"):
+        assert np.array_equal(dev[n].cpu().numpy(), prod[n]), n
+    # the caller changes a bound array in place and binds again: the batched
+    # form sees the new state
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, P)
+    b.set_reference(0, ref)
+    b.step(advdiff.params(BoundaryCondition=1, **pd), nsteps=1)
+    dev["Wflux_X"].mul_(0.5)
+    ad.set_fields({"Wflux_X": dev["Wflux_X"]}, bind=True)
+    b.step(advdiff.params(BoundaryCondition=1, **pd), nsteps=1)
+    b.sync()
+    g = b.get_tracer(0)
+    b.destroy()
+    dn1 = synth.Domain(spec=d.spec, arrays=dict(a, **{n: prod[n] for n in synth.F3}))
+    dn2 = synth.Domain(spec=d.spec, arrays=dict(dn1.arrays, Wflux_X=prod["Wflux_X"] * 0.5))
+    Q = P.copy()
+    assert O.step(dn1, Q, O.params(BoundaryCondition=1, **pd), ReferenceProp=ref) == 0
+    assert O.step(dn2, Q, O.params(BoundaryCondition=1, **pd), ReferenceProp=ref) == 0
+    wp = d.water_mask()
+    assert np.linalg.norm(g[wp] - Q[wp]) / np.linalg.norm(Q[wp]) <= 1e-6
+    # a copy upload of one field stops borrowing it; the others stay bound
+    qx = a["Wflux_X"] * 0.25
+    ad.set_fields({"Wflux_X": qx})
+    dev["Wflux_X"].zero_()
+    got = ad.get_fields()
+    assert np.array_equal(got["Wflux_X"], qx)
+    assert np.array_equal(got["VolumeZ"], dev["VolumeZ"].cpu().numpy())
+    ad.kill()
+    del dev
