@@ -159,7 +159,7 @@ std::mutex g_bmu;
 std::map<int, Batch*> g_batch;
 int g_next_bid = 1;
 constexpr int kMassBlocks = 1024;
-constexpr int kPackBlocks = 2048;            // blocks of the per-cell repack pass
+constexpr int kPackBlocks = 8192;            // blocks of the per-cell repack pass
 
 Batch* blookup(const int* bid)
 {

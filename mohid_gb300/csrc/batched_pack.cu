@@ -67,6 +67,68 @@ __device__ __forceinline__ unsigned long long abs_bits(double x)
     return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
+// v - (double)vh rounded to FP32, vh = f64_to_f32(v) (the low part of the
+// volume pair v ~ vh + vlo), with integer instructions: at v's scale
+// 2^(e - 1075) the difference is an integer D of at most 29 bits, converted
+// with one rounding to nearest and scaled by a power of two (exact).  Values
+// whose pair leaves the FP32 normal range take the FP64 path.
+__device__ __forceinline__ float f64_lo_f32(double v, float vh)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned hb = __float_as_uint(vh);
+    const int ef = (int)((hb >> 23) & 0xff);
+    if (e < 949 || e > 1150 || ef == 0 || ef == 255) return f64_to_f32(v - (double)vh);
+    const long long M = (long long)((b & 0xfffffffffffffull) | (1ull << 52));
+    const int c = ef - (e - 896);                  // 1 where rounding carried into the exponent
+    const long long H = (long long)((hb & 0x7fffffu) | 0x800000u) << (29 + c);
+    const long long D = (b >> 63) ? H - M : M - H; // v - vh in units of 2^(e - 1075), |D| <= 2^28
+    return __int2float_rn((int)D) * __int_as_float((e - 1075 + 127) << 23);
+}
+
+// The constant-preservation check of one cell without FP64 arithmetic: the
+// budget R = qw - qe + qs - qn + qb - qt - dv (or R = qt alone, on the top cell
+// of an open boundary column) summed exactly as 64-bit integers at the scale
+// of the largest term (its 53-bit mantissa at bits 5..57, so seven terms
+// cannot overflow; bits below 2^-57 of it are dropped).  Returns |R| - tol *
+// max |term| where that is positive (the cell fails the check), else 0.
+// u (< 2^62) as FP32 from its two 32-bit halves (64-bit conversions would
+// run on the FP64 pipe)
+__device__ __forceinline__ float u64_to_f32(unsigned long long u)
+{
+    return fmaf(__uint2float_rn((unsigned)(u >> 32)), 4294967296.f, __uint2float_rn((unsigned)u));
+}
+
+__device__ __forceinline__ double budget_excess(const double (&x)[7], bool bp, float tol)
+{
+    // the largest exponent (a zero term counts as exponent 1), then each term
+    // at that scale, its fields taken again from its bits
+    int emax = 1;
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+        emax = max(emax, (int)((unsigned long long)__double_as_longlong(x[q]) >> 52) & 0x7ff);
+    if (emax == 0x7ff) return 1.0;                 // Inf or NaN: fails
+    long long S = 0;
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x[q]);
+        const int e = (int)((b >> 52) & 0x7ff);
+        const unsigned long long m = (b & 0xfffffffffffffull) | (e ? (1ull << 52) : 0ull);
+        const int sh = emax - (e ? e : 1);
+        const unsigned long long v = sh > 57 ? 0ull : (m << 5) >> sh;
+        mx = v > mx ? v : mx;
+        // qe, qn, qt and dv enter with a minus sign
+        const bool neg = ((b >> 63) != 0) != (q == 1 || q == 3 || q == 5 || q == 6);
+        if (!bp || q == 5) S += neg ? -(long long)v : (long long)v;
+    }
+    const unsigned long long aS = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
+    const float d = u64_to_f32(aS) - tol * u64_to_f32(mx);
+    if (!(d > 0.f)) return 0.0;
+    // rare: back to absolute units, 2^(emax - 1080)
+    return (double)d * (emax > 57 ? __longlong_as_double((long long)(emax - 57) << 52) : 1e-300);
+}
+
 // Neumaier-compensated accumulation s + c += x
 __device__ __forceinline__ void neu_add(double& s, double& c, double x)
 {
@@ -147,12 +209,12 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_fields(PackIn in, PackOut 
         const float vh = f64_to_f32(v);
         out.Vhi[g] = vh;
         if (same_bits(v, vo)) {
-            out.Vlo[g] = f64_to_f32(v - (double)vh);
+            out.Vlo[g] = f64_lo_f32(v, vh);
             out.RV[g] = vh != 0.f ? __frcp_rn(vh) : 0.f;
             out.DVR[g] = 0.f;
         } else {
             *out.moving = 1u;
-            out.Vlo[g] = f64_to_f32(v - (double)vh);
+            out.Vlo[g] = f64_lo_f32(v, vh);
             const float rv = vh != 0.f ? __frcp_rn(vh) : 0.f;
             out.RV[g] = rv;
             out.DVR[g] = f64_to_f32(v - vo) * rv;
@@ -206,7 +268,7 @@ struct FuseArgs {
 };
 
 template <bool MASKS>
-__global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut out, BLayout L, FuseArgs f)
+__global__ void __launch_bounds__(kRowThreads, 6) k_pack_state(PackIn in, PackOut out, BLayout L, FuseArgs f)
 {
     const int NI = L.ni + 2, NJ = L.nj + 2, nk = L.nk;
     const long long sk = (long long)NI * NJ;
@@ -215,6 +277,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut o
         for (int q = 0; q < 5; ++q) iv[q] = out.inv[q];
     double vs = 0.0, cm = 0.0;
     bool changed = false;
+    const float tolf = (float)f.tol;
     for_rows(L, 0, L.nk + 2, [&](long long e, long long g, int i, int j, int k) {
         put(out.Qx, out.halfQ, iv[0], g, in.Qx[e]);
         put(out.Qy, out.halfQ, iv[1], g, in.Qy[e]);
@@ -228,7 +291,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut o
         const double v = in.V[e], vo = in.Vold[e];
         const float vh = f64_to_f32(v);
         out.Vhi[g] = vh;
-        out.Vlo[g] = f64_to_f32(v - (double)vh);
+        out.Vlo[g] = f64_lo_f32(v, vh);
         const float rv = vh != 0.f ? __frcp_rn(vh) : 0.f;
         out.RV[g] = rv;
         const bool still = same_bits(v, vo);
@@ -289,11 +352,9 @@ __global__ void __launch_bounds__(kRowThreads) k_pack_state(PackIn in, PackOut o
             const double qb = (fl & F_CFW) ? in.Qz[e] : 0.0;
             const double qt = (k < nk) ? (cft ? in.Qz[e + sk] : 0.0) : in.Qz[e + sk];
             const double dv = still ? 0.0 : (v - vo) * f.rDT;
-            unsigned long long m = abs_bits(qw);
-            m = max(m, abs_bits(qe)); m = max(m, abs_bits(qs)); m = max(m, abs_bits(qn));
-            m = max(m, abs_bits(qb)); m = max(m, abs_bits(qt)); m = max(m, abs_bits(dv));
-            const double r = bp ? qt : qw - qe + qs - qn + qb - qt - dv;
-            cm = fmax(cm, fma(-f.tol, __longlong_as_double((long long)m), fabs(r)));
+            const double terms[7] = {qw, qe, qs, qn, qb, qt, dv};
+            const double x = budget_excess(terms, bp, tolf);
+            if (__double_as_longlong(x) != 0 && x > cm) cm = x;   // x != 0 only where the check fails
         }
     });
     if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) *f.vchanged = 1u;

@@ -27,6 +27,9 @@ def main():
     ap.add_argument("--sched", type=int, default=-1,
                     help="batched schedule (0 one CTA per tile, 1 tile list) instead of the autotuner's choice")
     ap.add_argument("--split", type=int, default=4, help="largest tracer group per launch with --sched")
+    ap.add_argument("--rebind", action="store_true",
+                    help="batched form: a new hydrodynamic state before every step (the FP64 fields bound "
+                         "again from device memory, then the repack), as a coupled time loop does")
     args = ap.parse_args()
     build.build()
     import torch
@@ -49,14 +52,27 @@ def main():
             b.set_tracer(t, P)
             if refs:
                 b.set_reference(t, refs[t])
-        b.step(p, nsteps=args.warmup)
+        if args.rebind:
+            dev = {n: torch.from_numpy(d.arrays[n]).cuda() for n in synth.F3}
+
+            def run(n):
+                for _ in range(n):
+                    ad.set_fields(dev, bind=True)
+                    b.step(p, nsteps=1)
+        else:
+            def run(n):
+                b.step(p, nsteps=n)
+        run(args.warmup)
         b.sync()
         t0 = time.perf_counter()
-        b.step(p, nsteps=args.steps)
+        run(args.steps)
         b.sync()
         el = time.perf_counter() - t0
         print(f"schedule {b.schedule()}")
         b.destroy()
+        if args.rebind:
+            ad.set_fields(dev, device=True)            # the instance's own copies again
+            del dev
     else:
         bufs = [(torch.from_numpy(P).cuda(), torch.empty_like(torch.from_numpy(P)).cuda()) for P in tr]
         R = [torch.from_numpy(r).cuda() for r in refs] if refs else None
