@@ -108,10 +108,10 @@ typedef struct mohid_ad_params {
     int    NullDif;               /* LOGICAL                                          */
     int    BoundaryCondition;     /* MOHID_BC_*; 4 and 8 also act without a reference */
     double DecayTime;             /* [s]                                              */
-    int    AdvectionNudging;      /* LOGICAL, must be .false. (not implemented)       */
+    int    AdvectionNudging;      /* LOGICAL: nudging near open boundaries (plain form) */
     int    AdvectionNudgingCells;
     int    CellFluxes;            /* LOGICAL: record the face fluxes (plain form)     */
-    int    NoAdvFlux, NoDifFlux;  /* LOGICAL: use the NoFlux masks (plain form)        */
+    int    NoAdvFlux, NoDifFlux;  /* LOGICAL: use the NoFlux masks                    */
     int    Optimize, FirstProperty; /* LOGICAL; accepted, results follow the general path */
     int    Vertical1D, XZFlow;    /* LOGICAL, StartAdvectionDiffusion options          */
     int    Docycle_method;        /* 1 (default) or 2, ModuleModel.F90:641-646        */
@@ -352,10 +352,14 @@ int mohid_ad_kill(int* id, int* stat);
  *            1 = FP16 transports with a per-field scale,
  *            2 = FP16 transports and diffusivities with per-field scales.
  * Supported options: AdvMethodH UpwindOrder1 or P2_TVD (any limiter),
- * implicit upwind vertical advection, implicit vertical diffusion,
- * Docycle_method 1, closed or MassConservation open boundaries.  Other
- * options (NullGradient and Cyclic boundaries among them, with or without a
- * reference) return MOHID_AD_ERR_UNSUPPORTED (use the plain form).
+ * explicit horizontal advection, implicit upwind vertical advection,
+ * implicit vertical diffusion, Docycle_method 1; closed boundaries or the
+ * open boundaries MassConservation, ImposedValue, NullGradient, SubModel,
+ * MassConservNullGrad and Cyclic; discharges
+ * (mohid_ad_batched_set_discharge_conc); the NoFlux masks on batches without
+ * references.  Other options (Orlanski boundaries, AdvectionNudging,
+ * CellFluxes, implicit horizontal advection among them) return
+ * MOHID_AD_ERR_UNSUPPORTED (use the plain form).
  */
 int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat);
 
@@ -368,6 +372,21 @@ int mohid_ad_batched_pack_hydro(const int* bid, int* stat);
  * the Size box, on the host (*on_device == 0) or on the device. */
 int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP, const int* on_device, int* stat);
 int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, const int* on_device, int* stat);
+
+/*
+ * Discharge concentrations of tracer t (0-based): DischConc of SetDischarges
+ * (ModuleAdvectionDiffusion.F90:978-1075), one value per discharge cell of the
+ * plain instance's mohid_ad_set_discharges call and in its order; WP calls
+ * SetDischarges per property with that property's concentrations
+ * (WP:14763-14770).  The cells, flows, withdrawal factors (DischConcMF, which
+ * the tracers share), vertical distribution and bypass flags are those of
+ * mohid_ad_set_discharges.  With discharges set on the plain instance every
+ * tracer needs its concentrations before a step (MOHID_AD_ERR_OPTION
+ * otherwise); the tracers are then held as absolute values and the mass fixer
+ * does not run (the discharges add and remove mass).  Ensembles reject
+ * members with discharges.
+ */
+int mohid_ad_batched_set_discharge_conc(const int* bid, const int* t, const double* DischConc, int* stat);
 
 /* Exterior (reference) concentration of tracer t for open boundaries
  * (ReferenceProp of AdvectionDiffusion); once set for any tracer, every

@@ -94,6 +94,7 @@ _AD_SIGS = {
     "mohid_ad_batched_set_tracer": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
     "mohid_ad_batched_get_tracer": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
     "mohid_ad_batched_set_reference": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_set_discharge_conc": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p]),
     "mohid_ad_batched_step": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_mass": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
     "mohid_ad_batched_boundary_flux": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),

@@ -60,6 +60,15 @@ class Batch:
                                                      C.byref(C.c_int(dev)), C.byref(st))
         N.check(rc, "mohid_ad_batched_set_reference")
 
+    def set_discharge_conc(self, t: int, conc):
+        """DischConc of tracer t: one value per discharge cell of the plain
+        instance's set_discharges, in its order (mohid_ad_batched_set_discharge_conc)."""
+        c = np.ascontiguousarray(conc, dtype=np.float64)
+        st = C.c_int(0)
+        rc = self.lib.mohid_ad_batched_set_discharge_conc(C.byref(self._bid), C.byref(C.c_int(t)),
+                                                          c.ctypes.data_as(C.c_void_p), C.byref(st))
+        N.check(rc, "mohid_ad_batched_set_discharge_conc")
+
     def step(self, p: N.MohidAdParams, nsteps: int = 1, graph: bool = False):
         st = C.c_int(0)
         rc = self.lib.mohid_ad_batched_step(C.byref(self._bid), C.byref(p), C.byref(C.c_int(nsteps)),

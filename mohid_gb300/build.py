@@ -28,9 +28,10 @@ CUDA_UNITS = [
     ("batched_kernel.cu", []),
     ("batched_kernel_obc.cu", []),
 ] + [
-    # the batched step's kernels: one unit per boundary form and storage
+    # the batched step's kernels: one unit per form (closed, MassConservation
+    # open boundaries, every boundary treatment and discharges) and storage
     ("batched_inst.cu", [f"-DMOHID_INST_OBC={o}", f"-DMOHID_INST_STORAGE={st}"], f"batched_inst_{o}{st}")
-    for o in (0, 1) for st in (0, 1, 2)
+    for o in (0, 1, 2) for st in (0, 1, 2)
 ] + [
     ("ensemble_kernel.cu", []),
     ("batched_pack.cu", []),

@@ -642,7 +642,8 @@ int mohid_ad_set_discharges(const int* id, const int* DischNumber, const int* Di
     // ignored, their cells, the layers of each cell
     const int fillInt = -9999999, uniformVert = 5;   // FillValueInt, DischUniform_
     const int ni = in->ni, nj = in->nj, nk = in->nk, sj = ni + 2;
-    std::vector<std::pair<int, mohid::DischTerm>> terms;   // (column, term)
+    struct Term { int col; mohid::DischTerm t; int cell; };   // column, term, discharge cell n
+    std::vector<Term> terms;
     int n = 0;
     for (int dis = 0; dis < nd; ++dis) {
         if (IgnoreDisch[dis]) continue;
@@ -666,19 +667,25 @@ int mohid_ad_set_discharges(const int* id, const int* DischNumber, const int* Di
                 t.k = k; t.kmin = kmin; t.kmax = kmax;
                 t.flags = (uniform ? 1 : 0) | (ByPass[dis] ? 2 : 0);
                 t.flow = DischFlow[n]; t.conc = DischConc[n]; t.concMF = DischConcMF[n];
-                terms.emplace_back(i + sj * j, t);
+                terms.push_back({i + sj * j, t, n});
             }
         }
     }
     // by column, then layer, keeping the reference's order among equal cells
-    std::stable_sort(terms.begin(), terms.end(), [](const auto& x, const auto& y) {
-        return x.first != y.first ? x.first < y.first : x.second.k < y.second.k;
+    std::stable_sort(terms.begin(), terms.end(), [](const Term& x, const Term& y) {
+        return x.col != y.col ? x.col < y.col : x.t.k < y.t.k;
     });
     std::vector<int> start(in->n2 + 1, 0);
-    for (const auto& t : terms) ++start[(size_t)t.first + 1];
+    for (const auto& t : terms) ++start[(size_t)t.col + 1];
     for (size_t c = 0; c < in->n2; ++c) start[c + 1] += start[c];
     std::vector<mohid::DischTerm> tv(terms.size());
-    for (size_t q = 0; q < terms.size(); ++q) tv[q] = terms[q].second;
+    for (size_t q = 0; q < terms.size(); ++q) tv[q] = terms[q].t;
+    // host copies for the batched form (its own layout, a concentration per tracer)
+    in->hTermCol.resize(terms.size());
+    in->hTermCell.resize(terms.size());
+    for (size_t q = 0; q < terms.size(); ++q) { in->hTermCol[q] = terms[q].col; in->hTermCell[q] = terms[q].cell; }
+    in->hTerms = tv;
+    in->nDischCells = n;
     CK(cudaSetDevice(in->device));
     CK(cudaStreamSynchronize(in->stream));              // no step still reads the old lists
     if (!in->dStart.p) {
@@ -693,6 +700,7 @@ int mohid_ad_set_discharges(const int* id, const int* DischNumber, const int* Di
     }
     CK(cudaMemcpy(in->dStart.p, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
     in->hasDisch = !tv.empty();
+    ++in->dischVersion;
     return ok(stat);
 }
 
@@ -703,6 +711,8 @@ int mohid_ad_unset_discharges(const int* id, int* stat)
     CK(cudaSetDevice(in->device));
     CK(cudaStreamSynchronize(in->stream));
     in->hasDisch = false;
+    in->hTerms.clear(); in->hTermCol.clear(); in->hTermCell.clear();
+    ++in->dischVersion;
     return ok(stat);
 }
 
@@ -712,6 +722,7 @@ int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, c
     if (!in) return fail(MOHID_AD_ERR_ID, stat, "unknown instance id");
     if (!NoFluxU && !NoFluxV && !NoFluxW) {
         in->hasNoFlux = false;
+        ++in->nofluxVersion;
         return ok(stat);
     }
     if (!NoFluxU || !NoFluxV || !NoFluxW) return fail(MOHID_AD_ERR_NULLPTR, stat, "give all three masks or none");
@@ -727,6 +738,7 @@ int mohid_ad_set_noflux(const int* id, const int* NoFluxU, const int* NoFluxV, c
     }
     CK(cudaStreamSynchronize(in->stream));
     in->hasNoFlux = true;
+    ++in->nofluxVersion;
     return ok(stat);
 }
 

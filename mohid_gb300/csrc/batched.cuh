@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "common.cuh"
+
 namespace mohid {
 
 // Batched layout of one domain: x = i + kXOff (i = -2..ni+2), y = j + kYOff
@@ -15,8 +17,9 @@ constexpr int kYOff = 2;
 constexpr int kTX = 32;   // tile width along i (one warp)
 constexpr int kTY = 8;    // tile height along j (warps per CTA)
 
-// cell flag bits
-constexpr uint8_t F_WP = 1, F_OP = 2, F_CFU = 4, F_CFV = 8, F_CFW = 16, F_LP = 32;
+// cell flag bits; F_NDW / F_NAW: the cell's bottom face carries no diffusion /
+// no advection (NoDifFlux / NoAdvFlux with NoFluxW, set by noflux_flags)
+constexpr uint8_t F_WP = 1, F_OP = 2, F_CFU = 4, F_CFV = 8, F_CFW = 16, F_LP = 32, F_NDW = 64, F_NAW = 128;
 // column flag bits
 constexpr uint8_t C_SOLVE = 1, C_OPTOP = 2, C_CFWTOP = 4, C_BP = 8, C_SD = 16;
 // face flag bits of a cell's west (U: between j-1 and j) and south (V: between
@@ -86,6 +89,15 @@ struct BatchArgs {
     const int* refIdx;
     long long rts;
     int rk;
+    // discharges (or null; compiled into the open-boundary instantiation): the
+    // terms of column c2 of the layout at dTerms[dStart[c2] .. dStart[c2 + 1])
+    // (by layer, in the reference's order), tracer t's concentration of term q
+    // at dConc[q * ntAll + t]; DWZ (FP64, Size box) for the uniform vertical
+    // distribution
+    const int* dStart;
+    const DischTerm* dTerms;
+    const float* dConc;
+    const double* DWZ;
     float* W;                           // scratch: THOMASZ W per cell (batched layout)
     float* G;                           // scratch: THOMASZ G of the launch's tracers per cell, nt
                                         // floats per cell (cell c at G + c * nt)
@@ -235,9 +247,23 @@ cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int*
 // ImposeNullGradient (AD:1926-1987) on nt batched FP32 tracers (stride ts):
 // at each layer the boundary columns `cols` (Size-box 2-D offsets, the
 // reference's order) take in turn the mean of their neighbours across compute
-// faces; KFloor over the Size box
-cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* fflag, const int* cols, int ncols,
+// faces (the cell flags' F_CFU / F_CFV); KFloor over the Size box
+cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* flag, const int* cols, int ncols,
                                   const int* KFloor, const BLayout& L, cudaStream_t s);
+// Prop_CyclicBoundary (AD:2121-2224) on nt batched FP32 tracers after the
+// solve: the boundary columns `cols` take their compact references (Ref, row
+// q of column q, rk values, tracer stride rts; less corr[t]), then the rows and
+// columns whose two ends are boundary points (BP: BoundaryPoints2D, Size box)
+// copy the interior values next to the opposite end from KFloor up
+cudaError_t cyclic_batched(float* P, long long ts, int nt, const float* Ref, long long rts, int rk,
+                           const double* corr, const int* cols, int ncols, const int* BP, const int* KFloor,
+                           const BLayout& L, cudaStream_t s);
+// NoAdvFlux / NoDifFlux with the NoFluxU/V/W masks (Size box, may be null when
+// both are off) folded into the packed cell and face flags; both off restores
+// the unmasked flags.  OP, CFU, CFV, KF: the instance's masks and KFloorZ
+cudaError_t noflux_flags(const int* OP, const int* CFU, const int* CFV, const int* NFU, const int* NFV,
+                         const int* NFW, const int* KF, bool noAdv, bool noDif, uint8_t* flag, uint8_t* fflag,
+                         const BLayout& L, cudaStream_t s);
 cudaError_t pack_shift_f32(const double* src, float* dst, const int* WP, double shift, const BLayout& L,
                            cudaStream_t s);
 cudaError_t water_mean(const double* src, const int* WP, const BLayout& L, double* partial, int nblocks,

@@ -43,6 +43,16 @@ struct Batch {
     DevBuf<int> kfloor;
     DevBuf<float> PA, PB, Ref;           // tracers (ping-pong); references of the boundary columns
     DevBuf<int> refIdx;                  // per column of the layout: its row in Ref, or -1
+    // discharges of the plain instance in the batched layout, with each
+    // tracer's concentrations (mohid_ad_batched_set_discharge_conc)
+    DevBuf<int> dStart;
+    DevBuf<mohid::DischTerm> dTerms;
+    DevBuf<float> dConc;
+    std::vector<std::vector<double>> hConc;   // per tracer: DischConc of the discharge cells
+    unsigned dischVersion = ~0u;         // the instance's discharges the lists hold
+    bool dischDirty = true;              // concentrations changed since the upload
+    bool dischOn = false;                // the steps apply discharges
+    unsigned dischUploads = 0;           // bumped by every upload of the lists
     DevBuf<float> Wsc, Gsc;              // THOMASZ W and G per cell, scratch of the step kernel
     // mass fixer (static volumes): VolumeZ as an FP32 pair, the fixer state
     // (volume, targets, constants, corrections, boundary fluxes), per-tile
@@ -75,6 +85,7 @@ struct Batch {
     int graphFix = -1;                   // fixer / open-boundary launches the graph holds
     bool graphLast = false;              // the graph ends with the call's last step
     unsigned graphPack = ~0u;            // packed hydrodynamics the graph's arguments hold
+    unsigned graphDisch = ~0u;           // discharge upload the graph's arguments hold (dischUploads)
                                          // (FP16 scales, tile count)
     // asynchronous repack of a new hydrodynamic state (on the instance's
     // stream) and tracer loads (on their own stream, with their own scratch),
@@ -109,6 +120,10 @@ struct Batch {
     double checkedDT = -1.0;
     int checkedFlags = -1;
     bool shiftOk = true;
+    // NoAdvFlux (1) / NoDifFlux (2) folded into the packed flags, and the
+    // instance's NoFlux masks they were formed from (noflux_flags)
+    int nfApplied = 0;
+    unsigned nfVersion = ~0u;
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
     int ensemble = 0;                    // id of the ensemble stepping this batch, or 0
@@ -134,6 +149,7 @@ struct Batch {
         RV.release(); DVR.release(); flag.release(); fflag.release(); cflag.release(); fc.release();
         kfloor.release();
         partial.release(); scratch.release(); stage.release(); refIdx.release();
+        dStart.release(); dTerms.release(); dConc.release();
         mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release();
         obpart.release(); obcol.release(); obcnt.release();
         tl.release(); tcost.release();
@@ -218,14 +234,18 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     if (p->ImpExp_DifH != 0.0) { why = "horizontal diffusion must be explicit (reference ERR02)"; return MOHID_AD_ERR_OPTION; }
     if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->Docycle_method != 1) { why = "batched form follows Docycle_method 1"; return MOHID_AD_ERR_UNSUPPORTED; }
-    if (p->AdvectionNudging || p->CellFluxes || p->NoAdvFlux || p->NoDifFlux) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->AdvectionNudging || p->CellFluxes) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if ((p->NoAdvFlux || p->NoDifFlux) && (hasRef || ensemble)) {
+        why = "batched form: NoFlux masks with open-boundary references or in ensembles (use the plain form)";
+        return MOHID_AD_ERR_UNSUPPORTED;
+    }
     const int bc = p->BoundaryCondition;
     if (hasRef) {
         if (bc != 1 && bc != 2 && bc != 4 && bc != 5 && bc != 6 && bc != 7 && bc != 8) {
             why = "invalid BoundaryCondition (reference Set_Internal_State ERR01)"; return MOHID_AD_ERR_OPTION;
         }
-        if (bc == MOHID_BC_ORLANSKI || bc == MOHID_BC_CYCLIC) {
-            why = "batched form: Orlanski and Cyclic boundaries (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
+        if (bc == MOHID_BC_ORLANSKI) {
+            why = "batched form: Orlanski boundaries (use the plain form)"; return MOHID_AD_ERR_UNSUPPORTED;
         }
         if (ensemble && bc != MOHID_BC_MASS_CONSERVATION) {
             why = "ensembles: closed or MassConservation open boundaries"; return MOHID_AD_ERR_UNSUPPORTED;
@@ -255,7 +275,51 @@ bool fix_active(const Batch* b)
 bool bc_fixable(const Batch* b, const mohid_ad_params* p)
 {
     const int bc = p->BoundaryCondition;
+    if (b->dischOn) return false;                // discharges add and remove mass
     return b->hasRef ? bc == MOHID_BC_MASS_CONSERVATION : bc != MOHID_BC_NULL_GRADIENT;
+}
+
+// The plain instance's discharges in the batched layout with every tracer's
+// concentrations; dischOn says whether the steps apply them.  Terms keep the
+// instance's order (by column, j outer and i inner, then layer and the
+// reference's order), which is also the batched layout's column order.
+int ensure_discharges(Batch* b, int* stat)
+{
+    Instance* in = b->in;
+    b->dischOn = in->hasDisch;
+    if (!in->hasDisch) return ok(stat);
+    for (int t = 0; t < b->nt; ++t)
+        if (t >= (int)b->hConc.size() || (int)b->hConc[t].size() != in->nDischCells)
+            return fail(MOHID_AD_ERR_OPTION, stat,
+                        "set the discharge concentrations of every tracer (mohid_ad_batched_set_discharge_conc)");
+    if (b->dischVersion == in->dischVersion && !b->dischDirty) return ok(stat);
+    const size_t nq = in->hTerms.size();
+    const int sj = in->ni + 2;
+    std::vector<int> start((size_t)b->L.n2 + 1, 0);
+    for (size_t q = 0; q < nq; ++q) {
+        const int c = in->hTermCol[q];
+        ++start[(size_t)b->L.at2(c % sj, c / sj) + 1];
+    }
+    for (long long c = 0; c < b->L.n2; ++c) start[(size_t)c + 1] += start[(size_t)c];
+    std::vector<float> conc(nq * (size_t)b->nt);
+    for (size_t q = 0; q < nq; ++q)
+        for (int t = 0; t < b->nt; ++t) conc[q * (size_t)b->nt + t] = (float)b->hConc[t][(size_t)in->hTermCell[q]];
+    CK(cudaStreamSynchronize(in->stream));      // no step still reads the old lists
+    auto bad = [&](cudaError_t e) { return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e)); };
+    cudaError_t e;
+    if (!b->dStart.p && (e = b->dStart.alloc((size_t)b->L.n2 + 1)) != cudaSuccess) return bad(e);
+    b->dTerms.release(); b->dConc.release();
+    if ((e = b->dTerms.alloc(std::max<size_t>(1, nq))) != cudaSuccess) return bad(e);
+    if ((e = b->dConc.alloc(std::max<size_t>(1, conc.size()))) != cudaSuccess) return bad(e);
+    CK(cudaMemcpy(b->dStart.p, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+    if (nq) {
+        CK(cudaMemcpy(b->dTerms.p, in->hTerms.data(), sizeof(mohid::DischTerm) * nq, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(b->dConc.p, conc.data(), sizeof(float) * conc.size(), cudaMemcpyHostToDevice));
+    }
+    b->dischVersion = in->dischVersion;
+    b->dischDirty = false;
+    ++b->dischUploads;
+    return ok(stat);
 }
 
 // which of the fixer's launches a step makes (fixer, boundary flux, target drop)
@@ -331,6 +395,7 @@ int pack_enqueue(Batch* b, int* stat)
     }
     b->packingMasks = masks;
     b->packingMask = in->maskVersion;
+    if (masks) b->nfApplied = 0;                 // the flags formed again hold no NoFlux bits
     b->packingRef = b->hasRef;
     CK(cudaMemcpyAsync(&b->hp->moving, b->moving.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(&b->hp->vchanged, b->vchanged.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -450,6 +515,22 @@ int ensure_packed(Batch* b, int* stat)
     return pack_finalize(b, stat);
 }
 
+// the packed flags carry the step's NoAdvFlux / NoDifFlux (after ensure_packed)
+int ensure_noflux(Batch* b, const mohid_ad_params* p, int* stat)
+{
+    Instance* in = b->in;
+    const int want = (p->NoAdvFlux ? 1 : 0) | (p->NoDifFlux ? 2 : 0);
+    if (want && !in->hasNoFlux)
+        return fail(MOHID_AD_ERR_NULLPTR, stat, "NoAdvFlux / NoDifFlux need the NoFluxU/V/W masks (mohid_ad_set_noflux)");
+    if (want == b->nfApplied && (want == 0 || b->nfVersion == in->nofluxVersion)) return ok(stat);
+    CK(mohid::noflux_flags(in->OP.p, in->CFU.p, in->CFV.p, want ? in->NFU.p : nullptr, want ? in->NFV.p : nullptr,
+                           want ? in->NFW.p : nullptr, in->KFloor.p, (want & 1) != 0, (want & 2) != 0, b->flag.p,
+                           b->fflag.p, b->L, in->stream));
+    b->nfApplied = want;
+    b->nfVersion = in->nofluxVersion;
+    return ok(stat);
+}
+
 // sums: the launch accumulates the mass fixer's per-tile sums (when the fixer runs)
 mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, const float* Pin, float* Pout,
                             bool sums = true)
@@ -501,6 +582,10 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.xzflow = p->XZFlow != 0;
     a.status = in->status.p;
     a.bc = p->BoundaryCondition;
+    a.dStart = b->dischOn ? b->dStart.p : nullptr;
+    a.dTerms = b->dischOn ? b->dTerms.p : nullptr;
+    a.dConc = b->dischOn ? b->dConc.p : nullptr;
+    a.DWZ = in->DWZ.p;
     return a;
 }
 
@@ -511,10 +596,13 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     Instance* in = b->in;
     cudaStream_t s = in->stream;
     // without references the boundary columns get ordinary rows, whose budget
-    // must close like any other cell's: the check then covers them in full
-    const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0) | (b->hasRef ? 4 : 0);
+    // must close like any other cell's: the check then covers them in full.
+    // Discharges are sources the constant does not follow, and faces without
+    // advection (NoAdvFlux) break the budget of their cells: absolute values.
+    const int flags = (p->XZFlow ? 1 : 0) | (p->Vertical1D ? 2 : 0) | (b->hasRef ? 4 : 0) | (b->dischOn ? 8 : 0) |
+                      (p->NoAdvFlux ? 16 : 0);
     if (b->checkedVersion != in->hydroVersion || b->checkedDT != p->DTProp || b->checkedFlags != flags) {
-        bool okc = (flags & 3) == 0;
+        bool okc = (flags & 27) == 0;
         if (okc && b->preContVersion == in->hydroVersion && b->preContDT == p->DTProp && b->preCont >= 0.0 &&
             b->preContRef == b->hasRef) {
             okc = b->preCont <= 0.0;             // computed with the repack
@@ -533,8 +621,10 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
     }
     if (!b->shiftOk) {
         CK(fix_fold(b));                         // constants as corrected by the mass fixer
+        bool conv = false;
         for (int t = 0; t < b->nt; ++t) {
             if (b->shift[t] == 0.0) continue;
+            conv = true;
             const long long off = (long long)t * b->L.n3;
             CK(mohid::unshift(b->PA.p + off, b->flag.p, b->shift[t], b->L.n3, s));
             CK(mohid::unshift(b->PB.p + off, b->flag.p, b->shift[t], b->L.n3, s));
@@ -545,6 +635,15 @@ int ensure_shift_valid(Batch* b, const mohid_ad_params* p, int* stat)
                 b->refShift[t] = 0.0;
             }
             b->shift[t] = 0.0;
+        }
+        if (conv) {
+            // the fixer's copy of the constants follows (after the fold the
+            // corrections are zero): a later fold must not bring the old
+            // constants back onto absolute values
+            std::vector<double> zero((size_t)b->nt, 0.0);
+            CK(cudaMemcpyAsync(b->mfix.p + 1 + b->nt, zero.data(), sizeof(double) * zero.size(),
+                               cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
         }
     }
     return ok(stat);
@@ -606,8 +705,18 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
     // ImposeNullGradient after the solve, whether or not a reference is given (AD:1874-1880)
     if (p->BoundaryCondition == MOHID_BC_NULL_GRADIENT) {
         Instance* in = b->in;
-        cudaError_t e = mohid::null_gradient_batched(Pout, b->L.n3, b->nt, b->fflag.p, in->bcols.p, in->nbcols,
+        cudaError_t e = mohid::null_gradient_batched(Pout, b->L.n3, b->nt, b->flag.p, in->bcols.p, in->nbcols,
                                                      in->KFloor.p, b->L, s);
+        if (e != cudaSuccess) return e;
+    }
+    // Prop_CyclicBoundary after the solve (AD:1874-1880); the walk gave the
+    // boundary rows their old values, as for NullGradient
+    if (p->BoundaryCondition == MOHID_BC_CYCLIC && b->hasRef) {
+        Instance* in = b->in;
+        const int rk = b->L.nk + 2;
+        cudaError_t e = mohid::cyclic_batched(Pout, b->L.n3, b->nt, b->Ref.p, (long long)in->nbcols * rk, rk,
+                                              b->mfix.p + 1 + 2 * b->nt, in->bcols.p, in->nbcols, in->BP2D.p,
+                                              in->KFloor.p, b->L, s);
         if (e != cudaSuccess) return e;
     }
     if (!real) return cudaSuccess;
@@ -916,6 +1025,25 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
     return ok(stat);
 }
 
+// DischConc of tracer t: one value per discharge cell of the plain instance's
+// mohid_ad_set_discharges call, in its order (SetDischarges AD:978-1075, called
+// per property with the property's concentrations, WP:14763-14770)
+int mohid_ad_batched_set_discharge_conc(const int* bid, const int* t, const double* DischConc, int* stat)
+{
+    TraceRange trace_("mohid_ad_batched_set_discharge_conc");
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    Instance* in = b->in;
+    if (!in->hasDisch) return fail(MOHID_AD_ERR_OPTION, stat, "the plain instance has no discharges set");
+    if (in->nDischCells > 0 && !DischConc) return fail(MOHID_AD_ERR_NULLPTR, stat, "DischConc is NULL");
+    if ((int)b->hConc.size() < b->nt) b->hConc.resize(b->nt);
+    b->hConc[*t].assign(DischConc, DischConc + in->nDischCells);
+    b->dischDirty = true;
+    return ok(stat);
+}
+
 int mohid_ad_batched_set_reference(const int* bid, const int* t, const double* ReferenceProp,
                                    const int* on_device, int* stat)
 {
@@ -967,6 +1095,8 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     int code = check_batched_params(p, b->hasRef, why);
     if (code) return fail(code, stat, why);
     if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
+    CK(cudaSetDevice(b->in->device));
+    if ((code = ensure_discharges(b, stat)) != 0) return code;
     b->bcFix = bc_fixable(b, p);
     if (b->hasRef)
         for (int t = 0; t < b->nt; ++t)
@@ -979,6 +1109,10 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     CK(cudaSetDevice(in->device));
+    {
+        int c = ensure_noflux(b, p, stat);
+        if (c) return c;
+    }
     {
         int c = ensure_shift_valid(b, p, stat);
         if (c) return c;
@@ -1003,6 +1137,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
                            b->graphSched == b->sched && b->graphSplit == b->split &&
                            b->graphFix == fix_key(b) && b->graphLast == glast &&
                            b->graphPack == b->packedVersion &&
+                           b->graphDisch == (b->dischOn ? b->dischUploads : ~0u) &&
                            std::memcmp(&b->graphParams, p, sizeof(*p)) == 0;
         if (!reuse) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -1027,6 +1162,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphFix = fix_key(b);
             b->graphLast = glast;
             b->graphPack = b->packedVersion;
+            b->graphDisch = b->dischOn ? b->dischUploads : ~0u;
         }
         CK(cudaGraphLaunch(b->graph, s));
     }
@@ -1046,11 +1182,14 @@ int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* sta
     if (code) return fail(code, stat, why);
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
+    if ((code = ensure_discharges(b, stat)) != 0) return code;
     {
         int c = ensure_packed(b, stat);
         if (c) return c;
     }
-    int c = ensure_shift_valid(b, p, stat);
+    int c = ensure_noflux(b, p, stat);
+    if (c) return c;
+    c = ensure_shift_valid(b, p, stat);
     if (c) return c;
     return autotune(b, p, stat);
 }
@@ -1246,6 +1385,10 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
         std::string why;
         int code = check_batched_params(&p[q], b->hasRef, why, true);
         if (code) return fail(code, stat, "member " + std::to_string(q) + ": " + why);
+        if (b->in->hasDisch)
+            return fail(MOHID_AD_ERR_UNSUPPORTED, stat, "member " + std::to_string(q) +
+                        ": ensembles without discharges (use a batch per domain)");
+        b->dischOn = false;
         b->bcFix = bc_fixable(b, &p[q]);
         if (p[q].AdvMethodH != method || (method != MOHID_UPWIND_ORDER1 && p[q].TVDLimitationH != limiter))
             return fail(MOHID_AD_ERR_OPTION, stat, "members must share AdvMethodH and TVDLimitationH");
@@ -1258,7 +1401,9 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
             int c = ensure_packed(b, stat);
             if (c) return c;
         }
-        int c = ensure_shift_valid(b, &p[q], stat);
+        int c = ensure_noflux(b, &p[q], stat);   // clears the bits of an earlier stand-alone step
+        if (c) return c;
+        c = ensure_shift_valid(b, &p[q], stat);
         if (c) return c;
         if (fix_active(b)) b->fixDirty = true;
         if (b->cur != E->cur) return fail(MOHID_AD_ERR_OPTION, stat, "a member was stepped outside the ensemble");

@@ -55,20 +55,26 @@ cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// open boundaries (reference concentrations set) take the instantiation
-// that carries the MassConservation boundary terms
+// discharges, and open boundaries (reference concentrations set) other than
+// MassConservation, take the form with every boundary treatment and the
+// discharge terms; MassConservation alone the form with its terms only
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
                            bool halfK, const int2* tiles, int ntl, cudaStream_t s)
 {
     const int storage = halfQ ? (halfK ? 2 : 1) : 0;
-    if (a.Ref) {
-        if (storage == 2) return launch_batched_unit<true, 2>(a, m, method, limiter, tiles, ntl, s);
-        if (storage == 1) return launch_batched_unit<true, 1>(a, m, method, limiter, tiles, ntl, s);
-        return launch_batched_unit<true, 0>(a, m, method, limiter, tiles, ntl, s);
+    if (a.dStart || (a.Ref && a.bc != 1)) {
+        if (storage == 2) return launch_batched_unit<2, 2>(a, m, method, limiter, tiles, ntl, s);
+        if (storage == 1) return launch_batched_unit<2, 1>(a, m, method, limiter, tiles, ntl, s);
+        return launch_batched_unit<2, 0>(a, m, method, limiter, tiles, ntl, s);
     }
-    if (storage == 2) return launch_batched_unit<false, 2>(a, m, method, limiter, tiles, ntl, s);
-    if (storage == 1) return launch_batched_unit<false, 1>(a, m, method, limiter, tiles, ntl, s);
-    return launch_batched_unit<false, 0>(a, m, method, limiter, tiles, ntl, s);
+    if (a.Ref) {
+        if (storage == 2) return launch_batched_unit<1, 2>(a, m, method, limiter, tiles, ntl, s);
+        if (storage == 1) return launch_batched_unit<1, 1>(a, m, method, limiter, tiles, ntl, s);
+        return launch_batched_unit<1, 0>(a, m, method, limiter, tiles, ntl, s);
+    }
+    if (storage == 2) return launch_batched_unit<0, 2>(a, m, method, limiter, tiles, ntl, s);
+    if (storage == 1) return launch_batched_unit<0, 1>(a, m, method, limiter, tiles, ntl, s);
+    return launch_batched_unit<0, 0>(a, m, method, limiter, tiles, ntl, s);
 }
 
 cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int* cost,

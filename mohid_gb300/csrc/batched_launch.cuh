@@ -11,7 +11,7 @@ namespace mohid {
 namespace launch_detail {
 using namespace tile;
 
-template <int NT, int METHOD, int LIM, typename QT, typename KT, bool OBC>
+template <int NT, int METHOD, int LIM, typename QT, typename KT, int OBC>
 __global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : (NT <= 4 ? 3 : 2))
 batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M, const int2* __restrict__ tiles, int ntl)
 {
@@ -29,10 +29,10 @@ batched_kernel(const BatchArgs A, const __grid_constant__ TmaMaps M, const int2*
     }
 }
 
-template <int NT, int METHOD, int LIM, typename QT, typename KT, bool OBC>
+template <int NT, int METHOD, int LIM, typename QT, typename KT, int OBC>
 cudaError_t launch_t(const BatchArgs& a, const TmaMaps& m, const int2* tiles, int ntl, cudaStream_t s)
 {
-    const size_t smem = Smem<NT, QT, KT>::bytes(a.L.nk);
+    const size_t smem = Smem<NT, QT, KT>::bytes(a.L.nk, OBC == 2);
     auto kern = batched_kernel<NT, METHOD, LIM, QT, KT, OBC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -58,7 +58,7 @@ cudaError_t launch_t(const BatchArgs& a, const TmaMaps& m, const int2* tiles, in
     return cudaGetLastError();
 }
 
-template <int NT, typename QT, typename KT, bool OBC>
+template <int NT, typename QT, typename KT, int OBC>
 cudaError_t launch_m(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles, int ntl,
                      cudaStream_t s)
 {
@@ -74,7 +74,7 @@ cudaError_t launch_m(const BatchArgs& a, const TmaMaps& m, int method, int limit
 
 // the kernels of one storage (QT transports, KT diffusivities) for every
 // tracer group size and scheme
-template <bool OBC, typename QT, typename KT>
+template <int OBC, typename QT, typename KT>
 cudaError_t launch_storage(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles, int ntl,
                            cudaStream_t s)
 {
@@ -90,10 +90,12 @@ cudaError_t launch_storage(const BatchArgs& a, const TmaMaps& m, int method, int
 
 }  // namespace launch_detail
 
-// One instantiation unit per boundary form (OBC: the MassConservation terms
-// compiled in) and storage (0: FP32, 1: FP16 transports, 2: FP16 transports
-// and diffusivities): batched_inst.cu, compiled once per pair in parallel.
-template <bool OBC, int STORAGE>
+// One instantiation unit per form (OBC 0: closed boundaries, 1: the
+// MassConservation terms compiled in, 2: every open-boundary treatment and
+// the discharge terms)
+// and storage (0: FP32, 1: FP16 transports, 2: FP16 transports and
+// diffusivities): batched_inst.cu, compiled once per pair in parallel.
+template <int OBC, int STORAGE>
 cudaError_t launch_batched_unit(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles,
                                 int ntl, cudaStream_t s)
 {
@@ -104,11 +106,14 @@ cudaError_t launch_batched_unit(const BatchArgs& a, const TmaMaps& m, int method
 #define MOHID_BATCHED_UNIT(OBC, STORAGE)                                                                   \
     template cudaError_t launch_batched_unit<OBC, STORAGE>(const BatchArgs&, const TmaMaps&, int, int,     \
                                                            const int2*, int, cudaStream_t)
-extern MOHID_BATCHED_UNIT(false, 0);
-extern MOHID_BATCHED_UNIT(false, 1);
-extern MOHID_BATCHED_UNIT(false, 2);
-extern MOHID_BATCHED_UNIT(true, 0);
-extern MOHID_BATCHED_UNIT(true, 1);
-extern MOHID_BATCHED_UNIT(true, 2);
+extern MOHID_BATCHED_UNIT(0, 0);
+extern MOHID_BATCHED_UNIT(0, 1);
+extern MOHID_BATCHED_UNIT(0, 2);
+extern MOHID_BATCHED_UNIT(1, 0);
+extern MOHID_BATCHED_UNIT(1, 1);
+extern MOHID_BATCHED_UNIT(1, 2);
+extern MOHID_BATCHED_UNIT(2, 0);
+extern MOHID_BATCHED_UNIT(2, 1);
+extern MOHID_BATCHED_UNIT(2, 2);
 
 }  // namespace mohid

@@ -490,8 +490,10 @@ __global__ void k_ref_index(const int* __restrict__ cols, int ncols, int sj, BLa
 // columns in the reference's order at layer k (k = 0..KUB from |KFloorZ|), so
 // a cell sees the new values of the boundary cells swept before it.  The
 // neighbours across compute faces are water cells, stored relative to the
-// same constant as the boundary cell, so their mean is taken as stored.
-__global__ void k_null_gradient_b(float* P, long long ts, int nt, const uint8_t* __restrict__ fflag,
+// same constant as the boundary cell, so their mean is taken as stored.  The
+// compute faces come from the cell flags (F_CFU of a cell is its west face,
+// F_CFV its south face), which the NoFlux masks leave alone.
+__global__ void k_null_gradient_b(float* P, long long ts, int nt, const uint8_t* __restrict__ flag,
                                   const int* __restrict__ cols, int ncols, const int* __restrict__ KFloor, BLayout L)
 {
     const int nk1 = L.nk + 1;
@@ -504,12 +506,104 @@ __global__ void k_null_gradient_b(float* P, long long ts, int nt, const uint8_t*
         const int kf = KFloor[c];
         if (k < (kf < 0 ? -kf : kf)) continue;
         const long long a = L.at(c % sj, c / sj, k);
-        const float cv1 = (fflag[a + 1] & FV_ACT) ? 1.f : 0.f, cv0 = (fflag[a] & FV_ACT) ? 1.f : 0.f;
-        const float cu1 = (fflag[a + L.px] & FU_ACT) ? 1.f : 0.f, cu0 = (fflag[a] & FU_ACT) ? 1.f : 0.f;
+        const float cv1 = (flag[a + 1] & F_CFV) ? 1.f : 0.f, cv0 = (flag[a] & F_CFV) ? 1.f : 0.f;
+        const float cu1 = (flag[a + L.px] & F_CFU) ? 1.f : 0.f, cu0 = (flag[a] & F_CFU) ? 1.f : 0.f;
         const float aux = cv1 + cv0 + cu1 + cu0;
         if (aux <= 0.f) continue;
         Pt[a] = (Pt[a + 1] * cv1 + Pt[a - 1] * cv0 + Pt[a + L.px] * cu1 + Pt[a - L.px] * cu0) / aux;
     }
+}
+
+// Prop_CyclicBoundary (AD:2121-2224) on nt batched FP32 tracers, after the
+// solve, in two launches.  First every boundary column takes its reference at
+// k = 1..KUB: thread (q, k, t), the reference stored relative to the tracer's
+// constant, less the mass fixer's correction of it (corr[t]) as in the walk.
+__global__ void k_cyclic_ref_b(float* P, long long ts, int nt, const float* __restrict__ Ref, long long rts,
+                               int rk, const double* __restrict__ corr, const int* __restrict__ cols, int ncols,
+                               BLayout L)
+{
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int nk = L.nk;
+    if (e >= (long long)ncols * nk * nt) return;
+    const int k = 1 + (int)(e % nk), q = (int)((e / nk) % ncols), t = (int)(e / ((long long)nk * ncols));
+    const int c = cols[q], sj = L.ni + 2;
+    P[(long long)t * ts + L.at(c % sj, c / sj, k)] = Ref[(long long)t * rts + (long long)q * rk + k] - (float)corr[t];
+}
+// Then each row i = 2..IUB-1 whose two ends (j = 1, JUB) are boundary points
+// copies the interior values next to the opposite end, and likewise each
+// column j = 2..JUB-1 with i = 1, IUB, from the source column's KFloorZ up
+// (clamped to the box, AD:2160-2215).  No copy reads a cell another copy
+// writes (the row copies write j = 1, JUB and read j = 2, JUB-1 of rows
+// 2..IUB-1; the column copies write i = 1, IUB), so one thread per (copy, k,
+// tracer) keeps the reference's result.  Copy m: m < 2 (ni-2) rows (even m the
+// j = 1 end), then columns.
+__global__ void k_cyclic_copy_b(float* P, long long ts, int nt, const int* __restrict__ BP,
+                                const int* __restrict__ KF, BLayout L)
+{
+    const int ni = L.ni, nj = L.nj, nk1 = L.nk + 1, sj = ni + 2;
+    const long long nrow = 2LL * (ni > 2 ? ni - 2 : 0), ncol = 2LL * (nj > 2 ? nj - 2 : 0);
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (nrow + ncol) * nk1 * nt) return;
+    const int k = (int)(e % nk1);
+    const long long m = (e / nk1) % (nrow + ncol);
+    const int t = (int)(e / ((nrow + ncol) * nk1));
+    int di, dj, si, sjj;                         // destination and source cells
+    if (m < nrow) {
+        const int i = 2 + (int)(m / 2);
+        if (BP[i + sj] != 1 || BP[i + sj * nj] != 1) return;
+        di = i; si = i;
+        if (m % 2 == 0) { dj = 1; sjj = nj - 1; } else { dj = nj; sjj = 2; }
+    } else {
+        const int j = 2 + (int)((m - nrow) / 2);
+        if (BP[1 + sj * j] != 1 || BP[ni + sj * j] != 1) return;
+        dj = j; sjj = j;
+        if ((m - nrow) % 2 == 0) { di = 1; si = ni - 1; } else { di = ni; si = 2; }
+    }
+    const int kf = KF[si + sj * sjj];
+    if (k < (kf < 0 ? 0 : kf)) return;
+    float* Pt = P + (long long)t * ts;
+    Pt[L.at(di, dj, k)] = Pt[L.at(si, sjj, k)];
+}
+
+// NoAdvFlux / NoDifFlux folded into the flag bytes over the work box, where
+// the reference zeroes the masked faces' coefficients: the advective bit of a
+// west (south) face is cleared where NoFluxU (NoFluxV) == 1 and NoAdvFlux is
+// on (AD:4434-4443, AD:4804-4813), its compute bit, which carries the
+// diffusion, where NoDifFlux is on (AD:2496-2500, AD:2527-2531); F_NDW marks
+// a bottom face with NoFluxW == 1 under NoDifFlux (AD:2741-2745), F_NAW one
+// under NoAdvFlux on a column open at KUB, from KFloorZ up (AD:3004-3013).
+// Both bits of each face are formed again from the masks first, so noAdv =
+// noDif = 0 restores the unmasked flags (the TVD bits are left as they are).
+__global__ void __launch_bounds__(kRowThreads)
+k_noflux_flags(const int* __restrict__ OP, const int* __restrict__ CFU, const int* __restrict__ CFV,
+               const int* __restrict__ NFU, const int* __restrict__ NFV, const int* __restrict__ NFW,
+               const int* __restrict__ KF, int noAdv, int noDif, uint8_t* flag, uint8_t* fflag, BLayout L)
+{
+    const int NI = L.ni + 2;
+    const long long sk = (long long)NI * (L.nj + 2);
+    for_rows(L, 1, L.nk, [&](long long e, long long g, int i, int j, int k) {
+        if (i < 1 || i > L.ni || j < 1 || j > L.nj) return;
+        const bool op = OP[e] == 1;
+        const bool cfu = CFU[e] == 1 && j != L.nj + 1, cfv = CFV[e] == 1 && i != L.ni + 1;
+        uint8_t ff = fflag[g] & (uint8_t)(FU_TVDP | FU_TVDN | FV_TVDP | FV_TVDN);
+        if (cfu) {
+            if (!(noDif && NFU[e] == 1)) ff |= FU_ACT;
+            if (op && OP[e - NI] == 1 && !(noAdv && NFU[e] == 1)) ff |= FU_ADV;
+        }
+        if (cfv) {
+            if (!(noDif && NFV[e] == 1)) ff |= FV_ACT;
+            if (op && OP[e - 1] == 1 && !(noAdv && NFV[e] == 1)) ff |= FV_ADV;
+        }
+        fflag[g] = ff;
+        uint8_t fl = flag[g] & (uint8_t)~(F_NDW | F_NAW);
+        if (noDif && NFW[e] == 1) fl |= F_NDW;
+        if (noAdv && NFW[e] == 1) {
+            const long long c = i + (long long)NI * j;
+            const int kf = KF[c];
+            if (OP[c + sk * L.nk] == 1 && k >= (kf < 0 ? 0 : kf)) fl |= F_NAW;
+        }
+        flag[g] = fl;
+    });
 }
 
 // add the stored constant back: anomaly -> absolute values (water cells)
@@ -945,12 +1039,39 @@ cudaError_t ref_index(const int* cols, int ncols, int ni, const BLayout& L, int*
     k_ref_index<<<(ncols + 255) / 256, 256, 0, s>>>(cols, ncols, ni + 2, L, idx);
     return cudaGetLastError();
 }
-cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* fflag, const int* cols, int ncols,
+cudaError_t null_gradient_batched(float* P, long long ts, int nt, const uint8_t* flag, const int* cols, int ncols,
                                   const int* KFloor, const BLayout& L, cudaStream_t s)
 {
     if (ncols <= 0 || nt <= 0) return cudaSuccess;
     const int n = (L.nk + 1) * nt;
-    k_null_gradient_b<<<(n + 63) / 64, 64, 0, s>>>(P, ts, nt, fflag, cols, ncols, KFloor, L);
+    k_null_gradient_b<<<(n + 63) / 64, 64, 0, s>>>(P, ts, nt, flag, cols, ncols, KFloor, L);
+    return cudaGetLastError();
+}
+cudaError_t cyclic_batched(float* P, long long ts, int nt, const float* Ref, long long rts, int rk,
+                           const double* corr, const int* cols, int ncols, const int* BP, const int* KFloor,
+                           const BLayout& L, cudaStream_t s)
+{
+    if (nt <= 0) return cudaSuccess;
+    const long long n1 = (long long)ncols * L.nk * nt;
+    if (n1 > 0) {
+        k_cyclic_ref_b<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(P, ts, nt, Ref, rts, rk, corr, cols, ncols, L);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    const long long lines = 2LL * (L.ni > 2 ? L.ni - 2 : 0) + 2LL * (L.nj > 2 ? L.nj - 2 : 0);
+    const long long n2 = lines * (L.nk + 1) * nt;
+    if (n2 <= 0) return cudaSuccess;
+    k_cyclic_copy_b<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(P, ts, nt, BP, KFloor, L);
+    return cudaGetLastError();
+}
+cudaError_t noflux_flags(const int* OP, const int* CFU, const int* CFV, const int* NFU, const int* NFV,
+                         const int* NFW, const int* KF, bool noAdv, bool noDif, uint8_t* flag, uint8_t* fflag,
+                         const BLayout& L, cudaStream_t s)
+{
+    if (L.nk < 1) return cudaSuccess;
+    if ((noAdv || noDif) && (!NFU || !NFV || !NFW)) return cudaErrorInvalidValue;
+    k_noflux_flags<<<row_blocks(L, L.nk), kRowThreads, 0, s>>>(OP, CFU, CFV, NFU, NFV, NFW, KF, noAdv ? 1 : 0,
+                                                                noDif ? 1 : 0, flag, fflag, L);
     return cudaGetLastError();
 }
 cudaError_t unshift(float* P, const uint8_t* flag, double shift, long long n, cudaStream_t s)

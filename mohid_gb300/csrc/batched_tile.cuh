@@ -106,7 +106,9 @@ struct Smem {
     static constexpr int oRed = oCY + al128(NSF * 16);      // the mass fixer's per-warp sums
     static constexpr int oBar = oRed + al128(TY * NT * 2 * 4);
     static constexpr int oEnd = oBar + 128;
-    static size_t bytes(int) { return (size_t)oEnd; }
+    static constexpr int oDis = oEnd;                       // a row's discharge sources, per thread
+    // dis: the discharge instantiation, which also holds oDis
+    static size_t bytes(int, bool dis = false) { return (size_t)(dis ? oDis + al128(NTH * NT * 4) : oEnd); }
 };
 
 // ---- PTX helpers: mbarrier and bulk tensor copies ---------------------------
@@ -383,6 +385,18 @@ __device__ __forceinline__ void face_flux(const unsigned char* st, float* out, c
     }
 }
 
+// The flow of a discharge term into its layer (Discharges AD:4057-4075): the
+// cell's flow, or with the uniform vertical distribution its share by layer
+// thickness over layers kmin..kmax (FP64 as the reference, rare columns only).
+__device__ __forceinline__ float disch_flow(const BatchArgs& A, const DischTerm& T, int i, int j, int k)
+{
+    if (!(T.flags & 1)) return (float)T.flow;
+    const long long NI = A.L.ni + 2, sk = NI * (A.L.nj + 2), c = i + NI * j;
+    double wc = 0.0;
+    for (int kk = T.kmin; kk <= T.kmax; ++kk) wc = wc + A.DWZ[c + sk * kk];
+    return (float)(T.flow * A.DWZ[c + sk * k] / wc);
+}
+
 // s + c += a as an unevaluated FP32 pair (Knuth's TwoSum: the rounding error of
 // s + a is carried in c); the _rn intrinsics keep the compiler from fusing
 __device__ __forceinline__ void two_sum_acc(float& s, float& c, float a)
@@ -432,7 +446,12 @@ __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
 // The layer body is compiled once per stage buffer (the walk advances two
 // layers per iteration), so every shared-memory access is a per-thread offset
 // computed once per tile plus a constant.
-template <int NT, int METHOD, int LIM, typename QT, typename KT, bool OBC>
+//
+// OBC selects the form: 0 closed boundaries, 1 with the MassConservation
+// open-boundary terms, 2 with every open-boundary treatment and the
+// discharges, so that no form carries the registers and code of terms it
+// does not apply (form 1 serves MassConservation batches and ensembles).
+template <int NT, int METHOD, int LIM, typename QT, typename KT, int OBC>
 __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, int bx, int by,
                                           unsigned char* smem_raw, uint32_t& phase)
 {
@@ -518,6 +537,9 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
     // concentrations: the closed form carries none of their instructions
     const bool obcCol = OBC && (cf & C_BP) && A.Ref != nullptr;
     const float* refc = obcCol ? A.Ref + (long long)A.refIdx[c2] * A.rk : nullptr;   // this column's row
+    // discharge terms of this column, dq0 .. dq1 (discharge instantiation only)
+    int dq0 = 0, dq1 = 0;
+    if (OBC == 2 && A.dStart && solve) { dq0 = A.dStart[c2]; dq1 = A.dStart[c2 + 1]; }
     // own-column values of the face below row k slide up the walk: transport,
     // conductance Kz * area / DZZ (AD:2736-2765), cell flags of rows k-1 and k
     float qz = 0.f, kzb = 0.f;
@@ -528,7 +550,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
         qz = ldg_as<QT>(A.Qz, a, A.qsz);
         fl = A.flag[a];
         flm = A.flag[a - L.sl];
-        if (vdif && (fl & F_CFW)) {
+        if (vdif && (fl & (F_CFW | F_NDW)) == F_CFW) {
             float kz = A.coefV * ldg_as<KT>(A.DiffV, a, A.ksv) + A.backV;
             if (A.nullDif && qz == 0.f) kz = 0.f;
             kzb = kz * areaCol * A.DZZ[a - L.sl];          // DZZ holds 1/DZZ
@@ -598,7 +620,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             const float ratio = open ? 1.f - dvr : 1.f;
             // VerticalDiffusion, implicit: faces k (below) and k+1 (above)
             float kza = 0.f;
-            if (vdif && (flp & F_CFW)) {
+            if (vdif && (flp & (F_CFW | F_NDW)) == F_CFW) {     // NoDifFlux: F_NDW
                 float kz = A.coefV * tofl<KT>(reinterpret_cast<const KT*>(st + SL::oDv)[own], A.ksv) + A.backV;
                 if (A.nullDif && qzp == 0.f) kz = 0.f;
                 kza = kz * areaCol * reinterpret_cast<const float*>(st + SL::oDz)[own];   // 1/DZZ(k)
@@ -607,13 +629,43 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             float D = -aux2, E = 1.f + aux2 + aux1, Fc = -aux1;
             if (open && top) E += dtv * qzp;
             if (vadv && open) {                          // VerticalAdvection, upwind, implicit
-                if (k > kb && (flm & F_OP)) {
+                // (faces under NoAdvFlux carry F_NAW on the cell above them)
+                if (k > kb && (flm & F_OP) && !(fl & F_NAW)) {
                     D -= fmaxf(qz, 0.f) * dtv;
                     E -= fminf(qz, 0.f) * dtv;
                 }
-                if (!top && (flp & F_OP)) {
+                if (!top && (flp & (F_OP | F_NAW)) == F_OP) {
                     E += fmaxf(qzp, 0.f) * dtv;
                     Fc += fminf(qzp, 0.f) * dtv;
+                }
+            }
+            // discharges (AD:4025-4128), rare rows: withdrawals (not bypassed)
+            // from open cells enter E; each tracer's sources gather in shared
+            // memory (dsrc, tracer stride NTH), read by the tracer loop below.
+            // A water cell that is not open and takes an inflow restarts from
+            // P * Vold / V plus the source (dfill)
+            bool dis = false, dfill = false;
+            float* dsrc = reinterpret_cast<float*>(smem_raw + SM::oDis) + tid;
+            if (OBC == 2 && dq1 > dq0) {
+                for (int q = dq0; q < dq1; ++q) {
+                    const DischTerm T = A.dTerms[q];
+                    if (T.k != k) continue;
+                    const float fl = disch_flow(A, T, i, j, k);
+                    const float* cq = A.dConc + (long long)q * A.ntAll + A.t0;
+                    if (!dis) {
+                        for (int t = 0; t < NT; ++t) dsrc[t * NTH] = 0.f;
+                        dis = true;
+                    }
+                    if (open) {
+                        if ((T.flags & 2) || fl > 0.f) {
+                            for (int t = 0; t < NT; ++t) dsrc[t * NTH] += fl * dtv * cq[t];
+                        } else {
+                            E -= fl * dtv * (float)T.concMF;
+                        }
+                    } else if (fl > 0.f) {
+                        for (int t = 0; t < NT; ++t) dsrc[t * NTH] = fl * dtv * cq[t];
+                        dfill = true;
+                    }
                 }
             }
             // open boundary cells (OpenBoundaryCondition AD:5369-5742).
@@ -628,7 +680,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             bool ident = false;
             const uint8_t* ffl = st + SL::oF + fO;
             if (obc) {
-                if (A.bc == 1 || A.bc == 7) {
+                if (OBC == 1 || A.bc == 1 || A.bc == 7) {
                     const QT* qx = reinterpret_cast<const QT*>(st + SL::oQX);
                     const QT* qy = reinterpret_cast<const QT*>(st + SL::oQY);
                     wfob = obc_wfob((ffl[0] & FU_ACT) ? tofl<QT>(qx[own], A.qsx) : 0.f,
@@ -637,9 +689,9 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                                     (ffl[1] & FV_ACT) ? tofl<QT>(qy[qyO + 1], A.qsy) : 0.f,
                                     (fl & F_CFW) ? qz : 0.f, (flp & F_CFW) ? qzp : 0.f, dvr, rVk, DT);
                     if (wfob >= 0.f) E += wfob * dtv;
-                    else ident = A.bc == 7;
+                    else ident = OBC == 2 && A.bc == 7;
                 } else {
-                    ident = true;
+                    ident = OBC == 2;
                 }
                 if (ident) { D = 0.f; E = 1.f; Fc = 0.f; }
             }
@@ -656,10 +708,11 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             for (int t = 0; t < NT; ++t) {
                 const float Pc = P[t * (TY + 4) * PBX + pbO];
                 float TI = Pc * ratio;
+                if (OBC == 2 && dis) TI = (dfill ? Pc * (1.f - dvr) : TI) + dsrc[t * NTH];
                 if (horiz)
                     TI = fmaf(dtv, (FX[t * NWF + own] - FX[t * NWF + own + TX]) +
                                    (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);
-                if (OBC && ident) {
+                if (OBC == 2 && ident) {
                     const float* Pt = P + t * (TY + 4) * PBX + pbO;   // the neighbours: i +- 1, j +- PBX
                     if (A.bc == 2 || A.bc == 5) {
                         // the interior mean over the neighbours that are open

@@ -82,11 +82,18 @@ struct Instance {
     // NoFluxU/V/W masks (mohid_ad_set_noflux), used by NoAdvFlux / NoDifFlux
     DevBuf<int> NFU, NFV, NFW;
     bool hasNoFlux = false;
+    unsigned nofluxVersion = 0;        // bumped by every mohid_ad_set_noflux
     // discharges (mohid_ad_set_discharges): per-column term lists
     std::vector<int> hKFloor;          // KFloorZ (host copy, Size box 2-D)
     DevBuf<int> dStart;
     DevBuf<mohid::DischTerm> dTerms;
     bool hasDisch = false;
+    // host copies of the terms in the same order: term, its Size-box column and
+    // its discharge cell n (the index into DischConc); bumped on every change
+    std::vector<mohid::DischTerm> hTerms;
+    std::vector<int> hTermCol, hTermCell;
+    int nDischCells = 0;
+    unsigned dischVersion = 0;
     DevBuf<unsigned int> status;
     unsigned int* hstatus = nullptr;   // pinned
 

@@ -88,12 +88,13 @@ def test_batched_open_boundaries(gpu, grid, opt, decay):
 
 @pytest.mark.parametrize("grid", ["open", "nsopen", "allopen"])
 @pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee"])
-@pytest.mark.parametrize("bc,decay", [(2, 0.0), (2, 300.0), (5, 0.0), (7, 0.0), (4, 0.0)])
+@pytest.mark.parametrize("bc,decay", [(2, 0.0), (2, 300.0), (5, 0.0), (7, 0.0), (4, 0.0), (8, 0.0)])
 def test_batched_other_open_boundaries(gpu, grid, opt, bc, decay):
     # ImposedValue, SubModel (identity rows with the interior mean decayed
     # towards the reference), MassConservNullGrad (inflow rows take the
-    # neighbours' mean) and NullGradient (the sweep after the solve), one step
-    # and five steps against the oracle
+    # neighbours' mean), NullGradient (the sweep after the solve) and Cyclic
+    # (references, then the copies across the domain after the solve), one
+    # step and five steps against the oracle
     if grid == "allopen":
         d = synth.generate(synth.GenSpec(ni=40, nj=33, nk=6, land_frac=0.1, land_kind=1, seed=11, open_sides=15,
                                          bathy_kind=1, dt=30.0))
@@ -123,9 +124,115 @@ def test_batched_null_gradient_without_reference(gpu, grid):
         assert rel_l2(d, g, w) <= TOL
 
 
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee"])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_batched_discharges(gpu, grid, opt, seed):
+    # SetDischarges with each tracer's concentrations: point and uniform
+    # discharges, inflows, withdrawals (DischConcMF), a bypass and an ignored
+    # discharge, with MassConservation boundaries where the grid is open; one
+    # step at 1e-6 and five at 1e-5 against the oracle
+    from tests.cases import discharges
+    d = domain(grid)
+    tr = [d.tracer(3, 1.0, 0.5, seed=2), d.tracer(1, 5.0, 20.0, seed=4)]
+    refs = [d.reference(2.0, 0.3, seed=3), d.reference(12.0, 0.2, seed=5)] if d.spec.open_sides else None
+    ds = discharges(d, seed=seed)
+    concs = [ds["Conc"], ds["Conc"] * 3.0 + 10.0]
+    pd = dict(DTProp=30.0, **BATCH_OPTIONS[opt])
+    for steps, tol in ((1, 1e-6), (5, TOL)):
+        ad = advdiff.AdvectionDiffusion(d)
+        ad.set_hydro()
+        ad.set_discharges(ds)
+        b = batched.Batch(ad, len(tr))
+        for t, P in enumerate(tr):
+            b.set_tracer(t, P)
+            b.set_discharge_conc(t, concs[t])
+            if refs:
+                b.set_reference(t, refs[t])
+        b.step(advdiff.params(**pd), nsteps=steps, graph=steps > 1)
+        b.sync()
+        got = [b.get_tracer(t) for t in range(len(tr))]
+        b.destroy()
+        ad.kill()
+        for t, P in enumerate(tr):
+            Q = P.copy()
+            for _ in range(steps):
+                assert O.step(d, Q, O.params(**pd), ReferenceProp=refs[t] if refs else None,
+                              Disch=dict(ds, Conc=concs[t])) == 0
+            assert rel_l2(d, got[t], Q) <= tol
+
+
+def test_batched_discharges_need_every_concentration(gpu):
+    from tests.cases import discharges
+    d = domain("coast")
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    ad.set_discharges(discharges(d, seed=0))
+    b = batched.Batch(ad, 2)
+    b.set_tracer(0, d.tracer(3, 1.0, 0.5, seed=2))
+    b.set_tracer(1, d.tracer(3, 1.0, 0.5, seed=3))
+    b.set_discharge_conc(0, discharges(d, seed=0)["Conc"])
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        b.step(advdiff.params(DTProp=30.0))
+    assert ei.value.code == 3
+    b.destroy()
+    ad.kill()
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "layer1"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee"])
+@pytest.mark.parametrize("flags", [dict(NoAdvFlux=1), dict(NoDifFlux=1), dict(NoAdvFlux=1, NoDifFlux=1)])
+def test_batched_noflux_masks(gpu, grid, opt, flags):
+    # NoAdvFlux / NoDifFlux with the instance's NoFluxU/V/W masks: one step at
+    # 1e-6, then four more alternating with and without the options (the
+    # flags are formed again each time) at 1e-5, against the oracle
+    from tests.cases import noflux_masks
+    d = domain(grid)
+    nf = noflux_masks(d, seed=5)
+    tr = [d.tracer(3, 1.0, 0.5, seed=2), d.tracer(1, 5.0, 20.0, seed=4)]
+    base = dict(DTProp=30.0, **BATCH_OPTIONS[opt])
+    seq = [dict(base, **flags), base, dict(base, **flags), dict(base, **flags), base]
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, len(tr))
+    for t, P in enumerate(tr):
+        b.set_tracer(t, P)
+    with pytest.raises(advdiff.N.MohidAdError) as ei:        # the masks are required
+        b.step(advdiff.params(**seq[0]))
+    assert ei.value.code == 9
+    ad.set_noflux(nf)
+    want = [P.copy() for P in tr]
+    work = O.Work(d)
+    for n, pd in enumerate(seq):
+        b.step(advdiff.params(**pd), nsteps=1)
+        b.sync()
+        for Q in want:
+            assert O.step(d, Q, O.params(**pd), work=work, NoFlux=nf) == 0
+        for t, Q in enumerate(want):
+            assert rel_l2(d, b.get_tracer(t), Q) <= (1e-6 if n == 0 else TOL)
+    b.destroy()
+    ad.kill()
+
+
+def test_batched_noflux_rejected_with_references(gpu):
+    from tests.cases import noflux_masks
+    d = domain("open")
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    ad.set_noflux(noflux_masks(d, seed=5))
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, d.tracer(3, 1.0, 0.5, seed=2))
+    b.set_reference(0, d.reference(2.0, 0.3, seed=3))
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        b.step(advdiff.params(DTProp=30.0, NoAdvFlux=1))
+    assert ei.value.code == 4
+    b.destroy()
+    ad.kill()
+
+
 def test_batched_rejects_boundary_conditions_like_the_plain_form(gpu):
-    # Orlanski and Cyclic stay with the plain form (MOHID_AD_ERR_UNSUPPORTED);
-    # codes the reference rejects give MOHID_AD_ERR_OPTION as there
+    # Orlanski stays with the plain form (MOHID_AD_ERR_UNSUPPORTED); codes
+    # the reference rejects give MOHID_AD_ERR_OPTION as there
     d = domain("open")
     ad = advdiff.AdvectionDiffusion(d)
     ad.set_hydro()
@@ -136,7 +243,7 @@ def test_batched_rejects_boundary_conditions_like_the_plain_form(gpu):
             b.step(advdiff.params(DTProp=30.0, BoundaryCondition=bc))
         assert ei.value.code == code
     b.set_reference(0, d.reference(2.0, 0.3, seed=2))
-    for bc, code in ((6, 4), (8, 4), (3, 3)):
+    for bc, code in ((6, 4), (3, 3)):
         with pytest.raises(advdiff.N.MohidAdError) as ei:
             b.step(advdiff.params(DTProp=30.0, BoundaryCondition=bc))
         assert ei.value.code == code
