@@ -110,7 +110,7 @@ typedef struct mohid_ad_params {
     double DecayTime;             /* [s]                                              */
     int    AdvectionNudging;      /* LOGICAL: nudging near open boundaries (plain form) */
     int    AdvectionNudgingCells;
-    int    CellFluxes;            /* LOGICAL: record the face fluxes (plain form)     */
+    int    CellFluxes;            /* LOGICAL: record the face fluxes                  */
     int    NoAdvFlux, NoDifFlux;  /* LOGICAL: use the NoFlux masks                    */
     int    Optimize, FirstProperty; /* LOGICAL; accepted, results follow the general path */
     int    Vertical1D, XZFlow;    /* LOGICAL, StartAdvectionDiffusion options          */
@@ -357,9 +357,9 @@ int mohid_ad_kill(int* id, int* stat);
  * open boundaries MassConservation, ImposedValue, NullGradient, SubModel,
  * MassConservNullGrad and Cyclic; discharges
  * (mohid_ad_batched_set_discharge_conc); the NoFlux masks on batches without
- * references.  Other options (Orlanski boundaries, AdvectionNudging,
- * CellFluxes, implicit horizontal advection among them) return
- * MOHID_AD_ERR_UNSUPPORTED (use the plain form).
+ * references; CellFluxes (mohid_ad_batched_get_adv_flux / _dif_flux).
+ * Other options (Orlanski boundaries, AdvectionNudging, implicit horizontal
+ * advection among them) return MOHID_AD_ERR_UNSUPPORTED (use the plain form).
  */
 int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const int* storage, int* stat);
 
@@ -387,6 +387,21 @@ int mohid_ad_batched_get_tracer(const int* bid, const int* t, double* PROP, cons
  * members with discharges.
  */
 int mohid_ad_batched_set_discharge_conc(const int* bid, const int* t, const double* DischConc, int* stat);
+
+/*
+ * GetAdvFlux / GetDifFlux (ModuleAdvectionDiffusion.F90:697-860) of tracer t
+ * (0-based) of the batch: the face fluxes of its last step, which the last
+ * mohid_ad_batched_step call must have made with p->CellFluxes
+ * (MOHID_AD_ERR_OPTION otherwise, and after the tracer or the hydrodynamics
+ * were loaded again).  Same arrays and conventions as mohid_ad_get_adv_flux /
+ * mohid_ad_get_dif_flux; FP32 arithmetic.  They are formed on request from
+ * the field before and after that step, so steps with CellFluxes cost nothing
+ * more.  Ensembles reject CellFluxes.
+ */
+int mohid_ad_batched_get_adv_flux(const int* bid, const int* t, double* AdvFluxX, double* AdvFluxY,
+                                  double* AdvFluxZ, const int* on_device, int* stat);
+int mohid_ad_batched_get_dif_flux(const int* bid, const int* t, double* DifFluxX, double* DifFluxY,
+                                  double* DifFluxZ, const int* on_device, int* stat);
 
 /* Exterior (reference) concentration of tracer t for open boundaries
  * (ReferenceProp of AdvectionDiffusion); once set for any tracer, every

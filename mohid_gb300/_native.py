@@ -97,6 +97,10 @@ _AD_SIGS = {
     "mohid_ad_batched_set_discharge_conc": (C.c_int, [c_int_p, c_int_p, C.c_void_p, c_int_p]),
     "mohid_ad_batched_step": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_mass": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
+    "mohid_ad_batched_get_adv_flux": (C.c_int, [c_int_p, c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p,
+                                                c_int_p]),
+    "mohid_ad_batched_get_dif_flux": (C.c_int, [c_int_p, c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p,
+                                                c_int_p]),
     "mohid_ad_batched_boundary_flux": (C.c_int, [c_int_p, c_int_p, c_double_p, c_int_p]),
     "mohid_ad_set_discharges": (C.c_int, [c_int_p, c_int_p] + [C.c_void_p] * 12 + [c_int_p]),
     "mohid_ad_unset_discharges": (C.c_int, [c_int_p, c_int_p]),

@@ -102,6 +102,21 @@ class Batch:
         N.check(self.lib.mohid_ad_batched_set_mass_fix(C.byref(self._bid), C.byref(C.c_int(int(on))), C.byref(st)),
                 "mohid_ad_batched_set_mass_fix")
 
+    def cell_fluxes(self, t: int) -> dict:
+        """The face fluxes of tracer t's last step (made with CellFluxes=1):
+        AdvFluxX/Y/Z, DifFluxX/Y/Z as Size-box float64 arrays
+        (mohid_ad_batched_get_adv_flux / _dif_flux)."""
+        shape = self.ad.domain.shape3
+        out = {n: np.empty(shape) for n in ("AdvFluxX", "AdvFluxY", "AdvFluxZ", "DifFluxX", "DifFluxY", "DifFluxZ")}
+        st = C.c_int(0)
+        for fn, names in (("mohid_ad_batched_get_adv_flux", ("AdvFluxX", "AdvFluxY", "AdvFluxZ")),
+                          ("mohid_ad_batched_get_dif_flux", ("DifFluxX", "DifFluxY", "DifFluxZ"))):
+            rc = getattr(self.lib, fn)(C.byref(self._bid), C.byref(C.c_int(t)),
+                                       *(out[n].ctypes.data_as(C.c_void_p) for n in names),
+                                       C.byref(C.c_int(0)), C.byref(st))
+            N.check(rc, fn)
+        return out
+
     def mass(self, t: int) -> float:
         m = C.c_double(0.0)
         st = C.c_int(0)

@@ -27,6 +27,7 @@ CUDA_UNITS = [
     ("plain_f64.cu", ["--fmad=false"]),
     ("batched_kernel.cu", []),
     ("batched_kernel_obc.cu", []),
+    ("batched_flux.cu", []),
 ] + [
     # the batched step's kernels: one unit per form (closed, MassConservation
     # open boundaries, every boundary treatment and discharges) and storage

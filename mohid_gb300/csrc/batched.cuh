@@ -207,6 +207,14 @@ cudaError_t obc_columns(const uint8_t* cflag, const BLayout& L, int* cnt, int* l
 // mass fixer: a covers every tracer of the batch (t0 = 0) with the step's input
 // and output buffers; partials to a.obpart (a.nob = kObcBlocks blocks).
 cudaError_t obc_flux(const BatchArgs& a, const int* list, bool halfQ, cudaStream_t s);
+// CellFluxes of one tracer's last step (batched_flux.cu): the advective (adv)
+// or diffusive face fluxes through each cell's west, south and bottom face,
+// from the field before the step (Pold, explicit horizontal terms) and after it
+// (Pnew, implicit vertical terms), into out[0 .. 3 n3) over the Size box;
+// stored values + shift + *corr are the absolute values (corr may be null)
+cudaError_t cell_fluxes_batched(const BatchArgs& a, const float* Pold, const float* Pnew, double shift,
+                                const double* corr, bool adv, double* out, long long n3, int method, int limiter,
+                                bool halfQ, bool halfK, cudaStream_t s);
 // the same for `nb` batches from their argument records (device): mpart and
 // obpart of each record select what runs for that batch
 cudaError_t mass_fix_step_many(const BatchArgs* As, int nb, int ntmax, cudaStream_t s);

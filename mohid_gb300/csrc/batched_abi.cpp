@@ -124,6 +124,11 @@ struct Batch {
     // instance's NoFlux masks they were formed from (noflux_flags)
     int nfApplied = 0;
     unsigned nfVersion = ~0u;
+    // CellFluxes: the last step call asked for them (with these options) and
+    // the ping-pong buffers still hold that step's old and new fields
+    bool fluxLast = false;
+    mohid_ad_params fluxParams{};
+    DevBuf<double> fluxOut;              // 3 Size-box arrays, allocated on first use
     bool hasRef = false;
     bool cur = false;                    // false: PA holds the current state
     int ensemble = 0;                    // id of the ensemble stepping this batch, or 0
@@ -150,7 +155,7 @@ struct Batch {
         kfloor.release();
         partial.release(); scratch.release(); stage.release(); refIdx.release();
         dStart.release(); dTerms.release(); dConc.release();
-        mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release();
+        mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release(); fluxOut.release();
         obpart.release(); obcol.release(); obcnt.release();
         tl.release(); tcost.release();
         dscale.release(); dinv.release(); vchanged.release(); tpartial.release(); tscratch.release();
@@ -234,7 +239,8 @@ int check_batched_params(const mohid_ad_params* p, bool hasRef, std::string& why
     if (p->ImpExp_DifH != 0.0) { why = "horizontal diffusion must be explicit (reference ERR02)"; return MOHID_AD_ERR_OPTION; }
     if (p->ImpExp_AdvXX != 0.0 || p->ImpExp_AdvYY != 0.0) { why = "implicit horizontal advection not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
     if (p->Docycle_method != 1) { why = "batched form follows Docycle_method 1"; return MOHID_AD_ERR_UNSUPPORTED; }
-    if (p->AdvectionNudging || p->CellFluxes) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->AdvectionNudging) { why = "option not implemented"; return MOHID_AD_ERR_UNSUPPORTED; }
+    if (p->CellFluxes && ensemble) { why = "ensembles: CellFluxes (step the batch alone)"; return MOHID_AD_ERR_UNSUPPORTED; }
     if ((p->NoAdvFlux || p->NoDifFlux) && (hasRef || ensemble)) {
         why = "batched form: NoFlux masks with open-boundary references or in ensembles (use the plain form)";
         return MOHID_AD_ERR_UNSUPPORTED;
@@ -950,6 +956,7 @@ int mohid_ad_batched_pack_hydro(const int* bid, int* stat)
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     CK(cudaSetDevice(b->in->device));
+    b->fluxLast = false;                         // the fluxes read the packed fields of their step
     return ensure_packed(b, stat);
 }
 
@@ -960,6 +967,7 @@ int mohid_ad_batched_set_tracer(const int* bid, const int* t, const double* PROP
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!t || !PROP || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
     if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    b->fluxLast = false;                         // the buffers no longer hold the last step's fields
     Instance* in = b->in;
     if (!in->hydro) return fail(MOHID_AD_ERR_OPTION, stat, "the plain instance has no hydrodynamics set");
     CK(cudaSetDevice(in->device));
@@ -1096,6 +1104,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     if (code) return fail(code, stat, why);
     if (*nsteps < 1) return fail(MOHID_AD_ERR_BOUNDS, stat, "nsteps must be >= 1");
     CK(cudaSetDevice(b->in->device));
+    b->fluxLast = false;                         // set again once the steps are enqueued
     if ((code = ensure_discharges(b, stat)) != 0) return code;
     b->bcFix = bc_fixable(b, p);
     if (b->hasRef)
@@ -1123,9 +1132,14 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     if (fix_active(b)) b->fixDirty = true;
+    auto done = [&]() {
+        b->fluxLast = p->CellFluxes != 0;
+        if (b->fluxLast) b->fluxParams = *p;
+        return ok(stat);
+    };
     if (!*use_graph) {
         for (int n = 0; n < *nsteps; ++n) CK(enqueue_step(b, p, s, true, n == *nsteps - 1));
-        return ok(stat);
+        return done();
     }
     // CUDA graph of an even number of steps: the ping-pong returns to the
     // buffer it started from, so the graph stays valid for that parity; an
@@ -1167,7 +1181,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         CK(cudaGraphLaunch(b->graph, s));
     }
     if (*nsteps % 2) CK(enqueue_step(b, p, s, true, true));
-    return ok(stat);
+    return done();
 }
 
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat)
@@ -1182,6 +1196,7 @@ int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* sta
     if (code) return fail(code, stat, why);
     Instance* in = b->in;
     CK(cudaSetDevice(in->device));
+    b->fluxLast = false;
     if ((code = ensure_discharges(b, stat)) != 0) return code;
     {
         int c = ensure_packed(b, stat);
@@ -1283,6 +1298,52 @@ int mohid_ad_batched_boundary_flux(const int* bid, const int* t, double* flux, i
     return ok(stat);
 }
 
+// CellFluxes of tracer *t's last step (GetAdvFlux / GetDifFlux, AD:697-860),
+// formed from the ping-pong buffers (batched_flux.cu)
+static int batched_get_fluxes(const int* bid, const int* t, bool adv, double* X, double* Y, double* Z,
+                              const int* on_device, int* stat)
+{
+    Batch* b = blookup(bid);
+    if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
+    if (!t || !on_device) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
+    if (*t < 0 || *t >= b->nt) return fail(MOHID_AD_ERR_BOUNDS, stat, "tracer index out of range");
+    if (!b->fluxLast) return fail(MOHID_AD_ERR_OPTION, stat, "the last step was not made with CellFluxes");
+    Instance* in = b->in;
+    CK(cudaSetDevice(in->device));
+    if (!b->fluxOut.p) {
+        cudaError_t e = b->fluxOut.alloc((size_t)3 * in->n3);
+        if (e != cudaSuccess) return fail(MOHID_AD_ERR_ALLOC, stat, cuda_msg("cudaMalloc", e));
+    }
+    cudaStream_t s = in->stream;
+    const mohid_ad_params& p = b->fluxParams;
+    const long long off = (long long)*t * b->L.n3;
+    mohid::BatchArgs a = make_bargs(b, &p, 0, b->nt, b->cur_in(), b->cur_out(), false);
+    CK(mohid::cell_fluxes_batched(a, b->cur_out() + off, b->cur_in() + off, b->shift[*t],
+                                  b->mfix.p + 1 + 2 * b->nt + *t, adv, b->fluxOut.p, (long long)in->n3,
+                                  p.AdvMethodH, p.TVDLimitationH, b->storage >= 1, b->storage >= 2, s));
+    const cudaMemcpyKind kind = *on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    double* dst[3] = {X, Y, Z};
+    for (int q = 0; q < 3; ++q)
+        if (dst[q])
+            CK(cudaMemcpyAsync(dst[q], b->fluxOut.p + (size_t)q * in->n3, sizeof(double) * in->n3, kind, s));
+    CK(cudaStreamSynchronize(s));
+    return ok(stat);
+}
+
+int mohid_ad_batched_get_adv_flux(const int* bid, const int* t, double* AdvFluxX, double* AdvFluxY,
+                                  double* AdvFluxZ, const int* on_device, int* stat)
+{
+    TraceRange trace_("mohid_ad_batched_get_adv_flux");
+    return batched_get_fluxes(bid, t, true, AdvFluxX, AdvFluxY, AdvFluxZ, on_device, stat);
+}
+
+int mohid_ad_batched_get_dif_flux(const int* bid, const int* t, double* DifFluxX, double* DifFluxY,
+                                  double* DifFluxZ, const int* on_device, int* stat)
+{
+    TraceRange trace_("mohid_ad_batched_get_dif_flux");
+    return batched_get_fluxes(bid, t, false, DifFluxX, DifFluxY, DifFluxZ, on_device, stat);
+}
+
 int mohid_ad_batched_sync(const int* bid, int* stat)
 {
     Batch* b = blookup(bid);
@@ -1382,6 +1443,7 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
     CK(cudaSetDevice(E->device));
     for (size_t q = 0; q < n; ++q) {
         Batch* b = E->m[q];
+        b->fluxLast = false;
         std::string why;
         int code = check_batched_params(&p[q], b->hasRef, why, true);
         if (code) return fail(code, stat, "member " + std::to_string(q) + ": " + why);

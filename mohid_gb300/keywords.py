@@ -33,7 +33,8 @@ import dataclasses
 import re
 from pathlib import Path
 
-__all__ = ["KeywordError", "EnterData", "PropertyOptions", "property_options", "step_directions"]
+__all__ = ["KeywordError", "EnterData", "PropertyOptions", "property_options", "step_directions", "BatchPlan",
+           "batch_plan"]
 
 
 class KeywordError(ValueError):
@@ -218,3 +219,47 @@ def step_directions(opt: PropertyOptions, step: int) -> dict:
         return dict(ImpExp_AdvXX=0.0, ImpExp_AdvYY=0.0)
     x = step % 2 == 0
     return dict(ImpExp_AdvXX=1.0 if x else 0.0, ImpExp_AdvYY=0.0 if x else 1.0)
+
+
+@dataclasses.dataclass
+class BatchPlan:
+    """How the transported properties of a WaterProperties file map onto the
+    library: groups of properties that share every option go through one
+    batched call each (mohid_ad_batched_*), the rest through the plain FP64
+    form one property at a time, in file order within each list."""
+    batches: list          # list of lists of property names
+    plain: list            # property names
+
+
+def _batchable(opt: PropertyOptions) -> bool:
+    """The options the batched form takes (mohid_ad_batched_create's list in
+    include/mohid_ad.h): explicit UpwindOrder1 or P2_TVD horizontal advection,
+    implicit upwind vertical advection and implicit vertical diffusion, every
+    boundary condition but Orlanski, no AdvectionNudging."""
+    p = opt.params
+    return (not opt.implicit_h and p["AdvMethodH"] in (1, 4) and p["AdvMethodV"] == 1 and
+            p["ImpExp_AdvV"] == 1.0 and p["ImpExp_DifV"] == 1.0 and p["BoundaryCondition"] != 6 and
+            not p["AdvectionNudging"])
+
+
+def batch_plan(data: EnterData) -> BatchPlan:
+    """Group the transported properties (ADVECTION_DIFFUSION on) of a data
+    file: Advection_Diffusion_Processes calls AdvectionDiffusion once per
+    property with the same hydrodynamics (WP:14603-14824), so properties whose
+    options (and discharge flag) are equal can share one batched step."""
+    groups: dict = {}
+    order: list = []
+    plain: list = []
+    for blk in data.blocks():
+        opt = property_options(data, blk)
+        if not opt.advection_diffusion:
+            continue
+        if not _batchable(opt):
+            plain.append(opt.name)
+            continue
+        key = (tuple(sorted(opt.params.items())), opt.discharges)
+        if key not in groups:
+            groups[key] = []
+            order.append(key)
+        groups[key].append(opt.name)
+    return BatchPlan(batches=[groups[k] for k in order], plain=plain)

@@ -214,6 +214,98 @@ def test_batched_noflux_masks(gpu, grid, opt, flags):
     ad.kill()
 
 
+def _batched_fluxes(d, tr, refs, pd, steps, nf=None):
+    """(per tracer: oracle fluxes, batched fluxes) of the last of `steps` steps."""
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    if nf is not None:
+        ad.set_noflux(nf)
+    b = batched.Batch(ad, len(tr))
+    for t, P in enumerate(tr):
+        b.set_tracer(t, P)
+        if refs:
+            b.set_reference(t, refs[t])
+    b.step(advdiff.params(**pd), nsteps=steps, graph=steps > 1)
+    b.sync()
+    got = [b.cell_fluxes(t) for t in range(len(tr))]
+    b.destroy()
+    ad.kill()
+    out = []
+    for t, P in enumerate(tr):
+        Q = P.copy()
+        work = O.Work(d)
+        for _ in range(steps):
+            assert O.step(d, Q, O.params(**pd), ReferenceProp=refs[t] if refs else None, work=work,
+                          NoFlux=nf) == 0
+        out.append((O.cell_fluxes(d, work), got[t]))
+    return out
+
+
+# FP32 fluxes against FP64 ones: relative L2 per array.  The explicit
+# horizontal fluxes of a first step see the loaded field (rounded once to
+# FP32); the others see a field after FP32 steps, and the diffusive ones are
+# differences of neighbouring values, which the field's error enters relative
+# to the difference.
+FLUX_TOL = {1: 1e-5, 3: 2e-5}
+
+
+@pytest.mark.parametrize("grid", ["coast", "zlevel", "open"])
+@pytest.mark.parametrize("opt", ["upwind1", "tvd_superbee", "tvd_pdm", "nulldif", "xzflow", "vertical1d",
+                                 "background"])
+def test_batched_cell_fluxes(gpu, grid, opt):
+    # GetAdvFlux / GetDifFlux of the batched form against the oracle's, after
+    # one step and after three (the last step's fluxes); arrays the oracle
+    # leaves zero are zero
+    d = domain(grid)
+    tr = [d.tracer(3, 1.0, 0.5, seed=2), d.tracer(1, 5.0, 20.0, seed=4)]
+    refs = [d.reference(2.0, 0.3, seed=3), d.reference(12.0, 0.2, seed=5)] if d.spec.open_sides else None
+    pd = dict(DTProp=30.0, CellFluxes=1, **BATCH_OPTIONS[opt])
+    for steps in (1, 3):
+        for want, got in _batched_fluxes(d, tr, refs, pd, steps):
+            for n in O.FLUX_NAMES:
+                w, g = want[n], got[n]
+                nw = float(np.linalg.norm(w))
+                if nw == 0.0:
+                    assert not g.any(), n
+                else:
+                    assert float(np.linalg.norm(g - w)) <= FLUX_TOL[steps] * nw, (n, steps)
+
+
+@pytest.mark.parametrize("flags", [dict(NoAdvFlux=1), dict(NoDifFlux=1)])
+def test_batched_cell_fluxes_noflux(gpu, flags):
+    # masked faces carry no flux, except DifFluxZ, which the reference forms
+    # from the unmasked diffusivity
+    from tests.cases import noflux_masks
+    d = domain("coast")
+    nf = noflux_masks(d, seed=5)
+    tr = [d.tracer(3, 1.0, 0.5, seed=2)]
+    pd = dict(DTProp=30.0, CellFluxes=1, **flags, **BATCH_OPTIONS["tvd_superbee"])
+    for want, got in _batched_fluxes(d, tr, None, pd, 1, nf=nf):
+        for n in O.FLUX_NAMES:
+            w, g = want[n], got[n]
+            assert float(np.linalg.norm(g - w)) <= FLUX_TOL[1] * float(np.linalg.norm(w)), n
+
+
+def test_batched_cell_fluxes_need_the_option(gpu):
+    d = domain("coast")
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, d.tracer(3, 1.0, 0.5, seed=2))
+    b.step(advdiff.params(DTProp=30.0))
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        b.cell_fluxes(0)
+    assert ei.value.code == 3
+    b.step(advdiff.params(DTProp=30.0, CellFluxes=1))
+    b.cell_fluxes(0)
+    b.set_tracer(0, d.tracer(3, 1.0, 0.5, seed=3))       # the buffers no longer hold that step
+    with pytest.raises(advdiff.N.MohidAdError) as ei:
+        b.cell_fluxes(0)
+    assert ei.value.code == 3
+    b.destroy()
+    ad.kill()
+
+
 def test_batched_noflux_rejected_with_references(gpu):
     from tests.cases import noflux_masks
     d = domain("open")

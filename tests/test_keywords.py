@@ -121,3 +121,49 @@ def test_options_drive_the_oracle(built):
         R = dom.reference(2.0, 0.3, seed=2)
         assert O.step(dom, P, O.params(**p), ReferenceProp=R) == 0
         assert np.isfinite(P).all()
+
+
+def test_batch_plan():
+    text = """ADV_METHOD_H : 4
+TVD_LIMIT_H : 4
+<beginproperty>
+NAME : temperature
+<endproperty>
+<beginproperty>
+NAME : salinity
+<endproperty>
+<beginproperty>
+NAME : fecal coliforms
+DECAY_TIME : 86400.
+<endproperty>
+<beginproperty>
+NAME : oxygen
+DISCHARGES : 1
+<endproperty>
+<beginproperty>
+NAME : nitrate
+DISCHARGES : 1
+<endproperty>
+<beginproperty>
+NAME : ammonia
+ADVECTION_H_IMP_EXP : 0
+<endproperty>
+<beginproperty>
+NAME : sediment
+BOUNDARY_CONDITION : 6
+<endproperty>
+<beginproperty>
+NAME : chlorophyll
+ADVECTION_NUDGING : 1
+<endproperty>
+<beginproperty>
+NAME : age
+ADVECTION_DIFFUSION : 0
+<endproperty>
+"""
+    plan = K.batch_plan(K.EnterData(text))
+    # equal options share a batch; decay time and discharges make their own;
+    # implicit horizontal advection, Orlanski and nudging go to the plain form;
+    # untransported properties appear nowhere
+    assert plan.batches == [["temperature", "salinity"], ["fecal coliforms"], ["oxygen", "nitrate"]]
+    assert plan.plain == ["ammonia", "sediment", "chlorophyll"]
