@@ -423,26 +423,29 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
 
 /* Autotuner.  No counterpart in the reference.  Times each launch schedule of
  * the batch on the batch itself and keeps the fastest.  The schedules are one
- * CTA per 32 x 8 tile, or a persistent grid over the tiles that hold water with
- * the deepest first (the column-length-aware schedule for z-level domains);
- * with 4 or more tracers, 4 or 2 tracers per launch (with 8 or more also 8,
- * with 10 or more also 10).
+ * CTA per tile, or a persistent grid over the tiles that hold water with the
+ * deepest first (the column-length-aware schedule for z-level domains); tiles
+ * of 32 columns by 8 or by 4 rows (a warp per row); with 4 or more tracers, 4
+ * or 2 tracers per launch (with 8 or more also 8, with 10 or more also 10).
  * Each candidate runs a warm-up and two timed steps that leave the tracers
  * unchanged.  The first mohid_ad_batched_step of a batch runs it; call it
  * again after a change that
  * may favour another schedule. */
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat);
 
-/* Set the schedule by hand (*sched 0 or 1, *split 10, 8, 4 or 2) instead of the autotuner. */
-int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat);
+/* Set the schedule by hand (*sched 0 or 1, *split 10, 8, 4 or 2, *tile_rows 8
+ * or 4; tile_rows NULL keeps the tile height) instead of the autotuner. */
+int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, const int* tile_rows,
+                                  int* stat);
 
 /* The schedule in use: kernel launches per step (the step kernels, and with
  * open boundaries the boundary flux and the mass fixer's finish), schedule (0
  * one CTA per tile, 1 tile list), largest tracer group per launch, and
  * launches made once per mohid_ad_batched_step call (the mass fixer's finish on
- * closed domains, which runs after the call's last step only).  Any output
- * pointer may be NULL. */
-int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call, int* stat);
+ * closed domains, which runs after the call's last step only), and the tile
+ * height (rows of 32 columns).  Any output pointer may be NULL. */
+int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call,
+                              int* tile_rows, int* stat);
 
 /* Mass fixer (*on != 0, the default).  No counterpart in the reference, whose
  * FP64 arithmetic conserves mass to round-off; it restores that for the FP32

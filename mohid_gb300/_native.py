@@ -112,8 +112,8 @@ _AD_SIGS = {
     "mohid_ad_get_dif_flux": (C.c_int, [c_int_p, C.c_void_p, C.c_void_p, C.c_void_p, c_int_p, c_int_p]),
     "mohid_ad_batched_set_mass_fix": (C.c_int, [c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_autotune": (C.c_int, [c_int_p, C.POINTER(MohidAdParams), c_int_p]),
-    "mohid_ad_batched_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
-    "mohid_ad_batched_set_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    "mohid_ad_batched_set_schedule": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "mohid_ad_batched_sync": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_batched_destroy": (C.c_int, [c_int_p, c_int_p]),
     "mohid_ad_ensemble_create": (C.c_int, [c_int_p, c_int_p, c_int_p, c_int_p]),

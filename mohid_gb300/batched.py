@@ -81,20 +81,25 @@ class Batch:
         N.check(self.lib.mohid_ad_batched_autotune(C.byref(self._bid), C.byref(p), C.byref(st)),
                 "mohid_ad_batched_autotune")
 
-    def set_schedule(self, sched: int, split: int = 4):
-        """Fix the launch schedule by hand (0 one CTA per tile, 1 tile list; 10, 8, 4 or 2 tracers per launch)."""
+    def set_schedule(self, sched: int, split: int = 4, rows: int | None = None):
+        """Fix the launch schedule by hand (0 one CTA per tile, 1 tile list; 10, 8, 4 or 2 tracers per
+        launch; tiles of 8 or 4 rows, None keeps the height)."""
         st = C.c_int(0)
+        r = C.byref(C.c_int(rows)) if rows is not None else None
         N.check(self.lib.mohid_ad_batched_set_schedule(C.byref(self._bid), C.byref(C.c_int(sched)),
-                                                       C.byref(C.c_int(split)), C.byref(st)),
+                                                       C.byref(C.c_int(split)), r, C.byref(st)),
                 "mohid_ad_batched_set_schedule")
 
     def schedule(self) -> dict:
         """{'launches': kernel launches per step, 'sched': 0 grid / 1 tile list, 'split': 10, 8, 4 or 2,
-        'per_call': launches made once per step() call (the closed-domain mass fixer's finish)}."""
-        n, sc, sp, pc, st = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        'per_call': launches made once per step() call (the closed-domain mass fixer's finish),
+        'rows': tile height (rows of 32 columns)}."""
+        n, sc, sp, pc, ro, st = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
         N.check(self.lib.mohid_ad_batched_schedule(C.byref(self._bid), C.byref(n), C.byref(sc), C.byref(sp),
-                                                   C.byref(pc), C.byref(st)), "mohid_ad_batched_schedule")
-        return {"launches": n.value, "sched": sc.value, "split": sp.value, "per_call": pc.value}
+                                                   C.byref(pc), C.byref(ro), C.byref(st)),
+                "mohid_ad_batched_schedule")
+        return {"launches": n.value, "sched": sc.value, "split": sp.value, "per_call": pc.value,
+                "rows": ro.value}
 
     def set_mass_fix(self, on: bool):
         """Mass fixer on (default) or off (mohid_ad_batched_set_mass_fix)."""

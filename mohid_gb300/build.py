@@ -30,9 +30,11 @@ CUDA_UNITS = [
     ("batched_flux.cu", []),
 ] + [
     # the batched step's kernels: one unit per form (closed, MassConservation
-    # open boundaries, every boundary treatment and discharges) and storage
-    ("batched_inst.cu", [f"-DMOHID_INST_OBC={o}", f"-DMOHID_INST_STORAGE={st}"], f"batched_inst_{o}{st}")
-    for o in (0, 1, 2) for st in (0, 1, 2)
+    # open boundaries, every boundary treatment and discharges), storage and
+    # tile height
+    ("batched_inst.cu", [f"-DMOHID_INST_OBC={o}", f"-DMOHID_INST_STORAGE={st}", f"-DMOHID_INST_TY={ty}"],
+     f"batched_inst_{o}{st}_{ty}")
+    for o in (0, 1, 2) for st in (0, 1, 2) for ty in (8, 4)
 ] + [
     ("ensemble_kernel.cu", []),
     ("batched_pack.cu", []),

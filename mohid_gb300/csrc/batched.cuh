@@ -15,7 +15,9 @@ namespace mohid {
 constexpr int kXOff = 31;
 constexpr int kYOff = 2;
 constexpr int kTX = 32;   // tile width along i (one warp)
-constexpr int kTY = 8;    // tile height along j (warps per CTA)
+constexpr int kTY = 8;    // tile height along j (warps per CTA): the largest, and the ensembles'
+// the tile heights the single-domain kernels are built for (the autotuner's choice)
+constexpr int kTileRows[2] = {8, 4};
 
 // cell flag bits; F_NDW / F_NAW: the cell's bottom face carries no diffusion /
 // no advection (NoDifFlux / NoAdvFlux with NoFluxW, set by noflux_flags)
@@ -136,12 +138,13 @@ struct TmaMaps {
 };
 
 // tiles == null: one CTA per tile of the grid; otherwise a persistent grid over
-// the ntl (bx, by) tiles listed
+// the ntl (bx, by) tiles listed.  ty: the tile height (kTileRows); the maps'
+// boxes and the argument's tile counts must be those of that height
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                           bool halfK, const int2* tiles, int ntl, cudaStream_t s);
-// per tile (by * tilesX + bx): layers the walk visits, 0 for a tile without water
-cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int* cost,
-                       cudaStream_t s);
+                           bool halfK, const int2* tiles, int ntl, int ty, cudaStream_t s);
+// per tile (by * tilesX + bx) of 32 x ty cells: layers the walk visits, 0 for a tile without water
+cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int ty,
+                       int* cost, cudaStream_t s);
 size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk);
 // ensemble: one persistent grid over the (domain, bx, by, -) tiles of many
 // domains with FP32 storage; As/Ms are device tables indexed by domain
@@ -152,9 +155,10 @@ cudaError_t launch_ensemble(const BatchArgs* As, const TmaMaps* Ms, const int4* 
 cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s);
 // resident CTAs of the ensemble kernel on `device` (0 on error)
 int ensemble_slots(int nt, int method, int limiter, int device);
-// box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order
+// box extents (elements, x y z w) of the kNumMaps maps in TmaMaps order, for
+// tiles of 32 x ty cells
 constexpr int kNumMaps = 13;
-void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4]);
+void batched_boxes(bool halfQ, bool halfK, int nt, int ty, int box[kNumMaps][4]);
 
 // packing (Fortran FP64 Size box <-> batched layout)
 // All hydrodynamic fields of one update in one pass: transports and

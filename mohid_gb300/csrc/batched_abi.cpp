@@ -72,16 +72,20 @@ struct Batch {
     bool packingMasks = true;            // the pack in flight formed flags and schedule from the masks
     DevBuf<double> vpart;                // per-block water-volume sums of the pack
     bool fixDirty = false;               // the device constants / corrections differ from `shift`
-    int tilesX = 0, ntiles = 0;
     // launch schedule: one CTA per tile, or a persistent grid over the tiles
-    // holding water, costliest first; tracers per launch; chosen by timing
-    DevBuf<int2> tl;
-    DevBuf<int> tcost;
-    int ntl = 0;
+    // holding water, costliest first; tracers per launch; the tile height
+    // (kTileRows[th]); chosen by timing.  Tile counts, lists, costs and
+    // tensor maps are kept for each height (index h of kTileRows)
+    int tilesX = 0, ntiles[2] = {0, 0};
+    DevBuf<int2> tl[2];
+    DevBuf<int> tcost[2];
+    int ntl[2] = {0, 0};
     int sched = 0;                       // 0 grid, 1 tile list
     int split = 4;                       // largest tracer group per launch: 10, 8, 4 or 2
+    int th = 0;                          // tile height in use: kTileRows[th] rows
+    int sumsTh = 0;                      // the height the fixer's per-tile sums are laid out for
     bool tuned = false;
-    int graphSched = -1, graphSplit = -1;
+    int graphSched = -1, graphSplit = -1, graphTh = -1;
     int graphFix = -1;                   // fixer / open-boundary launches the graph holds
     bool graphLast = false;              // the graph ends with the call's last step
     unsigned graphPack = ~0u;            // packed hydrodynamics the graph's arguments hold
@@ -102,7 +106,7 @@ struct Batch {
         double contDT;
     };
     PackHost* hp = nullptr;              // pinned
-    int* hcost = nullptr;                // pinned, per tile
+    int* hcost[2] = {nullptr, nullptr};  // pinned, per tile of each height
     DevBuf<float> dscale, dinv;
     DevBuf<unsigned> vchanged;
     DevBuf<double> tpartial, tscratch;   // scratch of the tracer loads
@@ -136,8 +140,9 @@ struct Batch {
     unsigned packedVersion = ~0u;
     DevBuf<double> partial, scratch, stage;
     double* hmass = nullptr;             // pinned
-    mohid::TmaMaps maps{};               // shared-field maps (valid after a pack)
-    CUtensorMap mapP[2][5];              // tracer maps: input buffer (A/B) x group size (1, 2, 4, 8, 10)
+    mohid::TmaMaps maps[2]{};            // shared-field maps per tile height (valid after a pack)
+    CUtensorMap mapP[2][2][5];           // tracer maps: tile height x input buffer (A/B) x group size
+                                         // (1, 2, 4, 8, 10)
     bool mapsOk = false;
     cudaGraphExec_t graph = nullptr;
     int graphSteps = 0;
@@ -157,12 +162,14 @@ struct Batch {
         dStart.release(); dTerms.release(); dConc.release();
         mfix.release(); mpart.release(); moving.release(); Vprev.release(); vpart.release(); fluxOut.release();
         obpart.release(); obcol.release(); obcnt.release();
-        tl.release(); tcost.release();
+        for (int h = 0; h < 2; ++h) { tl[h].release(); tcost[h].release(); }
         dscale.release(); dinv.release(); vchanged.release(); tpartial.release(); tscratch.release();
         if (hp) cudaFreeHost(hp);
-        if (hcost) cudaFreeHost(hcost);
+        for (int h = 0; h < 2; ++h) {
+            if (hcost[h]) cudaFreeHost(hcost[h]);
+            hcost[h] = nullptr;
+        }
         hp = nullptr;
-        hcost = nullptr;
         if (cs) cudaStreamDestroy(cs);
         if (packEv) cudaEventDestroy(packEv);
         cs = nullptr;
@@ -393,11 +400,14 @@ int pack_enqueue(Batch* b, int* stat)
         CK(mohid::pack_columns(in->DUX.p, in->DVY.p, in->DZX.p, in->DZY.p, in->KFloor.p, in->BP2D.p,
                                in->WP.p, in->OP.p, in->CFW.p, in->hasSD ? in->SD.p : nullptr,
                                b->fc.p, b->areaCol.p, b->kfloor.p, b->cflag.p, L, s));
-        CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles, b->tcost.p, s));
+        for (int h = 0; h < 2; ++h) {
+            CK(mohid::tile_costs(b->cflag.p, b->kfloor.p, L, b->tilesX, b->ntiles[h], mohid::kTileRows[h],
+                                 b->tcost[h].p, s));
+            CK(cudaMemcpyAsync(b->hcost[h], b->tcost[h].p, sizeof(int) * b->ntiles[h], cudaMemcpyDeviceToHost, s));
+        }
         CK(mohid::obc_columns(b->cflag.p, L, b->obcnt.p, b->obcol.p, s));
         // tiles left out of a schedule keep no stale mass-fixer sums
-        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles, s));
-        CK(cudaMemcpyAsync(b->hcost, b->tcost.p, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles[1], s));
     }
     b->packingMasks = masks;
     b->packingMask = in->maskVersion;
@@ -411,9 +421,10 @@ int pack_enqueue(Batch* b, int* stat)
         CK(cudaMemcpyAsync(&b->hp->cont, b->scratch.p + 5, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(b->packEv, s));
     // tensor maps of the shared fields and of the tracer buffers (host only)
-    {
+    for (int h = 0; h < 2; ++h) {
+        const int ty = mohid::kTileRows[h];
         int box[mohid::kNumMaps][4];
-        mohid::batched_boxes(hq, hk, 1, box);
+        mohid::batched_boxes(hq, hk, 1, ty, box);
         const CUtensorMapDataType tq = hq ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         const CUtensorMapDataType tk = hk ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         const int eq = hq ? 2 : 4, ek = hk ? 2 : 4;
@@ -423,7 +434,7 @@ int pack_enqueue(Batch* b, int* stat)
         const void* vis = hk ? (const void*)b->Vis16.p : (const void*)b->Vis32.p;
         const void* dif = hk ? (const void*)b->Dif16.p : (const void*)b->Dif32.p;
         bool okm = true;
-        mohid::TmaMaps& M = b->maps;
+        mohid::TmaMaps& M = b->maps[h];
         okm &= encode_map(&M.F, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, b->fflag.p, L, 1, box[1]);
         okm &= encode_map(&M.V, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b->RV.p, L, 1, box[2]);
         okm &= encode_map(&M.Vis, tk, ek, vis, L, 1, box[3]);
@@ -441,13 +452,13 @@ int pack_enqueue(Batch* b, int* stat)
             for (int g = 0; g < 5; ++g) {
                 if (gs[g] > b->nt) continue;
                 int bb[mohid::kNumMaps][4];
-                mohid::batched_boxes(hq, hk, gs[g], bb);
-                okm &= encode_map(&b->mapP[buf][g], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                mohid::batched_boxes(hq, hk, gs[g], ty, bb);
+                okm &= encode_map(&b->mapP[h][buf][g], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                                   buf ? b->PB.p : b->PA.p, L, b->nt, bb[0], 4);
             }
         if (!okm) return fail(MOHID_AD_ERR_CUDA, stat, "cuTensorMapEncodeTiled failed");
-        b->mapsOk = true;
     }
+    b->mapsOk = true;
     b->packPending = true;
     b->packingVersion = in->hydroVersion;
     return ok(stat);
@@ -487,15 +498,21 @@ int pack_finalize(Batch* b, int* stat)
         b->packedVersion = b->packingVersion;
         return ok(stat);
     }
-    // tile schedule: tiles holding water, most layers first (stable by tile index)
-    std::vector<int> order;
-    for (int q = 0; q < b->ntiles; ++q)
-        if (b->hcost[q] > 0) order.push_back(q);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->hcost[x] > b->hcost[y]; });
-    std::vector<int2> list(order.size());
-    for (size_t q = 0; q < order.size(); ++q) list[q] = make_int2(order[q] % b->tilesX, order[q] / b->tilesX);
-    b->ntl = (int)list.size();
-    if (b->ntl) CK(cudaMemcpy(b->tl.p, list.data(), sizeof(int2) * list.size(), cudaMemcpyHostToDevice));
+    // tile schedules of both heights: tiles holding water, most layers first
+    // (stable by tile index)
+    for (int h = 0; h < 2; ++h) {
+        const int* hc = b->hcost[h];
+        std::vector<int> order;
+        for (int q = 0; q < b->ntiles[h]; ++q)
+            if (hc[q] > 0) order.push_back(q);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hc[x] > hc[y]; });
+        std::vector<int2> list(order.size());
+        for (size_t q = 0; q < order.size(); ++q) list[q] = make_int2(order[q] % b->tilesX, order[q] / b->tilesX);
+        b->ntl[h] = (int)list.size();
+        if (b->ntl[h])
+            CK(cudaMemcpy(b->tl[h].p, list.data(), sizeof(int2) * list.size(), cudaMemcpyHostToDevice));
+    }
+    b->sumsTh = -1;                              // the memset above cleared the per-tile sums
     b->preCont = h.cont;
     b->preContDT = h.contDT;
     b->preContVersion = b->packingVersion;
@@ -576,7 +593,7 @@ mohid::BatchArgs make_bargs(Batch* b, const mohid_ad_params* p, int t0, int nt, 
     a.obpart = fix_active(b) && b->hasRef ? b->obpart.p : nullptr;
     a.nob = mohid::kObcBlocks;
     a.tilesX = b->tilesX;
-    a.ntiles = b->ntiles;
+    a.ntiles = b->ntiles[b->ensemble ? 0 : b->th];   // ensembles walk 8-row tiles
     a.ntAll = b->nt;
     a.DT = (float)p->DTProp;
     a.schmidtH = (float)p->schmidt_H;
@@ -696,15 +713,16 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
     const bool sums = last;
     const float* Pin = b->cur_in();
     float* Pout = b->cur_out();
-    const int2* tiles = (b->sched == 1 && b->ntl > 0) ? b->tl.p : nullptr;
+    const int h = b->th;
+    const int2* tiles = (b->sched == 1 && b->ntl[h] > 0) ? b->tl[h].p : nullptr;
     int t0 = 0;
     while (t0 < b->nt) {
         const int g = group_size(b, b->nt - t0);
         mohid::BatchArgs a = make_bargs(b, p, t0, g, Pin, Pout, sums);
-        mohid::TmaMaps m = b->maps;
-        m.P = b->mapP[b->cur ? 1 : 0][map_index(g)];
+        mohid::TmaMaps m = b->maps[h];
+        m.P = b->mapP[h][b->cur ? 1 : 0][map_index(g)];
         cudaError_t e = mohid::launch_batched(a, m, p->AdvMethodH, p->TVDLimitationH, b->storage >= 1,
-                                              b->storage >= 2, tiles, b->ntl, s);
+                                              b->storage >= 2, tiles, b->ntl[h], mohid::kTileRows[h], s);
         if (e != cudaSuccess) return e;
         t0 += g;
     }
@@ -731,7 +749,7 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
         if (b->hasRef)                           // the target follows the boundary flux
             e = mohid::obc_flux(make_bargs(b, p, 0, b->nt, Pin, Pout), b->obcol.p, b->storage >= 1, s);
         if (e == cudaSuccess)
-            e = mohid::mass_fix_step(sums ? b->mpart.p : nullptr, b->ntiles, b->nt, b->mfix.p,
+            e = mohid::mass_fix_step(sums ? b->mpart.p : nullptr, b->ntiles[h], b->nt, b->mfix.p,
                                      b->hasRef ? b->obpart.p : nullptr, mohid::kObcBlocks, s);
         if (e != cudaSuccess) return e;
     } else if (!fix_active(b) && b->hasRef) {
@@ -744,40 +762,44 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
 }
 
 // Autotuner: time every candidate launch schedule (one CTA per tile, or the
-// persistent tile list) and tracer grouping (4 or 2 per launch when there are
-// 4 or more tracers) on the batch itself -- a warm-up step and two timed steps
-// each, which leave the tracer state as it was -- and keep the fastest.
+// persistent tile list), tile height (8 or 4 rows of 32 columns) and tracer
+// grouping (4 or 2 per launch when there are 4 or more tracers, 8 and 10 with
+// as many) on the batch itself -- a warm-up step and two timed steps each,
+// which leave the tracer state as it was -- and keep the fastest.
 int autotune(Batch* b, const mohid_ad_params* p, int* stat)
 {
     cudaStream_t s = b->in->stream;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int bestSched = 0, bestSplit = 4;
+    int bestSched = 0, bestSplit = 4, bestTh = 0;
     float best = 1e30f;
     cudaError_t err = cudaSuccess;
     for (int split : {10, 8, 4, 2}) {
         if ((split == 10 && b->nt < 10) || (split == 8 && b->nt < 8) || (split == 2 && b->nt < 4)) continue;
-        for (int sched : {0, 1}) {
-            if (sched == 1 && b->ntl == 0) continue;
-            b->sched = sched;
-            b->split = split;
-            err = enqueue_step(b, p, s, false, false);
-            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-            for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false, false);
-            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-            if (err != cudaSuccess) break;
-            if (ms < best) { best = ms; bestSched = sched; bestSplit = split; }
-        }
+        for (int h = 0; h < 2 && err == cudaSuccess; ++h)
+            for (int sched : {0, 1}) {
+                if (sched == 1 && b->ntl[h] == 0) continue;
+                b->sched = sched;
+                b->split = split;
+                b->th = h;
+                err = enqueue_step(b, p, s, false, false);
+                if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+                for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false, false);
+                if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                if (err != cudaSuccess) break;
+                if (ms < best) { best = ms; bestSched = sched; bestSplit = split; bestTh = h; }
+            }
         if (err != cudaSuccess) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     b->sched = bestSched;
     b->split = bestSplit;
+    b->th = bestTh;
     if (err != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("autotune", err));
     b->tuned = true;
     return ok(stat);
@@ -912,20 +934,23 @@ int mohid_ad_batched_create(int* bid, const int* id, const int* ntracers, const 
         if ((e = b->Gsc.alloc(n3 * (size_t)gmax)) != cudaSuccess) return bad(e, "cudaMalloc");
     }
     b->tilesX = (in->ni + mohid::kTX - 1) / mohid::kTX;
-    b->ntiles = b->tilesX * ((in->nj + mohid::kTY - 1) / mohid::kTY);
+    for (int h = 0; h < 2; ++h)
+        b->ntiles[h] = b->tilesX * ((in->nj + mohid::kTileRows[h] - 1) / mohid::kTileRows[h]);
     if ((e = b->Vhi.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Vlo.alloc(n3)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->mfix.alloc(1 + 4 * (size_t)b->nt)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->obpart.alloc((size_t)(b->nt + 1) * mohid::kObcBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->obcol.alloc(n2 + 1)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->obcnt.alloc(mohid::kObcBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = cudaMallocHost((void**)&b->hcost, sizeof(int) * (size_t)b->ntiles)) != cudaSuccess)
-        return bad(e, "cudaMallocHost");
+    if ((e = b->mpart.alloc((size_t)b->nt * b->ntiles[1])) != cudaSuccess) return bad(e, "cudaMalloc");
+    for (int h = 0; h < 2; ++h) {
+        if ((e = cudaMallocHost((void**)&b->hcost[h], sizeof(int) * (size_t)b->ntiles[h])) != cudaSuccess)
+            return bad(e, "cudaMallocHost");
+        if ((e = b->tl[h].alloc(b->ntiles[h])) != cudaSuccess) return bad(e, "cudaMalloc");
+        if ((e = b->tcost[h].alloc(b->ntiles[h])) != cudaSuccess) return bad(e, "cudaMalloc");
+    }
     if ((e = b->moving.alloc(1)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->Vprev.alloc(in->n3)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->tl.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
-    if ((e = b->tcost.alloc(b->ntiles)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->partial.alloc(2 * kMassBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->vpart.alloc(2 * kPackBlocks)) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = b->scratch.alloc(8)) != cudaSuccess) return bad(e, "cudaMalloc");
@@ -1132,6 +1157,11 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
         if (c) return c;
     }
     if (fix_active(b)) b->fixDirty = true;
+    // the fixer's per-tile sums are laid out by the tile height in use; the
+    // tiles a list schedule leaves out must read zero in that layout
+    if (b->sumsTh != -1 && b->sumsTh != b->th)
+        CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles[1], s));
+    b->sumsTh = b->th;
     auto done = [&]() {
         b->fluxLast = p->CellFluxes != 0;
         if (b->fluxLast) b->fluxParams = *p;
@@ -1148,7 +1178,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
     if (pairs > 0) {
         const bool glast = *nsteps % 2 == 0;          // the graph holds the call's last step
         const bool reuse = b->graph && b->graphSteps == 2 * pairs && b->graphCur == b->cur &&
-                           b->graphSched == b->sched && b->graphSplit == b->split &&
+                           b->graphSched == b->sched && b->graphSplit == b->split && b->graphTh == b->th &&
                            b->graphFix == fix_key(b) && b->graphLast == glast &&
                            b->graphPack == b->packedVersion &&
                            b->graphDisch == (b->dischOn ? b->dischUploads : ~0u) &&
@@ -1173,6 +1203,7 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
             b->graphParams = *p;
             b->graphSched = b->sched;
             b->graphSplit = b->split;
+            b->graphTh = b->th;
             b->graphFix = fix_key(b);
             b->graphLast = glast;
             b->graphPack = b->packedVersion;
@@ -1209,20 +1240,29 @@ int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* sta
     return autotune(b, p, stat);
 }
 
-int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, int* stat)
+int mohid_ad_batched_set_schedule(const int* bid, const int* sched, const int* split, const int* tile_rows,
+                                  int* stat)
 {
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
     if (!sched || !split) return fail(MOHID_AD_ERR_NULLPTR, stat, "NULL argument");
     if ((*sched != 0 && *sched != 1) || (*split != 10 && *split != 8 && *split != 4 && *split != 2))
         return fail(MOHID_AD_ERR_OPTION, stat, "schedule must be 0 or 1 and split 10, 8, 4 or 2");
+    int th = b->th;
+    if (tile_rows) {
+        if (*tile_rows == mohid::kTileRows[0]) th = 0;
+        else if (*tile_rows == mohid::kTileRows[1]) th = 1;
+        else return fail(MOHID_AD_ERR_OPTION, stat, "tile_rows must be 8 or 4");
+    }
     b->sched = *sched;
     b->split = *split;
+    b->th = th;
     b->tuned = true;
     return ok(stat);
 }
 
-int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call, int* stat)
+int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* split, int* per_call,
+                              int* tile_rows, int* stat)
 {
     Batch* b = blookup(bid);
     if (!b) return fail(MOHID_AD_ERR_ID, stat, "unknown batch id");
@@ -1230,6 +1270,7 @@ int mohid_ad_batched_schedule(const int* bid, int* launches, int* sched, int* sp
     if (per_call) *per_call = launches_per_call(b);
     if (sched) *sched = b->sched;
     if (split) *split = b->split;
+    if (tile_rows) *tile_rows = mohid::kTileRows[b->th];
     return ok(stat);
 }
 
@@ -1469,6 +1510,9 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
         if (c) return c;
         if (fix_active(b)) b->fixDirty = true;
         if (b->cur != E->cur) return fail(MOHID_AD_ERR_OPTION, stat, "a member was stepped outside the ensemble");
+        if (b->sumsTh != -1 && b->sumsTh != 0)     // ensembles walk 8-row tiles
+            CK(cudaMemsetAsync(b->mpart.p, 0, sizeof(double) * (size_t)b->nt * b->ntiles[1], b->in->stream));
+        b->sumsTh = 0;
     }
     // members' own streams (packing, tracer loads) before the ensemble's
     for (size_t q = 0; q < n; ++q)
@@ -1485,8 +1529,8 @@ int mohid_ad_ensemble_step(const int* eid, const mohid_ad_params* p, const int* 
             float* Pout = c ? b->PA.p : b->PB.p;
             for (int l = 0; l < 2; ++l)
                 hA[(c * 2 + l) * n + q] = make_bargs(b, &p[q], 0, b->nt, Pin, Pout, l == 1);
-            hM[c * n + q] = b->maps;
-            hM[c * n + q].P = b->mapP[c][gi];
+            hM[c * n + q] = b->maps[0];              // ensembles walk 8-row tiles
+            hM[c * n + q].P = b->mapP[0][c][gi];
         }
     const bool same = E->uploaded && std::memcmp(hA.data(), E->hA.data(), hA.size() * sizeof(hA[0])) == 0 &&
                       std::memcmp(hM.data(), E->hM.data(), hM.size() * sizeof(hM[0])) == 0;

@@ -8,6 +8,7 @@ using namespace tile;
 namespace {
 
 // tile cost for the schedule: layers walked (KUB - lowest KFloor + 1), 0 without water
+template <int TY>
 __global__ void k_tile_cost(const uint8_t* cflag, const int* kfloor, BLayout L, int tilesX, int ntiles, int* cost)
 {
     const int tile = blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,9 +43,18 @@ __global__ void k_wait_probe(uint32_t polls, unsigned* status)
 template <int NT>
 size_t smem_n(bool halfQ, bool halfK, int nk)
 {
-    if (halfQ && halfK) return Smem<NT, __half, __half>::bytes(nk);
-    if (halfQ) return Smem<NT, __half, float>::bytes(nk);
-    return Smem<NT, float, float>::bytes(nk);
+    if (halfQ && halfK) return Smem<NT, __half, __half, kTY>::bytes(nk);
+    if (halfQ) return Smem<NT, __half, float, kTY>::bytes(nk);
+    return Smem<NT, float, float, kTY>::bytes(nk);
+}
+
+template <int OBC, int STORAGE>
+cudaError_t launch_ty(const BatchArgs& a, const TmaMaps& m, int method, int limiter, const int2* tiles, int ntl,
+                      int ty, cudaStream_t s)
+{
+    if (ty == 4) return launch_batched_unit<OBC, STORAGE, 4>(a, m, method, limiter, tiles, ntl, s);
+    if (ty == 8) return launch_batched_unit<OBC, STORAGE, 8>(a, m, method, limiter, tiles, ntl, s);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -59,28 +69,30 @@ cudaError_t wait_probe(unsigned polls, unsigned* status, cudaStream_t s)
 // MassConservation, take the form with every boundary treatment and the
 // discharge terms; MassConservation alone the form with its terms only
 cudaError_t launch_batched(const BatchArgs& a, const TmaMaps& m, int method, int limiter, bool halfQ,
-                           bool halfK, const int2* tiles, int ntl, cudaStream_t s)
+                           bool halfK, const int2* tiles, int ntl, int ty, cudaStream_t s)
 {
     const int storage = halfQ ? (halfK ? 2 : 1) : 0;
     if (a.dStart || (a.Ref && a.bc != 1)) {
-        if (storage == 2) return launch_batched_unit<2, 2>(a, m, method, limiter, tiles, ntl, s);
-        if (storage == 1) return launch_batched_unit<2, 1>(a, m, method, limiter, tiles, ntl, s);
-        return launch_batched_unit<2, 0>(a, m, method, limiter, tiles, ntl, s);
+        if (storage == 2) return launch_ty<2, 2>(a, m, method, limiter, tiles, ntl, ty, s);
+        if (storage == 1) return launch_ty<2, 1>(a, m, method, limiter, tiles, ntl, ty, s);
+        return launch_ty<2, 0>(a, m, method, limiter, tiles, ntl, ty, s);
     }
     if (a.Ref) {
-        if (storage == 2) return launch_batched_unit<1, 2>(a, m, method, limiter, tiles, ntl, s);
-        if (storage == 1) return launch_batched_unit<1, 1>(a, m, method, limiter, tiles, ntl, s);
-        return launch_batched_unit<1, 0>(a, m, method, limiter, tiles, ntl, s);
+        if (storage == 2) return launch_ty<1, 2>(a, m, method, limiter, tiles, ntl, ty, s);
+        if (storage == 1) return launch_ty<1, 1>(a, m, method, limiter, tiles, ntl, ty, s);
+        return launch_ty<1, 0>(a, m, method, limiter, tiles, ntl, ty, s);
     }
-    if (storage == 2) return launch_batched_unit<0, 2>(a, m, method, limiter, tiles, ntl, s);
-    if (storage == 1) return launch_batched_unit<0, 1>(a, m, method, limiter, tiles, ntl, s);
-    return launch_batched_unit<0, 0>(a, m, method, limiter, tiles, ntl, s);
+    if (storage == 2) return launch_ty<0, 2>(a, m, method, limiter, tiles, ntl, ty, s);
+    if (storage == 1) return launch_ty<0, 1>(a, m, method, limiter, tiles, ntl, ty, s);
+    return launch_ty<0, 0>(a, m, method, limiter, tiles, ntl, ty, s);
 }
 
-cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int* cost,
-                       cudaStream_t s)
+cudaError_t tile_costs(const uint8_t* cflag, const int* kfloor, const BLayout& L, int tilesX, int ntiles, int ty,
+                       int* cost, cudaStream_t s)
 {
-    k_tile_cost<<<(ntiles + 127) / 128, 128, 0, s>>>(cflag, kfloor, L, tilesX, ntiles, cost);
+    if (ty == 4) k_tile_cost<4><<<(ntiles + 127) / 128, 128, 0, s>>>(cflag, kfloor, L, tilesX, ntiles, cost);
+    else if (ty == 8) k_tile_cost<8><<<(ntiles + 127) / 128, 128, 0, s>>>(cflag, kfloor, L, tilesX, ntiles, cost);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
@@ -94,7 +106,7 @@ size_t batched_smem_bytes(int nt, bool halfQ, bool halfK, int nk)
 }
 
 // box extents of the tensor maps (elements), for the host-side encoder
-void batched_boxes(bool halfQ, bool halfK, int nt, int box[kNumMaps][4])
+void batched_boxes(bool halfQ, bool halfK, int nt, int TY, int box[kNumMaps][4])
 {
     const int qyX = halfQ ? Box<__half>::qyX : Box<float>::qyX;
     const int visX = halfK ? Box<__half>::visX : Box<float>::visX;

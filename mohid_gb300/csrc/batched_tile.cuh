@@ -44,8 +44,13 @@ namespace mohid {
 namespace tile {
 
 
-constexpr int TX = kTX, TY = kTY, NTH = TX * TY;
-constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
+constexpr int TX = kTX;
+// a tile is TX = 32 cells along i (the lanes of a warp) by TY rows along j
+// (one warp each): NTH threads, NWF west faces and NSF south faces
+template <int TY> struct TileGeom {
+    static constexpr int NTH = TX * TY;
+    static constexpr int NWF = (TY + 1) * TX, NSF = TY * (TX + 1);
+};
 
 // ---- TMA stage layout -------------------------------------------------------
 // Box origins sit on 16-byte boundaries of the batched layout (x = i + 31):
@@ -58,7 +63,7 @@ template <> struct Box<__half> { static constexpr int visX = 48, visOff = 8, qyX
 
 constexpr int al128(int b) { return (b + 127) / 128 * 128; }
 
-template <int NT, typename QT, typename KT>
+template <int NT, typename QT, typename KT, int TY>
 struct StageLayout {
     static constexpr int qyX = Box<QT>::qyX, visX = Box<KT>::visX;
     static constexpr int bP = NT * (TY + 4) * PBX * 4;
@@ -92,9 +97,10 @@ struct StageLayout {
         bP + bF + bV + bVis + bQX + bAU + bQY + bAV + bVo + bQz + bDv + bDz + bFn;
 };
 
-template <int NT, typename QT, typename KT>
+template <int NT, typename QT, typename KT, int TY>
 struct Smem {
-    using SL = StageLayout<NT, QT, KT>;
+    using SL = StageLayout<NT, QT, KT, TY>;
+    static constexpr int NTH = TileGeom<TY>::NTH, NWF = TileGeom<TY>::NWF, NSF = TileGeom<TY>::NSF;
     static constexpr int oStage0 = 0;
     static constexpr int oStage1 = SL::size;
     // face fluxes, double-buffered by layer parity: [FX | FY] x 2
@@ -328,14 +334,14 @@ __device__ __forceinline__ void l2_discard(const void* a)
 // P2_TVD limiters, theta = psi*(1-Cr)/2); diffusive flux
 // HorizontalDiffusionXX/YY AD:5185-5196 with Kx from
 // Convert_Visc_Dif_Horizontal AD:2487-2494.
-template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT>
+template <bool WEST, int NT, int METHOD, int LIM, typename QT, typename KT, int TY>
 __device__ __forceinline__ void face_flux(const unsigned char* st, float* out, const float4 cf, const BatchArgs& A,
                                           int pb, int vb, int visb, int qo, int ao, int fo)
 {
-    using SL = StageLayout<NT, QT, KT>;
+    using SL = StageLayout<NT, QT, KT, TY>;
     constexpr int pst = WEST ? PBX : 1, vst = WEST ? VBX : 1;
     constexpr int visst = WEST ? Box<KT>::visX : 1;
-    constexpr int cs = WEST ? NWF : NSF;
+    constexpr int cs = WEST ? TileGeom<TY>::NWF : TileGeom<TY>::NSF;
     constexpr int tst = (TY + 4) * PBX;              // tracer stride of the stage's tracer tile
     constexpr uint8_t ACT = WEST ? FU_ACT : FV_ACT, ADV = WEST ? FU_ADV : FV_ADV;
     constexpr uint8_t TVDP = WEST ? FU_TVDP : FV_TVDP, TVDN = WEST ? FU_TVDN : FV_TVDN;
@@ -423,10 +429,10 @@ struct WalkWords {
 };
 
 // once per CTA, before the first tile walk
-template <int NT, typename QT, typename KT>
+template <int NT, typename QT, typename KT, int TY>
 __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
 {
-    using SM = Smem<NT, QT, KT>;
+    using SM = Smem<NT, QT, KT, TY>;
     WalkWords* ww = reinterpret_cast<WalkWords*>(smem_raw + SM::oBar);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         ww->done = 0;
@@ -436,7 +442,7 @@ __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
     }
 }
 
-// One transport step of the 32 x 8 tile (bx, by) of one domain: the k-walk
+// One transport step of the 32 x TY tile (bx, by) of one domain: the k-walk
 // with the face fluxes and the THOMASZ factorisation, then the
 // back-substitution.  `phase` carries the stage parities from one walk to the
 // next in the same CTA.  Returns false when a stage never arrived (the status
@@ -451,12 +457,13 @@ __device__ __forceinline__ void walk_init(unsigned char* smem_raw)
 // open-boundary terms, 2 with every open-boundary treatment and the
 // discharges, so that no form carries the registers and code of terms it
 // does not apply (form 1 serves MassConservation batches and ensembles).
-template <int NT, int METHOD, int LIM, typename QT, typename KT, int OBC>
+template <int NT, int METHOD, int LIM, typename QT, typename KT, int OBC, int TY>
 __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, int bx, int by,
                                           unsigned char* smem_raw, uint32_t& phase)
 {
-    using SL = StageLayout<NT, QT, KT>;
-    using SM = Smem<NT, QT, KT>;
+    using SL = StageLayout<NT, QT, KT, TY>;
+    using SM = Smem<NT, QT, KT, TY>;
+    constexpr int NTH = TileGeom<TY>::NTH, NWF = TileGeom<TY>::NWF, NSF = TileGeom<TY>::NSF;
     constexpr int visX = Box<KT>::visX, visOff = Box<KT>::visOff;
     WalkWords* ww = reinterpret_cast<WalkWords*>(smem_raw + SM::oBar);
     uint64_t* bar = ww->bar;
@@ -593,10 +600,13 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
         // ---- faces of the tile at layer k: own west and south faces; the
         //      east row (warp 0) and north column (warp 1) close the tile
         if (horiz && ok) {
-            face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX + own, CX[own], A, pbO, vbO, visO, own, own, fO);
-            face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY + fs, CY[fs], A, pbO, vbO, visO, qyO, avO, fO);
-            if (xW) face_flux<true, NT, METHOD, LIM, QT, KT>(st, FX + fiX, CX[fiX], A, pbX, vbX, visXo, qoX, aoX, foX);
-            else if (xS) face_flux<false, NT, METHOD, LIM, QT, KT>(st, FY + fiX, CY[fiX], A, pbX, vbX, visXo, qoX, aoX, foX);
+            face_flux<true, NT, METHOD, LIM, QT, KT, TY>(st, FX + own, CX[own], A, pbO, vbO, visO, own, own, fO);
+            face_flux<false, NT, METHOD, LIM, QT, KT, TY>(st, FY + fs, CY[fs], A, pbO, vbO, visO, qyO, avO, fO);
+            if (xW)
+                face_flux<true, NT, METHOD, LIM, QT, KT, TY>(st, FX + fiX, CX[fiX], A, pbX, vbX, visXo, qoX, aoX, foX);
+            else if (xS)
+                face_flux<false, NT, METHOD, LIM, QT, KT, TY>(st, FY + fiX, CY[fiX], A, pbX, vbX, visXo, qoX, aoX,
+                                                              foX);
         }
         if (__syncthreads_or(!ok)) {               // a stage never arrived: leave cleanly
             if (tid == 0) {

@@ -14,6 +14,9 @@ namespace mohid {
 using namespace tile;
 namespace {
 
+constexpr int TY = kTY;                            // ensembles walk 32 x 8 tiles
+constexpr int NTH = TileGeom<TY>::NTH;
+
 template <int NT, int METHOD, int LIM, bool OBC>
 __global__ void __launch_bounds__(NTH, NT <= 2 ? 4 : 3)
 ensemble_kernel(const BatchArgs* __restrict__ As, const TmaMaps* __restrict__ Ms,
@@ -25,7 +28,7 @@ ensemble_kernel(const BatchArgs* __restrict__ As, const TmaMaps* __restrict__ Ms
     static_assert(sizeof(BatchArgs) % sizeof(int) == 0, "BatchArgs copied by words");
     const int tid = threadIdx.y * TX + threadIdx.x;
     uint32_t phase = 0;                            // bit s: parity of stage buffer s
-    walk_init<NT, float, float>(smem_raw);
+    walk_init<NT, float, float, TY>(smem_raw);
     int cur = -1;
     for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
         const int4 t = tiles[e];                   // (domain, bx, by, -)
@@ -36,7 +39,7 @@ ensemble_kernel(const BatchArgs* __restrict__ As, const TmaMaps* __restrict__ Ms
             __syncthreads();
             cur = t.x;
         }
-        if (!tile_walk<NT, METHOD, LIM, float, float, OBC>(sA, Ms[t.x], t.y, t.z, smem_raw, phase)) return;
+        if (!tile_walk<NT, METHOD, LIM, float, float, OBC, TY>(sA, Ms[t.x], t.y, t.z, smem_raw, phase)) return;
     }
 }
 
@@ -44,7 +47,7 @@ template <int NT, int METHOD, int LIM, bool OBC>
 cudaError_t ens_launch_t(const BatchArgs* As, const TmaMaps* Ms, const int4* tiles, int ntiles, int grid,
                          cudaStream_t s)
 {
-    const size_t smem = Smem<NT, float, float>::bytes(0);
+    const size_t smem = Smem<NT, float, float, TY>::bytes(0);
     auto kern = ensemble_kernel<NT, METHOD, LIM, OBC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -55,7 +58,7 @@ cudaError_t ens_launch_t(const BatchArgs* As, const TmaMaps* Ms, const int4* til
 template <int NT, int METHOD, int LIM>
 int ens_slots_t(int device)
 {
-    const size_t smem = Smem<NT, float, float>::bytes(0);
+    const size_t smem = Smem<NT, float, float, TY>::bytes(0);
     auto kern = ensemble_kernel<NT, METHOD, LIM, true>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
     int per = 0, sms = 0;

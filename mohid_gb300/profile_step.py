@@ -27,6 +27,7 @@ def main():
     ap.add_argument("--sched", type=int, default=-1,
                     help="batched schedule (0 one CTA per tile, 1 tile list) instead of the autotuner's choice")
     ap.add_argument("--split", type=int, default=4, help="largest tracer group per launch with --sched")
+    ap.add_argument("--rows", type=int, default=8, help="tile height (8 or 4) with --sched")
     ap.add_argument("--rebind", action="store_true",
                     help="batched form: a new hydrodynamic state before every step (the FP64 fields bound "
                          "again from device memory, then the repack), as a coupled time loop does")
@@ -47,7 +48,7 @@ def main():
         b = batched.Batch(ad, len(tr), args.storage)
         b.set_mass_fix(not args.no_mass_fix)
         if args.sched >= 0:
-            b.set_schedule(args.sched, args.split)   # no autotuner launches before the profiled ones
+            b.set_schedule(args.sched, args.split, args.rows)   # no autotuner launches before the profiled ones
         for t, P in enumerate(tr):
             b.set_tracer(t, P)
             if refs:
