@@ -653,7 +653,9 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             // from open cells enter E; each tracer's sources gather in shared
             // memory (dsrc, tracer stride NTH), read by the tracer loop below.
             // A water cell that is not open and takes an inflow restarts from
-            // P * Vold / V plus the source (dfill)
+            // P * Vold / V plus the source (dfill).  The _rn intrinsics fix the
+            // rounding, so that the walk's two inlined copies (grid and tile
+            // list) cannot contract these differently
             bool dis = false, dfill = false;
             float* dsrc = reinterpret_cast<float*>(smem_raw + SM::oDis) + tid;
             if (OBC == 2 && dq1 > dq0) {
@@ -661,6 +663,7 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                     const DischTerm T = A.dTerms[q];
                     if (T.k != k) continue;
                     const float fl = disch_flow(A, T, i, j, k);
+                    const float fdt = __fmul_rn(fl, dtv);
                     const float* cq = A.dConc + (long long)q * A.ntAll + A.t0;
                     if (!dis) {
                         for (int t = 0; t < NT; ++t) dsrc[t * NTH] = 0.f;
@@ -668,12 +671,13 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
                     }
                     if (open) {
                         if ((T.flags & 2) || fl > 0.f) {
-                            for (int t = 0; t < NT; ++t) dsrc[t * NTH] += fl * dtv * cq[t];
+                            for (int t = 0; t < NT; ++t)
+                                dsrc[t * NTH] = __fadd_rn(dsrc[t * NTH], __fmul_rn(fdt, cq[t]));
                         } else {
-                            E -= fl * dtv * (float)T.concMF;
+                            E = __fsub_rn(E, __fmul_rn(fdt, (float)T.concMF));
                         }
                     } else if (fl > 0.f) {
-                        for (int t = 0; t < NT; ++t) dsrc[t * NTH] = fl * dtv * cq[t];
+                        for (int t = 0; t < NT; ++t) dsrc[t * NTH] = __fmul_rn(fdt, cq[t]);
                         dfill = true;
                     }
                 }
@@ -718,7 +722,8 @@ __device__ __forceinline__ bool tile_walk(const BatchArgs& A, const TmaMaps& M, 
             for (int t = 0; t < NT; ++t) {
                 const float Pc = P[t * (TY + 4) * PBX + pbO];
                 float TI = Pc * ratio;
-                if (OBC == 2 && dis) TI = (dfill ? Pc * (1.f - dvr) : TI) + dsrc[t * NTH];
+                if (OBC == 2 && dis)
+                    TI = __fadd_rn(dfill ? __fmul_rn(Pc, __fsub_rn(1.f, dvr)) : TI, dsrc[t * NTH]);
                 if (horiz)
                     TI = fmaf(dtv, (FX[t * NWF + own] - FX[t * NWF + own + TX]) +
                                    (FY[t * NSF + fs] - FY[t * NSF + fs + 1]), TI);

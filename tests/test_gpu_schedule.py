@@ -108,3 +108,42 @@ def test_autotune_keeps_state(gpu):
         b.set_schedule(2, 4)
     b.destroy()
     ad.kill()
+
+
+@pytest.mark.parametrize("form", ["mass_conservation", "imposed_value", "discharges"])
+@pytest.mark.parametrize("storage", [batched.FP32, batched.FP16_QK])
+def test_tile_heights_agree_open(gpu, form, storage):
+    # the open-boundary forms (MassConservation alone; every boundary
+    # treatment with discharges) at both tile heights and both schedules: the
+    # same bits with the mass fixer off
+    from tests.cases import discharges
+    d = domain("open")
+    tr = [d.tracer(3, 1.0 + t, 0.5, seed=t) for t in range(3)]
+    refs = [d.reference(2.0 + t, 0.3, seed=10 + t) for t in range(3)]
+    pd = dict(PD, DTProp=30.0, BoundaryCondition=2 if form == "imposed_value" else 1)
+    ds = discharges(d, seed=1) if form == "discharges" else None
+
+    def run(sched, rows):
+        ad = advdiff.AdvectionDiffusion(d)
+        ad.set_hydro()
+        if ds is not None:
+            ad.set_discharges(ds)
+        b = batched.Batch(ad, len(tr), storage)
+        b.set_mass_fix(False)
+        for t, P in enumerate(tr):
+            b.set_tracer(t, P)
+            if ds is not None:
+                b.set_discharge_conc(t, ds["Conc"] * (t + 1))
+            b.set_reference(t, refs[t])
+        b.set_schedule(sched, 4, rows)
+        b.step(advdiff.params(**pd), nsteps=4, graph=True)
+        b.sync()
+        got = [b.get_tracer(t) for t in range(len(tr))]
+        b.destroy()
+        ad.kill()
+        return got
+
+    ref = run(0, 8)
+    for sched, rows in ((1, 8), (0, 4), (1, 4)):
+        for a, g in zip(ref, run(sched, rows)):
+            assert np.array_equal(a, g)
