@@ -428,9 +428,9 @@ int mohid_ad_batched_step(const int* bid, const mohid_ad_params* p, const int* n
  * of 32 columns by 8 or by 4 rows (a warp per row); with 4 or more tracers, 4
  * or 2 tracers per launch (with 8 or more also 8, with 10 or more also 10).
  * Each candidate runs a warm-up and two timed steps that leave the tracers
- * unchanged.  The first mohid_ad_batched_step of a batch runs it; call it
- * again after a change that
- * may favour another schedule. */
+ * unchanged, in two rounds over all candidates; each keeps its faster time.
+ * The first mohid_ad_batched_step of a batch runs it; call it again after a
+ * change that may favour another schedule. */
 int mohid_ad_batched_autotune(const int* bid, const mohid_ad_params* p, int* stat);
 
 /* Set the schedule by hand (*sched 0 or 1, *split 10, 8, 4 or 2, *tile_rows 8

@@ -765,41 +765,47 @@ cudaError_t enqueue_step(Batch* b, const mohid_ad_params* p, cudaStream_t s, boo
 // persistent tile list), tile height (8 or 4 rows of 32 columns) and tracer
 // grouping (4 or 2 per launch when there are 4 or more tracers, 8 and 10 with
 // as many) on the batch itself -- a warm-up step and two timed steps each,
-// which leave the tracer state as it was -- and keep the fastest.
+// which leave the tracer state as it was -- in two rounds over all the
+// candidates, and keep the one with the fastest of its two times (a single
+// round let clock ramp-up or one slow measurement pick a slower schedule).
 int autotune(Batch* b, const mohid_ad_params* p, int* stat)
 {
     cudaStream_t s = b->in->stream;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int bestSched = 0, bestSplit = 4, bestTh = 0;
-    float best = 1e30f;
-    cudaError_t err = cudaSuccess;
+    struct Cand { int split, h, sched; float ms; };
+    std::vector<Cand> cands;
     for (int split : {10, 8, 4, 2}) {
         if ((split == 10 && b->nt < 10) || (split == 8 && b->nt < 8) || (split == 2 && b->nt < 4)) continue;
-        for (int h = 0; h < 2 && err == cudaSuccess; ++h)
-            for (int sched : {0, 1}) {
-                if (sched == 1 && b->ntl[h] == 0) continue;
-                b->sched = sched;
-                b->split = split;
-                b->th = h;
-                err = enqueue_step(b, p, s, false, false);
-                if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-                for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false, false);
-                if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                float ms = 0.f;
-                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-                if (err != cudaSuccess) break;
-                if (ms < best) { best = ms; bestSched = sched; bestSplit = split; bestTh = h; }
-            }
-        if (err != cudaSuccess) break;
+        for (int h = 0; h < 2; ++h)
+            for (int sched : {0, 1})
+                if (sched == 0 || b->ntl[h] > 0) cands.push_back({split, h, sched, 1e30f});
     }
+    cudaError_t err = cudaSuccess;
+    for (int round = 0; round < 2 && err == cudaSuccess; ++round)
+        for (Cand& c : cands) {
+            b->sched = c.sched;
+            b->split = c.split;
+            b->th = c.h;
+            err = enqueue_step(b, p, s, false, false);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+            for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(b, p, s, false, false);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err != cudaSuccess) break;
+            c.ms = std::min(c.ms, ms);
+        }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->sched = bestSched;
-    b->split = bestSplit;
-    b->th = bestTh;
+    Cand best{4, 0, 0, 1e30f};
+    for (const Cand& c : cands)
+        if (c.ms < best.ms) best = c;
+    b->sched = best.sched;
+    b->split = best.split;
+    b->th = best.h;
     if (err != cudaSuccess) return fail(MOHID_AD_ERR_CUDA, stat, cuda_msg("autotune", err));
     b->tuned = true;
     return ok(stat);
