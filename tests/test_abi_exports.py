@@ -52,3 +52,23 @@ def test_default_params_cpu_callable(built):
     assert p.ImpExp_AdvV == 1.0 and p.ImpExp_DifV == 1.0 and p.Docycle_method == 1
     assert p.SchmidtBackground_V == 1e-8
     assert N.ad_lib().mohid_ad_version().startswith(b"mohid-gb300")
+
+
+def _prototypes():
+    """{name: parameter count} of every function include/*.h declares."""
+    out = {}
+    for h in (ROOT / "include").glob("*.h"):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(mohid_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt):
+            args = " ".join(m.group(2).split())
+            out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    # every binding passes as many arguments as its C prototype takes, so a
+    # signature change in the header cannot go unnoticed by the Python mirror
+    protos = _prototypes()
+    assert set(protos) == set(N.AD_SYMBOLS)
+    wrong = {n: (protos[n], len(N._AD_SIGS[n][1])) for n in protos if protos[n] != len(N._AD_SIGS[n][1])}
+    assert not wrong, wrong
