@@ -1,0 +1,101 @@
+"""Known answer independent of the reference's restatement: advection at
+Courant number 1 shifts a field by exactly one cell per step.
+
+On a single layer with V = VolumeZOld = 1, DT = 1, no diffusion and a
+transport of +1 (or -1) on every compute face of one direction, the explicit
+update of a cell is TI = P + F_in - F_out with F = Q * P_upwind, so a cell
+with compute faces on both sides takes its upstream neighbour's value; a cell
+against the upstream wall empties and the one against the downstream wall
+keeps its value plus the inflow.  With P2_TVD the weight 0.5 * psi * (1 - Cr)
+is 0 at Cr = +1, so every limiter gives the same shift for positive
+transports (for negative ones the reference's signed Courant number gives
+0.5 * psi * 2, which is not a shift; those run with upwind only).  Integer
+values keep every operation exact.
+"""
+import numpy as np
+import pytest
+
+from mohid_gb300 import advdiff, batched
+from oracle import oracle as O
+from tests.cases import domain
+
+SCHEMES = {
+    "upwind1": dict(),
+    "tvd_minmod": dict(AdvMethodH=4, TVDLimitationH=1, Upwind2H=1),
+    "tvd_vanleer": dict(AdvMethodH=4, TVDLimitationH=2, Upwind2H=1),
+    "tvd_muscl": dict(AdvMethodH=4, TVDLimitationH=3, Upwind2H=1),
+    "tvd_superbee": dict(AdvMethodH=4, TVDLimitationH=4, Upwind2H=1),
+    "tvd_pdm": dict(AdvMethodH=4, TVDLimitationH=5, Upwind2H=1),
+}
+CASES = [(ax, q, s) for ax in ("j", "i") for q in (1.0, -1.0) for s in SCHEMES if q > 0 or s == "upwind1"]
+
+
+def channel(axis, q):
+    """The single-layer test grid as a uniform channel along j (Wflux_X) or i
+    (Wflux_Y) with transport q on every compute face of that direction."""
+    d = domain("layer1", dt=1.0)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    a["VolumeZ"][...] = 1.0
+    a["VolumeZOld"][...] = 1.0
+    name, cf = ("Wflux_X", "ComputeFacesU3D") if axis == "j" else ("Wflux_Y", "ComputeFacesV3D")
+    a[name][...] = np.where(a[cf] == 1, q, 0.0)
+    P = np.zeros(d.shape3)
+    rng = np.random.default_rng(5)
+    P[1, 1:d.nj + 1, 1:d.ni + 1] = rng.integers(0, 64, size=(d.nj, d.ni)).astype(np.float64)
+    return d, P
+
+
+def shifted(d, P, axis, q):
+    """The closed-form result of one step (work-box cells of the layer)."""
+    a = d.arrays
+    cf = a["ComputeFacesU3D" if axis == "j" else "ComputeFacesV3D"][1]
+    L = P[1]
+    out = L.copy()
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            if axis == "j":
+                w, e, pw, pe = cf[j, i], cf[j + 1, i], L[j - 1, i], L[j + 1, i]
+            else:
+                w, e, pw, pe = cf[j, i], cf[j, i + 1], L[j, i - 1], L[j, i + 1]
+            p = L[j, i]
+            if q > 0:
+                out[j, i] = p * (1 - e) + pw * w if (w or e) else p
+            else:
+                out[j, i] = p * (1 - w) + pe * e if (w or e) else p
+    return out[1:d.nj + 1, 1:d.ni + 1]
+
+
+def params(s):
+    return dict(DTProp=1.0, SchmidtBackground_V=0.0, **SCHEMES[s])
+
+
+@pytest.mark.parametrize("axis,q,scheme", CASES)
+def test_oracle_shifts_one_cell(axis, q, scheme):
+    d, P = channel(axis, q)
+    want = shifted(d, P, axis, q)
+    assert not np.array_equal(want, P[1, 1:d.nj + 1, 1:d.ni + 1])      # the field moves
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**params(scheme))) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("axis,q,scheme", CASES)
+def test_gpu_forms_shift_one_cell(gpu, axis, q, scheme):
+    d, P = channel(axis, q)
+    want = shifted(d, P, axis, q)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P.copy()
+    ad.step(Pg, advdiff.params(**params(scheme)))                     # FP64 drop-in: exact
+    assert np.array_equal(Pg[1, 1:d.nj + 1, 1:d.ni + 1], want)
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, P)
+    b.step(advdiff.params(**params(scheme)))
+    b.sync()
+    got = b.get_tracer(0)[1, 1:d.nj + 1, 1:d.ni + 1]
+    b.destroy()
+    ad.kill()
+    assert np.max(np.abs(got - want)) <= 1e-6 * np.max(np.abs(want))  # FP32 form
