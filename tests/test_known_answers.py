@@ -1,5 +1,6 @@
-"""Known answer independent of the reference's restatement: advection at
-Courant number 1 shifts a field by exactly one cell per step.
+"""Known answers independent of the reference's restatement.
+
+Advection at Courant number 1 shifts a field by exactly one cell per step.
 
 On a single layer with V = VolumeZOld = 1, DT = 1, no diffusion and a
 transport of +1 (or -1) on every compute face of one direction, the explicit
@@ -9,8 +10,14 @@ against the upstream wall empties and the one against the downstream wall
 keeps its value plus the inflow.  With P2_TVD the weight 0.5 * psi * (1 - Cr)
 is 0 at Cr = +1, so every limiter gives the same shift for positive
 transports (for negative ones the reference's signed Courant number gives
-0.5 * psi * 2, which is not a shift; those run with upwind only).  Integer
-values keep every operation exact.
+0.5 * psi * 2, which is not a shift; those run with upwind only).
+
+Horizontal diffusion with unit metrics (DUX = DVY = DZX = DZY = AreaU = AreaV
+= Visc_H = V = 1, Schmidt 1) and DT = 1/4 is the discrete Laplacian: Kx = 1
+(Convert_Visc_Dif_Horizontal's distance-weighted mean of equal viscosities),
+each compute face moves (P_neighbour - P) / 4 into the cell.
+
+Integer values keep every operation exact.
 """
 import numpy as np
 import pytest
@@ -99,3 +106,61 @@ def test_gpu_forms_shift_one_cell(gpu, axis, q, scheme):
     b.destroy()
     ad.kill()
     assert np.max(np.abs(got - want)) <= 1e-6 * np.max(np.abs(want))  # FP32 form
+
+
+def unit_grid():
+    """The single-layer test grid with unit metrics, no transport and unit
+    viscosity, and an integer field."""
+    d = domain("layer1", dt=0.25)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZX", "DZY", "AreaU", "AreaV", "Visc_H", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    P = np.zeros(d.shape3)
+    rng = np.random.default_rng(9)
+    P[1, 1:d.nj + 1, 1:d.ni + 1] = rng.integers(0, 64, size=(d.nj, d.ni)).astype(np.float64)
+    return d, P
+
+
+def laplacian_step(d, P):
+    a = d.arrays
+    cu, cv, L = a["ComputeFacesU3D"][1], a["ComputeFacesV3D"][1], P[1]
+    out = np.empty((d.nj, d.ni))
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            p = L[j, i]
+            out[j - 1, i - 1] = p + 0.25 * (cu[j, i] * (L[j - 1, i] - p) + cu[j + 1, i] * (L[j + 1, i] - p) +
+                                            cv[j, i] * (L[j, i - 1] - p) + cv[j, i + 1] * (L[j, i + 1] - p))
+    return out
+
+
+DIFF = dict(DTProp=0.25, SchmidtBackground_V=0.0)
+
+
+def test_oracle_diffuses_by_the_laplacian():
+    d, P = unit_grid()
+    want = laplacian_step(d, P)
+    assert not np.array_equal(want, P[1, 1:d.nj + 1, 1:d.ni + 1])
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**DIFF)) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want)
+
+
+@pytest.mark.gpu
+def test_gpu_forms_diffuse_by_the_laplacian(gpu):
+    d, P = unit_grid()
+    want = laplacian_step(d, P)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    Pg = P.copy()
+    ad.step(Pg, advdiff.params(**DIFF))
+    assert np.array_equal(Pg[1, 1:d.nj + 1, 1:d.ni + 1], want)
+    b = batched.Batch(ad, 1)
+    b.set_tracer(0, P)
+    b.step(advdiff.params(**DIFF))
+    b.sync()
+    got = b.get_tracer(0)[1, 1:d.nj + 1, 1:d.ni + 1]
+    b.destroy()
+    ad.kill()
+    assert np.max(np.abs(got - want)) <= 1e-6 * np.max(np.abs(want))
