@@ -731,7 +731,7 @@ def main():
 # measured by this run; the capture and its command are in
 # profiles/batched_kernel_512x512x40_2tracers.md.
 TRAFFIC: dict = {
-    ("cfg2", "batched_kernel<2>"): 623.725568e6 + 112.851968e6,
+    ("cfg2", "batched_kernel<2>"): 623.833856e6 + 113.142528e6,
 }
 
 if __name__ == "__main__":
