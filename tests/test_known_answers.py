@@ -17,7 +17,12 @@ Horizontal diffusion with unit metrics (DUX = DVY = DZX = DZY = AreaU = AreaV
 (Convert_Visc_Dif_Horizontal's distance-weighted mean of equal viscosities),
 each compute face moves (P_neighbour - P) / 4 into the cell.
 
-Integer values keep every operation exact.
+Implicit horizontal advection at Courant number 1 is a recurrence down each
+line (2 x - x_upstream = P between compute faces), exact in dyadic values.
+Vertical diffusion through a single face of a column is a 2 x 2 system whose
+sum is kept and whose difference shrinks by 1 / (1 + 2 a).
+
+Integer values keep every operation exact (the vertical case to a few ulps).
 """
 import numpy as np
 import pytest
@@ -164,3 +169,61 @@ def test_gpu_forms_diffuse_by_the_laplacian(gpu):
     b.destroy()
     ad.kill()
     assert np.max(np.abs(got - want)) <= 1e-6 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("axis", ["j", "i"])
+def test_oracle_implicit_advection_recurrence(axis):
+    # ImpExp_AdvXX (YY) = 1 at Courant number 1: along each line the implicit
+    # upwind rows are 2 x - x_upstream = P between two compute faces, x = P / 2
+    # against the upstream wall (outflow only) and x - x_upstream = P against
+    # the downstream wall (inflow only), solved by THOMAS_3D along the line
+    d, P = channel(axis, 1.0)
+    a = d.arrays
+    cf = a["ComputeFacesU3D" if axis == "j" else "ComputeFacesV3D"][1]
+    L = P[1]
+    want = L.copy()
+    if axis == "j":
+        for i in range(1, d.ni + 1):
+            x = 0.0
+            for j in range(1, d.nj + 1):
+                w, e = cf[j, i], cf[j + 1, i]
+                x = (L[j, i] + w * x) / (1.0 + e)
+                want[j, i] = x
+    else:
+        for j in range(1, d.nj + 1):
+            x = 0.0
+            for i in range(1, d.ni + 1):
+                w, e = cf[j, i], cf[j, i + 1]
+                x = (L[j, i] + w * x) / (1.0 + e)
+                want[j, i] = x
+    Q = P.copy()
+    imp = dict(ImpExp_AdvXX=1.0) if axis == "j" else dict(ImpExp_AdvYY=1.0)
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, **imp)) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
+
+
+def test_oracle_vertical_diffusion_through_one_face():
+    # a column whose only diffusive face is the one between layers 4 and 5:
+    # with a = Kz * DUX * DVY / DZZ * DT / V = 1 the two cells solve
+    # [[2, -1], [-1, 2]] x = P: their sum is kept and their difference shrinks
+    # by 1 / (1 + 2 a) = 1/3; every other layer keeps its value (THOMASZ rounds
+    # the thirds, so those two agree to a few ulps)
+    d = domain("column", dt=1.0)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZZ", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    a["ComputeFacesW3D"][...] = 0                  # a lone column has none of its own
+    a["ComputeFacesW3D"][5, 1, 1] = 1
+    a["Diff_V"][5, 1, 1] = 1.0
+    P = np.zeros(d.shape3)
+    P[1:d.nk + 1, 1, 1] = np.arange(1, d.nk + 1, dtype=np.float64) * 8.0
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, SchmidtCoef_V=1.0)) == 0
+    p4, p5 = P[4, 1, 1], P[5, 1, 1]
+    x4, x5 = Q[4, 1, 1], Q[5, 1, 1]
+    assert abs((x4 + x5) - (p4 + p5)) <= 4 * np.spacing(p4 + p5)
+    assert abs((x4 - x5) - (p4 - p5) / 3.0) <= 8 * np.spacing(p4 + p5)
+    others = [k for k in range(1, d.nk + 1) if k not in (4, 5)]
+    assert np.array_equal(Q[others, 1, 1], P[others, 1, 1])
