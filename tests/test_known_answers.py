@@ -19,8 +19,9 @@ each compute face moves (P_neighbour - P) / 4 into the cell.
 
 Implicit horizontal advection at Courant number 1 is a recurrence down each
 line (2 x - x_upstream = P between compute faces), exact in dyadic values.
-Vertical diffusion through a single face of a column is a 2 x 2 system whose
-sum is kept and whose difference shrinks by 1 / (1 + 2 a).
+Implicit upwind vertical advection at Courant number 1 is the same recurrence
+up a column.  Vertical diffusion through a single face of a column is a 2 x 2
+system whose sum is kept and whose difference shrinks by 1 / (1 + 2 a).
 
 Integer values keep every operation exact (the vertical case to a few ulps).
 """
@@ -227,3 +228,34 @@ def test_oracle_vertical_diffusion_through_one_face():
     assert abs((x4 - x5) - (p4 - p5) / 3.0) <= 8 * np.spacing(p4 + p5)
     others = [k for k in range(1, d.nk + 1) if k not in (4, 5)]
     assert np.array_equal(Q[others, 1, 1], P[others, 1, 1])
+
+
+def test_oracle_implicit_vertical_advection_recurrence():
+    # upward transport 1 through every interior face of a column (V = 1,
+    # DT = 1, closed surface, no diffusion): implicit upwind rows are
+    # 2 x - x_below = P, x = P / 2 at the bed (outflow only) and
+    # x - x_below = P at the top (inflow only); THOMASZ solves them exactly
+    d = domain("column", dt=1.0)
+    a = d.arrays
+    nk = d.nk
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZZ", "DWZ", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    a["OpenPoints3D"][...] = 0
+    a["OpenPoints3D"][1:nk + 1, 1, 1] = 1
+    a["ComputeFacesW3D"][...] = 0
+    a["ComputeFacesW3D"][2:nk + 1, 1, 1] = 1
+    a["Wflux_Z"][2:nk + 1, 1, 1] = 1.0
+    P = np.zeros(d.shape3)
+    P[1:nk + 1, 1, 1] = np.random.default_rng(3).integers(0, 64, size=nk).astype(np.float64)
+    want = np.empty(nk)
+    x = 0.0
+    for k in range(1, nk + 1):
+        inflow = 1.0 if k > 1 else 0.0
+        outflow = 1.0 if k < nk else 0.0
+        x = (P[k, 1, 1] + inflow * x) / (1.0 + outflow)
+        want[k - 1] = x
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0)) == 0
+    assert np.array_equal(Q[1:nk + 1, 1, 1], want)
