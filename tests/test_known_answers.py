@@ -23,7 +23,13 @@ Implicit upwind vertical advection at Courant number 1 is the same recurrence
 up a column.  Vertical diffusion through a single face of a column is a 2 x 2
 system whose sum is kept and whose difference shrinks by 1 / (1 + 2 a).
 
-Integer values keep every operation exact (the vertical case to a few ulps).
+With open boundary columns at both ends of a Courant-1 channel and DecayTime
+0, MassConservation makes the inflow cell take its reference and the outflow
+cell (P + P_west) / 2, and ImposedValue makes every boundary cell its
+reference.
+
+Integer values keep every operation exact (the vertical diffusion case to a
+few ulps).
 """
 import numpy as np
 import pytest
@@ -259,3 +265,43 @@ def test_oracle_implicit_vertical_advection_recurrence():
     Q = P.copy()
     assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0)) == 0
     assert np.array_equal(Q[1:nk + 1, 1, 1], want)
+
+
+def open_channel():
+    """The Courant-1 channel along j with the columns at j = 1 and j = JUB
+    marked as boundary points, and an integer reference field."""
+    d, P = channel("j", 1.0)
+    a = d.arrays
+    a["BoundaryPoints2D"][...] = 0
+    a["BoundaryPoints2D"][1, 1:d.ni + 1] = 1
+    a["BoundaryPoints2D"][d.nj, 1:d.ni + 1] = 1
+    R = np.zeros(d.shape3)
+    R[1, 1:d.nj + 1, 1:d.ni + 1] = np.random.default_rng(11).integers(0, 64, size=(d.nj, d.ni)).astype(np.float64)
+    return d, P, R
+
+
+@pytest.mark.parametrize("scheme", ["upwind1", "tvd_superbee"])
+def test_oracle_mass_conservation_boundary_feeds_the_channel(scheme):
+    # MassConservation, DecayTime 0: the inflow cell (j = 1) empties through
+    # its east face and takes -WFOB * DT * Ref = Ref; the outflow cell (j = JUB)
+    # gains its west neighbour and loses WFOB * DT * x implicitly, so
+    # x = (P + P_west) / 2; the interior shifts by one cell
+    d, P, R = open_channel()
+    L, nj = P[1], d.nj
+    want = L.copy()
+    want[2:nj, :] = L[1:nj - 1, :]
+    want[1, :] = R[1, 1, :]
+    want[nj, :] = (L[nj, :] + L[nj - 1, :]) / 2.0
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=1, **params(scheme)), ReferenceProp=R) == 0
+    assert np.array_equal(Q[1, 1:nj + 1, 1:d.ni + 1], want[1:nj + 1, 1:d.ni + 1])
+
+
+def test_oracle_imposed_value_boundary_takes_the_reference():
+    # ImposedValue, DecayTime 0: the boundary cells are identity rows with the
+    # reference (decay factor 1), whatever the interior does
+    d, P, R = open_channel()
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=2, **params("upwind1")), ReferenceProp=R) == 0
+    for j in (1, d.nj):
+        assert np.array_equal(Q[1, j, 1:d.ni + 1], R[1, j, 1:d.ni + 1])
