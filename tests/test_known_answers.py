@@ -26,7 +26,10 @@ system whose sum is kept and whose difference shrinks by 1 / (1 + 2 a).
 With open boundary columns at both ends of a Courant-1 channel and DecayTime
 0, MassConservation makes the inflow cell take its reference and the outflow
 cell (P + P_west) / 2, and ImposedValue makes every boundary cell its
-reference.
+reference; a DecayTime blends the inflow's exterior value by 1 / (1 +
+DecayTime / DT).  In a still layer with Q * DT / V = 1 a point inflow adds its
+concentration, a withdrawal with ConcMF = 1 leaves half, and a bypassed
+withdrawal adds Q * DT / V * Conc.
 
 Integer values keep every operation exact (the vertical diffusion case to a
 few ulps).
@@ -305,3 +308,41 @@ def test_oracle_imposed_value_boundary_takes_the_reference():
     assert O.step(d, Q, O.params(BoundaryCondition=2, **params("upwind1")), ReferenceProp=R) == 0
     for j in (1, d.nj):
         assert np.array_equal(Q[1, j, 1:d.ni + 1], R[1, j, 1:d.ni + 1])
+
+
+@pytest.mark.parametrize("decay,tdec", [(1.0, 0.5), (3.0, 0.25)])
+def test_oracle_boundary_decay_blends_the_inflow(decay, tdec):
+    # MassConservation with DecayTime: the inflow carries the exterior value
+    # P * (1 - tdec) + Ref * tdec, tdec = 1 / (1 + DecayTime / DT)
+    d, P, R = open_channel()
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=1, DecayTime=decay, **params("upwind1")), ReferenceProp=R) == 0
+    want = P[1, 1, 1:d.ni + 1] * (1.0 - tdec) + R[1, 1, 1:d.ni + 1] * tdec
+    assert np.array_equal(Q[1, 1, 1:d.ni + 1], want)
+
+
+def test_oracle_discharges_add_and_withdraw():
+    # a still layer (V = VolumeZOld = 1, DT = 1, no transport or diffusion):
+    # a point inflow of Q = 1 adds Q * DT / V * Conc to its cell, a withdrawal
+    # of Q = -1 with ConcMF = 1 leaves implicitly (E = 1 + 1: half remains), a
+    # bypassed withdrawal adds Q * DT / V * Conc like an inflow
+    d = domain("layer1", dt=1.0)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    a["VolumeZ"][...] = 1.0
+    a["VolumeZOld"][...] = 1.0
+    P = np.zeros(d.shape3)
+    P[1, 1:d.nj + 1, 1:d.ni + 1] = np.random.default_rng(13).integers(0, 64, size=(d.nj, d.ni)).astype(np.float64)
+    cells = [(2, 3), (4, 5), (6, 2)]                   # (j, i): inflow, withdrawal, bypassed withdrawal
+    ds = dict(nCells=np.array([1, 1, 1]), ignore=np.array([0, 0, 0]), bypass=np.array([0, 0, 1]),
+              vert=np.array([1, 1, 1]), I=np.array([c[1] for c in cells]), J=np.array([c[0] for c in cells]),
+              K=np.array([1, 1, 1]), Kmin=np.array([-9999999] * 3), Kmax=np.array([-9999999] * 3),
+              Flow=np.array([1.0, -1.0, -1.0]), Conc=np.array([5.0, 7.0, 3.0]), ConcMF=np.array([2.0, 1.0, 4.0]))
+    want = P[1].copy()
+    want[2, 3] += 5.0
+    want[4, 5] /= 2.0
+    want[6, 2] += -1.0 * 3.0
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0), Disch=ds) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
