@@ -29,7 +29,9 @@ cell (P + P_west) / 2, and ImposedValue makes every boundary cell its
 reference; a DecayTime blends the inflow's exterior value by 1 / (1 +
 DecayTime / DT).  In a still layer with Q * DT / V = 1 a point inflow adds its
 concentration, a withdrawal with ConcMF = 1 leaves half, and a bypassed
-withdrawal adds Q * DT / V * Conc.
+withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
+both answers; the cell fluxes of the two first answers are the upstream value
+(advection) and -(P - P_west) (diffusion) on each compute face.
 
 Integer values keep every operation exact (the vertical diffusion case to a
 few ulps).
@@ -346,3 +348,64 @@ def test_oracle_discharges_add_and_withdraw():
     Q = P.copy()
     assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0), Disch=ds) == 0
     assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
+
+
+def test_oracle_noflux_masks_stop_the_shift_and_the_laplacian():
+    # NoAdvFlux / NoDifFlux: a masked face carries nothing, so the known
+    # answers hold with the masked faces taken out of the compute faces
+    d, P = channel("j", 1.0)
+    a = d.arrays
+    rng = np.random.default_rng(17)
+    nfu = ((a["ComputeFacesU3D"] == 1) & (rng.random(a["ComputeFacesU3D"].shape) < 0.3)).astype(np.int32)
+    zero = np.zeros_like(nfu)
+    nf = (nfu, zero, zero)
+    cfu = a["ComputeFacesU3D"].copy()
+    a["ComputeFacesU3D"][...] = cfu * (1 - nfu)            # the faces that still carry flux
+    want = shifted(d, P, "j", 1.0)
+    a["ComputeFacesU3D"][...] = cfu
+    Q = P.copy()
+    assert O.step(d, Q, O.params(NoAdvFlux=1, **params("upwind1")), NoFlux=nf) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want)
+
+    d, P = unit_grid()
+    a = d.arrays
+    nfu = ((a["ComputeFacesU3D"] == 1) & (rng.random(a["ComputeFacesU3D"].shape) < 0.3)).astype(np.int32)
+    nfv = ((a["ComputeFacesV3D"] == 1) & (rng.random(a["ComputeFacesV3D"].shape) < 0.3)).astype(np.int32)
+    cfu, cfv = a["ComputeFacesU3D"].copy(), a["ComputeFacesV3D"].copy()
+    a["ComputeFacesU3D"][...] = cfu * (1 - nfu)
+    a["ComputeFacesV3D"][...] = cfv * (1 - nfv)
+    want = laplacian_step(d, P)
+    a["ComputeFacesU3D"][...] = cfu
+    a["ComputeFacesV3D"][...] = cfv
+    Q = P.copy()
+    assert O.step(d, Q, O.params(NoDifFlux=1, **DIFF), NoFlux=(nfu, nfv, np.zeros_like(nfu))) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want)
+
+
+def test_oracle_cell_fluxes_of_the_known_steps():
+    # CellFluxes (GetAdvFlux / GetDifFlux): at Courant number 1 the advective
+    # flux through a compute face is the upstream value; with unit metrics the
+    # diffusive flux through a west face is -(P - P_west)
+    d, P = channel("j", 1.0)
+    work = O.Work(d)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(CellFluxes=1, **params("upwind1")), work=work) == 0
+    f = O.cell_fluxes(d, work)
+    cf = d.arrays["ComputeFacesU3D"][1]
+    L = P[1]
+    want = np.zeros_like(L)
+    want[1:, :] = cf[1:, :] * L[:-1, :]
+    assert np.array_equal(f["AdvFluxX"][1], want)
+    assert not f["DifFluxX"].any() and not f["AdvFluxY"].any()
+
+    d, P = unit_grid()
+    work = O.Work(d)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(CellFluxes=1, **DIFF), work=work) == 0
+    f = O.cell_fluxes(d, work)
+    cf = d.arrays["ComputeFacesU3D"][1]
+    L = P[1]
+    want = np.zeros_like(L)
+    want[1:, :] = -cf[1:, :] * (L[1:, :] - L[:-1, :])
+    assert np.array_equal(f["DifFluxX"][1], want)
+    assert not f["AdvFluxX"].any()
