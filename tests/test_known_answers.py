@@ -27,7 +27,8 @@ With open boundary columns at both ends of a Courant-1 channel and DecayTime
 0, MassConservation makes the inflow cell take its reference and the outflow
 cell (P + P_west) / 2, and ImposedValue makes every boundary cell its
 reference; a DecayTime blends the inflow's exterior value by 1 / (1 +
-DecayTime / DT).  In a still layer with Q * DT / V = 1 a point inflow adds its
+DecayTime / DT); Cyclic keeps the boundary rows in the solve, then gives them
+their references and copies the interior next to the opposite end.  In a still layer with Q * DT / V = 1 a point inflow adds its
 concentration, a withdrawal with ConcMF = 1 leaves half, and a bypassed
 withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
 both answers; the cell fluxes of the two first answers are the upstream value
@@ -409,3 +410,23 @@ def test_oracle_cell_fluxes_of_the_known_steps():
     want[1:, :] = -cf[1:, :] * (L[1:, :] - L[:-1, :])
     assert np.array_equal(f["DifFluxX"][1], want)
     assert not f["AdvFluxX"].any()
+
+
+def test_oracle_cyclic_boundaries_copy_across_the_channel():
+    # Cyclic: the boundary rows keep their old values in the solve (the
+    # interior shifts, taking the old j = 1 value into j = 2); after it every
+    # boundary cell takes its reference, then each row i = 2..IUB-1 whose two
+    # ends are boundary points copies the interior next to the opposite end
+    d, P, R = open_channel()
+    L, nj, ni = P[1], d.nj, d.ni
+    new = L.copy()
+    new[2:nj, :] = L[1:nj - 1, :]                    # the interior's Courant-1 shift
+    want = new.copy()
+    want[1, :] = R[1, 1, :]
+    want[nj, :] = R[1, nj, :]
+    for i in range(2, ni):
+        want[1, i] = new[nj - 1, i]
+        want[nj, i] = new[2, i]
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=8, **params("upwind1")), ReferenceProp=R) == 0
+    assert np.array_equal(Q[1, 1:nj + 1, 1:ni + 1], want[1:nj + 1, 1:ni + 1])
