@@ -430,3 +430,93 @@ def test_oracle_cyclic_boundaries_copy_across_the_channel():
     Q = P.copy()
     assert O.step(d, Q, O.params(BoundaryCondition=8, **params("upwind1")), ReferenceProp=R) == 0
     assert np.array_equal(Q[1, 1:nj + 1, 1:ni + 1], want[1:nj + 1, 1:ni + 1])
+
+
+def _case(name):
+    """(domain, field, params, ReferenceProp, discharges, NoFlux masks,
+    batched form takes it) of the known-answer cases run on the GPU forms."""
+    R = ds = nf = None
+    if name == "implicit_j":
+        d, P = channel("j", 1.0)
+        pd = dict(params("upwind1"), ImpExp_AdvXX=1.0)
+        return d, P, pd, R, ds, nf, False
+    if name in ("mass_conservation", "imposed_value", "cyclic", "decay"):
+        d, P, R = open_channel()
+        bc = {"mass_conservation": 1, "imposed_value": 2, "cyclic": 8, "decay": 1}[name]
+        pd = dict(params("tvd_superbee"), BoundaryCondition=bc, DecayTime=3.0 if name == "decay" else 0.0)
+        return d, P, pd, R, ds, nf, True
+    if name == "discharges":
+        d = domain("layer1", dt=1.0)
+        a = d.arrays
+        for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+            a[n][...] = 0.0
+        a["VolumeZ"][...] = 1.0
+        a["VolumeZOld"][...] = 1.0
+        P = np.zeros(d.shape3)
+        P[1, 1:d.nj + 1, 1:d.ni + 1] = np.random.default_rng(13).integers(0, 64, size=(d.nj, d.ni)).astype(float)
+        ds = dict(nCells=np.array([1, 1, 1]), ignore=np.array([0, 0, 0]), bypass=np.array([0, 0, 1]),
+                  vert=np.array([1, 1, 1]), I=np.array([3, 5, 2]), J=np.array([2, 4, 6]), K=np.array([1, 1, 1]),
+                  Kmin=np.array([-9999999] * 3), Kmax=np.array([-9999999] * 3),
+                  Flow=np.array([1.0, -1.0, -1.0]), Conc=np.array([5.0, 7.0, 3.0]), ConcMF=np.array([2.0, 1.0, 4.0]))
+        return d, P, dict(DTProp=1.0, SchmidtBackground_V=0.0), R, ds, nf, True
+    if name in ("noflux_adv", "noflux_dif"):
+        d, P = channel("j", 1.0) if name == "noflux_adv" else unit_grid()
+        a = d.arrays
+        rng = np.random.default_rng(17)
+        nfu = ((a["ComputeFacesU3D"] == 1) & (rng.random(a["ComputeFacesU3D"].shape) < 0.3)).astype(np.int32)
+        nfv = ((a["ComputeFacesV3D"] == 1) & (rng.random(a["ComputeFacesV3D"].shape) < 0.3)).astype(np.int32)
+        nf = (nfu, nfv, np.zeros_like(nfu))
+        pd = dict(params("upwind1"), NoAdvFlux=1) if name == "noflux_adv" else dict(DIFF, NoDifFlux=1)
+        return d, P, pd, R, ds, nf, True
+    raise ValueError(name)
+
+
+GPU_CASES = ["implicit_j", "mass_conservation", "imposed_value", "cyclic", "decay", "discharges", "noflux_adv",
+             "noflux_dif"]
+
+
+def _oracle(name):
+    d, P, pd, R, ds, nf, _ = _case(name)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**pd), ReferenceProp=R, Disch=ds, NoFlux=nf) == 0
+    return Q
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_known_answer_cases_build(name):
+    # the cases the GPU test below runs, on the oracle
+    Q = _oracle(name)
+    assert np.isfinite(Q).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_gpu_forms_on_the_known_answer_cases(gpu, name):
+    # the FP64 drop-in equals the oracle bit for bit on every case (whose
+    # closed forms the CPU tests above pin); the batched form, where it takes
+    # the options, to 1e-6
+    d, P, pd, R, ds, nf, batch_ok = _case(name)
+    want = _oracle(name)
+    ad = advdiff.AdvectionDiffusion(d)
+    ad.set_hydro()
+    if nf is not None:
+        ad.set_noflux(nf)
+    if ds is not None:
+        ad.set_discharges(ds)
+    Pg = P.copy()
+    ad.step(Pg, advdiff.params(**pd), R)
+    assert np.array_equal(Pg, want)
+    if batch_ok:
+        b = batched.Batch(ad, 1)
+        b.set_tracer(0, P)
+        if ds is not None:
+            b.set_discharge_conc(0, ds["Conc"])
+        if R is not None:
+            b.set_reference(0, R)
+        b.step(advdiff.params(**pd))
+        b.sync()
+        got = b.get_tracer(0)
+        b.destroy()
+        c = (1, slice(1, d.nj + 1), slice(1, d.ni + 1))
+        assert np.max(np.abs(got[c] - want[c])) <= 1e-6 * np.max(np.abs(want[c]))
+    ad.kill()
