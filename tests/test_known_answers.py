@@ -520,3 +520,23 @@ def test_gpu_forms_on_the_known_answer_cases(gpu, name):
         c = (1, slice(1, d.nj + 1), slice(1, d.ni + 1))
         assert np.max(np.abs(got[c] - want[c])) <= 1e-6 * np.max(np.abs(want[c]))
     ad.kill()
+
+
+@pytest.mark.parametrize("name", GPU_CASES + ["shift_j", "shift_i_neg", "laplacian"])
+def test_python_restatement_on_the_known_answer_cases(name):
+    # the second, pure-Python restatement gives the oracle's bits on the
+    # closed-form cases too (so both reproduce the closed forms)
+    from oracle import ref_py
+    if name == "shift_j":
+        (d, P), pd, R, ds, nf = channel("j", 1.0), params("tvd_superbee"), None, None, None
+    elif name == "shift_i_neg":
+        (d, P), pd, R, ds, nf = channel("i", -1.0), params("upwind1"), None, None, None
+    elif name == "laplacian":
+        (d, P), pd, R, ds, nf = unit_grid(), DIFF, None, None, None
+    else:
+        d, P, pd, R, ds, nf, _ = _case(name)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**pd), ReferenceProp=R, Disch=ds, NoFlux=nf) == 0
+    Pp = P.copy()
+    ref_py.step(d, Pp, dict(O.DEFAULTS, **pd), ReferenceProp=R, Disch=ds, NoFlux=nf)
+    assert np.array_equal(Pp, Q)
