@@ -34,6 +34,10 @@ withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
 both answers; the cell fluxes of the two first answers are the upstream value
 (advection) and -(P - P_west) (diffusion) on each compute face.
 
+AdvectionNudging scales each cell's advective terms by
+n = min(d_i, d_j, nCells) / nCells on grids at least 2 nCells wide, d the
+distance in cells to the nearer edge.
+
 Integer values keep every operation exact (the vertical diffusion case to a
 few ulps).
 """
@@ -539,4 +543,30 @@ def test_python_restatement_on_the_known_answer_cases(name):
     assert O.step(d, Q, O.params(**pd), ReferenceProp=R, Disch=ds, NoFlux=nf) == 0
     Pp = P.copy()
     ref_py.step(d, Pp, dict(O.DEFAULTS, **pd), ReferenceProp=R, Disch=ds, NoFlux=nf)
+    assert np.array_equal(Pp, Q)
+
+
+def test_oracle_nudging_scales_the_shift():
+    # AdvectionNudging with nCells = 2 on the 6 x 7 layer (at least 2 nCells
+    # wide, so the reference's in-order distances are the distances to the
+    # nearer edge): each cell's advective terms enter scaled by
+    # n = min(d_i, d_j, nCells) / nCells, so at Courant number 1 a cell gets
+    # P + n * (P_west * w - P * e)
+    d, P = channel("j", 1.0)
+    nc = 2
+    cf = d.arrays["ComputeFacesU3D"][1]
+    L = P[1]
+    want = L.copy()
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            di, dj = min(i, d.ni - i + 1), min(j, d.nj - j + 1)
+            n = min(di, dj, nc) / nc
+            want[j, i] = L[j, i] + n * (L[j - 1, i] * cf[j, i] - L[j, i] * cf[j + 1, i])
+    pd = dict(params("upwind1"), AdvectionNudging=1, AdvectionNudgingCells=nc)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**pd)) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
+    from oracle import ref_py
+    Pp = P.copy()
+    ref_py.step(d, Pp, dict(O.DEFAULTS, **pd))
     assert np.array_equal(Pp, Q)
