@@ -34,7 +34,8 @@ withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
 both answers; the cell fluxes of the two first answers are the upstream value
 (advection) and -(P - P_west) (diffusion) on each compute face.
 
-AdvectionNudging scales each cell's advective terms by
+CentralDif and LeapFrog take the face value (P_west + P) / 2 at Courant
+number 1.  AdvectionNudging scales each cell's advective terms by
 n = min(d_i, d_j, nCells) / nCells on grids at least 2 nCells wide, d the
 distance in cells to the nearer edge.
 
@@ -570,3 +571,20 @@ def test_oracle_nudging_scales_the_shift():
     Pp = P.copy()
     ref_py.step(d, Pp, dict(O.DEFAULTS, **pd))
     assert np.array_equal(Pp, Q)
+
+
+@pytest.mark.parametrize("method", [5, 6])
+def test_oracle_central_face_at_courant_one(method):
+    # CentralDif (5) and LeapFrog (6) take the face value (P_west + P) / 2 at
+    # Courant number 1, so a cell gets P + w (P_west + P) / 2 - e (P + P_east) / 2
+    d, P = channel("j", 1.0)
+    cf = d.arrays["ComputeFacesU3D"][1]
+    L = P[1]
+    want = L.copy()
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            want[j, i] = L[j, i] + cf[j, i] * 0.5 * (L[j - 1, i] + L[j, i]) - \
+                cf[j + 1, i] * 0.5 * (L[j, i] + L[j + 1, i])
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, AdvMethodH=method)) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
