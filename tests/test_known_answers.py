@@ -20,7 +20,9 @@ each compute face moves (P_neighbour - P) / 4 into the cell.
 Implicit horizontal advection at Courant number 1 is a recurrence down each
 line (2 x - x_upstream = P between compute faces), exact in dyadic values.
 Implicit upwind vertical advection at Courant number 1 is the same recurrence
-up a column.  Vertical diffusion through a single face of a column is a 2 x 2
+up a column; explicit vertical advection (upwind or P2_TVD) shifts the column
+up one layer, and explicit vertical diffusion through one face with
+a = 1/4 exchanges a (P5 - P4).  Vertical diffusion through a single face of a column is a 2 x 2
 system whose sum is kept and whose difference shrinks by 1 / (1 + 2 a).
 
 With open boundary columns at both ends of a Courant-1 channel and DecayTime
@@ -588,3 +590,64 @@ def test_oracle_central_face_at_courant_one(method):
     Q = P.copy()
     assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, AdvMethodH=method)) == 0
     assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
+
+
+def upward_column():
+    """A lone column with every interior face a compute face, transport 1
+    upward through them (V = 1, DT = 1, closed surface), an integer field."""
+    d = domain("column", dt=1.0)
+    a = d.arrays
+    nk = d.nk
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZZ", "DWZ", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    a["OpenPoints3D"][...] = 0
+    a["OpenPoints3D"][1:nk + 1, 1, 1] = 1
+    a["ComputeFacesW3D"][...] = 0
+    a["ComputeFacesW3D"][2:nk + 1, 1, 1] = 1
+    a["Wflux_Z"][2:nk + 1, 1, 1] = 1.0
+    P = np.zeros(d.shape3)
+    P[1:nk + 1, 1, 1] = np.random.default_rng(3).integers(0, 64, size=nk).astype(np.float64)
+    return d, P
+
+
+@pytest.mark.parametrize("vopt", [dict(), dict(AdvMethodV=4, TVDLimitationV=4, Upwind2V=1)])
+def test_oracle_explicit_vertical_advection_shifts_up(vopt):
+    # ImpExp_AdvV = 0 at Courant number 1: each layer takes the one below; the
+    # bed empties, the top keeps its value plus the inflow (P2_TVD's weight
+    # vanishes at Cr = 1 as horizontally)
+    d, P = upward_column()
+    nk = d.nk
+    c = P[:, 1, 1]
+    want = c.copy()
+    want[1] = 0.0
+    want[2:nk] = c[1:nk - 1]
+    want[nk] = c[nk] + c[nk - 1]
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, ImpExp_AdvV=0.0, **vopt)) == 0
+    assert np.array_equal(Q[1:nk + 1, 1, 1], want[1:nk + 1])
+
+
+def test_oracle_explicit_vertical_diffusion_through_one_face():
+    # ImpExp_DifV = 0, one diffusive face between layers 4 and 5 with
+    # a = Kz * DUX * DVY / DZZ * DT / V = 1/4: the pair exchanges
+    # a * (P5 - P4), the other layers keep their values
+    d = domain("column", dt=0.25)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZZ", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    a["ComputeFacesW3D"][...] = 0
+    a["ComputeFacesW3D"][5, 1, 1] = 1
+    a["Diff_V"][5, 1, 1] = 1.0
+    P = np.zeros(d.shape3)
+    P[1:d.nk + 1, 1, 1] = np.arange(1, d.nk + 1, dtype=np.float64) * 8.0
+    want = P[:, 1, 1].copy()
+    flux = 0.25 * (P[5, 1, 1] - P[4, 1, 1])
+    want[4] += flux
+    want[5] -= flux
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=0.25, SchmidtBackground_V=0.0, ImpExp_DifV=0.0)) == 0
+    assert np.array_equal(Q[1:d.nk + 1, 1, 1], want[1:d.nk + 1])
