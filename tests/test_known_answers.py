@@ -310,12 +310,14 @@ def test_oracle_mass_conservation_boundary_feeds_the_channel(scheme):
     assert np.array_equal(Q[1, 1:nj + 1, 1:d.ni + 1], want[1:nj + 1, 1:d.ni + 1])
 
 
-def test_oracle_imposed_value_boundary_takes_the_reference():
-    # ImposedValue, DecayTime 0: the boundary cells are identity rows with the
-    # reference (decay factor 1), whatever the interior does
+@pytest.mark.parametrize("bc", [2, 5])
+def test_oracle_imposed_value_boundary_takes_the_reference(bc):
+    # ImposedValue (2) and SubModel (5), DecayTime 0: the boundary cells are
+    # identity rows with the interior mean decayed fully towards the reference
+    # (decay factor 1), whatever the interior does
     d, P, R = open_channel()
     Q = P.copy()
-    assert O.step(d, Q, O.params(BoundaryCondition=2, **params("upwind1")), ReferenceProp=R) == 0
+    assert O.step(d, Q, O.params(BoundaryCondition=bc, **params("upwind1")), ReferenceProp=R) == 0
     for j in (1, d.nj):
         assert np.array_equal(Q[1, j, 1:d.ni + 1], R[1, j, 1:d.ni + 1])
 
