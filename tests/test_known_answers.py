@@ -30,7 +30,9 @@ With open boundary columns at both ends of a Courant-1 channel and DecayTime
 cell (P + P_west) / 2, and ImposedValue makes every boundary cell its
 reference; a DecayTime blends the inflow's exterior value by 1 / (1 +
 DecayTime / DT); Cyclic keeps the boundary rows in the solve, then gives them
-their references and copies the interior next to the opposite end.  In a still layer with Q * DT / V = 1 a point inflow adds its
+their references and copies the interior next to the opposite end;
+MassConservNullGrad makes the inflow cell the mean of its old neighbours
+across compute faces.  In a still layer with Q * DT / V = 1 a point inflow adds its
 concentration, a withdrawal with ConcMF = 1 leaves half, and a bypassed
 withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
 both answers; the cell fluxes of the two first answers are the upstream value
@@ -653,3 +655,22 @@ def test_oracle_explicit_vertical_diffusion_through_one_face():
     Q = P.copy()
     assert O.step(d, Q, O.params(DTProp=0.25, SchmidtBackground_V=0.0, ImpExp_DifV=0.0)) == 0
     assert np.array_equal(Q[1:d.nk + 1, 1, 1], want[1:d.nk + 1])
+
+
+def test_oracle_mass_conserv_null_grad_boundary():
+    # MassConservNullGrad (7): the inflow cell (j = 1) becomes the mean of its
+    # old neighbours across compute faces (east, and north / south along the
+    # boundary row where those are compute faces); the outflow cell leaves
+    # implicitly as with MassConservation, (P + P_west) / 2
+    d, P, R = open_channel()
+    a = d.arrays
+    cu, cv, L, nj, ni = a["ComputeFacesU3D"][1], a["ComputeFacesV3D"][1], P[1], d.nj, d.ni
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=7, **params("upwind1")), ReferenceProp=R) == 0
+    for i in range(1, ni + 1):
+        nb = [(cu[2, i], L[2, i]), (cv[1, i + 1], L[1, i + 1]), (cv[1, i], L[1, i - 1])]
+        w = sum(c for c, _ in nb)
+        mean = sum(c * v for c, v in nb) / w
+        assert abs(Q[1, 1, i] - mean) <= 2 * np.spacing(max(abs(mean), 1.0))
+    assert np.array_equal(Q[1, nj, 1:ni + 1], (L[nj, 1:ni + 1] + L[nj - 1, 1:ni + 1]) / 2.0)
+    assert np.array_equal(Q[1, 2:nj, 1:ni + 1], L[1:nj - 1, 1:ni + 1])
