@@ -32,7 +32,8 @@ reference; a DecayTime blends the inflow's exterior value by 1 / (1 +
 DecayTime / DT); Cyclic keeps the boundary rows in the solve, then gives them
 their references and copies the interior next to the opposite end;
 MassConservNullGrad makes the inflow cell the mean of its old neighbours
-across compute faces.  In a still layer with Q * DT / V = 1 a point inflow adds its
+across compute faces; NullGradient, with boundary points that do not
+neighbour one another, the mean of its neighbours' new values.  In a still layer with Q * DT / V = 1 a point inflow adds its
 concentration, a withdrawal with ConcMF = 1 leaves half, and a bypassed
 withdrawal adds Q * DT / V * Conc.  NoFlux masks take their faces out of
 both answers; the cell fluxes of the two first answers are the upstream value
@@ -674,3 +675,29 @@ def test_oracle_mass_conserv_null_grad_boundary():
         assert abs(Q[1, 1, i] - mean) <= 2 * np.spacing(max(abs(mean), 1.0))
     assert np.array_equal(Q[1, nj, 1:ni + 1], (L[nj, 1:ni + 1] + L[nj - 1, 1:ni + 1]) / 2.0)
     assert np.array_equal(Q[1, 2:nj, 1:ni + 1], L[1:nj - 1, 1:ni + 1])
+
+
+def test_oracle_null_gradient_boundary_mean():
+    # NullGradient (4) with boundary points at every other cell of the j = 1
+    # row, so that no boundary cell neighbours another and the in-order sweep
+    # has no order to depend on: the boundary rows keep their old values in
+    # the solve (the east neighbour then holds the boundary cell's old value,
+    # shifted in), and each boundary cell becomes the mean of its neighbours'
+    # new values across compute faces; the other cells of the row, against the
+    # upstream wall, empty
+    d, P = channel("j", 1.0)
+    a = d.arrays
+    a["BoundaryPoints2D"][...] = 0
+    a["BoundaryPoints2D"][1, 1:d.ni + 1:2] = 1
+    cu, cv, L, ni = a["ComputeFacesU3D"][1], a["ComputeFacesV3D"][1], P[1], d.ni
+    Q = P.copy()
+    assert O.step(d, Q, O.params(BoundaryCondition=4, **params("upwind1"))) == 0
+    new = np.zeros_like(L)
+    new[2, :] = L[1, :]                         # the east neighbours: the old boundary-row values
+    for i in range(1, ni + 1, 2):
+        nb = [(cu[2, i], new[2, i]), (cv[1, i + 1], 0.0), (cv[1, i], 0.0)]   # row neighbours emptied
+        w = sum(c for c, _ in nb)
+        mean = sum(c * v for c, v in nb) / w
+        assert abs(Q[1, 1, i] - mean) <= 2 * np.spacing(max(abs(mean), 1.0))
+    for i in range(2, ni + 1, 2):
+        assert Q[1, 1, i] == 0.0
