@@ -225,13 +225,16 @@ def test_oracle_implicit_advection_recurrence(axis):
     assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], want[1:d.nj + 1, 1:d.ni + 1])
 
 
-def test_oracle_vertical_diffusion_through_one_face():
-    # a column whose only diffusive face is the one between layers 4 and 5:
-    # with a = Kz * DUX * DVY / DZZ * DT / V = 1 the two cells solve
-    # [[2, -1], [-1, 2]] x = P: their sum is kept and their difference shrinks
-    # by 1 / (1 + 2 a) = 1/3; every other layer keeps its value (THOMASZ rounds
-    # the thirds, so those two agree to a few ulps)
-    d = domain("column", dt=1.0)
+@pytest.mark.parametrize("theta,dt", [(1.0, 1.0), (0.5, 1.0), (0.5, 0.25)])
+def test_oracle_vertical_diffusion_through_one_face(theta, dt):
+    # a column whose only diffusive face is the one between layers 4 and 5,
+    # a = Kz * DUX * DVY / DZZ * DT / V = DT, implicit weight theta
+    # (ImpExp_DifV): the two cells solve
+    # [[1 + a theta, -a theta], [-a theta, 1 + a theta]] x = P + a (1 - theta) (P5 - P4) (-1, +1),
+    # so their sum is kept and their difference scales by
+    # (1 - 2 a (1 - theta)) / (1 + 2 a theta); every other layer keeps its
+    # value (THOMASZ rounds the divisions, so the pair agrees to a few ulps)
+    d = domain("column", dt=dt)
     a = d.arrays
     for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
         a[n][...] = 0.0
@@ -243,11 +246,13 @@ def test_oracle_vertical_diffusion_through_one_face():
     P = np.zeros(d.shape3)
     P[1:d.nk + 1, 1, 1] = np.arange(1, d.nk + 1, dtype=np.float64) * 8.0
     Q = P.copy()
-    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, SchmidtCoef_V=1.0)) == 0
+    assert O.step(d, Q, O.params(DTProp=dt, SchmidtBackground_V=0.0, SchmidtCoef_V=1.0, ImpExp_DifV=theta)) == 0
     p4, p5 = P[4, 1, 1], P[5, 1, 1]
     x4, x5 = Q[4, 1, 1], Q[5, 1, 1]
+    a_ = dt
     assert abs((x4 + x5) - (p4 + p5)) <= 4 * np.spacing(p4 + p5)
-    assert abs((x4 - x5) - (p4 - p5) / 3.0) <= 8 * np.spacing(p4 + p5)
+    want = (p4 - p5) * (1.0 - 2.0 * a_ * (1.0 - theta)) / (1.0 + 2.0 * a_ * theta)
+    assert abs((x4 - x5) - want) <= 8 * np.spacing(p4 + p5)
     others = [k for k in range(1, d.nk + 1) if k not in (4, 5)]
     assert np.array_equal(Q[others, 1, 1], P[others, 1, 1])
 
