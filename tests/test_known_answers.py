@@ -257,7 +257,8 @@ def test_oracle_vertical_diffusion_through_one_face(theta, dt):
     assert np.array_equal(Q[others, 1, 1], P[others, 1, 1])
 
 
-def test_oracle_implicit_vertical_advection_recurrence():
+@pytest.mark.parametrize("docycle", [1, 2])
+def test_oracle_implicit_vertical_advection_recurrence(docycle):
     # upward transport 1 through every interior face of a column (V = 1,
     # DT = 1, closed surface, no diffusion): implicit upwind rows are
     # 2 x - x_below = P, x = P / 2 at the bed (outflow only) and
@@ -284,7 +285,7 @@ def test_oracle_implicit_vertical_advection_recurrence():
         x = (P[k, 1, 1] + inflow * x) / (1.0 + outflow)
         want[k - 1] = x
     Q = P.copy()
-    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0)) == 0
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0, Docycle_method=docycle)) == 0
     assert np.array_equal(Q[1:nk + 1, 1, 1], want)
 
 
@@ -706,3 +707,24 @@ def test_oracle_null_gradient_boundary_mean():
         assert abs(Q[1, 1, i] - mean) <= 2 * np.spacing(max(abs(mean), 1.0))
     for i in range(2, ni + 1, 2):
         assert Q[1, 1, i] == 0.0
+
+
+def test_oracle_small_depths_skip_vertical_diffusion():
+    # a column flagged in SmallDepths takes no vertical diffusion
+    # (VerticalDiffusion skips it): the one-face exchange leaves it unchanged
+    d = domain("column", dt=1.0)
+    a = d.arrays
+    for n in ("Wflux_X", "Wflux_Y", "Wflux_Z", "Visc_H", "Diff_V"):
+        a[n][...] = 0.0
+    for n in ("DUX", "DVY", "DZZ", "VolumeZ", "VolumeZOld"):
+        a[n][...] = 1.0
+    a["ComputeFacesW3D"][...] = 0
+    a["ComputeFacesW3D"][5, 1, 1] = 1
+    a["Diff_V"][5, 1, 1] = 1.0
+    P = np.zeros(d.shape3)
+    P[1:d.nk + 1, 1, 1] = np.arange(1, d.nk + 1, dtype=np.float64) * 8.0
+    sd = np.zeros(a["KFloorZ"].shape, dtype=np.int32)
+    sd[1, 1] = 1
+    Q = P.copy()
+    assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0), SmallDepths=sd) == 0
+    assert np.array_equal(Q[1:d.nk + 1, 1, 1], P[1:d.nk + 1, 1, 1])
