@@ -728,3 +728,20 @@ def test_oracle_small_depths_skip_vertical_diffusion():
     Q = P.copy()
     assert O.step(d, Q, O.params(DTProp=1.0, SchmidtBackground_V=0.0), SmallDepths=sd) == 0
     assert np.array_equal(Q[1:d.nk + 1, 1, 1], P[1:d.nk + 1, 1, 1])
+
+
+@pytest.mark.parametrize("case", ["vertical1d", "xzflow", "nulldif"])
+def test_oracle_options_that_stop_the_known_answers(case):
+    # Vertical1D drops the horizontal terms (a single layer then keeps its
+    # values); XZFlow drops the y direction (a channel along i keeps its
+    # values); NullDif zeroes diffusion across faces without transport (the
+    # Laplacian grid has none, so it keeps its values)
+    if case == "vertical1d":
+        (d, P), pd = channel("j", 1.0), dict(params("upwind1"), Vertical1D=1)
+    elif case == "xzflow":
+        (d, P), pd = channel("i", 1.0), dict(params("upwind1"), XZFlow=1)
+    else:
+        (d, P), pd = unit_grid(), dict(DIFF, NullDif=1)
+    Q = P.copy()
+    assert O.step(d, Q, O.params(**pd)) == 0
+    assert np.array_equal(Q[1, 1:d.nj + 1, 1:d.ni + 1], P[1, 1:d.nj + 1, 1:d.ni + 1])
