@@ -12,8 +12,6 @@ if str(ROOT) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "long: minutes-long accuracy runs at the workloads' sizes "
-                                       "(-m 'gpu and not long' leaves them out)")
 
 
 def _has_gpu() -> bool:
